@@ -1,0 +1,186 @@
+"""ORACLE — test infrastructure, not the product.
+
+ctypes front end of the plain-C restatement in ``oracle/sdfc_oracle.c`` of the
+reference redmax point-vs-SDF contact path.  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this
+module, as the checker; the product never does.
+
+Every function cites the reference function it restates (paths relative to the
+reference project root, ``rm/`` = ``simulation/redmax/``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "sdfc_oracle.c")
+_LIB = os.path.join(_HERE, "_build", "libsdfc_oracle.so")
+
+COLLISION_VALUE = 11
+COLLISION_DERIV = 146
+# (name, offset, shape) of the derivative blocks of orc_collision's output
+COLLISION_BLOCKS = [
+    ("dd_dxw", 11, (3,)), ("dd_dq2", 14, (6,)), ("dn_dxw", 20, (3, 3)), ("dn_dq2", 29, (3, 6)),
+    ("dddot_dxw", 47, (3,)), ("dddot_dxwdot", 50, (3,)), ("dddot_dq2", 53, (6,)),
+    ("dddot_dphi2", 59, (6,)), ("dtdot_dxw", 65, (3, 3)), ("dtdot_dxwdot", 74, (3, 3)),
+    ("dtdot_dq2", 83, (3, 6)), ("dtdot_dphi2", 101, (3, 6)), ("dxi2_dxw", 119, (3, 3)),
+    ("dxi2_dq2", 128, (3, 6)),
+]
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement (no FMA contraction, see the C file header)."""
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+        os.makedirs(os.path.dirname(_LIB), exist_ok=True)
+        tmp = _LIB + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, _SRC, "-lm"])
+        os.replace(tmp, _LIB)
+    return _LIB
+
+
+class _Grid(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int), ("nk", ctypes.c_int),
+                ("min_box", ctypes.c_double * 3), ("max_box", ctypes.c_double * 3),
+                ("dx", ctypes.c_double * 3), ("col_th", ctypes.c_double),
+                ("v", ctypes.POINTER(ctypes.c_double))]
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("kn", ctypes.c_double), ("kt", ctypes.c_double), ("mu", ctypes.c_double),
+                ("damping", ctypes.c_double), ("scale", ctypes.c_double), ("contact_scale", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        d = ctypes.c_double
+        P = ctypes.POINTER
+        _lib.orc_query_sdf.restype = d
+        _lib.orc_query_sdf.argtypes = [P(_Grid), P(d), ctypes.c_int]
+        _lib.orc_distance.restype = d
+        _lib.orc_distance.argtypes = [P(_Grid), P(d), P(d)]
+        _lib.orc_collision.restype = None
+        _lib.orc_collision.argtypes = [P(_Grid), P(d), P(d), P(d), P(d), ctypes.c_int, P(d)]
+        _lib.orc_detect.restype = ctypes.c_int
+        _lib.orc_detect.argtypes = [P(_Grid), P(d), P(d), P(d), ctypes.c_int, P(ctypes.c_int), P(d)]
+        _lib.orc_pair_eval.restype = ctypes.c_int
+        _lib.orc_pair_eval.argtypes = [P(_Grid), P(d), ctypes.c_int, P(d), P(d), P(d), P(d), P(_Params),
+                                       ctypes.c_int, P(d), P(d), P(d), P(ctypes.c_int)]
+        _lib.orc_query_dsdf.argtypes = [P(_Grid), P(d), P(d)]
+        _lib.orc_query_ddsdf.argtypes = [P(_Grid), P(d), P(d)]
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+@dataclass
+class Grid:
+    """An SDF body's grid (rm/Body/BodySDFObj.h:13-16); values indexed [k, j, i] (i fastest)."""
+    values: np.ndarray  # shape (nk, nj, ni), float64
+    min_box: np.ndarray
+    max_box: np.ndarray
+    dx: np.ndarray
+    col_th: float
+
+    def _c(self):
+        v = _f64(self.values)
+        self._keep = v
+        nk, nj, ni = v.shape
+        g = _Grid(ni, nj, nk, (ctypes.c_double * 3)(*self.min_box), (ctypes.c_double * 3)(*self.max_box),
+                  (ctypes.c_double * 3)(*self.dx), float(self.col_th), _dp(v))
+        return g
+
+
+@dataclass
+class Params:
+    """ForceGeneralSDFContact coefficients (rm/Force/ForceGeneralSDFContact.h:16-20)."""
+    kn: float = 1.0
+    kt: float = 0.0
+    mu: float = 0.0
+    damping: float = 0.0
+    scale: float = 1.0
+    contact_scale: float = 1.0
+
+    def _c(self):
+        return _Params(self.kn, self.kt, self.mu, self.damping, self.scale, self.contact_scale)
+
+
+def query_sdf(grid: Grid, x, outside_accurate=False) -> float:
+    """BodySDFObj::query_SDF (rm/Body/BodySDFObj.cpp:123-174)."""
+    g = grid._c()
+    return lib().orc_query_sdf(ctypes.byref(g), _dp(_f64(x)), int(outside_accurate))
+
+
+def query_dsdf(grid: Grid, x) -> np.ndarray:
+    """BodySDFObj::query_dSDF (rm/Body/BodySDFObj.cpp:176-187)."""
+    g = grid._c()
+    out = np.zeros(3)
+    lib().orc_query_dsdf(ctypes.byref(g), _dp(_f64(x)), _dp(out))
+    return out
+
+
+def query_ddsdf(grid: Grid, x) -> np.ndarray:
+    """BodySDFObj::query_ddSDF (rm/Body/BodySDFObj.cpp:189-205)."""
+    g = grid._c()
+    out = np.zeros(9)
+    lib().orc_query_ddsdf(ctypes.byref(g), _dp(_f64(x)), _dp(out))
+    return out.reshape(3, 3)
+
+
+def distance(grid: Grid, E_B, xw) -> float:
+    """BodySDFObj::distance (rm/Body/BodySDFObj.cpp:207-213)."""
+    g = grid._c()
+    return lib().orc_distance(ctypes.byref(g), _dp(_f64(E_B)), _dp(_f64(xw)))
+
+
+def collision(grid: Grid, E_B, phi_B, xw, xw_dot, want_deriv=True) -> np.ndarray:
+    """BodySDFObj::collision (rm/Body/BodySDFObj.cpp:239-377); flat output, see COLLISION_BLOCKS."""
+    g = grid._c()
+    out = np.zeros(COLLISION_DERIV)
+    lib().orc_collision(ctypes.byref(g), _dp(_f64(E_B)), _dp(_f64(phi_B)), _dp(_f64(xw)), _dp(_f64(xw_dot)),
+                        int(want_deriv), _dp(out))
+    return out if want_deriv else out[:COLLISION_VALUE]
+
+
+def detect(grid: Grid, E_A, E_B, pts):
+    """collision_detection_general_SDF (rm/CollisionDetection/CollisionDetection.cpp:124-147).
+
+    Returns (active ids ascending, per-point distance)."""
+    g = grid._c()
+    p = _f64(pts).reshape(-1, 3)
+    ids = np.zeros(max(len(p), 1), dtype=np.int32)
+    dist = np.zeros(len(p))
+    n = lib().orc_detect(ctypes.byref(g), _dp(_f64(E_A)), _dp(_f64(E_B)), _dp(p), len(p),
+                         ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(dist))
+    return ids[:n].copy(), dist
+
+
+def pair_eval(grid: Grid, pts, E_A, phi_A, E_B, phi_B, params: Params, want_deriv=True):
+    """ForceGeneralSDFContact::computeForce[WithDerivative] (rm/Force/ForceGeneralSDFContact.cpp:46-105,
+    147-447) for one (contact body A, SDF body B) pair.  Returns (fm[12], Km[12,12], Dm[12,12], ids)."""
+    g = grid._c()
+    p = _f64(pts).reshape(-1, 3)
+    fm = np.zeros(12)
+    Km = np.zeros(144)
+    Dm = np.zeros(144)
+    ids = np.zeros(max(len(p), 1), dtype=np.int32)
+    prm = params._c()
+    n = lib().orc_pair_eval(ctypes.byref(g), _dp(p), len(p), _dp(_f64(E_A)), _dp(_f64(phi_A)), _dp(_f64(E_B)),
+                            _dp(_f64(phi_B)), ctypes.byref(prm), int(want_deriv), _dp(fm), _dp(Km), _dp(Dm),
+                            ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return fm, Km.reshape(12, 12), Dm.reshape(12, 12), ids[:n].copy()

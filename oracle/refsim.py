@@ -1,0 +1,261 @@
+"""ORACLE — test infrastructure, not the product.
+
+ctypes front end of ``oracle/_ref/libredmax_ref.so``: the reference redmax
+simulator compiled from its own sources (``oracle/ref/Makefile``) plus the
+extern "C" harness ``oracle/ref/ref_harness.cpp``.  It exists only where the
+reference sources are present; it pins the C restatement and generates the
+golden fixtures.  Nothing outside ``tests/`` and ``tests/golden/`` uses it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libredmax_ref.so")
+REFERENCE_ROOT = os.environ.get("SDFC_REFERENCE_ROOT", "/root/reference")
+
+
+def available() -> bool:
+    return os.path.exists(LIB_PATH)
+
+
+def build(jobs: int = 8) -> bool:
+    """Compile the reference + harness if the reference sources are present."""
+    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "simulation", "redmax")):
+        return False
+    subprocess.check_call(["make", "-s", "-C", os.path.join(_HERE, "ref"), f"REF={REFERENCE_ROOT}", f"-j{jobs}"])
+    return available()
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(LIB_PATH)
+        d, i, c = ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_char_p
+        v = ctypes.c_void_p
+        L.ref_sim_create.restype = v
+        L.ref_sim_create.argtypes = [c, c]
+        L.ref_sim_destroy.argtypes = [v]
+        L.ref_sim_ndof.argtypes = [v, ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.ref_body_index.argtypes = [v, c]
+        L.ref_body_mass_props.argtypes = [v, c, d, d, d, d]
+        L.ref_body_num_contact_points.argtypes = [v, c]
+        L.ref_body_get_contact_points.argtypes = [v, c, d, i]
+        L.ref_body_set_contact_points.argtypes = [v, c, d, i]
+        L.ref_body_set_sdf.argtypes = [v, c, i, i, i, d, d, d, ctypes.c_double, d]
+        L.ref_body_get_sdf_shape.argtypes = [v, c, ctypes.POINTER(i), d, d, d, d]
+        L.ref_body_get_sdf_values.argtypes = [v, c, d]
+        L.ref_body_set_pose.argtypes = [v, c, d, d]
+        L.ref_body_set_contact_scale.argtypes = [v, c, ctypes.c_double]
+        L.ref_collision.argtypes = [v, c, d, d, i, d]
+        L.ref_distance.argtypes = [v, c, d, i, d]
+        L.ref_pair_eval.argtypes = [v, c, c] + [ctypes.c_double] * 5 + [i, d, d, d, ctypes.POINTER(i), i,
+                                                                         ctypes.POINTER(i)]
+        L.ref_sim_reset.argtypes = [v, i]
+        L.ref_sim_set_state_init.argtypes = [v, d, d]
+        L.ref_sim_set_external_force.argtypes = [v, c, d]
+        L.ref_sim_forward.argtypes = [v, i]
+        L.ref_sim_is_converged.argtypes = [v]
+        L.ref_sim_get_state.argtypes = [v, d, d]
+        L.ref_sim_backward.argtypes = [v, d, i, d, d]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"reference harness: {what} failed ({rc})")
+
+
+# --------------------------------------------------------------------------- scene files
+
+def write_obj(path, V, F):
+    with open(path, "w") as f:
+        for v in V:
+            f.write(f"v {v[0]:.9g} {v[1]:.9g} {v[2]:.9g}\n")
+        for t in F:
+            f.write(f"f {t[0] + 1} {t[1] + 1} {t[2] + 1}\n")
+
+
+def box_mesh(half=(0.5, 0.5, 0.5), center=(0.0, 0.0, 0.0)):
+    hx, hy, hz = half
+    cx, cy, cz = center
+    V = np.array([[cx + sx * hx, cy + sy * hy, cz + sz * hz]
+                  for sz in (-1, 1) for sy in (-1, 1) for sx in (-1, 1)])
+    F = np.array([[0, 2, 1], [1, 2, 3], [4, 5, 6], [5, 7, 6], [0, 1, 4], [1, 5, 4],
+                  [2, 6, 3], [3, 6, 7], [0, 4, 2], [2, 4, 6], [1, 3, 5], [3, 7, 5]])
+    return V, F
+
+
+def two_body_xml(obj_a, obj_b, joint_a="free3d-exp", dx=0.1, col_th=0.01, kn=1e5, kt=1e3, mu=0.3, damping=1e3,
+                 timestep=5e-3, gravity=(0.0, 0.0, -9.8), pos_a=(0.0, 0.0, 0.0), res=20):
+    """XML for a moving contact body A ("A", joint `joint_a`) against a fixed SDF body B ("B").
+
+    Follows the planner's scene layout (examples/run_joint_plan.py:140-178): both bodies are SDF bodies
+    with OBJ_TO_JOINT transforms; only the A-points-vs-B-grid contact is listed."""
+    g = " ".join(repr(float(x)) for x in gravity)
+    pa = " ".join(repr(float(x)) for x in pos_a)
+    return f"""
+<redmax model="pair">
+<option integrator="BDF1" timestep="{timestep!r}" gravity="{g}"/>
+<robot>
+  <link name="A">
+    <joint name="A" type="{joint_a}" axis="0. 0. 0." pos="{pa}" quat="1 0 0 0" frame="WORLD" damping="0"/>
+    <body name="A" type="SDF" filename="{obj_a}" pos="0 0 0" quat="1 0 0 0" scale="1 1 1"
+          transform_type="OBJ_TO_JOINT" density="1" dx="{dx!r}" res="{res}" col_th="{col_th!r}" mu="0"
+          rgba="1 1 1 1"/>
+  </link>
+</robot>
+<robot>
+  <link name="B">
+    <joint name="B" type="fixed" pos="0 0 0" quat="1 0 0 0" frame="WORLD" damping="0"/>
+    <body name="B" type="SDF" filename="{obj_b}" pos="0 0 0" quat="1 0 0 0" scale="1 1 1"
+          transform_type="OBJ_TO_JOINT" density="1" dx="{dx!r}" res="{res}" col_th="{col_th!r}" mu="0"
+          rgba="1 1 1 1"/>
+  </link>
+</robot>
+<contact>
+  <general_SDF_contact general_body="A" SDF_body="B" kn="{kn!r}" kt="{kt!r}" mu="{mu!r}" damping="{damping!r}"/>
+</contact>
+</redmax>
+"""
+
+
+class RefSim:
+    """One reference Simulation built from an XML string (rm/Simulation_Constructor.cpp:123)."""
+
+    def __init__(self, xml: str, asset_folder: str):
+        self._h = lib().ref_sim_create(xml.encode(), asset_folder.encode())
+        if not self._h:
+            raise RuntimeError("reference Simulation construction failed")
+        nr, nm = ctypes.c_int(), ctypes.c_int()
+        lib().ref_sim_ndof(self._h, ctypes.byref(nr), ctypes.byref(nm))
+        self.ndof_r, self.ndof_m = nr.value, nm.value
+
+    def close(self):
+        if self._h:
+            lib().ref_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # bodies -------------------------------------------------------------
+    def mass_props(self, name):
+        m = np.zeros(1)
+        I = np.zeros(6)
+        Eji = np.zeros(16)
+        E0i = np.zeros(16)
+        _check(lib().ref_body_mass_props(self._h, name.encode(), _dp(m), _dp(I), _dp(Eji), _dp(E0i)), "mass_props")
+        return float(m[0]), I, Eji.reshape(4, 4), E0i.reshape(4, 4)
+
+    def contact_points(self, name):
+        n = lib().ref_body_num_contact_points(self._h, name.encode())
+        out = np.zeros((n, 3))
+        lib().ref_body_get_contact_points(self._h, name.encode(), _dp(out), n)
+        return out
+
+    def set_contact_points(self, name, pts):
+        p = _f64(pts).reshape(-1, 3)
+        _check(lib().ref_body_set_contact_points(self._h, name.encode(), _dp(p), len(p)), "set_contact_points")
+
+    def set_sdf(self, name, values, min_box, max_box, dx, col_th):
+        v = _f64(values)
+        nk, nj, ni = v.shape
+        _check(lib().ref_body_set_sdf(self._h, name.encode(), ni, nj, nk, _dp(_f64(min_box)), _dp(_f64(max_box)),
+                                      _dp(_f64(dx)), float(col_th), _dp(v)), "set_sdf")
+
+    def sdf(self, name):
+        nijk = (ctypes.c_int * 3)()
+        mn, mx, dx, ct = np.zeros(3), np.zeros(3), np.zeros(3), np.zeros(1)
+        _check(lib().ref_body_get_sdf_shape(self._h, name.encode(), nijk, _dp(mn), _dp(mx), _dp(dx), _dp(ct)),
+               "sdf_shape")
+        ni, nj, nk = nijk
+        v = np.zeros((nk, nj, ni))
+        lib().ref_body_get_sdf_values(self._h, name.encode(), _dp(v))
+        return v, mn, mx, dx, float(ct[0])
+
+    def set_pose(self, name, E, phi):
+        _check(lib().ref_body_set_pose(self._h, name.encode(), _dp(_f64(E)), _dp(_f64(phi))), "set_pose")
+
+    def set_contact_scale(self, name, s):
+        _check(lib().ref_body_set_contact_scale(self._h, name.encode(), float(s)), "set_contact_scale")
+
+    # queries ------------------------------------------------------------
+    def collision(self, name, xw, xw_dot, want_deriv=True):
+        out = np.zeros(146)
+        _check(lib().ref_collision(self._h, name.encode(), _dp(_f64(xw)), _dp(_f64(xw_dot)), int(want_deriv),
+                                   _dp(out)), "collision")
+        return out if want_deriv else out[:11]
+
+    def distance(self, name, xw):
+        p = _f64(xw).reshape(-1, 3)
+        out = np.zeros(len(p))
+        _check(lib().ref_distance(self._h, name.encode(), _dp(p), len(p), _dp(out)), "distance")
+        return out
+
+    def pair_eval(self, a, b, kn, kt, mu, damping, scale=1.0, want_deriv=True):
+        fm, Km, Dm = np.zeros(12), np.zeros(144), np.zeros(144)
+        cap = max(lib().ref_body_num_contact_points(self._h, a.encode()), 1)
+        ids = np.zeros(cap, dtype=np.int32)
+        n = ctypes.c_int()
+        _check(lib().ref_pair_eval(self._h, a.encode(), b.encode(), kn, kt, mu, damping, scale, int(want_deriv),
+                                   _dp(fm), _dp(Km), _dp(Dm), ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                   cap, ctypes.byref(n)), "pair_eval")
+        return fm, Km.reshape(12, 12), Dm.reshape(12, 12), ids[:n.value].copy()
+
+    # stepping -----------------------------------------------------------
+    def reset(self, backward=False):
+        _check(lib().ref_sim_reset(self._h, int(backward)), "reset")
+
+    def set_state_init(self, q, qdot):
+        _check(lib().ref_sim_set_state_init(self._h, _dp(_f64(q)), _dp(_f64(qdot))), "set_state_init")
+
+    def set_external_force(self, name, f6):
+        _check(lib().ref_sim_set_external_force(self._h, name.encode(), _dp(_f64(f6))), "set_external_force")
+
+    def forward(self, n):
+        _check(lib().ref_sim_forward(self._h, int(n)), "forward")
+
+    def is_converged(self):
+        return bool(lib().ref_sim_is_converged(self._h))
+
+    def state(self):
+        q, qd = np.zeros(self.ndof_r), np.zeros(self.ndof_r)
+        _check(lib().ref_sim_get_state(self._h, _dp(q), _dp(qd)), "get_state")
+        return q, qd
+
+    def backward(self, df_dq, T):
+        g0, gd0 = np.zeros(self.ndof_r), np.zeros(self.ndof_r)
+        _check(lib().ref_sim_backward(self._h, _dp(_f64(df_dq)), int(T), _dp(g0), _dp(gd0)), "backward")
+        return g0, gd0
+
+
+def make_pair_sim(joint_a="free3d-exp", half_a=(0.3, 0.3, 0.3), half_b=(0.5, 0.5, 0.5), workdir=None, **kw):
+    """A two-box reference scene whose grid / points the caller overwrites."""
+    workdir = workdir or tempfile.mkdtemp(prefix="refsim_")
+    Va, Fa = box_mesh(half_a)
+    Vb, Fb = box_mesh(half_b)
+    write_obj(os.path.join(workdir, "a.obj"), Va, Fa)
+    write_obj(os.path.join(workdir, "b.obj"), Vb, Fb)
+    xml = two_body_xml("a.obj", "b.obj", joint_a=joint_a, **kw)
+    return RefSim(xml, workdir), workdir

@@ -1,0 +1,61 @@
+/*
+ * ORACLE — test infrastructure, not the product.  See sdfc_oracle.c.
+ */
+#ifndef SDFC_ORACLE_H
+#define SDFC_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* An SDF grid as BodySDFObj holds it (simulation/redmax/Body/BodySDFObj.h:13-16). */
+typedef struct {
+    int ni, nj, nk;
+    double min_box[3], max_box[3];
+    double dx[3];   /* _dx, _dy, _dz */
+    double col_th;  /* _col_th, added to every distance */
+    const double* v; /* ni*nj*nk values, i fastest */
+} orc_grid;
+
+/* ForceGeneralSDFContact coefficients (simulation/redmax/Force/ForceGeneralSDFContact.h:16-20)
+ * plus the contact body's _contact_scale. */
+typedef struct {
+    double kn, kt, mu, damping, scale, contact_scale;
+} orc_params;
+
+/* Layout of orc_collision's output (row-major blocks). */
+enum {
+    ORC_COLLISION_VALUE = 11, /* d, n[3], ddot, tdot[3], xi2[3] */
+    ORC_C_DD_DXW = 11,
+    ORC_C_DD_DQ2 = 14,
+    ORC_C_DN_DXW = 20,
+    ORC_C_DN_DQ2 = 29,
+    ORC_C_DDDOT_DXW = 47,
+    ORC_C_DDDOT_DXWDOT = 50,
+    ORC_C_DDDOT_DQ2 = 53,
+    ORC_C_DDDOT_DPHI2 = 59,
+    ORC_C_DTDOT_DXW = 65,
+    ORC_C_DTDOT_DXWDOT = 74,
+    ORC_C_DTDOT_DQ2 = 83,
+    ORC_C_DTDOT_DPHI2 = 101,
+    ORC_C_DXI2_DXW = 119,
+    ORC_C_DXI2_DQ2 = 128,
+    ORC_COLLISION_DERIV = 146
+};
+
+double orc_query_sdf(const orc_grid* g, const double* x, int outside_accurate);
+void orc_query_dsdf(const orc_grid* g, const double* x, double* v);
+void orc_query_ddsdf(const orc_grid* g, const double* x, double* H);
+double orc_distance(const orc_grid* g, const double* E_B, const double* xw);
+void orc_collision(const orc_grid* g, const double* E_B, const double* phi_B, const double* xw,
+                   const double* xw_dot, int want_deriv, double* out);
+int orc_detect(const orc_grid* g, const double* E_A, const double* E_B, const double* pts, int n, int* ids,
+               double* dist_out);
+int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double* E_A, const double* phi_A,
+                  const double* E_B, const double* phi_B, const orc_params* prm, int want_deriv, double* fm,
+                  double* Km, double* Dm, int* ids);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
