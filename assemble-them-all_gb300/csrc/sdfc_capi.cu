@@ -1,0 +1,494 @@
+// C ABI of libsdfcontact (include/sdfc.h): contexts, uploads, batches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sdfc.h"
+#include "sdfc_kernels.cuh"
+
+using sdfc::GridDesc;
+using sdfc::InstanceDesc;
+using sdfc::PointsDesc;
+
+namespace {
+
+struct DeviceBuffer {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sdfc_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<GridDesc> grids;     // host copies of the descriptors
+    std::vector<PointsDesc> points;
+    std::vector<void*> allocations;  // every device allocation owned by the context
+    GridDesc* d_grids = nullptr;
+    PointsDesc* d_points = nullptr;
+    int grid_cap = 0, points_cap = 0;
+    sdfc_batch* single = nullptr;     // cached one-instance batch of sdfc_evaluate
+    int single_points = -1, single_grid = -1;
+    std::vector<sdfc_batch*> batches;  // live batches, destroyed with the context
+};
+
+struct sdfc_batch {
+    sdfc_context* ctx = nullptr;
+    int n = 0;
+    int total_tiles = 0;
+    std::vector<InstanceDesc> inst;
+    InstanceDesc* d_inst = nullptr;
+    int* d_tile_inst = nullptr;
+    int* d_ids = nullptr;
+    int* d_tile_count = nullptr;
+    double* d_partial = nullptr;
+    unsigned long long* d_recheck = nullptr;
+    // staging of the host-array entry points
+    double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
+    double* d_out = nullptr;  // n x 300: fm | Km | Dm
+    int* d_int = nullptr;     // n x 2: n_active | status
+    double* h_in = nullptr;   // pinned
+    double* h_out = nullptr;  // pinned
+    int* h_int = nullptr;     // pinned
+};
+
+namespace {
+
+int fail(sdfc_context* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                              \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) return fail((ctx), SDFC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+int dev_alloc(sdfc_context* ctx, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return SDFC_OK;
+}
+
+int use_device(sdfc_context* ctx) {
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return SDFC_OK;
+}
+
+template <class T>
+int sync_table(sdfc_context* ctx, std::vector<T>& host, T** d_table, int* cap) {
+    if ((int)host.size() > *cap) {
+        int ncap = std::max(64, *cap * 2);
+        while (ncap < (int)host.size()) ncap *= 2;
+        void* p = nullptr;
+        int rc = dev_alloc(ctx, &p, sizeof(T) * ncap);
+        if (rc) return rc;
+        if (*d_table) cudaFree(*d_table);
+        *d_table = (T*)p;
+        *cap = ncap;
+    }
+    CUDA_TRY(ctx, cudaMemcpy(*d_table, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice));
+    return SDFC_OK;
+}
+
+void free_batch(sdfc_batch* b) {
+    if (!b) return;
+    cudaFree(b->d_inst);
+    cudaFree(b->d_tile_inst);
+    cudaFree(b->d_ids);
+    cudaFree(b->d_tile_count);
+    cudaFree(b->d_partial);
+    cudaFree(b->d_recheck);
+    cudaFree(b->d_in);
+    cudaFree(b->d_out);
+    cudaFree(b->d_int);
+    cudaFreeHost(b->h_in);
+    cudaFreeHost(b->h_out);
+    cudaFreeHost(b->h_int);
+    delete b;
+}
+
+int run_batch(sdfc_batch* b, const double* EA, const double* phiA, const double* EB, const double* phiB,
+              const double* prm, bool deriv, double* fm, double* Km, double* Dm, int* n_active, int* status,
+              cudaStream_t stream) {
+    sdfc_context* ctx = b->ctx;
+    sdfc::BatchInputs in{EA, phiA, EB, phiB, prm};
+    sdfc::BatchOutputs out{fm, Km, Dm, n_active, status};
+    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->total_tiles, in, ctx->d_grids, ctx->d_points, b->d_ids,
+                        b->d_tile_count, b->d_recheck, stream);
+    sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, b->d_ids, b->d_tile_count, b->d_partial,
+                       deriv, stream);
+    sdfc::launch_finalize(b->d_inst, b->n, b->d_tile_count, b->d_partial, deriv, out, stream);
+    CUDA_TRY(ctx, cudaGetLastError());
+    return SDFC_OK;
+}
+
+bool all_finite(const double* v, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdfc_create(sdfc_context** out, int device) {
+    if (!out) return SDFC_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return SDFC_ERR_CUDA;
+    auto* ctx = new sdfc_context();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return SDFC_ERR_CUDA;
+    }
+    *out = ctx;
+    return SDFC_OK;
+}
+
+void sdfc_destroy(sdfc_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (sdfc_batch* b : ctx->batches) free_batch(b);
+    free_batch(ctx->single);
+    for (void* p : ctx->allocations) cudaFree(p);
+    cudaFree(ctx->d_grids);
+    cudaFree(ctx->d_points);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* sdfc_last_error(const sdfc_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
+                     const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (!values || !min_box || !max_box || !dxyz || !grid)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: null argument");
+    if (ni < 2 || nj < 2 || nk < 2) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: each extent must be >= 2");
+    if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: unknown storage");
+    const int nn[3] = {ni, nj, nk};
+    for (int a = 0; a < 3; ++a) {
+        if (!(dxyz[a] > 0.0) || !std::isfinite(dxyz[a]) || !std::isfinite(min_box[a]) || !std::isfinite(max_box[a]) ||
+            !(max_box[a] > min_box[a]))
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: invalid box or spacing");
+        // the reference's cell index floor((x - min) / dx) must stay < n for x <= max
+        if (std::floor((max_box[a] - min_box[a]) / dxyz[a]) > nn[a] - 1)
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: box extends past the last grid node");
+    }
+    if (!std::isfinite(col_th)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite col_th");
+    const size_t n = (size_t)ni * nj * nk;
+    if (!all_finite(values, n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite value");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+
+    std::vector<float> v32(n);
+    double vmax = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        v32[i] = (float)values[i];
+        vmax = std::max(vmax, std::fabs(values[i]));
+    }
+    // Lipschitz bound of the trilinear interpolant: per axis the largest
+    // neighbour difference over the spacing.
+    double lip2 = 0.0;
+    const size_t st[3] = {1, (size_t)ni, (size_t)ni * nj};
+    for (int a = 0; a < 3; ++a) {
+        double m = 0.0;
+        for (int k = 0; k < nk; ++k)
+            for (int j = 0; j < nj; ++j)
+                for (int i = 0; i < ni; ++i) {
+                    int c[3] = {i, j, k};
+                    if (c[a] + 1 >= nn[a]) continue;
+                    size_t idx = i + st[1] * j + st[2] * k;
+                    m = std::max(m, std::fabs(values[idx + st[a]] - values[idx]));
+                }
+        lip2 += (m / dxyz[a]) * (m / dxyz[a]);
+    }
+    GridDesc g{};
+    g.ni = ni;
+    g.nj = nj;
+    g.nk = nk;
+    g.storage = storage;
+    for (int a = 0; a < 3; ++a) {
+        g.min_box[a] = min_box[a];
+        g.max_box[a] = max_box[a];
+        g.dx[a] = dxyz[a];
+        g.fmin[a] = (float)min_box[a];
+        g.fmax[a] = (float)max_box[a];
+        g.finv_dx[a] = (float)(1.0 / dxyz[a]);
+    }
+    g.col_th = col_th;
+    g.lip = (float)(std::sqrt(lip2) * 1.0001);
+    g.vmax = (float)(vmax * 1.0001);
+    void* p32 = nullptr;
+    if ((rc = dev_alloc(ctx, &p32, n * sizeof(float)))) return rc;
+    ctx->allocations.push_back(p32);
+    CUDA_TRY(ctx, cudaMemcpy(p32, v32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    g.v32 = (const float*)p32;
+    if (storage == SDFC_STORAGE_F64) {
+        void* p64 = nullptr;
+        if ((rc = dev_alloc(ctx, &p64, n * sizeof(double)))) return rc;
+        ctx->allocations.push_back(p64);
+        CUDA_TRY(ctx, cudaMemcpy(p64, values, n * sizeof(double), cudaMemcpyHostToDevice));
+        g.v64 = (const double*)p64;
+    }
+    ctx->grids.push_back(g);
+    if ((rc = sync_table(ctx, ctx->grids, &ctx->d_grids, &ctx->grid_cap))) {
+        ctx->grids.pop_back();
+        return rc;
+    }
+    *grid = (int)ctx->grids.size() - 1;
+    return SDFC_OK;
+}
+
+int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage, int* points) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if ((!xyz && n > 0) || n < 0 || !points) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_points: bad argument");
+    if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_points: unknown storage");
+    if (!all_finite(xyz, 3 * (size_t)n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_points: non-finite point");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    std::vector<float> s32(3 * (size_t)n);
+    std::vector<double> s64(3 * (size_t)n);
+    double r = 0.0;
+    for (int i = 0; i < n; ++i) {
+        for (int a = 0; a < 3; ++a) {
+            s64[(size_t)a * n + i] = xyz[3 * (size_t)i + a];
+            s32[(size_t)a * n + i] = (float)xyz[3 * (size_t)i + a];
+        }
+        r = std::max(r, std::sqrt(xyz[3 * i] * xyz[3 * i] + xyz[3 * i + 1] * xyz[3 * i + 1] + xyz[3 * i + 2] * xyz[3 * i + 2]));
+    }
+    PointsDesc P{};
+    P.n = n;
+    P.storage = storage;
+    P.radius = (float)(r * 1.0001);
+    void* p32 = nullptr;
+    if ((rc = dev_alloc(ctx, &p32, s32.size() * sizeof(float)))) return rc;
+    ctx->allocations.push_back(p32);
+    CUDA_TRY(ctx, cudaMemcpy(p32, s32.data(), s32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    P.x32 = (const float*)p32;
+    if (storage == SDFC_STORAGE_F64) {
+        void* p64 = nullptr;
+        if ((rc = dev_alloc(ctx, &p64, s64.size() * sizeof(double)))) return rc;
+        ctx->allocations.push_back(p64);
+        CUDA_TRY(ctx, cudaMemcpy(p64, s64.data(), s64.size() * sizeof(double), cudaMemcpyHostToDevice));
+        P.x64 = (const double*)p64;
+    }
+    ctx->points.push_back(P);
+    if ((rc = sync_table(ctx, ctx->points, &ctx->d_points, &ctx->points_cap))) {
+        ctx->points.pop_back();
+        return rc;
+    }
+    *points = (int)ctx->points.size() - 1;
+    return SDFC_OK;
+}
+
+static int batch_create_impl(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** out) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (n <= 0 || !points || !grids || !out) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_create: bad argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    auto* b = new sdfc_batch();
+    b->ctx = ctx;
+    b->n = n;
+    b->inst.resize(n);
+    std::vector<int> tile_inst;
+    int tiles = 0;
+    for (int k = 0; k < n; ++k) {
+        if (points[k] < 0 || points[k] >= (int)ctx->points.size() || grids[k] < 0 || grids[k] >= (int)ctx->grids.size()) {
+            delete b;
+            return fail(ctx, SDFC_ERR_NOT_FOUND, "batch_create: unknown point-set or grid handle");
+        }
+        int np = ctx->points[points[k]].n;
+        int nt = (np + sdfc::kTile - 1) / sdfc::kTile;
+        if (nt > sdfc::kMaxTilesPerInstance) {
+            delete b;
+            return fail(ctx, SDFC_ERR_CAPACITY, "batch_create: point set larger than kTile*kMaxTilesPerInstance");
+        }
+        b->inst[k] = InstanceDesc{points[k], grids[k], tiles, nt};
+        for (int t = 0; t < nt; ++t) tile_inst.push_back(k);
+        tiles += nt;
+    }
+    b->total_tiles = tiles;
+    auto alloc = [&](void** p, size_t bytes) { return dev_alloc(ctx, p, bytes); };
+    if ((rc = alloc((void**)&b->d_inst, sizeof(InstanceDesc) * n)) ||
+        (rc = alloc((void**)&b->d_tile_inst, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_ids, sizeof(int) * (size_t)std::max(tiles, 1) * sdfc::kTile)) ||
+        (rc = alloc((void**)&b->d_tile_count, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
+        (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
+        (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
+        (rc = alloc((void**)&b->d_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv)) ||
+        (rc = alloc((void**)&b->d_int, sizeof(int) * (size_t)n * 2))) {
+        free_batch(b);
+        return rc;
+    }
+    if (cudaMallocHost((void**)&b->h_in, sizeof(double) * (size_t)n * 50) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_int, sizeof(int) * (size_t)n * 2) != cudaSuccess) {
+        free_batch(b);
+        return fail(ctx, SDFC_ERR_CUDA, "batch_create: cudaMallocHost failed");
+    }
+    cudaError_t e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && tiles > 0)
+        e = cudaMemcpy(b->d_tile_inst, tile_inst.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_recheck, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_tile_count, 0, sizeof(int) * std::max(tiles, 1));
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return fail(ctx, SDFC_ERR_CUDA, std::string("batch_create: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return SDFC_OK;
+}
+
+int sdfc_batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** out) {
+    int rc = batch_create_impl(ctx, n, points, grids, out);
+    if (rc == SDFC_OK) ctx->batches.push_back(*out);
+    return rc;
+}
+
+void sdfc_batch_destroy(sdfc_batch* b) {
+    if (!b) return;
+    sdfc_context* ctx = b->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    auto it = std::find(ctx->batches.begin(), ctx->batches.end(), b);
+    if (it != ctx->batches.end()) ctx->batches.erase(it);
+    free_batch(b);
+}
+
+int sdfc_batch_evaluate_device(sdfc_batch* b, const double* E_A, const double* phi_A, const double* E_B,
+                               const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
+                               double* Dm, int* n_active, int* status, void* stream) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!E_A || !phi_A || !E_B || !phi_B || !params || !fm || !n_active || !status || (want_deriv && (!Km || !Dm)))
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_evaluate_device: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return run_batch(b, E_A, phi_A, E_B, phi_B, params, want_deriv != 0, fm, Km, Dm, n_active, status, s);
+}
+
+int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, const double* E_B, const double* phi_B,
+                        const sdfc_params* params, int want_deriv, double* fm, double* Km, double* Dm, int* n_active,
+                        int* status) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!E_A || !phi_A || !E_B || !phi_B || !params || !fm || (want_deriv && (!Km || !Dm)))
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_evaluate: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    const size_t n = (size_t)b->n;
+    double* h = b->h_in;
+    std::memcpy(h, E_A, sizeof(double) * 16 * n);
+    std::memcpy(h + 16 * n, phi_A, sizeof(double) * 6 * n);
+    std::memcpy(h + 22 * n, E_B, sizeof(double) * 16 * n);
+    std::memcpy(h + 38 * n, phi_B, sizeof(double) * 6 * n);
+    for (size_t k = 0; k < n; ++k) {
+        double* p = h + 44 * n + 6 * k;
+        p[0] = params[k].kn;
+        p[1] = params[k].kt;
+        p[2] = params[k].mu;
+        p[3] = params[k].damping;
+        p[4] = params[k].scale;
+        p[5] = params[k].contact_scale;
+    }
+    cudaStream_t s = ctx->stream;
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->d_in, h, sizeof(double) * 50 * n, cudaMemcpyHostToDevice, s));
+    double* d = b->d_in;
+    double* o = b->d_out;
+    rc = run_batch(b, d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n, want_deriv != 0, o, o + 12 * n, o + 156 * n,
+                   b->d_int, b->d_int + n, s);
+    if (rc) return rc;
+    const size_t nout = want_deriv ? 300 * n : 12 * n;
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->h_out, o, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->h_int, b->d_int, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    std::memcpy(fm, b->h_out, sizeof(double) * 12 * n);
+    if (want_deriv) {
+        std::memcpy(Km, b->h_out + 12 * n, sizeof(double) * 144 * n);
+        std::memcpy(Dm, b->h_out + 156 * n, sizeof(double) * 144 * n);
+    }
+    if (n_active) std::memcpy(n_active, b->h_int, sizeof(int) * n);
+    if (status) std::memcpy(status, b->h_int + n, sizeof(int) * n);
+    return SDFC_OK;
+}
+
+int sdfc_batch_recheck_count(sdfc_batch* b, unsigned long long* count, int reset) {
+    if (!b || !count) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpy(count, b->d_recheck, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    if (reset) CUDA_TRY(ctx, cudaMemset(b->d_recheck, 0, sizeof(unsigned long long)));
+    return SDFC_OK;
+}
+
+int sdfc_evaluate(sdfc_context* ctx, int points, int grid, const double* E_A, const double* phi_A, const double* E_B,
+                  const double* phi_B, const sdfc_params* params, int want_deriv, double* fm, double* Km, double* Dm,
+                  int* n_active) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (!ctx->single || ctx->single_points != points || ctx->single_grid != grid) {
+        int rc = use_device(ctx);
+        if (rc) return rc;
+        cudaStreamSynchronize(ctx->stream);
+        free_batch(ctx->single);
+        ctx->single = nullptr;
+        ctx->single_points = ctx->single_grid = -1;
+        sdfc_batch* b = nullptr;
+        rc = batch_create_impl(ctx, 1, &points, &grid, &b);
+        if (rc) return rc;
+        ctx->single = b;
+        ctx->single_points = points;
+        ctx->single_grid = grid;
+    }
+    int status = 0, nact = 0;
+    int rc = sdfc_batch_evaluate(ctx->single, E_A, phi_A, E_B, phi_B, params, want_deriv, fm, Km, Dm, &nact, &status);
+    if (rc) return rc;
+    if (n_active) *n_active = nact;
+    return SDFC_OK;
+}
+
+int sdfc_active_ids(sdfc_context* ctx, int* ids, int cap, int* n) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (!n || (cap > 0 && !ids)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "active_ids: bad argument");
+    sdfc_batch* b = ctx->single;
+    if (!b) return fail(ctx, SDFC_ERR_NOT_FOUND, "active_ids: no evaluation yet");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    const int tiles = b->total_tiles;
+    std::vector<int> counts(std::max(tiles, 1));
+    if (tiles > 0)
+        CUDA_TRY(ctx, cudaMemcpy(counts.data(), b->d_tile_count, sizeof(int) * tiles, cudaMemcpyDeviceToHost));
+    int total = 0;
+    for (int t = 0; t < tiles; ++t) {
+        int c = counts[t];
+        int take = std::max(0, std::min(c, cap - total));
+        if (take > 0)
+            CUDA_TRY(ctx, cudaMemcpy(ids + total, b->d_ids + (size_t)t * sdfc::kTile, sizeof(int) * take,
+                                     cudaMemcpyDeviceToHost));
+        total += c;
+    }
+    *n = total;
+    return SDFC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,211 @@
+"""Python host side of libsdfcontact (include/sdfc.h), through ctypes.
+
+The GPU path is the only path: if the shared library is missing this module
+raises on import, and every call goes to the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsdfcontact.so")
+
+SDFC_OK = 0
+STORAGE_F64 = 0
+STORAGE_F32 = 1
+
+# every symbol include/sdfc.h declares
+EXPORTS = (
+    "sdfc_create", "sdfc_destroy", "sdfc_last_error", "sdfc_upload_grid", "sdfc_upload_points",
+    "sdfc_evaluate", "sdfc_active_ids", "sdfc_batch_create", "sdfc_batch_destroy", "sdfc_batch_evaluate",
+    "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count",
+)
+
+
+class SdfcError(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    """sdfc_params: ForceGeneralSDFContact's kn, kt, mu, damping, scale and the contact body's contact_scale."""
+    _fields_ = [("kn", ctypes.c_double), ("kt", ctypes.c_double), ("mu", ctypes.c_double),
+                ("damping", ctypes.c_double), ("scale", ctypes.c_double), ("contact_scale", ctypes.c_double)]
+
+    def __init__(self, kn=1.0, kt=0.0, mu=0.0, damping=0.0, scale=1.0, contact_scale=1.0):
+        super().__init__(kn, kt, mu, damping, scale, contact_scale)
+
+    def as_row(self):
+        return np.array([self.kn, self.kt, self.mu, self.damping, self.scale, self.contact_scale])
+
+
+_lib = None
+
+
+def lib():
+    """Loads libsdfcontact.so; raises if it was not built (no fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SdfcError(f"{LIB_PATH} is missing: run the package build (build.build()) first")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER
+        d, i, v = P(ctypes.c_double), ctypes.c_int, ctypes.c_void_p
+        L.sdfc_create.argtypes = [P(v), i]
+        L.sdfc_destroy.argtypes = [v]
+        L.sdfc_destroy.restype = None
+        L.sdfc_last_error.argtypes = [v]
+        L.sdfc_last_error.restype = ctypes.c_char_p
+        L.sdfc_upload_grid.argtypes = [v, d, i, i, i, d, d, d, ctypes.c_double, i, P(i)]
+        L.sdfc_upload_points.argtypes = [v, d, i, i, P(i)]
+        L.sdfc_evaluate.argtypes = [v, i, i, d, d, d, d, P(Params), i, d, d, d, P(i)]
+        L.sdfc_active_ids.argtypes = [v, P(i), i, P(i)]
+        L.sdfc_batch_create.argtypes = [v, i, P(i), P(i), P(v)]
+        L.sdfc_batch_destroy.argtypes = [v]
+        L.sdfc_batch_destroy.restype = None
+        L.sdfc_batch_evaluate.argtypes = [v, d, d, d, d, P(Params), i, d, d, d, P(i), P(i)]
+        L.sdfc_batch_evaluate_device.argtypes = [v, v, v, v, v, v, i, v, v, v, v, v, v]
+        L.sdfc_batch_recheck_count.argtypes = [v, P(ctypes.c_ulonglong), i]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Context:
+    """A device context (sdfc_create): owns uploaded grids and point sets."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        rc = lib().sdfc_create(ctypes.byref(self._h), int(device))
+        if rc != SDFC_OK:
+            raise SdfcError(f"sdfc_create failed ({rc}): no usable CUDA device {device}")
+        self.device = device
+        self._npoints = {}
+        self._batches = []
+
+    def _check(self, rc, what):
+        if rc != SDFC_OK:
+            raise SdfcError(f"{what} failed ({rc}): {lib().sdfc_last_error(self._h).decode()}")
+
+    def close(self):
+        if self._h:
+            lib().sdfc_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_grid(self, values, min_box, max_box, dx, col_th, storage=STORAGE_F32) -> int:
+        """values: (nk, nj, ni) array (i fastest), as BodySDFObj::_SDF."""
+        v = _f64(values)
+        nk, nj, ni = v.shape
+        h = ctypes.c_int()
+        self._check(lib().sdfc_upload_grid(self._h, _dp(v), ni, nj, nk, _dp(_f64(min_box, 3)), _dp(_f64(max_box, 3)),
+                                           _dp(_f64(dx, 3)), float(col_th), int(storage), ctypes.byref(h)),
+                    "sdfc_upload_grid")
+        return h.value
+
+    def upload_points(self, xyz, storage=STORAGE_F32) -> int:
+        p = _f64(xyz).reshape(-1, 3)
+        h = ctypes.c_int()
+        self._check(lib().sdfc_upload_points(self._h, _dp(p), len(p), int(storage), ctypes.byref(h)),
+                    "sdfc_upload_points")
+        self._npoints[h.value] = len(p)
+        return h.value
+
+    def evaluate(self, points, grid, E_A, phi_A, E_B, phi_B, params: Params, want_deriv=True):
+        """One ForceGeneralSDFContact call; returns (fm[12], Km[12,12], Dm[12,12], n_active)."""
+        fm = np.zeros(12)
+        Km = np.zeros(144)
+        Dm = np.zeros(144)
+        n = ctypes.c_int()
+        self._check(lib().sdfc_evaluate(self._h, int(points), int(grid), _dp(_f64(E_A, 16)), _dp(_f64(phi_A, 6)),
+                                        _dp(_f64(E_B, 16)), _dp(_f64(phi_B, 6)), ctypes.byref(params),
+                                        int(bool(want_deriv)), _dp(fm), _dp(Km), _dp(Dm), ctypes.byref(n)),
+                    "sdfc_evaluate")
+        return fm, Km.reshape(12, 12), Dm.reshape(12, 12), n.value
+
+    def active_ids(self, cap=None):
+        n = ctypes.c_int()
+        if cap is None:
+            self._check(lib().sdfc_active_ids(self._h, None, 0, ctypes.byref(n)), "sdfc_active_ids")
+            cap = n.value
+        ids = np.zeros(max(cap, 1), dtype=np.int32)
+        self._check(lib().sdfc_active_ids(self._h, _ip(ids), cap, ctypes.byref(n)), "sdfc_active_ids")
+        return ids[:min(cap, n.value)].copy()
+
+    def batch(self, points, grids) -> "Batch":
+        return Batch(self, points, grids)
+
+
+class Batch:
+    """sdfc_batch: n pair instances evaluated by one set of launches."""
+
+    def __init__(self, ctx: Context, points, grids):
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.int32))
+        grd = np.ascontiguousarray(np.asarray(grids, dtype=np.int32))
+        if pts.shape != grd.shape or pts.ndim != 1:
+            raise ValueError("points and grids must be equal-length 1-D handle arrays")
+        self.ctx = ctx
+        self.n = len(pts)
+        self._h = ctypes.c_void_p()
+        ctx._check(lib().sdfc_batch_create(ctx._h, self.n, _ip(pts), _ip(grd), ctypes.byref(self._h)),
+                   "sdfc_batch_create")
+
+    def close(self):
+        if self._h and self.ctx._h:
+            lib().sdfc_batch_destroy(self._h)
+        self._h = ctypes.c_void_p()
+
+    def evaluate(self, E_A, phi_A, E_B, phi_B, params, want_deriv=True):
+        """Host arrays in, host arrays out: (fm[n,12], Km[n,12,12], Dm[n,12,12], n_active[n], status[n])."""
+        n = self.n
+        prm = (Params * n)()
+        for k in range(n):
+            p = params[k] if isinstance(params, (list, tuple)) else params
+            prm[k] = p
+        fm = np.zeros(12 * n)
+        Km = np.zeros(144 * n) if want_deriv else np.zeros(1)
+        Dm = np.zeros(144 * n) if want_deriv else np.zeros(1)
+        nact = np.zeros(n, dtype=np.int32)
+        st = np.zeros(n, dtype=np.int32)
+        self.ctx._check(lib().sdfc_batch_evaluate(self._h, _dp(_f64(E_A, 16 * n)), _dp(_f64(phi_A, 6 * n)),
+                                                  _dp(_f64(E_B, 16 * n)), _dp(_f64(phi_B, 6 * n)), prm,
+                                                  int(bool(want_deriv)), _dp(fm), _dp(Km), _dp(Dm), _ip(nact),
+                                                  _ip(st)), "sdfc_batch_evaluate")
+        if want_deriv:
+            return fm.reshape(n, 12), Km.reshape(n, 12, 12), Dm.reshape(n, 12, 12), nact, st
+        return fm.reshape(n, 12), None, None, nact, st
+
+    def evaluate_device(self, E_A, phi_A, E_B, phi_B, params, fm, Km, Dm, n_active, status, want_deriv=True,
+                        stream=0):
+        """Device pointers (ints, e.g. torch tensor.data_ptr()); enqueued on `stream` without syncing."""
+        self.ctx._check(lib().sdfc_batch_evaluate_device(self._h, E_A, phi_A, E_B, phi_B, params,
+                                                         int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active,
+                                                         status, stream or None), "sdfc_batch_evaluate_device")
+
+    def recheck_count(self, reset=False) -> int:
+        c = ctypes.c_ulonglong()
+        self.ctx._check(lib().sdfc_batch_recheck_count(self._h, ctypes.byref(c), int(bool(reset))),
+                        "sdfc_batch_recheck_count")
+        return c.value

@@ -1,0 +1,137 @@
+/*
+ * sdfc.h — C ABI of the GB300 point-vs-SDF penalty contact library
+ * (libsdfcontact.so).
+ *
+ * It replaces, for the redmax simulator of Assemble-Them-All, the contact
+ * force between the surface points of one body and the signed-distance grid
+ * of another:
+ *
+ *   ForceGeneralSDFContact::computeForce               simulation/redmax/Force/ForceGeneralSDFContact.cpp:46-67
+ *   ForceGeneralSDFContact::computeForceWithDerivative simulation/redmax/Force/ForceGeneralSDFContact.cpp:69-105
+ *     (the Force plugin interface, simulation/redmax/Force/Force.h:40-47)
+ *   collision_detection_general_SDF                    simulation/redmax/CollisionDetection/CollisionDetection.cpp:124-147
+ *   BodySDFObj::distance / collision                   simulation/redmax/Body/BodySDFObj.cpp:207-377
+ *
+ * Conventions (the reference's):
+ *   - poses E are 4x4 row-major homogeneous matrices [R p; 0 1] (Body::_E_0i);
+ *   - body twists phi = (w, v) are in the body frame (Body::_phi);
+ *   - grids are indexed values[i + ni*(j + nj*k)] in the SDF body's frame
+ *     (BodySDFObj::_SDF, simulation/externals/sdfgen/array3.h:70-79), with
+ *     _min_box, _max_box, _dx/_dy/_dz and _col_th as in BodySDFObj.h:13-15;
+ *   - contact points are the contact body's Body::_contact_points, body frame;
+ *   - fm is the 12-vector [body A (6); body B (6)] and Km = dfm/dq, Dm =
+ *     dfm/dphi the 12x12 row-major blocks that ForceGeneralSDFContact adds
+ *     into the simulator's maximal-coordinate arrays (ForceGeneralSDFContact.cpp:88-99).
+ *     The library writes (=) these sub-blocks; the caller adds them at the
+ *     bodies' indices as the reference does.
+ *
+ * All entry points return SDFC_OK (0) or a negative status; no C++ exception
+ * crosses this boundary.  Host arrays are caller-owned; device memory is owned
+ * by the context.  A context is bound to one CUDA device and is not
+ * thread-safe (the reference calls its forces from one thread).
+ */
+#ifndef SDFC_H
+#define SDFC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDFC_OK 0
+#define SDFC_ERR_INVALID_ARGUMENT (-1)
+#define SDFC_ERR_CUDA (-2)
+#define SDFC_ERR_NOT_FOUND (-3)
+#define SDFC_ERR_CAPACITY (-4)
+
+/* storage of grid values / contact points on the device */
+#define SDFC_STORAGE_F64 0
+#define SDFC_STORAGE_F32 1
+
+typedef struct sdfc_context sdfc_context;
+typedef struct sdfc_batch sdfc_batch;
+
+/* Contact coefficients of one pair: ForceGeneralSDFContact::_kn, _kt, _mu,
+ * _damping, _scale (ForceGeneralSDFContact.h:16-20) and the contact body's
+ * Body::_contact_scale.  kn and kt are used scaled by scale*contact_scale
+ * (ForceGeneralSDFContact.cpp:155-156). */
+typedef struct {
+    double kn, kt, mu, damping, scale, contact_scale;
+} sdfc_params;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device`.  Replaces nothing in the
+ * reference (it has no device state); owns all device buffers. */
+int sdfc_create(sdfc_context** ctx, int device);
+void sdfc_destroy(sdfc_context* ctx);
+/* Message of the last failing call on this context (never NULL). */
+const char* sdfc_last_error(const sdfc_context* ctx);
+
+/* Uploads an SDF body's grid (BodySDFObj::_SDF and its box/spacing/threshold,
+ * BodySDFObj.h:13-16; filled by BodySDFObj::precompute_SDF / load_SDF,
+ * BodySDFObj.cpp:38-116).  `values` holds ni*nj*nk doubles, i fastest.
+ * storage = SDFC_STORAGE_F32 keeps FP32 values (exact for grids made by sdfgen,
+ * which computes in FP32); SDFC_STORAGE_F64 keeps FP64 values.  Rejects
+ * grids on which the reference's cell index could leave the array
+ * ((max_box - min_box)/dx >= n on some axis), non-finite values, n < 2.
+ * Writes a handle to *grid. */
+int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
+                     const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid);
+
+/* Uploads a contact body's contact points (Body::_contact_points, body frame;
+ * BodyMeshObj::precompute_contact_points, simulation/redmax/Body/BodyMeshObj.cpp:184-238).
+ * `xyz` holds n points as x,y,z doubles.  SDFC_STORAGE_F32 stores them as
+ * FP32 (exact when they are FP32-representable).  Writes a handle to *points. */
+int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage, int* points);
+
+/* ---------------------------------------------------------------- one pair */
+
+/* One Force call of one ForceGeneralSDFContact(contact body A, SDF body B):
+ * detection (CollisionDetection.cpp:124-147) then the contact sums
+ * (ForceGeneralSDFContact.cpp:147-219 for want_deriv == 0, :221-447 with
+ * want_deriv != 0).  Host arrays: E_A, E_B [16]; phi_A, phi_B [6]; fm [12];
+ * Km, Dm [144] (only written when want_deriv; may be NULL otherwise).
+ * *n_active receives the size of the active contact set. */
+int sdfc_evaluate(sdfc_context* ctx, int points, int grid, const double* E_A, const double* phi_A, const double* E_B,
+                  const double* phi_B, const sdfc_params* params, int want_deriv, double* fm, double* Km, double* Dm,
+                  int* n_active);
+
+/* Active contact ids (indices into the contact body's points, ascending, as
+ * collision_detection_general_SDF lists them) of the last sdfc_evaluate on
+ * this context.  Writes min(cap, n) ids and *n = n. */
+int sdfc_active_ids(sdfc_context* ctx, int* ids, int cap, int* n);
+
+/* ---------------------------------------------------------------- batches */
+
+/* A batch of n pair instances with fixed topology: instance k pits point set
+ * points[k] against grid grids[k].  This is the planner's inner loop
+ * (examples/run_joint_plan.py:511-589: many candidate pull directions and
+ * assemblies) folded into one launch per evaluation; the reference runs these
+ * as separate processes (utils/parallel.py:10). */
+int sdfc_batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** batch);
+void sdfc_batch_destroy(sdfc_batch* batch);
+
+/* Evaluates every instance.  Arrays are per instance, row-major, HOST memory:
+ * E_A, E_B [n*16]; phi_A, phi_B [n*6]; params [n]; fm [n*12]; Km, Dm [n*144]
+ * (want_deriv only); n_active [n]; status [n] (bit 0: a non-finite output).
+ * Host<->device copies are part of the call. */
+int sdfc_batch_evaluate(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
+                        const double* phi_B, const sdfc_params* params, int want_deriv, double* fm, double* Km,
+                        double* Dm, int* n_active, int* status);
+
+/* Same with DEVICE arrays, enqueued on `stream` (a cudaStream_t, NULL for the
+ * context's stream) without synchronising; capturable in a CUDA graph.
+ * params is an n x 6 device array (kn, kt, mu, damping, scale, contact_scale). */
+int sdfc_batch_evaluate_device(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
+                               const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
+                               double* Dm, int* n_active, int* status, void* stream);
+
+/* Number of points the last evaluations of this batch re-checked in FP64
+ * because their FP32 distance fell inside the guard band (diagnostic; the
+ * counter accumulates until reset with reset != 0). */
+int sdfc_batch_recheck_count(sdfc_batch* batch, unsigned long long* count, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDFC_H */

@@ -1,0 +1,161 @@
+"""GPU parity: libsdfcontact (through its C ABI) against the reference's golden
+vectors and the oracle restatement on the same seeded inputs.
+
+Bars: the active contact set is identical (the reference's ids, ascending);
+fm to 1e-10 and Km, Dm to 1e-8 in the reference's relative-error convention
+(simulation/redmax/Utils.h:362-381).  The reference computes the SDF gradient
+and Hessian by central differences; inside a grid cell these equal the
+interpolant's analytic derivatives up to FP64 round-off of the differences,
+which bounds the Km/Dm agreement."""
+import numpy as np
+import pytest
+
+from _helpers import assert_close, load
+from conftest import submodule
+
+pytestmark = pytest.mark.gpu
+
+FM_REL = 1e-10
+JAC_REL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def sdfc():
+    submodule("build").build()
+    return submodule("sdfc")
+
+
+@pytest.fixture(scope="module")
+def ctx(sdfc):
+    c = sdfc.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def fx():
+    return load("pair_eval.npz")
+
+
+def params_of(sdfc, row):
+    return sdfc.Params(*[float(x) for x in row])
+
+
+@pytest.mark.parametrize("storage", [0, 1])
+def test_golden_single_pair(sdfc, ctx, fx, storage):
+    grid = ctx.upload_grid(fx["grid"], fx["min_box"], fx["max_box"], fx["dx"], float(fx["col_th"]), storage)
+    pts = ctx.upload_points(fx["points"], storage)
+    for k in range(len(fx["fm"])):
+        prm = params_of(sdfc, fx["params"][k])
+        args = (pts, grid, fx["EA"][k], fx["phiA"][k], fx["EB"][k], fx["phiB"][k], prm)
+        fm_v, _, _, n_v = ctx.evaluate(*args, want_deriv=False)
+        ids_v = ctx.active_ids()
+        fm, Km, Dm, n = ctx.evaluate(*args, want_deriv=True)
+        ids = ctx.active_ids()
+        ref_ids = fx["ids"][k][: fx["n_active"][k]]
+        assert n == n_v == len(ref_ids)
+        assert np.array_equal(ids, ref_ids) and np.array_equal(ids_v, ref_ids), f"case {k}"
+        assert_close(f"case {k} fm value", fm_v, fx["fm_v"][k], rel=FM_REL)
+        assert_close(f"case {k} fm", fm, fx["fm"][k], rel=FM_REL)
+        assert_close(f"case {k} Km", Km, fx["Km"][k], rel=JAC_REL)
+        assert_close(f"case {k} Dm", Dm, fx["Dm"][k], rel=JAC_REL)
+
+
+def test_golden_batch_equals_single(sdfc, ctx, fx):
+    grid = ctx.upload_grid(fx["grid"], fx["min_box"], fx["max_box"], fx["dx"], float(fx["col_th"]), 1)
+    pts = ctx.upload_points(fx["points"], 1)
+    n = len(fx["fm"])
+    b = ctx.batch([pts] * n, [grid] * n)
+    prms = [params_of(sdfc, fx["params"][k]) for k in range(n)]
+    fm, Km, Dm, nact, st = b.evaluate(fx["EA"], fx["phiA"], fx["EB"], fx["phiB"], prms, want_deriv=True)
+    assert not st.any()
+    for k in range(n):
+        assert nact[k] == fx["n_active"][k]
+        assert_close(f"batch {k} fm", fm[k], fx["fm"][k], rel=FM_REL)
+        assert_close(f"batch {k} Km", Km[k], fx["Km"][k], rel=JAC_REL)
+        assert_close(f"batch {k} Dm", Dm[k], fx["Dm"][k], rel=JAC_REL)
+    # deterministic: a second evaluation is bit-identical
+    fm2, Km2, Dm2, _, _ = b.evaluate(fx["EA"], fx["phiA"], fx["EB"], fx["phiB"], prms, want_deriv=True)
+    assert np.array_equal(fm, fm2) and np.array_equal(Km, Km2) and np.array_equal(Dm, Dm2)
+    b.close()
+
+
+def test_oracle_larger_uneven_batch(sdfc, ctx, oracle, workloads):
+    """Uneven instances (different point sets and grids) in one batch, against the oracle."""
+    rng = np.random.default_rng(42)
+    g64 = workloads.socket_grid(64, dtype=np.float64)
+    g40 = workloads.socket_grid(40, dtype=np.float32)
+    grids = [(ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, st), g)
+             for g, st in ((g64, 0), (g40, 1))]
+    psets = [workloads.peg_points(n, seed=s) for n, s in ((20000, 1), (3000, 2), (9000, 3))]
+    phs = [ctx.upload_points(p, 1) for p in psets]
+    inst = [(0, 0), (1, 1), (2, 0), (0, 1), (1, 0), (2, 1)]
+    b = ctx.batch([phs[a] for a, _ in inst], [grids[c][0] for _, c in inst])
+    n = len(inst)
+    EA = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.02),
+                                  [0.02 * rng.normal(), 0.02 * rng.normal(), 0.2 * rng.normal()]) for _ in range(n)])
+    EB = np.stack([np.eye(4)] * n)
+    phiA = rng.normal(size=(n, 6)) * 0.3
+    phiB = np.zeros((n, 6))
+    prm = [sdfc.Params(1e5, [1e3, 1e1][k % 2], 0.3, 1e3, 1.0, 1.0) for k in range(n)]
+    fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
+    assert not st.any()
+    for k, (a, c) in enumerate(inst):
+        g = grids[c][1]
+        og = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
+        op = oracle.Params(prm[k].kn, prm[k].kt, prm[k].mu, prm[k].damping, 1.0, 1.0)
+        rf, rK, rD, rids = oracle.pair_eval(og, psets[a], EA[k], phiA[k], EB[k], phiB[k], op, True)
+        assert nact[k] == len(rids) and len(rids) > 0
+        assert_close(f"inst {k} fm", fm[k], rf, rel=FM_REL)
+        assert_close(f"inst {k} Km", Km[k], rK, rel=JAC_REL)
+        assert_close(f"inst {k} Dm", Dm[k], rD, rel=JAC_REL)
+    b.close()
+
+
+def test_edge_cases(sdfc, ctx, oracle, workloads):
+    g = workloads.socket_grid(16, dtype=np.float32)
+    grid = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+    og = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
+    prm = sdfc.Params(1e5, 1e3, 0.3, 1e3)
+    op = oracle.Params(1e5, 1e3, 0.3, 1e3)
+    I, z = np.eye(4), np.zeros(6)
+    # empty point set
+    empty = ctx.upload_points(np.zeros((0, 3)), 1)
+    fm, Km, Dm, n = ctx.evaluate(empty, grid, I, z, I, z, prm)
+    assert n == 0 and not fm.any() and not Km.any() and not Dm.any()
+    # every point outside the grid box: nothing active
+    far = ctx.upload_points(np.full((100, 3), 7.0), 1)
+    fm, Km, Dm, n = ctx.evaluate(far, grid, I, z, I, z, prm)
+    assert n == 0 and not fm.any()
+    # points on grid nodes and cell faces (the reference's stencil straddles cells there)
+    ax = g.min_box[0] + g.dx[0] * np.arange(3, 13)
+    P = np.array([[x, y, zz] for x in ax[::3] for y in ax[::3] for zz in ax]).astype(np.float32).astype(np.float64)
+    P = P[np.abs(workloads.socket_sdf(P)) < 0.3]
+    nodes = ctx.upload_points(P, 1)
+    EA = workloads.pose(p=[0.004, -0.003, 0.002])
+    fm, Km, Dm, n = ctx.evaluate(nodes, grid, EA, z, I, z, prm)
+    rf, rK, rD, rids = oracle.pair_eval(og, P, EA, z, I, z, op, True)
+    assert n == len(rids) and n > 0
+    assert np.array_equal(ctx.active_ids(), rids)
+    assert_close("nodes fm", fm, rf, rel=FM_REL)
+    assert_close("nodes Km", Km, rK, rel=JAC_REL)
+    assert_close("nodes Dm", Dm, rD, rel=JAC_REL)
+    # minimal 2x2x2 grid
+    v = np.array([-0.1, 0.2, 0.1, 0.3, 0.0, 0.4, 0.2, 0.5]).reshape(2, 2, 2)
+    tiny = ctx.upload_grid(v, [0, 0, 0], [1, 1, 1], [1, 1, 1], 0.0, 0)
+    Q = np.random.default_rng(0).uniform(0, 1, (500, 3))
+    qp = ctx.upload_points(Q, 0)
+    fm, Km, Dm, n = ctx.evaluate(qp, tiny, I, z, I, z, prm)
+    rf, rK, rD, rids = oracle.pair_eval(oracle.Grid(v, [0, 0, 0], [1, 1, 1], [1, 1, 1], 0.0), Q, I, z, I, z, op, True)
+    assert n == len(rids)
+    assert_close("tiny fm", fm, rf, rel=FM_REL)
+    assert_close("tiny Km", Km, rK, rel=JAC_REL)
+
+
+def test_invalid_arguments(sdfc, ctx):
+    with pytest.raises(sdfc.SdfcError):
+        ctx.upload_grid(np.zeros((4, 4, 4)), [0, 0, 0], [5, 5, 5], [1, 1, 1], 0.0)  # box past the last node
+    with pytest.raises(sdfc.SdfcError):
+        ctx.upload_grid(np.full((4, 4, 4), np.nan), [0, 0, 0], [3, 3, 3], [1, 1, 1], 0.0)
+    with pytest.raises(sdfc.SdfcError):
+        ctx.batch([12345], [0])
