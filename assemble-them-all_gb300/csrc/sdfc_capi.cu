@@ -34,6 +34,7 @@ struct sdfc_context {
     GridDesc* d_grids = nullptr;
     PointsDesc* d_points = nullptr;
     int grid_cap = 0, points_cap = 0;
+    int deriv_mode = SDFC_DERIV_ANALYTIC;
     sdfc_batch* single = nullptr;     // cached one-instance batch of sdfc_evaluate
     int single_points = -1, single_grid = -1;
     std::vector<sdfc_batch*> batches;  // live batches, destroyed with the context
@@ -43,6 +44,7 @@ struct sdfc_batch {
     sdfc_context* ctx = nullptr;
     int n = 0;
     int total_tiles = 0;
+    int deriv_mode = SDFC_DERIV_ANALYTIC;
     std::vector<InstanceDesc> inst;
     InstanceDesc* d_inst = nullptr;
     int* d_tile_inst = nullptr;
@@ -126,7 +128,7 @@ int run_batch(sdfc_batch* b, const double* EA, const double* phiA, const double*
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->total_tiles, in, ctx->d_grids, ctx->d_points, b->d_ids,
                         b->d_tile_count, b->d_recheck, stream);
     sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, b->d_ids, b->d_tile_count, b->d_partial,
-                       deriv, stream);
+                       deriv, b->deriv_mode == SDFC_DERIV_STENCIL, stream);
     sdfc::launch_finalize(b->d_inst, b->n, b->d_tile_count, b->d_partial, deriv, out, stream);
     CUDA_TRY(ctx, cudaGetLastError());
     return SDFC_OK;
@@ -171,6 +173,23 @@ void sdfc_destroy(sdfc_context* ctx) {
 }
 
 const char* sdfc_last_error(const sdfc_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int sdfc_set_derivative_mode(sdfc_context* ctx, int mode) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (mode != SDFC_DERIV_ANALYTIC && mode != SDFC_DERIV_STENCIL)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "set_derivative_mode: unknown mode");
+    ctx->deriv_mode = mode;
+    if (ctx->single) ctx->single->deriv_mode = mode;
+    return SDFC_OK;
+}
+
+int sdfc_batch_set_derivative_mode(sdfc_batch* b, int mode) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    if (mode != SDFC_DERIV_ANALYTIC && mode != SDFC_DERIV_STENCIL)
+        return fail(b->ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_set_derivative_mode: unknown mode");
+    b->deriv_mode = mode;
+    return SDFC_OK;
+}
 
 int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
                      const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
@@ -305,6 +324,7 @@ static int batch_create_impl(sdfc_context* ctx, int n, const int* points, const 
     auto* b = new sdfc_batch();
     b->ctx = ctx;
     b->n = n;
+    b->deriv_mode = ctx->deriv_mode;
     b->inst.resize(n);
     std::vector<int> tile_inst;
     int tiles = 0;

@@ -111,31 +111,64 @@ __device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, in
     return g.storage == 0 ? g.v64[idx] : (double)__ldg(g.v32 + idx);
 }
 
+// FP64 arithmetic in the reference's operation order without FMA contraction.
+// With these, the grid-frame point and query_SDF reproduce the reference's
+// x86-64 (SSE2, no FMA) results bit for bit: same products, same sums, same
+// IEEE division and rounding.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+// (1 - c) * a + c * b
+__device__ __forceinline__ double lerp_ref(double c, double a, double b) {
+    return add_rn(mul_rn(sub_rn(1.0, c), a), mul_rn(c, b));
+}
+// A v and A^T v, sums left to right
+__device__ __forceinline__ V3 mul_ref(const M3& A, V3 v) {
+    return {add_rn(add_rn(mul_rn(A.m[0], v.x), mul_rn(A.m[1], v.y)), mul_rn(A.m[2], v.z)),
+            add_rn(add_rn(mul_rn(A.m[3], v.x), mul_rn(A.m[4], v.y)), mul_rn(A.m[5], v.z)),
+            add_rn(add_rn(mul_rn(A.m[6], v.x), mul_rn(A.m[7], v.y)), mul_rn(A.m[8], v.z))};
+}
+__device__ __forceinline__ V3 mulT_ref(const M3& A, V3 v) {
+    return {add_rn(add_rn(mul_rn(A.m[0], v.x), mul_rn(A.m[3], v.y)), mul_rn(A.m[6], v.z)),
+            add_rn(add_rn(mul_rn(A.m[1], v.x), mul_rn(A.m[4], v.y)), mul_rn(A.m[7], v.z)),
+            add_rn(add_rn(mul_rn(A.m[2], v.x), mul_rn(A.m[5], v.y)), mul_rn(A.m[8], v.z))};
+}
+// Contact point in world and in the SDF body's frame:
+//   xw = R_A xi + p_A (CollisionDetection.cpp:136), x = R_B^T (xw - p_B) (BodySDFObj.cpp:211)
+__device__ __forceinline__ V3 world_point(const M3& RA, V3 pA, V3 xi) {
+    V3 r = mul_ref(RA, xi);
+    return {add_rn(r.x, pA.x), add_rn(r.y, pA.y), add_rn(r.z, pA.z)};
+}
+__device__ __forceinline__ V3 grid_point(const M3& RB, V3 pB, V3 xw) {
+    return mulT_ref(RB, v3(sub_rn(xw.x, pB.x), sub_rn(xw.y, pB.y), sub_rn(xw.z, pB.z)));
+}
+
 // Trilinear interpolation of the cell containing x (x inside the box), the
-// inside branch of BodySDFObj::query_SDF (BodySDFObj.cpp:130-155).  Cell
-// indices are clamped to the grid; the grid check at upload guarantees the
-// reference's index arithmetic stays in range, so the clamp changes nothing.
+// inside branch of BodySDFObj::query_SDF (BodySDFObj.cpp:130-155), in the
+// reference's operation order.  Cell indices are clamped to the grid; the
+// grid check at upload guarantees the reference's index arithmetic stays in
+// range, so the clamp changes nothing.
 __device__ __forceinline__ double trilinear(const GridDesc& g, V3 x) {
-    double ci = (x.x - g.min_box[0]) / g.dx[0];
-    double cj = (x.y - g.min_box[1]) / g.dx[1];
-    double ck = (x.z - g.min_box[2]) / g.dx[2];
+    double ci = sub_rn(x.x, g.min_box[0]) / g.dx[0];
+    double cj = sub_rn(x.y, g.min_box[1]) / g.dx[1];
+    double ck = sub_rn(x.z, g.min_box[2]) / g.dx[2];
     int i = (int)floor(ci), j = (int)floor(cj), k = (int)floor(ck);
-    ci = ci - i;
-    cj = cj - j;
-    ck = ck - k;
+    ci = sub_rn(ci, (double)i);
+    cj = sub_rn(cj, (double)j);
+    ck = sub_rn(ck, (double)k);
     i = min(max(i, 0), g.ni - 1);
     j = min(max(j, 0), g.nj - 1);
     k = min(max(k, 0), g.nk - 1);
     int ip = (i == g.ni - 1) ? i : i + 1;
     int jp = (j == g.nj - 1) ? j : j + 1;
     int kp = (k == g.nk - 1) ? k : k + 1;
-    double v00 = (1 - ci) * grid_value(g, i, j, k) + ci * grid_value(g, ip, j, k);
-    double v10 = (1 - ci) * grid_value(g, i, jp, k) + ci * grid_value(g, ip, jp, k);
-    double v01 = (1 - ci) * grid_value(g, i, j, kp) + ci * grid_value(g, ip, j, kp);
-    double v11 = (1 - ci) * grid_value(g, i, jp, kp) + ci * grid_value(g, ip, jp, kp);
-    double vk0 = (1 - cj) * v00 + cj * v10;
-    double vk1 = (1 - cj) * v01 + cj * v11;
-    return (1 - ck) * vk0 + ck * vk1;
+    double v00 = lerp_ref(ci, grid_value(g, i, j, k), grid_value(g, ip, j, k));
+    double v10 = lerp_ref(ci, grid_value(g, i, jp, k), grid_value(g, ip, jp, k));
+    double v01 = lerp_ref(ci, grid_value(g, i, j, kp), grid_value(g, ip, j, kp));
+    double v11 = lerp_ref(ci, grid_value(g, i, jp, kp), grid_value(g, ip, jp, kp));
+    double vk0 = lerp_ref(cj, v00, v10);
+    double vk1 = lerp_ref(cj, v01, v11);
+    return lerp_ref(ck, vk0, vk1);
 }
 
 __device__ __forceinline__ bool in_box(const GridDesc& g, V3 x) {
@@ -150,7 +183,9 @@ __device__ inline double query_sdf(const GridDesc& g, V3 x, bool outside_accurat
     // distance to the box plus the value at the closest box point, :159-167
     V3 xb = v3(fmin(fmax(x.x, g.min_box[0]), g.max_box[0]), fmin(fmax(x.y, g.min_box[1]), g.max_box[1]),
                fmin(fmax(x.z, g.min_box[2]), g.max_box[2]));
-    return norm(x - xb) + trilinear(g, xb);
+    V3 dv = v3(sub_rn(x.x, xb.x), sub_rn(x.y, xb.y), sub_rn(x.z, xb.z));
+    double n2 = add_rn(add_rn(mul_rn(dv.x, dv.x), mul_rn(dv.y, dv.y)), mul_rn(dv.z, dv.z));
+    return add_rn(__dsqrt_rn(n2), trilinear(g, xb));
 }
 
 // Value, gradient and Hessian of the SDF at x, following the reference's
@@ -191,7 +226,7 @@ __device__ inline void sdf_stencil(const GridDesc& g, V3 x, SdfJet& J, bool want
     double xs = query_sdf(g, x, true);
     const double ee = e * e;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) J.h[a] = (gp[a] + gm[a] - 2 * xs) / ee;
+    for (int a = 0; a < 3; ++a) J.h[a] = sub_rn(add_rn(gp[a], gm[a]), mul_rn(2.0, xs)) / ee;
     const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -209,9 +244,12 @@ __device__ inline void sdf_stencil(const GridDesc& g, V3 x, SdfJet& J, bool want
     }
 }
 
-__device__ inline void sdf_jet(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian) {
+// stencil_only = true evaluates the reference's 26-query stencil for every
+// point (bit-identical SDF derivatives); otherwise the analytic cell
+// derivatives are used wherever the stencil stays inside one cell.
+__device__ inline void sdf_jet(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian, bool stencil_only = false) {
     J.v = query_sdf(g, x, false);
-    if (in_box(g, x)) {
+    if (!stencil_only && in_box(g, x)) {
         double cx = (x.x - g.min_box[0]) / g.dx[0];
         double cy = (x.y - g.min_box[1]) / g.dx[1];
         double cz = (x.z - g.min_box[2]) / g.dx[2];
@@ -276,9 +314,10 @@ struct ContactForce {
 // `valid == false` marks a padding lane: the grid is not read and the result is
 // discarded by the caller, but the lane still walks the same code so that warp
 // collectives downstream see every lane.
-__device__ __forceinline__ void jet_or_pad(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian, bool valid) {
+__device__ __forceinline__ void jet_or_pad(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian, bool valid,
+                                           bool stencil_only) {
     if (valid) {
-        sdf_jet(g, x, J, want_hessian);
+        sdf_jet(g, x, J, want_hessian, stencil_only);
     } else {
         J.v = -1.0;
         J.g = v3(1.0, 0.0, 0.0);
@@ -288,13 +327,13 @@ __device__ __forceinline__ void jet_or_pad(const GridDesc& g, V3 x, SdfJet& J, b
 }
 
 __device__ inline ContactForce contact_force(const GridDesc& g, V3 xi1, const BodyState& A, const BodyState& B,
-                                      const ContactParams& cp, bool valid = true) {
-    V3 xw1 = mul(A.P.R, xi1) + A.P.p;
+                                      const ContactParams& cp, bool valid = true, bool stencil_only = false) {
+    V3 xw1 = world_point(A.P.R, A.P.p, xi1);
     V3 u1 = cross(A.w, xi1) + A.v;  // skew(xi1)^T w1 + v1
     V3 xw1d = mul(A.P.R, u1);
-    V3 x = mulT(B.P.R, xw1 - B.P.p);
+    V3 x = grid_point(B.P.R, B.P.p, xw1);
     SdfJet J;
-    jet_or_pad(g, x, J, false, valid);
+    jet_or_pad(g, x, J, false, valid, stencil_only);
     double d = J.v + g.col_th;
     double gn = norm(J.g);
     V3 e = v3(J.g.x / gn, J.g.y / gn, J.g.z / gn);
@@ -339,17 +378,18 @@ __device__ inline ContactForce contact_force(const GridDesc& g, V3 xi1, const Bo
 // Dm columns), sink.column(c, N1, N2, T2) receives the column's factors.
 template <class Sink>
 __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1, const BodyState& A, const BodyState& B,
-                                       const ContactParams& cp, Sink& sink, bool valid = true) {
+                                       const ContactParams& cp, Sink& sink, bool valid = true,
+                                       bool stencil_only = false) {
     const M3& R1 = A.P.R;
     const M3& R2 = B.P.R;
     // kinematics of the contact point, :238-252
-    V3 xw1 = mul(R1, xi1) + A.P.p;
+    V3 xw1 = world_point(R1, A.P.p, xi1);
     V3 u1 = cross(A.w, xi1) + A.v;
     V3 xw1d = mul(R1, u1);
     // collision, :292-310
-    V3 x = mulT(R2, xw1 - B.P.p);
+    V3 x = grid_point(R2, B.P.p, xw1);
     SdfJet J;
-    jet_or_pad(g, x, J, true, valid);
+    jet_or_pad(g, x, J, true, valid, stencil_only);
     const double d = J.v + g.col_th;
     const V3 gr = J.g;
     const double gn = norm(gr);

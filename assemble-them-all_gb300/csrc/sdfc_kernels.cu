@@ -84,8 +84,7 @@ __device__ __forceinline__ V3 load_point(const PointsDesc& P, int id) {
 // distance() of the reference on the FP64 path (BodySDFObj.cpp:207-213 after
 // CollisionDetection.cpp:136): xw = R_A xi + p_A, x = R_B^T (xw - p_B).
 __device__ __forceinline__ double exact_distance(const GridDesc& g, const Pose& A, const Pose& B, V3 xi) {
-    V3 xw = mul(A.R, xi) + A.p;
-    V3 x = mulT(B.R, xw - B.p);
+    V3 x = grid_point(B.R, B.p, world_point(A.R, A.p, xi));
     return query_sdf(g, x, false) + g.col_th;
 }
 
@@ -221,7 +220,7 @@ struct WarpSink {
     }
 };
 
-template <bool DERIV>
+template <bool DERIV, bool STENCIL>
 __global__ void __launch_bounds__(kChunk) force_kernel(const InstanceDesc* __restrict__ inst, BatchInputs in,
                                                        const GridDesc* __restrict__ grids,
                                                        const PointsDesc* __restrict__ points,
@@ -285,9 +284,9 @@ __global__ void __launch_bounds__(kChunk) force_kernel(const InstanceDesc* __res
             }
             WarpSink<NV> sink{acc + warp * NV, lane, valid, v3(0, 0, 0), v3(0, 0, 0)};
             if constexpr (DERIV) {
-                contact_force_jacobian(g, xi, A, B, cp, sink, valid);
+                contact_force_jacobian(g, xi, A, B, cp, sink, valid, STENCIL);
             } else {
-                ContactForce F = contact_force(g, xi, A, B, cp, valid);
+                ContactForce F = contact_force(g, xi, A, B, cp, valid, STENCIL);
                 sink.force(F.xi1, F.f1, F.xi2, F.f2);
             }
         }
@@ -343,14 +342,12 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int total
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                   const PointsDesc* d_points, const int* d_ids, const int* d_tile_count, double* d_partial,
-                  bool deriv, cudaStream_t stream) {
+                  bool deriv, bool stencil, cudaStream_t stream) {
     if (n_inst <= 0) return;
     dim3 grid(kSlots, n_inst);
-    if (deriv)
-        force_kernel<true><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, d_ids, d_tile_count, d_partial);
-    else
-        force_kernel<false><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, d_ids, d_tile_count,
-                                                         d_partial);
+    auto* k = deriv ? (stencil ? force_kernel<true, true> : force_kernel<true, false>)
+                    : (stencil ? force_kernel<false, true> : force_kernel<false, false>);
+    k<<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, d_ids, d_tile_count, d_partial);
 }
 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, const int* d_tile_count, const double* d_partial,

@@ -74,7 +74,7 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int total
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                   const PointsDesc* d_points, const int* d_ids, const int* d_tile_count, double* d_partial,
-                  bool deriv, cudaStream_t stream);
+                  bool deriv, bool stencil, cudaStream_t stream);
 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, const int* d_tile_count, const double* d_partial,
                      bool deriv, BatchOutputs out, cudaStream_t stream);

@@ -22,8 +22,11 @@ STORAGE_F32 = 1
 EXPORTS = (
     "sdfc_create", "sdfc_destroy", "sdfc_last_error", "sdfc_upload_grid", "sdfc_upload_points",
     "sdfc_evaluate", "sdfc_active_ids", "sdfc_batch_create", "sdfc_batch_destroy", "sdfc_batch_evaluate",
-    "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count",
+    "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count", "sdfc_set_derivative_mode",
+    "sdfc_batch_set_derivative_mode",
 )
+DERIV_ANALYTIC = 0
+DERIV_STENCIL = 1
 
 
 class SdfcError(RuntimeError):
@@ -69,6 +72,8 @@ def lib():
         L.sdfc_batch_evaluate.argtypes = [v, d, d, d, d, P(Params), i, d, d, d, P(i), P(i)]
         L.sdfc_batch_evaluate_device.argtypes = [v, v, v, v, v, v, i, v, v, v, v, v, v]
         L.sdfc_batch_recheck_count.argtypes = [v, P(ctypes.c_ulonglong), i]
+        L.sdfc_set_derivative_mode.argtypes = [v, i]
+        L.sdfc_batch_set_derivative_mode.argtypes = [v, i]
         _lib = L
     return _lib
 
@@ -154,6 +159,10 @@ class Context:
         self._check(lib().sdfc_active_ids(self._h, _ip(ids), cap, ctypes.byref(n)), "sdfc_active_ids")
         return ids[:min(cap, n.value)].copy()
 
+    def set_derivative_mode(self, mode: int):
+        """DERIV_ANALYTIC or DERIV_STENCIL for sdfc_evaluate and later batches."""
+        self._check(lib().sdfc_set_derivative_mode(self._h, int(mode)), "sdfc_set_derivative_mode")
+
     def batch(self, points, grids) -> "Batch":
         return Batch(self, points, grids)
 
@@ -176,6 +185,9 @@ class Batch:
         if self._h and self.ctx._h:
             lib().sdfc_batch_destroy(self._h)
         self._h = ctypes.c_void_p()
+
+    def set_derivative_mode(self, mode: int):
+        self.ctx._check(lib().sdfc_batch_set_derivative_mode(self._h, int(mode)), "sdfc_batch_set_derivative_mode")
 
     def evaluate(self, E_A, phi_A, E_B, phi_B, params, want_deriv=True):
         """Host arrays in, host arrays out: (fm[n,12], Km[n,12,12], Dm[n,12,12], n_active[n], status[n])."""

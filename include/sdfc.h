@@ -47,6 +47,18 @@ extern "C" {
 #define SDFC_STORAGE_F64 0
 #define SDFC_STORAGE_F32 1
 
+/* How the SDF gradient and Hessian of an active contact are evaluated.
+ * The reference takes central differences of the trilinear interpolant with
+ * step 1e-5 (BodySDFObj::query_dSDF / query_ddSDF, BodySDFObj.cpp:176-205).
+ * SDFC_DERIV_ANALYTIC (default): the interpolant's analytic cell derivatives
+ *   wherever that stencil stays inside one cell (equal to the differences up
+ *   to their FP64 round-off, which the 1/eps^2 of the Hessian amplifies), and
+ *   the reference's stencil elsewhere.
+ * SDFC_DERIV_STENCIL: the reference's 26-query stencil for every contact, in
+ *   the reference's operation order (bit-identical gradient and Hessian). */
+#define SDFC_DERIV_ANALYTIC 0
+#define SDFC_DERIV_STENCIL 1
+
 typedef struct sdfc_context sdfc_context;
 typedef struct sdfc_batch sdfc_batch;
 
@@ -66,6 +78,8 @@ int sdfc_create(sdfc_context** ctx, int device);
 void sdfc_destroy(sdfc_context* ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char* sdfc_last_error(const sdfc_context* ctx);
+/* Derivative mode of sdfc_evaluate and of batches created afterwards. */
+int sdfc_set_derivative_mode(sdfc_context* ctx, int mode);
 
 /* Uploads an SDF body's grid (BodySDFObj::_SDF and its box/spacing/threshold,
  * BodySDFObj.h:13-16; filled by BodySDFObj::precompute_SDF / load_SDF,
@@ -110,6 +124,8 @@ int sdfc_active_ids(sdfc_context* ctx, int* ids, int cap, int* n);
  * as separate processes (utils/parallel.py:10). */
 int sdfc_batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** batch);
 void sdfc_batch_destroy(sdfc_batch* batch);
+/* Derivative mode of this batch (SDFC_DERIV_ANALYTIC or SDFC_DERIV_STENCIL). */
+int sdfc_batch_set_derivative_mode(sdfc_batch* batch, int mode);
 
 /* Evaluates every instance.  Arrays are per instance, row-major, HOST memory:
  * E_A, E_B [n*16]; phi_A, phi_B [n*6]; params [n]; fm [n*12]; Km, Dm [n*144]
