@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Benchmark of the batched point-vs-SDF contact evaluation on GB300.
+
+Workload (the batched BFS direction sweep on the peg-in-hole): 1024 pair
+instances, each a 50k-point peg (cylinder r=0.49, length 2) against a socket
+(cube [-1,1]^3 minus a z bore of r=0.5) stored as a 128^3 FP32 SDF grid; each
+instance is pushed 0.0201 sideways along the lateral part of its Fibonacci-
+sphere pull direction (a penetration of 1e-4 beyond the 0.01 collision
+threshold) and moves along it.  Seeded synthetic inputs stand in for the
+reference's download-only assembly datasets.
+
+A step is one force evaluation with derivatives of the whole batch: detection
+over every point of every instance, then force, dF/dq and dF/dqdot of every
+active contact (ForceGeneralSDFContact::computeForceWithDerivative,
+simulation/redmax/Force/ForceGeneralSDFContact.cpp:69-105), reduced per
+instance in FP64.  The metric is contact-point evaluations per second.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference path (oracle/) on
+the host cores on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "assemble-them-all_gb300"
+W = importlib.import_module(f"{PKG}.workloads")
+
+METRIC = "SDF contact pts/s (batched force+Jacobian evaluation)"
+UNIT = "contact-pts/s"
+COL_TH = 0.01
+PARAMS = (1e5, 1e3, 0.3, 1e3, 1.0, 1.0)  # kn, kt, mu, damping, scale, contact_scale
+L2_BYTES = 129 * 2 ** 20
+
+
+def instance_states(n, rank=0):
+    """Pose / twist of each instance from its pull direction."""
+    dirs = W.fibonacci_directions(n * max(1, rank + 1))[rank * n:(rank + 1) * n] if rank else W.fibonacci_directions(n)
+    EA = np.zeros((n, 4, 4))
+    phiA = np.zeros((n, 6))
+    for k, d in enumerate(dirs):
+        lat = np.array([d[0], d[1], 0.0])
+        ln = np.linalg.norm(lat)
+        lat = lat / ln if ln > 1e-6 else np.array([1.0, 0.0, 0.0])
+        R = W.rotvec_to_matrix(0.002 * np.array([-lat[1], lat[0], 0.0]))
+        EA[k] = W.pose(R, 0.0201 * lat + np.array([0.0, 0.0, 0.25 * d[2]]))
+        phiA[k, 3:] = 0.01 * d
+    EB = np.broadcast_to(np.eye(4), (n, 4, 4)).copy()
+    phiB = np.zeros((n, 6))
+    return EA, phiA, EB, phiB
+
+
+def build_workload(n_inst, n_pts, grid_n, rank=0):
+    grid = W.socket_grid(grid_n, dtype=np.float32)
+    pts = W.peg_points(n_pts, seed=0)
+    return grid, pts, instance_states(n_inst, rank)
+
+
+# --------------------------------------------------------------------------- CPU baseline (oracle)
+_G = {}
+
+
+def _cpu_init(grid_vals, mn, mx, dx, pts):
+    from oracle import oracle as O
+    _G["O"] = O
+    _G["grid"] = O.Grid(grid_vals, mn, mx, dx, COL_TH)
+    _G["pts"] = pts
+    _G["prm"] = O.Params(*PARAMS)
+
+
+def _cpu_eval(args):
+    EA, phiA, EB, phiB = args
+    O = _G["O"]
+    t = time.perf_counter()
+    O.pair_eval(_G["grid"], _G["pts"], EA, phiA, EB, phiB, _G["prm"], True)
+    return time.perf_counter() - t
+
+
+def cpu_pool(grid, pts, procs):
+    from oracle import oracle as O
+    O.build()
+    ctx = mp.get_context("spawn")
+    return ctx.Pool(procs, initializer=_cpu_init, initargs=(grid.values, grid.min_box, grid.max_box, grid.dx, pts))
+
+
+def cpu_time(pool, states, idx):
+    EA, phiA, EB, phiB = states
+    t = time.perf_counter()
+    pool.map(_cpu_eval, [(EA[k], phiA[k], EB[k], phiB[k]) for k in idx], chunksize=1)
+    return time.perf_counter() - t
+
+
+# --------------------------------------------------------------------------- helpers
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("SDFC_BENCH_BACKEND") != "gloo" else "gloo")
+    return world, rank
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.out = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.out), exist_ok=True)
+            self.fh = open(self.out, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={device_index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.out):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of `name` from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "ncu_dram_per_launch.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == name:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+# --------------------------------------------------------------------------- arms
+def run_reference(args, world, rank):
+    """The reference path's CPU cost on the host cores (oracle port), on a bounded sample."""
+    if rank != 0:
+        return
+    grid, pts, states = build_workload(args.instances, args.points, args.grid)
+    procs = os.cpu_count() or 1
+    pool = cpu_pool(grid, pts, procs)
+    sample = max(procs, args.cpu_sample)
+    rng = np.random.default_rng(0)
+    for _ in range(args.warmup):
+        cpu_time(pool, states, rng.choice(args.instances, procs, replace=False))
+    times = []
+    for _ in range(args.steps):
+        times.append(cpu_time(pool, states, rng.choice(args.instances, sample, replace=False)))
+    pool.close()
+    per_step = float(np.mean(times))
+    value = sample * args.points / per_step
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{sample} of {args.instances} instances per step, derivative evaluation"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": "batched BFS direction sweep, peg-in-hole (force+Jacobian evaluation)",
+            "instances": args.instances, "points_per_instance": args.points, "grid": f"{args.grid}^3 fp32",
+            "directions": "fibonacci sphere", "active_set": "peg pressed 1e-4 into the bore wall",
+            "l2": "flushed between timed steps (256 MiB write)", "parallelism": "instances per GPU (replicas)"}
+
+
+def run_gpu(args, world, rank):
+    grid, pts, states = build_workload(args.instances, args.points, args.grid, rank)
+    pool = None
+    if rank == 0 and not args.no_cpu_baseline:
+        pool = cpu_pool(grid, pts, os.cpu_count() or 1)  # spawned before the first CUDA call
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    sdfc = importlib.import_module(f"{PKG}.sdfc")
+    dev = torch.cuda.current_device()
+    ctx = sdfc.Context(dev)
+    g = ctx.upload_grid(grid.values, grid.min_box, grid.max_box, grid.dx, COL_TH, sdfc.STORAGE_F32)
+    p = ctx.upload_points(pts, sdfc.STORAGE_F32)
+    n = args.instances
+    batch = ctx.batch([p] * n, [g] * n)
+    EA, phiA, EB, phiB = states
+    prm_rows = np.tile(np.array(PARAMS), (n, 1))
+    cuda = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()  # noqa: E731
+    dEA, dphiA, dEB, dphiB, dprm = cuda(EA), cuda(phiA), cuda(EB), cuda(phiB), cuda(prm_rows)
+    fm = torch.zeros(n, 12, dtype=torch.float64, device="cuda")
+    Km = torch.zeros(n, 144, dtype=torch.float64, device="cuda")
+    Dm = torch.zeros(n, 144, dtype=torch.float64, device="cuda")
+    nact = torch.zeros(n, dtype=torch.int32, device="cuda")
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        batch.evaluate_device(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
+                              fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
+                              want_deriv=True, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert not st.any().item(), "non-finite contact output"
+    n_active = int(nact.sum().item())
+
+    # timed region: K steps, each bracketed by CUDA events on the launching stream, L2 flushed between
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0 = time.perf_counter()
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dist_barrier(world)
+    step_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    step_ms = dist_max(step_ms, world)
+    pts_per_step = n * args.points
+    value = world * pts_per_step / (step_ms / 1e3)
+
+    # per-phase device times (separate pass with events between the launches)
+    batch.set_timing(True)
+    phases = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.zero_()
+        step()
+        phases.append(batch.last_timing())
+    batch.set_timing(False)
+    det_ms, frc_ms, red_ms = (float(np.mean([x[i] for x in phases])) for i in range(3))
+    rechecked = batch.recheck_count(reset=True)
+
+    # e2e through the C ABI with host buffers (H2D of the instance states, D2H of fm/Km/Dm)
+    params_c = [sdfc.Params(*PARAMS)] * n
+    e2e_t = []
+    for k in range(max(3, args.steps // 2) + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        batch.evaluate(EA, phiA, EB, phiB, params_c, want_deriv=True)
+        if k:
+            e2e_t.append(time.perf_counter() - t)
+    e2e_s = dist_max(float(np.mean(e2e_t)), world)
+    h2d = n * 50 * 8
+    d2h = n * (300 * 8 + 2 * 4)
+
+    if rank != 0:
+        return
+    peaks = load_peaks()
+    hbm_peak = peaks["hbm_gbs"] if peaks else 6800.0
+    # algorithmic bytes: detection reads 12 B per point and 8 FP32 corners (32 B) per query
+    det_bytes = pts_per_step * (12 + 8 * 4)
+    # forces: per active contact its id (4 B), point (12 B) and 8 FP32 corners; per instance-slot 300 FP64 partials
+    frc_bytes = n_active * (4 + 12 + 32) + n * 8 * 300 * 8
+    kernels = {
+        "detect_kernel": {"ms": det_ms, "bytes": det_bytes},
+        "force_kernel": {"ms": frc_ms, "bytes": frc_bytes},
+        "finalize_kernel": {"ms": red_ms, "bytes": n * 8 * 300 * 8 + n * 300 * 8},
+    }
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    ach = kernels[dom]["bytes"] / (kernels[dom]["ms"] / 1e3) / 1e9
+    traffic = profile_traffic(dom)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (fp32 detection prefilter)", "data": "synthetic",
+        "config": workload_config(args),
+        "e2e": {"value": world * pts_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": ach / hbm_peak, "traffic": traffic,
+                     "peak_source": "measured" if peaks else "fallback"},
+        "phases_ms": {"detect": det_ms, "force": frc_ms, "reduce": red_ms},
+        "active_contacts_per_step": n_active, "fp64_rechecked_points_per_step": rechecked / (len(phases) or 1),
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    if pool is not None:
+        procs = os.cpu_count() or 1
+        sample = max(procs, args.cpu_sample)
+        rng = np.random.default_rng(0)
+        cpu_time(pool, states, rng.choice(n, procs, replace=False))
+        ct = cpu_time(pool, states, rng.choice(n, sample, replace=False))
+        pool.close()
+        line["cpu_baseline"] = {"value": sample * args.points / ct, "unit": UNIT, "cores": procs, "kind": "port",
+                                "sample": f"{sample} of {n} instances, derivative evaluation, one process per core"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--instances", type=int, default=1024)
+    ap.add_argument("--points", type=int, default=50000)
+    ap.add_argument("--grid", type=int, default=128)
+    ap.add_argument("--cpu-sample", type=int, default=512, help="instances per CPU-baseline step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank)
+
+
+if __name__ == "__main__":
+    main()
