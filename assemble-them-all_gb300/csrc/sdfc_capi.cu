@@ -35,6 +35,8 @@ struct sdfc_context {
     PointsDesc* d_points = nullptr;
     int grid_cap = 0, points_cap = 0;
     int deriv_mode = SDFC_DERIV_ANALYTIC;
+    int precision = SDFC_PRECISION_FP64;
+    std::vector<std::vector<int>> point_order;  // per point set: stored index -> caller's index
     sdfc_batch* single = nullptr;     // cached one-instance batch of sdfc_evaluate
     int single_points = -1, single_grid = -1;
     std::vector<sdfc_batch*> batches;  // live batches, destroyed with the context
@@ -45,13 +47,18 @@ struct sdfc_batch {
     int n = 0;
     int total_tiles = 0;
     int deriv_mode = SDFC_DERIV_ANALYTIC;
+    int precision = SDFC_PRECISION_FP64;
     std::vector<InstanceDesc> inst;
     InstanceDesc* d_inst = nullptr;
     int* d_tile_inst = nullptr;
     int* d_ids = nullptr;
     int* d_tile_count = nullptr;
+    int* d_tile_queue = nullptr;
+    sdfc::Prefilter* d_prefilter = nullptr;
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
+    int* d_squeue = nullptr;
+    int* d_squeue_count = nullptr;
     // staging of the host-array entry points
     double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
     double* d_out = nullptr;  // n x 300: fm | Km | Dm
@@ -59,6 +66,8 @@ struct sdfc_batch {
     double* h_in = nullptr;   // pinned
     double* h_out = nullptr;  // pinned
     int* h_int = nullptr;     // pinned
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -108,7 +117,11 @@ void free_batch(sdfc_batch* b) {
     cudaFree(b->d_tile_inst);
     cudaFree(b->d_ids);
     cudaFree(b->d_tile_count);
+    cudaFree(b->d_tile_queue);
+    cudaFree(b->d_prefilter);
     cudaFree(b->d_partial);
+    cudaFree(b->d_squeue);
+    cudaFree(b->d_squeue_count);
     cudaFree(b->d_recheck);
     cudaFree(b->d_in);
     cudaFree(b->d_out);
@@ -116,6 +129,8 @@ void free_batch(sdfc_batch* b) {
     cudaFreeHost(b->h_in);
     cudaFreeHost(b->h_out);
     cudaFreeHost(b->h_int);
+    for (cudaEvent_t e : b->ev)
+        if (e) cudaEventDestroy(e);
     delete b;
 }
 
@@ -125,11 +140,17 @@ int run_batch(sdfc_batch* b, const double* EA, const double* phiA, const double*
     sdfc_context* ctx = b->ctx;
     sdfc::BatchInputs in{EA, phiA, EB, phiB, prm};
     sdfc::BatchOutputs out{fm, Km, Dm, n_active, status};
-    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->total_tiles, in, ctx->d_grids, ctx->d_points, b->d_ids,
-                        b->d_tile_count, b->d_recheck, stream);
-    sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, b->d_ids, b->d_tile_count, b->d_partial,
-                       deriv, b->deriv_mode == SDFC_DERIV_STENCIL, stream);
-    sdfc::launch_finalize(b->d_inst, b->n, b->d_tile_count, b->d_partial, deriv, out, stream);
+    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids,     b->d_tile_count,  b->d_tile_queue,
+                          b->d_partial,   b->d_recheck, b->d_squeue,      b->d_squeue_count};
+    if (b->timing) cudaEventRecord(b->ev[0], stream);
+    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream);
+    if (b->timing) cudaEventRecord(b->ev[1], stream);
+    sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, deriv,
+                       b->deriv_mode == SDFC_DERIV_STENCIL,
+                       b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64, stream);
+    if (b->timing) cudaEventRecord(b->ev[2], stream);
+    sdfc::launch_finalize(b->d_inst, b->n, sc, deriv, out, stream);
+    if (b->timing) cudaEventRecord(b->ev[3], stream);
     CUDA_TRY(ctx, cudaGetLastError());
     return SDFC_OK;
 }
@@ -180,6 +201,23 @@ int sdfc_set_derivative_mode(sdfc_context* ctx, int mode) {
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "set_derivative_mode: unknown mode");
     ctx->deriv_mode = mode;
     if (ctx->single) ctx->single->deriv_mode = mode;
+    return SDFC_OK;
+}
+
+int sdfc_set_precision(sdfc_context* ctx, int precision) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "set_precision: unknown precision");
+    ctx->precision = precision;
+    if (ctx->single) ctx->single->precision = precision;
+    return SDFC_OK;
+}
+
+int sdfc_batch_set_precision(sdfc_batch* b, int precision) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
+        return fail(b->ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_set_precision: unknown precision");
+    b->precision = precision;
     return SDFC_OK;
 }
 
@@ -245,7 +283,10 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
         g.min_box[a] = min_box[a];
         g.max_box[a] = max_box[a];
         g.dx[a] = dxyz[a];
+        g.inv_dx[a] = 1.0 / dxyz[a];
+        g.org[a] = min_box[a] * g.inv_dx[a];
         g.fmin[a] = (float)min_box[a];
+        g.fdx[a] = (float)dxyz[a];
         g.fmax[a] = (float)max_box[a];
         g.finv_dx[a] = (float)(1.0 / dxyz[a]);
     }
@@ -257,11 +298,19 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     ctx->allocations.push_back(p32);
     CUDA_TRY(ctx, cudaMemcpy(p32, v32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
     g.v32 = (const float*)p32;
-    if (storage == SDFC_STORAGE_F64) {
+    {
+        // FP64 values of the grid as stored: the caller's doubles, or the FP32 values widened
+        std::vector<double> w64;
+        const double* src = values;
+        if (storage == SDFC_STORAGE_F32) {
+            w64.resize(n);
+            for (size_t i = 0; i < n; ++i) w64[i] = (double)v32[i];
+            src = w64.data();
+        }
         void* p64 = nullptr;
         if ((rc = dev_alloc(ctx, &p64, n * sizeof(double)))) return rc;
         ctx->allocations.push_back(p64);
-        CUDA_TRY(ctx, cudaMemcpy(p64, values, n * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(ctx, cudaMemcpy(p64, src, n * sizeof(double), cudaMemcpyHostToDevice));
         g.v64 = (const double*)p64;
     }
     ctx->grids.push_back(g);
@@ -273,6 +322,42 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     return SDFC_OK;
 }
 
+// Stored order of a point set: Morton (Z-order) of the points quantised to
+// 2^10 cells per axis of their bounding box, ties kept in input order.  Points
+// adjacent in this order are adjacent in space, so a warp's 32 points read a
+// handful of grid cells and the gathers coalesce.
+static std::vector<int> morton_order(const double* xyz, int n) {
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    if (n < 2) return order;
+    double lo[3] = {xyz[0], xyz[1], xyz[2]}, hi[3] = {xyz[0], xyz[1], xyz[2]};
+    for (int i = 1; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], xyz[3 * (size_t)i + a]);
+            hi[a] = std::max(hi[a], xyz[3 * (size_t)i + a]);
+        }
+    auto spread = [](uint32_t v) {  // 10 bits -> every third bit
+        v &= 0x3ffu;
+        v = (v | (v << 16)) & 0x030000ffu;
+        v = (v | (v << 8)) & 0x0300f00fu;
+        v = (v | (v << 4)) & 0x030c30c3u;
+        v = (v | (v << 2)) & 0x09249249u;
+        return v;
+    };
+    std::vector<uint32_t> code(n);
+    for (int i = 0; i < n; ++i) {
+        uint32_t q[3];
+        for (int a = 0; a < 3; ++a) {
+            double ext = hi[a] - lo[a];
+            double t = ext > 0 ? (xyz[3 * (size_t)i + a] - lo[a]) / ext : 0.0;
+            q[a] = (uint32_t)std::min(1023.0, std::max(0.0, std::floor(t * 1024.0)));
+        }
+        code[i] = spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+    return order;
+}
+
 int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage, int* points) {
     if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
     if ((!xyz && n > 0) || n < 0 || !points) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_points: bad argument");
@@ -281,15 +366,17 @@ int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage,
     if (!all_finite(xyz, 3 * (size_t)n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_points: non-finite point");
     int rc = use_device(ctx);
     if (rc) return rc;
+    std::vector<int> order = morton_order(xyz, n);
     std::vector<float> s32(3 * (size_t)n);
     std::vector<double> s64(3 * (size_t)n);
     double r = 0.0;
-    for (int i = 0; i < n; ++i) {
+    for (int k = 0; k < n; ++k) {
+        const double* q = xyz + 3 * (size_t)order[k];
         for (int a = 0; a < 3; ++a) {
-            s64[(size_t)a * n + i] = xyz[3 * (size_t)i + a];
-            s32[(size_t)a * n + i] = (float)xyz[3 * (size_t)i + a];
+            s64[(size_t)a * n + k] = q[a];
+            s32[(size_t)a * n + k] = (float)q[a];
         }
-        r = std::max(r, std::sqrt(xyz[3 * i] * xyz[3 * i] + xyz[3 * i + 1] * xyz[3 * i + 1] + xyz[3 * i + 2] * xyz[3 * i + 2]));
+        r = std::max(r, std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]));
     }
     PointsDesc P{};
     P.n = n;
@@ -300,7 +387,14 @@ int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage,
     ctx->allocations.push_back(p32);
     CUDA_TRY(ctx, cudaMemcpy(p32, s32.data(), s32.size() * sizeof(float), cudaMemcpyHostToDevice));
     P.x32 = (const float*)p32;
-    if (storage == SDFC_STORAGE_F64) {
+    void* pord = nullptr;
+    if ((rc = dev_alloc(ctx, &pord, (size_t)n * sizeof(int)))) return rc;
+    ctx->allocations.push_back(pord);
+    CUDA_TRY(ctx, cudaMemcpy(pord, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice));
+    P.orig = (const int*)pord;
+    if (storage == SDFC_STORAGE_F32)  // the points as stored: FP32, widened
+        for (size_t k = 0; k < s64.size(); ++k) s64[k] = (double)s32[k];
+    {
         void* p64 = nullptr;
         if ((rc = dev_alloc(ctx, &p64, s64.size() * sizeof(double)))) return rc;
         ctx->allocations.push_back(p64);
@@ -308,8 +402,10 @@ int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage,
         P.x64 = (const double*)p64;
     }
     ctx->points.push_back(P);
+    ctx->point_order.push_back(std::move(order));
     if ((rc = sync_table(ctx, ctx->points, &ctx->d_points, &ctx->points_cap))) {
         ctx->points.pop_back();
+        ctx->point_order.pop_back();
         return rc;
     }
     *points = (int)ctx->points.size() - 1;
@@ -325,6 +421,7 @@ static int batch_create_impl(sdfc_context* ctx, int n, const int* points, const 
     b->ctx = ctx;
     b->n = n;
     b->deriv_mode = ctx->deriv_mode;
+    b->precision = ctx->precision;
     b->inst.resize(n);
     std::vector<int> tile_inst;
     int tiles = 0;
@@ -349,6 +446,10 @@ static int batch_create_impl(sdfc_context* ctx, int n, const int* points, const 
         (rc = alloc((void**)&b->d_tile_inst, sizeof(int) * std::max(tiles, 1))) ||
         (rc = alloc((void**)&b->d_ids, sizeof(int) * (size_t)std::max(tiles, 1) * sdfc::kTile)) ||
         (rc = alloc((void**)&b->d_tile_count, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_tile_queue, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
+        (rc = alloc((void**)&b->d_squeue, sizeof(int) * sdfc::squeue_capacity(n, tiles))) ||
+        (rc = alloc((void**)&b->d_squeue_count, sizeof(int) * (size_t)n * sdfc::kSlots)) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
@@ -368,6 +469,8 @@ static int batch_create_impl(sdfc_context* ctx, int n, const int* points, const 
         e = cudaMemcpy(b->d_tile_inst, tile_inst.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_recheck, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(b->d_tile_count, 0, sizeof(int) * std::max(tiles, 1));
+    if (e == cudaSuccess) e = cudaMemset(b->d_tile_queue, 0, sizeof(int) * std::max(tiles, 1));
+    if (e == cudaSuccess) e = cudaMemset(b->d_squeue_count, 0, sizeof(int) * (size_t)n * sdfc::kSlots);
     if (e != cudaSuccess) {
         free_batch(b);
         return fail(ctx, SDFC_ERR_CUDA, std::string("batch_create: ") + cudaGetErrorString(e));
@@ -401,7 +504,7 @@ int sdfc_batch_evaluate_device(sdfc_batch* b, const double* E_A, const double* p
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_evaluate_device: null argument");
     int rc = use_device(ctx);
     if (rc) return rc;
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;
     return run_batch(b, E_A, phi_A, E_B, phi_B, params, want_deriv != 0, fm, Km, Dm, n_active, status, s);
 }
 
@@ -447,6 +550,28 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
     }
     if (n_active) std::memcpy(n_active, b->h_int, sizeof(int) * n);
     if (status) std::memcpy(status, b->h_int + n, sizeof(int) * n);
+    return SDFC_OK;
+}
+
+int sdfc_batch_set_timing(sdfc_batch* b, int enable) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    if (enable && !b->ev[0])
+        for (cudaEvent_t& e : b->ev) CUDA_TRY(ctx, cudaEventCreate(&e));
+    b->timing = enable != 0;
+    return SDFC_OK;
+}
+
+int sdfc_batch_last_timing(sdfc_batch* b, float* ms) {
+    if (!b || !ms) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!b->timing) return fail(ctx, SDFC_ERR_NOT_FOUND, "last_timing: timing is not enabled");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    CUDA_TRY(ctx, cudaEventSynchronize(b->ev[3]));
+    for (int k = 0; k < 3; ++k) CUDA_TRY(ctx, cudaEventElapsedTime(ms + k, b->ev[k], b->ev[k + 1]));
     return SDFC_OK;
 }
 
@@ -498,15 +623,20 @@ int sdfc_active_ids(sdfc_context* ctx, int* ids, int cap, int* n) {
     std::vector<int> counts(std::max(tiles, 1));
     if (tiles > 0)
         CUDA_TRY(ctx, cudaMemcpy(counts.data(), b->d_tile_count, sizeof(int) * tiles, cudaMemcpyDeviceToHost));
-    int total = 0;
+    std::vector<int> all;
     for (int t = 0; t < tiles; ++t) {
-        int c = counts[t];
-        int take = std::max(0, std::min(c, cap - total));
-        if (take > 0)
-            CUDA_TRY(ctx, cudaMemcpy(ids + total, b->d_ids + (size_t)t * sdfc::kTile, sizeof(int) * take,
-                                     cudaMemcpyDeviceToHost));
-        total += c;
+        if (counts[t] <= 0) continue;
+        size_t at = all.size();
+        all.resize(at + counts[t]);
+        CUDA_TRY(ctx, cudaMemcpy(all.data() + at, b->d_ids + (size_t)t * sdfc::kTile, sizeof(int) * counts[t],
+                                 cudaMemcpyDeviceToHost));
     }
+    // stored indices -> the caller's indices, ascending as the reference lists them
+    const std::vector<int>& order = ctx->point_order[ctx->single_points];
+    for (int& v : all) v = order[v];
+    std::sort(all.begin(), all.end());
+    const int total = (int)all.size();
+    for (int k = 0; k < total && k < cap; ++k) ids[k] = all[k];
     *n = total;
     return SDFC_OK;
 }

@@ -4,58 +4,114 @@
 //   BodySDFObj::collision              simulation/redmax/Body/BodySDFObj.cpp:239-377
 //   ForceGeneralSDFContact::computeForce[WithDerivative](contacts, ...)
 //                                      simulation/redmax/Force/ForceGeneralSDFContact.cpp:147-447
-// in FP64, but organised for a GPU thread:
+// organised for a GPU thread:
+//   * the grid-frame point and the penetration depth d are FP64, computed in the
+//     reference's operation order without FMA contraction, so d is bit-identical
+//     to the reference's BodySDFObj::distance;
+//   * the rest of the contact algebra is templated on its arithmetic type T:
+//     T = double is the parity path, T = float the throughput path (GB300 runs
+//     FP32 at 64x its FP64 rate); sums over contacts are always FP64;
 //   * the SDF gradient / Hessian are the analytic derivatives of the trilinear
 //     interpolant of the point's cell.  Inside a cell these equal the
 //     reference's central differences (step 1e-5, BodySDFObj.cpp:176-205) up to
 //     FP64 round-off; when any stencil point of those differences leaves the
-//     cell or the box, the exact 26-query stencil is evaluated instead, so the
-//     result follows the reference in every case;
+//     cell or the box, the exact 26-query stencil is evaluated instead (and a
+//     stencil-only mode evaluates it for every contact);
 //   * every 6x6 block of Km/Dm is written as Gamma^T N (Gamma = [skew(xi)^T, I],
 //     simulation/redmax/Utils.h:196): the body-A rows of the contact's Jacobian
-//     columns are [xi1 x N1_j; N1_j] and the body-B rows are
-//     [xi2 x N2_j + T2_j; N2_j], with N1_j, N2_j, T2_j 3-vectors per column j.
-//     The 24 columns (q1, q2, phi1, phi2) are produced one at a time and handed
-//     to a sink, so a thread never holds a 12x12 block.
+//     column j are [xi1 x N1_j; N1_j] and the body-B rows
+//     [xi2 x N2_j + T2_j; N2_j], with N1_j, N2_j, T2_j 3-vectors.  The 24
+//     columns (q1, q2, phi1, phi2) are produced one at a time and handed to a
+//     sink, so a thread never holds a 12x12 block.
 #pragma once
 
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 namespace sdfc {
 
 // ---------------------------------------------------------------- small vectors
-struct V3 {
-    double x, y, z;
+template <typename T>
+struct Vec3 {
+    T x, y, z;
 };
+template <typename T>
+struct Mat3 {  // row-major
+    T m[9];
+};
+using V3 = Vec3<double>;
+using M3 = Mat3<double>;
+
+template <typename T>
+__device__ __forceinline__ Vec3<T> vec3(T a, T b, T c) {
+    return {a, b, c};
+}
 __device__ __forceinline__ V3 v3(double a, double b, double c) { return {a, b, c}; }
-__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }
-__device__ __forceinline__ V3 operator*(double s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+template <typename T>
+__device__ __forceinline__ Vec3<T> operator+(Vec3<T> a, Vec3<T> b) {
+    return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> operator-(Vec3<T> a, Vec3<T> b) {
+    return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> operator-(Vec3<T> a) {
+    return {-a.x, -a.y, -a.z};
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> operator*(T s, Vec3<T> a) {
+    return {s * a.x, s * a.y, s * a.z};
+}
+template <typename T>
+__device__ __forceinline__ T dot(Vec3<T> a, Vec3<T> b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> cross(Vec3<T> a, Vec3<T> b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
-__device__ __forceinline__ double norm(V3 a) { return sqrt(dot(a, a)); }
-__device__ __forceinline__ double comp(V3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
-__device__ __forceinline__ V3 unit(int k) { return {k == 0 ? 1.0 : 0.0, k == 1 ? 1.0 : 0.0, k == 2 ? 1.0 : 0.0}; }
-
-// 3x3 row-major
-struct M3 {
-    double m[9];
-};
-__device__ __forceinline__ V3 mul(const M3& A, V3 v) {
+template <typename T>
+__device__ __forceinline__ T norm(Vec3<T> a) {
+    return sqrt(dot(a, a));
+}
+template <typename T>
+__device__ __forceinline__ T comp(Vec3<T> a, int k) {
+    return k == 0 ? a.x : (k == 1 ? a.y : a.z);
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> unit(int k) {
+    return {k == 0 ? T(1) : T(0), k == 1 ? T(1) : T(0), k == 2 ? T(1) : T(0)};
+}
+template <typename T, typename U>
+__device__ __forceinline__ Vec3<T> cast(Vec3<U> a) {
+    return {(T)a.x, (T)a.y, (T)a.z};
+}
+template <typename T, typename U>
+__device__ __forceinline__ Mat3<T> cast(const Mat3<U>& A) {
+    Mat3<T> B;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) B.m[k] = (T)A.m[k];
+    return B;
+}
+template <typename T>
+__device__ __forceinline__ Vec3<T> mul(const Mat3<T>& A, Vec3<T> v) {
     return {A.m[0] * v.x + A.m[1] * v.y + A.m[2] * v.z, A.m[3] * v.x + A.m[4] * v.y + A.m[5] * v.z,
             A.m[6] * v.x + A.m[7] * v.y + A.m[8] * v.z};
 }
-__device__ __forceinline__ V3 mulT(const M3& A, V3 v) {  // A^T v
+template <typename T>
+__device__ __forceinline__ Vec3<T> mulT(const Mat3<T>& A, Vec3<T> v) {  // A^T v
     return {A.m[0] * v.x + A.m[3] * v.y + A.m[6] * v.z, A.m[1] * v.x + A.m[4] * v.y + A.m[7] * v.z,
             A.m[2] * v.x + A.m[5] * v.y + A.m[8] * v.z};
 }
-__device__ __forceinline__ V3 col(const M3& A, int c) { return {A.m[c], A.m[3 + c], A.m[6 + c]}; }
-__device__ __forceinline__ M3 mul(const M3& A, const M3& B) {
-    M3 C;
+template <typename T>
+__device__ __forceinline__ Vec3<T> col(const Mat3<T>& A, int c) {
+    return {A.m[c], A.m[3 + c], A.m[6 + c]};
+}
+template <typename T>
+__device__ __forceinline__ Mat3<T> mul(const Mat3<T>& A, const Mat3<T>& B) {
+    Mat3<T> C;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -63,7 +119,8 @@ __device__ __forceinline__ M3 mul(const M3& A, const M3& B) {
             C.m[3 * r + c] = A.m[3 * r] * B.m[c] + A.m[3 * r + 1] * B.m[3 + c] + A.m[3 * r + 2] * B.m[6 + c];
     return C;
 }
-__device__ __forceinline__ M3 transpose(const M3& A) {
+template <typename T>
+__device__ __forceinline__ Mat3<T> transpose(const Mat3<T>& A) {
     return {{A.m[0], A.m[3], A.m[6], A.m[1], A.m[4], A.m[7], A.m[2], A.m[5], A.m[8]}};
 }
 
@@ -73,20 +130,25 @@ __device__ __forceinline__ M3 transpose(const M3& A) {
 struct GridDesc {
     int ni, nj, nk;
     int storage;  // 0 = FP64 values, 1 = FP32 values
-    double min_box[3], max_box[3], dx[3];
+    double min_box[3], max_box[3], dx[3], inv_dx[3];
+    double org[3];  // min_box / dx (cell coordinate of the origin), for the fast depth path
     double col_th;
-    const double* v64;   // storage 0
-    const float* v32;    // FP32 copy: always present (prefilter); the values for storage 1
-    float fmin[3], fmax[3], finv_dx[3];  // FP32 prefilter constants
+    const double* v64;   // FP64 values (storage 1: the FP32 values widened), read for active contacts
+    const float* v32;    // FP32 values (storage 0: rounded), read by detection and the FP32 derivatives
+    float fmin[3], fmax[3], finv_dx[3], fdx[3];  // FP32 constants
     float lip;        // bound on |grad| of the interpolant over the grid
     float vmax;       // max |value|
 };
 
+// A contact body's points, stored on the device in a spatially sorted order
+// (Morton order in the body frame) so that a warp's points share grid cells;
+// `orig` maps a stored index back to the caller's point index.
 struct PointsDesc {
     int n;
     int storage;       // 0 = FP64 SoA, 1 = FP32 SoA
-    const float* x32;  // FP32 SoA copy (x[n], y[n], z[n]); exact when storage == 1
-    const double* x64; // FP64 SoA (storage 0 only)
+    const float* x32;  // FP32 SoA (x[n], y[n], z[n]); exact when storage == 1
+    const double* x64; // FP64 SoA (storage 1: the FP32 points widened)
+    const int* orig;   // stored index -> caller's index
     float radius;      // max |xi|
 };
 
@@ -107,8 +169,7 @@ __device__ __forceinline__ Pose load_pose(const double* E) {
 }
 
 __device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, int k) {
-    size_t idx = (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k);
-    return g.storage == 0 ? g.v64[idx] : (double)__ldg(g.v32 + idx);
+    return __ldg(g.v64 + (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k));
 }
 
 // FP64 arithmetic in the reference's operation order without FMA contraction.
@@ -143,33 +204,45 @@ __device__ __forceinline__ V3 grid_point(const M3& RB, V3 pB, V3 xw) {
     return mulT_ref(RB, v3(sub_rn(xw.x, pB.x), sub_rn(xw.y, pB.y), sub_rn(xw.z, pB.z)));
 }
 
-// Trilinear interpolation of the cell containing x (x inside the box), the
-// inside branch of BodySDFObj::query_SDF (BodySDFObj.cpp:130-155), in the
-// reference's operation order.  Cell indices are clamped to the grid; the
-// grid check at upload guarantees the reference's index arithmetic stays in
-// range, so the clamp changes nothing.
-__device__ __forceinline__ double trilinear(const GridDesc& g, V3 x) {
+// Cell of a point inside the box: integer cell and fractional position,
+// computed as the reference does ((x - min) / dx, floor, subtract).
+struct Cell {
+    int i, j, k;
+    double u, v, w;
+};
+__device__ __forceinline__ Cell cell_of(const GridDesc& g, V3 x) {
     double ci = sub_rn(x.x, g.min_box[0]) / g.dx[0];
     double cj = sub_rn(x.y, g.min_box[1]) / g.dx[1];
     double ck = sub_rn(x.z, g.min_box[2]) / g.dx[2];
-    int i = (int)floor(ci), j = (int)floor(cj), k = (int)floor(ck);
-    ci = sub_rn(ci, (double)i);
-    cj = sub_rn(cj, (double)j);
-    ck = sub_rn(ck, (double)k);
-    i = min(max(i, 0), g.ni - 1);
-    j = min(max(j, 0), g.nj - 1);
-    k = min(max(k, 0), g.nk - 1);
+    Cell c;
+    c.i = (int)floor(ci);
+    c.j = (int)floor(cj);
+    c.k = (int)floor(ck);
+    c.u = sub_rn(ci, (double)c.i);
+    c.v = sub_rn(cj, (double)c.j);
+    c.w = sub_rn(ck, (double)c.k);
+    return c;
+}
+
+// Trilinear interpolation at a cell position, the inside branch of
+// BodySDFObj::query_SDF (BodySDFObj.cpp:130-155), in the reference's operation
+// order.  Cell indices are clamped to the grid; the grid check at upload
+// guarantees the reference's index arithmetic stays in range, so the clamp
+// changes nothing.
+__device__ __forceinline__ double trilinear_at(const GridDesc& g, Cell c) {
+    int i = min(max(c.i, 0), g.ni - 1), j = min(max(c.j, 0), g.nj - 1), k = min(max(c.k, 0), g.nk - 1);
     int ip = (i == g.ni - 1) ? i : i + 1;
     int jp = (j == g.nj - 1) ? j : j + 1;
     int kp = (k == g.nk - 1) ? k : k + 1;
-    double v00 = lerp_ref(ci, grid_value(g, i, j, k), grid_value(g, ip, j, k));
-    double v10 = lerp_ref(ci, grid_value(g, i, jp, k), grid_value(g, ip, jp, k));
-    double v01 = lerp_ref(ci, grid_value(g, i, j, kp), grid_value(g, ip, j, kp));
-    double v11 = lerp_ref(ci, grid_value(g, i, jp, kp), grid_value(g, ip, jp, kp));
-    double vk0 = lerp_ref(cj, v00, v10);
-    double vk1 = lerp_ref(cj, v01, v11);
-    return lerp_ref(ck, vk0, vk1);
+    double v00 = lerp_ref(c.u, grid_value(g, i, j, k), grid_value(g, ip, j, k));
+    double v10 = lerp_ref(c.u, grid_value(g, i, jp, k), grid_value(g, ip, jp, k));
+    double v01 = lerp_ref(c.u, grid_value(g, i, j, kp), grid_value(g, ip, j, kp));
+    double v11 = lerp_ref(c.u, grid_value(g, i, jp, kp), grid_value(g, ip, jp, kp));
+    double vk0 = lerp_ref(c.v, v00, v10);
+    double vk1 = lerp_ref(c.v, v01, v11);
+    return lerp_ref(c.w, vk0, vk1);
 }
+__device__ __forceinline__ double trilinear(const GridDesc& g, V3 x) { return trilinear_at(g, cell_of(g, x)); }
 
 __device__ __forceinline__ bool in_box(const GridDesc& g, V3 x) {
     return x.x >= g.min_box[0] && x.x <= g.max_box[0] && x.y >= g.min_box[1] && x.y <= g.max_box[1] &&
@@ -188,27 +261,19 @@ __device__ inline double query_sdf(const GridDesc& g, V3 x, bool outside_accurat
     return add_rn(__dsqrt_rn(n2), trilinear(g, xb));
 }
 
-// Value, gradient and Hessian of the SDF at x, following the reference's
-// query_SDF / query_dSDF / query_ddSDF.  Returns the value query_SDF(x, false).
+// Value, gradient and Hessian of the SDF at x (query_SDF / query_dSDF /
+// query_ddSDF of the reference).  The value is always FP64.
+template <typename T>
 struct SdfJet {
     double v;      // query_SDF(x) (FLT_MAX outside the box)
-    V3 g;          // query_dSDF(x)
-    double h[6];   // query_ddSDF(x): xx, yy, zz, xy, xz, yz
-    bool stencil;  // true when the exact 26-query stencil was used
+    Vec3<T> g;     // query_dSDF(x)
+    T h[6];        // query_ddSDF(x): xx, yy, zz, xy, xz, yz
 };
 
 constexpr double kFdEps = 1e-5;  // BodySDFObj.cpp:178,191
 
-__device__ __forceinline__ bool same_cell(double xa, double mn, double mx, double dx, int cell, int n) {
-    // The FD stencil point xa stays inside the box and in `cell` (and `cell`
-    // is not the clamped top cell).
-    if (!(xa >= mn && xa <= mx)) return false;
-    int c = (int)floor((xa - mn) / dx);
-    return c == cell && cell < n - 1;
-}
-
-__device__ inline void sdf_stencil(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian) {
-    // Exact reference stencil, BodySDFObj.cpp:176-205.
+// The reference's stencil (BodySDFObj.cpp:176-205), bit-identical in FP64.
+__device__ inline void sdf_stencil(const GridDesc& g, V3 x, V3& grad, double* hess, bool want_hessian) {
     const double e = kFdEps, h = kFdEps / 2;
     double gp[3], gm[3];
 #pragma unroll
@@ -220,13 +285,12 @@ __device__ inline void sdf_stencil(const GridDesc& g, V3 x, SdfJet& J, bool want
         gp[a] = query_sdf(g, xp, true);
         gm[a] = query_sdf(g, xm, true);
     }
-    J.g = v3((gp[0] - gm[0]) / (2 * e), (gp[1] - gm[1]) / (2 * e), (gp[2] - gm[2]) / (2 * e));
-    J.stencil = true;
+    grad = v3((gp[0] - gm[0]) / (2 * e), (gp[1] - gm[1]) / (2 * e), (gp[2] - gm[2]) / (2 * e));
     if (!want_hessian) return;
     double xs = query_sdf(g, x, true);
     const double ee = e * e;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) J.h[a] = sub_rn(add_rn(gp[a], gm[a]), mul_rn(2.0, xs)) / ee;
+    for (int a = 0; a < 3; ++a) hess[a] = sub_rn(add_rn(gp[a], gm[a]), mul_rn(2.0, xs)) / ee;
     const int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -240,55 +304,66 @@ __device__ inline void sdf_stencil(const GridDesc& g, V3 x, SdfJet& J, bool want
         mp[a] = c[a] - h; mp[b] = c[b] + h;
         double s = query_sdf(g, v3(pp[0], pp[1], pp[2]), true) + query_sdf(g, v3(mm[0], mm[1], mm[2]), true) -
                    query_sdf(g, v3(pm[0], pm[1], pm[2]), true) - query_sdf(g, v3(mp[0], mp[1], mp[2]), true);
-        J.h[3 + q] = s / ee;
+        hess[3 + q] = s / ee;
     }
+}
+
+// True when the reference's stencil around x stays inside x's cell on every
+// axis (no stencil point in another cell or outside the box, and the cell is
+// not the clamped top cell).  The test keeps a margin of 2 eps from the
+// faces, so a false "inside" cannot happen; a false "outside" only costs the
+// (exact) stencil evaluation.
+__device__ __forceinline__ bool stencil_in_cell(const GridDesc& g, const Cell& c) {
+    const double m = 2.0 * kFdEps;
+    return c.i >= 0 && c.j >= 0 && c.k >= 0 && c.i < g.ni - 1 && c.j < g.nj - 1 && c.k < g.nk - 1 &&
+           c.u * g.dx[0] > m && (1.0 - c.u) * g.dx[0] > m && c.v * g.dx[1] > m && (1.0 - c.v) * g.dx[1] > m &&
+           c.w * g.dx[2] > m && (1.0 - c.w) * g.dx[2] > m;
 }
 
 // stencil_only = true evaluates the reference's 26-query stencil for every
 // point (bit-identical SDF derivatives); otherwise the analytic cell
-// derivatives are used wherever the stencil stays inside one cell.
-__device__ inline void sdf_jet(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian, bool stencil_only = false) {
-    J.v = query_sdf(g, x, false);
-    if (!stencil_only && in_box(g, x)) {
-        double cx = (x.x - g.min_box[0]) / g.dx[0];
-        double cy = (x.y - g.min_box[1]) / g.dx[1];
-        double cz = (x.z - g.min_box[2]) / g.dx[2];
-        int i = (int)floor(cx), j = (int)floor(cy), k = (int)floor(cz);
-        const double e = kFdEps;
-        bool interior = same_cell(x.x + e, g.min_box[0], g.max_box[0], g.dx[0], i, g.ni) &&
-                        same_cell(x.x - e, g.min_box[0], g.max_box[0], g.dx[0], i, g.ni) &&
-                        same_cell(x.y + e, g.min_box[1], g.max_box[1], g.dx[1], j, g.nj) &&
-                        same_cell(x.y - e, g.min_box[1], g.max_box[1], g.dx[1], j, g.nj) &&
-                        same_cell(x.z + e, g.min_box[2], g.max_box[2], g.dx[2], k, g.nk) &&
-                        same_cell(x.z - e, g.min_box[2], g.max_box[2], g.dx[2], k, g.nk);
-        if (interior) {
-            // analytic derivatives of the cell's trilinear interpolant
-            double u = cx - i, v = cy - j, w = cz - k;
-            double c000 = grid_value(g, i, j, k), c100 = grid_value(g, i + 1, j, k);
-            double c010 = grid_value(g, i, j + 1, k), c110 = grid_value(g, i + 1, j + 1, k);
-            double c001 = grid_value(g, i, j, k + 1), c101 = grid_value(g, i + 1, j, k + 1);
-            double c011 = grid_value(g, i, j + 1, k + 1), c111 = grid_value(g, i + 1, j + 1, k + 1);
-            double a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;  // d/du
-            double b0 = (1 - u) * c000 + u * c100, b1 = (1 - u) * c010 + u * c110;              // along v
-            double b2 = (1 - u) * c001 + u * c101, b3 = (1 - u) * c011 + u * c111;
-            double gu = (1 - v) * ((1 - w) * a00 + w * a01) + v * ((1 - w) * a10 + w * a11);
-            double gv = (1 - w) * (b1 - b0) + w * (b3 - b2);
-            double gw = ((1 - v) * b2 + v * b3) - ((1 - v) * b0 + v * b1);
-            J.g = v3(gu / g.dx[0], gv / g.dx[1], gw / g.dx[2]);
+// derivatives (in T) are used wherever the stencil stays inside one cell.
+template <typename T>
+__device__ inline void sdf_jet(const GridDesc& g, V3 x, SdfJet<T>& J, bool want_hessian, bool stencil_only) {
+    if (in_box(g, x)) {
+        Cell c = cell_of(g, x);
+        J.v = trilinear_at(g, c);
+        if (!stencil_only && stencil_in_cell(g, c)) {
+            const T u = (T)c.u, v = (T)c.v, w = (T)c.w;
+            const int i = c.i, j = c.j, k = c.k;
+            T c000 = (T)grid_value(g, i, j, k), c100 = (T)grid_value(g, i + 1, j, k);
+            T c010 = (T)grid_value(g, i, j + 1, k), c110 = (T)grid_value(g, i + 1, j + 1, k);
+            T c001 = (T)grid_value(g, i, j, k + 1), c101 = (T)grid_value(g, i + 1, j, k + 1);
+            T c011 = (T)grid_value(g, i, j + 1, k + 1), c111 = (T)grid_value(g, i + 1, j + 1, k + 1);
+            T a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;  // d/du
+            T b0 = (1 - u) * c000 + u * c100, b1 = (1 - u) * c010 + u * c110;              // along v
+            T b2 = (1 - u) * c001 + u * c101, b3 = (1 - u) * c011 + u * c111;
+            T gu = (1 - v) * ((1 - w) * a00 + w * a01) + v * ((1 - w) * a10 + w * a11);
+            T gv = (1 - w) * (b1 - b0) + w * (b3 - b2);
+            T gw = ((1 - v) * b2 + v * b3) - ((1 - v) * b0 + v * b1);
+            const T ix = (T)g.inv_dx[0], iy = (T)g.inv_dx[1], iz = (T)g.inv_dx[2];
+            J.g = vec3<T>(gu * ix, gv * iy, gw * iz);
             if (want_hessian) {
-                J.h[0] = J.h[1] = J.h[2] = 0.0;
-                J.h[3] = ((1 - w) * (a10 - a00) + w * (a11 - a01)) / (g.dx[0] * g.dx[1]);
-                J.h[4] = ((1 - v) * (a01 - a00) + v * (a11 - a10)) / (g.dx[0] * g.dx[2]);
-                J.h[5] = ((b3 - b2) - (b1 - b0)) / (g.dx[1] * g.dx[2]);
+                J.h[0] = J.h[1] = J.h[2] = T(0);
+                J.h[3] = ((1 - w) * (a10 - a00) + w * (a11 - a01)) * (ix * iy);
+                J.h[4] = ((1 - v) * (a01 - a00) + v * (a11 - a10)) * (ix * iz);
+                J.h[5] = ((b3 - b2) - (b1 - b0)) * (iy * iz);
             }
-            J.stencil = false;
             return;
         }
+    } else {
+        J.v = (double)FLT_MAX;
     }
-    sdf_stencil(g, x, J, want_hessian);
+    V3 gr;
+    double hs[6];
+    sdf_stencil(g, x, gr, hs, want_hessian);
+    J.g = cast<T>(gr);
+    if (want_hessian)
+        for (int k = 0; k < 6; ++k) J.h[k] = (T)hs[k];
 }
 
-__device__ __forceinline__ V3 hess_mul(const double* h, V3 v) {
+template <typename T>
+__device__ __forceinline__ Vec3<T> hess_mul(const T* h, Vec3<T> v) {
     return {h[0] * v.x + h[3] * v.y + h[4] * v.z, h[3] * v.x + h[1] * v.y + h[5] * v.z,
             h[4] * v.x + h[5] * v.y + h[2] * v.z};
 }
@@ -305,63 +380,220 @@ struct BodyState {
     V3 w, v;  // phi = (w, v), body frame
 };
 
-// Value-only force of one active contact: fm = [Gamma1^T f1; Gamma2^T f2]
-// (ForceGeneralSDFContact::computeForce, :147-219, with BodySDFObj::collision value form :239-274).
-struct ContactForce {
-    V3 xi1, xi2, f1, f2;
+// Per-instance state of a pair as a force thread holds it: the FP64 poses and
+// twists (exact path), their casts to the algebra type T, the coefficients,
+// and the composite transform grid frame <- contact body frame (fast path).
+template <typename T>
+struct PairState {
+    BodyState A, B;
+    Mat3<T> R1, R2;
+    Vec3<T> w1, v1, w2, v2;
+    ContactParams cp;
+    M3 RT;  // R_B^T R_A
+    V3 pT;  // R_B^T (p_A - p_B)
 };
 
-// `valid == false` marks a padding lane: the grid is not read and the result is
-// discarded by the caller, but the lane still walks the same code so that warp
-// collectives downstream see every lane.
-__device__ __forceinline__ void jet_or_pad(const GridDesc& g, V3 x, SdfJet& J, bool want_hessian, bool valid,
-                                           bool stencil_only) {
-    if (valid) {
-        sdf_jet(g, x, J, want_hessian, stencil_only);
-    } else {
+template <typename T>
+__device__ __forceinline__ void make_pair_state(const double* EA, const double* phiA, const double* EB,
+                                                const double* phiB, const double* prm, PairState<T>& S) {
+    S.A.P = load_pose(EA);
+    S.B.P = load_pose(EB);
+    S.A.w = v3(phiA[0], phiA[1], phiA[2]);
+    S.A.v = v3(phiA[3], phiA[4], phiA[5]);
+    S.B.w = v3(phiB[0], phiB[1], phiB[2]);
+    S.B.v = v3(phiB[3], phiB[4], phiB[5]);
+    S.R1 = cast<T>(S.A.P.R);
+    S.R2 = cast<T>(S.B.P.R);
+    S.w1 = cast<T>(S.A.w);
+    S.v1 = cast<T>(S.A.v);
+    S.w2 = cast<T>(S.B.w);
+    S.v2 = cast<T>(S.B.v);
+    S.cp.kn = prm[0] * prm[4] * prm[5];
+    S.cp.kt = prm[1] * prm[4] * prm[5];
+    S.cp.mu = prm[2];
+    S.cp.kd = prm[3];
+    S.RT = mul(transpose(S.B.P.R), S.A.P.R);
+    S.pT = mulT(S.B.P.R, S.A.P.p - S.B.P.p);
+}
+
+// Cell of an active contact for the FP32 throughput path: the grid-frame point
+// through the composite FP64 transform and the cell coordinate by one FP64
+// fused multiply-add per axis.  `ok` is false when the reference's derivative
+// stencil (+-1e-5 per axis) could reach another cell or the clamped top cell;
+// such contacts take the exact path.  The integer cell comes from the FP32
+// coordinate: where it disagrees with the FP64 floor the FP64 fraction lies
+// within FP32 round-off of a face, which `ok` rejects.  Active contacts lie
+// inside the grid box (detection guarantees it), so no box test is needed.
+struct FastCell {
+    V3 y;
+    double ud, vd, wd;
+    int i, j, k;
+    bool ok;
+};
+
+template <typename T>
+__device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const M3& RT, V3 pT, V3 xi) {
+    FastCell c;
+    c.y = v3(fma(RT.m[0], xi.x, fma(RT.m[1], xi.y, fma(RT.m[2], xi.z, pT.x))),
+             fma(RT.m[3], xi.x, fma(RT.m[4], xi.y, fma(RT.m[5], xi.z, pT.y))),
+             fma(RT.m[6], xi.x, fma(RT.m[7], xi.y, fma(RT.m[8], xi.z, pT.z))));
+    const double cx = fma(c.y.x, g.inv_dx[0], -g.org[0]);
+    const double cy = fma(c.y.y, g.inv_dx[1], -g.org[1]);
+    const double cz = fma(c.y.z, g.inv_dx[2], -g.org[2]);
+    c.i = (int)floorf((float)cx);
+    c.j = (int)floorf((float)cy);
+    c.k = (int)floorf((float)cz);
+    c.ud = cx - (double)c.i;
+    c.vd = cy - (double)c.j;
+    c.wd = cz - (double)c.k;
+    // the stencil stays in the cell when every face is more than eps away
+    // (a margin of 1.0001 eps absorbs the FP32 evaluation of this test)
+    const float m = (float)(1.0001 * 1e-5);
+    const float u = (float)c.ud, v = (float)c.vd, w = (float)c.wd;
+    c.ok = c.i >= 0 && c.j >= 0 && c.k >= 0 && c.i < g.ni - 1 && c.j < g.nj - 1 && c.k < g.nk - 1 &&
+           u * g.fdx[0] > m && (1.f - u) * g.fdx[0] > m && v * g.fdx[1] > m && (1.f - v) * g.fdx[1] > m &&
+           w * g.fdx[2] > m && (1.f - w) * g.fdx[2] > m;
+    return c;
+}
+
+// Grid-frame point, depth and SDF jet of one contact.
+//   Exact path (T = double, the stencil mode, and contacts whose stencil
+//   leaves the cell): the reference's operation order, bit-identical depth.
+//   Fast path (T = float with a FastCell `fc` whose `ok` is set): the depth by
+//   FP64 trilinear interpolation at the FastCell, the gradient / Hessian in
+//   FP32; the depth then differs from the reference's by FP64 round-off only.
+// `valid == false` marks a padding lane: the grid is not read and the result
+// is discarded by the caller, but the lane still walks the same code so that
+// warp collectives downstream see every lane.
+template <typename T>
+__device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S, V3 xi, const FastCell* fc,
+                                        bool want_hessian, bool valid, bool stencil_only, V3& x, double& d,
+                                        SdfJet<T>& J) {
+    if (!valid) {
+        x = xi;
+        d = -1.0;
         J.v = -1.0;
-        J.g = v3(1.0, 0.0, 0.0);
-        for (int k = 0; k < 6; ++k) J.h[k] = 0.0;
-        J.stencil = false;
+        J.g = vec3<T>(1, 0, 0);
+        for (int k = 0; k < 6; ++k) J.h[k] = T(0);
+        return;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        if (fc && fc->ok && !stencil_only) {
+            const int i = fc->i, j = fc->j, k = fc->k;
+            const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
+            const size_t b = (size_t)i + sj * (size_t)j + sk * (size_t)k;
+            const double ud = fc->ud, vd = fc->vd, wd = fc->wd;
+            const double e000 = __ldg(g.v64 + b), e100 = __ldg(g.v64 + b + 1);
+            const double e010 = __ldg(g.v64 + b + sj), e110 = __ldg(g.v64 + b + sj + 1);
+            const double e001 = __ldg(g.v64 + b + sk), e101 = __ldg(g.v64 + b + sk + 1);
+            const double e011 = __ldg(g.v64 + b + sk + sj), e111 = __ldg(g.v64 + b + sk + sj + 1);
+            const double q0 = fma(ud, e100 - e000, e000), q1 = fma(ud, e110 - e010, e010);
+            const double q2 = fma(ud, e101 - e001, e001), q3 = fma(ud, e111 - e011, e011);
+            const double r0 = fma(vd, q1 - q0, q0), r1 = fma(vd, q3 - q2, q2);
+            J.v = fma(wd, r1 - r0, r0);
+            x = fc->y;
+            d = J.v + g.col_th;
+            // FP32 analytic derivatives of the cell's interpolant
+            const float u = (float)ud, v = (float)vd, w = (float)wd;
+            const float c000 = __ldg(g.v32 + b), c100 = __ldg(g.v32 + b + 1);
+            const float c010 = __ldg(g.v32 + b + sj), c110 = __ldg(g.v32 + b + sj + 1);
+            const float c001 = __ldg(g.v32 + b + sk), c101 = __ldg(g.v32 + b + sk + 1);
+            const float c011 = __ldg(g.v32 + b + sk + sj), c111 = __ldg(g.v32 + b + sk + sj + 1);
+            const float a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;
+            const float b0 = fmaf(u, a00, c000), b1 = fmaf(u, a10, c010);
+            const float b2 = fmaf(u, a01, c001), b3 = fmaf(u, a11, c011);
+            const float gu = (1 - v) * ((1 - w) * a00 + w * a01) + v * ((1 - w) * a10 + w * a11);
+            const float gv = (1 - w) * (b1 - b0) + w * (b3 - b2);
+            const float gw = ((1 - v) * b2 + v * b3) - ((1 - v) * b0 + v * b1);
+            const float ix = g.finv_dx[0], iy = g.finv_dx[1], iz = g.finv_dx[2];
+            J.g = vec3<float>(gu * ix, gv * iy, gw * iz);
+            if (want_hessian) {
+                J.h[0] = J.h[1] = J.h[2] = 0.f;
+                J.h[3] = ((1 - w) * (a10 - a00) + w * (a11 - a01)) * (ix * iy);
+                J.h[4] = ((1 - v) * (a01 - a00) + v * (a11 - a10)) * (ix * iz);
+                J.h[5] = ((b3 - b2) - (b1 - b0)) * (iy * iz);
+            }
+            return;
+        }
+    }
+    x = grid_point(S.B.P.R, S.B.P.p, world_point(S.A.P.R, S.A.P.p, xi));
+    sdf_jet(g, x, J, want_hessian, stencil_only);
+    d = J.v + g.col_th;
+}
+
+// The force-law scalars s1 = -kn d + kd ddot d and sK = kn d - kd ddot d
+// (ForceGeneralSDFContact.cpp:300, 328): in the reference's expression for the
+// FP64 path, from the FP64 depth rounded once for the FP32 path.
+template <typename T>
+__device__ __forceinline__ void force_scalars(const ContactParams& cp, double dd, T ddot, T& s1, T& sK) {
+    if constexpr (std::is_same<T, float>::value) {
+        const float df = (float)dd;
+        const float k = (float)cp.kd * ddot - (float)cp.kn;
+        s1 = df * k;
+        sK = -s1;
+    } else {
+        s1 = -cp.kn * dd + cp.kd * ddot * dd;
+        sK = cp.kn * dd - cp.kd * ddot * dd;
     }
 }
 
-__device__ inline ContactForce contact_force(const GridDesc& g, V3 xi1, const BodyState& A, const BodyState& B,
-                                      const ContactParams& cp, bool valid = true, bool stencil_only = false) {
-    V3 xw1 = world_point(A.P.R, A.P.p, xi1);
-    V3 u1 = cross(A.w, xi1) + A.v;  // skew(xi1)^T w1 + v1
-    V3 xw1d = mul(A.P.R, u1);
-    V3 x = grid_point(B.P.R, B.P.p, xw1);
-    SdfJet J;
-    jet_or_pad(g, x, J, false, valid, stencil_only);
-    double d = J.v + g.col_th;
-    double gn = norm(J.g);
-    V3 e = v3(J.g.x / gn, J.g.y / gn, J.g.z / gn);
-    V3 n = mul(B.P.R, e);
-    V3 xi2 = x - d * e;
-    V3 xdot = cross(x, B.w) + mulT(B.P.R, xw1d) - B.v;
-    double ddot = dot(J.g, xdot);
-    V3 xw2d = mul(B.P.R, cross(B.w, xi2) + B.v);
-    V3 vw = xw1d - xw2d;
-    V3 t = vw - dot(n, vw) * n;
-    double s1 = -cp.kn * d + cp.kd * ddot * d;
-    double sK = cp.kn * d - cp.kd * ddot * d;
-    V3 rho1 = mulT(A.P.R, n), rho2 = e;  // R2^T n = e
-    ContactForce F;
+// Static-friction test mu |fc| >= kt |tdot| - eps (ForceGeneralSDFContact.cpp:202, 365).
+template <typename T>
+__device__ __forceinline__ bool static_friction(const ContactParams& cp, T fc_norm, T tn) {
+    if constexpr (std::is_same<T, float>::value)
+        return (float)cp.mu * fc_norm >= (float)cp.kt * tn - (float)kFrictionEps;
+    else
+        return cp.mu * fc_norm >= cp.kt * tn - kFrictionEps;
+}
+
+// Value-only force of one active contact: fm = [Gamma1^T f1; Gamma2^T f2]
+// (ForceGeneralSDFContact::computeForce, :147-219, with BodySDFObj::collision value form :239-274).
+template <typename T>
+struct ContactForce {
+    Vec3<T> xi1, xi2, f1, f2;
+};
+
+template <typename T>
+__device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
+                                                bool valid, bool stencil_only) {
+    V3 xd;
+    double dd;
+    SdfJet<T> J;
+    contact_geometry(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J);
+    const ContactParams& cp = S.cp;
+    const Mat3<T>& R1 = S.R1;
+    const Mat3<T>& R2 = S.R2;
+    const Vec3<T> xi1 = cast<T>(xi1d);
+    const Vec3<T> x = cast<T>(xd);
+    const Vec3<T> xw1d = mul(R1, cross(S.w1, xi1) + S.v1);  // R1 (skew(xi1)^T w1 + v1)
+    const T gn = norm(J.g);
+    const Vec3<T> e = vec3<T>(J.g.x / gn, J.g.y / gn, J.g.z / gn);
+    const Vec3<T> n = mul(R2, e);
+    const T d = (T)dd;
+    const Vec3<T> xi2 = x - d * e;
+    const Vec3<T> xdot = cross(x, S.w2) + mulT(R2, xw1d) - S.v2;
+    const T ddot = dot(J.g, xdot);
+    const Vec3<T> vw = xw1d - mul(R2, cross(S.w2, xi2) + S.v2);
+    const Vec3<T> t = vw - dot(n, vw) * n;
+    T s1, sK;
+    force_scalars(cp, dd, ddot, s1, sK);
+    const Vec3<T> rho1 = mulT(R1, n), rho2 = e;  // R2^T n = e
+    ContactForce<T> F;
     F.xi1 = xi1;
     F.xi2 = xi2;
     F.f1 = s1 * rho1;
     F.f2 = sK * rho2;
     if (cp.mu > kFrictionEps) {
-        V3 c1 = cross(xi1, rho1);
-        double fc_norm = fabs(s1) * sqrt(dot(c1, c1) + dot(rho1, rho1));
-        double tn = norm(t);
-        V3 tau1 = mulT(A.P.R, t), tau2 = mulT(B.P.R, t);
-        if (cp.mu * fc_norm >= cp.kt * tn - kFrictionEps) {
-            F.f1 = F.f1 - cp.kt * tau1;
-            F.f2 = F.f2 + cp.kt * tau2;
+        const Vec3<T> c1 = cross(xi1, rho1);
+        const T fc_norm = fabs(s1) * sqrt(dot(c1, c1) + dot(rho1, rho1));
+        const T tn = norm(t);
+        const Vec3<T> tau1 = mulT(R1, t), tau2 = mulT(R2, t);
+        const T mu = (T)cp.mu, kt = (T)cp.kt;
+        if (static_friction(cp, fc_norm, tn)) {
+            F.f1 = F.f1 - kt * tau1;
+            F.f2 = F.f2 + kt * tau2;
         } else {
-            double r = cp.mu * fc_norm / tn;
+            const T r = mu * fc_norm / tn;
             F.f1 = F.f1 - r * tau1;
             F.f2 = F.f2 + r * tau2;
         }
@@ -376,73 +608,75 @@ __device__ inline ContactForce contact_force(const GridDesc& g, V3 xi1, const Bo
 // sink.force(xi1, f1, xi2, f2) receives the force; then, for each of the 24
 // columns c (0-5: dq1, 6-11: dq2 -> Km columns; 12-17: dphi1, 18-23: dphi2 ->
 // Dm columns), sink.column(c, N1, N2, T2) receives the column's factors.
-template <class Sink>
-__device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1, const BodyState& A, const BodyState& B,
-                                       const ContactParams& cp, Sink& sink, bool valid = true,
-                                       bool stencil_only = false) {
-    const M3& R1 = A.P.R;
-    const M3& R2 = B.P.R;
-    // kinematics of the contact point, :238-252
-    V3 xw1 = world_point(R1, A.P.p, xi1);
-    V3 u1 = cross(A.w, xi1) + A.v;
-    V3 xw1d = mul(R1, u1);
+template <typename T, class Sink>
+__device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
+                                              Sink& sink, bool valid, bool stencil_only) {
     // collision, :292-310
-    V3 x = grid_point(R2, B.P.p, xw1);
-    SdfJet J;
-    jet_or_pad(g, x, J, true, valid, stencil_only);
-    const double d = J.v + g.col_th;
-    const V3 gr = J.g;
-    const double gn = norm(gr);
-    const V3 e = v3(gr.x / gn, gr.y / gn, gr.z / gn);
-    const V3 n = mul(R2, e);
-    const V3 xi2 = x - d * e;
-    const V3 xdot = cross(x, B.w) + mulT(R2, xw1d) - B.v;
-    const double ddot = dot(gr, xdot);
-    const V3 wxi = cross(B.w, xi2) + B.v;
-    const V3 xw2d = mul(R2, wxi);
-    const V3 vw = xw1d - xw2d;
-    const double nvw = dot(n, vw);
-    const V3 t = vw - nvw * n;
+    V3 xd;
+    double dd;
+    SdfJet<T> J;
+    contact_geometry(g, S, xi1d, fc, true, valid, stencil_only, xd, dd, J);
+    const ContactParams& cp = S.cp;
+    const Mat3<T>& R1 = S.R1;
+    const Mat3<T>& R2 = S.R2;
+    const Vec3<T>& w1 = S.w1;
+    const Vec3<T>& v1 = S.v1;
+    const Vec3<T>& w2 = S.w2;
+    const Vec3<T>& v2 = S.v2;
+    const Vec3<T> xi1 = cast<T>(xi1d);
+    const Vec3<T> x = cast<T>(xd);
+    const T d = (T)dd;
+    // kinematics of the contact point, :238-252
+    const Vec3<T> u1 = cross(w1, xi1) + v1;  // skew(xi1)^T w1 + v1
+    const Vec3<T> xw1d = mul(R1, u1);
+    const Vec3<T> gr = J.g;
+    const T gn = norm(gr);
+    const Vec3<T> e = vec3<T>(gr.x / gn, gr.y / gn, gr.z / gn);
+    const Vec3<T> n = mul(R2, e);
+    const Vec3<T> xi2 = x - d * e;
+    const Vec3<T> xdot = cross(x, w2) + mulT(R2, xw1d) - v2;
+    const T ddot = dot(gr, xdot);
+    const Vec3<T> wxi = cross(w2, xi2) + v2;
+    const Vec3<T> vw = xw1d - mul(R2, wxi);
+    const T nvw = dot(n, vw);
+    const Vec3<T> t = vw - nvw * n;
 
     // derivatives of the collision quantities wrt xw / xw_dot, :316-373
-    // de/dx = (I - e e^T) H / |g|
-    M3 Hm;
+    Mat3<T> Hm;
     Hm.m[0] = J.h[0]; Hm.m[1] = J.h[3]; Hm.m[2] = J.h[4];
     Hm.m[3] = J.h[3]; Hm.m[4] = J.h[1]; Hm.m[5] = J.h[5];
     Hm.m[6] = J.h[4]; Hm.m[7] = J.h[5]; Hm.m[8] = J.h[2];
-    M3 De;
+    Mat3<T> De;  // de/dg = (|g| I - g g^T / |g|) / |g|^2
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            De.m[3 * r + c] = (gn * (r == c ? 1.0 : 0.0) - comp(gr, r) * comp(gr, c) / gn) / (gn * gn);
-    const M3 de_dx = mul(De, Hm);
-    const M3 R2T = transpose(R2);
-    const M3 de_dxw = mul(de_dx, R2T);
-    const M3 dn_dxw = mul(R2, de_dxw);
-    const V3 dd_dxw = mul(R2, gr);  // row vector g^T R2^T
-    // dxi2/dxw = R2^T - e dd_dxw^T - d de_dxw
-    M3 dxi2_dxw;
+            De.m[3 * r + c] = (gn * (r == c ? T(1) : T(0)) - comp(gr, r) * comp(gr, c) / gn) / (gn * gn);
+    const Mat3<T> de_dx = mul(De, Hm);
+    const Mat3<T> R2T = transpose(R2);
+    const Mat3<T> de_dxw = mul(de_dx, R2T);
+    const Mat3<T> dn_dxw = mul(R2, de_dxw);
+    const Vec3<T> dd_dxw = mul(R2, gr);  // row vector g^T R2^T
+    Mat3<T> dxi2_dxw;  // R2^T - e dd_dxw^T - d de_dxw
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             dxi2_dxw.m[3 * r + c] = R2T.m[3 * r + c] - comp(e, r) * comp(dd_dxw, c) - d * de_dxw.m[3 * r + c];
-    const V3 Hxdot = hess_mul(J.h, xdot);
-    // dddot/dxw = (g^T skew(w2)^T + xdot^T H) R2^T ; as a column vector R2 (skew(w2) g + H xdot)
-    const V3 dddot_dxw = mul(R2, cross(B.w, gr) + Hxdot);
-    const V3 dddot_dxwd = dd_dxw;  // g^T R2^T
-    // dxw2dot/dxw = R2 skew(w2) dxi2_dxw
-    M3 Sw;
-    Sw.m[0] = 0; Sw.m[1] = -B.w.z; Sw.m[2] = B.w.y;
-    Sw.m[3] = B.w.z; Sw.m[4] = 0; Sw.m[5] = -B.w.x;
-    Sw.m[6] = -B.w.y; Sw.m[7] = B.w.x; Sw.m[8] = 0;
-    const M3 R2Sw = mul(R2, Sw);
-    const M3 dxw2d_dxw = mul(R2Sw, dxi2_dxw);
+    const Vec3<T> Hxdot = hess_mul(J.h, xdot);
+    // dddot/dxw = (g^T skew(w2)^T + xdot^T H) R2^T, as a column vector R2 (w2 x g + H xdot)
+    const Vec3<T> dddot_dxw = mul(R2, cross(w2, gr) + Hxdot);
+    const Vec3<T> dddot_dxwd = dd_dxw;  // g^T R2^T
+    Mat3<T> Sw;
+    Sw.m[0] = 0; Sw.m[1] = -w2.z; Sw.m[2] = w2.y;
+    Sw.m[3] = w2.z; Sw.m[4] = 0; Sw.m[5] = -w2.x;
+    Sw.m[6] = -w2.y; Sw.m[7] = w2.x; Sw.m[8] = 0;
+    const Mat3<T> R2Sw = mul(R2, Sw);
+    const Mat3<T> dxw2d_dxw = mul(R2Sw, dxi2_dxw);  // dxw2dot/dxw = R2 skew(w2) dxi2_dxw
     // dtdot/dxw = -dxw2d_dxw - nvw dn_dxw - n (vw^T dn_dxw) + n n^T dxw2d_dxw
-    const V3 vdn = mulT(dn_dxw, vw);
-    const V3 ndx = mulT(dxw2d_dxw, n);
-    M3 dt_dxw;
+    const Vec3<T> vdn = mulT(dn_dxw, vw);
+    const Vec3<T> ndx = mulT(dxw2d_dxw, n);
+    Mat3<T> dt_dxw;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -451,25 +685,25 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1, const B
                                   comp(n, r) * comp(ndx, c);
     // dtdot/dxw_dot = I - n n^T (applied as P v = v - n (n.v))
 
-    // force-law scalars, :300-328
-    const double kn = cp.kn, kt = cp.kt, mu = cp.mu, kd = cp.kd;
-    const double s1 = -kn * d + kd * ddot * d;
-    const double sK = kn * d - kd * ddot * d;
-    const V3 rho1 = mulT(R1, n);
-    const V3 rho2 = e;
-    const V3 xr1 = cross(xi1, rho1);
-    V3 f1 = s1 * rho1, f2 = sK * rho2;
+    // force-law scalars, :300-328 (the depth-dependent magnitudes from the FP64 depth)
+    const T kn = (T)cp.kn, kt = (T)cp.kt, mu = (T)cp.mu, kd = (T)cp.kd;
+    T s1, sK;
+    force_scalars(cp, dd, ddot, s1, sK);
+    const Vec3<T> rho1 = mulT(R1, n);
+    const Vec3<T> rho2 = e;  // R2^T n
+    const Vec3<T> xr1 = cross(xi1, rho1);
+    Vec3<T> f1 = s1 * rho1, f2 = sK * rho2;
 
-    const bool friction = mu > kFrictionEps;
-    double fc_norm = 0.0, tn = 0.0, ratio = 0.0;
+    const bool friction = cp.mu > kFrictionEps;
+    T fc_norm = 0, tn = 0, ratio = 0;
     bool stat = true;
-    V3 tau1 = v3(0, 0, 0), tau2 = v3(0, 0, 0);
+    Vec3<T> tau1 = vec3<T>(0, 0, 0), tau2 = vec3<T>(0, 0, 0);
     if (friction) {
         fc_norm = fabs(s1) * sqrt(dot(xr1, xr1) + dot(rho1, rho1));
         tn = norm(t);
         tau1 = mulT(R1, t);
         tau2 = mulT(R2, t);
-        stat = mu * fc_norm >= kt * tn - kFrictionEps;
+        stat = static_friction(cp, fc_norm, tn);
         ratio = fc_norm / tn;
         if (stat) {
             f1 = f1 - kt * tau1;
@@ -481,24 +715,20 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1, const B
     }
     sink.force(xi1, f1, xi2, f2);
 
-    // q2-column ingredients (collision derivatives wrt the SDF body's pose)
-    //   dx_dq2 = [skew(x) | -I]
-    //   dn_dq2[:,j] = R2 de_dx dx_dq2[:,j] (+ R2 (e_j x e), j<3)
-    //   dddot_dq2 (row) = g^T(-Sw Sx + skew(R2^T xw_dot)) + (H xdot)^T Sx | g^T Sw - (H xdot)^T
-    const V3 rxd = mulT(R2, xw1d);
+    const Vec3<T> rxd = mulT(R2, xw1d);
 
 #pragma unroll 1
     for (int c = 0; c < 24; ++c) {
         const int blk = c / 6, j = c % 6;
         const bool kcol = blk < 2;  // Km column (dq) vs Dm column (dphi)
-        double dd_j = 0.0, dddot_j = 0.0;
-        V3 dn_j = v3(0, 0, 0), dt_j = v3(0, 0, 0), dxi2_j = v3(0, 0, 0);
+        T dd_j = 0, dddot_j = 0;
+        Vec3<T> dn_j = vec3<T>(0, 0, 0), dt_j = vec3<T>(0, 0, 0), dxi2_j = vec3<T>(0, 0, 0);
         if (blk == 0 || blk == 2) {
             // through the contact point: dxw1/dq1 = [-R1 skew(xi1) | R1] = dxw1dot/dphi1,
             // dxw1dot/dq1 = [-R1 skew(u1) | 0]
-            V3 a = (j < 3) ? mul(R1, cross(unit(j), xi1)) : col(R1, j - 3);  // -R1 skew(xi1) e_j = R1 (e_j x xi1)
+            Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
             if (blk == 0) {
-                V3 b = (j < 3) ? mul(R1, cross(unit(j), u1)) : v3(0, 0, 0);
+                Vec3<T> b = (j < 3) ? mul(R1, cross(unit<T>(j), u1)) : vec3<T>(0, 0, 0);
                 dd_j = dot(dd_dxw, a);
                 dddot_j = dot(dddot_dxw, a) + dot(dddot_dxwd, b);
                 dn_j = mul(dn_dxw, a);
@@ -509,71 +739,68 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1, const B
                 dt_j = a - dot(n, a) * n;
             }
         } else if (blk == 1) {
-            // dx_dq2 column
-            V3 dxj = (j < 3) ? cross(unit(j), x) : -unit(j - 3);  // skew(x) e_j = x x e_j = -(e_j x x)
-            if (j < 3) dxj = -dxj;
+            // dx/dq2 = [skew(x) | -I]
+            Vec3<T> dxj = (j < 3) ? cross(x, unit<T>(j)) : -unit<T>(j - 3);
             dd_j = dot(gr, dxj);
-            V3 de_j = mul(de_dx, dxj);
+            Vec3<T> de_j = mul(de_dx, dxj);
             dn_j = mul(R2, de_j);
-            if (j < 3) dn_j = dn_j + mul(R2, cross(unit(j), e));
+            if (j < 3) dn_j = dn_j + mul(R2, cross(unit<T>(j), e));
             dxi2_j = dxj - dd_j * e - d * de_j;
             if (j < 3) {
-                // g^T(-Sw Sx + skew(rxd)) e_j + (H xdot)^T Sx e_j
-                V3 sxe = cross(x, unit(j));  // Sx e_j
-                dddot_j = dot(gr, -cross(B.w, sxe) + cross(rxd, unit(j))) + dot(Hxdot, sxe);
+                // g^T(-Sw Sx + skew(R2^T xw_dot)) e_j + (H xdot)^T Sx e_j
+                Vec3<T> sxe = cross(x, unit<T>(j));
+                dddot_j = dot(gr, -cross(w2, sxe) + cross(rxd, unit<T>(j))) + dot(Hxdot, sxe);
             } else {
-                dddot_j = dot(gr, cross(B.w, unit(j - 3))) - comp(Hxdot, j - 3);
+                dddot_j = dot(gr, cross(w2, unit<T>(j - 3))) - comp(Hxdot, j - 3);
             }
             // dxw2dot/dq2 = [-R2 skew(w2 x xi2 + v2) + R2 Sw dxi2_dq2.left | R2 Sw dxi2_dq2.right]
-            V3 dxw2d_j = mul(R2Sw, dxi2_j);
-            if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit(j)));
+            Vec3<T> dxw2d_j = mul(R2Sw, dxi2_j);
+            if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit<T>(j)));
             // dtdot/dq2 = -dxw2d - nvw dn - n (vw.dn - n.dxw2d)
             dt_j = -dxw2d_j - nvw * dn_j - (dot(vw, dn_j) - dot(n, dxw2d_j)) * n;
         } else {  // blk == 3: dphi2
+            Vec3<T> q;
             if (j < 3) {
-                V3 sxe = cross(x, unit(j));
-                dddot_j = dot(gr, sxe);
-                // dxw2dot/dphi2 col = R2 (e_j x xi2); dtdot = -(I - nn^T) that
-                V3 q = mul(R2, cross(unit(j), xi2));
-                dt_j = -(q - dot(n, q) * n);
+                dddot_j = dot(gr, cross(x, unit<T>(j)));
+                q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
             } else {
                 dddot_j = -comp(gr, j - 3);
-                V3 q = col(R2, j - 3);
-                dt_j = -(q - dot(n, q) * n);
+                q = col(R2, j - 3);
             }
+            dt_j = -(q - dot(n, q) * n);
         }
 
         // normal-force columns
-        V3 N1, N2, T2 = v3(0, 0, 0);
+        Vec3<T> N1, N2, T2 = vec3<T>(0, 0, 0);
         if (kcol) {
-            double r = kn * dd_j - kd * dddot_j * d - kd * ddot * dd_j;
+            T r = kn * dd_j - kd * dddot_j * d - kd * ddot * dd_j;
             N1 = -r * rho1 - sK * mulT(R1, dn_j);
             N2 = r * rho2 + sK * mulT(R2, dn_j);
-            if (blk == 0 && j < 3) N1 = N1 - sK * cross(rho1, unit(j));
-            if (blk == 1 && j < 3) N2 = N2 + sK * cross(rho2, unit(j));
+            if (blk == 0 && j < 3) N1 = N1 - sK * cross(rho1, unit<T>(j));
+            if (blk == 1 && j < 3) N2 = N2 + sK * cross(rho2, unit<T>(j));
             T2 = -sK * cross(rho2, dxi2_j);
         } else {
-            double r = kd * dddot_j * d;
+            T r = kd * dddot_j * d;
             N1 = r * rho1;
             N2 = -r * rho2;
         }
         if (friction) {
             // dfc_norm = fc1^T dfc1 / |fc1|, with dfc1 = Gamma1^T N1 and fc1 = s1 Gamma1^T rho1
-            double dfn = s1 * (dot(xr1, cross(xi1, N1)) + dot(rho1, N1)) / fc_norm;
-            double dtn = dot(t, dt_j) / tn;
+            T dfn = s1 * (dot(xr1, cross(xi1, N1)) + dot(rho1, N1)) / fc_norm;
+            T dtn = dot(t, dt_j) / tn;
             if (stat) {
                 N1 = N1 - kt * mulT(R1, dt_j);
                 N2 = N2 + kt * mulT(R2, dt_j);
-                if (blk == 0 && j < 3) N1 = N1 - kt * cross(tau1, unit(j));
-                if (blk == 1 && j < 3) N2 = N2 + kt * cross(tau2, unit(j));
+                if (blk == 0 && j < 3) N1 = N1 - kt * cross(tau1, unit<T>(j));
+                if (blk == 1 && j < 3) N2 = N2 + kt * cross(tau2, unit<T>(j));
                 if (kcol) T2 = T2 - kt * cross(tau2, dxi2_j);
             } else {
-                double cm = mu / tn;
-                double s = dfn - ratio * dtn;
+                T cm = mu / tn;
+                T s = dfn - ratio * dtn;
                 N1 = N1 - cm * (s * tau1 + fc_norm * mulT(R1, dt_j));
                 N2 = N2 + cm * (s * tau2 + fc_norm * mulT(R2, dt_j));
-                if (blk == 0 && j < 3) N1 = N1 - (mu * ratio) * cross(tau1, unit(j));
-                if (blk == 1 && j < 3) N2 = N2 + (mu * ratio) * cross(tau2, unit(j));
+                if (blk == 0 && j < 3) N1 = N1 - (mu * ratio) * cross(tau1, unit<T>(j));
+                if (blk == 1 && j < 3) N2 = N2 + (mu * ratio) * cross(tau2, unit<T>(j));
                 if (kcol) T2 = T2 - (mu * ratio) * cross(tau2, dxi2_j);
             }
         }

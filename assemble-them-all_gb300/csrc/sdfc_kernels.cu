@@ -10,23 +10,14 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kU = 5.9604644775390625e-08;  // 2^-24, unit round-off of FP32
 
-// FP32 prefilter constants of one instance, shared by a detection CTA.
-struct Prefilter {
-    float R[9], p[3];            // point -> grid frame: x = R xi + p
-    float gmin[3], ginv[3];      // grid origin and 1/dx
-    float lo_in[3], hi_in[3];    // certainly inside the box between these
-    float lo_out[3], hi_out[3];  // certainly outside beyond these
-    float col_th;
-    float guard;                 // bound on |d32 - d64|, times a safety factor
-};
-
+// ------------------------------------------------------------------ prefilter
 // Builds the FP32 transform and the error bound of the FP32 distance.
 //   Position: y32 = fl(R) fl(xi) + fl(p) in FP32 differs from the FP64 grid-frame
 //   point by at most eps_pos = u (10 (sqrt3 r + |p|) + 4 (|min| + sqrt3 r + |p|))
 //   (rounding of R, p, xi, the 9 multiply-adds, and the cell-coordinate
 //   arithmetic (y - min) / dx expressed in length).
 //   Value: the FP32 trilinear of FP32-rounded values adds <= 12 u vmax and the
-//   threshold u |col_th|; a distance error is at most lip * eps_pos + those.
+//   threshold 2 u |col_th|; a distance error is at most lip * eps_pos + those.
 //   The guard band is 4x that bound.
 __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pose& A, const Pose& B,
                                Prefilter& f) {
@@ -55,30 +46,42 @@ __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pos
     f.guard = (float)(4.0 * bound) + 1e-30f;
 }
 
+__global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchInputs in,
+                            const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
+                            Prefilter* __restrict__ pref) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const InstanceDesc I = inst[i];
+    Prefilter f;
+    make_prefilter(grids[I.grid], points[I.points], load_pose(in.EA + 16 * (size_t)i), load_pose(in.EB + 16 * (size_t)i),
+                   f);
+    pref[i] = f;
+}
+
 // FP32 trilinear interpolation for a point certainly inside the box.
-__device__ __forceinline__ float trilinear32(const GridDesc& g, const Prefilter& f, float x, float y, float z) {
+__device__ __forceinline__ float trilinear32(const float* __restrict__ v, int ni, int nj, int nk, const Prefilter& f,
+                                             float x, float y, float z) {
     float cx = (x - f.gmin[0]) * f.ginv[0];
     float cy = (y - f.gmin[1]) * f.ginv[1];
     float cz = (z - f.gmin[2]) * f.ginv[2];
-    int i = min(max((int)floorf(cx), 0), g.ni - 2);
-    int j = min(max((int)floorf(cy), 0), g.nj - 2);
-    int k = min(max((int)floorf(cz), 0), g.nk - 2);
-    float u = cx - (float)i, v = cy - (float)j, w = cz - (float)k;
-    const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
-    const float* b = g.v32 + (size_t)i + sj * (size_t)j + sk * (size_t)k;
+    int i = min(max((int)floorf(cx), 0), ni - 2);
+    int j = min(max((int)floorf(cy), 0), nj - 2);
+    int k = min(max((int)floorf(cz), 0), nk - 2);
+    float u = cx - (float)i, w1 = cy - (float)j, w2 = cz - (float)k;
+    const size_t sj = (size_t)ni, sk = (size_t)ni * (size_t)nj;
+    const float* b = v + (size_t)i + sj * (size_t)j + sk * (size_t)k;
     float c000 = __ldg(b), c100 = __ldg(b + 1);
     float c010 = __ldg(b + sj), c110 = __ldg(b + sj + 1);
     float c001 = __ldg(b + sk), c101 = __ldg(b + sk + 1);
     float c011 = __ldg(b + sk + sj), c111 = __ldg(b + sk + sj + 1);
     float a0 = fmaf(u, c100 - c000, c000), a1 = fmaf(u, c110 - c010, c010);
     float a2 = fmaf(u, c101 - c001, c001), a3 = fmaf(u, c111 - c011, c011);
-    float b0 = fmaf(v, a1 - a0, a0), b1 = fmaf(v, a3 - a2, a2);
-    return fmaf(w, b1 - b0, b0);
+    float b0 = fmaf(w1, a1 - a0, a0), b1 = fmaf(w1, a3 - a2, a2);
+    return fmaf(w2, b1 - b0, b0);
 }
 
 __device__ __forceinline__ V3 load_point(const PointsDesc& P, int id) {
-    if (P.storage == 0) return v3(P.x64[id], P.x64[P.n + id], P.x64[2 * (size_t)P.n + id]);
-    return v3((double)__ldg(P.x32 + id), (double)__ldg(P.x32 + P.n + id), (double)__ldg(P.x32 + 2 * (size_t)P.n + id));
+    return v3(__ldg(P.x64 + id), __ldg(P.x64 + P.n + id), __ldg(P.x64 + 2 * (size_t)P.n + id));
 }
 
 // distance() of the reference on the FP64 path (BodySDFObj.cpp:207-213 after
@@ -90,117 +93,367 @@ __device__ __forceinline__ double exact_distance(const GridDesc& g, const Pose& 
 
 // ------------------------------------------------------------------ detection
 __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDesc* __restrict__ inst,
-                                                                const int* __restrict__ tile_inst, BatchInputs in,
+                                                                const int* __restrict__ tile_inst,
+                                                                const Prefilter* __restrict__ pref,
                                                                 const GridDesc* __restrict__ grids,
                                                                 const PointsDesc* __restrict__ points,
                                                                 int* __restrict__ ids, int* __restrict__ tile_count,
-                                                                unsigned long long* __restrict__ recheck) {
-    __shared__ GridDesc g;
-    __shared__ PointsDesc P;
+                                                                int* __restrict__ tile_queue) {
     __shared__ Prefilter f;
-    __shared__ Pose A, B;
-    __shared__ int warp_cnt[kDetectThreads / 32];
-    __shared__ int base;
+    __shared__ const float* gv;
+    __shared__ const float* px;
+    __shared__ int gn[3], pn;
+    __shared__ int warp_act[kDetectThreads / 32], warp_q[kDetectThreads / 32];
+    __shared__ int base_act, base_q;
     const int t = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int i = tile_inst[t];
     const InstanceDesc I = inst[i];
+    if (tid < (int)(sizeof(Prefilter) / sizeof(float)))
+        reinterpret_cast<float*>(&f)[tid] = reinterpret_cast<const float*>(pref + i)[tid];
     if (tid == 0) {
-        g = grids[I.grid];
-        P = points[I.points];
-        A = load_pose(in.EA + 16 * (size_t)i);
-        B = load_pose(in.EB + 16 * (size_t)i);
-        make_prefilter(g, P, A, B, f);
-        base = 0;
+        const GridDesc& g = grids[I.grid];
+        gv = g.v32;
+        gn[0] = g.ni;
+        gn[1] = g.nj;
+        gn[2] = g.nk;
+        px = points[I.points].x32;
+        pn = points[I.points].n;
+        base_act = 0;
+        base_q = 0;
     }
     __syncthreads();
+    const int n = pn;
     const int first = (t - I.tile0) * kTile;
-    const int count = min(kTile, P.n - first);
+    const int count = min(kTile, n - first);
     int* out = ids + (size_t)t * kTile;
-    int n_recheck = 0;
+    const float* __restrict__ xs = px;
     for (int r0 = 0; r0 < count; r0 += kDetectThreads) {
         const int local = r0 + tid;
-        const int pid = first + local;
-        bool active = false;
+        const int sid = first + local;
+        bool active = false, queue = false;
         if (local < count) {
-            float xi, yi, zi;
-            if (P.storage == 0) {
-                xi = (float)P.x64[pid];
-                yi = (float)P.x64[P.n + pid];
-                zi = (float)P.x64[2 * (size_t)P.n + pid];
-            } else {
-                xi = __ldg(P.x32 + pid);
-                yi = __ldg(P.x32 + P.n + pid);
-                zi = __ldg(P.x32 + 2 * (size_t)P.n + pid);
-            }
-            float x = fmaf(f.R[0], xi, fmaf(f.R[1], yi, fmaf(f.R[2], zi, f.p[0])));
-            float y = fmaf(f.R[3], xi, fmaf(f.R[4], yi, fmaf(f.R[5], zi, f.p[1])));
-            float z = fmaf(f.R[6], xi, fmaf(f.R[7], yi, fmaf(f.R[8], zi, f.p[2])));
-            bool maybe_in = x >= f.lo_out[0] && x <= f.hi_out[0] && y >= f.lo_out[1] && y <= f.hi_out[1] &&
-                            z >= f.lo_out[2] && z <= f.hi_out[2];
+            const float xi = __ldg(xs + sid), yi = __ldg(xs + n + sid), zi = __ldg(xs + 2 * (size_t)n + sid);
+            const float x = fmaf(f.R[0], xi, fmaf(f.R[1], yi, fmaf(f.R[2], zi, f.p[0])));
+            const float y = fmaf(f.R[3], xi, fmaf(f.R[4], yi, fmaf(f.R[5], zi, f.p[1])));
+            const float z = fmaf(f.R[6], xi, fmaf(f.R[7], yi, fmaf(f.R[8], zi, f.p[2])));
+            const bool maybe_in = x >= f.lo_out[0] && x <= f.hi_out[0] && y >= f.lo_out[1] && y <= f.hi_out[1] &&
+                                  z >= f.lo_out[2] && z <= f.hi_out[2];
             if (maybe_in) {
-                bool surely_in = x >= f.lo_in[0] && x <= f.hi_in[0] && y >= f.lo_in[1] && y <= f.hi_in[1] &&
-                                 z >= f.lo_in[2] && z <= f.hi_in[2];
-                bool exact = !surely_in;
+                const bool surely_in = x >= f.lo_in[0] && x <= f.hi_in[0] && y >= f.lo_in[1] && y <= f.hi_in[1] &&
+                                       z >= f.lo_in[2] && z <= f.hi_in[2];
                 if (surely_in) {
-                    float d32 = trilinear32(g, f, x, y, z) + f.col_th;
+                    const float d32 = trilinear32(gv, gn[0], gn[1], gn[2], f, x, y, z) + f.col_th;
                     if (fabsf(d32) <= f.guard)
-                        exact = true;
+                        queue = true;
                     else
                         active = d32 < 0.0f;
-                }
-                if (exact) {
-                    ++n_recheck;
-                    active = exact_distance(g, A, B, load_point(P, pid)) < 0.0;
+                } else {
+                    queue = true;
                 }
             }
         }
-        // ordered compaction: ascending point ids within the tile
-        const unsigned m = __ballot_sync(kFull, active);
-        if (lane == 0) warp_cnt[warp] = __popc(m);
+        // ordered compaction: ascending active stored indices from the start of
+        // the tile's slots, queued ones from the end (descending positions)
+        const unsigned ma = __ballot_sync(kFull, active), mq = __ballot_sync(kFull, queue);
+        if (lane == 0) {
+            warp_act[warp] = __popc(ma);
+            warp_q[warp] = __popc(mq);
+        }
         __syncthreads();
-        int off = base;
-        for (int w = 0; w < warp; ++w) off += warp_cnt[w];
-        off += __popc(m & ((1u << lane) - 1u));
-        if (active) out[off] = pid;
+        int oa = base_act, oq = base_q;
+        for (int w = 0; w < warp; ++w) {
+            oa += warp_act[w];
+            oq += warp_q[w];
+        }
+        const unsigned below = (1u << lane) - 1u;
+        if (active) out[oa + __popc(ma & below)] = sid;
+        if (queue) out[kTile - 1 - (oq + __popc(mq & below))] = sid;
         __syncthreads();
         if (tid == 0) {
-            int s = 0;
-            for (int w = 0; w < kDetectThreads / 32; ++w) s += warp_cnt[w];
-            base += s;
+            int sa = 0, sq = 0;
+            for (int w = 0; w < kDetectThreads / 32; ++w) {
+                sa += warp_act[w];
+                sq += warp_q[w];
+            }
+            base_act += sa;
+            base_q += sq;
         }
         __syncthreads();
     }
-    if (tid == 0) tile_count[t] = base;
-    if (recheck) {
-        for (int o = 16; o > 0; o >>= 1) n_recheck += __shfl_xor_sync(kFull, n_recheck, o);
-        if (lane == 0 && n_recheck) atomicAdd(recheck, (unsigned long long)n_recheck);
+    if (tid == 0) {
+        tile_count[t] = base_act;
+        tile_queue[t] = base_q;
+    }
+}
+
+// One warp per tile: the reference's FP64 distance for the queued points,
+// appended (ascending) after the tile's FP32-classified actives.
+__global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restrict__ inst,
+                                                     const int* __restrict__ tile_inst, BatchInputs in,
+                                                     const GridDesc* __restrict__ grids,
+                                                     const PointsDesc* __restrict__ points, int* __restrict__ ids,
+                                                     int* __restrict__ tile_count, const int* __restrict__ tile_queue,
+                                                     unsigned long long* __restrict__ recheck) {
+    __shared__ int qs[kTile];
+    const int t = blockIdx.x;
+    const int q = tile_queue[t];
+    if (q == 0) return;
+    const int lane = threadIdx.x;
+    const int i = tile_inst[t];
+    const InstanceDesc I = inst[i];
+    const GridDesc g = grids[I.grid];
+    const PointsDesc P = points[I.points];
+    const Pose A = load_pose(in.EA + 16 * (size_t)i), B = load_pose(in.EB + 16 * (size_t)i);
+    int* out = ids + (size_t)t * kTile;
+    // queued stored indices sit at descending positions from the end: read them
+    // back in ascending order before any write can reach those slots
+    for (int k = lane; k < q; k += 32) qs[k] = out[kTile - 1 - k];
+    __syncwarp();
+    int base = tile_count[t];
+    for (int r0 = 0; r0 < q; r0 += 32) {
+        const int k = r0 + lane;
+        bool active = false;
+        int sid = 0;
+        if (k < q) {
+            sid = qs[k];
+            active = exact_distance(g, A, B, load_point(P, sid)) < 0.0;
+        }
+        const unsigned m = __ballot_sync(kFull, active);
+        if (active) out[base + __popc(m & ((1u << lane) - 1u))] = sid;
+        base += __popc(m);
+    }
+    if (lane == 0) {
+        tile_count[t] = base;
+        if (recheck) atomicAdd(recheck, (unsigned long long)q);
     }
 }
 
 // ------------------------------------------------------------------ forces
-// Warp-level sink: sums each produced value over the warp's 32 contacts with a
-// shuffle butterfly and adds it to the warp's shared-memory row.
-template <int NV>
+// Per-warp accumulator of one output value.  FP64 for the FP64 path; for the
+// FP32 path an FP32 pair (hi, lo) updated by Knuth's TwoSum, which keeps the
+// rounding error of every addition, so the running sum carries about twice
+// FP32's precision without touching GB300's slow FP64 pipe.
+template <typename T>
+struct Accum;
+template <>
+struct Accum<double> {
+    double v;
+    __device__ __forceinline__ void zero() { v = 0.0; }
+    __device__ __forceinline__ void add(double x) { v += x; }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <>
+struct Accum<float> {
+    float hi, lo;
+    __device__ __forceinline__ void zero() { hi = lo = 0.f; }
+    __device__ __forceinline__ void add(float x) {
+        const float s = hi + x;
+        const float bb = s - hi;
+        const float err = (hi - (s - bb)) + (x - bb);
+        hi = s;
+        lo += err;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Sum over the 32 lanes of 12 values per lane by recursive halving: at each
+// of the first four levels a lane keeps half of its remaining values and
+// trades the other half with its partner (8 + 4 + 2 + 1 shuffles), the fifth
+// level adds the two lane halves.  Lane L ends with the warp total of value
+// (L >> 1) & 15 (values 12-15 are zero padding), so 12 even lanes then add
+// their totals to 12 different accumulators at once.
+template <typename T>
+__device__ __forceinline__ T warp_reduce12(const T (&v)[12], int lane) {
+    T a[8];
+    const bool h16 = lane & 16;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const T lo = v[k], hi = k + 8 < 12 ? v[k + 8] : T(0);
+        const T send = h16 ? lo : hi;
+        a[k] = (h16 ? hi : lo) + __shfl_xor_sync(kFull, send, 16);
+    }
+    const bool h8 = lane & 8;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const T send = h8 ? a[k] : a[k + 4];
+        a[k] = (h8 ? a[k + 4] : a[k]) + __shfl_xor_sync(kFull, send, 8);
+    }
+    const bool h4 = lane & 4;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const T send = h4 ? a[k] : a[k + 2];
+        a[k] = (h4 ? a[k + 2] : a[k]) + __shfl_xor_sync(kFull, send, 4);
+    }
+    const bool h2 = lane & 2;
+    {
+        const T send = h2 ? a[0] : a[1];
+        a[0] = (h2 ? a[1] : a[0]) + __shfl_xor_sync(kFull, send, 2);
+    }
+    return a[0] + __shfl_xor_sync(kFull, a[0], 1);
+}
+
+// Warp-level sink: sums each group of 12 produced values over the warp's 32
+// contacts and adds the warp totals to the warp's shared-memory accumulators.
+template <int NV, typename T>
 struct WarpSink {
-    double* acc;  // this warp's NV accumulators
+    Accum<T>* acc;  // this warp's NV accumulators
     int lane;
     bool valid;
-    V3 xi1, xi2;
+    Vec3<T> xi1, xi2;
 
-    __device__ __forceinline__ void add(int idx, double v) {
-        v = valid ? v : 0.0;
+    // values v[r] go to accumulator base + stride * r
+    __device__ __forceinline__ void add12(T (&v)[12], int base, int stride) {
+        if (!valid)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-        if (lane == 0) acc[idx] += v;
-    }
-    __device__ __forceinline__ void add3(int idx, int stride, V3 v) {
-        add(idx, v.x);
-        add(idx + stride, v.y);
-        add(idx + 2 * stride, v.z);
+            for (int r = 0; r < 12; ++r) v[r] = T(0);
+        const T sum = warp_reduce12(v, lane);
+        const int slot = (lane >> 1) & 15;
+        if (!(lane & 1) && slot < 12) acc[base + stride * slot].add(sum);
     }
     // fm = [xi1 x f1; f1; xi2 x f2; f2]  (Gamma^T f, simulation/redmax/Utils.h:196)
-    __device__ __forceinline__ void force(V3 a1, V3 f1, V3 a2, V3 f2) {
+    __device__ __forceinline__ void force(Vec3<T> a1, Vec3<T> f1, Vec3<T> a2, Vec3<T> f2) {
+        xi1 = a1;
+        xi2 = a2;
+        const Vec3<T> t1 = cross(a1, f1), t2 = cross(a2, f2);
+        T v[12] = {t1.x, t1.y, t1.z, f1.x, f1.y, f1.z, t2.x, t2.y, t2.z, f2.x, f2.y, f2.z};
+        add12(v, 0, 1);
+    }
+    // column c of [Km | Dm]: rows [xi1 x N1; N1; xi2 x N2 + T2; N2]
+    __device__ __forceinline__ void column(int c, Vec3<T> N1, Vec3<T> N2, Vec3<T> T2) {
+        if constexpr (NV == kOutDeriv) {
+            const Vec3<T> r0 = cross(xi1, N1), r2 = cross(xi2, N2) + T2;
+            T v[12] = {r0.x, r0.y, r0.z, N1.x, N1.y, N1.z, r2.x, r2.y, r2.z, N2.x, N2.y, N2.z};
+            add12(v, c < 12 ? 12 + c : 156 + (c - 12), 12);
+        }
+    }
+};
+
+// The FP32 path fits 128 registers, so four CTAs (16 warps) share an SM; the
+// FP64 path is left its full register budget.
+template <typename T>
+constexpr int force_min_blocks() {
+    return std::is_same<T, float>::value ? 4 : 1;
+}
+
+template <bool DERIV, bool STENCIL, typename T>
+__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(const InstanceDesc* __restrict__ inst, BatchInputs in,
+                                                       const GridDesc* __restrict__ grids,
+                                                       const PointsDesc* __restrict__ points,
+                                                       const int* __restrict__ ids,
+                                                       const int* __restrict__ tile_count,
+                                                       double* __restrict__ partial, int* __restrict__ squeue,
+                                                       int* __restrict__ squeue_count) {
+    constexpr int NV = DERIV ? kOutDeriv : kOutValue;
+    constexpr int NW = kChunk / 32;
+    constexpr bool kDefer = std::is_same<T, float>::value && !STENCIL;
+    __shared__ Accum<T> acc[NW * NV];
+    __shared__ int prefix[kMaxTilesPerInstance + 1];
+    __shared__ GridDesc g;
+    __shared__ PointsDesc P;
+    __shared__ PairState<T> S;
+    __shared__ int wq[NW], qbase;
+    const int i = blockIdx.y, s = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const InstanceDesc I = inst[i];
+    if (warp == 0) {
+        // inclusive prefix of the instance's tile counts, 32 tiles at a time
+        int run = 0;
+        if (lane == 0) prefix[0] = 0;
+        for (int k0 = 0; k0 < I.ntiles; k0 += 32) {
+            const int k = k0 + lane;
+            int v = k < I.ntiles ? tile_count[I.tile0 + k] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(kFull, v, o);
+                if (lane >= o) v += u;
+            }
+            if (k < I.ntiles) prefix[k + 1] = run + v;
+            run += __shfl_sync(kFull, v, 31);
+        }
+    } else if (tid == 32) {
+        g = grids[I.grid];
+        P = points[I.points];
+        make_pair_state(in.EA + 16 * (size_t)i, in.phiA + 6 * (size_t)i, in.EB + 16 * (size_t)i,
+                        in.phiB + 6 * (size_t)i, in.prm + 6 * (size_t)i, S);
+    }
+    for (int k = tid; k < NW * NV; k += kChunk) acc[k].zero();
+    if (tid == 0) qbase = 0;
+    __syncthreads();
+    const int total = prefix[I.ntiles];
+    const int nchunks = (total + kChunk - 1) / kChunk;
+    int* queue = squeue + squeue_offset(i, I.tile0, I.ntiles, s);
+    if (s < nchunks) {
+        for (int chunk = s; chunk < nchunks; chunk += kSlots) {
+            const int c = chunk * kChunk + tid;
+            const bool valid = c < total;
+            V3 xi = v3(0, 0, 0);
+            int sid = 0;
+            if (valid) {
+                int lo = 0, hi = I.ntiles;  // largest k with prefix[k] <= c
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (prefix[mid] <= c)
+                        lo = mid;
+                    else
+                        hi = mid;
+                }
+                sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
+                xi = load_point(P, sid);
+            }
+            FastCell fc;
+            const FastCell* fcp = nullptr;
+            bool here = valid;
+            if constexpr (kDefer) {
+                fc = fast_cell<T>(g, S.RT, S.pT, xi);
+                fcp = &fc;
+                const bool defer = valid && !fc.ok;
+                here = valid && fc.ok;
+                // queue the deferred contacts of this chunk in order
+                const unsigned m = __ballot_sync(kFull, defer);
+                if (lane == 0) wq[warp] = __popc(m);
+                __syncthreads();
+                int off = qbase;
+                for (int w = 0; w < warp; ++w) off += wq[w];
+                if (defer) queue[off + __popc(m & ((1u << lane) - 1u))] = sid;
+                __syncthreads();
+                if (tid == 0)
+                    for (int w = 0; w < NW; ++w) qbase += wq[w];
+            }
+            WarpSink<NV, T> sink{acc + warp * NV, lane, here, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
+            if constexpr (DERIV) {
+                contact_force_jacobian<T>(g, xi, S, fcp, sink, here, STENCIL);
+            } else {
+                ContactForce<T> F = contact_force<T>(g, xi, S, fcp, here, STENCIL);
+                sink.force(F.xi1, F.f1, F.xi2, F.f2);
+            }
+        }
+    }
+    if constexpr (kDefer) {
+        __syncthreads();
+        if (tid == 0) squeue_count[(size_t)i * kSlots + s] = qbase;
+    }
+    __syncthreads();
+    double* row = partial + ((size_t)i * kSlots + s) * NV;
+    for (int k = tid; k < NV; k += kChunk) {
+        double v = 0.0;
+        for (int w = 0; w < NW; ++w) v += acc[w * NV + k].value();
+        row[k] = v;
+    }
+}
+
+// Per-thread sink of stencil_kernel: adds each value of one contact, in FP64,
+// straight into the thread's own (instance, slot) partial row.
+template <int NV, typename T>
+struct LaneSink {
+    double* row;
+    Vec3<T> xi1, xi2;
+    __device__ __forceinline__ void add3(int idx, int stride, Vec3<T> v) {
+        row[idx] += (double)v.x;
+        row[idx + stride] += (double)v.y;
+        row[idx + 2 * stride] += (double)v.z;
+    }
+    __device__ __forceinline__ void force(Vec3<T> a1, Vec3<T> f1, Vec3<T> a2, Vec3<T> f2) {
         xi1 = a1;
         xi2 = a2;
         add3(0, 1, cross(a1, f1));
@@ -208,8 +461,7 @@ struct WarpSink {
         add3(6, 1, cross(a2, f2));
         add3(9, 1, f2);
     }
-    // column c of [Km | Dm]: rows [xi1 x N1; N1; xi2 x N2 + T2; N2]
-    __device__ __forceinline__ void column(int c, V3 N1, V3 N2, V3 T2) {
+    __device__ __forceinline__ void column(int c, Vec3<T> N1, Vec3<T> N2, Vec3<T> T2) {
         if constexpr (NV == kOutDeriv) {
             const int base = c < 12 ? 12 + c : 156 + (c - 12);
             add3(base, 12, cross(xi1, N1));
@@ -220,83 +472,37 @@ struct WarpSink {
     }
 };
 
-template <bool DERIV, bool STENCIL>
-__global__ void __launch_bounds__(kChunk) force_kernel(const InstanceDesc* __restrict__ inst, BatchInputs in,
-                                                       const GridDesc* __restrict__ grids,
-                                                       const PointsDesc* __restrict__ points,
-                                                       const int* __restrict__ ids,
-                                                       const int* __restrict__ tile_count,
-                                                       double* __restrict__ partial) {
+// The contacts force_kernel deferred: one thread per (instance, slot) queue,
+// each contact through the exact path, in queue order.
+template <bool DERIV>
+__global__ void __launch_bounds__(128) stencil_kernel(const InstanceDesc* __restrict__ inst, int n_inst, BatchInputs in,
+                                                      const GridDesc* __restrict__ grids,
+                                                      const PointsDesc* __restrict__ points,
+                                                      const int* __restrict__ squeue,
+                                                      const int* __restrict__ squeue_count,
+                                                      double* __restrict__ partial) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
-    constexpr int NW = kChunk / 32;
-    __shared__ double acc[NW * NV];
-    __shared__ int prefix[kMaxTilesPerInstance + 1];
-    __shared__ GridDesc g;
-    __shared__ PointsDesc P;
-    const int i = blockIdx.y, s = blockIdx.x;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_inst * kSlots) return;
+    const int count = squeue_count[q];
+    if (count == 0) return;
+    const int i = q / kSlots, s = q % kSlots;
     const InstanceDesc I = inst[i];
-    if (tid == 0) {
-        int run = 0;
-        prefix[0] = 0;
-        for (int k = 0; k < I.ntiles; ++k) {
-            run += tile_count[I.tile0 + k];
-            prefix[k + 1] = run;
+    const GridDesc g = grids[I.grid];
+    const PointsDesc P = points[I.points];
+    PairState<float> S;
+    make_pair_state(in.EA + 16 * (size_t)i, in.phiA + 6 * (size_t)i, in.EB + 16 * (size_t)i, in.phiB + 6 * (size_t)i,
+                    in.prm + 6 * (size_t)i, S);
+    const int* queue = squeue + squeue_offset(i, I.tile0, I.ntiles, s);
+    LaneSink<NV, float> sink{partial + (size_t)q * NV, vec3<float>(0, 0, 0), vec3<float>(0, 0, 0)};
+    for (int k = 0; k < count; ++k) {
+        const V3 xi = load_point(P, queue[k]);
+        if constexpr (DERIV) {
+            contact_force_jacobian<float>(g, xi, S, nullptr, sink, true, false);
+        } else {
+            ContactForce<float> F = contact_force<float>(g, xi, S, nullptr, true, false);
+            sink.force(F.xi1, F.f1, F.xi2, F.f2);
         }
-        g = grids[I.grid];
-        P = points[I.points];
-    }
-    for (int k = tid; k < NW * NV; k += kChunk) acc[k] = 0.0;
-    __syncthreads();
-    const int total = prefix[I.ntiles];
-    const int nchunks = (total + kChunk - 1) / kChunk;
-    if (s < nchunks) {
-        BodyState A, B;
-        A.P = load_pose(in.EA + 16 * (size_t)i);
-        B.P = load_pose(in.EB + 16 * (size_t)i);
-        const double* pa = in.phiA + 6 * (size_t)i;
-        const double* pb = in.phiB + 6 * (size_t)i;
-        A.w = v3(pa[0], pa[1], pa[2]);
-        A.v = v3(pa[3], pa[4], pa[5]);
-        B.w = v3(pb[0], pb[1], pb[2]);
-        B.v = v3(pb[3], pb[4], pb[5]);
-        const double* pr = in.prm + 6 * (size_t)i;
-        ContactParams cp;
-        cp.kn = pr[0] * pr[4] * pr[5];
-        cp.kt = pr[1] * pr[4] * pr[5];
-        cp.mu = pr[2];
-        cp.kd = pr[3];
-        for (int chunk = s; chunk < nchunks; chunk += kSlots) {
-            const int c = chunk * kChunk + tid;
-            const bool valid = c < total;
-            V3 xi = v3(0, 0, 0);
-            if (valid) {
-                int lo = 0, hi = I.ntiles;  // largest k with prefix[k] <= c
-                while (hi - lo > 1) {
-                    int mid = (lo + hi) >> 1;
-                    if (prefix[mid] <= c)
-                        lo = mid;
-                    else
-                        hi = mid;
-                }
-                const int pid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
-                xi = load_point(P, pid);
-            }
-            WarpSink<NV> sink{acc + warp * NV, lane, valid, v3(0, 0, 0), v3(0, 0, 0)};
-            if constexpr (DERIV) {
-                contact_force_jacobian(g, xi, A, B, cp, sink, valid, STENCIL);
-            } else {
-                ContactForce F = contact_force(g, xi, A, B, cp, valid, STENCIL);
-                sink.force(F.xi1, F.f1, F.xi2, F.f2);
-            }
-        }
-    }
-    __syncthreads();
-    double* row = partial + ((size_t)i * kSlots + s) * NV;
-    for (int k = tid; k < NV; k += kChunk) {
-        double v = 0.0;
-        for (int w = 0; w < NW; ++w) v += acc[w * NV + k];
-        row[k] = v;
     }
 }
 
@@ -330,28 +536,56 @@ __global__ void zero_status_kernel(int* status, int n) {
     if (i < n) status[i] = 0;
 }
 
+template <bool DERIV, bool STENCIL>
+void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, const InstanceDesc* d_inst,
+                    BatchInputs in, const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s) {
+    if (precision == kMixed) {
+        force_kernel<DERIV, STENCIL, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
+                                                                         s.tile_count, s.partial, s.squeue,
+                                                                         s.squeue_count);
+        if (!STENCIL)
+            stencil_kernel<DERIV><<<(n_inst * kSlots + 127) / 128, 128, 0, stream>>>(
+                d_inst, n_inst, in, d_grids, d_points, s.squeue, s.squeue_count, s.partial);
+    } else {
+        force_kernel<DERIV, STENCIL, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
+                                                                          s.tile_count, s.partial, s.squeue,
+                                                                          s.squeue_count);
+    }
+}
+
 }  // namespace
 
-void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int total_tiles, BatchInputs in,
-                   const GridDesc* d_grids, const PointsDesc* d_points, int* d_ids, int* d_tile_count,
-                   unsigned long long* d_recheck, cudaStream_t stream) {
+void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
+                   const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream) {
+    if (n_inst <= 0) return;
+    prep_kernel<<<(n_inst + 127) / 128, 128, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter);
     if (total_tiles <= 0) return;
-    detect_kernel<<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points, d_ids,
-                                                              d_tile_count, d_recheck);
+    detect_kernel<<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids, d_points,
+                                                              s.ids, s.tile_count, s.tile_queue);
+    recheck_kernel<<<total_tiles, 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points, s.ids, s.tile_count,
+                                                   s.tile_queue, s.recheck);
 }
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
-                  const PointsDesc* d_points, const int* d_ids, const int* d_tile_count, double* d_partial,
-                  bool deriv, bool stencil, cudaStream_t stream) {
+                  const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
+                  cudaStream_t stream) {
     if (n_inst <= 0) return;
     dim3 grid(kSlots, n_inst);
-    auto* k = deriv ? (stencil ? force_kernel<true, true> : force_kernel<true, false>)
-                    : (stencil ? force_kernel<false, true> : force_kernel<false, false>);
-    k<<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, d_ids, d_tile_count, d_partial);
+    if (deriv) {
+        if (stencil)
+            launch_force_t<true, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+        else
+            launch_force_t<true, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+    } else {
+        if (stencil)
+            launch_force_t<false, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+        else
+            launch_force_t<false, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+    }
 }
 
-void launch_finalize(const InstanceDesc* d_inst, int n_inst, const int* d_tile_count, const double* d_partial,
-                     bool deriv, BatchOutputs out, cudaStream_t stream) {
+void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
+                     cudaStream_t stream) {
     if (n_inst <= 0) return;
     zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out.status, n_inst);
     const int NV = deriv ? kOutDeriv : kOutValue;
@@ -359,9 +593,9 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, const int* d_tile_c
     const int threads = 256;
     const unsigned blocks = (unsigned)((total + threads - 1) / threads);
     if (deriv)
-        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, d_tile_count, d_partial, out);
+        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out);
     else
-        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, d_tile_count, d_partial, out);
+        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out);
 }
 
 }  // namespace sdfc

@@ -1,24 +1,36 @@
 // Kernels of the batched point-vs-SDF contact evaluation (sm_103a).
 //
 // One evaluation of a batch of pair instances (contact body A's points against
-// SDF body B's grid, each instance with its own poses) runs three launches:
+// SDF body B's grid, each instance with its own poses) runs these launches:
 //
+//   prep_kernel      one thread per instance: the FP32 point transform into B's
+//                    grid frame and the error bound ("guard band") of the FP32
+//                    distance, from the instance's FP64 poses.
 //   detect_kernel    one CTA per tile of kTile points of one instance.  Every
-//                    point is transformed into B's grid frame and its distance
-//                    evaluated in FP32 with a rigorous error bound; points whose
-//                    FP32 distance lies inside the bound ("guard band") or near
-//                    the box faces are re-evaluated in FP64 exactly as the
-//                    reference does.  Active ids (distance < 0) are compacted
-//                    in ascending order per tile (ballot + CTA scan), which is
-//                    the order the reference's detection loop produces
-//                    (simulation/redmax/CollisionDetection/CollisionDetection.cpp:124-147).
+//                    point's distance is evaluated in FP32; points whose FP32
+//                    distance is outside the guard band are classified there,
+//                    the others (and points near the box faces) are queued in
+//                    the tile for an exact FP64 recheck.  Active stored indices
+//                    are compacted in ascending order (ballot + CTA scan).
+//   recheck_kernel   one warp per tile with queued points: the reference's FP64
+//                    distance (BodySDFObj::distance, bit-identical), appending
+//                    the active ones to the tile's list in ascending order.
+//                    Detection as a whole restates
+//                    simulation/redmax/CollisionDetection/CollisionDetection.cpp:124-147.
 //   force_kernel     one CTA per (instance, slot).  The instance's active
 //                    contacts are cut into chunks of kChunk; slot s takes chunks
-//                    s, s+kSlots, ...  Each thread evaluates one contact in FP64;
-//                    the per-contact force (12 values) and, with derivatives, the
-//                    24 Jacobian columns (288 values) are summed over the warp
-//                    with shuffles and over the CTA in shared memory, in a fixed
+//                    s, s+kSlots, ...  Each thread evaluates one contact; the
+//                    per-contact force (12 values) and, with derivatives, the 24
+//                    Jacobian columns (288 values) are summed over the warp with
+//                    shuffles and over the CTA in FP64 shared memory, in a fixed
 //                    order, into one partial row per (instance, slot).
+//                    On the FP32 path a contact whose derivative stencil could
+//                    leave its cell is not evaluated there: it is queued (in
+//                    order) for stencil_kernel, so that no warp runs the long
+//                    FP64 stencil for one lane while 31 wait.
+//   stencil_kernel   one thread per (instance, slot) queue: the queued contacts
+//                    through the exact path (the reference's FP64 stencil), FP32
+//                    algebra, added in queue order to the (instance, slot) row.
 //   finalize_kernel  sums the kSlots partial rows of each instance in order and
 //                    scatters them into fm / Km / Dm.
 //
@@ -47,6 +59,16 @@ struct InstanceDesc {
     int ntiles;
 };
 
+// FP32 prefilter constants of one instance (written by prep_kernel).
+struct Prefilter {
+    float R[9], p[3];            // point -> grid frame: x = R xi + p
+    float gmin[3], ginv[3];      // grid origin and 1/dx
+    float lo_in[3], hi_in[3];    // certainly inside the box between these
+    float lo_out[3], hi_out[3];  // certainly outside beyond these
+    float col_th;
+    float guard;                 // bound on |d32 - d64|, times a safety factor
+};
+
 // Per-evaluation inputs, device pointers (row-major 4x4 poses, body twists).
 struct BatchInputs {
     const double* EA;    // n x 16
@@ -61,22 +83,44 @@ struct BatchOutputs {
     double* Km;      // n x 144 (may be null for value-only evaluations)
     double* Dm;      // n x 144
     int* n_active;   // n
-    int* status;     // n: bit 0 = non-finite output, bit 1 = FP64 recheck count overflow (unused)
+    int* status;     // n: bit 0 = non-finite output
 };
 
-struct DetectStats {
-    unsigned long long rechecked;  // points re-evaluated in FP64 (diagnostic)
+// Scratch of a batch: device buffers sized at batch creation.
+struct BatchScratch {
+    Prefilter* prefilter;       // n
+    int* ids;                   // total_tiles x kTile: active stored indices, queued rechecks at the tail
+    int* tile_count;            // total_tiles: active count per tile
+    int* tile_queue;            // total_tiles: queued recheck count per tile
+    double* partial;            // n x kSlots x kOutDeriv
+    unsigned long long* recheck;  // diagnostic counter of FP64 rechecks
+    int* squeue;                // deferred exact-stencil contacts (stored point indices), see stencil_kernel
+    int* squeue_count;          // n x kSlots
 };
 
-void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int total_tiles, BatchInputs in,
-                   const GridDesc* d_grids, const PointsDesc* d_points, int* d_ids, int* d_tile_count,
-                   unsigned long long* d_recheck, cudaStream_t stream);
+// Region of the deferred-contact queue of (instance, slot): slot s of an
+// instance with `ntiles` tiles takes at most ntiles*kTile/kSlots + kChunk
+// contacts (its chunks s, s+kSlots, ... of kChunk contacts).
+__host__ __device__ inline size_t squeue_slot_size(int ntiles) {
+    return (size_t)ntiles * kTile / kSlots + kChunk;
+}
+__host__ __device__ inline size_t squeue_offset(int inst, int tile0, int ntiles, int slot) {
+    return (size_t)tile0 * kTile + (size_t)inst * kSlots * kChunk + (size_t)slot * squeue_slot_size(ntiles);
+}
+__host__ __device__ inline size_t squeue_capacity(int n_inst, int total_tiles) {
+    return (size_t)total_tiles * kTile + (size_t)n_inst * kSlots * kChunk;
+}
+
+enum Precision { kFP64 = 0, kMixed = 1 };
+
+void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
+                   const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream);
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
-                  const PointsDesc* d_points, const int* d_ids, const int* d_tile_count, double* d_partial,
-                  bool deriv, bool stencil, cudaStream_t stream);
+                  const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
+                  cudaStream_t stream);
 
-void launch_finalize(const InstanceDesc* d_inst, int n_inst, const int* d_tile_count, const double* d_partial,
-                     bool deriv, BatchOutputs out, cudaStream_t stream);
+void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
+                     cudaStream_t stream);
 
 }  // namespace sdfc

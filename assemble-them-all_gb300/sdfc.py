@@ -23,8 +23,11 @@ EXPORTS = (
     "sdfc_create", "sdfc_destroy", "sdfc_last_error", "sdfc_upload_grid", "sdfc_upload_points",
     "sdfc_evaluate", "sdfc_active_ids", "sdfc_batch_create", "sdfc_batch_destroy", "sdfc_batch_evaluate",
     "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count", "sdfc_set_derivative_mode",
-    "sdfc_batch_set_derivative_mode",
+    "sdfc_batch_set_derivative_mode", "sdfc_batch_set_timing", "sdfc_batch_last_timing", "sdfc_set_precision",
+    "sdfc_batch_set_precision",
 )
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
 DERIV_ANALYTIC = 0
 DERIV_STENCIL = 1
 
@@ -74,6 +77,10 @@ def lib():
         L.sdfc_batch_recheck_count.argtypes = [v, P(ctypes.c_ulonglong), i]
         L.sdfc_set_derivative_mode.argtypes = [v, i]
         L.sdfc_batch_set_derivative_mode.argtypes = [v, i]
+        L.sdfc_batch_set_timing.argtypes = [v, i]
+        L.sdfc_set_precision.argtypes = [v, i]
+        L.sdfc_batch_set_precision.argtypes = [v, i]
+        L.sdfc_batch_last_timing.argtypes = [v, P(ctypes.c_float)]
         _lib = L
     return _lib
 
@@ -163,6 +170,10 @@ class Context:
         """DERIV_ANALYTIC or DERIV_STENCIL for sdfc_evaluate and later batches."""
         self._check(lib().sdfc_set_derivative_mode(self._h, int(mode)), "sdfc_set_derivative_mode")
 
+    def set_precision(self, precision: int):
+        """PRECISION_FP64 or PRECISION_MIXED for sdfc_evaluate and later batches."""
+        self._check(lib().sdfc_set_precision(self._h, int(precision)), "sdfc_set_precision")
+
     def batch(self, points, grids) -> "Batch":
         return Batch(self, points, grids)
 
@@ -214,7 +225,19 @@ class Batch:
         """Device pointers (ints, e.g. torch tensor.data_ptr()); enqueued on `stream` without syncing."""
         self.ctx._check(lib().sdfc_batch_evaluate_device(self._h, E_A, phi_A, E_B, phi_B, params,
                                                          int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active,
-                                                         status, stream or None), "sdfc_batch_evaluate_device")
+                                                         status, stream), "sdfc_batch_evaluate_device")
+
+    def set_precision(self, precision: int):
+        self.ctx._check(lib().sdfc_batch_set_precision(self._h, int(precision)), "sdfc_batch_set_precision")
+
+    def set_timing(self, enable=True):
+        self.ctx._check(lib().sdfc_batch_set_timing(self._h, int(bool(enable))), "sdfc_batch_set_timing")
+
+    def last_timing(self):
+        """(detect_ms, force_ms, reduce_ms) of the last evaluation."""
+        ms = (ctypes.c_float * 3)()
+        self.ctx._check(lib().sdfc_batch_last_timing(self._h, ms), "sdfc_batch_last_timing")
+        return tuple(float(x) for x in ms)
 
     def recheck_count(self, reset=False) -> int:
         c = ctypes.c_ulonglong()

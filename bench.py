@@ -13,7 +13,10 @@ A step is one force evaluation with derivatives of the whole batch: detection
 over every point of every instance, then force, dF/dq and dF/dqdot of every
 active contact (ForceGeneralSDFContact::computeForceWithDerivative,
 simulation/redmax/Force/ForceGeneralSDFContact.cpp:69-105), reduced per
-instance in FP64.  The metric is contact-point evaluations per second.
+instance in FP64.  The metric is contact-point evaluations per second of the
+batched mixed-precision path (FP64 penetration depth and sums, FP32
+per-contact algebra); the line also carries the plain per-instance FP64 GPU
+path on the same inputs and the mixed path's error against it.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -233,6 +236,15 @@ def workload_config(args):
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": "instances per GPU (replicas)"}
 
 
+def rel_err(a, b):
+    """|a - b| / max(min(|a|, |b|), 1e-4) (simulation/redmax/Utils.h:362-381), worst over instances."""
+    a = a.reshape(len(a), -1)
+    b = b.reshape(len(b), -1)
+    e = np.linalg.norm(a - b, axis=1)
+    d = np.maximum(np.minimum(np.linalg.norm(a, axis=1), np.linalg.norm(b, axis=1)), 1e-4)
+    return float(np.max(e / d))
+
+
 def run_gpu(args, world, rank):
     grid, pts, states = build_workload(args.instances, args.points, args.grid, rank)
     pool = None
@@ -248,6 +260,7 @@ def run_gpu(args, world, rank):
     p = ctx.upload_points(pts, sdfc.STORAGE_F32)
     n = args.instances
     batch = ctx.batch([p] * n, [g] * n)
+    batch.set_precision(sdfc.PRECISION_MIXED if args.precision == "mixed" else sdfc.PRECISION_FP64)
     EA, phiA, EB, phiB = states
     prm_rows = np.tile(np.array(PARAMS), (n, 1))
     cuda = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()  # noqa: E731
@@ -258,52 +271,77 @@ def run_gpu(args, world, rank):
     nact = torch.zeros(n, dtype=torch.int32, device="cuda")
     st = torch.zeros(n, dtype=torch.int32, device="cuda")
     flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
-
-    def step():
-        batch.evaluate_device(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
-                              fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
-                              want_deriv=True, stream=stream.cuda_stream)
-
-    for _ in range(args.warmup):
-        step()
+    stream = torch.cuda.Stream()
     torch.cuda.synchronize()
-    assert not st.any().item(), "non-finite contact output"
-    n_active = int(nact.sum().item())
 
-    # timed region: K steps, each bracketed by CUDA events on the launching stream, L2 flushed between
-    dist_barrier(world)
-    torch.cuda.synchronize()
-    clocks = ClockSampler(dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    t0 = time.perf_counter()
-    for a, b in ev:
-        flush.zero_()
-        a.record(stream)
-        step()
-        b.record(stream)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    clk = clocks.stop()
-    dist_barrier(world)
-    step_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-    step_ms = dist_max(step_ms, world)
-    pts_per_step = n * args.points
-    value = world * pts_per_step / (step_ms / 1e3)
+    def step(b=batch):
+        b.evaluate_device(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
+                          fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
+                          want_deriv=True, stream=stream.cuda_stream)
 
-    # per-phase device times (separate pass with events between the launches)
-    batch.set_timing(True)
-    phases = []
-    for _ in range(max(3, args.steps // 2)):
-        flush.zero_()
-        step()
-        phases.append(batch.last_timing())
-    batch.set_timing(False)
-    det_ms, frc_ms, red_ms = (float(np.mean([x[i] for x in phases])) for i in range(3))
-    rechecked = batch.recheck_count(reset=True)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        stream.synchronize()
+        assert not st.any().item(), "non-finite contact output"
+        n_active = int(nact.sum().item())
+        out_fast = (fm.cpu().numpy().copy(), Km.cpu().numpy().copy(), Dm.cpu().numpy().copy())
+
+        # timed region: K steps, each bracketed by CUDA events on the launching stream, L2 flushed between
+        dist_barrier(world)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        t0 = time.perf_counter()
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+        dist_barrier(world)
+        step_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        step_ms = dist_max(step_ms, world)
+        pts_per_step = n * args.points
+        value = world * pts_per_step / (step_ms / 1e3)
+
+        # per-phase device times (separate pass with events between the launches)
+        batch.set_timing(True)
+        phases = []
+        for _ in range(max(3, args.steps // 2)):
+            flush.zero_()
+            stream.synchronize()
+            batch.evaluate_device(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(),
+                                  dprm.data_ptr(), fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(),
+                                  st.data_ptr(), want_deriv=True, stream=stream.cuda_stream)
+            phases.append(batch.last_timing())
+        batch.set_timing(False)
+        det_ms, frc_ms, red_ms = (float(np.mean([x[i] for x in phases])) for i in range(3))
+        rechecked = batch.recheck_count(reset=True) / (args.warmup + args.steps + len(phases))
+
+    # plain per-instance FP64 GPU path on the same inputs: one FP64 evaluation per instance
+    plain = ctx.batch([p], [g])
+    plain.set_precision(sdfc.PRECISION_FP64)
+    params_c = [sdfc.Params(*PARAMS)] * n
+    ref = [np.zeros((n, 12)), np.zeros((n, 12, 12)), np.zeros((n, 12, 12))]
+    sample = min(n, args.plain_sample)
+    plain_t = []
+    for k in range(n):
+        t = time.perf_counter()
+        f_, K_, D_, _, _ = plain.evaluate(EA[k:k + 1], phiA[k:k + 1], EB[k:k + 1], phiB[k:k + 1], params_c[:1])
+        if k < sample:
+            plain_t.append(time.perf_counter() - t)
+        ref[0][k], ref[1][k], ref[2][k] = f_[0], K_[0], D_[0]
+        if k + 1 >= sample and not args.full_error:
+            break
+    m = n if args.full_error else sample
+    err = {"fm": rel_err(out_fast[0][:m], ref[0][:m]), "Km": rel_err(out_fast[1][:m], ref[1][:m]),
+           "Dm": rel_err(out_fast[2][:m], ref[2][:m]), "instances": m}
+    plain_rate = args.points / float(np.mean(plain_t[1:] if len(plain_t) > 1 else plain_t))
 
     # e2e through the C ABI with host buffers (H2D of the instance states, D2H of fm/Km/Dm)
-    params_c = [sdfc.Params(*PARAMS)] * n
     e2e_t = []
     for k in range(max(3, args.steps // 2) + 1):
         flush.zero_()
@@ -325,7 +363,7 @@ def run_gpu(args, world, rank):
     # forces: per active contact its id (4 B), point (12 B) and 8 FP32 corners; per instance-slot 300 FP64 partials
     frc_bytes = n_active * (4 + 12 + 32) + n * 8 * 300 * 8
     kernels = {
-        "detect_kernel": {"ms": det_ms, "bytes": det_bytes},
+        "detect": {"ms": det_ms, "bytes": det_bytes},
         "force_kernel": {"ms": frc_ms, "bytes": frc_bytes},
         "finalize_kernel": {"ms": red_ms, "bytes": n * 8 * 300 * 8 + n * 300 * 8},
     }
@@ -335,7 +373,9 @@ def run_gpu(args, world, rank):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 (fp32 detection prefilter)", "data": "synthetic",
+        "vs_baseline": None,
+        "dtype": "f64 depth/sums, f32 per-contact algebra" if args.precision == "mixed" else "f64",
+        "data": "synthetic",
         "config": workload_config(args),
         "e2e": {"value": world * pts_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
@@ -343,8 +383,11 @@ def run_gpu(args, world, rank):
                      "frac": ach / hbm_peak, "traffic": traffic,
                      "peak_source": "measured" if peaks else "fallback"},
         "phases_ms": {"detect": det_ms, "force": frc_ms, "reduce": red_ms},
-        "active_contacts_per_step": n_active, "fp64_rechecked_points_per_step": rechecked / (len(phases) or 1),
-        "gpu_launches": 4 * args.steps,
+        "plain_fp64_per_instance": {"value": plain_rate, "unit": UNIT, "instances_timed": len(plain_t),
+                                    "speedup_of_batched": value / plain_rate},
+        "error_vs_fp64_path": err,
+        "active_contacts_per_step": n_active, "fp64_rechecked_points_per_step": rechecked,
+        "gpu_launches": (7 if args.precision == "mixed" else 6) * args.steps,
         "clocks": clk,
         "wall_s": wall,
     }
@@ -371,6 +414,9 @@ def main():
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=512, help="instances per CPU-baseline step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
+    ap.add_argument("--plain-sample", type=int, default=64, help="instances timed on the per-instance FP64 path")
+    ap.add_argument("--full-error", action="store_true", help="compare every instance against the FP64 path")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank = dist_setup()

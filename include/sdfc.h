@@ -59,6 +59,16 @@ extern "C" {
 #define SDFC_DERIV_ANALYTIC 0
 #define SDFC_DERIV_STENCIL 1
 
+/* Arithmetic of the per-contact force and Jacobian terms.  In both the
+ * grid-frame point and the penetration depth are FP64 (bit-identical to the
+ * reference's BodySDFObj::distance) and all sums over contacts are FP64.
+ * SDFC_PRECISION_FP64 (default): every per-contact term in FP64.
+ * SDFC_PRECISION_MIXED: the normal, tangential velocity, SDF derivatives and
+ *   the 24 Jacobian columns in FP32 (warp partial sums of 32 contacts in FP32),
+ *   for throughput; its error against the FP64 path is stated in the tests. */
+#define SDFC_PRECISION_FP64 0
+#define SDFC_PRECISION_MIXED 1
+
 typedef struct sdfc_context sdfc_context;
 typedef struct sdfc_batch sdfc_batch;
 
@@ -78,8 +88,9 @@ int sdfc_create(sdfc_context** ctx, int device);
 void sdfc_destroy(sdfc_context* ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char* sdfc_last_error(const sdfc_context* ctx);
-/* Derivative mode of sdfc_evaluate and of batches created afterwards. */
+/* Derivative mode and precision of sdfc_evaluate and of batches created afterwards. */
 int sdfc_set_derivative_mode(sdfc_context* ctx, int mode);
+int sdfc_set_precision(sdfc_context* ctx, int precision);
 
 /* Uploads an SDF body's grid (BodySDFObj::_SDF and its box/spacing/threshold,
  * BodySDFObj.h:13-16; filled by BodySDFObj::precompute_SDF / load_SDF,
@@ -124,8 +135,9 @@ int sdfc_active_ids(sdfc_context* ctx, int* ids, int cap, int* n);
  * as separate processes (utils/parallel.py:10). */
 int sdfc_batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** batch);
 void sdfc_batch_destroy(sdfc_batch* batch);
-/* Derivative mode of this batch (SDFC_DERIV_ANALYTIC or SDFC_DERIV_STENCIL). */
+/* Derivative mode (SDFC_DERIV_*) and precision (SDFC_PRECISION_*) of this batch. */
 int sdfc_batch_set_derivative_mode(sdfc_batch* batch, int mode);
+int sdfc_batch_set_precision(sdfc_batch* batch, int precision);
 
 /* Evaluates every instance.  Arrays are per instance, row-major, HOST memory:
  * E_A, E_B [n*16]; phi_A, phi_B [n*6]; params [n]; fm [n*12]; Km, Dm [n*144]
@@ -135,12 +147,21 @@ int sdfc_batch_evaluate(sdfc_batch* batch, const double* E_A, const double* phi_
                         const double* phi_B, const sdfc_params* params, int want_deriv, double* fm, double* Km,
                         double* Dm, int* n_active, int* status);
 
-/* Same with DEVICE arrays, enqueued on `stream` (a cudaStream_t, NULL for the
- * context's stream) without synchronising; capturable in a CUDA graph.
+/* Same with DEVICE arrays, enqueued on `stream` (a cudaStream_t; NULL is the
+ * legacy default stream) without synchronising; capturable in a CUDA graph.
  * params is an n x 6 device array (kn, kt, mu, damping, scale, contact_scale). */
 int sdfc_batch_evaluate_device(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
                                const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
                                double* Dm, int* n_active, int* status, void* stream);
+
+/* Per-phase device time of the last evaluation of this batch, the GPU
+ * counterpart of ForceGeneralSDFContact's "collision detection" and "compute
+ * force" timers (Force::Timer, simulation/redmax/Force/Force.h:15-36;
+ * ForceGeneralSDFContact.cpp:65-66).  Enable with sdfc_batch_set_timing(b, 1)
+ * (CUDA events are then recorded between the launches); ms[0] = detection,
+ * ms[1] = contact forces, ms[2] = reduction.  Synchronises on the events. */
+int sdfc_batch_set_timing(sdfc_batch* batch, int enable);
+int sdfc_batch_last_timing(sdfc_batch* batch, float* ms);
 
 /* Number of points the last evaluations of this batch re-checked in FP64
  * because their FP32 distance fell inside the guard band (diagnostic; the

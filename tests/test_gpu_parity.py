@@ -9,12 +9,14 @@ Bars, in the reference's relative-error convention (simulation/redmax/Utils.h:36
     the stencil stays in one cell): fm to 1e-10, Km and Dm to 1e-6.  The
     reference's Hessian is a second difference with step 1e-5, so its own
     round-off is about ulp(SDF) / 1e-10, which reaches Km through the
-    d * dn/dq terms; 1e-6 covers penetrations of a few tenths.
+    d * dn/dq terms; 1e-6 covers penetrations of a few tenths;
+  * mixed precision (FP64 depth and sums, FP32 per-contact algebra): fm, Km
+    and Dm to 1e-5, the bar the batched throughput path is held to.
 """
 import numpy as np
 import pytest
 
-from _helpers import assert_close, load
+from _helpers import assert_close, load, rel_err
 from conftest import submodule
 
 pytestmark = pytest.mark.gpu
@@ -23,6 +25,7 @@ FM_REL = 1e-10
 JAC_REL = 1e-6
 FM_REL_STENCIL = 1e-12
 JAC_REL_STENCIL = 1e-10
+MIXED_REL = 1e-5
 
 
 @pytest.fixture(scope="module")
@@ -166,6 +169,16 @@ def test_edge_cases(sdfc, ctx, oracle, workloads):
     assert_close("nodes fm", fm, rf, rel=FM_REL)
     assert_close("nodes Km", Km, rK, rel=JAC_REL)
     assert_close("nodes Dm", Dm, rD, rel=JAC_REL)
+    # mixed precision: these contacts sit on cell faces and take the deferred exact path
+    ctx.set_precision(sdfc.PRECISION_MIXED)
+    for deriv in (True, False):
+        fm, Km, Dm, n = ctx.evaluate(nodes, grid, EA, z, I, z, prm, want_deriv=deriv)
+        assert n == len(rids)
+        assert_close(f"nodes fm (mixed, deriv={deriv})", fm, rf, rel=MIXED_REL)
+        if deriv:
+            assert_close("nodes Km (mixed)", Km, rK, rel=MIXED_REL)
+            assert_close("nodes Dm (mixed)", Dm, rD, rel=MIXED_REL)
+    ctx.set_precision(sdfc.PRECISION_FP64)
     ctx.set_derivative_mode(sdfc.DERIV_STENCIL)
     fm, Km, Dm, n = ctx.evaluate(nodes, grid, EA, z, I, z, prm)
     ctx.set_derivative_mode(sdfc.DERIV_ANALYTIC)
@@ -191,3 +204,53 @@ def test_invalid_arguments(sdfc, ctx):
         ctx.upload_grid(np.full((4, 4, 4), np.nan), [0, 0, 0], [3, 3, 3], [1, 1, 1], 0.0)
     with pytest.raises(sdfc.SdfcError):
         ctx.batch([12345], [0])
+
+
+def test_mixed_precision_golden(sdfc, ctx, fx):
+    grid = ctx.upload_grid(fx["grid"], fx["min_box"], fx["max_box"], fx["dx"], float(fx["col_th"]), 1)
+    pts = ctx.upload_points(fx["points"], 1)
+    n = len(fx["fm"])
+    b = ctx.batch([pts] * n, [grid] * n)
+    b.set_precision(sdfc.PRECISION_MIXED)
+    prms = [params_of(sdfc, fx["params"][k]) for k in range(n)]
+    fm, Km, Dm, nact, st = b.evaluate(fx["EA"], fx["phiA"], fx["EB"], fx["phiB"], prms, want_deriv=True)
+    fmv, _, _, nactv, _ = b.evaluate(fx["EA"], fx["phiA"], fx["EB"], fx["phiB"], prms, want_deriv=False)
+    assert not st.any()
+    worst = {"fm": 0.0, "Km": 0.0, "Dm": 0.0}
+    for k in range(n):
+        assert nact[k] == nactv[k] == fx["n_active"][k]
+        assert_close(f"mixed {k} fm value", fmv[k], fx["fm_v"][k], rel=MIXED_REL, abs_=1e-9)
+        for name, a, ref in (("fm", fm[k], fx["fm"][k]), ("Km", Km[k], fx["Km"][k]), ("Dm", Dm[k], fx["Dm"][k])):
+            assert_close(f"mixed {k} {name}", a, ref, rel=MIXED_REL, abs_=1e-9)
+            worst[name] = max(worst[name], rel_err(a, ref)[0])
+    print("mixed-precision worst relative error vs the reference:", worst)
+    b.close()
+
+
+def test_mixed_precision_uneven_batch(sdfc, ctx, oracle, workloads):
+    rng = np.random.default_rng(7)
+    g = workloads.socket_grid(96, dtype=np.float32)
+    gh = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+    psets = [workloads.peg_points(n, seed=s) for n, s in ((30000, 4), (5000, 5))]
+    phs = [ctx.upload_points(p, 1) for p in psets]
+    n = 8
+    which = [k % 2 for k in range(n)]
+    b = ctx.batch([phs[w] for w in which], [gh] * n)
+    b.set_precision(sdfc.PRECISION_MIXED)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    EA = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.003),
+                                  [0.0202 * np.cos(a), 0.0202 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
+    EB = np.stack([np.eye(4)] * n)
+    phiA = rng.normal(size=(n, 6)) * 0.2
+    phiB = np.zeros((n, 6))
+    prm = [sdfc.Params(1e5, [1e3, 1e1][k % 2], 0.3, 1e3, 1.0, 1.0) for k in range(n)]
+    fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
+    og = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
+    for k in range(n):
+        op = oracle.Params(prm[k].kn, prm[k].kt, prm[k].mu, prm[k].damping, 1.0, 1.0)
+        rf, rK, rD, rids = oracle.pair_eval(og, psets[which[k]], EA[k], phiA[k], EB[k], phiB[k], op, True)
+        assert nact[k] == len(rids) > 0
+        assert_close(f"inst {k} fm", fm[k], rf, rel=MIXED_REL, abs_=1e-9)
+        assert_close(f"inst {k} Km", Km[k], rK, rel=MIXED_REL, abs_=1e-9)
+        assert_close(f"inst {k} Dm", Dm[k], rD, rel=MIXED_REL, abs_=1e-9)
+    b.close()
