@@ -24,7 +24,7 @@ EXPORTS = (
     "sdfc_evaluate", "sdfc_active_ids", "sdfc_batch_create", "sdfc_batch_destroy", "sdfc_batch_evaluate",
     "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count", "sdfc_set_derivative_mode",
     "sdfc_batch_set_derivative_mode", "sdfc_batch_set_timing", "sdfc_batch_last_timing", "sdfc_set_precision",
-    "sdfc_batch_set_precision",
+    "sdfc_batch_set_precision", "sdfc_evaluate_noalloc",
 )
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -79,6 +79,8 @@ def lib():
         L.sdfc_batch_set_derivative_mode.argtypes = [v, i]
         L.sdfc_batch_set_timing.argtypes = [v, i]
         L.sdfc_set_precision.argtypes = [v, i]
+        L.sdfc_evaluate_noalloc.argtypes = [v, i, i, i, d, d, d, ctypes.c_double, v, i, v, v, v, v, v, i, v, v, v,
+                                            v, v]
         L.sdfc_batch_set_precision.argtypes = [v, i]
         L.sdfc_batch_last_timing.argtypes = [v, P(ctypes.c_float)]
         _lib = L
@@ -244,3 +246,16 @@ class Batch:
         self.ctx._check(lib().sdfc_batch_recheck_count(self._h, ctypes.byref(c), int(bool(reset))),
                         "sdfc_batch_recheck_count")
         return c.value
+
+
+def evaluate_noalloc(grid_values_dev, shape, min_box, max_box, dx, col_th, points_dev, n, E_A, phi_A, E_B, phi_B,
+                     params, fm, Km, Dm, n_active, want_deriv=True, stream=0):
+    """sdfc_evaluate_noalloc: every array argument except min_box / max_box / dx is a device pointer (int).
+
+    For callers that must not allocate device memory at call time; see include/sdfc.h."""
+    ni, nj, nk = shape
+    rc = lib().sdfc_evaluate_noalloc(grid_values_dev, ni, nj, nk, _dp(_f64(min_box, 3)), _dp(_f64(max_box, 3)),
+                                     _dp(_f64(dx, 3)), float(col_th), points_dev, int(n), E_A, phi_A, E_B, phi_B,
+                                     params, int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active, stream)
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_evaluate_noalloc failed ({rc})")

@@ -168,6 +168,36 @@ int sdfc_batch_last_timing(sdfc_batch* batch, float* ms);
  * counter accumulates until reset with reset != 0). */
 int sdfc_batch_recheck_count(sdfc_batch* batch, unsigned long long* count, int reset);
 
+/* ---------------------------------------------------------------- allocation-free evaluation */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need a contact force: inside a real-time or hard-latency
+ * loop (cudaMalloc may synchronise the device), under a host application
+ * that owns all device memory through its own pool, or while recording into a
+ * CUDA stream capture.  One Force call of one (contact body A, SDF body B)
+ * pair like sdfc_evaluate with want_deriv (FP64 arithmetic, analytic cell
+ * derivatives), needing no context: every argument marked "device" is
+ * caller-owned device memory on the current device; min_box, max_box and dxyz
+ * are host arrays.  Grid: ni*nj*nk FP64 values, i fastest; points: n points as
+ * x,y,z doubles; E_A, E_B [16], phi_A, phi_B [6], params [6] (kn, kt, mu,
+ * damping, scale, contact_scale); outputs fm [12], Km, Dm [144] (want_deriv
+ * only), n_active [1].  Enqueued on `stream` (a cudaStream_t; NULL is the
+ * legacy default stream) without synchronising.
+ *
+ * Its working memory is a file-scope device array of about 2.6 MB that every
+ * GPU loading the library holds until exit; n may not exceed
+ * SDFC_NOALLOC_MAX_POINTS (larger n returns SDFC_ERR_CAPACITY).  The first
+ * call on a device looks up that array's device address; make that first call
+ * before any stream capture begins.  All calls share the array: calls whose
+ * work may overlap on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller.  Nothing carries over between calls. */
+#define SDFC_NOALLOC_MAX_POINTS 131072
+int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, int nk, const double* min_box,
+                          const double* max_box, const double* dxyz, double col_th, const double* points, int n,
+                          const double* E_A, const double* phi_A, const double* E_B, const double* phi_B,
+                          const double* params, int want_deriv, double* fm, double* Km, double* Dm, int* n_active,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif
