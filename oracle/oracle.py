@@ -184,3 +184,106 @@ def pair_eval(grid: Grid, pts, E_A, phi_A, E_B, phi_B, params: Params, want_deri
                             _dp(_f64(phi_B)), ctypes.byref(prm), int(want_deriv), _dp(fm), _dp(Km), _dp(Dm),
                             ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
     return fm, Km.reshape(12, 12), Dm.reshape(12, 12), ids[:n].copy()
+
+
+# --------------------------------------------------------------------------- BDF1 of one translational mover
+
+class _Mover(ctypes.Structure):
+    _fields_ = [("mass", ctypes.c_double), ("inertia", ctypes.c_double * 6), ("E_pj0", ctypes.c_double * 16),
+                ("E_ji", ctypes.c_double * 16), ("gravity", ctypes.c_double * 3), ("h", ctypes.c_double),
+                ("f_ext", ctypes.c_double * 6), ("joint_stiffness", ctypes.c_double),
+                ("joint_damping", ctypes.c_double), ("q_rest", ctypes.c_double * 3)]
+
+
+class _Pair(ctypes.Structure):
+    _fields_ = [("grid", ctypes.POINTER(_Grid)), ("pts", ctypes.POINTER(ctypes.c_double)), ("n_pts", ctypes.c_int),
+                ("mover_is_contact", ctypes.c_int), ("E_fixed", ctypes.c_double * 16), ("prm", _Params)]
+
+
+@dataclass
+class Mover:
+    """One body on a translational joint (Body::_mass/_Inertia/_E_ji, Joint::_E_pj_0, options)."""
+    mass: float
+    inertia: np.ndarray
+    E_ji: np.ndarray
+    E_pj0: np.ndarray = None
+    gravity: tuple = (0.0, 0.0, -9.8)
+    h: float = 5e-3
+    f_ext: np.ndarray = None
+    joint_stiffness: float = 0.0
+    joint_damping: float = 0.0
+
+    def _c(self):
+        E_pj0 = np.eye(4) if self.E_pj0 is None else self.E_pj0
+        f = np.zeros(6) if self.f_ext is None else self.f_ext
+        return _Mover(float(self.mass), (ctypes.c_double * 6)(*_f64(self.inertia)),
+                      (ctypes.c_double * 16)(*_f64(E_pj0).ravel()), (ctypes.c_double * 16)(*_f64(self.E_ji).ravel()),
+                      (ctypes.c_double * 3)(*self.gravity), float(self.h), (ctypes.c_double * 6)(*_f64(f)),
+                      float(self.joint_stiffness), float(self.joint_damping), (ctypes.c_double * 3)(0, 0, 0))
+
+
+@dataclass
+class ScenePair:
+    """One contact of the mover with a fixed body (grid of the SDF body, points of the contact body)."""
+    grid: Grid
+    pts: np.ndarray
+    mover_is_contact: bool
+    E_fixed: np.ndarray
+    params: Params
+
+
+def _lib_sim():
+    L = lib()
+    if not hasattr(L, "_sim_ready"):
+        P = ctypes.POINTER
+        d = ctypes.c_double
+        L.orc_bdf1_step.restype = ctypes.c_int
+        L.orc_bdf1_step.argtypes = [P(_Mover), P(_Pair), ctypes.c_int, P(d), P(d), P(ctypes.c_int), P(ctypes.c_int)]
+        L.orc_bdf1_eval.restype = None
+        L.orc_bdf1_eval.argtypes = [P(_Mover), P(_Pair), ctypes.c_int, P(d), P(d), P(d), P(d), P(d)]
+        L._sim_ready = True
+    return L
+
+
+def _pairs_c(pairs):
+    keep = []
+    arr = (_Pair * max(1, len(pairs)))()
+    for k, sp in enumerate(pairs):
+        g = sp.grid._c()
+        p = _f64(sp.pts).reshape(-1, 3)
+        keep += [g, p, sp.grid]
+        arr[k] = _Pair(ctypes.pointer(g), _dp(p), len(p), int(bool(sp.mover_is_contact)),
+                       (ctypes.c_double * 16)(*_f64(sp.E_fixed).ravel()), sp.params._c())
+    return arr, keep
+
+
+def bdf1_steps(mover: Mover, pairs, q, qdot, steps=1):
+    """Simulation::forward with BDF1 (Simulation.cpp:914-990, 1248-1270) for one translational mover:
+    returns (q_his[steps+1, 3], qdot_his, converged[steps], iters[steps], evals[steps])."""
+    L = _lib_sim()
+    m = mover._c()
+    arr, keep = _pairs_c(pairs)
+    q = _f64(q).copy()
+    qd = _f64(qdot).copy()
+    qs, qds, conv, its, evs = [q.copy()], [qd.copy()], [], [], []
+    it, ev = ctypes.c_int(), ctypes.c_int()
+    for _ in range(steps):
+        c = L.orc_bdf1_step(ctypes.byref(m), arr, len(pairs), _dp(q), _dp(qd), ctypes.byref(it), ctypes.byref(ev))
+        qs.append(q.copy())
+        qds.append(qd.copy())
+        conv.append(bool(c))
+        its.append(it.value)
+        evs.append(ev.value)
+    return np.array(qs), np.array(qds), np.array(conv), np.array(its), np.array(evs)
+
+
+def bdf1_eval(mover: Mover, pairs, q0, qdot0, q1, want_H=True):
+    """g and H of BDF1 at q1 (Simulation::evaluate_g_with_derivatives_BDF1, Simulation.cpp:1094-1165)."""
+    L = _lib_sim()
+    m = mover._c()
+    arr, keep = _pairs_c(pairs)
+    g = np.zeros(3)
+    H = np.zeros(9)
+    L.orc_bdf1_eval(ctypes.byref(m), arr, len(pairs), _dp(_f64(q0)), _dp(_f64(qdot0)), _dp(_f64(q1)), _dp(g),
+                    _dp(H) if want_H else None)
+    return g, H.reshape(3, 3)

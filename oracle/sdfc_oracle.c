@@ -802,3 +802,178 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
     if (own) free(ids);
     return n_active;
 }
+
+/* ------------------------------------------------------------------ BDF1 of one translational mover */
+
+/* Joint::update (Q = [I q; 0 1], E_pj = E_pj0 Q; JointTranslational.cpp:9-40,
+ * Joint.cpp) then Body::update (E_0i = E_0j E_ji, phi = Ad(E_ij) S_j qdot;
+ * Body.cpp:138-156).  For the translational joint S_j = [0; I], so
+ * phi = (0, R_ji^T qdot). */
+void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, double* E0i, double* phi) {
+    double Q[16] = {1, 0, 0, q[0], 0, 1, 0, q[1], 0, 0, 1, q[2], 0, 0, 0, 1};
+    double E0j[16];
+    mm(m->E_pj0, Q, E0j, 4, 4, 4);
+    mm(E0j, m->E_ji, E0i, 4, 4, 4);
+    double Rji[9], pji[3];
+    pose_split(m->E_ji, Rji, pji);
+    double v[3];
+    m3t_vec(Rji, qdot, v);
+    phi[0] = phi[1] = phi[2] = 0.0;
+    phi[3] = v[0];
+    phi[4] = v[1];
+    phi[5] = v[2];
+}
+
+/* Simulation::evaluate_g_BDF1 / evaluate_g_with_derivatives_BDF1 (Simulation.cpp:1081-1165)
+ * with Simulation::computeMatrices (:379-503) specialised to one translational mover:
+ * J = Ad(E_ij) S_j = [0; R_ji^T] is constant, so Jdot = dJ/dq = 0, M = J^T Mm J,
+ * f = J^T fm + fr, K = J^T Km J + Kr, D = J^T Dm J + Dr.  fm is the mover's gravity
+ * and external force (Body::computeMaximalForce, Body.cpp:247-271; its Coriolis term
+ * only has angular rows, which J^T drops) plus every contact's mover block. */
+void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0, const double* qdot0,
+                   const double* q1, double* g, double* H) {
+    const double h = m->h;
+    double qd1[3], E0i[16], phi[6], R0i[9], p0i[3], Rji[9], pji[3];
+    for (int k = 0; k < 3; ++k) qd1[k] = (q1[k] - q0[k]) / h;
+    orc_mover_pose(m, q1, qd1, E0i, phi);
+    pose_split(E0i, R0i, p0i);
+    pose_split(m->E_ji, Rji, pji);
+    /* linear rows of fm for the mover: gravity + external */
+    double fl[3], Kll[9] = {0}, Dll[9] = {0}, mg[3], ft[3];
+    for (int k = 0; k < 3; ++k) mg[k] = m->mass * m->gravity[k];
+    m3t_vec(R0i, mg, fl);
+    m3t_vec(R0i, m->f_ext + 3, ft);
+    for (int k = 0; k < 3; ++k) fl[k] += m->inertia[3 + k] * ft[k];
+    const double zero6[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < n_pairs; ++c) {
+        const orc_pair* P = pairs + c;
+        double fm[12], Km[144], Dm[144];
+        const double *EA, *phiA, *EB, *phiB;
+        if (P->mover_is_contact) {
+            EA = E0i; phiA = phi; EB = P->E_fixed; phiB = zero6;
+        } else {
+            EA = P->E_fixed; phiA = zero6; EB = E0i; phiB = phi;
+        }
+        orc_pair_eval(P->grid, P->pts, P->n_pts, EA, phiA, EB, phiB, &P->prm, H != NULL, fm, Km, Dm, NULL);
+        const int o = P->mover_is_contact ? 0 : 6;
+        for (int r = 0; r < 3; ++r) {
+            fl[r] += fm[o + 3 + r];
+            if (H)
+                for (int s = 0; s < 3; ++s) {
+                    Kll[3 * r + s] += Km[(o + 3 + r) * 12 + o + 3 + s];
+                    Dll[3 * r + s] += Dm[(o + 3 + r) * 12 + o + 3 + s];
+                }
+        }
+    }
+    /* reduced: f = R_ji fl + fr; M = R_ji diag(m) R_ji^T */
+    double f[3], M[9], Md[9] = {0};
+    m3_vec(Rji, fl, f);
+    for (int k = 0; k < 3; ++k) f[k] += -m->joint_stiffness * (q1[k] - m->q_rest[k]) - m->joint_damping * qd1[k];
+    for (int k = 0; k < 3; ++k) Md[4 * k] = m->inertia[3 + k];
+    double RjiT[9], T[9];
+    m3_transpose(Rji, RjiT);
+    m3_mul(Rji, Md, T);
+    m3_mul(T, RjiT, M);
+    double dq[3];
+    for (int k = 0; k < 3; ++k) dq[k] = q1[k] - q0[k] - h * qdot0[k];
+    double Mdq[3];
+    m3_vec(M, dq, Mdq);
+    for (int k = 0; k < 3; ++k) g[k] = Mdq[k] - h * h * f[k];
+    if (H) {
+        double K[9], D[9];
+        m3_mul(Rji, Kll, T);
+        m3_mul(T, RjiT, K);
+        m3_mul(Rji, Dll, T);
+        m3_mul(T, RjiT, D);
+        for (int k = 0; k < 3; ++k) {
+            K[4 * k] -= m->joint_stiffness;
+            D[4 * k] -= m->joint_damping;
+        }
+        for (int k = 0; k < 9; ++k) H[k] = M[k] - h * h * K[k] - h * D[k];
+    }
+}
+
+/* 3x3 solve by Gaussian elimination with partial pivoting (the algorithm of Eigen's
+ * PartialPivLU used by Simulation::newton, Simulation.cpp:1028). */
+static void solve3(const double* A_in, const double* b_in, double* x) {
+    double A[9], b[3];
+    memcpy(A, A_in, sizeof A);
+    memcpy(b, b_in, sizeof b);
+    for (int c = 0; c < 3; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 3; ++r)
+            if (fabs(A[3 * r + c]) > fabs(A[3 * p + c])) p = r;
+        if (p != c) {
+            for (int k = 0; k < 3; ++k) {
+                double t = A[3 * c + k];
+                A[3 * c + k] = A[3 * p + k];
+                A[3 * p + k] = t;
+            }
+            double t = b[c];
+            b[c] = b[p];
+            b[p] = t;
+        }
+        for (int r = c + 1; r < 3; ++r) {
+            double l = A[3 * r + c] / A[3 * c + c];
+            for (int k = c; k < 3; ++k) A[3 * r + k] -= l * A[3 * c + k];
+            b[r] -= l * b[c];
+        }
+    }
+    for (int r = 2; r >= 0; --r) {
+        double s = b[r];
+        for (int k = r + 1; k < 3; ++k) s -= A[3 * r + k] * x[k];
+        x[r] = s / A[3 * r + r];
+    }
+}
+
+/* Simulation::integration_BDF1 (Simulation.cpp:1248-1270) with Simulation::newton
+ * (:999-1079): tolerance 1e-8 on |g|, at most max(20 ndof, 100) iterations, backtracking
+ * line search halving alpha up to 20 times, 3 consecutive line-search failures stop. */
+int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double* q, double* qdot, int* iters,
+                  int* evals) {
+    const double h = m->h, tol = 1e-8;
+    const int max_iter = 100, max_ls = 20, max_strike = 3;
+    double q0[3], qd0[3], x[3];
+    for (int k = 0; k < 3; ++k) {
+        q0[k] = q[k];
+        qd0[k] = qdot[k];
+        x[k] = q0[k] + h * qd0[k];
+    }
+    int converged = 0, strike = 0, it = 0, ev = 0;
+    for (; it < max_iter; ++it) {
+        double g[3], H[9], dx[3], mg[3];
+        orc_bdf1_eval(m, pairs, n_pairs, q0, qd0, x, g, H);
+        ++ev;
+        for (int k = 0; k < 3; ++k) mg[k] = -g[k];
+        solve3(H, mg, dx);
+        const double gnorm = norm3(g);
+        double alpha = 1.0, gn[3] = {0, 0, 0};
+        int ok = 0;
+        for (int trial = 0; trial < max_ls; ++trial, alpha *= 0.5) {
+            double xt[3] = {x[0] + alpha * dx[0], x[1] + alpha * dx[1], x[2] + alpha * dx[2]};
+            orc_bdf1_eval(m, pairs, n_pairs, q0, qd0, xt, gn, NULL);
+            ++ev;
+            if (norm3(gn) < gnorm) {
+                ok = 1;
+                break;
+            }
+        }
+        if (ok) {
+            strike = 0;
+        } else if (++strike >= max_strike) {
+            break;
+        }
+        for (int k = 0; k < 3; ++k) x[k] = x[k] + alpha * dx[k];
+        if (norm3(gn) < tol) {
+            converged = 1;
+            break;
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        qdot[k] = (x[k] - q0[k]) / h;
+        q[k] = x[k];
+    }
+    if (iters) *iters = it + (converged ? 1 : 0);
+    if (evals) *evals = ev;
+    return converged;
+}

@@ -55,6 +55,38 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
                   const double* E_B, const double* phi_B, const orc_params* prm, int want_deriv, double* fm,
                   double* Km, double* Dm, int* ids);
 
+/* ---------------------------------------------------------------- one moving body, BDF1 */
+
+/* The moving part of the planner's scene (examples/run_joint_plan.py:140-178): one
+ * body on a translational joint (3 dof) attached to the world, every other part
+ * fixed.  Fields are the reference's: Body::_mass, Body::_Inertia, Joint::_E_pj_0,
+ * Body::_E_ji, Simulation option gravity and timestep, Body::_f_external (world
+ * frame), Joint::_Kr/_Dr/_q_rest. */
+typedef struct {
+    double mass, inertia[6], E_pj0[16], E_ji[16], gravity[3], h, f_ext[6];
+    double joint_stiffness, joint_damping, q_rest[3];
+} orc_mover;
+
+/* One ForceGeneralSDFContact of the scene: the mover against one fixed body. */
+typedef struct {
+    const orc_grid* grid; /* the SDF body's grid */
+    const double* pts;    /* the contact body's points (n x 3, body frame) */
+    int n_pts;
+    int mover_is_contact; /* 1: mover's points vs the fixed body's grid; 0: the reverse */
+    double E_fixed[16];   /* pose of the fixed body */
+    orc_params prm;
+} orc_pair;
+
+/* Mover pose and body twist for joint state (q, qdot) (Joint::update + Body::update). */
+void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, double* E0i, double* phi);
+/* g and H of BDF1 at q1 (Simulation::evaluate_g[_with_derivatives]_BDF1), H may be NULL. */
+void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0, const double* qdot0,
+                   const double* q1, double* g, double* H);
+/* One implicit-Euler step (Simulation::integration_BDF1 + newton); updates q, qdot.
+ * Returns 1 if Newton converged.  iters / evals may be NULL. */
+int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double* q, double* qdot, int* iters,
+                  int* evals);
+
 #ifdef __cplusplus
 }
 #endif

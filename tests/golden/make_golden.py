@@ -9,6 +9,9 @@ and stores inputs and outputs as compressed .npz files:
                   of poses, velocities and coefficient variants: fm, Km, Dm, active ids
   collision.npz   BodySDFObj::collision with derivatives (simulation/redmax/Body/BodySDFObj.cpp:278-377)
                   at random points
+  sim_trans.npz   Simulation::forward with BDF1 (simulation/redmax/Simulation.cpp:914-1079, 1248-1270)
+                  of a peg on a translational joint against a fixed socket: the scene and the
+                  reference's joint trajectory and Newton convergence flags
 
 Usage (where the reference sources are present):
     make -C oracle/ref -j8 && python tests/golden/make_golden.py
@@ -108,5 +111,56 @@ def main():
     print("active counts:", rows["n_active"])
 
 
+def f32(x):
+    return float(np.float32(x))
+
+
+def make_sim_fixture(steps=40):
+    """A 3-dof peg (box mesh for its mass properties, peg points as its contact points) on a
+    translational joint, pushed into a fixed socket; both scene files use the planner's layout."""
+    import tempfile
+    wd = tempfile.mkdtemp(prefix="golden_sim_")
+    Va, Fa = refsim.box_mesh((0.3, 0.25, 0.9))
+    Vb, Fb = refsim.box_mesh((1.0, 1.0, 1.0))
+    refsim.write_obj(os.path.join(wd, "a.obj"), Va, Fa)
+    refsim.write_obj(os.path.join(wd, "b.obj"), Vb, Fb)
+    kn, kt, mu, kd, h, gravity = 1e5, 1e3, 0.3, 1e3, 5e-3, (0.0, 0.0, -9.8)
+    xml = refsim.two_body_xml("a.obj", "b.obj", joint_a="translational", kn=kn, kt=kt, mu=mu, damping=kd,
+                              timestep=h, gravity=gravity, col_th=COL_TH)
+    sim = refsim.RefSim(xml, wd)
+    mA, IA, EjiA, E0iA = sim.mass_props("A")
+    _, _, _, E0iB = sim.mass_props("B")
+    grid = W.socket_grid(48, dtype=np.float32)
+    mn, mx, dx = grid.min_box, grid.max_box, grid.dx
+    n = grid.values.shape[0]
+    ax = [mn[a] + dx[a] * np.arange(n) for a in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    world = np.stack([X, Y, Z], -1) @ E0iB[:3, :3].T + E0iB[:3, 3]  # grid nodes are in B's body frame
+    vals = W.socket_sdf(world).astype(np.float32).astype(np.float64)
+    sim.set_sdf("B", vals, mn, mx, dx, COL_TH)
+    pw = W.peg_points(3000, seed=2)
+    pts = (pw - E0iA[:3, 3]) @ E0iA[:3, :3]  # into A's body frame at q = 0
+    sim.set_contact_points("A", pts)
+    q0, qd0 = np.array([0.012, 0.0, 0.0]), np.array([0.5, 0.0, -0.2])
+    F = np.array([0.0, 0.0, 0.0, 2.0, 0.5, 1.0])
+    sim.set_state_init(q0, qd0)
+    sim.reset(False)
+    sim.set_external_force("A", F)
+    qs, qds, conv = [q0], [qd0], []
+    for _ in range(steps):
+        sim.forward(1)
+        q, qd = sim.state()
+        qs.append(q)
+        qds.append(qd)
+        conv.append(sim.is_converged())
+    np.savez_compressed(os.path.join(HERE, "sim_trans.npz"), grid=vals, min_box=mn, max_box=mx, dx=dx,
+                        col_th=COL_TH, points=pts, mass=mA, inertia=IA, E_ji=EjiA, E_fixed=E0iB,
+                        params=np.array([f32(kn), f32(kt), f32(mu), f32(kd), 1.0, 1.0]), h=f32(h),
+                        gravity=np.array(gravity), f_ext=F, q0=q0, qdot0=qd0, q=np.array(qs), qdot=np.array(qds),
+                        converged=np.array(conv))
+    print("sim trajectory: final q", qs[-1], "all converged", all(conv))
+
+
 if __name__ == "__main__":
     main()
+    make_sim_fixture()
