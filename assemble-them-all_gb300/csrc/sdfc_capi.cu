@@ -9,79 +9,25 @@
 #include <vector>
 
 #include "sdfc.h"
+#include "sdfc_internal.h"
 #include "sdfc_kernels.cuh"
 
 using sdfc::GridDesc;
 using sdfc::InstanceDesc;
 using sdfc::PointsDesc;
+using sdfc_impl::dev_alloc;
+using sdfc_impl::fail;
+using sdfc_impl::free_batch;
+using sdfc_impl::use_device;
 
-namespace {
+#define CUDA_TRY(ctx, call) SDFC_CUDA_TRY(ctx, call)
 
-struct DeviceBuffer {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
-
-}  // namespace
-
-struct sdfc_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    std::vector<GridDesc> grids;     // host copies of the descriptors
-    std::vector<PointsDesc> points;
-    std::vector<void*> allocations;  // every device allocation owned by the context
-    GridDesc* d_grids = nullptr;
-    PointsDesc* d_points = nullptr;
-    int grid_cap = 0, points_cap = 0;
-    int deriv_mode = SDFC_DERIV_ANALYTIC;
-    int precision = SDFC_PRECISION_FP64;
-    std::vector<std::vector<int>> point_order;  // per point set: stored index -> caller's index
-    sdfc_batch* single = nullptr;     // cached one-instance batch of sdfc_evaluate
-    int single_points = -1, single_grid = -1;
-    std::vector<sdfc_batch*> batches;  // live batches, destroyed with the context
-};
-
-struct sdfc_batch {
-    sdfc_context* ctx = nullptr;
-    int n = 0;
-    int total_tiles = 0;
-    int deriv_mode = SDFC_DERIV_ANALYTIC;
-    int precision = SDFC_PRECISION_FP64;
-    std::vector<InstanceDesc> inst;
-    InstanceDesc* d_inst = nullptr;
-    int* d_tile_inst = nullptr;
-    int* d_ids = nullptr;
-    int* d_tile_count = nullptr;
-    int* d_tile_queue = nullptr;
-    sdfc::Prefilter* d_prefilter = nullptr;
-    double* d_partial = nullptr;
-    unsigned long long* d_recheck = nullptr;
-    int* d_squeue = nullptr;
-    int* d_squeue_count = nullptr;
-    // staging of the host-array entry points
-    double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
-    double* d_out = nullptr;  // n x 300: fm | Km | Dm
-    int* d_int = nullptr;     // n x 2: n_active | status
-    double* h_in = nullptr;   // pinned
-    double* h_out = nullptr;  // pinned
-    int* h_int = nullptr;     // pinned
-    bool timing = false;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-};
-
-namespace {
+namespace sdfc_impl {
 
 int fail(sdfc_context* ctx, int code, const std::string& msg) {
     if (ctx) ctx->err = msg;
     return code;
 }
-
-#define CUDA_TRY(ctx, call)                                                                              \
-    do {                                                                                                 \
-        cudaError_t e_ = (call);                                                                         \
-        if (e_ != cudaSuccess) return fail((ctx), SDFC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
 
 int dev_alloc(sdfc_context* ctx, void** p, size_t bytes) {
     if (bytes == 0) bytes = 16;
@@ -92,22 +38,6 @@ int dev_alloc(sdfc_context* ctx, void** p, size_t bytes) {
 
 int use_device(sdfc_context* ctx) {
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    return SDFC_OK;
-}
-
-template <class T>
-int sync_table(sdfc_context* ctx, std::vector<T>& host, T** d_table, int* cap) {
-    if ((int)host.size() > *cap) {
-        int ncap = std::max(64, *cap * 2);
-        while (ncap < (int)host.size()) ncap *= 2;
-        void* p = nullptr;
-        int rc = dev_alloc(ctx, &p, sizeof(T) * ncap);
-        if (rc) return rc;
-        if (*d_table) cudaFree(*d_table);
-        *d_table = (T*)p;
-        *cap = ncap;
-    }
-    CUDA_TRY(ctx, cudaMemcpy(*d_table, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice));
     return SDFC_OK;
 }
 
@@ -134,25 +64,60 @@ void free_batch(sdfc_batch* b) {
     delete b;
 }
 
-int run_batch(sdfc_batch* b, const double* EA, const double* phiA, const double* EB, const double* phiB,
-              const double* prm, bool deriv, double* fm, double* Km, double* Dm, int* n_active, int* status,
+int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
               cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
-    sdfc::BatchInputs in{EA, phiA, EB, phiB, prm};
-    sdfc::BatchOutputs out{fm, Km, Dm, n_active, status};
     sdfc::BatchScratch sc{b->d_prefilter, b->d_ids,     b->d_tile_count,  b->d_tile_queue,
                           b->d_partial,   b->d_recheck, b->d_squeue,      b->d_squeue_count};
+    const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
+    const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     if (b->timing) cudaEventRecord(b->ev[0], stream);
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream);
     if (b->timing) cudaEventRecord(b->ev[1], stream);
-    sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, deriv,
-                       b->deriv_mode == SDFC_DERIV_STENCIL,
-                       b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64, stream);
+    if (in.mode) {
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, true, stencil, prec, stream);
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, false, stencil, prec, stream);
+    } else {
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, deriv, stencil, prec, stream);
+    }
     if (b->timing) cudaEventRecord(b->ev[2], stream);
-    sdfc::launch_finalize(b->d_inst, b->n, sc, deriv, out, stream);
+    if (in.mode) {
+        sdfc::launch_finalize(b->d_inst, b->n, sc, true, out, stream, in.mode, true);
+        sdfc::launch_finalize(b->d_inst, b->n, sc, false, out, stream, in.mode, false);
+    } else {
+        sdfc::launch_finalize(b->d_inst, b->n, sc, deriv, out, stream);
+    }
     if (b->timing) cudaEventRecord(b->ev[3], stream);
     CUDA_TRY(ctx, cudaGetLastError());
     return SDFC_OK;
+}
+
+}  // namespace sdfc_impl
+
+namespace {
+
+template <class T>
+int sync_table(sdfc_context* ctx, std::vector<T>& host, T** d_table, int* cap) {
+    if ((int)host.size() > *cap) {
+        int ncap = std::max(64, *cap * 2);
+        while (ncap < (int)host.size()) ncap *= 2;
+        void* p = nullptr;
+        int rc = dev_alloc(ctx, &p, sizeof(T) * ncap);
+        if (rc) return rc;
+        if (*d_table) cudaFree(*d_table);
+        *d_table = (T*)p;
+        *cap = ncap;
+    }
+    CUDA_TRY(ctx, cudaMemcpy(*d_table, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice));
+    return SDFC_OK;
+}
+
+int run_batch(sdfc_batch* b, const double* EA, const double* phiA, const double* EB, const double* phiB,
+              const double* prm, bool deriv, double* fm, double* Km, double* Dm, int* n_active, int* status,
+              cudaStream_t stream) {
+    sdfc::BatchInputs in{EA, phiA, EB, phiB, prm};
+    sdfc::BatchOutputs out{fm, Km, Dm, n_active, status};
+    return sdfc_impl::run_batch(b, in, deriv, out, stream);
 }
 
 bool all_finite(const double* v, size_t n) {
@@ -162,6 +127,73 @@ bool all_finite(const double* v, size_t n) {
 }
 
 }  // namespace
+
+int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** out) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (n <= 0 || !points || !grids || !out) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_create: bad argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    auto* b = new sdfc_batch();
+    b->ctx = ctx;
+    b->n = n;
+    b->deriv_mode = ctx->deriv_mode;
+    b->precision = ctx->precision;
+    b->inst.resize(n);
+    std::vector<int> tile_inst;
+    int tiles = 0;
+    for (int k = 0; k < n; ++k) {
+        if (points[k] < 0 || points[k] >= (int)ctx->points.size() || grids[k] < 0 || grids[k] >= (int)ctx->grids.size()) {
+            delete b;
+            return fail(ctx, SDFC_ERR_NOT_FOUND, "batch_create: unknown point-set or grid handle");
+        }
+        int np = ctx->points[points[k]].n;
+        int nt = (np + sdfc::kTile - 1) / sdfc::kTile;
+        if (nt > sdfc::kMaxTilesPerInstance) {
+            delete b;
+            return fail(ctx, SDFC_ERR_CAPACITY, "batch_create: point set larger than kTile*kMaxTilesPerInstance");
+        }
+        b->inst[k] = InstanceDesc{points[k], grids[k], tiles, nt};
+        for (int t = 0; t < nt; ++t) tile_inst.push_back(k);
+        tiles += nt;
+    }
+    b->total_tiles = tiles;
+    auto alloc = [&](void** p, size_t bytes) { return dev_alloc(ctx, p, bytes); };
+    if ((rc = alloc((void**)&b->d_inst, sizeof(InstanceDesc) * n)) ||
+        (rc = alloc((void**)&b->d_tile_inst, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_ids, sizeof(int) * (size_t)std::max(tiles, 1) * sdfc::kTile)) ||
+        (rc = alloc((void**)&b->d_tile_count, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_tile_queue, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
+        (rc = alloc((void**)&b->d_squeue, sizeof(int) * sdfc::squeue_capacity(n, tiles))) ||
+        (rc = alloc((void**)&b->d_squeue_count, sizeof(int) * (size_t)n * sdfc::kSlots)) ||
+        (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
+        (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
+        (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
+        (rc = alloc((void**)&b->d_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv)) ||
+        (rc = alloc((void**)&b->d_int, sizeof(int) * (size_t)n * 2))) {
+        free_batch(b);
+        return rc;
+    }
+    if (cudaMallocHost((void**)&b->h_in, sizeof(double) * (size_t)n * 50) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_int, sizeof(int) * (size_t)n * 2) != cudaSuccess) {
+        free_batch(b);
+        return fail(ctx, SDFC_ERR_CUDA, "batch_create: cudaMallocHost failed");
+    }
+    cudaError_t e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && tiles > 0)
+        e = cudaMemcpy(b->d_tile_inst, tile_inst.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_recheck, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_tile_count, 0, sizeof(int) * std::max(tiles, 1));
+    if (e == cudaSuccess) e = cudaMemset(b->d_tile_queue, 0, sizeof(int) * std::max(tiles, 1));
+    if (e == cudaSuccess) e = cudaMemset(b->d_squeue_count, 0, sizeof(int) * (size_t)n * sdfc::kSlots);
+    if (e != cudaSuccess) {
+        free_batch(b);
+        return fail(ctx, SDFC_ERR_CUDA, std::string("batch_create: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return SDFC_OK;
+}
 
 extern "C" {
 
@@ -184,6 +216,7 @@ void sdfc_destroy(sdfc_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (sdfc_sim* s : ctx->sims) sdfc_impl::free_sim(s);
     for (sdfc_batch* b : ctx->batches) free_batch(b);
     free_batch(ctx->single);
     for (void* p : ctx->allocations) cudaFree(p);
@@ -412,75 +445,9 @@ int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage,
     return SDFC_OK;
 }
 
-static int batch_create_impl(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** out) {
-    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
-    if (n <= 0 || !points || !grids || !out) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_create: bad argument");
-    int rc = use_device(ctx);
-    if (rc) return rc;
-    auto* b = new sdfc_batch();
-    b->ctx = ctx;
-    b->n = n;
-    b->deriv_mode = ctx->deriv_mode;
-    b->precision = ctx->precision;
-    b->inst.resize(n);
-    std::vector<int> tile_inst;
-    int tiles = 0;
-    for (int k = 0; k < n; ++k) {
-        if (points[k] < 0 || points[k] >= (int)ctx->points.size() || grids[k] < 0 || grids[k] >= (int)ctx->grids.size()) {
-            delete b;
-            return fail(ctx, SDFC_ERR_NOT_FOUND, "batch_create: unknown point-set or grid handle");
-        }
-        int np = ctx->points[points[k]].n;
-        int nt = (np + sdfc::kTile - 1) / sdfc::kTile;
-        if (nt > sdfc::kMaxTilesPerInstance) {
-            delete b;
-            return fail(ctx, SDFC_ERR_CAPACITY, "batch_create: point set larger than kTile*kMaxTilesPerInstance");
-        }
-        b->inst[k] = InstanceDesc{points[k], grids[k], tiles, nt};
-        for (int t = 0; t < nt; ++t) tile_inst.push_back(k);
-        tiles += nt;
-    }
-    b->total_tiles = tiles;
-    auto alloc = [&](void** p, size_t bytes) { return dev_alloc(ctx, p, bytes); };
-    if ((rc = alloc((void**)&b->d_inst, sizeof(InstanceDesc) * n)) ||
-        (rc = alloc((void**)&b->d_tile_inst, sizeof(int) * std::max(tiles, 1))) ||
-        (rc = alloc((void**)&b->d_ids, sizeof(int) * (size_t)std::max(tiles, 1) * sdfc::kTile)) ||
-        (rc = alloc((void**)&b->d_tile_count, sizeof(int) * std::max(tiles, 1))) ||
-        (rc = alloc((void**)&b->d_tile_queue, sizeof(int) * std::max(tiles, 1))) ||
-        (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
-        (rc = alloc((void**)&b->d_squeue, sizeof(int) * sdfc::squeue_capacity(n, tiles))) ||
-        (rc = alloc((void**)&b->d_squeue_count, sizeof(int) * (size_t)n * sdfc::kSlots)) ||
-        (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
-        (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
-        (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
-        (rc = alloc((void**)&b->d_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv)) ||
-        (rc = alloc((void**)&b->d_int, sizeof(int) * (size_t)n * 2))) {
-        free_batch(b);
-        return rc;
-    }
-    if (cudaMallocHost((void**)&b->h_in, sizeof(double) * (size_t)n * 50) != cudaSuccess ||
-        cudaMallocHost((void**)&b->h_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv) != cudaSuccess ||
-        cudaMallocHost((void**)&b->h_int, sizeof(int) * (size_t)n * 2) != cudaSuccess) {
-        free_batch(b);
-        return fail(ctx, SDFC_ERR_CUDA, "batch_create: cudaMallocHost failed");
-    }
-    cudaError_t e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && tiles > 0)
-        e = cudaMemcpy(b->d_tile_inst, tile_inst.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(b->d_recheck, 0, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMemset(b->d_tile_count, 0, sizeof(int) * std::max(tiles, 1));
-    if (e == cudaSuccess) e = cudaMemset(b->d_tile_queue, 0, sizeof(int) * std::max(tiles, 1));
-    if (e == cudaSuccess) e = cudaMemset(b->d_squeue_count, 0, sizeof(int) * (size_t)n * sdfc::kSlots);
-    if (e != cudaSuccess) {
-        free_batch(b);
-        return fail(ctx, SDFC_ERR_CUDA, std::string("batch_create: ") + cudaGetErrorString(e));
-    }
-    *out = b;
-    return SDFC_OK;
-}
 
 int sdfc_batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** out) {
-    int rc = batch_create_impl(ctx, n, points, grids, out);
+    int rc = sdfc_impl::batch_create(ctx, n, points, grids, out);
     if (rc == SDFC_OK) ctx->batches.push_back(*out);
     return rc;
 }
@@ -598,7 +565,7 @@ int sdfc_evaluate(sdfc_context* ctx, int points, int grid, const double* E_A, co
         ctx->single = nullptr;
         ctx->single_points = ctx->single_grid = -1;
         sdfc_batch* b = nullptr;
-        rc = batch_create_impl(ctx, 1, &points, &grid, &b);
+        rc = sdfc_impl::batch_create(ctx, 1, &points, &grid, &b);
         if (rc) return rc;
         ctx->single = b;
         ctx->single_points = points;

@@ -1,0 +1,79 @@
+// Internal structures of libsdfcontact shared by its C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "sdfc.h"
+#include "sdfc_kernels.cuh"
+
+struct sdfc_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<sdfc::GridDesc> grids;  // host copies of the descriptors
+    std::vector<sdfc::PointsDesc> points;
+    std::vector<void*> allocations;  // every device allocation owned by the context
+    sdfc::GridDesc* d_grids = nullptr;
+    sdfc::PointsDesc* d_points = nullptr;
+    int grid_cap = 0, points_cap = 0;
+    int deriv_mode = SDFC_DERIV_ANALYTIC;
+    int precision = SDFC_PRECISION_FP64;
+    std::vector<std::vector<int>> point_order;  // per point set: stored index -> caller's index
+    sdfc_batch* single = nullptr;     // cached one-instance batch of sdfc_evaluate
+    int single_points = -1, single_grid = -1;
+    std::vector<sdfc_batch*> batches;  // live batches, destroyed with the context
+    std::vector<sdfc_sim*> sims;       // live simulations, destroyed with the context
+};
+
+struct sdfc_batch {
+    sdfc_context* ctx = nullptr;
+    int n = 0;
+    int total_tiles = 0;
+    int deriv_mode = SDFC_DERIV_ANALYTIC;
+    int precision = SDFC_PRECISION_FP64;
+    std::vector<sdfc::InstanceDesc> inst;
+    sdfc::InstanceDesc* d_inst = nullptr;
+    int* d_tile_inst = nullptr;
+    int* d_ids = nullptr;
+    int* d_tile_count = nullptr;
+    int* d_tile_queue = nullptr;
+    sdfc::Prefilter* d_prefilter = nullptr;
+    double* d_partial = nullptr;
+    unsigned long long* d_recheck = nullptr;
+    int* d_squeue = nullptr;
+    int* d_squeue_count = nullptr;
+    // staging of the host-array entry points
+    double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
+    double* d_out = nullptr;  // n x 300: fm | Km | Dm
+    int* d_int = nullptr;     // n x 2: n_active | status
+    double* h_in = nullptr;   // pinned
+    double* h_out = nullptr;  // pinned
+    int* h_int = nullptr;     // pinned
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace sdfc_impl {
+
+int fail(sdfc_context* ctx, int code, const std::string& msg);
+int dev_alloc(sdfc_context* ctx, void** p, size_t bytes);
+int use_device(sdfc_context* ctx);
+int batch_create(sdfc_context* ctx, int n, const int* points, const int* grids, sdfc_batch** out);
+void free_batch(sdfc_batch* b);
+void free_sim(sdfc_sim* s);
+// One evaluation of every instance (in.mode null) with `deriv`, or, with
+// in.mode set, each instance as it requests (0 skip, 1 value, 2 derivatives).
+int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
+              cudaStream_t stream);
+
+}  // namespace sdfc_impl
+
+#define SDFC_CUDA_TRY(ctx, call)                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return sdfc_impl::fail((ctx), SDFC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)

@@ -50,7 +50,7 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
                             const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
                             Prefilter* __restrict__ pref) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (in.mode && in.mode[i] == 0)) return;
     const InstanceDesc I = inst[i];
     Prefilter f;
     make_prefilter(grids[I.grid], points[I.points], load_pose(in.EA + 16 * (size_t)i), load_pose(in.EB + 16 * (size_t)i),
@@ -98,7 +98,8 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                                                                 const GridDesc* __restrict__ grids,
                                                                 const PointsDesc* __restrict__ points,
                                                                 int* __restrict__ ids, int* __restrict__ tile_count,
-                                                                int* __restrict__ tile_queue) {
+                                                                int* __restrict__ tile_queue,
+                                                                const int* __restrict__ mode) {
     __shared__ Prefilter f;
     __shared__ const float* gv;
     __shared__ const float* px;
@@ -108,6 +109,13 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
     const int t = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int i = tile_inst[t];
+    if (mode && mode[i] == 0) {  // instance not requested this time: its tiles are empty
+        if (tid == 0) {
+            tile_count[t] = 0;
+            tile_queue[t] = 0;
+        }
+        return;
+    }
     const InstanceDesc I = inst[i];
     if (tid < (int)(sizeof(Prefilter) / sizeof(float)))
         reinterpret_cast<float*>(&f)[tid] = reinterpret_cast<const float*>(pref + i)[tid];
@@ -354,6 +362,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     __shared__ PairState<T> S;
     __shared__ int wq[NW], qbase;
     const int i = blockIdx.y, s = blockIdx.x;
+    if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const InstanceDesc I = inst[i];
     if (warp == 0) {
@@ -484,9 +493,10 @@ __global__ void __launch_bounds__(128) stencil_kernel(const InstanceDesc* __rest
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_inst * kSlots) return;
+    const int i = q / kSlots, s = q % kSlots;
+    if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
     const int count = squeue_count[q];
     if (count == 0) return;
-    const int i = q / kSlots, s = q % kSlots;
     const InstanceDesc I = inst[i];
     const GridDesc g = grids[I.grid];
     const PointsDesc P = points[I.points];
@@ -508,11 +518,12 @@ __global__ void __launch_bounds__(128) stencil_kernel(const InstanceDesc* __rest
 
 template <bool DERIV>
 __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
-                                const double* __restrict__ partial, BatchOutputs out) {
+                                const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)n_inst * NV) return;
     const int i = (int)(idx / NV), k = (int)(idx % NV);
+    if (mode && mode[i] != (DERIV ? 2 : 1)) return;
     const double* p = partial + (size_t)i * kSlots * NV + k;
     double v = 0.0;
     for (int s = 0; s < kSlots; ++s) v += p[(size_t)s * NV];
@@ -561,7 +572,7 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
     prep_kernel<<<(n_inst + 127) / 128, 128, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter);
     if (total_tiles <= 0) return;
     detect_kernel<<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids, d_points,
-                                                              s.ids, s.tile_count, s.tile_queue);
+                                                              s.ids, s.tile_count, s.tile_queue, in.mode);
     recheck_kernel<<<total_tiles, 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points, s.ids, s.tile_count,
                                                    s.tile_queue, s.recheck);
 }
@@ -585,17 +596,17 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
 }
 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, const int* mode, bool zero_status) {
     if (n_inst <= 0) return;
-    zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out.status, n_inst);
+    if (zero_status) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out.status, n_inst);
     const int NV = deriv ? kOutDeriv : kOutValue;
     const size_t total = (size_t)n_inst * NV;
     const int threads = 256;
     const unsigned blocks = (unsigned)((total + threads - 1) / threads);
     if (deriv)
-        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out);
+        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode);
     else
-        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out);
+        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode);
 }
 
 }  // namespace sdfc

@@ -76,6 +76,9 @@ struct BatchInputs {
     const double* EB;    // n x 16
     const double* phiB;  // n x 6
     const double* prm;   // n x 6: kn, kt, mu, damping, scale, contact_scale
+    // optional per-instance request (null: every instance, with the launch's
+    // derivative flag): 0 skip, 1 value only, 2 with derivatives
+    const int* mode = nullptr;
 };
 
 struct BatchOutputs {
@@ -120,7 +123,10 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
                   cudaStream_t stream);
 
+// Zeroes the status words, then finalizes.  With in.mode set, only the
+// instances whose request matches `deriv` are finalized (zero_status = false
+// lets a second, value-only pass keep the first pass's status bits).
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
-                     cudaStream_t stream);
+                     cudaStream_t stream, const int* mode = nullptr, bool zero_status = true);
 
 }  // namespace sdfc

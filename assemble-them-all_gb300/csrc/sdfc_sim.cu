@@ -1,0 +1,530 @@
+// Batched implicit-Euler (BDF1) steps of planner scenes; see include/sdfc.h.
+//
+// Restates, per scene, redmax's Simulation::integration_BDF1 + Simulation::newton
+// (simulation/redmax/Simulation.cpp:999-1079, 1248-1270) with the reduced system of
+// Simulation::computeMatrices (:379-503) for one mover on a translational joint
+// (simulation/redmax/Joint/JointTranslational.cpp:9-40): J = Ad(E_ij) S_j = [0; R_ji^T]
+// is constant, so M = J^T Mm J, f = J^T fm + fr, K = J^T Km J + Kr, D = J^T Dm J + Dr.
+//
+// Every scene runs the reference's Newton iteration as a small state machine;
+// one "round" gives every unfinished scene exactly one force evaluation (with
+// derivatives at a Newton point, value-only at a line-search trial), so a
+// round is one batched evaluation of all contact pairs plus two tiny kernels:
+//   sim_pose_kernel    per pair: the mover's pose / twist at the scene's current
+//                      point, the pair's inputs and request (skip/value/derivative)
+//   (batched evaluation of every requested pair)
+//   sim_newton_kernel  per scene: g (and H), the 3x3 FP64 solve, line-search
+//                      bookkeeping, convergence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "sdfc_internal.h"
+
+using sdfc_impl::dev_alloc;
+using sdfc_impl::fail;
+using sdfc_impl::use_device;
+
+namespace {
+
+constexpr double kTol = 1e-8;     // Simulation.cpp:1008
+constexpr int kMaxLineSearch = 20;  // :1011
+constexpr int kMaxStrike = 3;     // :1014
+
+enum Phase : int { kNewton = 0, kLine = 1, kDone = 2 };
+
+struct MoverDev {
+    double mass, inertia[6], E_pj0[16], E_ji[16], gravity[3], h, Kr, Dr;
+    int max_iter;
+};
+
+struct SceneState {
+    double q0[3], qd0[3], x[3], dx[3], xt[3];
+    double gnorm, alpha;
+    int phase, iter, trial, strike, converged;
+};
+
+__device__ __forceinline__ void mat4_mul(const double* A, const double* B, double* C) {
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += A[4 * r + k] * B[4 * k + c];
+            C[4 * r + c] = s;
+        }
+}
+
+// Joint::update (E_pj = E_pj0 Q, Q = [I q; 0 1]) and Body::update (E_0i = E_0j E_ji,
+// phi = Ad(E_ij) S_j qdot = (0, R_ji^T qdot)); Joint.cpp, Body.cpp:138-156.
+__device__ void mover_pose(const MoverDev& m, const double* q, const double* qd, double* E0i, double* phi) {
+    const double Q[16] = {1, 0, 0, q[0], 0, 1, 0, q[1], 0, 0, 1, q[2], 0, 0, 0, 1};
+    double E0j[16];
+    mat4_mul(m.E_pj0, Q, E0j);
+    mat4_mul(E0j, m.E_ji, E0i);
+    phi[0] = phi[1] = phi[2] = 0.0;
+    for (int r = 0; r < 3; ++r) phi[3 + r] = m.E_ji[r] * qd[0] + m.E_ji[4 + r] * qd[1] + m.E_ji[8 + r] * qd[2];
+}
+
+__global__ void sim_begin_kernel(int n, const MoverDev* __restrict__ mover, const double* __restrict__ q,
+                                 const double* __restrict__ qd, SceneState* __restrict__ st, int* remaining) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *remaining = n;
+    if (i >= n) return;
+    SceneState s;
+    const double h = mover[i].h;
+    for (int k = 0; k < 3; ++k) {
+        s.q0[k] = q[3 * i + k];
+        s.qd0[k] = qd[3 * i + k];
+        s.x[k] = s.q0[k] + h * s.qd0[k];  // initial guess, Simulation.cpp:1256
+        s.dx[k] = s.xt[k] = 0.0;
+    }
+    s.gnorm = 0.0;
+    s.alpha = 1.0;
+    s.phase = kNewton;
+    s.iter = s.trial = s.strike = s.converged = 0;
+    st[i] = s;
+}
+
+__global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, const int* __restrict__ role,
+                                const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
+                                const SceneState* __restrict__ st, double* __restrict__ EA, double* __restrict__ phiA,
+                                double* __restrict__ EB, double* __restrict__ phiB, int* __restrict__ mode) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pairs) return;
+    const int i = pair_inst[k];
+    const SceneState& s = st[i];
+    if (s.phase == kDone) {
+        mode[k] = 0;
+        return;
+    }
+    const MoverDev& m = mover[i];
+    const double* p = s.phase == kNewton ? s.x : s.xt;
+    double qd[3], E0i[16], phi[6];
+    for (int c = 0; c < 3; ++c) qd[c] = (p[c] - s.q0[c]) / m.h;
+    mover_pose(m, p, qd, E0i, phi);
+    double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
+    double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
+    double *Ef = role[k] ? EB + 16 * (size_t)k : EA + 16 * (size_t)k;
+    double *pf = role[k] ? phiB + 6 * (size_t)k : phiA + 6 * (size_t)k;
+    for (int c = 0; c < 16; ++c) {
+        Em[c] = E0i[c];
+        Ef[c] = E_fixed[16 * (size_t)k + c];
+    }
+    for (int c = 0; c < 6; ++c) {
+        pm[c] = phi[c];
+        pf[c] = 0.0;
+    }
+    mode[k] = s.phase == kNewton ? 2 : 1;
+}
+
+// 3x3 solve by Gaussian elimination with partial pivoting (the algorithm of the
+// reference's PartialPivLU, Simulation.cpp:1028).
+__device__ void solve3(const double* A_in, const double* b_in, double* x) {
+    double A[9], b[3];
+    for (int k = 0; k < 9; ++k) A[k] = A_in[k];
+    for (int k = 0; k < 3; ++k) b[k] = b_in[k];
+    for (int c = 0; c < 3; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 3; ++r)
+            if (fabs(A[3 * r + c]) > fabs(A[3 * p + c])) p = r;
+        if (p != c) {
+            for (int k = 0; k < 3; ++k) {
+                const double t = A[3 * c + k];
+                A[3 * c + k] = A[3 * p + k];
+                A[3 * p + k] = t;
+            }
+            const double t = b[c];
+            b[c] = b[p];
+            b[p] = t;
+        }
+        for (int r = c + 1; r < 3; ++r) {
+            const double l = A[3 * r + c] / A[3 * c + c];
+            for (int k = c; k < 3; ++k) A[3 * r + k] -= l * A[3 * c + k];
+            b[r] -= l * b[c];
+        }
+    }
+    for (int r = 2; r >= 0; --r) {
+        double s = b[r];
+        for (int k = r + 1; k < 3; ++k) s -= A[3 * r + k] * x[k];
+        x[r] = s / A[3 * r + r];
+    }
+}
+
+__device__ __forceinline__ double norm3d(const double* v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+__global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
+                                  const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
+                                  const double* __restrict__ fm, const double* __restrict__ Km,
+                                  const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    SceneState s = st[i];
+    if (s.phase == kDone) return;
+    const MoverDev& m = mover[i];
+    const bool newton = s.phase == kNewton;
+    const double* p = newton ? s.x : s.xt;
+    const double h = m.h;
+    double qd[3], E0i[16], phi[6];
+    for (int c = 0; c < 3; ++c) qd[c] = (p[c] - s.q0[c]) / h;
+    mover_pose(m, p, qd, E0i, phi);
+    // fm (linear rows) of the mover: gravity and external force (Body.cpp:247-271) + contacts
+    double fl[3], Kll[9] = {0}, Dll[9] = {0};
+    const double* fe = f_ext + 6 * (size_t)i;
+    for (int r = 0; r < 3; ++r) {
+        double g = 0.0, e = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            g += E0i[4 * c + r] * (m.mass * m.gravity[c]);
+            e += E0i[4 * c + r] * fe[3 + c];
+        }
+        fl[r] = g + m.inertia[3 + r] * e;
+    }
+    for (int k = pair_begin[i]; k < pair_begin[i + 1]; ++k) {
+        const int o = role[k] ? 0 : 6;
+        for (int r = 0; r < 3; ++r) {
+            fl[r] += fm[12 * (size_t)k + o + 3 + r];
+            if (newton)
+                for (int c = 0; c < 3; ++c) {
+                    Kll[3 * r + c] += Km[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+                    Dll[3 * r + c] += Dm[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+                }
+        }
+    }
+    // reduced system: f = R_ji fl + fr, M = R_ji diag(m) R_ji^T
+    double R[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) R[3 * r + c] = m.E_ji[4 * r + c];
+    double f[3], M[9], g[3];
+    for (int r = 0; r < 3; ++r) {
+        f[r] = R[3 * r] * fl[0] + R[3 * r + 1] * fl[1] + R[3 * r + 2] * fl[2];
+        f[r] += -m.Kr * p[r] - m.Dr * qd[r];
+        for (int c = 0; c < 3; ++c)
+            M[3 * r + c] = R[3 * r] * m.inertia[3] * R[3 * c] + R[3 * r + 1] * m.inertia[4] * R[3 * c + 1] +
+                           R[3 * r + 2] * m.inertia[5] * R[3 * c + 2];
+    }
+    double dq[3];
+    for (int k = 0; k < 3; ++k) dq[k] = p[k] - s.q0[k] - h * s.qd0[k];
+    for (int r = 0; r < 3; ++r) g[r] = M[3 * r] * dq[0] + M[3 * r + 1] * dq[1] + M[3 * r + 2] * dq[2] - h * h * f[r];
+    bool done = false;
+    if (newton) {
+        // H = M - h^2 K - h D, K = R Kll R^T - Kr I, D = R Dll R^T - Dr I
+        double H[9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                double K = 0.0, D = 0.0;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        K += R[3 * r + a] * Kll[3 * a + b] * R[3 * c + b];
+                        D += R[3 * r + a] * Dll[3 * a + b] * R[3 * c + b];
+                    }
+                if (r == c) {
+                    K -= m.Kr;
+                    D -= m.Dr;
+                }
+                H[3 * r + c] = M[3 * r + c] - h * h * K - h * D;
+            }
+        const double mg[3] = {-g[0], -g[1], -g[2]};
+        solve3(H, mg, s.dx);
+        s.gnorm = norm3d(g);
+        s.alpha = 1.0;
+        s.trial = 0;
+        for (int k = 0; k < 3; ++k) s.xt[k] = s.x[k] + s.dx[k];
+        s.phase = kLine;
+    } else {
+        const double gn = norm3d(g);
+        bool step_done = false;
+        if (gn < s.gnorm) {  // line search succeeded
+            s.strike = 0;
+            for (int k = 0; k < 3; ++k) s.x[k] = s.xt[k];
+            step_done = true;
+        } else if (++s.trial < kMaxLineSearch) {
+            s.alpha *= 0.5;
+            for (int k = 0; k < 3; ++k) s.xt[k] = s.x[k] + s.alpha * s.dx[k];
+        } else {  // 20 failures: alpha = 0.5^20
+            s.alpha *= 0.5;
+            if (++s.strike >= kMaxStrike) {
+                done = true;  // stops before the update, Simulation.cpp:1052-1054
+            } else {
+                for (int k = 0; k < 3; ++k) s.x[k] = s.x[k] + s.alpha * s.dx[k];
+                step_done = true;
+            }
+        }
+        if (step_done) {
+            ++s.iter;
+            if (gn < kTol) {
+                s.converged = 1;
+                done = true;
+            } else if (s.iter >= m.max_iter) {
+                done = true;
+            } else {
+                s.phase = kNewton;
+            }
+        }
+    }
+    if (done) {
+        s.phase = kDone;
+        atomicSub(remaining, 1);
+    }
+    st[i] = s;
+}
+
+__global__ void sim_end_kernel(int n, const MoverDev* __restrict__ mover, const SceneState* __restrict__ st,
+                               double* __restrict__ q, double* __restrict__ qd, int* __restrict__ converged) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SceneState& s = st[i];
+    for (int k = 0; k < 3; ++k) {
+        q[3 * i + k] = s.x[k];
+        qd[3 * i + k] = (s.x[k] - s.q0[k]) / mover[i].h;
+    }
+    converged[i] = s.converged;
+}
+
+}  // namespace
+
+struct sdfc_sim {
+    sdfc_context* ctx = nullptr;
+    int n = 0, n_pairs = 0;
+    sdfc_batch* batch = nullptr;
+    std::vector<int> order;  // sorted pair k -> caller's pair index
+    MoverDev* d_mover = nullptr;
+    SceneState* d_state = nullptr;
+    double *d_q = nullptr, *d_qd = nullptr, *d_fext = nullptr;
+    int *d_pair_inst = nullptr, *d_role = nullptr, *d_pair_begin = nullptr;
+    double* d_Efixed = nullptr;
+    double *d_EA = nullptr, *d_phiA = nullptr, *d_EB = nullptr, *d_phiB = nullptr, *d_prm = nullptr;
+    int* d_mode = nullptr;
+    double *d_fm = nullptr, *d_Km = nullptr, *d_Dm = nullptr;
+    int *d_nact = nullptr, *d_status = nullptr, *d_conv = nullptr, *d_remaining = nullptr;
+    int* h_remaining = nullptr;
+    long long rounds = 0, evaluations = 0;
+    std::vector<void*> allocations;
+};
+
+namespace sdfc_impl {
+
+void free_sim(sdfc_sim* s) {
+    if (!s) return;
+    for (void* p : s->allocations) cudaFree(p);
+    if (s->h_remaining) cudaFreeHost(s->h_remaining);
+    if (s->batch) sdfc_impl::free_batch(s->batch);
+    delete s;
+}
+
+}  // namespace sdfc_impl
+
+namespace {
+
+using sdfc_impl::free_sim;
+
+template <class T>
+int alloc(sdfc_sim* s, T** p, size_t count) {
+    void* v = nullptr;
+    int rc = dev_alloc(s->ctx, &v, sizeof(T) * std::max<size_t>(count, 1));
+    if (rc) return rc;
+    s->allocations.push_back(v);
+    *p = (T*)v;
+    return SDFC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pairs, const sdfc_scene_pair* pairs,
+                    sdfc_sim** out) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (n <= 0 || !movers || n_pairs < 0 || (n_pairs > 0 && !pairs) || !out)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: bad argument");
+    for (int i = 0; i < n; ++i) {
+        if (movers[i].joint != SDFC_JOINT_TRANSLATIONAL)
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: only SDFC_JOINT_TRANSLATIONAL movers");
+        if (!(movers[i].h > 0.0)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: time step must be > 0");
+    }
+    for (int k = 0; k < n_pairs; ++k)
+        if (pairs[k].instance < 0 || pairs[k].instance >= n)
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: pair instance out of range");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    auto* s = new sdfc_sim();
+    s->ctx = ctx;
+    s->n = n;
+    s->n_pairs = n_pairs;
+    // pairs grouped by scene (stable), so each scene's pairs are contiguous
+    s->order.resize(n_pairs);
+    std::iota(s->order.begin(), s->order.end(), 0);
+    std::stable_sort(s->order.begin(), s->order.end(),
+                     [&](int a, int b) { return pairs[a].instance < pairs[b].instance; });
+    std::vector<int> pts(n_pairs), grd(n_pairs), inst(n_pairs), role(n_pairs), begin(n + 1, 0);
+    std::vector<double> Ef(16 * (size_t)n_pairs), prm(6 * (size_t)n_pairs);
+    for (int k = 0; k < n_pairs; ++k) {
+        const sdfc_scene_pair& P = pairs[s->order[k]];
+        pts[k] = P.points;
+        grd[k] = P.grid;
+        inst[k] = P.instance;
+        role[k] = P.mover_is_contact ? 1 : 0;
+        std::memcpy(&Ef[16 * (size_t)k], P.E_fixed, sizeof(double) * 16);
+        const double pr[6] = {P.params.kn, P.params.kt, P.params.mu, P.params.damping, P.params.scale,
+                              P.params.contact_scale};
+        std::memcpy(&prm[6 * (size_t)k], pr, sizeof pr);
+        begin[P.instance + 1]++;
+    }
+    for (int i = 0; i < n; ++i) begin[i + 1] += begin[i];
+    std::vector<MoverDev> md(n);
+    for (int i = 0; i < n; ++i) {
+        const sdfc_mover& m = movers[i];
+        MoverDev d{};
+        d.mass = m.mass;
+        std::memcpy(d.inertia, m.inertia, sizeof d.inertia);
+        std::memcpy(d.E_pj0, m.E_pj0, sizeof d.E_pj0);
+        std::memcpy(d.E_ji, m.E_ji, sizeof d.E_ji);
+        std::memcpy(d.gravity, m.gravity, sizeof d.gravity);
+        d.h = m.h;
+        d.Kr = m.joint_stiffness;
+        d.Dr = m.joint_damping;
+        d.max_iter = std::max(20 * 3, 100);  // Simulation.cpp:1009, ndof_r = 3
+        md[i] = d;
+    }
+    if (n_pairs > 0 && (rc = sdfc_impl::batch_create(ctx, n_pairs, pts.data(), grd.data(), &s->batch))) {
+        delete s;
+        return rc;
+    }
+    if ((rc = alloc(s, &s->d_mover, n)) || (rc = alloc(s, &s->d_state, n)) || (rc = alloc(s, &s->d_q, 3 * (size_t)n)) ||
+        (rc = alloc(s, &s->d_qd, 3 * (size_t)n)) || (rc = alloc(s, &s->d_fext, 6 * (size_t)n)) ||
+        (rc = alloc(s, &s->d_pair_inst, n_pairs)) || (rc = alloc(s, &s->d_role, n_pairs)) ||
+        (rc = alloc(s, &s->d_pair_begin, n + 1)) || (rc = alloc(s, &s->d_Efixed, 16 * (size_t)n_pairs)) ||
+        (rc = alloc(s, &s->d_EA, 16 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_phiA, 6 * (size_t)n_pairs)) ||
+        (rc = alloc(s, &s->d_EB, 16 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_phiB, 6 * (size_t)n_pairs)) ||
+        (rc = alloc(s, &s->d_prm, 6 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_mode, n_pairs)) ||
+        (rc = alloc(s, &s->d_fm, 12 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_Km, 144 * (size_t)n_pairs)) ||
+        (rc = alloc(s, &s->d_Dm, 144 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_nact, n_pairs)) ||
+        (rc = alloc(s, &s->d_status, n_pairs)) || (rc = alloc(s, &s->d_conv, n)) ||
+        (rc = alloc(s, &s->d_remaining, 1))) {
+        free_sim(s);
+        return rc;
+    }
+    if (cudaMallocHost((void**)&s->h_remaining, sizeof(int)) != cudaSuccess) {
+        free_sim(s);
+        return fail(ctx, SDFC_ERR_CUDA, "sim_create: cudaMallocHost failed");
+    }
+    cudaError_t e = cudaMemcpy(s->d_mover, md.data(), sizeof(MoverDev) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n_pairs > 0) {
+        e = cudaMemcpy(s->d_pair_inst, inst.data(), sizeof(int) * n_pairs, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(s->d_role, role.data(), sizeof(int) * n_pairs, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(s->d_Efixed, Ef.data(), sizeof(double) * Ef.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(s->d_prm, prm.data(), sizeof(double) * prm.size(), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_pair_begin, begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(s->d_q, 0, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_qd, 0, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_fext, 0, sizeof(double) * 6 * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_conv, 0, sizeof(int) * n);
+    if (e != cudaSuccess) {
+        free_sim(s);
+        return fail(ctx, SDFC_ERR_CUDA, std::string("sim_create: ") + cudaGetErrorString(e));
+    }
+    ctx->sims.push_back(s);
+    *out = s;
+    return SDFC_OK;
+}
+
+void sdfc_sim_destroy(sdfc_sim* s) {
+    if (!s) return;
+    sdfc_context* ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    auto it = std::find(ctx->sims.begin(), ctx->sims.end(), s);
+    if (it != ctx->sims.end()) ctx->sims.erase(it);
+    free_sim(s);
+}
+
+int sdfc_sim_set_precision(sdfc_sim* s, int precision) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
+        return fail(s->ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_precision: unknown precision");
+    if (s->batch) s->batch->precision = precision;
+    return SDFC_OK;
+}
+
+int sdfc_sim_set_state(sdfc_sim* s, const double* q, const double* qdot) {
+    if (!s || !q || !qdot) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_q, q, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd, qdot, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return SDFC_OK;
+}
+
+int sdfc_sim_get_state(sdfc_sim* s, double* q, double* qdot) {
+    if (!s || !q || !qdot) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(q, s->d_q, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(qdot, s->d_qd, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return SDFC_OK;
+}
+
+int sdfc_sim_set_external_force(sdfc_sim* s, const double* f) {
+    if (!s || !f) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_fext, f, sizeof(double) * 6 * s->n, cudaMemcpyHostToDevice, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return SDFC_OK;
+}
+
+int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
+    if (!s || num_steps < 0) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    const int n = s->n, np = s->n_pairs;
+    const int tb = 128;
+    const int max_rounds = 100 * (1 + kMaxLineSearch) + 1;
+    sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
+    in.mode = s->d_mode;
+    sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
+    for (int step = 0; step < num_steps; ++step) {
+        sim_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_mover, s->d_q, s->d_qd, s->d_state, s->d_remaining);
+        int active = n;
+        for (int r = 0; r < max_rounds; ++r) {
+            s->evaluations += active;
+            if (np > 0) {
+                sim_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, s->d_pair_inst, s->d_role, s->d_Efixed,
+                                                                  s->d_mover, s->d_state, s->d_EA, s->d_phiA, s->d_EB,
+                                                                  s->d_phiB, s->d_mode);
+                if ((rc = sdfc_impl::run_batch(s->batch, in, true, out, st))) return rc;
+            }
+            sim_newton_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
+                                                               s->d_fm, s->d_Km, s->d_Dm, s->d_state, s->d_remaining);
+            SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_remaining, s->d_remaining, sizeof(int), cudaMemcpyDeviceToHost, st));
+            SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+            ++s->rounds;
+            active = *s->h_remaining;
+            if (active == 0) break;
+        }
+        sim_end_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_mover, s->d_state, s->d_q, s->d_qd, s->d_conv);
+    }
+    SDFC_CUDA_TRY(ctx, cudaGetLastError());
+    if (converged)
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(converged, s->d_conv, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return SDFC_OK;
+}
+
+int sdfc_sim_stats(sdfc_sim* s, long long* rounds, long long* evaluations) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    if (rounds) *rounds = s->rounds;
+    if (evaluations) *evaluations = s->evaluations;
+    return SDFC_OK;
+}
+
+}  // extern "C"

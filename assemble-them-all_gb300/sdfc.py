@@ -24,8 +24,11 @@ EXPORTS = (
     "sdfc_evaluate", "sdfc_active_ids", "sdfc_batch_create", "sdfc_batch_destroy", "sdfc_batch_evaluate",
     "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count", "sdfc_set_derivative_mode",
     "sdfc_batch_set_derivative_mode", "sdfc_batch_set_timing", "sdfc_batch_last_timing", "sdfc_set_precision",
-    "sdfc_batch_set_precision", "sdfc_evaluate_noalloc",
+    "sdfc_batch_set_precision", "sdfc_evaluate_noalloc", "sdfc_sim_create", "sdfc_sim_destroy",
+    "sdfc_sim_set_precision", "sdfc_sim_set_state", "sdfc_sim_get_state", "sdfc_sim_set_external_force",
+    "sdfc_sim_step", "sdfc_sim_stats",
 )
+JOINT_TRANSLATIONAL = 3
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 DERIV_ANALYTIC = 0
@@ -34,6 +37,22 @@ DERIV_STENCIL = 1
 
 class SdfcError(RuntimeError):
     pass
+
+
+class Mover(ctypes.Structure):
+    """sdfc_mover: the moving part (Body::_mass, _Inertia, Joint::_E_pj_0, Body::_E_ji, gravity, timestep)."""
+    _fields_ = [("joint", ctypes.c_int), ("mass", ctypes.c_double), ("inertia", ctypes.c_double * 6),
+                ("E_pj0", ctypes.c_double * 16), ("E_ji", ctypes.c_double * 16), ("gravity", ctypes.c_double * 3),
+                ("h", ctypes.c_double), ("joint_stiffness", ctypes.c_double), ("joint_damping", ctypes.c_double)]
+
+    @classmethod
+    def make(cls, mass, inertia, E_ji, h, gravity=(0.0, 0.0, -9.8), E_pj0=None, joint=3, joint_stiffness=0.0,
+             joint_damping=0.0):
+        E_pj0 = np.eye(4) if E_pj0 is None else np.asarray(E_pj0, dtype=np.float64)
+        return cls(joint, float(mass), (ctypes.c_double * 6)(*np.asarray(inertia, dtype=np.float64)),
+                   (ctypes.c_double * 16)(*E_pj0.ravel()),
+                   (ctypes.c_double * 16)(*np.asarray(E_ji, dtype=np.float64).ravel()),
+                   (ctypes.c_double * 3)(*gravity), float(h), float(joint_stiffness), float(joint_damping))
 
 
 class Params(ctypes.Structure):
@@ -46,6 +65,17 @@ class Params(ctypes.Structure):
 
     def as_row(self):
         return np.array([self.kn, self.kt, self.mu, self.damping, self.scale, self.contact_scale])
+
+
+class ScenePair(ctypes.Structure):
+    """sdfc_scene_pair: one contact of scene `instance`'s mover with a fixed part."""
+    _fields_ = [("instance", ctypes.c_int), ("points", ctypes.c_int), ("grid", ctypes.c_int),
+                ("mover_is_contact", ctypes.c_int), ("E_fixed", ctypes.c_double * 16), ("params", Params)]
+
+    @classmethod
+    def make(cls, instance, points, grid, mover_is_contact, E_fixed, params):
+        return cls(int(instance), int(points), int(grid), int(bool(mover_is_contact)),
+                   (ctypes.c_double * 16)(*np.asarray(E_fixed, dtype=np.float64).ravel()), params)
 
 
 _lib = None
@@ -79,6 +109,15 @@ def lib():
         L.sdfc_batch_set_derivative_mode.argtypes = [v, i]
         L.sdfc_batch_set_timing.argtypes = [v, i]
         L.sdfc_set_precision.argtypes = [v, i]
+        L.sdfc_sim_create.argtypes = [v, i, P(Mover), i, P(ScenePair), P(v)]
+        L.sdfc_sim_destroy.argtypes = [v]
+        L.sdfc_sim_destroy.restype = None
+        L.sdfc_sim_set_precision.argtypes = [v, i]
+        L.sdfc_sim_set_state.argtypes = [v, d, d]
+        L.sdfc_sim_get_state.argtypes = [v, d, d]
+        L.sdfc_sim_set_external_force.argtypes = [v, d]
+        L.sdfc_sim_step.argtypes = [v, i, P(i)]
+        L.sdfc_sim_stats.argtypes = [v, P(ctypes.c_longlong), P(ctypes.c_longlong)]
         L.sdfc_evaluate_noalloc.argtypes = [v, i, i, i, d, d, d, ctypes.c_double, v, i, v, v, v, v, v, i, v, v, v,
                                             v, v]
         L.sdfc_batch_set_precision.argtypes = [v, i]
@@ -179,6 +218,9 @@ class Context:
     def batch(self, points, grids) -> "Batch":
         return Batch(self, points, grids)
 
+    def sim(self, movers, pairs) -> "Sim":
+        return Sim(self, movers, pairs)
+
 
 class Batch:
     """sdfc_batch: n pair instances evaluated by one set of launches."""
@@ -259,3 +301,47 @@ def evaluate_noalloc(grid_values_dev, shape, min_box, max_box, dx, col_th, point
                                      params, int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active, stream)
     if rc != SDFC_OK:
         raise SdfcError(f"sdfc_evaluate_noalloc failed ({rc})")
+
+
+class Sim:
+    """sdfc_sim: n planner scenes (one moving part each) stepped by batched BDF1 Newton."""
+
+    def __init__(self, ctx: Context, movers, pairs):
+        self.ctx = ctx
+        self.n = len(movers)
+        marr = (Mover * self.n)(*movers)
+        parr = (ScenePair * max(1, len(pairs)))(*pairs)
+        self._h = ctypes.c_void_p()
+        ctx._check(lib().sdfc_sim_create(ctx._h, self.n, marr, len(pairs), parr, ctypes.byref(self._h)),
+                   "sdfc_sim_create")
+
+    def close(self):
+        if self._h and self.ctx._h:
+            lib().sdfc_sim_destroy(self._h)
+        self._h = ctypes.c_void_p()
+
+    def set_precision(self, precision: int):
+        self.ctx._check(lib().sdfc_sim_set_precision(self._h, int(precision)), "sdfc_sim_set_precision")
+
+    def set_state(self, q, qdot):
+        self.ctx._check(lib().sdfc_sim_set_state(self._h, _dp(_f64(q, 3 * self.n)), _dp(_f64(qdot, 3 * self.n))),
+                        "sdfc_sim_set_state")
+
+    def get_state(self):
+        q, qd = np.zeros(3 * self.n), np.zeros(3 * self.n)
+        self.ctx._check(lib().sdfc_sim_get_state(self._h, _dp(q), _dp(qd)), "sdfc_sim_get_state")
+        return q.reshape(self.n, 3), qd.reshape(self.n, 3)
+
+    def set_external_force(self, f):
+        self.ctx._check(lib().sdfc_sim_set_external_force(self._h, _dp(_f64(f, 6 * self.n))),
+                        "sdfc_sim_set_external_force")
+
+    def step(self, num_steps=1):
+        conv = np.zeros(self.n, dtype=np.int32)
+        self.ctx._check(lib().sdfc_sim_step(self._h, int(num_steps), _ip(conv)), "sdfc_sim_step")
+        return conv.astype(bool)
+
+    def stats(self):
+        r, e = ctypes.c_longlong(), ctypes.c_longlong()
+        self.ctx._check(lib().sdfc_sim_stats(self._h, ctypes.byref(r), ctypes.byref(e)), "sdfc_sim_stats")
+        return r.value, e.value

@@ -71,6 +71,7 @@ extern "C" {
 
 typedef struct sdfc_context sdfc_context;
 typedef struct sdfc_batch sdfc_batch;
+typedef struct sdfc_sim sdfc_sim;
 
 /* Contact coefficients of one pair: ForceGeneralSDFContact::_kn, _kt, _mu,
  * _damping, _scale (ForceGeneralSDFContact.h:16-20) and the contact body's
@@ -167,6 +168,60 @@ int sdfc_batch_last_timing(sdfc_batch* batch, float* ms);
  * because their FP32 distance fell inside the guard band (diagnostic; the
  * counter accumulates until reset with reset != 0). */
 int sdfc_batch_recheck_count(sdfc_batch* batch, unsigned long long* count, int reset);
+
+/* ---------------------------------------------------------------- batched implicit-Euler steps */
+
+/* A batch of planner scenes stepped together: in each scene one part moves on
+ * a joint attached to the world and every other part is fixed, exactly the
+ * scene of the planner (examples/run_joint_plan.py:140-178, 218).  Each step
+ * is redmax's BDF1 step (Simulation::integration_BDF1 and Simulation::newton,
+ * simulation/redmax/Simulation.cpp:999-1079, 1248-1270) with its reduced
+ * system (Simulation::computeMatrices, :379-503): tolerance 1e-8 on |g|, at
+ * most max(20 ndof, 100) Newton iterations, backtracking line search halving
+ * the step up to 20 times, 3 consecutive line-search failures stop.  Every
+ * force evaluation of every scene of one Newton round runs as one batched
+ * evaluation on the GPU; the 3x3 solves run in FP64 on the GPU. */
+#define SDFC_JOINT_TRANSLATIONAL 3 /* JointTranslational: q = position (3 dof) */
+
+/* The moving part: Body::_mass, Body::_Inertia (Ixx, Iyy, Izz, m, m, m),
+ * Joint::_E_pj_0 (row-major 4x4), Body::_E_ji, the options gravity and
+ * timestep (the reference reads timestep as FP32), Joint::_Kr / _Dr. */
+typedef struct {
+    int joint;
+    double mass, inertia[6], E_pj0[16], E_ji[16];
+    double gravity[3], h;
+    double joint_stiffness, joint_damping;
+} sdfc_mover;
+
+/* One ForceGeneralSDFContact of scene `instance`: the mover against one fixed
+ * part.  mover_is_contact = 1: the mover's points (handle `points`) against the
+ * fixed part's grid (`grid`); 0: the fixed part's points against the mover's
+ * grid.  E_fixed is the fixed part's pose. */
+typedef struct {
+    int instance, points, grid, mover_is_contact;
+    double E_fixed[16];
+    sdfc_params params;
+} sdfc_scene_pair;
+
+int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pairs, const sdfc_scene_pair* pairs,
+                    sdfc_sim** sim);
+void sdfc_sim_destroy(sdfc_sim* sim);
+/* Precision of the force evaluations (SDFC_PRECISION_*); the solves are FP64. */
+int sdfc_sim_set_precision(sdfc_sim* sim, int precision);
+/* Joint state of every scene (host, n x ndof): Simulation::set_state / get_q / get_qdot. */
+int sdfc_sim_set_state(sdfc_sim* sim, const double* q, const double* qdot);
+int sdfc_sim_get_state(sdfc_sim* sim, double* q, double* qdot);
+/* External force on each mover (host, n x 6, world frame, torque then force):
+ * Simulation::set_body_external_force (Body::_f_external; the reference scales
+ * it by the inertia diagonal, Body.cpp:267-268). */
+int sdfc_sim_set_external_force(sdfc_sim* sim, const double* f);
+/* num_steps BDF1 steps of every scene (Simulation::forward, :914-990).
+ * converged (host, n, may be NULL): 1 where the last step's Newton converged
+ * (Simulation::is_converged). */
+int sdfc_sim_step(sdfc_sim* sim, int num_steps, int* converged);
+/* Totals since creation: Newton rounds (batched force evaluations) and scene
+ * force evaluations (diagnostic). */
+int sdfc_sim_stats(sdfc_sim* sim, long long* rounds, long long* evaluations);
 
 /* ---------------------------------------------------------------- allocation-free evaluation */
 
