@@ -46,6 +46,9 @@ UNIT = "contact-pts/s"
 COL_TH = 0.01
 PARAMS = (1e5, 1e3, 0.3, 1e3, 1.0, 1.0)  # kn, kt, mu, damping, scale, contact_scale
 L2_BYTES = 129 * 2 ** 20
+SIM_H = float(np.float32(5e-3))  # the reference reads the time step as FP32
+SIM_GRAVITY = (0.0, 0.0, -9.8)
+SIM_PULL = 1.0  # pull force magnitude along each direction (scaled by the mass, Body.cpp:267-268)
 
 
 def instance_states(n, rank=0):
@@ -89,6 +92,18 @@ def _cpu_eval(args):
     t = time.perf_counter()
     O.pair_eval(_G["grid"], _G["pts"], EA, phiA, EB, phiB, _G["prm"], True)
     return time.perf_counter() - t
+
+
+def _cpu_sim(args):
+    """One scene of the direction sweep stepped by the oracle's BDF1 restatement."""
+    d, steps = args
+    O = _G["O"]
+    m, inertia = W.cylinder_mass_props()
+    mover = O.Mover(m, inertia, np.eye(4), np.eye(4), SIM_GRAVITY, SIM_H, np.concatenate([np.zeros(3), d]))
+    pair = O.ScenePair(_G["grid"], _G["pts"], True, np.eye(4), _G["prm"])
+    t = time.perf_counter()
+    qs, qds, conv, its, evs = O.bdf1_steps(mover, [pair], np.zeros(3), np.zeros(3), steps)
+    return time.perf_counter() - t, int(evs.sum())
 
 
 def cpu_pool(grid, pts, procs):
@@ -214,6 +229,7 @@ def run_reference(args, world, rank):
     times = []
     for _ in range(args.steps):
         times.append(cpu_time(pool, states, rng.choice(args.instances, sample, replace=False)))
+    sim = cpu_sim_rate(pool, args.cpu_sim_scenes, min(args.sim_early, 25), procs) if args.sim_steps > 0 else None
     pool.close()
     per_step = float(np.mean(times))
     value = sample * args.points / per_step
@@ -226,6 +242,8 @@ def run_reference(args, world, rank):
                          "sample": f"{sample} of {args.instances} instances per step, derivative evaluation"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if sim is not None:
+        line["sim"] = sim
     print(json.dumps(line), flush=True)
 
 
@@ -354,6 +372,8 @@ def run_gpu(args, world, rank):
     h2d = n * 50 * 8
     d2h = n * (300 * 8 + 2 * 4)
 
+    sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 else None
+
     if rank != 0:
         return
     peaks = load_peaks()
@@ -397,10 +417,63 @@ def run_gpu(args, world, rank):
         rng = np.random.default_rng(0)
         cpu_time(pool, states, rng.choice(n, procs, replace=False))
         ct = cpu_time(pool, states, rng.choice(n, sample, replace=False))
-        pool.close()
         line["cpu_baseline"] = {"value": sample * args.points / ct, "unit": UNIT, "cores": procs, "kind": "port",
                                 "sample": f"{sample} of {n} instances, derivative evaluation, one process per core"}
+        if sim_res is not None:
+            line["cpu_baseline"]["sim"] = cpu_sim_rate(pool, args.cpu_sim_scenes, min(args.sim_early, 25), procs)
+        pool.close()
+    if sim_res is not None:
+        line["sim"] = sim_res
     print(json.dumps(line), flush=True)
+
+
+def run_sim(args, sdfc, ctx, g, p, n):
+    """The direction sweep stepped: n scenes (peg on a translational joint, fixed socket), each pulled along
+    its Fibonacci direction, args.sim_steps BDF1 steps through sdfc_sim_step (host state in and out)."""
+    dirs = W.fibonacci_directions(n)
+    m, inertia = W.cylinder_mass_props()
+    mover = sdfc.Mover.make(m, inertia, np.eye(4), SIM_H, SIM_GRAVITY)
+    prm = sdfc.Params(*PARAMS)
+    pairs = [sdfc.ScenePair.make(i, p, g, True, np.eye(4), prm) for i in range(n)]
+    sim = ctx.sim([mover] * n, pairs)
+    sim.set_precision(sdfc.PRECISION_MIXED if args.precision == "mixed" else sdfc.PRECISION_FP64)
+    F = np.zeros((n, 6))
+    F[:, 3:] = SIM_PULL * dirs
+    sim.set_state(np.zeros((n, 3)), np.zeros((n, 3)))
+    sim.set_external_force(F)
+    sim.step(1)  # warm-up step
+    sim.set_state(np.zeros((n, 3)), np.zeros((n, 3)))
+    r0, e0 = sim.stats()
+    t0 = time.perf_counter()
+    early = min(args.sim_steps, args.sim_early)
+    conv = sim.step(early)
+    t_early = time.perf_counter() - t0
+    r1, e1 = sim.stats()
+    if args.sim_steps > early:
+        conv = sim.step(args.sim_steps - early)
+    q, qd = sim.get_state()
+    wall = time.perf_counter() - t0
+    r2, e2 = sim.stats()
+    sim.close()
+    return {"scenes": n, "steps": args.sim_steps, "wall_s": wall,
+            "scene_steps_per_s": n * args.sim_steps / wall,
+            "contact_pts_per_s": (e2 - e0) * args.points / wall,
+            "rounds": r2 - r0, "scene_evaluations": e2 - e0,
+            "first_steps": {"steps": early, "wall_s": t_early, "scene_steps_per_s": n * early / t_early,
+                            "scene_evaluations": e1 - e0},
+            "converged_last_step": float(np.mean(conv)),
+            "final_z_mean": float(q[:, 2].mean())}
+
+
+def cpu_sim_rate(pool, n_scenes, steps, procs):
+    dirs = W.fibonacci_directions(1024)
+    idx = np.linspace(0, len(dirs) - 1, n_scenes).astype(int)
+    t = time.perf_counter()
+    res = pool.map(_cpu_sim, [(dirs[k], steps) for k in idx], chunksize=1)
+    wall = time.perf_counter() - t
+    evals = sum(r[1] for r in res)
+    return {"scene_steps_per_s": n_scenes * steps / wall, "steps": steps, "scenes": n_scenes, "cores": procs,
+            "scene_evaluations": evals, "wall_s": wall}
 
 
 def main():
@@ -417,6 +490,9 @@ def main():
     ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
     ap.add_argument("--plain-sample", type=int, default=64, help="instances timed on the per-instance FP64 path")
     ap.add_argument("--full-error", action="store_true", help="compare every instance against the FP64 path")
+    ap.add_argument("--sim-steps", type=int, default=500, help="BDF1 steps of the direction sweep (0: skip)")
+    ap.add_argument("--sim-early", type=int, default=25, help="steps also timed alone (compared with the CPU)")
+    ap.add_argument("--cpu-sim-scenes", type=int, default=32, help="scenes stepped by the CPU baseline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank = dist_setup()
