@@ -157,11 +157,13 @@ __device__ __forceinline__ double norm3d(const double* v) { return sqrt(v[0] * v
 __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
                                   const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
                                   const double* __restrict__ fm, const double* __restrict__ Km,
-                                  const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining) {
+                                  const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining,
+                                  unsigned long long* evaluations) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     SceneState s = st[i];
     if (s.phase == kDone) return;
+    atomicAdd(evaluations, 1ull);
     const MoverDev& m = mover[i];
     const bool newton = s.phase == kNewton;
     const double* p = newton ? s.x : s.xt;
@@ -297,15 +299,22 @@ struct sdfc_sim {
     int* d_mode = nullptr;
     double *d_fm = nullptr, *d_Km = nullptr, *d_Dm = nullptr;
     int *d_nact = nullptr, *d_status = nullptr, *d_conv = nullptr, *d_remaining = nullptr;
+    unsigned long long* d_evals = nullptr;
     int* h_remaining = nullptr;
-    long long rounds = 0, evaluations = 0;
+    long long rounds = 0;
     std::vector<void*> allocations;
+    // one Newton round (pose, batched evaluation, Newton update) as a CUDA graph,
+    // captured at the first step and after a precision change
+    cudaGraphExec_t round_exec = nullptr;
+    cudaStream_t capture_stream = nullptr;
 };
 
 namespace sdfc_impl {
 
 void free_sim(sdfc_sim* s) {
     if (!s) return;
+    if (s->round_exec) cudaGraphExecDestroy(s->round_exec);
+    if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
     for (void* p : s->allocations) cudaFree(p);
     if (s->h_remaining) cudaFreeHost(s->h_remaining);
     if (s->batch) sdfc_impl::free_batch(s->batch);
@@ -400,7 +409,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         (rc = alloc(s, &s->d_fm, 12 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_Km, 144 * (size_t)n_pairs)) ||
         (rc = alloc(s, &s->d_Dm, 144 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_nact, n_pairs)) ||
         (rc = alloc(s, &s->d_status, n_pairs)) || (rc = alloc(s, &s->d_conv, n)) ||
-        (rc = alloc(s, &s->d_remaining, 1))) {
+        (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, 1))) {
         free_sim(s);
         return rc;
     }
@@ -421,6 +430,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     if (e == cudaSuccess) e = cudaMemset(s->d_qd, 0, sizeof(double) * 3 * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_fext, 0, sizeof(double) * 6 * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_conv, 0, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_evals, 0, sizeof(unsigned long long));
     if (e != cudaSuccess) {
         free_sim(s);
         return fail(ctx, SDFC_ERR_CUDA, std::string("sim_create: ") + cudaGetErrorString(e));
@@ -445,6 +455,10 @@ int sdfc_sim_set_precision(sdfc_sim* s, int precision) {
     if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
         return fail(s->ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_precision: unknown precision");
     if (s->batch) s->batch->precision = precision;
+    if (s->round_exec) {  // the captured round launches the old precision's kernels
+        cudaGraphExecDestroy(s->round_exec);
+        s->round_exec = nullptr;
+    }
     return SDFC_OK;
 }
 
@@ -480,34 +494,72 @@ int sdfc_sim_set_external_force(sdfc_sim* s, const double* f) {
     return SDFC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Enqueues one Newton round on `st`.
+int enqueue_round(sdfc_sim* s, cudaStream_t st) {
+    const int n = s->n, np = s->n_pairs, tb = 128;
+    sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
+    in.mode = s->d_mode;
+    sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
+    if (np > 0) {
+        sim_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, s->d_pair_inst, s->d_role, s->d_Efixed, s->d_mover,
+                                                          s->d_state, s->d_EA, s->d_phiA, s->d_EB, s->d_phiB,
+                                                          s->d_mode);
+        int rc = sdfc_impl::run_batch(s->batch, in, true, out, st);
+        if (rc) return rc;
+    }
+    sim_newton_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext, s->d_fm,
+                                                       s->d_Km, s->d_Dm, s->d_state, s->d_remaining, s->d_evals);
+    return SDFC_OK;
+}
+
+// Captures one round into a graph (replayed every round: its kernels skip the
+// scenes that are done, so replaying it is always correct).
+int capture_round(sdfc_sim* s) {
+    sdfc_context* ctx = s->ctx;
+    if (!s->capture_stream)
+        SDFC_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    SDFC_CUDA_TRY(ctx, cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_round(s, s->capture_stream);
+    cudaError_t e = cudaStreamEndCapture(s->capture_stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("sim capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->round_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("sim instantiate: ") + cudaGetErrorString(e));
+    return SDFC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
     if (!s || num_steps < 0) return SDFC_ERR_INVALID_ARGUMENT;
     sdfc_context* ctx = s->ctx;
     int rc = use_device(ctx);
     if (rc) return rc;
+    if (!s->round_exec && (rc = capture_round(s))) return rc;
     cudaStream_t st = ctx->stream;
-    const int n = s->n, np = s->n_pairs;
+    const int n = s->n;
     const int tb = 128;
     const int max_rounds = 100 * (1 + kMaxLineSearch) + 1;
-    sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
-    in.mode = s->d_mode;
-    sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
+    const int per_check = 2;  // rounds enqueued between completion checks
     for (int step = 0; step < num_steps; ++step) {
         sim_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_mover, s->d_q, s->d_qd, s->d_state, s->d_remaining);
         int active = n;
-        for (int r = 0; r < max_rounds; ++r) {
-            s->evaluations += active;
-            if (np > 0) {
-                sim_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, s->d_pair_inst, s->d_role, s->d_Efixed,
-                                                                  s->d_mover, s->d_state, s->d_EA, s->d_phiA, s->d_EB,
-                                                                  s->d_phiB, s->d_mode);
-                if ((rc = sdfc_impl::run_batch(s->batch, in, true, out, st))) return rc;
-            }
-            sim_newton_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
-                                                               s->d_fm, s->d_Km, s->d_Dm, s->d_state, s->d_remaining);
+        for (int r = 0; r < max_rounds && active > 0; r += per_check) {
+            for (int k = 0; k < per_check; ++k) SDFC_CUDA_TRY(ctx, cudaGraphLaunch(s->round_exec, st));
             SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_remaining, s->d_remaining, sizeof(int), cudaMemcpyDeviceToHost, st));
             SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-            ++s->rounds;
+            s->rounds += per_check;
             active = *s->h_remaining;
             if (active == 0) break;
         }
@@ -522,8 +574,14 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
 
 int sdfc_sim_stats(sdfc_sim* s, long long* rounds, long long* evaluations) {
     if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    unsigned long long e = 0;
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpy(&e, s->d_evals, sizeof e, cudaMemcpyDeviceToHost));
     if (rounds) *rounds = s->rounds;
-    if (evaluations) *evaluations = s->evaluations;
+    if (evaluations) *evaluations = (long long)e;
     return SDFC_OK;
 }
 
