@@ -283,6 +283,189 @@ __global__ void sim_end_kernel(int n, const MoverDev* __restrict__ mover, const 
     converged[i] = s.converged;
 }
 
+// ---------------------------------------------------------------- adjoint (backward_BDF1)
+//
+// Simulation::backward_BDF1 (Simulation.cpp:1559-1634) needs, per step k, the H, M and
+// D that integration_BDF1 saves after convergence (:1262-1269): one derivative
+// evaluation at (q_k, qdot_k = (q_k - q_{k-1}) / h).  Here the forward keeps only the
+// trajectory q_0..q_T and the backward recomputes each step's H, D in reverse order,
+// one batched evaluation per step, while it runs the recursion
+//   z_k = H_k^{-T} (dL/dq_k - (-2M + h D_{k+1})^T z_{k+1} - M^T z_{k+2}).
+
+struct AdjState {
+    double z1[3], z2[3], D1[9], zs[3];  // z_{k+1}, z_{k+2}, D_{k+1}, sum of z
+};
+
+__global__ void adj_begin_kernel(int n, int T, AdjState* __restrict__ adj, int* __restrict__ t_dev) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        t_dev[0] = T;  // step being differentiated
+        t_dev[1] = T;  // horizon
+    }
+    if (i >= n) return;
+    AdjState a;
+    for (int c = 0; c < 3; ++c) a.z1[c] = a.z2[c] = a.zs[c] = 0.0;
+    for (int c = 0; c < 9; ++c) a.D1[c] = 0.0;
+    adj[i] = a;
+}
+
+// Pose of every pair at step t of the recorded trajectory (q_his is step-major:
+// q_his[(t * n + scene) * 3 + c]).
+__global__ void adj_pose_kernel(int n_pairs, int n, const int* __restrict__ pair_inst, const int* __restrict__ role,
+                                const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
+                                const double* __restrict__ q_his, const int* __restrict__ t_dev,
+                                double* __restrict__ EA, double* __restrict__ phiA, double* __restrict__ EB,
+                                double* __restrict__ phiB) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = t_dev[0];
+    if (k >= n_pairs || t < 1) return;
+    const int i = pair_inst[k];
+    const MoverDev& m = mover[i];
+    const double* q = q_his + 3 * ((size_t)t * n + i);
+    const double* qp = q_his + 3 * ((size_t)(t - 1) * n + i);
+    double qd[3], E0i[16], phi[6];
+    for (int c = 0; c < 3; ++c) qd[c] = (q[c] - qp[c]) / m.h;  // sim_end_kernel's qdot
+    mover_pose(m, q, qd, E0i, phi);
+    double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
+    double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
+    double *Ef = role[k] ? EB + 16 * (size_t)k : EA + 16 * (size_t)k;
+    double *pf = role[k] ? phiB + 6 * (size_t)k : phiA + 6 * (size_t)k;
+    for (int c = 0; c < 16; ++c) {
+        Em[c] = E0i[c];
+        Ef[c] = E_fixed[16 * (size_t)k + c];
+    }
+    for (int c = 0; c < 6; ++c) {
+        pm[c] = phi[c];
+        pf[c] = 0.0;
+    }
+}
+
+// Partial-pivoting LU of a 3x3 and the solve of A^T z = y with it (Eigen's
+// PartialPivLU::transpose().solve, Simulation.cpp:1587): U^T w = y, L^T u = w, z = P^T u.
+__device__ void lu3_solve_transposed(const double* A, const double* y, double* z) {
+    double LU[9], w[3], u[3];
+    int perm[3] = {0, 1, 2};
+    for (int k = 0; k < 9; ++k) LU[k] = A[k];
+    for (int c = 0; c < 3; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 3; ++r)
+            if (fabs(LU[3 * r + c]) > fabs(LU[3 * p + c])) p = r;
+        if (p != c) {
+            for (int k = 0; k < 3; ++k) {
+                const double t = LU[3 * c + k];
+                LU[3 * c + k] = LU[3 * p + k];
+                LU[3 * p + k] = t;
+            }
+            const int t = perm[c];
+            perm[c] = perm[p];
+            perm[p] = t;
+        }
+        for (int r = c + 1; r < 3; ++r) {
+            LU[3 * r + c] /= LU[3 * c + c];
+            for (int k = c + 1; k < 3; ++k) LU[3 * r + k] -= LU[3 * r + c] * LU[3 * c + k];
+        }
+    }
+    for (int r = 0; r < 3; ++r) {
+        double s = y[r];
+        for (int k = 0; k < r; ++k) s -= LU[3 * k + r] * w[k];
+        w[r] = s / LU[3 * r + r];
+    }
+    for (int r = 2; r >= 0; --r) {
+        double s = w[r];
+        for (int k = r + 1; k < 3; ++k) s -= LU[3 * k + r] * u[k];
+        u[r] = s;
+    }
+    for (int r = 0; r < 3; ++r) z[perm[r]] = u[r];
+}
+
+// One reverse step per scene.  At t = 1 it also writes the scene's gradients
+// (:1590-1614): gout[12 i ..] = dL/dq0[3], dL/dqdot0[3], dL/df_ext[6].  The external
+// force enters f as R_ji diag(m) R_0i^T fe (sim_newton_kernel), so
+// dL/dfe = h^2 R_0i diag(m) R_ji^T sum_k z_k (torque rows 0).
+__global__ void adj_step_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
+                                const MoverDev* __restrict__ mover, const double* __restrict__ Km,
+                                const double* __restrict__ Dm, const double* __restrict__ q_his,
+                                const double* __restrict__ df_dq, const int* __restrict__ t_dev,
+                                AdjState* __restrict__ adj, double* __restrict__ gout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = t_dev[0], T = t_dev[1];
+    if (i >= n || t < 1) return;
+    const MoverDev& m = mover[i];
+    const double h = m.h;
+    double Kll[9] = {0}, Dll[9] = {0};
+    for (int k = pair_begin[i]; k < pair_begin[i + 1]; ++k) {
+        const int o = role[k] ? 0 : 6;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                Kll[3 * r + c] += Km[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+                Dll[3 * r + c] += Dm[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+            }
+    }
+    double R[9], M[9], D[9], H[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) R[3 * r + c] = m.E_ji[4 * r + c];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            M[3 * r + c] = R[3 * r] * m.inertia[3] * R[3 * c] + R[3 * r + 1] * m.inertia[4] * R[3 * c + 1] +
+                           R[3 * r + 2] * m.inertia[5] * R[3 * c + 2];
+            double K = 0.0, Dv = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    K += R[3 * r + a] * Kll[3 * a + b] * R[3 * c + b];
+                    Dv += R[3 * r + a] * Dll[3 * a + b] * R[3 * c + b];
+                }
+            if (r == c) {
+                K -= m.Kr;
+                Dv -= m.Dr;
+            }
+            D[3 * r + c] = Dv;
+            H[3 * r + c] = M[3 * r + c] - h * h * K - h * Dv;
+        }
+    AdjState a = adj[i];
+    double y[3];
+    for (int c = 0; c < 3; ++c) y[c] = df_dq[((size_t)i * T + (t - 1)) * 3 + c];
+    if (t < T)  // step t + 1: dg/dq_t = -2M + h D_{t+1}
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) y[c] -= (-2.0 * M[3 * r + c] + h * a.D1[3 * r + c]) * a.z1[r];
+    if (t < T - 1)  // step t + 2: dg/dq_t = M
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) y[c] -= M[3 * r + c] * a.z2[r];
+    double z[3];
+    lu3_solve_transposed(H, y, z);
+    if (t == 1) {
+        double* go = gout + 12 * (size_t)i;
+        for (int c = 0; c < 3; ++c) {
+            double g0 = 0.0, gd0 = 0.0;
+            for (int r = 0; r < 3; ++r) {
+                g0 -= (-M[3 * r + c] + h * D[3 * r + c]) * z[r];
+                if (T > 1) g0 -= M[3 * r + c] * a.z1[r];
+                gd0 -= (-h * M[3 * r + c]) * z[r];
+            }
+            go[c] = g0;
+            go[3 + c] = gd0;
+        }
+        double zs[3], v[3], E0i[16], phi[6];
+        for (int c = 0; c < 3; ++c) zs[c] = a.zs[c] + z[c];
+        for (int c = 0; c < 3; ++c) v[c] = m.inertia[3 + c] * (R[c] * zs[0] + R[3 + c] * zs[1] + R[6 + c] * zs[2]);
+        const double q0[3] = {q_his[3 * (size_t)i], q_his[3 * (size_t)i + 1], q_his[3 * (size_t)i + 2]};
+        const double zero[3] = {0.0, 0.0, 0.0};
+        mover_pose(m, q0, zero, E0i, phi);  // R_0i does not depend on q
+        for (int c = 0; c < 3; ++c) {
+            go[6 + c] = 0.0;
+            go[9 + c] = h * h * (E0i[4 * c] * v[0] + E0i[4 * c + 1] * v[1] + E0i[4 * c + 2] * v[2]);
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        a.z2[c] = a.z1[c];
+        a.z1[c] = z[c];
+        a.zs[c] += z[c];
+    }
+    for (int c = 0; c < 9; ++c) a.D1[c] = D[c];
+    adj[i] = a;
+}
+
+__global__ void adj_advance_kernel(int* t_dev) { t_dev[0] -= 1; }
+
 }  // namespace
 
 struct sdfc_sim {
@@ -307,6 +490,15 @@ struct sdfc_sim {
     // captured at the first step and after a precision change
     cudaGraphExec_t round_exec = nullptr;
     cudaStream_t capture_stream = nullptr;
+    // adjoint: the recorded trajectory (step-major, (record_cap + 1) x n x 3), qdot_0,
+    // dL/dq (n x T x 3), per-scene recursion state, gradients, reverse step counter
+    int record_cap = 0, recorded = 0;
+    double *d_qhis = nullptr, *d_qd0rec = nullptr, *d_dfdq = nullptr;
+    size_t dfdq_cap = 0;
+    AdjState* d_adj = nullptr;
+    double* d_gout = nullptr;
+    int* d_t = nullptr;
+    cudaGraphExec_t back_exec = nullptr;
 };
 
 namespace sdfc_impl {
@@ -314,7 +506,11 @@ namespace sdfc_impl {
 void free_sim(sdfc_sim* s) {
     if (!s) return;
     if (s->round_exec) cudaGraphExecDestroy(s->round_exec);
+    if (s->back_exec) cudaGraphExecDestroy(s->back_exec);
     if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
+    cudaFree(s->d_qhis);
+    cudaFree(s->d_qd0rec);
+    cudaFree(s->d_dfdq);
     for (void* p : s->allocations) cudaFree(p);
     if (s->h_remaining) cudaFreeHost(s->h_remaining);
     if (s->batch) sdfc_impl::free_batch(s->batch);
@@ -409,7 +605,8 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         (rc = alloc(s, &s->d_fm, 12 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_Km, 144 * (size_t)n_pairs)) ||
         (rc = alloc(s, &s->d_Dm, 144 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_nact, n_pairs)) ||
         (rc = alloc(s, &s->d_status, n_pairs)) || (rc = alloc(s, &s->d_conv, n)) ||
-        (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, 1))) {
+        (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, 1)) || (rc = alloc(s, &s->d_adj, n)) ||
+        (rc = alloc(s, &s->d_gout, 12 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2))) {
         free_sim(s);
         return rc;
     }
@@ -455,9 +652,13 @@ int sdfc_sim_set_precision(sdfc_sim* s, int precision) {
     if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
         return fail(s->ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_precision: unknown precision");
     if (s->batch) s->batch->precision = precision;
-    if (s->round_exec) {  // the captured round launches the old precision's kernels
+    if (s->round_exec) {  // the captured rounds launch the old precision's kernels
         cudaGraphExecDestroy(s->round_exec);
         s->round_exec = nullptr;
+    }
+    if (s->back_exec) {
+        cudaGraphExecDestroy(s->back_exec);
+        s->back_exec = nullptr;
     }
     return SDFC_OK;
 }
@@ -469,6 +670,13 @@ int sdfc_sim_set_state(sdfc_sim* s, const double* q, const double* qdot) {
     if (rc) return rc;
     SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_q, q, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, ctx->stream));
     SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd, qdot, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, ctx->stream));
+    if (s->record_cap > 0) {  // a new initial state restarts the recording
+        s->recorded = 0;
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis, s->d_q, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
+                                           ctx->stream));
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd0rec, s->d_qd, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
+                                           ctx->stream));
+    }
     SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return SDFC_OK;
 }
@@ -537,15 +745,142 @@ int capture_round(sdfc_sim* s) {
     return SDFC_OK;
 }
 
+// Captures one reverse step of the adjoint (replayed T times; the step index lives
+// in device memory and the last kernel decrements it).
+int capture_backward(sdfc_sim* s) {
+    sdfc_context* ctx = s->ctx;
+    if (!s->capture_stream)
+        SDFC_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
+    const int n = s->n, np = s->n_pairs, tb = 128;
+    cudaStream_t st = s->capture_stream;
+    cudaGraph_t graph = nullptr;
+    SDFC_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = SDFC_OK;
+    if (np > 0) {
+        adj_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, n, s->d_pair_inst, s->d_role, s->d_Efixed, s->d_mover,
+                                                          s->d_qhis, s->d_t, s->d_EA, s->d_phiA, s->d_EB, s->d_phiB);
+        sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
+        sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
+        rc = sdfc_impl::run_batch(s->batch, in, true, out, st);
+    }
+    if (!rc) {
+        adj_step_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_Km, s->d_Dm,
+                                                         s->d_qhis, s->d_dfdq, s->d_t, s->d_adj, s->d_gout);
+        adj_advance_kernel<<<1, 1, 0, st>>>(s->d_t);
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("sim backward capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->back_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return fail(ctx, SDFC_ERR_CUDA, std::string("sim backward instantiate: ") + cudaGetErrorString(e));
+    return SDFC_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int sdfc_sim_record(sdfc_sim* s, int max_steps) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    if (max_steps < 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_record: max_steps must be >= 0");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (s->back_exec) {  // its kernels hold the old history pointer
+        cudaGraphExecDestroy(s->back_exec);
+        s->back_exec = nullptr;
+    }
+    cudaFree(s->d_qhis);
+    cudaFree(s->d_qd0rec);
+    s->d_qhis = s->d_qd0rec = nullptr;
+    s->record_cap = s->recorded = 0;
+    if (max_steps == 0) return SDFC_OK;
+    const size_t n3 = 3 * (size_t)s->n;
+    if ((rc = dev_alloc(ctx, (void**)&s->d_qhis, sizeof(double) * n3 * ((size_t)max_steps + 1))) ||
+        (rc = dev_alloc(ctx, (void**)&s->d_qd0rec, sizeof(double) * n3))) {
+        cudaFree(s->d_qhis);
+        s->d_qhis = nullptr;
+        return rc;
+    }
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis, s->d_q, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd0rec, s->d_qd, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    s->record_cap = max_steps;
+    return SDFC_OK;
+}
+
+int sdfc_sim_history(sdfc_sim* s, int* steps, double* q_his) {
+    if (!s || !steps) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    if (s->record_cap == 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_history: recording is off");
+    *steps = s->recorded;
+    if (!q_his) return SDFC_OK;
+    const int n = s->n, T1 = s->recorded + 1;
+    std::vector<double> h(3 * (size_t)n * T1);
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), s->d_qhis, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int t = 0; t < T1; ++t)  // step-major on the device, scene-major for the caller
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) q_his[(3 * ((size_t)i * T1 + t)) + c] = h[3 * ((size_t)t * n + i) + c];
+    return SDFC_OK;
+}
+
+int sdfc_sim_backward(sdfc_sim* s, const double* df_dq, double* df_dq0, double* df_dqdot0, double* df_dfext) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    if (!df_dq) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_backward: null df_dq");
+    if (s->record_cap == 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_backward: recording is off");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    const int n = s->n, T = s->recorded, tb = 128;
+    cudaStream_t st = ctx->stream;
+    std::vector<double> g(12 * (size_t)n, 0.0);
+    if (T > 0) {
+        const size_t need = 3 * (size_t)n * T;
+        if (need > s->dfdq_cap) {
+            if (s->back_exec) {  // its kernels hold the old dL/dq pointer
+                cudaGraphExecDestroy(s->back_exec);
+                s->back_exec = nullptr;
+            }
+            cudaFree(s->d_dfdq);
+            s->d_dfdq = nullptr;
+            s->dfdq_cap = 0;
+            if ((rc = dev_alloc(ctx, (void**)&s->d_dfdq, sizeof(double) * need))) return rc;
+            s->dfdq_cap = need;
+        }
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_dfdq, df_dq, sizeof(double) * need, cudaMemcpyHostToDevice, st));
+        adj_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, T, s->d_adj, s->d_t);
+        SDFC_CUDA_TRY(ctx, cudaGetLastError());
+        if (!s->back_exec && (rc = capture_backward(s))) return rc;
+        for (int t = T; t >= 1; --t) SDFC_CUDA_TRY(ctx, cudaGraphLaunch(s->back_exec, st));
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(g.data(), s->d_gout, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, st));
+        SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    }
+    for (int i = 0; i < n; ++i) {
+        const double* gi = &g[12 * (size_t)i];
+        if (df_dq0) std::memcpy(df_dq0 + 3 * (size_t)i, gi, sizeof(double) * 3);
+        if (df_dqdot0) std::memcpy(df_dqdot0 + 3 * (size_t)i, gi + 3, sizeof(double) * 3);
+        if (df_dfext) std::memcpy(df_dfext + 6 * (size_t)i, gi + 6, sizeof(double) * 6);
+    }
+    return SDFC_OK;
+}
 
 int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
     if (!s || num_steps < 0) return SDFC_ERR_INVALID_ARGUMENT;
     sdfc_context* ctx = s->ctx;
     int rc = use_device(ctx);
     if (rc) return rc;
+    if (s->record_cap > 0 && s->recorded + num_steps > s->record_cap)
+        return fail(ctx, SDFC_ERR_CAPACITY, "sim_step: more steps than sdfc_sim_record's max_steps");
     if (!s->round_exec && (rc = capture_round(s))) return rc;
     cudaStream_t st = ctx->stream;
     const int n = s->n;
@@ -564,6 +899,11 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
             if (active == 0) break;
         }
         sim_end_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_mover, s->d_state, s->d_q, s->d_qd, s->d_conv);
+        if (s->record_cap > 0) {
+            ++s->recorded;
+            SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis + 3 * (size_t)n * s->recorded, s->d_q, sizeof(double) * 3 * n,
+                                               cudaMemcpyDeviceToDevice, st));
+        }
     }
     SDFC_CUDA_TRY(ctx, cudaGetLastError());
     if (converged)

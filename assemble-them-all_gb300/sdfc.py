@@ -26,7 +26,7 @@ EXPORTS = (
     "sdfc_batch_set_derivative_mode", "sdfc_batch_set_timing", "sdfc_batch_last_timing", "sdfc_set_precision",
     "sdfc_batch_set_precision", "sdfc_evaluate_noalloc", "sdfc_sim_create", "sdfc_sim_destroy",
     "sdfc_sim_set_precision", "sdfc_sim_set_state", "sdfc_sim_get_state", "sdfc_sim_set_external_force",
-    "sdfc_sim_step", "sdfc_sim_stats",
+    "sdfc_sim_step", "sdfc_sim_stats", "sdfc_sim_record", "sdfc_sim_history", "sdfc_sim_backward",
 )
 JOINT_TRANSLATIONAL = 3
 PRECISION_FP64 = 0
@@ -118,6 +118,9 @@ def lib():
         L.sdfc_sim_set_external_force.argtypes = [v, d]
         L.sdfc_sim_step.argtypes = [v, i, P(i)]
         L.sdfc_sim_stats.argtypes = [v, P(ctypes.c_longlong), P(ctypes.c_longlong)]
+        L.sdfc_sim_record.argtypes = [v, i]
+        L.sdfc_sim_history.argtypes = [v, P(i), d]
+        L.sdfc_sim_backward.argtypes = [v, d, d, d, d]
         L.sdfc_evaluate_noalloc.argtypes = [v, i, i, i, d, d, d, ctypes.c_double, v, i, v, v, v, v, v, i, v, v, v,
                                             v, v]
         L.sdfc_batch_set_precision.argtypes = [v, i]
@@ -314,6 +317,7 @@ class Sim:
         self._h = ctypes.c_void_p()
         ctx._check(lib().sdfc_sim_create(ctx._h, self.n, marr, len(pairs), parr, ctypes.byref(self._h)),
                    "sdfc_sim_create")
+        self.generation = 0  # bumped by every call that changes the state or the recording
 
     def close(self):
         if self._h and self.ctx._h:
@@ -324,6 +328,7 @@ class Sim:
         self.ctx._check(lib().sdfc_sim_set_precision(self._h, int(precision)), "sdfc_sim_set_precision")
 
     def set_state(self, q, qdot):
+        self.generation += 1
         self.ctx._check(lib().sdfc_sim_set_state(self._h, _dp(_f64(q, 3 * self.n)), _dp(_f64(qdot, 3 * self.n))),
                         "sdfc_sim_set_state")
 
@@ -333,10 +338,12 @@ class Sim:
         return q.reshape(self.n, 3), qd.reshape(self.n, 3)
 
     def set_external_force(self, f):
+        self.generation += 1
         self.ctx._check(lib().sdfc_sim_set_external_force(self._h, _dp(_f64(f, 6 * self.n))),
                         "sdfc_sim_set_external_force")
 
     def step(self, num_steps=1):
+        self.generation += 1
         conv = np.zeros(self.n, dtype=np.int32)
         self.ctx._check(lib().sdfc_sim_step(self._h, int(num_steps), _ip(conv)), "sdfc_sim_step")
         return conv.astype(bool)
@@ -345,3 +352,31 @@ class Sim:
         r, e = ctypes.c_longlong(), ctypes.c_longlong()
         self.ctx._check(lib().sdfc_sim_stats(self._h, ctypes.byref(r), ctypes.byref(e)), "sdfc_sim_stats")
         return r.value, e.value
+
+    # adjoint (Simulation::reset(backward_flag=True) / get_q_his / backward)
+    def record(self, max_steps: int):
+        """Record the trajectory from the current state for up to max_steps steps (0 stops)."""
+        self.generation += 1
+        self.ctx._check(lib().sdfc_sim_record(self._h, int(max_steps)), "sdfc_sim_record")
+
+    def history(self):
+        """Recorded joint trajectory, shape (n, T+1, 3), q_0 first."""
+        T = ctypes.c_int()
+        self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), None), "sdfc_sim_history")
+        q = np.zeros((self.n, T.value + 1, 3))
+        self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), _dp(q)), "sdfc_sim_history")
+        return q
+
+    def backward(self, df_dq):
+        """Simulation::backward_BDF1 over the recorded steps for dL/dq_k (n, T, 3):
+        returns dL/dq0 (n, 3), dL/dqdot0 (n, 3), dL/d(external force) (n, 6)."""
+        df_dq = np.ascontiguousarray(df_dq, dtype=np.float64)
+        if df_dq.ndim != 3 or df_dq.shape[0] != self.n or df_dq.shape[2] != 3:
+            raise ValueError("df_dq must have shape (n, T, 3)")
+        T = ctypes.c_int()
+        self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), None), "sdfc_sim_history")
+        if df_dq.shape[1] != T.value:
+            raise ValueError(f"df_dq covers {df_dq.shape[1]} steps, {T.value} recorded")
+        g0, gd0, gf = np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros((self.n, 6))
+        self.ctx._check(lib().sdfc_sim_backward(self._h, _dp(df_dq), _dp(g0), _dp(gd0), _dp(gf)), "sdfc_sim_backward")
+        return g0, gd0, gf

@@ -223,6 +223,26 @@ int sdfc_sim_step(sdfc_sim* sim, int num_steps, int* converged);
  * force evaluations (diagnostic). */
 int sdfc_sim_stats(sdfc_sim* sim, long long* rounds, long long* evaluations);
 
+/* Adjoint of the rollout (Simulation::reset(backward_flag = true) + Simulation::backward,
+ * simulation/redmax/Simulation.cpp:1512-1634, integrator BDF1).
+ * sdfc_sim_record starts recording at the current state (q_0, qdot_0) for at most
+ * max_steps steps (sdfc_sim_step fails with SDFC_ERR_CAPACITY beyond it; 0 stops
+ * recording).  Only the joint trajectory is kept (n x 3 doubles per step) where the
+ * reference stores H_lu, M, D per step (BackwardData.h); the backward pass recomputes
+ * each step's H and D from it.  sdfc_sim_set_state restarts the recording. */
+int sdfc_sim_record(sdfc_sim* sim, int max_steps);
+/* Recorded steps T and, if q_his is not NULL, the trajectory (host, n x (T+1) x 3,
+ * q_0 first): Simulation::get_q_his. */
+int sdfc_sim_history(sdfc_sim* sim, int* steps, double* q_his);
+/* Simulation::backward_BDF1 for every scene over the T recorded steps.
+ * df_dq (host, n x T x 3): dL/dq_k for k = 1..T (BackwardInfo::_df_dq).
+ * Outputs (host, may be NULL): df_dq0 (n x 3) and df_dqdot0 (n x 3), the reference's
+ * BackwardResults::_df_dq0/_df_dqdot0 with zero direct terms, and df_dfext (n x 6,
+ * world frame, torque then force like sdfc_sim_set_external_force), which the
+ * reference does not compute: dL/d(external force), the force held constant over the
+ * T steps. */
+int sdfc_sim_backward(sdfc_sim* sim, const double* df_dq, double* df_dq0, double* df_dqdot0, double* df_dfext);
+
 /* ---------------------------------------------------------------- allocation-free evaluation */
 
 /* No counterpart in the reference.  For callers that cannot allocate device

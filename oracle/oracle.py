@@ -241,6 +241,12 @@ def _lib_sim():
         L.orc_bdf1_step.argtypes = [P(_Mover), P(_Pair), ctypes.c_int, P(d), P(d), P(ctypes.c_int), P(ctypes.c_int)]
         L.orc_bdf1_eval.restype = None
         L.orc_bdf1_eval.argtypes = [P(_Mover), P(_Pair), ctypes.c_int, P(d), P(d), P(d), P(d), P(d)]
+        L.orc_bdf1_eval_full.restype = None
+        L.orc_bdf1_eval_full.argtypes = [P(_Mover), P(_Pair), ctypes.c_int, P(d), P(d), P(d), P(d), P(d), P(d),
+                                         P(d)]
+        L.orc_bdf1_backward.restype = None
+        L.orc_bdf1_backward.argtypes = [P(_Mover), P(_Pair), ctypes.c_int, P(d), P(d), ctypes.c_int, P(d), P(d),
+                                        P(d), P(d)]
         L._sim_ready = True
     return L
 
@@ -287,3 +293,30 @@ def bdf1_eval(mover: Mover, pairs, q0, qdot0, q1, want_H=True):
     L.orc_bdf1_eval(ctypes.byref(m), arr, len(pairs), _dp(_f64(q0)), _dp(_f64(qdot0)), _dp(_f64(q1)), _dp(g),
                     _dp(H) if want_H else None)
     return g, H.reshape(3, 3)
+
+
+def bdf1_matrices(mover: Mover, pairs, q0, qdot0, q1):
+    """g, H, M, D of BDF1 at q1: the step data integration_BDF1 saves for the adjoint
+    (Simulation.cpp:1114-1163, 1262-1269)."""
+    L = _lib_sim()
+    m = mover._c()
+    arr, keep = _pairs_c(pairs)
+    g, H, M, D = np.zeros(3), np.zeros(9), np.zeros(9), np.zeros(9)
+    L.orc_bdf1_eval_full(ctypes.byref(m), arr, len(pairs), _dp(_f64(q0)), _dp(_f64(qdot0)), _dp(_f64(q1)), _dp(g),
+                         _dp(H), _dp(M), _dp(D))
+    return g, H.reshape(3, 3), M.reshape(3, 3), D.reshape(3, 3)
+
+
+def bdf1_backward(mover: Mover, pairs, q_his, qdot0, df_dq):
+    """Simulation::backward_BDF1 (Simulation.cpp:1559-1634) from a trajectory q_his[T+1, 3]
+    and dL/dq_k[T, 3]; returns (dL/dq0, dL/dqdot0, dL/df_ext[6])."""
+    L = _lib_sim()
+    m = mover._c()
+    arr, keep = _pairs_c(pairs)
+    q_his = _f64(q_his).reshape(-1, 3)
+    T = len(q_his) - 1
+    df_dq = _f64(df_dq).reshape(T, 3)
+    g0, gd0, gf = np.zeros(3), np.zeros(3), np.zeros(6)
+    L.orc_bdf1_backward(ctypes.byref(m), arr, len(pairs), _dp(q_his), _dp(_f64(qdot0)), T, _dp(df_dq), _dp(g0),
+                        _dp(gd0), _dp(gf))
+    return g0, gd0, gf

@@ -832,6 +832,12 @@ void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, dou
  * only has angular rows, which J^T drops) plus every contact's mover block. */
 void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0, const double* qdot0,
                    const double* q1, double* g, double* H) {
+    orc_bdf1_eval_full(m, pairs, n_pairs, q0, qdot0, q1, g, H, NULL, NULL);
+}
+
+void orc_bdf1_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
+                        const double* qdot0, const double* q1, double* g, double* H, double* M_out,
+                        double* D_out) {
     const double h = m->h;
     double qd1[3], E0i[16], phi[6], R0i[9], p0i[3], Rji[9], pji[3];
     for (int k = 0; k < 3; ++k) qd1[k] = (q1[k] - q0[k]) / h;
@@ -890,7 +896,9 @@ void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const
             D[4 * k] -= m->joint_damping;
         }
         for (int k = 0; k < 9; ++k) H[k] = M[k] - h * h * K[k] - h * D[k];
+        if (D_out) memcpy(D_out, D, sizeof D);
     }
+    if (M_out) memcpy(M_out, M, sizeof M);
 }
 
 /* 3x3 solve by Gaussian elimination with partial pivoting (the algorithm of Eigen's
@@ -976,4 +984,129 @@ int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double
     if (iters) *iters = it + (converged ? 1 : 0);
     if (evals) *evals = ev;
     return converged;
+}
+
+/* ------------------------------------------------------------------ adjoint of the BDF1 rollout */
+
+/* Partial-pivoting LU of a 3x3 (PA = LU, L unit lower, stored in one array) and the
+ * solve of A^T z = y with those factors (Eigen's PartialPivLU::transpose().solve, which
+ * the reference calls at Simulation.cpp:1587): U^T w = y, L^T u = w, z = P^T u. */
+static void lu3(const double* A_in, double* LU, int* perm) {
+    memcpy(LU, A_in, 9 * sizeof(double));
+    for (int k = 0; k < 3; ++k) perm[k] = k;
+    for (int c = 0; c < 3; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 3; ++r)
+            if (fabs(LU[3 * r + c]) > fabs(LU[3 * p + c])) p = r;
+        if (p != c) {
+            for (int k = 0; k < 3; ++k) {
+                double t = LU[3 * c + k];
+                LU[3 * c + k] = LU[3 * p + k];
+                LU[3 * p + k] = t;
+            }
+            int t = perm[c];
+            perm[c] = perm[p];
+            perm[p] = t;
+        }
+        for (int r = c + 1; r < 3; ++r) {
+            LU[3 * r + c] /= LU[3 * c + c];
+            for (int k = c + 1; k < 3; ++k) LU[3 * r + k] -= LU[3 * r + c] * LU[3 * c + k];
+        }
+    }
+}
+
+static void lu3_solve_transposed(const double* LU, const int* perm, const double* y, double* z) {
+    double w[3], u[3];
+    for (int r = 0; r < 3; ++r) { /* U^T w = y */
+        double s = y[r];
+        for (int k = 0; k < r; ++k) s -= LU[3 * k + r] * w[k];
+        w[r] = s / LU[3 * r + r];
+    }
+    for (int r = 2; r >= 0; --r) { /* L^T u = w */
+        double s = w[r];
+        for (int k = r + 1; k < 3; ++k) s -= LU[3 * k + r] * u[k];
+        u[r] = s;
+    }
+    for (int r = 0; r < 3; ++r) z[perm[r]] = u[r];
+}
+
+/* Simulation::backward_BDF1 (Simulation.cpp:1559-1634) for one translational mover, with
+ * the per-step H, M, D that the reference saves after each converged step
+ * (integration_BDF1, :1262-1269, evaluating evaluate_g_with_derivatives_BDF1 at q_k with
+ * qdot_k = (q_k - q_{k-1}) / h) recomputed here from the trajectory q_his[0..T].
+ * df_dq[T x 3] is dL/dq_k for k = 1..T.  Outputs dL/dq_0, dL/dqdot_0 and, beyond the
+ * reference, dL/df_ext (world-frame external force: the torque rows are 0 because the
+ * translational joint's J has no angular part): df_ext's direct term in f is
+ * R_ji diag(m) R_0i^T fe, so dL/dfe = h^2 R_0i diag(m) R_ji^T sum_k z_k. */
+void orc_bdf1_backward(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q_his,
+                       const double* qdot0, int T, const double* df_dq, double* df_dq0, double* df_dqdot0,
+                       double* df_dfext) {
+    const double h = m->h;
+    double* Ms = (double*)calloc((size_t)(T > 0 ? T : 1) * 27, sizeof(double));
+    double* Ds = Ms + 9 * (size_t)(T > 0 ? T : 1);
+    double* Hs = Ds + 9 * (size_t)(T > 0 ? T : 1);
+    double* z = (double*)calloc((size_t)(T > 0 ? T : 1) * 3, sizeof(double));
+    for (int k = 1; k <= T; ++k) { /* the saved step data */
+        double qd_prev[3], g[3];
+        const double* qp = q_his + 3 * (k - 1);
+        if (k == 1) {
+            memcpy(qd_prev, qdot0, sizeof qd_prev);
+        } else {
+            for (int c = 0; c < 3; ++c) qd_prev[c] = (qp[c] - q_his[3 * (k - 2) + c]) / h;
+        }
+        orc_bdf1_eval_full(m, pairs, n_pairs, qp, qd_prev, q_his + 3 * k, g, Hs + 9 * (k - 1), Ms + 9 * (k - 1),
+                           Ds + 9 * (k - 1));
+    }
+    for (int k = T - 1; k >= 0; --k) { /* z_k for step k + 1 */
+        double y[3], t[3], LU[9];
+        int perm[3];
+        for (int c = 0; c < 3; ++c) y[c] = df_dq[3 * k + c];
+        if (k < T - 1) {
+            double A[9];
+            for (int c = 0; c < 9; ++c) A[c] = -2.0 * Ms[9 * (k + 1) + c] + h * Ds[9 * (k + 1) + c];
+            m3t_vec(A, z + 3 * (k + 1), t);
+            for (int c = 0; c < 3; ++c) y[c] -= t[c];
+        }
+        if (k < T - 2) {
+            m3t_vec(Ms + 9 * (k + 2), z + 3 * (k + 2), t);
+            for (int c = 0; c < 3; ++c) y[c] -= t[c];
+        }
+        lu3(Hs + 9 * k, LU, perm);
+        lu3_solve_transposed(LU, perm, y, z + 3 * k);
+    }
+    double g0[3] = {0, 0, 0}, gd0[3] = {0, 0, 0}, t[3];
+    if (T > 0) {
+        double A[9], B[9];
+        for (int c = 0; c < 9; ++c) {
+            A[c] = -Ms[c] + h * Ds[c];
+            B[c] = -h * Ms[c];
+        }
+        m3t_vec(A, z, t);
+        for (int c = 0; c < 3; ++c) g0[c] -= t[c];
+        m3t_vec(B, z, t);
+        for (int c = 0; c < 3; ++c) gd0[c] -= t[c];
+    }
+    if (T > 1) {
+        m3t_vec(Ms + 9, z + 3, t);
+        for (int c = 0; c < 3; ++c) g0[c] -= t[c];
+    }
+    if (df_dq0) memcpy(df_dq0, g0, sizeof g0);
+    if (df_dqdot0) memcpy(df_dqdot0, gd0, sizeof gd0);
+    if (df_dfext) {
+        double zs[3] = {0, 0, 0}, E0i[16], phi[6], R0i[9], p0i[3], Rji[9], pji[3], v[3], w[3];
+        for (int k = 0; k < T; ++k)
+            for (int c = 0; c < 3; ++c) zs[c] += z[3 * k + c];
+        orc_mover_pose(m, q_his, qdot0, E0i, phi); /* R_0i is the same at every q */
+        pose_split(E0i, R0i, p0i);
+        pose_split(m->E_ji, Rji, pji);
+        m3t_vec(Rji, zs, v);
+        for (int c = 0; c < 3; ++c) v[c] *= m->inertia[3 + c];
+        m3_vec(R0i, v, w);
+        for (int c = 0; c < 3; ++c) {
+            df_dfext[c] = 0.0;
+            df_dfext[3 + c] = h * h * w[c];
+        }
+    }
+    free(Ms);
+    free(z);
 }

@@ -82,10 +82,20 @@ void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, dou
 /* g and H of BDF1 at q1 (Simulation::evaluate_g[_with_derivatives]_BDF1), H may be NULL. */
 void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0, const double* qdot0,
                    const double* q1, double* g, double* H);
+/* orc_bdf1_eval plus the reduced M and D = df/dqdot at q1 (either may be NULL). */
+void orc_bdf1_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
+                        const double* qdot0, const double* q1, double* g, double* H, double* M, double* D);
 /* One implicit-Euler step (Simulation::integration_BDF1 + newton); updates q, qdot.
  * Returns 1 if Newton converged.  iters / evals may be NULL. */
 int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double* q, double* qdot, int* iters,
                   int* evals);
+
+/* Adjoint of T BDF1 steps (Simulation::backward_BDF1) from the trajectory q_his[(T+1) x 3]
+ * and qdot_0: dL/dq_0, dL/dqdot_0 and dL/df_ext[6] for dL/dq_k = df_dq[(k-1) x 3].
+ * Any output may be NULL. */
+void orc_bdf1_backward(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q_his,
+                       const double* qdot0, int T, const double* df_dq, double* df_dq0, double* df_dqdot0,
+                       double* df_dfext);
 
 #ifdef __cplusplus
 }

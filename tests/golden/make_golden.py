@@ -153,11 +153,22 @@ def make_sim_fixture(steps=40):
         qs.append(q)
         qds.append(qd)
         conv.append(sim.is_converged())
+    # the reference's adjoint (Simulation::backward_BDF1, Simulation.cpp:1559-1634) of a loss whose
+    # gradient with respect to every q_k is a seeded random vector
+    T_bw = 20
+    df_dq = np.random.default_rng(99).normal(size=(T_bw, 3))
+    sim.set_state_init(q0, qd0)
+    sim.reset(True)
+    sim.set_external_force("A", F)
+    sim.forward(T_bw)
+    df_dq0, df_dqdot0 = sim.backward(df_dq.ravel(), T_bw)
     np.savez_compressed(os.path.join(HERE, "sim_trans.npz"), grid=vals, min_box=mn, max_box=mx, dx=dx,
                         col_th=COL_TH, points=pts, mass=mA, inertia=IA, E_ji=EjiA, E_fixed=E0iB,
                         params=np.array([f32(kn), f32(kt), f32(mu), f32(kd), 1.0, 1.0]), h=f32(h),
                         gravity=np.array(gravity), f_ext=F, q0=q0, qdot0=qd0, q=np.array(qs), qdot=np.array(qds),
-                        converged=np.array(conv))
+                        converged=np.array(conv), bw_steps=T_bw, bw_df_dq=df_dq, bw_df_dq0=df_dq0,
+                        bw_df_dqdot0=df_dqdot0)
+    print("reference adjoint: df_dq0", df_dq0, "df_dqdot0", df_dqdot0)
     print("sim trajectory: final q", qs[-1], "all converged", all(conv))
 
 
