@@ -50,8 +50,6 @@ void free_batch(sdfc_batch* b) {
     cudaFree(b->d_tile_queue);
     cudaFree(b->d_prefilter);
     cudaFree(b->d_partial);
-    cudaFree(b->d_squeue);
-    cudaFree(b->d_squeue_count);
     cudaFree(b->d_recheck);
     cudaFree(b->d_in);
     cudaFree(b->d_out);
@@ -67,8 +65,7 @@ void free_batch(sdfc_batch* b) {
 int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
               cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
-    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids,     b->d_tile_count,  b->d_tile_queue,
-                          b->d_partial,   b->d_recheck, b->d_squeue,      b->d_squeue_count};
+    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck};
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     if (b->timing) cudaEventRecord(b->ev[0], stream);
@@ -164,8 +161,6 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_tile_count, sizeof(int) * std::max(tiles, 1))) ||
         (rc = alloc((void**)&b->d_tile_queue, sizeof(int) * std::max(tiles, 1))) ||
         (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
-        (rc = alloc((void**)&b->d_squeue, sizeof(int) * sdfc::squeue_capacity(n, tiles))) ||
-        (rc = alloc((void**)&b->d_squeue_count, sizeof(int) * (size_t)n * sdfc::kSlots)) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
@@ -186,7 +181,6 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     if (e == cudaSuccess) e = cudaMemset(b->d_recheck, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(b->d_tile_count, 0, sizeof(int) * std::max(tiles, 1));
     if (e == cudaSuccess) e = cudaMemset(b->d_tile_queue, 0, sizeof(int) * std::max(tiles, 1));
-    if (e == cudaSuccess) e = cudaMemset(b->d_squeue_count, 0, sizeof(int) * (size_t)n * sdfc::kSlots);
     if (e != cudaSuccess) {
         free_batch(b);
         return fail(ctx, SDFC_ERR_CUDA, std::string("batch_create: ") + cudaGetErrorString(e));

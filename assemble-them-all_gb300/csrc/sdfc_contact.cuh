@@ -308,6 +308,50 @@ __device__ inline void sdf_stencil(const GridDesc& g, V3 x, V3& grad, double* he
     }
 }
 
+// sdf_stencil with its 19 queries spread over the lanes of one warp.  Every lane
+// of the warp must call it with the same x (warp-uniform control flow, all 32
+// lanes active).  Lane l < 19 evaluates one query point, the values are
+// exchanged by shuffles and every lane combines them in sdf_stencil's operation
+// order, so the results are bit-identical to sdf_stencil's.
+__device__ inline void sdf_stencil_warp(const GridDesc& g, V3 x, V3& grad, double* hess, bool want_hessian,
+                                        double& centre) {
+    const int lane = threadIdx.x & 31;
+    const double e = kFdEps, h = kFdEps / 2;
+    double c[3] = {x.x, x.y, x.z};
+    if (lane < 3) {  // gp[a]
+        c[lane] = c[lane] + e;
+    } else if (lane < 6) {  // gm[a]
+        c[lane - 3] = c[lane - 3] - e;
+    } else if (lane >= 7 && lane < 19) {  // mixed pair q: pp, mm, pm, mp
+        const int q = (lane - 7) >> 2, kind = (lane - 7) & 3;
+        const int a = q < 2 ? 0 : 1, b = q == 0 ? 1 : 2;
+        const double ca = c[a], cb = c[b];
+        c[a] = (kind == 0 || kind == 2) ? ca + h : ca - h;
+        c[b] = (kind == 0 || kind == 3) ? cb + h : cb - h;
+    }  // lane 6: the centre
+    const double v = lane < 19 ? query_sdf(g, v3(c[0], c[1], c[2]), true) : 0.0;
+    double gp[3], gm[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        gp[a] = __shfl_sync(0xffffffffu, v, a);
+        gm[a] = __shfl_sync(0xffffffffu, v, 3 + a);
+    }
+    grad = v3((gp[0] - gm[0]) / (2 * e), (gp[1] - gm[1]) / (2 * e), (gp[2] - gm[2]) / (2 * e));
+    const double xs = __shfl_sync(0xffffffffu, v, 6);
+    centre = xs;
+    if (!want_hessian) return;
+    const double ee = e * e;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) hess[a] = sub_rn(add_rn(gp[a], gm[a]), mul_rn(2.0, xs)) / ee;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double vpp = __shfl_sync(0xffffffffu, v, 7 + 4 * q), vmm = __shfl_sync(0xffffffffu, v, 8 + 4 * q);
+        const double vpm = __shfl_sync(0xffffffffu, v, 9 + 4 * q), vmp = __shfl_sync(0xffffffffu, v, 10 + 4 * q);
+        const double s = vpp + vmm - vpm - vmp;
+        hess[3 + q] = s / ee;
+    }
+}
+
 // True when the reference's stencil around x stays inside x's cell on every
 // axis (no stencil point in another cell or outside the box, and the cell is
 // not the clamped top cell).  The test keeps a margin of 2 eps from the
@@ -456,6 +500,51 @@ __device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const M3& RT, V
     return c;
 }
 
+// A contact's grid-frame point and SDF jet from the exact path, computed ahead
+// of contact_geometry by the whole warp (warp_exact_jets).
+template <typename T>
+struct ExactJet {
+    V3 x;
+    SdfJet<T> J;
+    bool set;
+};
+
+// The exact path for the warp's contacts whose derivative stencil leaves their
+// cell (`mine`): the reference-order grid point and depth, and the stencil
+// derivatives with their 19 queries spread over the warp's lanes, one contact
+// at a time, so that no lane walks a 19-query FP64 chain alone.  Must be called
+// by all 32 lanes.  Results equal sdf_jet's on the exact path.
+template <typename T>
+__device__ inline void warp_exact_jets(const GridDesc& g, const PairState<T>& S, V3 xi, bool mine, bool want_hessian,
+                                       ExactJet<T>& ej) {
+    ej.set = false;
+    V3 x = v3(0, 0, 0);
+    bool stencil = false;
+    if (mine) {
+        x = grid_point(S.B.P.R, S.B.P.p, world_point(S.A.P.R, S.A.P.p, xi));
+        // inside a cell the exact path takes the cell's own derivatives (sdf_jet)
+        stencil = !(in_box(g, x) && stencil_in_cell(g, cell_of(g, x)));
+    }
+    unsigned m = __ballot_sync(0xffffffffu, stencil);
+    const int lane = threadIdx.x & 31;
+    while (m) {
+        const int o = __ffs(m) - 1;
+        m &= m - 1;
+        const V3 xo = v3(__shfl_sync(0xffffffffu, x.x, o), __shfl_sync(0xffffffffu, x.y, o),
+                         __shfl_sync(0xffffffffu, x.z, o));
+        V3 gr;
+        double hs[6], centre;
+        sdf_stencil_warp(g, xo, gr, hs, want_hessian, centre);
+        if (lane == o) {
+            ej.set = true;
+            ej.x = xo;
+            ej.J.v = in_box(g, xo) ? centre : (double)FLT_MAX;
+            ej.J.g = cast<T>(gr);
+            for (int k = 0; k < 6; ++k) ej.J.h[k] = want_hessian ? (T)hs[k] : T(0);
+        }
+    }
+}
+
 // Grid-frame point, depth and SDF jet of one contact.
 //   Exact path (T = double, the stencil mode, and contacts whose stencil
 //   leaves the cell): the reference's operation order, bit-identical depth.
@@ -468,13 +557,19 @@ __device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const M3& RT, V
 template <typename T>
 __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S, V3 xi, const FastCell* fc,
                                         bool want_hessian, bool valid, bool stencil_only, V3& x, double& d,
-                                        SdfJet<T>& J) {
+                                        SdfJet<T>& J, const ExactJet<T>* ej = nullptr) {
     if (!valid) {
         x = xi;
         d = -1.0;
         J.v = -1.0;
         J.g = vec3<T>(1, 0, 0);
         for (int k = 0; k < 6; ++k) J.h[k] = T(0);
+        return;
+    }
+    if (ej && ej->set) {  // computed by the warp (warp_exact_jets)
+        x = ej->x;
+        J = ej->J;
+        d = J.v + g.col_th;
         return;
     }
     if constexpr (std::is_same<T, float>::value) {
@@ -555,11 +650,11 @@ struct ContactForce {
 
 template <typename T>
 __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
-                                                bool valid, bool stencil_only) {
+                                                bool valid, bool stencil_only, const ExactJet<T>* ej = nullptr) {
     V3 xd;
     double dd;
     SdfJet<T> J;
-    contact_geometry(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J);
+    contact_geometry(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;
@@ -610,12 +705,13 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
 // Dm columns), sink.column(c, N1, N2, T2) receives the column's factors.
 template <typename T, class Sink>
 __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
-                                              Sink& sink, bool valid, bool stencil_only) {
+                                              Sink& sink, bool valid, bool stencil_only,
+                                              const ExactJet<T>* ej = nullptr) {
     // collision, :292-310
     V3 xd;
     double dd;
     SdfJet<T> J;
-    contact_geometry(g, S, xi1d, fc, true, valid, stencil_only, xd, dd, J);
+    contact_geometry(g, S, xi1d, fc, true, valid, stencil_only, xd, dd, J, ej);
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;

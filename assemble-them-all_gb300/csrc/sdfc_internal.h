@@ -43,8 +43,6 @@ struct sdfc_batch {
     sdfc::Prefilter* d_prefilter = nullptr;
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
-    int* d_squeue = nullptr;
-    int* d_squeue_count = nullptr;
     // staging of the host-array entry points
     double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
     double* d_out = nullptr;  // n x 300: fm | Km | Dm

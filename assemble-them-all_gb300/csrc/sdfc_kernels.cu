@@ -350,17 +350,17 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
                                                        const PointsDesc* __restrict__ points,
                                                        const int* __restrict__ ids,
                                                        const int* __restrict__ tile_count,
-                                                       double* __restrict__ partial, int* __restrict__ squeue,
-                                                       int* __restrict__ squeue_count) {
+                                                       double* __restrict__ partial) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     constexpr int NW = kChunk / 32;
-    constexpr bool kDefer = std::is_same<T, float>::value && !STENCIL;
+    // FP32 algebra: contacts whose derivative stencil leaves the cell take the
+    // exact path with the warp's help (warp_exact_jets)
+    constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
     __shared__ Accum<T> acc[NW * NV];
     __shared__ int prefix[kMaxTilesPerInstance + 1];
     __shared__ GridDesc g;
     __shared__ PointsDesc P;
     __shared__ PairState<T> S;
-    __shared__ int wq[NW], qbase;
     const int i = blockIdx.y, s = blockIdx.x;
     if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -387,11 +387,9 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
                         in.phiB + 6 * (size_t)i, in.prm + 6 * (size_t)i, S);
     }
     for (int k = tid; k < NW * NV; k += kChunk) acc[k].zero();
-    if (tid == 0) qbase = 0;
     __syncthreads();
     const int total = prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
-    int* queue = squeue + squeue_offset(i, I.tile0, I.ntiles, s);
     if (s < nchunks) {
         for (int chunk = s; chunk < nchunks; chunk += kSlots) {
             const int c = chunk * kChunk + tid;
@@ -412,35 +410,22 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             }
             FastCell fc;
             const FastCell* fcp = nullptr;
-            bool here = valid;
-            if constexpr (kDefer) {
+            ExactJet<T> ej;
+            const ExactJet<T>* ejp = nullptr;
+            if constexpr (kWarpExact) {
                 fc = fast_cell<T>(g, S.RT, S.pT, xi);
                 fcp = &fc;
-                const bool defer = valid && !fc.ok;
-                here = valid && fc.ok;
-                // queue the deferred contacts of this chunk in order
-                const unsigned m = __ballot_sync(kFull, defer);
-                if (lane == 0) wq[warp] = __popc(m);
-                __syncthreads();
-                int off = qbase;
-                for (int w = 0; w < warp; ++w) off += wq[w];
-                if (defer) queue[off + __popc(m & ((1u << lane) - 1u))] = sid;
-                __syncthreads();
-                if (tid == 0)
-                    for (int w = 0; w < NW; ++w) qbase += wq[w];
+                warp_exact_jets<T>(g, S, xi, valid && !fc.ok, DERIV, ej);
+                ejp = &ej;
             }
-            WarpSink<NV, T> sink{acc + warp * NV, lane, here, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
+            WarpSink<NV, T> sink{acc + warp * NV, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
             if constexpr (DERIV) {
-                contact_force_jacobian<T>(g, xi, S, fcp, sink, here, STENCIL);
+                contact_force_jacobian<T>(g, xi, S, fcp, sink, valid, STENCIL, ejp);
             } else {
-                ContactForce<T> F = contact_force<T>(g, xi, S, fcp, here, STENCIL);
+                ContactForce<T> F = contact_force<T>(g, xi, S, fcp, valid, STENCIL, ejp);
                 sink.force(F.xi1, F.f1, F.xi2, F.f2);
             }
         }
-    }
-    if constexpr (kDefer) {
-        __syncthreads();
-        if (tid == 0) squeue_count[(size_t)i * kSlots + s] = qbase;
     }
     __syncthreads();
     double* row = partial + ((size_t)i * kSlots + s) * NV;
@@ -448,71 +433,6 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
         double v = 0.0;
         for (int w = 0; w < NW; ++w) v += acc[w * NV + k].value();
         row[k] = v;
-    }
-}
-
-// Per-thread sink of stencil_kernel: adds each value of one contact, in FP64,
-// straight into the thread's own (instance, slot) partial row.
-template <int NV, typename T>
-struct LaneSink {
-    double* row;
-    Vec3<T> xi1, xi2;
-    __device__ __forceinline__ void add3(int idx, int stride, Vec3<T> v) {
-        row[idx] += (double)v.x;
-        row[idx + stride] += (double)v.y;
-        row[idx + 2 * stride] += (double)v.z;
-    }
-    __device__ __forceinline__ void force(Vec3<T> a1, Vec3<T> f1, Vec3<T> a2, Vec3<T> f2) {
-        xi1 = a1;
-        xi2 = a2;
-        add3(0, 1, cross(a1, f1));
-        add3(3, 1, f1);
-        add3(6, 1, cross(a2, f2));
-        add3(9, 1, f2);
-    }
-    __device__ __forceinline__ void column(int c, Vec3<T> N1, Vec3<T> N2, Vec3<T> T2) {
-        if constexpr (NV == kOutDeriv) {
-            const int base = c < 12 ? 12 + c : 156 + (c - 12);
-            add3(base, 12, cross(xi1, N1));
-            add3(base + 36, 12, N1);
-            add3(base + 72, 12, cross(xi2, N2) + T2);
-            add3(base + 108, 12, N2);
-        }
-    }
-};
-
-// The contacts force_kernel deferred: one thread per (instance, slot) queue,
-// each contact through the exact path, in queue order.
-template <bool DERIV>
-__global__ void __launch_bounds__(128) stencil_kernel(const InstanceDesc* __restrict__ inst, int n_inst, BatchInputs in,
-                                                      const GridDesc* __restrict__ grids,
-                                                      const PointsDesc* __restrict__ points,
-                                                      const int* __restrict__ squeue,
-                                                      const int* __restrict__ squeue_count,
-                                                      double* __restrict__ partial) {
-    constexpr int NV = DERIV ? kOutDeriv : kOutValue;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n_inst * kSlots) return;
-    const int i = q / kSlots, s = q % kSlots;
-    if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
-    const int count = squeue_count[q];
-    if (count == 0) return;
-    const InstanceDesc I = inst[i];
-    const GridDesc g = grids[I.grid];
-    const PointsDesc P = points[I.points];
-    PairState<float> S;
-    make_pair_state(in.EA + 16 * (size_t)i, in.phiA + 6 * (size_t)i, in.EB + 16 * (size_t)i, in.phiB + 6 * (size_t)i,
-                    in.prm + 6 * (size_t)i, S);
-    const int* queue = squeue + squeue_offset(i, I.tile0, I.ntiles, s);
-    LaneSink<NV, float> sink{partial + (size_t)q * NV, vec3<float>(0, 0, 0), vec3<float>(0, 0, 0)};
-    for (int k = 0; k < count; ++k) {
-        const V3 xi = load_point(P, queue[k]);
-        if constexpr (DERIV) {
-            contact_force_jacobian<float>(g, xi, S, nullptr, sink, true, false);
-        } else {
-            ContactForce<float> F = contact_force<float>(g, xi, S, nullptr, true, false);
-            sink.force(F.xi1, F.f1, F.xi2, F.f2);
-        }
     }
 }
 
@@ -550,18 +470,12 @@ __global__ void zero_status_kernel(int* status, int n) {
 template <bool DERIV, bool STENCIL>
 void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, const InstanceDesc* d_inst,
                     BatchInputs in, const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s) {
-    if (precision == kMixed) {
+    if (precision == kMixed)
         force_kernel<DERIV, STENCIL, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                         s.tile_count, s.partial, s.squeue,
-                                                                         s.squeue_count);
-        if (!STENCIL)
-            stencil_kernel<DERIV><<<(n_inst * kSlots + 127) / 128, 128, 0, stream>>>(
-                d_inst, n_inst, in, d_grids, d_points, s.squeue, s.squeue_count, s.partial);
-    } else {
+                                                                         s.tile_count, s.partial);
+    else
         force_kernel<DERIV, STENCIL, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                          s.tile_count, s.partial, s.squeue,
-                                                                          s.squeue_count);
-    }
+                                                                          s.tile_count, s.partial);
 }
 
 }  // namespace

@@ -25,12 +25,11 @@
 //                    shuffles and over the CTA in FP64 shared memory, in a fixed
 //                    order, into one partial row per (instance, slot).
 //                    On the FP32 path a contact whose derivative stencil could
-//                    leave its cell is not evaluated there: it is queued (in
-//                    order) for stencil_kernel, so that no warp runs the long
-//                    FP64 stencil for one lane while 31 wait.
-//   stencil_kernel   one thread per (instance, slot) queue: the queued contacts
-//                    through the exact path (the reference's FP64 stencil), FP32
-//                    algebra, added in queue order to the (instance, slot) row.
+//                    leave its cell takes the exact path (the reference's FP64
+//                    stencil); the warp evaluates such contacts' 19 stencil
+//                    queries together, one contact at a time across its lanes
+//                    (warp_exact_jets), so that no lane runs the long FP64
+//                    stencil alone while 31 wait.
 //   finalize_kernel  sums the kSlots partial rows of each instance in order and
 //                    scatters them into fm / Km / Dm.
 //
@@ -97,22 +96,7 @@ struct BatchScratch {
     int* tile_queue;            // total_tiles: queued recheck count per tile
     double* partial;            // n x kSlots x kOutDeriv
     unsigned long long* recheck;  // diagnostic counter of FP64 rechecks
-    int* squeue;                // deferred exact-stencil contacts (stored point indices), see stencil_kernel
-    int* squeue_count;          // n x kSlots
 };
-
-// Region of the deferred-contact queue of (instance, slot): slot s of an
-// instance with `ntiles` tiles takes at most ntiles*kTile/kSlots + kChunk
-// contacts (its chunks s, s+kSlots, ... of kChunk contacts).
-__host__ __device__ inline size_t squeue_slot_size(int ntiles) {
-    return (size_t)ntiles * kTile / kSlots + kChunk;
-}
-__host__ __device__ inline size_t squeue_offset(int inst, int tile0, int ntiles, int slot) {
-    return (size_t)tile0 * kTile + (size_t)inst * kSlots * kChunk + (size_t)slot * squeue_slot_size(ntiles);
-}
-__host__ __device__ inline size_t squeue_capacity(int n_inst, int total_tiles) {
-    return (size_t)total_tiles * kTile + (size_t)n_inst * kSlots * kChunk;
-}
 
 enum Precision { kFP64 = 0, kMixed = 1 };
 

@@ -103,7 +103,12 @@ def _cpu_sim(args):
     pair = O.ScenePair(_G["grid"], _G["pts"], True, np.eye(4), _G["prm"])
     t = time.perf_counter()
     qs, qds, conv, its, evs = O.bdf1_steps(mover, [pair], np.zeros(3), np.zeros(3), steps)
-    return time.perf_counter() - t, int(evs.sum())
+    t_fwd = time.perf_counter() - t
+    w = np.zeros((steps, 3))
+    w[-1] = d  # L = displacement along the pull after the last step
+    t = time.perf_counter()
+    O.bdf1_backward(mover, [pair], qs, np.zeros(3), w)
+    return t_fwd, int(evs.sum()), time.perf_counter() - t
 
 
 def cpu_pool(grid, pts, procs):
@@ -407,7 +412,7 @@ def run_gpu(args, world, rank):
                                     "speedup_of_batched": value / plain_rate},
         "error_vs_fp64_path": err,
         "active_contacts_per_step": n_active, "fp64_rechecked_points_per_step": rechecked,
-        "gpu_launches": (7 if args.precision == "mixed" else 6) * args.steps,
+        "gpu_launches": 6 * args.steps,  # prep, detect, recheck, force, zero_status, finalize
         "clocks": clk,
         "wall_s": wall,
     }
@@ -443,6 +448,7 @@ def run_sim(args, sdfc, ctx, g, p, n):
     sim.set_external_force(F)
     sim.step(1)  # warm-up step
     sim.set_state(np.zeros((n, 3)), np.zeros((n, 3)))
+    sim.record(args.sim_steps)  # the trajectory for the adjoint (one device copy per step)
     r0, e0 = sim.stats()
     t0 = time.perf_counter()
     early = min(args.sim_steps, args.sim_early)
@@ -454,6 +460,13 @@ def run_sim(args, sdfc, ctx, g, p, n):
     q, qd = sim.get_state()
     wall = time.perf_counter() - t0
     r2, e2 = sim.stats()
+    # adjoint of the whole rollout for L_i = d_i . q_T (displacement along the pull):
+    # dL/dq0, dL/dqdot0 and dL/d(pull force) of every scene
+    w = np.zeros((n, args.sim_steps, 3))
+    w[:, -1] = dirs
+    t1 = time.perf_counter()
+    g0, gd0, gf = sim.backward(w)
+    t_bwd = time.perf_counter() - t1
     sim.close()
     return {"scenes": n, "steps": args.sim_steps, "wall_s": wall,
             "scene_steps_per_s": n * args.sim_steps / wall,
@@ -462,7 +475,9 @@ def run_sim(args, sdfc, ctx, g, p, n):
             "first_steps": {"steps": early, "wall_s": t_early, "scene_steps_per_s": n * early / t_early,
                             "scene_evaluations": e1 - e0},
             "converged_last_step": float(np.mean(conv)),
-            "final_z_mean": float(q[:, 2].mean())}
+            "final_z_mean": float(q[:, 2].mean()),
+            "adjoint": {"steps": args.sim_steps, "wall_s": t_bwd, "scene_steps_per_s": n * args.sim_steps / t_bwd,
+                        "finite": bool(np.isfinite(gf).all() and np.isfinite(g0).all())}}
 
 
 def cpu_sim_rate(pool, n_scenes, steps, procs):
@@ -472,8 +487,11 @@ def cpu_sim_rate(pool, n_scenes, steps, procs):
     res = pool.map(_cpu_sim, [(dirs[k], steps) for k in idx], chunksize=1)
     wall = time.perf_counter() - t
     evals = sum(r[1] for r in res)
+    t_fwd, t_bwd = sum(r[0] for r in res), sum(r[2] for r in res)
     return {"scene_steps_per_s": n_scenes * steps / wall, "steps": steps, "scenes": n_scenes, "cores": procs,
-            "scene_evaluations": evals, "wall_s": wall}
+            "scene_evaluations": evals, "wall_s": wall,
+            # forward and adjoint share the wall time; split it by their single-core times
+            "adjoint_scene_steps_per_s": n_scenes * steps / (wall * t_bwd / max(t_fwd + t_bwd, 1e-12))}
 
 
 def main():
