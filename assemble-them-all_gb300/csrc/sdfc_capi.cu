@@ -78,11 +78,12 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
         sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, deriv, stencil, prec, stream);
     }
     if (b->timing) cudaEventRecord(b->ev[2], stream);
+    const sdfc::BatchInputs* q2 = sdfc::force_skips_q2(true, stencil, prec) ? &in : nullptr;
     if (in.mode) {
-        sdfc::launch_finalize(b->d_inst, b->n, sc, true, out, stream, in.mode, true);
+        sdfc::launch_finalize(b->d_inst, b->n, sc, true, out, stream, in.mode, true, q2);
         sdfc::launch_finalize(b->d_inst, b->n, sc, false, out, stream, in.mode, false);
     } else {
-        sdfc::launch_finalize(b->d_inst, b->n, sc, deriv, out, stream);
+        sdfc::launch_finalize(b->d_inst, b->n, sc, deriv, out, stream, nullptr, true, deriv ? q2 : nullptr);
     }
     if (b->timing) cudaEventRecord(b->ev[3], stream);
     CUDA_TRY(ctx, cudaGetLastError());
@@ -467,6 +468,21 @@ int sdfc_batch_evaluate_device(sdfc_batch* b, const double* E_A, const double* p
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     return run_batch(b, E_A, phi_A, E_B, phi_B, params, want_deriv != 0, fm, Km, Dm, n_active, status, s);
+}
+
+int sdfc_batch_evaluate_masked_device(sdfc_batch* b, const double* E_A, const double* phi_A, const double* E_B,
+                                      const double* phi_B, const double* params, const int* request, double* fm,
+                                      double* Km, double* Dm, int* n_active, int* status, void* stream) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!E_A || !phi_A || !E_B || !phi_B || !params || !request || !fm || !Km || !Dm || !n_active || !status)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_evaluate_masked_device: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    sdfc::BatchInputs in{E_A, phi_A, E_B, phi_B, params};
+    in.mode = request;
+    sdfc::BatchOutputs out{fm, Km, Dm, n_active, status};
+    return sdfc_impl::run_batch(b, in, true, out, (cudaStream_t)stream);
 }
 
 int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, const double* E_B, const double* phi_B,

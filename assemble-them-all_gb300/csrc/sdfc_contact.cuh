@@ -706,7 +706,7 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
 template <typename T, class Sink>
 __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
                                               Sink& sink, bool valid, bool stencil_only,
-                                              const ExactJet<T>* ej = nullptr) {
+                                              const ExactJet<T>* ej = nullptr, bool skip_q2 = false) {
     // collision, :292-310
     V3 xd;
     double dd;
@@ -813,8 +813,11 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
 
     const Vec3<T> rxd = mulT(R2, xw1d);
 
+    // skip_q2: the dq2 columns of Km are left to the caller, which derives them
+    // from the summed dq1 columns (finalize_kernel)
 #pragma unroll 1
-    for (int c = 0; c < 24; ++c) {
+    for (int ci = 0; ci < (skip_q2 ? 18 : 24); ++ci) {
+        const int c = (skip_q2 && ci >= 6) ? ci + 6 : ci;
         const int blk = c / 6, j = c % 6;
         const bool kcol = blk < 2;  // Km column (dq) vs Dm column (dphi)
         T dd_j = 0, dddot_j = 0;

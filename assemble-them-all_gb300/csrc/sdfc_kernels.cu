@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             }
             WarpSink<NV, T> sink{acc + warp * NV, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
             if constexpr (DERIV) {
-                contact_force_jacobian<T>(g, xi, S, fcp, sink, valid, STENCIL, ejp);
+                contact_force_jacobian<T>(g, xi, S, fcp, sink, valid, STENCIL, ejp, kWarpExact);
             } else {
                 ContactForce<T> F = contact_force<T>(g, xi, S, fcp, valid, STENCIL, ejp);
                 sink.force(F.xi1, F.f1, F.xi2, F.f2);
@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
         }
     }
     __syncthreads();
-    double* row = partial + ((size_t)i * kSlots + s) * NV;
+    double* row = partial + ((size_t)i * kSlots + s) * kOutDeriv;  // one row stride for both passes
     for (int k = tid; k < NV; k += kChunk) {
         double v = 0.0;
         for (int w = 0; w < NW; ++w) v += acc[w * NV + k].value();
@@ -436,17 +436,64 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     }
 }
 
+// Column j of Ad(E_A^{-1} E_B) (twists ordered (w, v)): the map that turns the
+// dq1 columns of Km into its dq2 columns.  Every contact's force in the bodies'
+// frames is unchanged when both bodies move together, so for a world twist eps,
+// Km1 Ad(E_A^{-1}) eps + Km2 Ad(E_B^{-1}) eps = 0, i.e. Km2 = -Km1 Ad(E_A^{-1} E_B).
+// (Dm has no such identity in the reference: its friction damping is not a function
+// of the relative velocity alone.)
+__device__ inline void adjoint_column(const double* EA, const double* EB, int j, double* top, double* bot) {
+    double R[9], p[3];
+    for (int r = 0; r < 3; ++r) {
+        p[r] = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            double v = 0.0;
+            for (int k = 0; k < 3; ++k) v += EA[4 * k + r] * EB[4 * k + c];  // R_A^T R_B
+            R[3 * r + c] = v;
+        }
+        for (int k = 0; k < 3; ++k) p[r] += EA[4 * k + r] * (EB[4 * k + 3] - EA[4 * k + 3]);  // R_A^T (p_B - p_A)
+    }
+    if (j < 3) {
+        const double a[3] = {R[j], R[3 + j], R[6 + j]};
+        for (int r = 0; r < 3; ++r) top[r] = a[r];
+        bot[0] = p[1] * a[2] - p[2] * a[1];
+        bot[1] = p[2] * a[0] - p[0] * a[2];
+        bot[2] = p[0] * a[1] - p[1] * a[0];
+    } else {
+        for (int r = 0; r < 3; ++r) {
+            top[r] = 0.0;
+            bot[r] = R[3 * r + (j - 3)];
+        }
+    }
+}
+
+// EA / EB not null: the dq2 columns of Km were not accumulated (force_kernel's
+// skip_q2) and are derived here from the summed dq1 columns.
 template <bool DERIV>
 __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
-                                const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode) {
+                                const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode,
+                                const double* __restrict__ EA, const double* __restrict__ EB) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)n_inst * NV) return;
     const int i = (int)(idx / NV), k = (int)(idx % NV);
     if (mode && mode[i] != (DERIV ? 2 : 1)) return;
-    const double* p = partial + (size_t)i * kSlots * NV + k;
+    const double* p = partial + (size_t)i * kSlots * kOutDeriv + k;
     double v = 0.0;
-    for (int s = 0; s < kSlots; ++s) v += p[(size_t)s * NV];
+    if (DERIV && EA && k >= 12 && k < 156 && (k - 12) % 12 >= 6) {
+        const int r = (k - 12) / 12, j = (k - 12) % 12 - 6;
+        const double* row = partial + (size_t)i * kSlots * kOutDeriv + 12 + 12 * r;  // Km row r, dq1 columns
+        double km[6];
+        for (int c = 0; c < 6; ++c) {
+            km[c] = 0.0;
+            for (int s = 0; s < kSlots; ++s) km[c] += row[(size_t)s * kOutDeriv + c];
+        }
+        double top[3], bot[3];
+        adjoint_column(EA + 16 * (size_t)i, EB + 16 * (size_t)i, j, top, bot);
+        for (int c = 0; c < 3; ++c) v -= km[c] * top[c] + km[3 + c] * bot[c];
+    } else {
+        for (int s = 0; s < kSlots; ++s) v += p[(size_t)s * kOutDeriv];
+    }
     if (k < 12)
         out.fm[12 * (size_t)i + k] = v;
     else if (k < 156)
@@ -510,17 +557,23 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
 }
 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
-                     cudaStream_t stream, const int* mode, bool zero_status) {
+                     cudaStream_t stream, const int* mode, bool zero_status, const BatchInputs* derive_q2) {
     if (n_inst <= 0) return;
     if (zero_status) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out.status, n_inst);
     const int NV = deriv ? kOutDeriv : kOutValue;
     const size_t total = (size_t)n_inst * NV;
     const int threads = 256;
     const unsigned blocks = (unsigned)((total + threads - 1) / threads);
+    const double* EA = derive_q2 ? derive_q2->EA : nullptr;
+    const double* EB = derive_q2 ? derive_q2->EB : nullptr;
     if (deriv)
-        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode);
+        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA,
+                                                              EB);
     else
-        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode);
+        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
+                                                               nullptr, nullptr);
 }
+
+bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !stencil && precision == kMixed; }
 
 }  // namespace sdfc

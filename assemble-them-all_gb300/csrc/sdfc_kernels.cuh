@@ -110,7 +110,13 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
 // Zeroes the status words, then finalizes.  With in.mode set, only the
 // instances whose request matches `deriv` are finalized (zero_status = false
 // lets a second, value-only pass keep the first pass's status bits).
+// derive_q2: the inputs of the evaluation whose force pass skipped the dq2 columns
+// of Km (force_skips_q2); finalize derives them from the dq1 columns.
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
-                     cudaStream_t stream, const int* mode = nullptr, bool zero_status = true);
+                     cudaStream_t stream, const int* mode = nullptr, bool zero_status = true,
+                     const BatchInputs* derive_q2 = nullptr);
+// Whether launch_force's derivative pass leaves the dq2 columns of Km to finalize
+// (the FP32-algebra path outside the stencil mode).
+bool force_skips_q2(bool deriv, bool stencil, int precision);
 
 }  // namespace sdfc

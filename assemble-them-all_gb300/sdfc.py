@@ -22,7 +22,7 @@ STORAGE_F32 = 1
 EXPORTS = (
     "sdfc_create", "sdfc_destroy", "sdfc_last_error", "sdfc_upload_grid", "sdfc_upload_points",
     "sdfc_evaluate", "sdfc_active_ids", "sdfc_batch_create", "sdfc_batch_destroy", "sdfc_batch_evaluate",
-    "sdfc_batch_evaluate_device", "sdfc_batch_recheck_count", "sdfc_set_derivative_mode",
+    "sdfc_batch_evaluate_device", "sdfc_batch_evaluate_masked_device", "sdfc_batch_recheck_count", "sdfc_set_derivative_mode",
     "sdfc_batch_set_derivative_mode", "sdfc_batch_set_timing", "sdfc_batch_last_timing", "sdfc_set_precision",
     "sdfc_batch_set_precision", "sdfc_evaluate_noalloc", "sdfc_sim_create", "sdfc_sim_destroy",
     "sdfc_sim_set_precision", "sdfc_sim_set_state", "sdfc_sim_get_state", "sdfc_sim_set_external_force",
@@ -104,6 +104,7 @@ def lib():
         L.sdfc_batch_destroy.restype = None
         L.sdfc_batch_evaluate.argtypes = [v, d, d, d, d, P(Params), i, d, d, d, P(i), P(i)]
         L.sdfc_batch_evaluate_device.argtypes = [v, v, v, v, v, v, i, v, v, v, v, v, v]
+        L.sdfc_batch_evaluate_masked_device.argtypes = [v, v, v, v, v, v, v, v, v, v, v, v, v]
         L.sdfc_batch_recheck_count.argtypes = [v, P(ctypes.c_ulonglong), i]
         L.sdfc_set_derivative_mode.argtypes = [v, i]
         L.sdfc_batch_set_derivative_mode.argtypes = [v, i]
@@ -273,6 +274,13 @@ class Batch:
         self.ctx._check(lib().sdfc_batch_evaluate_device(self._h, E_A, phi_A, E_B, phi_B, params,
                                                          int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active,
                                                          status, stream), "sdfc_batch_evaluate_device")
+
+    def evaluate_masked_device(self, E_A, phi_A, E_B, phi_B, params, request, fm, Km, Dm, n_active, status,
+                               stream=0):
+        """Device pointers; request (device int32[n]): 0 skip, 1 fm only, 2 fm, Km, Dm."""
+        self.ctx._check(lib().sdfc_batch_evaluate_masked_device(self._h, E_A, phi_A, E_B, phi_B, params, request,
+                                                                fm, Km, Dm, n_active, status, stream),
+                        "sdfc_batch_evaluate_masked_device")
 
     def set_precision(self, precision: int):
         self.ctx._check(lib().sdfc_batch_set_precision(self._h, int(precision)), "sdfc_batch_set_precision")

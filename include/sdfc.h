@@ -155,6 +155,15 @@ int sdfc_batch_evaluate_device(sdfc_batch* batch, const double* E_A, const doubl
                                const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
                                double* Dm, int* n_active, int* status, void* stream);
 
+/* sdfc_batch_evaluate_device with a per-instance request (DEVICE int[n]): 0 skips the
+ * instance (its outputs are left as they are), 1 evaluates fm only
+ * (ForceGeneralSDFContact::computeForce), 2 fm, Km and Dm (computeForceWithDerivative).
+ * One launch set serves a batch whose instances need different things, e.g. the
+ * Newton and line-search points of batched implicit steps.  Km and Dm must be given. */
+int sdfc_batch_evaluate_masked_device(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
+                                      const double* phi_B, const double* params, const int* request, double* fm,
+                                      double* Km, double* Dm, int* n_active, int* status, void* stream);
+
 /* Per-phase device time of the last evaluation of this batch, the GPU
  * counterpart of ForceGeneralSDFContact's "collision detection" and "compute
  * force" timers (Force::Timer, simulation/redmax/Force/Force.h:15-36;

@@ -238,11 +238,15 @@ def test_mixed_precision_uneven_batch(sdfc, ctx, oracle, workloads):
     b = ctx.batch([phs[w] for w in which], [gh] * n)
     b.set_precision(sdfc.PRECISION_MIXED)
     ang = rng.uniform(0, 2 * np.pi, n)
-    EA = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.003),
-                                  [0.0202 * np.cos(a), 0.0202 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
-    EB = np.stack([np.eye(4)] * n)
+    rel = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.003),
+                                   [0.0202 * np.cos(a), 0.0202 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
+    # the socket placed in the world too (half the instances), so that the Km columns of
+    # body B, which the FP32 path derives from body A's, are checked under a general pose
+    EB = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.3), rng.normal(size=3))
+                   if k % 2 else np.eye(4) for k in range(n)])
+    EA = EB @ rel
     phiA = rng.normal(size=(n, 6)) * 0.2
-    phiB = np.zeros((n, 6))
+    phiB = rng.normal(size=(n, 6)) * 0.1
     prm = [sdfc.Params(1e5, [1e3, 1e1][k % 2], 0.3, 1e3, 1.0, 1.0) for k in range(n)]
     fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
     og = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
@@ -253,4 +257,63 @@ def test_mixed_precision_uneven_batch(sdfc, ctx, oracle, workloads):
         assert_close(f"inst {k} fm", fm[k], rf, rel=MIXED_REL, abs_=1e-9)
         assert_close(f"inst {k} Km", Km[k], rK, rel=MIXED_REL, abs_=1e-9)
         assert_close(f"inst {k} Dm", Dm[k], rD, rel=MIXED_REL, abs_=1e-9)
+    b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_masked_requests(sdfc, ctx, workloads, precision):
+    """Per-instance requests in one launch set (sdfc_batch_evaluate_masked_device):
+    0 skip, 1 fm only, 2 fm, Km, Dm.  Every requested instance is bit-identical to a
+    plain evaluation of its kind; skipped outputs stay untouched.  Many value
+    requests follow derivative ones, so any overlap of the two passes' scratch would
+    show; the poses of both bodies are general (rotated and offset)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    g = workloads.socket_grid(64, dtype=np.float32)
+    gh = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+    ph = ctx.upload_points(workloads.peg_points(6000, seed=8), 1)
+    n = 40
+    b = ctx.batch([ph] * n, [gh] * n)
+    b.set_precision(precision)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    EB = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.2), rng.normal(size=3) * 0.3)
+                   for _ in range(n)])
+    rel = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.004),
+                                   [0.025 * np.cos(a), 0.025 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
+    EA = EB @ rel  # the peg pressed into the socket, both placed in the world
+    phiA = rng.normal(size=(n, 6)) * 0.2
+    phiB = rng.normal(size=(n, 6)) * 0.1
+    prm = [sdfc.Params(1e5, [1e3, 1e1][k % 2], 0.3, 1e3, 1.0, 1.0) for k in range(n)]
+    req = np.array([2, 2] + [1] * 20 + [0, 2, 1] * 6, dtype=np.int32)
+    assert len(req) == n
+    fm2, Km2, Dm2, n2, _ = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
+    fm1, _, _, n1, _ = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=False)
+    assert (n2 > 0).all()
+
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
+    dEA, dphiA, dEB, dphiB = t(EA.reshape(n, 16)), t(phiA), t(EB.reshape(n, 16)), t(phiB)
+    dprm = t([[p.kn, p.kt, p.mu, p.damping, p.scale, p.contact_scale] for p in prm])
+    dreq = torch.tensor(req, device=dev)
+    fm = torch.full((n, 12), float("nan"), dtype=torch.float64, device=dev)
+    Km = torch.full((n, 144), float("nan"), dtype=torch.float64, device=dev)
+    Dm = torch.full((n, 144), float("nan"), dtype=torch.float64, device=dev)
+    nact = torch.full((n,), -7, dtype=torch.int32, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    b.evaluate_masked_device(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
+                             dreq.data_ptr(), fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(),
+                             st.data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+    torch.cuda.synchronize()
+    fm, Km, Dm, nact, st = (x.cpu().numpy() for x in (fm, Km, Dm, nact, st))
+    assert not st.any()
+    for k in range(n):
+        if req[k] == 2:
+            assert np.array_equal(fm[k], fm2[k]) and nact[k] == n2[k], k
+            assert np.array_equal(Km[k], Km2[k].ravel()) and np.array_equal(Dm[k], Dm2[k].ravel()), k
+        elif req[k] == 1:
+            assert np.array_equal(fm[k], fm1[k]) and nact[k] == n1[k], k
+            assert np.isnan(Km[k]).all() and np.isnan(Dm[k]).all(), k
+        else:
+            assert np.isnan(fm[k]).all() and np.isnan(Km[k]).all() and nact[k] == -7, k
     b.close()
