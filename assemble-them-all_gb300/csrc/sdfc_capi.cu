@@ -321,11 +321,30 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     g.col_th = col_th;
     g.lip = (float)(std::sqrt(lip2) * 1.0001);
     g.vmax = (float)(vmax * 1.0001);
-    void* p32 = nullptr;
-    if ((rc = dev_alloc(ctx, &p32, n * sizeof(float)))) return rc;
-    ctx->allocations.push_back(p32);
-    CUDA_TRY(ctx, cudaMemcpy(p32, v32.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-    g.v32 = (const float*)p32;
+    {
+        // cell-corner array: per cell its 8 FP32 corners (GridDesc::cells32)
+        const size_t ci = (size_t)ni - 1, cj = (size_t)nj - 1, ck = (size_t)nk - 1;
+        std::vector<float> cells(8 * ci * cj * ck);
+        for (size_t k = 0; k < ck; ++k)
+            for (size_t j = 0; j < cj; ++j)
+                for (size_t i = 0; i < ci; ++i) {
+                    float* c = &cells[8 * (i + ci * (j + cj * k))];
+                    const size_t b = i + (size_t)ni * (j + (size_t)nj * k), sj = (size_t)ni, sk = (size_t)ni * nj;
+                    c[0] = v32[b];
+                    c[1] = v32[b + 1];
+                    c[2] = v32[b + sj];
+                    c[3] = v32[b + sj + 1];
+                    c[4] = v32[b + sk];
+                    c[5] = v32[b + sk + 1];
+                    c[6] = v32[b + sk + sj];
+                    c[7] = v32[b + sk + sj + 1];
+                }
+        void* pc = nullptr;
+        if ((rc = dev_alloc(ctx, &pc, cells.size() * sizeof(float)))) return rc;
+        ctx->allocations.push_back(pc);
+        CUDA_TRY(ctx, cudaMemcpy(pc, cells.data(), cells.size() * sizeof(float), cudaMemcpyHostToDevice));
+        g.cells32 = (const float4*)pc;
+    }
     {
         // FP64 values of the grid as stored: the caller's doubles, or the FP32 values widened
         std::vector<double> w64;

@@ -134,7 +134,10 @@ struct GridDesc {
     double org[3];  // min_box / dx (cell coordinate of the origin), for the fast depth path
     double col_th;
     const double* v64;   // FP64 values (storage 1: the FP32 values widened), read for active contacts
-    const float* v32;    // FP32 values (storage 0: rounded), read by detection and the FP32 derivatives
+    // per cell (ni-1)(nj-1)(nk-1), i fastest: its 8 FP32 corner values in two float4,
+    // (c000, c100, c010, c110) and (c001, c101, c011, c111); read by detection and the
+    // FP32 derivatives with two 16-byte loads instead of eight scattered gathers
+    const float4* cells32;
     float fmin[3], fmax[3], finv_dx[3], fdx[3];  // FP32 constants
     float lip;        // bound on |grad| of the interpolant over the grid
     float vmax;       // max |value|
@@ -590,10 +593,10 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             d = J.v + g.col_th;
             // FP32 analytic derivatives of the cell's interpolant
             const float u = (float)ud, v = (float)vd, w = (float)wd;
-            const float c000 = __ldg(g.v32 + b), c100 = __ldg(g.v32 + b + 1);
-            const float c010 = __ldg(g.v32 + b + sj), c110 = __ldg(g.v32 + b + sj + 1);
-            const float c001 = __ldg(g.v32 + b + sk), c101 = __ldg(g.v32 + b + sk + 1);
-            const float c011 = __ldg(g.v32 + b + sk + sj), c111 = __ldg(g.v32 + b + sk + sj + 1);
+            const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
+            const float4 lo = __ldg(cq), hi = __ldg(cq + 1);
+            const float c000 = lo.x, c100 = lo.y, c010 = lo.z, c110 = lo.w;
+            const float c001 = hi.x, c101 = hi.y, c011 = hi.z, c111 = hi.w;
             const float a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;
             const float b0 = fmaf(u, a00, c000), b1 = fmaf(u, a10, c010);
             const float b2 = fmaf(u, a01, c001), b3 = fmaf(u, a11, c011);

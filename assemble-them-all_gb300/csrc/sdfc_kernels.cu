@@ -58,9 +58,10 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
     pref[i] = f;
 }
 
-// FP32 trilinear interpolation for a point certainly inside the box.
-__device__ __forceinline__ float trilinear32(const float* __restrict__ v, int ni, int nj, int nk, const Prefilter& f,
-                                             float x, float y, float z) {
+// FP32 trilinear interpolation for a point certainly inside the box, from the
+// cell-corner array (GridDesc::cells32).
+__device__ __forceinline__ float trilinear32(const float4* __restrict__ cells, int ni, int nj, int nk,
+                                             const Prefilter& f, float x, float y, float z) {
     float cx = (x - f.gmin[0]) * f.ginv[0];
     float cy = (y - f.gmin[1]) * f.ginv[1];
     float cz = (z - f.gmin[2]) * f.ginv[2];
@@ -68,12 +69,10 @@ __device__ __forceinline__ float trilinear32(const float* __restrict__ v, int ni
     int j = min(max((int)floorf(cy), 0), nj - 2);
     int k = min(max((int)floorf(cz), 0), nk - 2);
     float u = cx - (float)i, w1 = cy - (float)j, w2 = cz - (float)k;
-    const size_t sj = (size_t)ni, sk = (size_t)ni * (size_t)nj;
-    const float* b = v + (size_t)i + sj * (size_t)j + sk * (size_t)k;
-    float c000 = __ldg(b), c100 = __ldg(b + 1);
-    float c010 = __ldg(b + sj), c110 = __ldg(b + sj + 1);
-    float c001 = __ldg(b + sk), c101 = __ldg(b + sk + 1);
-    float c011 = __ldg(b + sk + sj), c111 = __ldg(b + sk + sj + 1);
+    const float4* q = cells + 2 * ((size_t)i + (size_t)(ni - 1) * ((size_t)j + (size_t)(nj - 1) * k));
+    const float4 lo = __ldg(q), hi = __ldg(q + 1);
+    float c000 = lo.x, c100 = lo.y, c010 = lo.z, c110 = lo.w;
+    float c001 = hi.x, c101 = hi.y, c011 = hi.z, c111 = hi.w;
     float a0 = fmaf(u, c100 - c000, c000), a1 = fmaf(u, c110 - c010, c010);
     float a2 = fmaf(u, c101 - c001, c001), a3 = fmaf(u, c111 - c011, c011);
     float b0 = fmaf(w1, a1 - a0, a0), b1 = fmaf(w1, a3 - a2, a2);
@@ -101,7 +100,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                                                                 int* __restrict__ tile_queue,
                                                                 const int* __restrict__ mode) {
     __shared__ Prefilter f;
-    __shared__ const float* gv;
+    __shared__ const float4* gv;
     __shared__ const float* px;
     __shared__ int gn[3], pn;
     __shared__ int warp_act[kDetectThreads / 32], warp_q[kDetectThreads / 32];
@@ -121,7 +120,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         reinterpret_cast<float*>(&f)[tid] = reinterpret_cast<const float*>(pref + i)[tid];
     if (tid == 0) {
         const GridDesc& g = grids[I.grid];
-        gv = g.v32;
+        gv = g.cells32;
         gn[0] = g.ni;
         gn[1] = g.nj;
         gn[2] = g.nk;

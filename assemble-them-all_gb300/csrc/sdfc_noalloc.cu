@@ -219,7 +219,7 @@ extern "C" int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, 
     }
     g.col_th = col_th;
     g.v64 = grid_values;
-    g.v32 = nullptr;
+    g.cells32 = nullptr;
 
     cudaStream_t s = (cudaStream_t)stream;
     const int rows = (n + kNaChunk - 1) / kNaChunk;
