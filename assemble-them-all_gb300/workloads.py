@@ -132,3 +132,192 @@ def pose(R=None, p=None) -> np.ndarray:
     if p is not None:
         E[:3, 3] = p
     return E
+
+
+# --------------------------------------------------------------------------- procedural multi-part assemblies
+#
+# Stand-ins for the reference's multi-part assembly datasets: a chain of box blocks along x, each
+# joined to the next by a tab on its +x face that sits in a slot of the next block's -x face, and
+# some blocks pierced by a z bore holding a pin (a part of its own).  Sizes are jittered by +-2%
+# (inside the 0.01 clearances) so the parts stay interlocked without overlapping.
+# Every part is a CSG of boxes and z cylinders in its own frame (centred at its placement); its
+# signed distance is the min/max composition of the primitives'.
+
+def _box_sdf(p, c, h):
+    q = np.abs(p - np.asarray(c)) - np.asarray(h)
+    return np.linalg.norm(np.maximum(q, 0.0), axis=-1) + np.minimum(q.max(axis=-1), 0.0)
+
+
+def _zcyl_sdf(p, c, r, hl):
+    d = p - np.asarray(c)
+    rr = np.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2)
+    e = np.stack([rr - r, np.abs(d[..., 2]) - hl], axis=-1)
+    return np.minimum(np.max(e, axis=-1), 0.0) + np.linalg.norm(np.maximum(e, 0.0), axis=-1)
+
+
+@dataclass
+class Primitive:
+    kind: str     # "box" or "zcyl"
+    c: tuple      # centre in the part frame
+    size: tuple   # box half-extents, or (radius, half-length)
+    sign: int     # +1 union (material), -1 subtraction (cut)
+
+    def sdf(self, p):
+        return _box_sdf(p, self.c, self.size) if self.kind == "box" else _zcyl_sdf(p, self.c, *self.size)
+
+    def area(self):
+        if self.kind == "box":
+            hx, hy, hz = self.size
+            return 8.0 * (hx * hy + hy * hz + hx * hz)
+        r, hl = self.size
+        return 2.0 * np.pi * r * 2.0 * hl + 2.0 * np.pi * r * r
+
+    def sample_surface(self, g, n):
+        c = np.asarray(self.c, dtype=np.float64)
+        if self.kind == "box":
+            h = np.asarray(self.size, dtype=np.float64)
+            areas = np.array([h[1] * h[2], h[1] * h[2], h[0] * h[2], h[0] * h[2], h[0] * h[1], h[0] * h[1]])
+            face = g.choice(6, size=n, p=areas / areas.sum())
+            u = g.uniform(-1.0, 1.0, (n, 3)) * h
+            ax = face // 2
+            u[np.arange(n), ax] = np.where(face % 2 == 0, -h[ax], h[ax])
+            return c + u
+        r, hl = self.size
+        side, cap = 2 * np.pi * r * 2 * hl, np.pi * r * r
+        which = g.uniform(0.0, side + 2 * cap, n)
+        th = g.uniform(0.0, 2 * np.pi, n)
+        z = g.uniform(-hl, hl, n)
+        rr = r * np.sqrt(g.uniform(0.0, 1.0, n))
+        zc = np.where(which < side + cap, -hl, hl)
+        lat = which < side
+        pts = np.where(lat[:, None], np.stack([r * np.cos(th), r * np.sin(th), z], -1),
+                       np.stack([rr * np.cos(th), rr * np.sin(th), zc], -1))
+        return c + pts
+
+
+@dataclass
+class Part:
+    prims: list        # Primitive list: the material ones first, then the cuts
+    position: np.ndarray  # placement of the part frame in the world (translation only)
+
+    def sdf(self, p):
+        d = None
+        for pr in self.prims:
+            if pr.sign > 0:
+                s = pr.sdf(p)
+                d = s if d is None else np.minimum(d, s)
+        for pr in self.prims:
+            if pr.sign < 0:
+                d = np.maximum(d, -pr.sdf(p))
+        return d
+
+    def bounds(self):
+        lo = np.full(3, np.inf)
+        hi = np.full(3, -np.inf)
+        for pr in self.prims:
+            if pr.sign < 0:
+                continue
+            c = np.asarray(pr.c)
+            h = np.asarray(pr.size) if pr.kind == "box" else np.array([pr.size[0], pr.size[0], pr.size[1]])
+            lo = np.minimum(lo, c - h)
+            hi = np.maximum(hi, c + h)
+        return lo, hi
+
+    def surface_points(self, n, seed, tol=1e-9):
+        """n points uniform (area-weighted) on the part's surface, part frame."""
+        g = np.random.default_rng(seed)
+        areas = np.array([pr.area() for pr in self.prims])
+        out = []
+        have = 0
+        while have < n:
+            m = max(2 * (n - have), 256)
+            which = g.choice(len(self.prims), size=m, p=areas / areas.sum())
+            cand = np.concatenate([self.prims[k].sample_surface(g, int((which == k).sum()))
+                                   for k in range(len(self.prims))])
+            keep = cand[np.abs(self.sdf(cand)) <= tol]
+            out.append(keep)
+            have += len(keep)
+        pts = np.concatenate(out)[:n]
+        return pts[g.permutation(len(pts))]
+
+    def mass_props(self, density=1.0):
+        """Mass and principal inertia diagonal (Ixx, Iyy, Izz, m, m, m) of the part's material
+        primitives taken as solids about the part frame (the cuts ignored: a stand-in for the
+        mesh integrals of BodyMeshObj)."""
+        m_tot, I = 0.0, np.zeros(3)
+        for pr in self.prims:
+            if pr.sign < 0:
+                continue
+            c = np.asarray(pr.c)
+            if pr.kind == "box":
+                a, b, cz = 2 * np.asarray(pr.size)
+                m = density * a * b * cz
+                Ic = m / 12.0 * np.array([b * b + cz * cz, a * a + cz * cz, a * a + b * b])
+            else:
+                r, hl = pr.size
+                m = density * np.pi * r * r * 2 * hl
+                L = 2 * hl
+                Ic = np.array([m * (3 * r * r + L * L) / 12, m * (3 * r * r + L * L) / 12, m * r * r / 2])
+            Ic = Ic + m * np.array([c[1] ** 2 + c[2] ** 2, c[0] ** 2 + c[2] ** 2, c[0] ** 2 + c[1] ** 2])
+            m_tot += m
+            I += Ic
+        return m_tot, np.array([I[0], I[1], I[2], m_tot, m_tot, m_tot])
+
+    def grid(self, n, dtype=np.float64, pad=0.1):
+        lo, hi = self.bounds()
+        return sample_grid(self.sdf, lo, hi, n, pad=pad, dtype=dtype)
+
+
+@dataclass
+class Assembly:
+    parts: list
+    n_points: list   # contact points per part
+    grid_n: list     # grid resolution per part
+    mover: int       # the pulled part
+    direction: np.ndarray
+
+
+def procedural_assembly(seed: int, n_parts: int = None, points=(2000, 200000), grids=(64, 128, 256),
+                        clearance: float = 0.01, jitter: float = 0.02) -> Assembly:
+    """A seeded interlocked assembly of 2-12 parts: boxes chained by tab-in-slot joints along x,
+    some with a z bore holding a pin.  Per part: contact points log-uniform in `points`, grid
+    resolution uniform over `grids`.  One part is pulled along a random axis direction."""
+    g = np.random.default_rng(seed)
+    n_parts = int(g.integers(2, 13)) if n_parts is None else int(n_parts)
+    n_pins = int(g.integers(0, n_parts // 2 + 1)) if n_parts > 2 else 0
+    n_blocks = max(n_parts - n_pins, 1 if n_parts == 1 else 2)
+    n_pins = n_parts - n_blocks
+    J = lambda v: v * (1.0 + g.uniform(-jitter, jitter))
+    tab_h = 0.15  # tab half-width / half-height
+    tab_t = 0.3   # tab protrusion (= slot depth)
+    parts = []
+    for k in range(n_blocks):
+        h = (0.5, J(0.5), J(0.5))
+        prims = [Primitive("box", (0.0, 0.0, 0.0), h, +1)]
+        if k + 1 < n_blocks:  # tab into the next block
+            prims.append(Primitive("box", (0.5 + tab_t / 2, 0.0, 0.0), (tab_t / 2, J(tab_h), J(tab_h)), +1))
+        if k > 0:  # slot for the previous block's tab
+            prims.append(Primitive("box", (-0.5 + tab_t / 2, 0.0, 0.0),
+                                   (tab_t / 2 + clearance, tab_h * (1 + jitter) + clearance,
+                                    tab_h * (1 + jitter) + clearance), -1))
+        # blocks half a clearance apart (placement jitter a tenth of it): no part overlaps another
+        # at rest, contacts come from the pull
+        parts.append(Part(prims, np.array([k * (1.0 + 0.5 * clearance) + g.uniform(-0.1, 0.1) * clearance,
+                                           0.0, 0.0])))
+    bored = sorted(g.choice(n_blocks, size=n_pins, replace=n_pins > n_blocks))
+    for b in bored:
+        blk = parts[b]
+        bx = g.uniform(-0.1, 0.1)  # bore away from the tab/slot axis in y
+        by = 0.3 * (1 if g.uniform() < 0.5 else -1)
+        r = J(0.1)
+        blk.prims.append(Primitive("zcyl", (bx, by, 0.0), (r + clearance, 2.0), -1))
+        pin = Part([Primitive("zcyl", (0.0, 0.0, 0.0), (r, J(0.7)), +1)],
+                   blk.position + np.array([bx, by, 0.0]))
+        parts.append(pin)
+    n_pts = [int(round(np.exp(g.uniform(np.log(points[0]), np.log(points[1]))))) for _ in parts]
+    grid_n = [int(g.choice(grids)) for _ in parts]
+    mover = int(g.integers(len(parts)))
+    axis = int(g.integers(3))
+    d = np.zeros(3)
+    d[axis] = 1.0 if g.uniform() < 0.5 else -1.0
+    return Assembly(parts, n_pts, grid_n, mover, d)

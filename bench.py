@@ -378,6 +378,10 @@ def run_gpu(args, world, rank):
     d2h = n * (300 * 8 + 2 * 4)
 
     sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 else None
+    if sim_res is not None:
+        plain = run_sim_plain(args, sdfc, ctx, g, p, n)
+        plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
+        sim_res["plain_fp64_per_instance"] = plain
 
     if rank != 0:
         return
@@ -478,6 +482,33 @@ def run_sim(args, sdfc, ctx, g, p, n):
             "final_z_mean": float(q[:, 2].mean()),
             "adjoint": {"steps": args.sim_steps, "wall_s": t_bwd, "scene_steps_per_s": n * args.sim_steps / t_bwd,
                         "finite": bool(np.isfinite(gf).all() and np.isfinite(g0).all())}}
+
+
+def run_sim_plain(args, sdfc, ctx, g, p, n_dirs, instances=4):
+    """The plain per-instance FP64 GPU path of the same scenes: one scene per sdfc_sim, FP64
+    force evaluations, over the same first steps as the batched run's first_steps figure."""
+    dirs = W.fibonacci_directions(n_dirs)
+    idx = np.linspace(0, n_dirs - 1, instances).astype(int)
+    m, inertia = W.cylinder_mass_props()
+    mover = sdfc.Mover.make(m, inertia, np.eye(4), SIM_H, SIM_GRAVITY)
+    prm = sdfc.Params(*PARAMS)
+    steps = min(args.sim_steps, args.sim_early)
+    total = 0.0
+    for k in idx:
+        sim = ctx.sim([mover], [sdfc.ScenePair.make(0, p, g, True, np.eye(4), prm)])
+        sim.set_precision(sdfc.PRECISION_FP64)
+        F = np.zeros((1, 6))
+        F[0, 3:] = SIM_PULL * dirs[k]
+        sim.set_external_force(F)
+        sim.set_state(np.zeros((1, 3)), np.zeros((1, 3)))
+        sim.step(1)  # warm-up (graph capture)
+        sim.set_state(np.zeros((1, 3)), np.zeros((1, 3)))
+        t0 = time.perf_counter()
+        sim.step(steps)
+        total += time.perf_counter() - t0
+        sim.close()
+    return {"scene_steps_per_s": instances * steps / total, "instances": int(instances), "steps": steps,
+            "precision": "fp64", "scenes_per_sim": 1}
 
 
 def cpu_sim_rate(pool, n_scenes, steps, procs):
