@@ -192,7 +192,8 @@ class _Mover(ctypes.Structure):
     _fields_ = [("mass", ctypes.c_double), ("inertia", ctypes.c_double * 6), ("E_pj0", ctypes.c_double * 16),
                 ("E_ji", ctypes.c_double * 16), ("gravity", ctypes.c_double * 3), ("h", ctypes.c_double),
                 ("f_ext", ctypes.c_double * 6), ("joint_stiffness", ctypes.c_double),
-                ("joint_damping", ctypes.c_double), ("q_rest", ctypes.c_double * 3)]
+                ("joint_damping", ctypes.c_double), ("q_rest", ctypes.c_double * 6), ("ndof", ctypes.c_int),
+                ("newton_tol", ctypes.c_double)]
 
 
 class _Pair(ctypes.Structure):
@@ -202,7 +203,8 @@ class _Pair(ctypes.Structure):
 
 @dataclass
 class Mover:
-    """One body on a translational joint (Body::_mass/_Inertia/_E_ji, Joint::_E_pj_0, options)."""
+    """One body on a joint to the world (Body::_mass/_Inertia/_E_ji, Joint::_E_pj_0, options):
+    ndof 3 = translational, 6 = free3d-exp (q = (p, r), r exponential rotation coordinates)."""
     mass: float
     inertia: np.ndarray
     E_ji: np.ndarray
@@ -212,6 +214,8 @@ class Mover:
     f_ext: np.ndarray = None
     joint_stiffness: float = 0.0
     joint_damping: float = 0.0
+    ndof: int = 3
+    newton_tol: float = 0.0  # 0: the reference's 1e-8; smaller for finite-difference checks
 
     def _c(self):
         E_pj0 = np.eye(4) if self.E_pj0 is None else self.E_pj0
@@ -219,7 +223,8 @@ class Mover:
         return _Mover(float(self.mass), (ctypes.c_double * 6)(*_f64(self.inertia)),
                       (ctypes.c_double * 16)(*_f64(E_pj0).ravel()), (ctypes.c_double * 16)(*_f64(self.E_ji).ravel()),
                       (ctypes.c_double * 3)(*self.gravity), float(self.h), (ctypes.c_double * 6)(*_f64(f)),
-                      float(self.joint_stiffness), float(self.joint_damping), (ctypes.c_double * 3)(0, 0, 0))
+                      float(self.joint_stiffness), float(self.joint_damping), (ctypes.c_double * 6)(*([0.0] * 6)),
+                      int(self.ndof), float(self.newton_tol))
 
 
 @dataclass
@@ -264,8 +269,8 @@ def _pairs_c(pairs):
 
 
 def bdf1_steps(mover: Mover, pairs, q, qdot, steps=1):
-    """Simulation::forward with BDF1 (Simulation.cpp:914-990, 1248-1270) for one translational mover:
-    returns (q_his[steps+1, 3], qdot_his, converged[steps], iters[steps], evals[steps])."""
+    """Simulation::forward with BDF1 (Simulation.cpp:914-990, 1248-1270) for one moving part:
+    returns (q_his[steps+1, ndof], qdot_his, converged[steps], iters[steps], evals[steps])."""
     L = _lib_sim()
     m = mover._c()
     arr, keep = _pairs_c(pairs)
@@ -288,11 +293,12 @@ def bdf1_eval(mover: Mover, pairs, q0, qdot0, q1, want_H=True):
     L = _lib_sim()
     m = mover._c()
     arr, keep = _pairs_c(pairs)
-    g = np.zeros(3)
-    H = np.zeros(9)
+    n = mover.ndof
+    g = np.zeros(n)
+    H = np.zeros(n * n)
     L.orc_bdf1_eval(ctypes.byref(m), arr, len(pairs), _dp(_f64(q0)), _dp(_f64(qdot0)), _dp(_f64(q1)), _dp(g),
                     _dp(H) if want_H else None)
-    return g, H.reshape(3, 3)
+    return g, H.reshape(n, n)
 
 
 def bdf1_matrices(mover: Mover, pairs, q0, qdot0, q1):
@@ -301,10 +307,11 @@ def bdf1_matrices(mover: Mover, pairs, q0, qdot0, q1):
     L = _lib_sim()
     m = mover._c()
     arr, keep = _pairs_c(pairs)
-    g, H, M, D = np.zeros(3), np.zeros(9), np.zeros(9), np.zeros(9)
+    n = mover.ndof
+    g, H, M, D = np.zeros(n), np.zeros(n * n), np.zeros(n * n), np.zeros(n * n)
     L.orc_bdf1_eval_full(ctypes.byref(m), arr, len(pairs), _dp(_f64(q0)), _dp(_f64(qdot0)), _dp(_f64(q1)), _dp(g),
                          _dp(H), _dp(M), _dp(D))
-    return g, H.reshape(3, 3), M.reshape(3, 3), D.reshape(3, 3)
+    return g, H.reshape(n, n), M.reshape(n, n), D.reshape(n, n)
 
 
 def bdf1_backward(mover: Mover, pairs, q_his, qdot0, df_dq):
@@ -313,10 +320,11 @@ def bdf1_backward(mover: Mover, pairs, q_his, qdot0, df_dq):
     L = _lib_sim()
     m = mover._c()
     arr, keep = _pairs_c(pairs)
-    q_his = _f64(q_his).reshape(-1, 3)
+    n = mover.ndof
+    q_his = _f64(q_his).reshape(-1, n)
     T = len(q_his) - 1
-    df_dq = _f64(df_dq).reshape(T, 3)
-    g0, gd0, gf = np.zeros(3), np.zeros(3), np.zeros(6)
+    df_dq = _f64(df_dq).reshape(T, n)
+    g0, gd0, gf = np.zeros(n), np.zeros(n), np.zeros(6)
     L.orc_bdf1_backward(ctypes.byref(m), arr, len(pairs), _dp(q_his), _dp(_f64(qdot0)), T, _dp(df_dq), _dp(g0),
                         _dp(gd0), _dp(gf))
     return g0, gd0, gf

@@ -803,13 +803,11 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
     return n_active;
 }
 
-/* ------------------------------------------------------------------ BDF1 of one translational mover */
+/* ------------------------------------------------------------------ BDF1 of one moving part */
 
-/* Joint::update (Q = [I q; 0 1], E_pj = E_pj0 Q; JointTranslational.cpp:9-40,
- * Joint.cpp) then Body::update (E_0i = E_0j E_ji, phi = Ad(E_ij) S_j qdot;
- * Body.cpp:138-156).  For the translational joint S_j = [0; I], so
- * phi = (0, R_ji^T qdot). */
-void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, double* E0i, double* phi) {
+/* ---- translational joint (3 dof) */
+
+static void trans_pose(const orc_mover* m, const double* q, const double* qdot, double* E0i, double* phi) {
     double Q[16] = {1, 0, 0, q[0], 0, 1, 0, q[1], 0, 0, 1, q[2], 0, 0, 0, 1};
     double E0j[16];
     mm(m->E_pj0, Q, E0j, 4, 4, 4);
@@ -830,18 +828,13 @@ void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, dou
  * f = J^T fm + fr, K = J^T Km J + Kr, D = J^T Dm J + Dr.  fm is the mover's gravity
  * and external force (Body::computeMaximalForce, Body.cpp:247-271; its Coriolis term
  * only has angular rows, which J^T drops) plus every contact's mover block. */
-void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0, const double* qdot0,
-                   const double* q1, double* g, double* H) {
-    orc_bdf1_eval_full(m, pairs, n_pairs, q0, qdot0, q1, g, H, NULL, NULL);
-}
-
-void orc_bdf1_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
-                        const double* qdot0, const double* q1, double* g, double* H, double* M_out,
-                        double* D_out) {
+static void trans_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
+                            const double* qdot0, const double* q1, double* g, double* H, double* M_out,
+                            double* D_out) {
     const double h = m->h;
     double qd1[3], E0i[16], phi[6], R0i[9], p0i[3], Rji[9], pji[3];
     for (int k = 0; k < 3; ++k) qd1[k] = (q1[k] - q0[k]) / h;
-    orc_mover_pose(m, q1, qd1, E0i, phi);
+    trans_pose(m, q1, qd1, E0i, phi);
     pose_split(E0i, R0i, p0i);
     pose_split(m->E_ji, Rji, pji);
     /* linear rows of fm for the mover: gravity + external */
@@ -901,67 +894,681 @@ void orc_bdf1_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, 
     if (M_out) memcpy(M_out, M, sizeof M);
 }
 
-/* 3x3 solve by Gaussian elimination with partial pivoting (the algorithm of Eigen's
- * PartialPivLU used by Simulation::newton, Simulation.cpp:1028). */
-static void solve3(const double* A_in, const double* b_in, double* x) {
-    double A[9], b[3];
-    memcpy(A, A_in, sizeof A);
-    memcpy(b, b_in, sizeof b);
-    for (int c = 0; c < 3; ++c) {
+/* ---- free joint with exponential rotation coordinates (6 dof: q = (p, r)) */
+
+/* small dense helpers (row-major) */
+static void mz(double* a, int n) { memset(a, 0, sizeof(double) * (size_t)n); }
+static void m3_add(const double* a, const double* b, double* c) {
+    for (int k = 0; k < 9; ++k) c[k] = a[k] + b[k];
+}
+static void m3_scale(const double* a, double s, double* c) {
+    for (int k = 0; k < 9; ++k) c[k] = a[k] * s;
+}
+static void m3_tmul(const double* a, const double* b, double* c) { /* c = a^T b */
+    double at[9];
+    m3_transpose(a, at);
+    m3_mul(at, b, c);
+}
+static void unskew3(const double* a, double* v) { /* math::unskew, rm/Utils.h:45-51 */
+    v[0] = a[7];
+    v[1] = a[2];
+    v[2] = a[3];
+}
+static void skew_of_cross(const double* a, const double* b, double* S) { /* skew(a x b) */
+    double c[3];
+    cross3(a, b, c);
+    skew3(c, S);
+}
+
+/* math::exp(Vector3): Rodrigues' formula (rm/Utils.h:108-124). */
+static void so3_exp(const double* w_in, double* R) {
+    double wl = norm3(w_in);
+    mz(R, 9);
+    R[0] = R[4] = R[8] = 1.0;
+    if (wl > 1e-12) {
+        const double wx = w_in[0] / wl, wy = w_in[1] / wl, wz = w_in[2] / wl;
+        const double c = cos(wl), s = sin(wl), c1 = 1.0 - c;
+        R[0] = c + wx * wx * c1;
+        R[1] = -wz * s + wx * wy * c1;
+        R[2] = wy * s + wx * wz * c1;
+        R[3] = wz * s + wx * wy * c1;
+        R[4] = c + wy * wy * c1;
+        R[5] = -wx * s + wy * wz * c1;
+        R[6] = -wy * s + wx * wz * c1;
+        R[7] = wx * s + wy * wz * c1;
+        R[8] = c + wz * wz * c1;
+    }
+}
+
+/* The rotation part of the joint and its derivatives (JointSphericalExp::update,
+ * rm/Joint/JointSphericalExp.cpp:13-190): R = exp(r), Rdot, T (body angular velocity =
+ * T rdot), Tdot, and their derivatives wrt r.  With d = 1 / |r|^2,
+ * A_j = (r_j [r] + [r x (I - R) e_j]) d and dR/dr_j = A_j R. */
+typedef struct {
+    double R[9], Rdot[9], T[9], Tdot[9];
+    double dR[3][9], dRdot[3][9], dT[3][9], dTdot[3][9];
+} orc_rot;
+
+static void rot_update(const double* q, const double* qd, orc_rot* o) {
+    double e[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    if (norm3(q) < 1e-9) { /* |q| < math::eps: the first-order expansion about R = I */
+        mz(o->R, 9);
+        o->R[0] = o->R[4] = o->R[8] = 1.0;
+        mz(o->Rdot, 9);
+        for (int j = 0; j < 3; ++j) {
+            double S[9];
+            skew3(e[j], S);
+            memcpy(o->dR[j], S, sizeof S);
+            for (int k = 0; k < 9; ++k) o->Rdot[k] += S[k] * qd[j];
+        }
+        mz(o->T, 9);
+        o->T[0] = o->T[4] = o->T[8] = 1.0;
+        for (int j = 0; j < 3; ++j) {
+            double P[9], v[3];
+            m3_tmul(o->Rdot, o->dR[j], P);
+            unskew3(P, v);
+            for (int r = 0; r < 3; ++r) o->Tdot[3 * r + j] = v[r];
+        }
+        for (int k = 0; k < 3; ++k)
+            for (int j = 0; j < 3; ++j) {
+                double P[9], v[3];
+                m3_tmul(o->dR[k], o->dR[j], P);
+                unskew3(P, v);
+                for (int r = 0; r < 3; ++r) o->dT[k][3 * r + j] = v[r];
+            }
+        /* this branch sets neither dRdot nor dTdot (JointSphericalExp.cpp:43-58); the free
+         * joint reads them as zero (their values before any rotation was ever evaluated) */
+        for (int k = 0; k < 3; ++k) {
+            mz(o->dRdot[k], 9);
+            mz(o->dTdot[k], 9);
+        }
+        return;
+    }
+    so3_exp(q, o->R);
+    const double q2 = dot3(q, q), d = 1.0 / q2;
+    const double qqd = dot3(q, qd);
+    double A[3][9], B[3][9], C[3][9], Ad[3][9], Bd[3][9], Cd[3][9], v[3][3];
+    double Sq[9], Sqd[9];
+    skew3(q, Sq);
+    skew3(qd, Sqd);
+    for (int j = 0; j < 3; ++j) {
+        for (int r = 0; r < 3; ++r) v[j][r] = e[j][r] - o->R[3 * r + j]; /* (I - R) e_j */
+        skew_of_cross(q, v[j], C[j]);
+        m3_scale(Sq, q[j], B[j]);
+        double BC[9];
+        m3_add(B[j], C[j], BC);
+        m3_scale(BC, d, A[j]);
+        m3_mul(A[j], o->R, o->dR[j]);
+    }
+    mz(o->Rdot, 9);
+    for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 9; ++k) o->Rdot[k] += o->dR[j][k] * qd[j];
+    const double ddot = -2.0 * qqd / (q2 * q2);
+    for (int j = 0; j < 3; ++j) {
+        double a[3], b[3], Rde[3], w[3];
+        cross3(qd, v[j], a);
+        for (int r = 0; r < 3; ++r) Rde[r] = o->Rdot[3 * r + j];
+        cross3(q, Rde, b);
+        for (int r = 0; r < 3; ++r) w[r] = a[r] - b[r];
+        skew3(w, Cd[j]);
+        for (int k = 0; k < 9; ++k) Bd[j][k] = qd[j] * Sq[k] + q[j] * Sqd[k];
+        for (int k = 0; k < 9; ++k) Ad[j][k] = (Bd[j][k] + Cd[j][k]) * d + (B[j][k] + C[j][k]) * ddot;
+    }
+    double dd_dq[3], dddot_dq[3], dA[3][3][9], dB[3][3][9], dC[3][3][9]; /* [j][k] */
+    for (int k = 0; k < 3; ++k) {
+        dd_dq[k] = -2.0 * q[k] / (q2 * q2);
+        for (int j = 0; j < 3; ++j) {
+            double Sek[9];
+            skew3(e[k], Sek);
+            for (int t = 0; t < 9; ++t) dB[j][k][t] = q[j] * Sek[t] + (j == k ? Sq[t] : 0.0);
+            double c1[9], dRe[3], c2v[3], c2[9];
+            skew_of_cross(e[k], v[j], c1);
+            for (int r = 0; r < 3; ++r) dRe[r] = o->dR[k][3 * r + j];
+            cross3(q, dRe, c2v);
+            for (int r = 0; r < 3; ++r) c2v[r] = -c2v[r];
+            skew3(c2v, c2);
+            m3_add(c1, c2, dC[j][k]);
+            for (int t = 0; t < 9; ++t) dA[j][k][t] = (dB[j][k][t] + dC[j][k][t]) * d + (B[j][t] + C[j][t]) * dd_dq[k];
+        }
+    }
+    for (int k = 0; k < 3; ++k) { /* dRdot/dq_k = sum_j (dA_jk R + A_j dR_k) qd_j */
+        mz(o->dRdot[k], 9);
+        for (int j = 0; j < 3; ++j) {
+            double P1[9], P2[9];
+            m3_mul(dA[j][k], o->R, P1);
+            m3_mul(A[j], o->dR[k], P2);
+            for (int t = 0; t < 9; ++t) o->dRdot[k][t] += (P1[t] + P2[t]) * qd[j];
+        }
+    }
+    double dAd[3][3][9];
+    for (int k = 0; k < 3; ++k) {
+        dddot_dq[k] = (-2.0 * qd[k] * q2 + 8.0 * qqd * q[k]) / (q2 * q2 * q2);
+        for (int j = 0; j < 3; ++j) {
+            double Sek[9], dBd[9], dCd[9], a[3], b[3], c[3], dRe[3], Rde[3], dRde[3], w[3];
+            skew3(e[k], Sek);
+            for (int t = 0; t < 9; ++t) dBd[t] = qd[j] * Sek[t] + (j == k ? Sqd[t] : 0.0);
+            for (int r = 0; r < 3; ++r) {
+                dRe[r] = o->dR[k][3 * r + j];
+                Rde[r] = o->Rdot[3 * r + j];
+                dRde[r] = o->dRdot[k][3 * r + j];
+            }
+            cross3(qd, dRe, a);
+            cross3(e[k], Rde, b);
+            cross3(q, dRde, c);
+            for (int r = 0; r < 3; ++r) w[r] = -a[r] - b[r] - c[r];
+            skew3(w, dCd);
+            for (int t = 0; t < 9; ++t)
+                dAd[j][k][t] = (dBd[t] + dCd[t]) * d + (Bd[j][t] + Cd[j][t]) * dd_dq[k] +
+                               (dB[j][k][t] + dC[j][k][t]) * ddot + (B[j][t] + C[j][t]) * dddot_dq[k];
+        }
+    }
+    double Rt[9], Rdt[9];
+    m3_transpose(o->R, Rt);
+    m3_transpose(o->Rdot, Rdt);
+    for (int j = 0; j < 3; ++j) {
+        double P[9], P1[9], P2[9], P3[9], t1[9], w[3];
+        m3_mul(Rt, o->dR[j], P);
+        unskew3(P, w);
+        for (int r = 0; r < 3; ++r) o->T[3 * r + j] = w[r];
+        /* Tdot_j = unskew(Rdot^T A_j R + R^T Adot_j R + R^T A_j Rdot) */
+        m3_mul(Rdt, A[j], t1);
+        m3_mul(t1, o->R, P1);
+        m3_mul(Rt, Ad[j], t1);
+        m3_mul(t1, o->R, P2);
+        m3_mul(Rt, A[j], t1);
+        m3_mul(t1, o->Rdot, P3);
+        for (int t = 0; t < 9; ++t) P[t] = P1[t] + P2[t] + P3[t];
+        unskew3(P, w);
+        for (int r = 0; r < 3; ++r) o->Tdot[3 * r + j] = w[r];
+        for (int k = 0; k < 3; ++k) {
+            double d2R[9], Q1[9], Q2[9], dRkt[9], dRdkt[9], S[9], u[3];
+            m3_mul(dA[j][k], o->R, Q1);
+            m3_mul(A[j], o->dR[k], Q2);
+            for (int t = 0; t < 9; ++t) d2R[t] = Q1[t] + Q2[t];
+            m3_transpose(o->dR[k], dRkt);
+            m3_transpose(o->dRdot[k], dRdkt);
+            /* dT_k col j = unskew(dR_k^T dR_j + R^T d2R_jk) */
+            m3_mul(dRkt, o->dR[j], Q1);
+            m3_mul(Rt, d2R, Q2);
+            for (int t = 0; t < 9; ++t) S[t] = Q1[t] + Q2[t];
+            unskew3(S, u);
+            for (int r = 0; r < 3; ++r) o->dT[k][3 * r + j] = u[r];
+            /* dTdot_k col j: the derivative of Tdot_j's three products wrt q_k */
+            const double* terms[9][3] = {
+                {dRdkt, A[j], o->R},     {Rdt, dA[j][k], o->R},  {Rdt, A[j], o->dR[k]},
+                {dRkt, Ad[j], o->R},     {Rt, dAd[j][k], o->R},  {Rt, Ad[j], o->dR[k]},
+                {dRkt, A[j], o->Rdot},   {Rt, dA[j][k], o->Rdot}, {Rt, A[j], o->dRdot[k]}};
+            mz(S, 9);
+            for (int q3 = 0; q3 < 9; ++q3) {
+                double X[9], Y[9];
+                m3_mul(terms[q3][0], terms[q3][1], X);
+                m3_mul(X, terms[q3][2], Y);
+                for (int t = 0; t < 9; ++t) S[t] += Y[t];
+            }
+            unskew3(S, u);
+            for (int r = 0; r < 3; ++r) o->dTdot[k][3 * r + j] = u[r];
+        }
+    }
+}
+
+/* T only (JointSphericalExp::inner_update, :192-235), for the reparameterisation. */
+static void rot_T(const double* q, double* T) {
+    const double zero[3] = {0, 0, 0};
+    orc_rot o;
+    rot_update(q, zero, &o);
+    memcpy(T, o.T, sizeof o.T);
+}
+
+/* 6x6 helpers */
+static void m6_mul(const double* a, const double* b, double* c) { mm(a, b, c, 6, 6, 6); }
+static void m6_transpose(const double* a, double* t) {
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) t[6 * c + r] = a[6 * r + c];
+}
+static void m6_vec(const double* a, const double* v, double* out) {
+    for (int r = 0; r < 6; ++r) {
+        double s = 0.0;
+        for (int c = 0; c < 6; ++c) s += a[6 * r + c] * v[c];
+        out[r] = s;
+    }
+}
+static void m6t_vec(const double* a, const double* v, double* out) {
+    for (int c = 0; c < 6; ++c) {
+        double s = 0.0;
+        for (int r = 0; r < 6; ++r) s += a[6 * r + c] * v[r];
+        out[c] = s;
+    }
+}
+/* math::Ad(E) (rm/Utils.h:85-94): [R 0; [p] R  R] */
+static void adjoint6(const double* E, double* A) {
+    double R[9], p[3], S[9], SR[9];
+    pose_split(E, R, p);
+    skew3(p, S);
+    m3_mul(S, R, SR);
+    mz(A, 36);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            A[6 * r + c] = R[3 * r + c];
+            A[6 * (r + 3) + c] = SR[3 * r + c];
+            A[6 * (r + 3) + c + 3] = R[3 * r + c];
+        }
+}
+static void pose_inverse(const double* E, double* Ei) {
+    double R[9], p[3];
+    pose_split(E, R, p);
+    mz(Ei, 16);
+    for (int r = 0; r < 3; ++r) {
+        double s = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            Ei[4 * r + c] = R[3 * c + r];
+            s += R[3 * c + r] * p[c];
+        }
+        Ei[4 * r + 3] = -s;
+    }
+    Ei[15] = 1.0;
+}
+
+/* Kinematics of the free body: JointFree3DExp::update (rm/Joint/JointFree3DExp.cpp:13-99),
+ * Joint::update (rm/Joint/Joint.cpp:93-121: E_pj = E_pj0 Q), Body::update (Body.cpp:138-156:
+ * E_0i = E_0j E_ji, phi = Ad(E_ij) phi_j) and Robot::computeJointJacobianWithDerivative for a
+ * joint attached to the world (rm/Robot.cpp:687-704): J = Ad(E_ij) S_j, Jdot = Ad(E_ij) S_j_dot,
+ * dJ/dq_k = Ad(E_ij) dS_j/dq_k, dJdot/dq_k = Ad(E_ij) dS_j_dot/dq_k. */
+typedef struct {
+    double E0i[16], phi[6];
+    double J[36], Jdot[36], dJ[6][36], dJdot[6][36];
+} orc_free_kin;
+
+static void free_kinematics(const orc_mover* m, const double* q, const double* qd, orc_free_kin* k) {
+    orc_rot o;
+    rot_update(q + 3, qd + 3, &o);
+    double S[36], Sd[36], dS[6][36], dSd[6][36];
+    mz(S, 36);
+    mz(Sd, 36);
+    for (int i = 0; i < 6; ++i) {
+        mz(dS[i], 36);
+        mz(dSd[i], 36);
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            S[6 * r + 3 + c] = o.T[3 * r + c];          /* angular rows, rotation columns */
+            S[6 * (r + 3) + c] = o.R[3 * c + r];        /* linear rows, translation columns: R^T */
+            Sd[6 * r + 3 + c] = o.Tdot[3 * r + c];
+            Sd[6 * (r + 3) + c] = o.Rdot[3 * c + r];
+            for (int i = 0; i < 3; ++i) {
+                dS[3 + i][6 * r + 3 + c] = o.dT[i][3 * r + c];
+                dS[3 + i][6 * (r + 3) + c] = o.dR[i][3 * c + r];
+                dSd[3 + i][6 * r + 3 + c] = o.dTdot[i][3 * r + c];
+                dSd[3 + i][6 * (r + 3) + c] = o.dRdot[i][3 * c + r];
+            }
+        }
+    double Q[16], Eij[16], Aij[36], E0j[16];
+    mz(Q, 16);
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) Q[4 * r + c] = o.R[3 * r + c];
+        Q[4 * r + 3] = q[r];
+    }
+    Q[15] = 1.0;
+    mm(m->E_pj0, Q, E0j, 4, 4, 4);
+    mm(E0j, m->E_ji, k->E0i, 4, 4, 4);
+    pose_inverse(m->E_ji, Eij);
+    adjoint6(Eij, Aij);
+    m6_mul(Aij, S, k->J);
+    m6_mul(Aij, Sd, k->Jdot);
+    for (int i = 0; i < 6; ++i) {
+        m6_mul(Aij, dS[i], k->dJ[i]);
+        m6_mul(Aij, dSd[i], k->dJdot[i]);
+    }
+    m6_vec(k->J, qd, k->phi);
+}
+
+/* Body::computeMaximalForceWithDerivative (rm/Body/Body.cpp:275-330): Coriolis
+ * ad(phi)^T (I phi), gravity R_0i^T m g, external I .* R_0i^T f_ext, with Km (wrt the body
+ * twist coordinates) and Dm (wrt phi); added to fm[6], Km[36], Dm[36]. */
+static void free_body_force(const orc_mover* m, const double* E0i, const double* phi, double* fm, double* Km,
+                            double* Dm) {
+    double R0i[9], p0i[3], fg[3], mg[3], fh[3], ft[3];
+    pose_split(E0i, R0i, p0i);
+    const double* I = m->inertia;
+    double adT[36], Sw[9], Sv[9];
+    skew3(phi, Sw);
+    skew3(phi + 3, Sv);
+    mz(adT, 36); /* ad(phi)^T = [Sw^T Sv^T; 0 Sw^T] */
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            adT[6 * r + c] = Sw[3 * c + r];
+            adT[6 * r + c + 3] = Sv[3 * c + r];
+            adT[6 * (r + 3) + c + 3] = Sw[3 * c + r];
+        }
+    double Iphi[6], fc[6];
+    for (int k = 0; k < 6; ++k) Iphi[k] = I[k] * phi[k];
+    m6_vec(adT, Iphi, fc);
+    for (int k = 0; k < 3; ++k) mg[k] = m->mass * m->gravity[k];
+    m3t_vec(R0i, mg, fg);
+    m3t_vec(R0i, m->f_ext, fh);
+    m3t_vec(R0i, m->f_ext + 3, ft);
+    for (int k = 0; k < 3; ++k) {
+        fm[k] += fc[k] + I[k] * fh[k];
+        fm[3 + k] += fc[3 + k] + fg[k] + I[3 + k] * ft[k];
+    }
+    if (!Km) return;
+    double S[9];
+    skew3(fg, S);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Km[6 * (3 + r) + c] += S[3 * r + c];
+    double Sh[9], St[9];
+    skew3(fh, Sh);
+    skew3(ft, St);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            Km[6 * r + c] += Sh[3 * r + c] * I[r];
+            Km[6 * (3 + r) + c] += St[3 * r + c] * I[3 + r];
+        }
+    for (int c = 0; c < 6; ++c)
+        for (int r = 0; r < 6; ++r) Dm[6 * r + c] += adT[6 * r + c] * I[c];
+    double Iw[3] = {I[0] * phi[0], I[1] * phi[1], I[2] * phi[2]};
+    double mv[3] = {I[3] * phi[3], I[4] * phi[4], I[5] * phi[5]};
+    double e[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int j = 0; j < 3; ++j) {
+        double a[3], b[3];
+        cross3(e[j], Iw, a);
+        cross3(e[j], mv, b);
+        for (int r = 0; r < 3; ++r) {
+            Dm[6 * r + j] -= a[r];
+            Dm[6 * r + 3 + j] -= b[r];
+            Dm[6 * (3 + r) + j] -= b[r];
+        }
+    }
+}
+
+/* One evaluation of the free mover at (q1, qdot1 = (q1 - q0) / h): g, H, M, D of
+ * Simulation::evaluate_g[_with_derivatives]_BDF1 (Simulation.cpp:1081-1165) with
+ * Simulation::computeMatrices (:422-503) for a single body:
+ *   M = J^T Mm J, f = J^T fm - J^T Mm Jdot qdot + fr,
+ *   dM/dq_k = dJ_k^T Mm J + (dJ_k^T Mm J)^T,
+ *   K = Kqvv + Kr + J^T Km J + J^T Dm (dJ/dq qdot) + [dJ_k^T fm]_k,
+ *   D = -J^T Mm Jdot - J^T Mm (dJ/dq qdot) + Dr + J^T Dm J,
+ *   H = M - h^2 K - h D + [dM/dq_k (q1 - q0 - h qdot0)]_k.
+ * Optional outputs: H, M, D (36 each) and J, E0i for the adjoint. */
+static void free_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
+                           const double* qdot0, const double* q1, double* g, double* H, double* M_out, double* D_out,
+                           double* J_out, double* E0i_out) {
+    const double h = m->h;
+    const int want = H != NULL || D_out != NULL;
+    double qd1[6];
+    for (int k = 0; k < 6; ++k) qd1[k] = (q1[k] - q0[k]) / h;
+    orc_free_kin kin;
+    free_kinematics(m, q1, qd1, &kin);
+    double fm[6] = {0}, Km[36] = {0}, Dm[36] = {0};
+    free_body_force(m, kin.E0i, kin.phi, fm, want ? Km : NULL, Dm);
+    const double zero6[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < n_pairs; ++c) {
+        const orc_pair* P = pairs + c;
+        double pf[12], pK[144], pD[144];
+        const double *EA, *phiA, *EB, *phiB;
+        if (P->mover_is_contact) {
+            EA = kin.E0i; phiA = kin.phi; EB = P->E_fixed; phiB = zero6;
+        } else {
+            EA = P->E_fixed; phiA = zero6; EB = kin.E0i; phiB = kin.phi;
+        }
+        orc_pair_eval(P->grid, P->pts, P->n_pts, EA, phiA, EB, phiB, &P->prm, want, pf, pK, pD, NULL);
+        const int o = P->mover_is_contact ? 0 : 6;
+        for (int r = 0; r < 6; ++r) {
+            fm[r] += pf[o + r];
+            if (want)
+                for (int s = 0; s < 6; ++s) {
+                    Km[6 * r + s] += pK[(o + r) * 12 + o + s];
+                    Dm[6 * r + s] += pD[(o + r) * 12 + o + s];
+                }
+        }
+    }
+    const double* Mm = m->inertia;
+    double MmJ[36], JT[36], M[36], MmJdot[36], JTMmJdot[36], fqvv[6], f[6], t6[6];
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) {
+            MmJ[6 * r + c] = kin.J[6 * r + c] * Mm[r];
+            MmJdot[6 * r + c] = kin.Jdot[6 * r + c] * Mm[r];
+        }
+    m6_transpose(kin.J, JT);
+    m6_mul(JT, MmJ, M);
+    m6_mul(JT, MmJdot, JTMmJdot); /* J^T Mm Jdot */
+    m6_vec(JTMmJdot, qd1, fqvv);
+    m6t_vec(kin.J, fm, t6);
+    for (int k = 0; k < 6; ++k) {
+        const double fr = -m->joint_stiffness * (q1[k] - m->q_rest[k]) - m->joint_damping * qd1[k];
+        f[k] = t6[k] - fqvv[k] + fr;
+    }
+    double dq[6], Mdq[6];
+    for (int k = 0; k < 6; ++k) dq[k] = q1[k] - q0[k] - h * qdot0[k];
+    m6_vec(M, dq, Mdq);
+    for (int k = 0; k < 6; ++k) g[k] = Mdq[k] - h * h * f[k];
+    if (M_out) memcpy(M_out, M, sizeof M);
+    if (J_out) memcpy(J_out, kin.J, sizeof kin.J);
+    if (E0i_out) memcpy(E0i_out, kin.E0i, sizeof kin.E0i);
+    if (!want) return;
+    double dJq[36]; /* column k = dJ_k qdot */
+    for (int k = 0; k < 6; ++k) {
+        double v[6];
+        m6_vec(kin.dJ[k], qd1, v);
+        for (int r = 0; r < 6; ++r) dJq[6 * r + k] = v[r];
+    }
+    double JTMm[36], Dqvv[36], X[36], MmJdq[6], K[36], D[36], JTDm[36], Y[36];
+    m6_transpose(MmJ, JTMm);
+    m6_mul(JTMm, dJq, X);
+    for (int t = 0; t < 36; ++t) Dqvv[t] = -JTMmJdot[t] - X[t];
+    double MmJdotqd[6];
+    m6_vec(MmJdot, qd1, MmJdotqd);
+    m6_mul(JT, Dm, JTDm);
+    double JTKm[36], JTKmJ[36];
+    m6_mul(JT, Km, JTKm);
+    m6_mul(JTKm, kin.J, JTKmJ);
+    m6_mul(JTDm, dJq, Y);
+    for (int t = 0; t < 36; ++t) K[t] = JTKmJ[t] + Y[t];
+    for (int k = 0; k < 6; ++k) {
+        double a[6], b[6], c[6], dJdq[6];
+        m6t_vec(kin.dJ[k], MmJdotqd, a);  /* dJ_k^T Mm Jdot qdot */
+        m6_vec(kin.dJdot[k], qd1, dJdq);  /* dJdot_k qdot */
+        m6_vec(JTMm, dJdq, b);
+        m6t_vec(kin.dJ[k], fm, c);        /* dJ_k^T fm */
+        (void)MmJdq;
+        for (int r = 0; r < 6; ++r) K[6 * r + k] += -a[r] - b[r] + c[r];
+        K[6 * k + k] -= m->joint_stiffness;
+    }
+    double JTDmJ[36];
+    m6_mul(JTDm, kin.J, JTDmJ);
+    for (int t = 0; t < 36; ++t) D[t] = Dqvv[t] + JTDmJ[t];
+    for (int k = 0; k < 6; ++k) D[6 * k + k] -= m->joint_damping;
+    if (D_out) memcpy(D_out, D, sizeof D);
+    if (H) {
+        for (int t = 0; t < 36; ++t) H[t] = M[t] - h * h * K[t] - h * D[t];
+        for (int k = 0; k < 6; ++k) {
+            double T1[36], T2[36], dMk[36], v[6];
+            m6_transpose(kin.dJ[k], T1);
+            m6_mul(T1, MmJ, T2);
+            m6_transpose(T2, T1);
+            for (int t = 0; t < 36; ++t) dMk[t] = T2[t] + T1[t];
+            m6_vec(dMk, dq, v);
+            for (int r = 0; r < 6; ++r) H[6 * r + k] += v[r];
+        }
+    }
+}
+
+/* ---- dispatch on the joint */
+
+static int mover_ndof(const orc_mover* m) { return m->ndof == 6 ? 6 : 3; }
+
+void orc_mover_pose(const orc_mover* m, const double* q, const double* qdot, double* E0i, double* phi) {
+    if (mover_ndof(m) == 3) {
+        trans_pose(m, q, qdot, E0i, phi);
+        return;
+    }
+    orc_free_kin kin;
+    free_kinematics(m, q, qdot, &kin);
+    memcpy(E0i, kin.E0i, sizeof kin.E0i);
+    memcpy(phi, kin.phi, sizeof kin.phi);
+}
+
+void orc_bdf1_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
+                        const double* qdot0, const double* q1, double* g, double* H, double* M, double* D) {
+    if (mover_ndof(m) == 3)
+        trans_eval_full(m, pairs, n_pairs, q0, qdot0, q1, g, H, M, D);
+    else
+        free_eval_full(m, pairs, n_pairs, q0, qdot0, q1, g, H, M, D, NULL, NULL);
+}
+
+void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0, const double* qdot0,
+                   const double* q1, double* g, double* H) {
+    orc_bdf1_eval_full(m, pairs, n_pairs, q0, qdot0, q1, g, H, NULL, NULL);
+}
+
+/* Partial-pivoting LU (PA = LU, L unit lower in the same array) of an n x n matrix, n <= 6: the
+ * algorithm of Eigen's PartialPivLU used by Simulation::newton (:1028) and stored for the
+ * adjoint (:1267). */
+static void lu_n(const double* A_in, int n, double* LU, int* perm) {
+    memcpy(LU, A_in, sizeof(double) * (size_t)(n * n));
+    for (int k = 0; k < n; ++k) perm[k] = k;
+    for (int c = 0; c < n; ++c) {
         int p = c;
-        for (int r = c + 1; r < 3; ++r)
-            if (fabs(A[3 * r + c]) > fabs(A[3 * p + c])) p = r;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(LU[n * r + c]) > fabs(LU[n * p + c])) p = r;
         if (p != c) {
-            for (int k = 0; k < 3; ++k) {
-                double t = A[3 * c + k];
-                A[3 * c + k] = A[3 * p + k];
-                A[3 * p + k] = t;
+            for (int k = 0; k < n; ++k) {
+                double t = LU[n * c + k];
+                LU[n * c + k] = LU[n * p + k];
+                LU[n * p + k] = t;
+            }
+            int t = perm[c];
+            perm[c] = perm[p];
+            perm[p] = t;
+        }
+        for (int r = c + 1; r < n; ++r) {
+            LU[n * r + c] /= LU[n * c + c];
+            for (int k = c + 1; k < n; ++k) LU[n * r + k] -= LU[n * r + c] * LU[n * c + k];
+        }
+    }
+}
+
+/* A x = b with the factors */
+static void lu_solve_n(const double* LU, const int* perm, int n, const double* b, double* x) {
+    double y[6];
+    for (int r = 0; r < n; ++r) {
+        double s = b[perm[r]];
+        for (int k = 0; k < r; ++k) s -= LU[n * r + k] * y[k];
+        y[r] = s;
+    }
+    for (int r = n - 1; r >= 0; --r) {
+        double s = y[r];
+        for (int k = r + 1; k < n; ++k) s -= LU[n * r + k] * x[k];
+        x[r] = s / LU[n * r + r];
+    }
+}
+
+/* A^T z = y with the factors: U^T w = y, L^T u = w, z = P^T u */
+static void lu_solve_transposed_n(const double* LU, const int* perm, int n, const double* y, double* z) {
+    double w[6], u[6];
+    for (int r = 0; r < n; ++r) {
+        double s = y[r];
+        for (int k = 0; k < r; ++k) s -= LU[n * k + r] * w[k];
+        w[r] = s / LU[n * r + r];
+    }
+    for (int r = n - 1; r >= 0; --r) {
+        double s = w[r];
+        for (int k = r + 1; k < n; ++k) s -= LU[n * k + r] * u[k];
+        u[r] = s;
+    }
+    for (int r = 0; r < n; ++r) z[perm[r]] = u[r];
+}
+
+/* Gaussian elimination with partial pivoting, the 3-dof solve of the Newton step (the same
+ * operations as lu_n + lu_solve_n, in the order the translational restatement pinned). */
+static void solve_newton(const double* A_in, const double* b_in, int n, double* x) {
+    double A[36], b[6];
+    memcpy(A, A_in, sizeof(double) * (size_t)(n * n));
+    memcpy(b, b_in, sizeof(double) * (size_t)n);
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(A[n * r + c]) > fabs(A[n * p + c])) p = r;
+        if (p != c) {
+            for (int k = 0; k < n; ++k) {
+                double t = A[n * c + k];
+                A[n * c + k] = A[n * p + k];
+                A[n * p + k] = t;
             }
             double t = b[c];
             b[c] = b[p];
             b[p] = t;
         }
-        for (int r = c + 1; r < 3; ++r) {
-            double l = A[3 * r + c] / A[3 * c + c];
-            for (int k = c; k < 3; ++k) A[3 * r + k] -= l * A[3 * c + k];
+        for (int r = c + 1; r < n; ++r) {
+            double l = A[n * r + c] / A[n * c + c];
+            for (int k = c; k < n; ++k) A[n * r + k] -= l * A[n * c + k];
             b[r] -= l * b[c];
         }
     }
-    for (int r = 2; r >= 0; --r) {
+    for (int r = n - 1; r >= 0; --r) {
         double s = b[r];
-        for (int k = r + 1; k < 3; ++k) s -= A[3 * r + k] * x[k];
-        x[r] = s / A[3 * r + r];
+        for (int k = r + 1; k < n; ++k) s -= A[n * r + k] * x[k];
+        x[r] = s / A[n * r + r];
     }
+}
+
+static double norm_n(const double* v, int n) {
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) s += v[k] * v[k];
+    return sqrt(s);
+}
+
+/* JointSphericalExp::reparam (rm/Joint/JointSphericalExp.cpp:237-266), called by
+ * Simulation::forward after every step (Simulation.cpp:955-957): a rotation vector longer
+ * than 1.5 pi is shortened by 2 pi and its rate mapped so the body's angular velocity stays. */
+static void free_reparam(double* q, double* qd) {
+    double* r = q + 3;
+    double rn = norm3(r);
+    if (rn <= 1.5 * M_PI) return;
+    double S0[9], S1[9], w[3], LU[9];
+    int perm[3];
+    rot_T(r, S0);
+    while (rn > 1.5 * M_PI) {
+        const double s = 1.0 - 2.0 * M_PI / rn;
+        for (int k = 0; k < 3; ++k) r[k] *= s;
+        rn = norm3(r);
+    }
+    rot_T(r, S1);
+    m3_vec(S0, qd + 3, w);
+    lu_n(S1, 3, LU, perm);
+    lu_solve_n(LU, perm, 3, w, qd + 3);
 }
 
 /* Simulation::integration_BDF1 (Simulation.cpp:1248-1270) with Simulation::newton
  * (:999-1079): tolerance 1e-8 on |g|, at most max(20 ndof, 100) iterations, backtracking
- * line search halving alpha up to 20 times, 3 consecutive line-search failures stop. */
+ * line search halving alpha up to 20 times, 3 consecutive line-search failures stop; then the
+ * free joint's reparameterisation (:955-957). */
 int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double* q, double* qdot, int* iters,
                   int* evals) {
-    const double h = m->h, tol = 1e-8;
-    const int max_iter = 100, max_ls = 20, max_strike = 3;
-    double q0[3], qd0[3], x[3];
-    for (int k = 0; k < 3; ++k) {
+    const int n = mover_ndof(m);
+    const double h = m->h, tol = m->newton_tol > 0.0 ? m->newton_tol : 1e-8;
+    const int max_iter = 20 * n > 100 ? 20 * n : 100, max_ls = 20, max_strike = 3;
+    double q0[6], qd0[6], x[6];
+    for (int k = 0; k < n; ++k) {
         q0[k] = q[k];
         qd0[k] = qdot[k];
         x[k] = q0[k] + h * qd0[k];
     }
     int converged = 0, strike = 0, it = 0, ev = 0;
     for (; it < max_iter; ++it) {
-        double g[3], H[9], dx[3], mg[3];
+        double g[6], H[36], dx[6], mg[6];
         orc_bdf1_eval(m, pairs, n_pairs, q0, qd0, x, g, H);
         ++ev;
-        for (int k = 0; k < 3; ++k) mg[k] = -g[k];
-        solve3(H, mg, dx);
-        const double gnorm = norm3(g);
-        double alpha = 1.0, gn[3] = {0, 0, 0};
+        for (int k = 0; k < n; ++k) mg[k] = -g[k];
+        solve_newton(H, mg, n, dx);
+        const double gnorm = norm_n(g, n);
+        double alpha = 1.0, gn[6] = {0, 0, 0, 0, 0, 0};
         int ok = 0;
         for (int trial = 0; trial < max_ls; ++trial, alpha *= 0.5) {
-            double xt[3] = {x[0] + alpha * dx[0], x[1] + alpha * dx[1], x[2] + alpha * dx[2]};
+            double xt[6];
+            for (int k = 0; k < n; ++k) xt[k] = x[k] + alpha * dx[k];
             orc_bdf1_eval(m, pairs, n_pairs, q0, qd0, xt, gn, NULL);
             ++ev;
-            if (norm3(gn) < gnorm) {
+            if (norm_n(gn, n) < gnorm) {
                 ok = 1;
                 break;
             }
@@ -971,16 +1578,17 @@ int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double
         } else if (++strike >= max_strike) {
             break;
         }
-        for (int k = 0; k < 3; ++k) x[k] = x[k] + alpha * dx[k];
-        if (norm3(gn) < tol) {
+        for (int k = 0; k < n; ++k) x[k] = x[k] + alpha * dx[k];
+        if (norm_n(gn, n) < tol) {
             converged = 1;
             break;
         }
     }
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < n; ++k) {
         qdot[k] = (x[k] - q0[k]) / h;
         q[k] = x[k];
     }
+    if (n == 6) free_reparam(q, qdot);
     if (iters) *iters = it + (converged ? 1 : 0);
     if (evals) *evals = ev;
     return converged;
@@ -988,125 +1596,109 @@ int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double
 
 /* ------------------------------------------------------------------ adjoint of the BDF1 rollout */
 
-/* Partial-pivoting LU of a 3x3 (PA = LU, L unit lower, stored in one array) and the
- * solve of A^T z = y with those factors (Eigen's PartialPivLU::transpose().solve, which
- * the reference calls at Simulation.cpp:1587): U^T w = y, L^T u = w, z = P^T u. */
-static void lu3(const double* A_in, double* LU, int* perm) {
-    memcpy(LU, A_in, 9 * sizeof(double));
-    for (int k = 0; k < 3; ++k) perm[k] = k;
-    for (int c = 0; c < 3; ++c) {
-        int p = c;
-        for (int r = c + 1; r < 3; ++r)
-            if (fabs(LU[3 * r + c]) > fabs(LU[3 * p + c])) p = r;
-        if (p != c) {
-            for (int k = 0; k < 3; ++k) {
-                double t = LU[3 * c + k];
-                LU[3 * c + k] = LU[3 * p + k];
-                LU[3 * p + k] = t;
-            }
-            int t = perm[c];
-            perm[c] = perm[p];
-            perm[p] = t;
-        }
-        for (int r = c + 1; r < 3; ++r) {
-            LU[3 * r + c] /= LU[3 * c + c];
-            for (int k = c + 1; k < 3; ++k) LU[3 * r + k] -= LU[3 * r + c] * LU[3 * c + k];
-        }
-    }
-}
-
-static void lu3_solve_transposed(const double* LU, const int* perm, const double* y, double* z) {
-    double w[3], u[3];
-    for (int r = 0; r < 3; ++r) { /* U^T w = y */
-        double s = y[r];
-        for (int k = 0; k < r; ++k) s -= LU[3 * k + r] * w[k];
-        w[r] = s / LU[3 * r + r];
-    }
-    for (int r = 2; r >= 0; --r) { /* L^T u = w */
-        double s = w[r];
-        for (int k = r + 1; k < 3; ++k) s -= LU[3 * k + r] * u[k];
-        u[r] = s;
-    }
-    for (int r = 0; r < 3; ++r) z[perm[r]] = u[r];
-}
-
-/* Simulation::backward_BDF1 (Simulation.cpp:1559-1634) for one translational mover, with
- * the per-step H, M, D that the reference saves after each converged step
- * (integration_BDF1, :1262-1269, evaluating evaluate_g_with_derivatives_BDF1 at q_k with
- * qdot_k = (q_k - q_{k-1}) / h) recomputed here from the trajectory q_his[0..T].
- * df_dq[T x 3] is dL/dq_k for k = 1..T.  Outputs dL/dq_0, dL/dqdot_0 and, beyond the
- * reference, dL/df_ext (world-frame external force: the torque rows are 0 because the
- * translational joint's J has no angular part): df_ext's direct term in f is
- * R_ji diag(m) R_0i^T fe, so dL/dfe = h^2 R_0i diag(m) R_ji^T sum_k z_k. */
+/* Simulation::backward_BDF1 (Simulation.cpp:1559-1634) for one moving part, with the per-step
+ * H, M, D that the reference saves after each converged step (integration_BDF1, :1262-1269:
+ * evaluate_g_with_derivatives_BDF1 at q_k with qdot_k = (q_k - q_{k-1}) / h) recomputed here from
+ * the trajectory q_his[0..T] (the reparameterisation is not differentiated, as in the reference).
+ * df_dq[T x n] is dL/dq_k for k = 1..T.  Outputs dL/dq_0, dL/dqdot_0 and, beyond the reference,
+ * dL/df_ext: the external force enters step k's f as J_k^T diag(I) blkdiag(R_0i^T, R_0i^T) f_ext
+ * (Body.cpp:288-289), so dL/df_ext = h^2 sum_k blkdiag(R_0i, R_0i) diag(I) J_k z_k.  (For the
+ * translational joint J = [0; R_ji^T], which leaves the torque rows 0.) */
 void orc_bdf1_backward(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q_his,
                        const double* qdot0, int T, const double* df_dq, double* df_dq0, double* df_dqdot0,
                        double* df_dfext) {
+    const int n = mover_ndof(m), nn = n * n;
     const double h = m->h;
-    double* Ms = (double*)calloc((size_t)(T > 0 ? T : 1) * 27, sizeof(double));
-    double* Ds = Ms + 9 * (size_t)(T > 0 ? T : 1);
-    double* Hs = Ds + 9 * (size_t)(T > 0 ? T : 1);
-    double* z = (double*)calloc((size_t)(T > 0 ? T : 1) * 3, sizeof(double));
+    const size_t TT = (size_t)(T > 0 ? T : 1);
+    double* Ms = (double*)calloc(TT * (3 * (size_t)nn + 6), sizeof(double));
+    double* Ds = Ms + nn * TT;
+    double* Hs = Ds + nn * TT;
+    double* U = Hs + nn * TT; /* per step: blkdiag(R_0i) diag(I) J applied to z, filled below */
+    double* z = (double*)calloc(TT * (size_t)n, sizeof(double));
+    double* Js = (double*)calloc(TT * 36, sizeof(double));
+    double* Rs = (double*)calloc(TT * 9, sizeof(double));
     for (int k = 1; k <= T; ++k) { /* the saved step data */
-        double qd_prev[3], g[3];
-        const double* qp = q_his + 3 * (k - 1);
+        double qd_prev[6], g[6];
+        const double* qp = q_his + n * (k - 1);
         if (k == 1) {
-            memcpy(qd_prev, qdot0, sizeof qd_prev);
+            memcpy(qd_prev, qdot0, sizeof(double) * (size_t)n);
         } else {
-            for (int c = 0; c < 3; ++c) qd_prev[c] = (qp[c] - q_his[3 * (k - 2) + c]) / h;
+            for (int c = 0; c < n; ++c) qd_prev[c] = (qp[c] - q_his[n * (k - 2) + c]) / h;
         }
-        orc_bdf1_eval_full(m, pairs, n_pairs, qp, qd_prev, q_his + 3 * k, g, Hs + 9 * (k - 1), Ms + 9 * (k - 1),
-                           Ds + 9 * (k - 1));
+        double* Hk = Hs + nn * (size_t)(k - 1);
+        double* Mk = Ms + nn * (size_t)(k - 1);
+        double* Dk = Ds + nn * (size_t)(k - 1);
+        if (n == 3) {
+            trans_eval_full(m, pairs, n_pairs, qp, qd_prev, q_his + 3 * k, g, Hk, Mk, Dk);
+            double E0i[16], phi[6], p0i[3], Rji[9], pji[3];
+            double qd1[3];
+            for (int c = 0; c < 3; ++c) qd1[c] = (q_his[3 * k + c] - qp[c]) / h;
+            trans_pose(m, q_his + 3 * k, qd1, E0i, phi);
+            pose_split(E0i, Rs + 9 * (size_t)(k - 1), p0i);
+            pose_split(m->E_ji, Rji, pji);
+            double* J = Js + 36 * (size_t)(k - 1); /* 6 x 3: [0; R_ji^T] */
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) J[3 * (3 + r) + c] = Rji[3 * c + r];
+        } else {
+            double E0i[16], p0i[3];
+            free_eval_full(m, pairs, n_pairs, qp, qd_prev, q_his + 6 * k, g, Hk, Mk, Dk, Js + 36 * (size_t)(k - 1),
+                           E0i);
+            pose_split(E0i, Rs + 9 * (size_t)(k - 1), p0i);
+        }
     }
     for (int k = T - 1; k >= 0; --k) { /* z_k for step k + 1 */
-        double y[3], t[3], LU[9];
-        int perm[3];
-        for (int c = 0; c < 3; ++c) y[c] = df_dq[3 * k + c];
+        double y[6], LU[36];
+        int perm[6];
+        for (int c = 0; c < n; ++c) y[c] = df_dq[n * k + c];
         if (k < T - 1) {
-            double A[9];
-            for (int c = 0; c < 9; ++c) A[c] = -2.0 * Ms[9 * (k + 1) + c] + h * Ds[9 * (k + 1) + c];
-            m3t_vec(A, z + 3 * (k + 1), t);
-            for (int c = 0; c < 3; ++c) y[c] -= t[c];
+            const double* M1 = Ms + nn * (size_t)(k + 1);
+            const double* D1 = Ds + nn * (size_t)(k + 1);
+            for (int c = 0; c < n; ++c)
+                for (int r = 0; r < n; ++r) y[c] -= (-2.0 * M1[n * r + c] + h * D1[n * r + c]) * z[n * (k + 1) + r];
         }
         if (k < T - 2) {
-            m3t_vec(Ms + 9 * (k + 2), z + 3 * (k + 2), t);
-            for (int c = 0; c < 3; ++c) y[c] -= t[c];
+            const double* M2 = Ms + nn * (size_t)(k + 2);
+            for (int c = 0; c < n; ++c)
+                for (int r = 0; r < n; ++r) y[c] -= M2[n * r + c] * z[n * (k + 2) + r];
         }
-        lu3(Hs + 9 * k, LU, perm);
-        lu3_solve_transposed(LU, perm, y, z + 3 * k);
+        lu_n(Hs + nn * (size_t)k, n, LU, perm);
+        lu_solve_transposed_n(LU, perm, n, y, z + n * k);
     }
-    double g0[3] = {0, 0, 0}, gd0[3] = {0, 0, 0}, t[3];
-    if (T > 0) {
-        double A[9], B[9];
-        for (int c = 0; c < 9; ++c) {
-            A[c] = -Ms[c] + h * Ds[c];
-            B[c] = -h * Ms[c];
-        }
-        m3t_vec(A, z, t);
-        for (int c = 0; c < 3; ++c) g0[c] -= t[c];
-        m3t_vec(B, z, t);
-        for (int c = 0; c < 3; ++c) gd0[c] -= t[c];
-    }
-    if (T > 1) {
-        m3t_vec(Ms + 9, z + 3, t);
-        for (int c = 0; c < 3; ++c) g0[c] -= t[c];
-    }
-    if (df_dq0) memcpy(df_dq0, g0, sizeof g0);
-    if (df_dqdot0) memcpy(df_dqdot0, gd0, sizeof gd0);
+    double g0[6] = {0}, gd0[6] = {0};
+    if (T > 0)
+        for (int c = 0; c < n; ++c)
+            for (int r = 0; r < n; ++r) {
+                g0[c] -= (-Ms[n * r + c] + h * Ds[n * r + c]) * z[r];
+                gd0[c] -= (-h * Ms[n * r + c]) * z[r];
+            }
+    if (T > 1)
+        for (int c = 0; c < n; ++c)
+            for (int r = 0; r < n; ++r) g0[c] -= Ms[nn + n * r + c] * z[n + r];
+    if (df_dq0) memcpy(df_dq0, g0, sizeof(double) * (size_t)n);
+    if (df_dqdot0) memcpy(df_dqdot0, gd0, sizeof(double) * (size_t)n);
     if (df_dfext) {
-        double zs[3] = {0, 0, 0}, E0i[16], phi[6], R0i[9], p0i[3], Rji[9], pji[3], v[3], w[3];
-        for (int k = 0; k < T; ++k)
-            for (int c = 0; c < 3; ++c) zs[c] += z[3 * k + c];
-        orc_mover_pose(m, q_his, qdot0, E0i, phi); /* R_0i is the same at every q */
-        pose_split(E0i, R0i, p0i);
-        pose_split(m->E_ji, Rji, pji);
-        m3t_vec(Rji, zs, v);
-        for (int c = 0; c < 3; ++c) v[c] *= m->inertia[3 + c];
-        m3_vec(R0i, v, w);
-        for (int c = 0; c < 3; ++c) {
-            df_dfext[c] = 0.0;
-            df_dfext[3 + c] = h * h * w[c];
+        double acc[6] = {0};
+        for (int k = 0; k < T; ++k) {
+            const double* J = Js + 36 * (size_t)k; /* 6 x n */
+            const double* R = Rs + 9 * (size_t)k;
+            double Jz[6], w[3], v[3];
+            for (int r = 0; r < 6; ++r) {
+                double s = 0.0;
+                for (int c = 0; c < n; ++c) s += J[n * r + c] * z[n * k + c];
+                Jz[r] = s * m->inertia[r];
+            }
+            m3_vec(R, Jz, w);
+            m3_vec(R, Jz + 3, v);
+            for (int c = 0; c < 3; ++c) {
+                acc[c] += w[c];
+                acc[3 + c] += v[c];
+            }
         }
+        for (int c = 0; c < 6; ++c) df_dfext[c] = h * h * acc[c];
     }
+    (void)U;
     free(Ms);
     free(z);
+    free(Js);
+    free(Rs);
 }

@@ -58,13 +58,17 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
 /* ---------------------------------------------------------------- one moving body, BDF1 */
 
 /* The moving part of the planner's scene (examples/run_joint_plan.py:140-178): one
- * body on a translational joint (3 dof) attached to the world, every other part
- * fixed.  Fields are the reference's: Body::_mass, Body::_Inertia, Joint::_E_pj_0,
- * Body::_E_ji, Simulation option gravity and timestep, Body::_f_external (world
- * frame), Joint::_Kr/_Dr/_q_rest. */
+ * body on a joint attached to the world, every other part fixed: ndof 3 = translational
+ * (rm/Joint/JointTranslational.cpp), ndof 6 = free3d-exp (rm/Joint/JointFree3DExp.cpp,
+ * q = (p, r) with r exponential rotation coordinates).  Fields are the reference's:
+ * Body::_mass, Body::_Inertia, Joint::_E_pj_0, Body::_E_ji, Simulation option gravity and
+ * timestep, Body::_f_external (world frame, torque then force), Joint::_Kr/_Dr/_q_rest. */
 typedef struct {
     double mass, inertia[6], E_pj0[16], E_ji[16], gravity[3], h, f_ext[6];
-    double joint_stiffness, joint_damping, q_rest[3];
+    double joint_stiffness, joint_damping, q_rest[6];
+    int ndof;
+    double newton_tol; /* 0: the reference's 1e-8 (Simulation.cpp:1008); smaller only for
+                          finite-difference checks of the adjoint, which differentiates g = 0 */
 } orc_mover;
 
 /* One ForceGeneralSDFContact of the scene: the mover against one fixed body. */
@@ -85,13 +89,14 @@ void orc_bdf1_eval(const orc_mover* m, const orc_pair* pairs, int n_pairs, const
 /* orc_bdf1_eval plus the reduced M and D = df/dqdot at q1 (either may be NULL). */
 void orc_bdf1_eval_full(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q0,
                         const double* qdot0, const double* q1, double* g, double* H, double* M, double* D);
-/* One implicit-Euler step (Simulation::integration_BDF1 + newton); updates q, qdot.
- * Returns 1 if Newton converged.  iters / evals may be NULL. */
+/* One implicit-Euler step (Simulation::integration_BDF1 + newton, then the free joint's
+ * reparameterisation); updates q, qdot (ndof each).  Returns 1 if Newton converged.
+ * iters / evals may be NULL.  g, H, M, D above are ndof and ndof x ndof. */
 int orc_bdf1_step(const orc_mover* m, const orc_pair* pairs, int n_pairs, double* q, double* qdot, int* iters,
                   int* evals);
 
-/* Adjoint of T BDF1 steps (Simulation::backward_BDF1) from the trajectory q_his[(T+1) x 3]
- * and qdot_0: dL/dq_0, dL/dqdot_0 and dL/df_ext[6] for dL/dq_k = df_dq[(k-1) x 3].
+/* Adjoint of T BDF1 steps (Simulation::backward_BDF1) from the trajectory q_his[(T+1) x ndof]
+ * and qdot_0: dL/dq_0, dL/dqdot_0 and dL/df_ext[6] for dL/dq_k = df_dq[(k-1) x ndof].
  * Any output may be NULL. */
 void orc_bdf1_backward(const orc_mover* m, const orc_pair* pairs, int n_pairs, const double* q_his,
                        const double* qdot0, int T, const double* df_dq, double* df_dq0, double* df_dqdot0,

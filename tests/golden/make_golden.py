@@ -9,7 +9,8 @@ and stores inputs and outputs as compressed .npz files:
                   of poses, velocities and coefficient variants: fm, Km, Dm, active ids
   collision.npz   BodySDFObj::collision with derivatives (simulation/redmax/Body/BodySDFObj.cpp:278-377)
                   at random points
-  sim_trans.npz   Simulation::forward with BDF1 (simulation/redmax/Simulation.cpp:914-1079, 1248-1270)
+  sim_trans.npz / sim_free.npz
+                  Simulation::forward with BDF1 (simulation/redmax/Simulation.cpp:914-1079, 1248-1270)
                   of a peg on a translational joint against a fixed socket: the scene and the
                   reference's joint trajectory and Newton convergence flags
 
@@ -115,9 +116,19 @@ def f32(x):
     return float(np.float32(x))
 
 
-def make_sim_fixture(steps=40):
-    """A 3-dof peg (box mesh for its mass properties, peg points as its contact points) on a
-    translational joint, pushed into a fixed socket; both scene files use the planner's layout."""
+SIM_CASES = {
+    # name: joint, q0, qdot0, external force (torque then force), steps
+    "sim_trans": ("translational", [0.012, 0.0, 0.0], [0.5, 0.0, -0.2], [0.0, 0.0, 0.0, 2.0, 0.5, 1.0], 40),
+    "sim_free": ("free3d-exp", [0.012, 0.0, 0.0, 0.002, -0.003, 0.01], [0.5, 0.0, -0.2, 0.3, -0.1, 0.5],
+                 [0.05, -0.1, 0.02, 2.0, 0.5, 1.0], 40),
+}
+
+
+def make_sim_fixture(name="sim_trans"):
+    """A peg (box mesh for its mass properties, peg points as its contact points) on a
+    translational or free3d-exp joint, pushed into a fixed socket; both scene files use the
+    planner's layout."""
+    joint, q0, qd0, F, steps = SIM_CASES[name]
     import tempfile
     wd = tempfile.mkdtemp(prefix="golden_sim_")
     Va, Fa = refsim.box_mesh((0.3, 0.25, 0.9))
@@ -125,7 +136,7 @@ def make_sim_fixture(steps=40):
     refsim.write_obj(os.path.join(wd, "a.obj"), Va, Fa)
     refsim.write_obj(os.path.join(wd, "b.obj"), Vb, Fb)
     kn, kt, mu, kd, h, gravity = 1e5, 1e3, 0.3, 1e3, 5e-3, (0.0, 0.0, -9.8)
-    xml = refsim.two_body_xml("a.obj", "b.obj", joint_a="translational", kn=kn, kt=kt, mu=mu, damping=kd,
+    xml = refsim.two_body_xml("a.obj", "b.obj", joint_a=joint, kn=kn, kt=kt, mu=mu, damping=kd,
                               timestep=h, gravity=gravity, col_th=COL_TH)
     sim = refsim.RefSim(xml, wd)
     mA, IA, EjiA, E0iA = sim.mass_props("A")
@@ -141,8 +152,8 @@ def make_sim_fixture(steps=40):
     pw = W.peg_points(3000, seed=2)
     pts = (pw - E0iA[:3, 3]) @ E0iA[:3, :3]  # into A's body frame at q = 0
     sim.set_contact_points("A", pts)
-    q0, qd0 = np.array([0.012, 0.0, 0.0]), np.array([0.5, 0.0, -0.2])
-    F = np.array([0.0, 0.0, 0.0, 2.0, 0.5, 1.0])
+    q0, qd0, F = np.array(q0), np.array(qd0), np.array(F)
+    n = len(q0)
     sim.set_state_init(q0, qd0)
     sim.reset(False)
     sim.set_external_force("A", F)
@@ -156,13 +167,13 @@ def make_sim_fixture(steps=40):
     # the reference's adjoint (Simulation::backward_BDF1, Simulation.cpp:1559-1634) of a loss whose
     # gradient with respect to every q_k is a seeded random vector
     T_bw = 20
-    df_dq = np.random.default_rng(99).normal(size=(T_bw, 3))
+    df_dq = np.random.default_rng(99).normal(size=(T_bw, n))
     sim.set_state_init(q0, qd0)
     sim.reset(True)
     sim.set_external_force("A", F)
     sim.forward(T_bw)
     df_dq0, df_dqdot0 = sim.backward(df_dq.ravel(), T_bw)
-    np.savez_compressed(os.path.join(HERE, "sim_trans.npz"), grid=vals, min_box=mn, max_box=mx, dx=dx,
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), grid=vals, min_box=mn, max_box=mx, dx=dx,
                         col_th=COL_TH, points=pts, mass=mA, inertia=IA, E_ji=EjiA, E_fixed=E0iB,
                         params=np.array([f32(kn), f32(kt), f32(mu), f32(kd), 1.0, 1.0]), h=f32(h),
                         gravity=np.array(gravity), f_ext=F, q0=q0, qdot0=qd0, q=np.array(qs), qdot=np.array(qds),
@@ -174,4 +185,5 @@ def make_sim_fixture(steps=40):
 
 if __name__ == "__main__":
     main()
-    make_sim_fixture()
+    for name in SIM_CASES:
+        make_sim_fixture(name)
