@@ -2,9 +2,12 @@
 //
 // Restates, per scene, redmax's Simulation::integration_BDF1 + Simulation::newton
 // (simulation/redmax/Simulation.cpp:999-1079, 1248-1270) with the reduced system of
-// Simulation::computeMatrices (:379-503) for one mover on a translational joint
-// (simulation/redmax/Joint/JointTranslational.cpp:9-40): J = Ad(E_ij) S_j = [0; R_ji^T]
-// is constant, so M = J^T Mm J, f = J^T fm + fr, K = J^T Km J + Kr, D = J^T Dm J + Dr.
+// Simulation::computeMatrices (:379-503) for one mover on a joint to the world:
+//   * translational (simulation/redmax/Joint/JointTranslational.cpp:9-40): J = Ad(E_ij) S_j =
+//     [0; R_ji^T] is constant, so M = J^T Mm J, f = J^T fm + fr, K = J^T Km J + Kr,
+//     D = J^T Dm J + Dr;
+//   * free3d-exp (simulation/redmax/Joint/JointFree3DExp.cpp): the full system with the
+//     configuration-dependent J, in sdfc_joint.cuh.
 //
 // Every scene runs the reference's Newton iteration as a small state machine;
 // one "round" gives every unfinished scene exactly one force evaluation (with
@@ -23,6 +26,7 @@
 #include <vector>
 
 #include "sdfc_internal.h"
+#include "sdfc_joint.cuh"
 
 using sdfc_impl::dev_alloc;
 using sdfc_impl::fail;
@@ -36,16 +40,34 @@ constexpr int kMaxStrike = 3;     // :1014
 
 enum Phase : int { kNewton = 0, kLine = 1, kDone = 2 };
 
+constexpr int kMaxDof = 6;
+
 struct MoverDev {
     double mass, inertia[6], E_pj0[16], E_ji[16], gravity[3], h, Kr, Dr;
     int max_iter;
+    int ndof;  // 3: translational, 6: free3d-exp
 };
 
 struct SceneState {
-    double q0[3], qd0[3], x[3], dx[3], xt[3];
+    double q0[kMaxDof], qd0[kMaxDof], x[kMaxDof], dx[kMaxDof], xt[kMaxDof];
     double gnorm, alpha;
     int phase, iter, trial, strike, converged;
 };
+
+__device__ inline sdfc_joint::FreeBody free_body(const MoverDev& m) {
+    sdfc_joint::FreeBody b;
+    b.mass = m.mass;
+    for (int k = 0; k < 6; ++k) b.inertia[k] = m.inertia[k];
+    for (int k = 0; k < 16; ++k) {
+        b.E_pj0[k] = m.E_pj0[k];
+        b.E_ji[k] = m.E_ji[k];
+    }
+    for (int k = 0; k < 3; ++k) b.gravity[k] = m.gravity[k];
+    b.h = m.h;
+    b.Kr = m.Kr;
+    b.Dr = m.Dr;
+    return b;
+}
 
 __device__ __forceinline__ void mat4_mul(const double* A, const double* B, double* C) {
     for (int r = 0; r < 4; ++r)
@@ -58,7 +80,7 @@ __device__ __forceinline__ void mat4_mul(const double* A, const double* B, doubl
 
 // Joint::update (E_pj = E_pj0 Q, Q = [I q; 0 1]) and Body::update (E_0i = E_0j E_ji,
 // phi = Ad(E_ij) S_j qdot = (0, R_ji^T qdot)); Joint.cpp, Body.cpp:138-156.
-__device__ void mover_pose(const MoverDev& m, const double* q, const double* qd, double* E0i, double* phi) {
+__device__ void trans_pose(const MoverDev& m, const double* q, const double* qd, double* E0i, double* phi) {
     const double Q[16] = {1, 0, 0, q[0], 0, 1, 0, q[1], 0, 0, 1, q[2], 0, 0, 0, 1};
     double E0j[16];
     mat4_mul(m.E_pj0, Q, E0j);
@@ -67,16 +89,24 @@ __device__ void mover_pose(const MoverDev& m, const double* q, const double* qd,
     for (int r = 0; r < 3; ++r) phi[3 + r] = m.E_ji[r] * qd[0] + m.E_ji[4 + r] * qd[1] + m.E_ji[8 + r] * qd[2];
 }
 
-__global__ void sim_begin_kernel(int n, const MoverDev* __restrict__ mover, const double* __restrict__ q,
+__device__ void mover_pose(const MoverDev& m, const double* q, const double* qd, double* E0i, double* phi) {
+    if (m.ndof == 6)
+        sdfc_joint::free_pose(m.E_pj0, m.E_ji, q, qd, E0i, phi);
+    else
+        trans_pose(m, q, qd, E0i, phi);
+}
+
+__global__ void sim_begin_kernel(int n, int nd, const MoverDev* __restrict__ mover, const double* __restrict__ q,
                                  const double* __restrict__ qd, SceneState* __restrict__ st, int* remaining) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *remaining = n;
     if (i >= n) return;
     SceneState s;
     const double h = mover[i].h;
-    for (int k = 0; k < 3; ++k) {
-        s.q0[k] = q[3 * i + k];
-        s.qd0[k] = qd[3 * i + k];
+    for (int k = 0; k < kMaxDof; ++k) s.q0[k] = s.qd0[k] = s.x[k] = s.dx[k] = s.xt[k] = 0.0;
+    for (int k = 0; k < nd; ++k) {
+        s.q0[k] = q[(size_t)nd * i + k];
+        s.qd0[k] = qd[(size_t)nd * i + k];
         s.x[k] = s.q0[k] + h * s.qd0[k];  // initial guess, Simulation.cpp:1256
         s.dx[k] = s.xt[k] = 0.0;
     }
@@ -101,8 +131,8 @@ __global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, 
     }
     const MoverDev& m = mover[i];
     const double* p = s.phase == kNewton ? s.x : s.xt;
-    double qd[3], E0i[16], phi[6];
-    for (int c = 0; c < 3; ++c) qd[c] = (p[c] - s.q0[c]) / m.h;
+    double qd[kMaxDof], E0i[16], phi[6];
+    for (int c = 0; c < m.ndof; ++c) qd[c] = (p[c] - s.q0[c]) / m.h;
     mover_pose(m, p, qd, E0i, phi);
     double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
     double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
@@ -119,70 +149,85 @@ __global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, 
     mode[k] = s.phase == kNewton ? 2 : 1;
 }
 
-// 3x3 solve by Gaussian elimination with partial pivoting (the algorithm of the
-// reference's PartialPivLU, Simulation.cpp:1028).
-__device__ void solve3(const double* A_in, const double* b_in, double* x) {
-    double A[9], b[3];
-    for (int k = 0; k < 9; ++k) A[k] = A_in[k];
-    for (int k = 0; k < 3; ++k) b[k] = b_in[k];
-    for (int c = 0; c < 3; ++c) {
+// n x n solve (n <= 6) by Gaussian elimination with partial pivoting (the algorithm of
+// the reference's PartialPivLU, Simulation.cpp:1028).
+__device__ void solve_n(const double* A_in, const double* b_in, int n, double* x) {
+    double A[kMaxDof * kMaxDof], b[kMaxDof];
+    for (int k = 0; k < n * n; ++k) A[k] = A_in[k];
+    for (int k = 0; k < n; ++k) b[k] = b_in[k];
+    for (int c = 0; c < n; ++c) {
         int p = c;
-        for (int r = c + 1; r < 3; ++r)
-            if (fabs(A[3 * r + c]) > fabs(A[3 * p + c])) p = r;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(A[n * r + c]) > fabs(A[n * p + c])) p = r;
         if (p != c) {
-            for (int k = 0; k < 3; ++k) {
-                const double t = A[3 * c + k];
-                A[3 * c + k] = A[3 * p + k];
-                A[3 * p + k] = t;
+            for (int k = 0; k < n; ++k) {
+                const double t = A[n * c + k];
+                A[n * c + k] = A[n * p + k];
+                A[n * p + k] = t;
             }
             const double t = b[c];
             b[c] = b[p];
             b[p] = t;
         }
-        for (int r = c + 1; r < 3; ++r) {
-            const double l = A[3 * r + c] / A[3 * c + c];
-            for (int k = c; k < 3; ++k) A[3 * r + k] -= l * A[3 * c + k];
+        for (int r = c + 1; r < n; ++r) {
+            const double l = A[n * r + c] / A[n * c + c];
+            for (int k = c; k < n; ++k) A[n * r + k] -= l * A[n * c + k];
             b[r] -= l * b[c];
         }
     }
-    for (int r = 2; r >= 0; --r) {
+    for (int r = n - 1; r >= 0; --r) {
         double s = b[r];
-        for (int k = r + 1; k < 3; ++k) s -= A[3 * r + k] * x[k];
-        x[r] = s / A[3 * r + r];
+        for (int k = r + 1; k < n; ++k) s -= A[n * r + k] * x[k];
+        x[r] = s / A[n * r + r];
     }
 }
 
-__device__ __forceinline__ double norm3d(const double* v) { return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+__device__ __forceinline__ double norm_n(const double* v, int n) {
+    double s = v[0] * v[0];
+    for (int k = 1; k < n; ++k) s += v[k] * v[k];
+    return sqrt(s);
+}
 
-__global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
-                                  const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
-                                  const double* __restrict__ fm, const double* __restrict__ Km,
-                                  const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining,
-                                  unsigned long long* evaluations) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    SceneState s = st[i];
-    if (s.phase == kDone) return;
-    atomicAdd(evaluations, 1ull);
-    const MoverDev& m = mover[i];
-    const bool newton = s.phase == kNewton;
-    const double* p = newton ? s.x : s.xt;
+// The free mover's contact sums: the mover's 6-row block of every pair's fm, Km, Dm.
+__device__ void free_contact_sums(int k0, int k1, const int* __restrict__ role, const double* __restrict__ fm,
+                                  const double* __restrict__ Km, const double* __restrict__ Dm, bool deriv,
+                                  double* fmc, double* Kmc, double* Dmc) {
+    for (int r = 0; r < 6; ++r) fmc[r] = 0.0;
+    for (int r = 0; r < 36; ++r) Kmc[r] = Dmc[r] = 0.0;
+    for (int k = k0; k < k1; ++k) {
+        const int o = role[k] ? 0 : 6;
+        for (int r = 0; r < 6; ++r) {
+            fmc[r] += fm[12 * (size_t)k + o + r];
+            if (deriv)
+                for (int c = 0; c < 6; ++c) {
+                    Kmc[6 * r + c] += Km[144 * (size_t)k + (o + r) * 12 + o + c];
+                    Dmc[6 * r + c] += Dm[144 * (size_t)k + (o + r) * 12 + o + c];
+                }
+        }
+    }
+}
+
+// The translational mover's g (and H) at p (SceneState point): reduced system of the
+// contacts' linear rows, gravity and external force.
+__device__ void trans_system(const MoverDev& m, const double* __restrict__ fe, const SceneState& s, const double* p,
+                             int k0, int k1, const int* __restrict__ role, const double* __restrict__ fm,
+                             const double* __restrict__ Km, const double* __restrict__ Dm, bool newton, double* g,
+                             double* H) {
     const double h = m.h;
     double qd[3], E0i[16], phi[6];
     for (int c = 0; c < 3; ++c) qd[c] = (p[c] - s.q0[c]) / h;
-    mover_pose(m, p, qd, E0i, phi);
+    trans_pose(m, p, qd, E0i, phi);
     // fm (linear rows) of the mover: gravity and external force (Body.cpp:247-271) + contacts
     double fl[3], Kll[9] = {0}, Dll[9] = {0};
-    const double* fe = f_ext + 6 * (size_t)i;
     for (int r = 0; r < 3; ++r) {
-        double g = 0.0, e = 0.0;
+        double gr = 0.0, e = 0.0;
         for (int c = 0; c < 3; ++c) {
-            g += E0i[4 * c + r] * (m.mass * m.gravity[c]);
+            gr += E0i[4 * c + r] * (m.mass * m.gravity[c]);
             e += E0i[4 * c + r] * fe[3 + c];
         }
-        fl[r] = g + m.inertia[3 + r] * e;
+        fl[r] = gr + m.inertia[3 + r] * e;
     }
-    for (int k = pair_begin[i]; k < pair_begin[i + 1]; ++k) {
+    for (int k = k0; k < k1; ++k) {
         const int o = role[k] ? 0 : 6;
         for (int r = 0; r < 3; ++r) {
             fl[r] += fm[12 * (size_t)k + o + 3 + r];
@@ -197,7 +242,7 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
     double R[9];
     for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) R[3 * r + c] = m.E_ji[4 * r + c];
-    double f[3], M[9], g[3];
+    double f[3], M[9];
     for (int r = 0; r < 3; ++r) {
         f[r] = R[3 * r] * fl[0] + R[3 * r + 1] * fl[1] + R[3 * r + 2] * fl[2];
         f[r] += -m.Kr * p[r] - m.Dr * qd[r];
@@ -208,47 +253,74 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
     double dq[3];
     for (int k = 0; k < 3; ++k) dq[k] = p[k] - s.q0[k] - h * s.qd0[k];
     for (int r = 0; r < 3; ++r) g[r] = M[3 * r] * dq[0] + M[3 * r + 1] * dq[1] + M[3 * r + 2] * dq[2] - h * h * f[r];
+    if (!newton) return;
+    // H = M - h^2 K - h D, K = R Kll R^T - Kr I, D = R Dll R^T - Dr I
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            double K = 0.0, D = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    K += R[3 * r + a] * Kll[3 * a + b] * R[3 * c + b];
+                    D += R[3 * r + a] * Dll[3 * a + b] * R[3 * c + b];
+                }
+            if (r == c) {
+                K -= m.Kr;
+                D -= m.Dr;
+            }
+            H[3 * r + c] = M[3 * r + c] - h * h * K - h * D;
+        }
+}
+
+__global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
+                                  const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
+                                  const double* __restrict__ fm, const double* __restrict__ Km,
+                                  const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining,
+                                  unsigned long long* evaluations) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    SceneState s = st[i];
+    if (s.phase == kDone) return;
+    atomicAdd(evaluations, 1ull);
+    const MoverDev& m = mover[i];
+    const int nd = m.ndof;
+    const bool newton = s.phase == kNewton;
+    const double* p = newton ? s.x : s.xt;
+    const double* fe = f_ext + 6 * (size_t)i;
+    double g[kMaxDof], H[kMaxDof * kMaxDof];
+    if (nd == 6) {
+        double fmc[6], Kmc[36], Dmc[36], M[36];
+        free_contact_sums(pair_begin[i], pair_begin[i + 1], role, fm, Km, Dm, newton, fmc, Kmc, Dmc);
+        sdfc_joint::free_system(free_body(m), fe, s.q0, s.qd0, p, fmc, Kmc, Dmc, newton, g, newton ? H : nullptr, M,
+                                nullptr, nullptr, nullptr);
+    } else {
+        trans_system(m, fe, s, p, pair_begin[i], pair_begin[i + 1], role, fm, Km, Dm, newton, g, H);
+    }
     bool done = false;
     if (newton) {
-        // H = M - h^2 K - h D, K = R Kll R^T - Kr I, D = R Dll R^T - Dr I
-        double H[9];
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) {
-                double K = 0.0, D = 0.0;
-                for (int a = 0; a < 3; ++a)
-                    for (int b = 0; b < 3; ++b) {
-                        K += R[3 * r + a] * Kll[3 * a + b] * R[3 * c + b];
-                        D += R[3 * r + a] * Dll[3 * a + b] * R[3 * c + b];
-                    }
-                if (r == c) {
-                    K -= m.Kr;
-                    D -= m.Dr;
-                }
-                H[3 * r + c] = M[3 * r + c] - h * h * K - h * D;
-            }
-        const double mg[3] = {-g[0], -g[1], -g[2]};
-        solve3(H, mg, s.dx);
-        s.gnorm = norm3d(g);
+        double mg[kMaxDof];
+        for (int k = 0; k < nd; ++k) mg[k] = -g[k];
+        solve_n(H, mg, nd, s.dx);
+        s.gnorm = norm_n(g, nd);
         s.alpha = 1.0;
         s.trial = 0;
-        for (int k = 0; k < 3; ++k) s.xt[k] = s.x[k] + s.dx[k];
+        for (int k = 0; k < nd; ++k) s.xt[k] = s.x[k] + s.dx[k];
         s.phase = kLine;
     } else {
-        const double gn = norm3d(g);
+        const double gn = norm_n(g, nd);
         bool step_done = false;
         if (gn < s.gnorm) {  // line search succeeded
             s.strike = 0;
-            for (int k = 0; k < 3; ++k) s.x[k] = s.xt[k];
+            for (int k = 0; k < nd; ++k) s.x[k] = s.xt[k];
             step_done = true;
         } else if (++s.trial < kMaxLineSearch) {
             s.alpha *= 0.5;
-            for (int k = 0; k < 3; ++k) s.xt[k] = s.x[k] + s.alpha * s.dx[k];
+            for (int k = 0; k < nd; ++k) s.xt[k] = s.x[k] + s.alpha * s.dx[k];
         } else {  // 20 failures: alpha = 0.5^20
             s.alpha *= 0.5;
             if (++s.strike >= kMaxStrike) {
                 done = true;  // stops before the update, Simulation.cpp:1052-1054
             } else {
-                for (int k = 0; k < 3; ++k) s.x[k] = s.x[k] + s.alpha * s.dx[k];
+                for (int k = 0; k < nd; ++k) s.x[k] = s.x[k] + s.alpha * s.dx[k];
                 step_done = true;
             }
         }
@@ -271,14 +343,20 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
     st[i] = s;
 }
 
-__global__ void sim_end_kernel(int n, const MoverDev* __restrict__ mover, const SceneState* __restrict__ st,
+__global__ void sim_end_kernel(int n, int nd, const MoverDev* __restrict__ mover, const SceneState* __restrict__ st,
                                double* __restrict__ q, double* __restrict__ qd, int* __restrict__ converged) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SceneState& s = st[i];
-    for (int k = 0; k < 3; ++k) {
-        q[3 * i + k] = s.x[k];
-        qd[3 * i + k] = (s.x[k] - s.q0[k]) / mover[i].h;
+    double x[kMaxDof], v[kMaxDof];
+    for (int k = 0; k < nd; ++k) {
+        x[k] = s.x[k];
+        v[k] = (s.x[k] - s.q0[k]) / mover[i].h;
+    }
+    if (nd == 6) sdfc_joint::free_reparam(x, v);  // Simulation::forward, Simulation.cpp:955-957
+    for (int k = 0; k < nd; ++k) {
+        q[(size_t)nd * i + k] = x[k];
+        qd[(size_t)nd * i + k] = v[k];
     }
     converged[i] = s.converged;
 }
@@ -291,9 +369,14 @@ __global__ void sim_end_kernel(int n, const MoverDev* __restrict__ mover, const 
 // trajectory q_0..q_T and the backward recomputes each step's H, D in reverse order,
 // one batched evaluation per step, while it runs the recursion
 //   z_k = H_k^{-T} (dL/dq_k - (-2M + h D_{k+1})^T z_{k+1} - M^T z_{k+2}).
+// (The free joint's reparameterisation between steps is not differentiated, as in the
+// reference.)
 
 struct AdjState {
-    double z1[3], z2[3], D1[9], zs[3];  // z_{k+1}, z_{k+2}, D_{k+1}, sum of z
+    double z1[kMaxDof], z2[kMaxDof];                       // z_{k+1}, z_{k+2}
+    double D1[kMaxDof * kMaxDof], M1[kMaxDof * kMaxDof];   // D_{k+1}, M_{k+1}
+    double M2[kMaxDof * kMaxDof];                          // M_{k+2}
+    double acc[6];  // sum over steps of blkdiag(R_0i) diag(I) J z (the external force's gradient / h^2)
 };
 
 __global__ void adj_begin_kernel(int n, int T, AdjState* __restrict__ adj, int* __restrict__ t_dev) {
@@ -304,27 +387,28 @@ __global__ void adj_begin_kernel(int n, int T, AdjState* __restrict__ adj, int* 
     }
     if (i >= n) return;
     AdjState a;
-    for (int c = 0; c < 3; ++c) a.z1[c] = a.z2[c] = a.zs[c] = 0.0;
-    for (int c = 0; c < 9; ++c) a.D1[c] = 0.0;
+    for (int c = 0; c < kMaxDof; ++c) a.z1[c] = a.z2[c] = 0.0;
+    for (int c = 0; c < kMaxDof * kMaxDof; ++c) a.D1[c] = a.M1[c] = a.M2[c] = 0.0;
+    for (int c = 0; c < 6; ++c) a.acc[c] = 0.0;
     adj[i] = a;
 }
 
 // Pose of every pair at step t of the recorded trajectory (q_his is step-major:
-// q_his[(t * n + scene) * 3 + c]).
-__global__ void adj_pose_kernel(int n_pairs, int n, const int* __restrict__ pair_inst, const int* __restrict__ role,
-                                const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
-                                const double* __restrict__ q_his, const int* __restrict__ t_dev,
-                                double* __restrict__ EA, double* __restrict__ phiA, double* __restrict__ EB,
-                                double* __restrict__ phiB) {
+// q_his[(t * n + scene) * nd + c]).
+__global__ void adj_pose_kernel(int n_pairs, int n, int nd, const int* __restrict__ pair_inst,
+                                const int* __restrict__ role, const double* __restrict__ E_fixed,
+                                const MoverDev* __restrict__ mover, const double* __restrict__ q_his,
+                                const int* __restrict__ t_dev, double* __restrict__ EA, double* __restrict__ phiA,
+                                double* __restrict__ EB, double* __restrict__ phiB) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int t = t_dev[0];
     if (k >= n_pairs || t < 1) return;
     const int i = pair_inst[k];
     const MoverDev& m = mover[i];
-    const double* q = q_his + 3 * ((size_t)t * n + i);
-    const double* qp = q_his + 3 * ((size_t)(t - 1) * n + i);
-    double qd[3], E0i[16], phi[6];
-    for (int c = 0; c < 3; ++c) qd[c] = (q[c] - qp[c]) / m.h;  // sim_end_kernel's qdot
+    const double* q = q_his + (size_t)nd * ((size_t)t * n + i);
+    const double* qp = q_his + (size_t)nd * ((size_t)(t - 1) * n + i);
+    double qd[kMaxDof], E0i[16], phi[6];
+    for (int c = 0; c < nd; ++c) qd[c] = (q[c] - qp[c]) / m.h;  // sim_end_kernel's qdot
     mover_pose(m, q, qd, E0i, phi);
     double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
     double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
@@ -340,127 +424,155 @@ __global__ void adj_pose_kernel(int n_pairs, int n, const int* __restrict__ pair
     }
 }
 
-// Partial-pivoting LU of a 3x3 and the solve of A^T z = y with it (Eigen's
-// PartialPivLU::transpose().solve, Simulation.cpp:1587): U^T w = y, L^T u = w, z = P^T u.
-__device__ void lu3_solve_transposed(const double* A, const double* y, double* z) {
-    double LU[9], w[3], u[3];
-    int perm[3] = {0, 1, 2};
-    for (int k = 0; k < 9; ++k) LU[k] = A[k];
-    for (int c = 0; c < 3; ++c) {
+// Partial-pivoting LU of an n x n matrix (n <= 6) and the solve of A^T z = y with it
+// (Eigen's PartialPivLU::transpose().solve, Simulation.cpp:1587): U^T w = y, L^T u = w,
+// z = P^T u.
+__device__ void lu_solve_transposed(const double* A, int n, const double* y, double* z) {
+    double LU[kMaxDof * kMaxDof], w[kMaxDof], u[kMaxDof];
+    int perm[kMaxDof];
+    for (int k = 0; k < n * n; ++k) LU[k] = A[k];
+    for (int k = 0; k < n; ++k) perm[k] = k;
+    for (int c = 0; c < n; ++c) {
         int p = c;
-        for (int r = c + 1; r < 3; ++r)
-            if (fabs(LU[3 * r + c]) > fabs(LU[3 * p + c])) p = r;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(LU[n * r + c]) > fabs(LU[n * p + c])) p = r;
         if (p != c) {
-            for (int k = 0; k < 3; ++k) {
-                const double t = LU[3 * c + k];
-                LU[3 * c + k] = LU[3 * p + k];
-                LU[3 * p + k] = t;
+            for (int k = 0; k < n; ++k) {
+                const double t = LU[n * c + k];
+                LU[n * c + k] = LU[n * p + k];
+                LU[n * p + k] = t;
             }
             const int t = perm[c];
             perm[c] = perm[p];
             perm[p] = t;
         }
-        for (int r = c + 1; r < 3; ++r) {
-            LU[3 * r + c] /= LU[3 * c + c];
-            for (int k = c + 1; k < 3; ++k) LU[3 * r + k] -= LU[3 * r + c] * LU[3 * c + k];
+        for (int r = c + 1; r < n; ++r) {
+            LU[n * r + c] /= LU[n * c + c];
+            for (int k = c + 1; k < n; ++k) LU[n * r + k] -= LU[n * r + c] * LU[n * c + k];
         }
     }
-    for (int r = 0; r < 3; ++r) {
+    for (int r = 0; r < n; ++r) {
         double s = y[r];
-        for (int k = 0; k < r; ++k) s -= LU[3 * k + r] * w[k];
-        w[r] = s / LU[3 * r + r];
+        for (int k = 0; k < r; ++k) s -= LU[n * k + r] * w[k];
+        w[r] = s / LU[n * r + r];
     }
-    for (int r = 2; r >= 0; --r) {
+    for (int r = n - 1; r >= 0; --r) {
         double s = w[r];
-        for (int k = r + 1; k < 3; ++k) s -= LU[3 * k + r] * u[k];
+        for (int k = r + 1; k < n; ++k) s -= LU[n * k + r] * u[k];
         u[r] = s;
     }
-    for (int r = 0; r < 3; ++r) z[perm[r]] = u[r];
+    for (int r = 0; r < n; ++r) z[perm[r]] = u[r];
 }
 
 // One reverse step per scene.  At t = 1 it also writes the scene's gradients
-// (:1590-1614): gout[12 i ..] = dL/dq0[3], dL/dqdot0[3], dL/df_ext[6].  The external
-// force enters f as R_ji diag(m) R_0i^T fe (sim_newton_kernel), so
-// dL/dfe = h^2 R_0i diag(m) R_ji^T sum_k z_k (torque rows 0).
-__global__ void adj_step_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
-                                const MoverDev* __restrict__ mover, const double* __restrict__ Km,
+// (:1590-1614): gout[18 i ..] = dL/dq0[nd] at 0, dL/dqdot0[nd] at 6, dL/df_ext[6] at 12.
+// The external force enters step t's f as J^T diag(I) blkdiag(R_0i^T, R_0i^T) f_ext
+// (Body.cpp:288-289), so dL/df_ext = h^2 sum_t blkdiag(R_0i) diag(I) J z_t.
+__global__ void adj_step_kernel(int n, int nd, const int* __restrict__ pair_begin, const int* __restrict__ role,
+                                const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
+                                const double* __restrict__ fm, const double* __restrict__ Km,
                                 const double* __restrict__ Dm, const double* __restrict__ q_his,
-                                const double* __restrict__ df_dq, const int* __restrict__ t_dev,
-                                AdjState* __restrict__ adj, double* __restrict__ gout) {
+                                const double* __restrict__ qd0_rec, const double* __restrict__ df_dq,
+                                const int* __restrict__ t_dev, AdjState* __restrict__ adj, double* __restrict__ gout) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int t = t_dev[0], T = t_dev[1];
     if (i >= n || t < 1) return;
     const MoverDev& m = mover[i];
     const double h = m.h;
-    double Kll[9] = {0}, Dll[9] = {0};
-    for (int k = pair_begin[i]; k < pair_begin[i + 1]; ++k) {
-        const int o = role[k] ? 0 : 6;
+    const double* q1 = q_his + (size_t)nd * ((size_t)t * n + i);
+    const double* q0 = q_his + (size_t)nd * ((size_t)(t - 1) * n + i);
+    double qd0[kMaxDof];
+    for (int c = 0; c < nd; ++c)
+        qd0[c] = t >= 2 ? (q0[c] - q_his[(size_t)nd * ((size_t)(t - 2) * n + i) + c]) / h : qd0_rec[(size_t)nd * i + c];
+    double M[36], D[36], H[36], J[36], R0i[9];  // J is 6 x nd
+    if (nd == 6) {
+        double fmc[6], Kmc[36], Dmc[36], g[6];
+        free_contact_sums(pair_begin[i], pair_begin[i + 1], role, fm, Km, Dm, true, fmc, Kmc, Dmc);
+        sdfc_joint::free_system(free_body(m), f_ext + 6 * (size_t)i, q0, qd0, q1, fmc, Kmc, Dmc, true, g, H, M, D, J,
+                                R0i);
+    } else {
+        double Kll[9] = {0}, Dll[9] = {0}, R[9];
+        for (int k = pair_begin[i]; k < pair_begin[i + 1]; ++k) {
+            const int o = role[k] ? 0 : 6;
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    Kll[3 * r + c] += Km[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+                    Dll[3 * r + c] += Dm[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+                }
+        }
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) R[3 * r + c] = m.E_ji[4 * r + c];
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 3; ++c) {
-                Kll[3 * r + c] += Km[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
-                Dll[3 * r + c] += Dm[144 * (size_t)k + (o + 3 + r) * 12 + o + 3 + c];
+                M[3 * r + c] = R[3 * r] * m.inertia[3] * R[3 * c] + R[3 * r + 1] * m.inertia[4] * R[3 * c + 1] +
+                               R[3 * r + 2] * m.inertia[5] * R[3 * c + 2];
+                double K = 0.0, Dv = 0.0;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        K += R[3 * r + a] * Kll[3 * a + b] * R[3 * c + b];
+                        Dv += R[3 * r + a] * Dll[3 * a + b] * R[3 * c + b];
+                    }
+                if (r == c) {
+                    K -= m.Kr;
+                    Dv -= m.Dr;
+                }
+                D[3 * r + c] = Dv;
+                H[3 * r + c] = M[3 * r + c] - h * h * K - h * Dv;
+            }
+        // J = [0; R_ji^T] (6 x 3); R_0i = R_pj0 R_ji does not depend on q
+        for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 3; ++c) J[3 * r + c] = r < 3 ? 0.0 : R[3 * c + (r - 3)];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+                R0i[3 * r + c] = m.E_pj0[4 * r] * R[c] + m.E_pj0[4 * r + 1] * R[3 + c] + m.E_pj0[4 * r + 2] * R[6 + c];
+    }
+    AdjState a = adj[i];
+    double y[kMaxDof];
+    for (int c = 0; c < nd; ++c) y[c] = df_dq[((size_t)i * T + (t - 1)) * nd + c];
+    if (t < T)  // step t + 1: dg/dq_t = -2 M_{t+1} + h D_{t+1}
+        for (int c = 0; c < nd; ++c)
+            for (int r = 0; r < nd; ++r) y[c] -= (-2.0 * a.M1[nd * r + c] + h * a.D1[nd * r + c]) * a.z1[r];
+    if (t < T - 1)  // step t + 2: dg/dq_t = M_{t+2}
+        for (int c = 0; c < nd; ++c)
+            for (int r = 0; r < nd; ++r) y[c] -= a.M2[nd * r + c] * a.z2[r];
+    double z[kMaxDof];
+    lu_solve_transposed(H, nd, y, z);
+    {
+        double Jz[6];
+        for (int r = 0; r < 6; ++r) {
+            double v = 0.0;
+            for (int c = 0; c < nd; ++c) v += J[nd * r + c] * z[c];
+            Jz[r] = v * m.inertia[r];
+        }
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                a.acc[r] += R0i[3 * r + c] * Jz[c];
+                a.acc[3 + r] += R0i[3 * r + c] * Jz[3 + c];
             }
     }
-    double R[9], M[9], D[9], H[9];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) R[3 * r + c] = m.E_ji[4 * r + c];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) {
-            M[3 * r + c] = R[3 * r] * m.inertia[3] * R[3 * c] + R[3 * r + 1] * m.inertia[4] * R[3 * c + 1] +
-                           R[3 * r + 2] * m.inertia[5] * R[3 * c + 2];
-            double K = 0.0, Dv = 0.0;
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) {
-                    K += R[3 * r + a] * Kll[3 * a + b] * R[3 * c + b];
-                    Dv += R[3 * r + a] * Dll[3 * a + b] * R[3 * c + b];
-                }
-            if (r == c) {
-                K -= m.Kr;
-                Dv -= m.Dr;
-            }
-            D[3 * r + c] = Dv;
-            H[3 * r + c] = M[3 * r + c] - h * h * K - h * Dv;
-        }
-    AdjState a = adj[i];
-    double y[3];
-    for (int c = 0; c < 3; ++c) y[c] = df_dq[((size_t)i * T + (t - 1)) * 3 + c];
-    if (t < T)  // step t + 1: dg/dq_t = -2M + h D_{t+1}
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r) y[c] -= (-2.0 * M[3 * r + c] + h * a.D1[3 * r + c]) * a.z1[r];
-    if (t < T - 1)  // step t + 2: dg/dq_t = M
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r) y[c] -= M[3 * r + c] * a.z2[r];
-    double z[3];
-    lu3_solve_transposed(H, y, z);
     if (t == 1) {
-        double* go = gout + 12 * (size_t)i;
-        for (int c = 0; c < 3; ++c) {
+        double* go = gout + 18 * (size_t)i;
+        for (int c = 0; c < nd; ++c) {
             double g0 = 0.0, gd0 = 0.0;
-            for (int r = 0; r < 3; ++r) {
-                g0 -= (-M[3 * r + c] + h * D[3 * r + c]) * z[r];
-                if (T > 1) g0 -= M[3 * r + c] * a.z1[r];
-                gd0 -= (-h * M[3 * r + c]) * z[r];
+            for (int r = 0; r < nd; ++r) {
+                g0 -= (-M[nd * r + c] + h * D[nd * r + c]) * z[r];  // step 1
+                if (T > 1) g0 -= a.M1[nd * r + c] * a.z1[r];           // step 2
+                gd0 -= (-h * M[nd * r + c]) * z[r];
             }
             go[c] = g0;
-            go[3 + c] = gd0;
+            go[6 + c] = gd0;
         }
-        double zs[3], v[3], E0i[16], phi[6];
-        for (int c = 0; c < 3; ++c) zs[c] = a.zs[c] + z[c];
-        for (int c = 0; c < 3; ++c) v[c] = m.inertia[3 + c] * (R[c] * zs[0] + R[3 + c] * zs[1] + R[6 + c] * zs[2]);
-        const double q0[3] = {q_his[3 * (size_t)i], q_his[3 * (size_t)i + 1], q_his[3 * (size_t)i + 2]};
-        const double zero[3] = {0.0, 0.0, 0.0};
-        mover_pose(m, q0, zero, E0i, phi);  // R_0i does not depend on q
-        for (int c = 0; c < 3; ++c) {
-            go[6 + c] = 0.0;
-            go[9 + c] = h * h * (E0i[4 * c] * v[0] + E0i[4 * c + 1] * v[1] + E0i[4 * c + 2] * v[2]);
-        }
+        for (int c = 0; c < 6; ++c) go[12 + c] = h * h * a.acc[c];
     }
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < nd; ++c) {
         a.z2[c] = a.z1[c];
         a.z1[c] = z[c];
-        a.zs[c] += z[c];
     }
-    for (int c = 0; c < 9; ++c) a.D1[c] = D[c];
+    for (int c = 0; c < nd * nd; ++c) {
+        a.M2[c] = a.M1[c];
+        a.M1[c] = M[c];
+        a.D1[c] = D[c];
+    }
     adj[i] = a;
 }
 
@@ -471,6 +583,7 @@ __global__ void adj_advance_kernel(int* t_dev) { t_dev[0] -= 1; }
 struct sdfc_sim {
     sdfc_context* ctx = nullptr;
     int n = 0, n_pairs = 0;
+    int nd = 3;  // joint dofs of every mover (3 translational, 6 free3d-exp)
     sdfc_batch* batch = nullptr;
     std::vector<int> order;  // sorted pair k -> caller's pair index
     MoverDev* d_mover = nullptr;
@@ -543,10 +656,13 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     if (n <= 0 || !movers || n_pairs < 0 || (n_pairs > 0 && !pairs) || !out)
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: bad argument");
     for (int i = 0; i < n; ++i) {
-        if (movers[i].joint != SDFC_JOINT_TRANSLATIONAL)
-            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: only SDFC_JOINT_TRANSLATIONAL movers");
+        if (movers[i].joint != SDFC_JOINT_TRANSLATIONAL && movers[i].joint != SDFC_JOINT_FREE3D_EXP)
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: unknown joint type");
+        if (movers[i].joint != movers[0].joint)
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: all movers of a sim share one joint type");
         if (!(movers[i].h > 0.0)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: time step must be > 0");
     }
+    const int nd = movers[0].joint == SDFC_JOINT_FREE3D_EXP ? 6 : 3;
     for (int k = 0; k < n_pairs; ++k)
         if (pairs[k].instance < 0 || pairs[k].instance >= n)
             return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_create: pair instance out of range");
@@ -556,6 +672,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     s->ctx = ctx;
     s->n = n;
     s->n_pairs = n_pairs;
+    s->nd = nd;
     // pairs grouped by scene (stable), so each scene's pairs are contiguous
     s->order.resize(n_pairs);
     std::iota(s->order.begin(), s->order.end(), 0);
@@ -588,15 +705,16 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         d.h = m.h;
         d.Kr = m.joint_stiffness;
         d.Dr = m.joint_damping;
-        d.max_iter = std::max(20 * 3, 100);  // Simulation.cpp:1009, ndof_r = 3
+        d.max_iter = std::max(20 * nd, 100);  // Simulation.cpp:1009
+        d.ndof = nd;
         md[i] = d;
     }
     if (n_pairs > 0 && (rc = sdfc_impl::batch_create(ctx, n_pairs, pts.data(), grd.data(), &s->batch))) {
         delete s;
         return rc;
     }
-    if ((rc = alloc(s, &s->d_mover, n)) || (rc = alloc(s, &s->d_state, n)) || (rc = alloc(s, &s->d_q, 3 * (size_t)n)) ||
-        (rc = alloc(s, &s->d_qd, 3 * (size_t)n)) || (rc = alloc(s, &s->d_fext, 6 * (size_t)n)) ||
+    if ((rc = alloc(s, &s->d_mover, n)) || (rc = alloc(s, &s->d_state, n)) || (rc = alloc(s, &s->d_q, (size_t)nd * n)) ||
+        (rc = alloc(s, &s->d_qd, (size_t)nd * n)) || (rc = alloc(s, &s->d_fext, 6 * (size_t)n)) ||
         (rc = alloc(s, &s->d_pair_inst, n_pairs)) || (rc = alloc(s, &s->d_role, n_pairs)) ||
         (rc = alloc(s, &s->d_pair_begin, n + 1)) || (rc = alloc(s, &s->d_Efixed, 16 * (size_t)n_pairs)) ||
         (rc = alloc(s, &s->d_EA, 16 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_phiA, 6 * (size_t)n_pairs)) ||
@@ -606,7 +724,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         (rc = alloc(s, &s->d_Dm, 144 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_nact, n_pairs)) ||
         (rc = alloc(s, &s->d_status, n_pairs)) || (rc = alloc(s, &s->d_conv, n)) ||
         (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, 1)) || (rc = alloc(s, &s->d_adj, n)) ||
-        (rc = alloc(s, &s->d_gout, 12 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2))) {
+        (rc = alloc(s, &s->d_gout, 18 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2))) {
         free_sim(s);
         return rc;
     }
@@ -623,8 +741,8 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         if (e == cudaSuccess) e = cudaMemcpy(s->d_prm, prm.data(), sizeof(double) * prm.size(), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemcpy(s->d_pair_begin, begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(s->d_q, 0, sizeof(double) * 3 * n);
-    if (e == cudaSuccess) e = cudaMemset(s->d_qd, 0, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_q, 0, sizeof(double) * nd * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_qd, 0, sizeof(double) * nd * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_fext, 0, sizeof(double) * 6 * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_conv, 0, sizeof(int) * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_evals, 0, sizeof(unsigned long long));
@@ -668,14 +786,13 @@ int sdfc_sim_set_state(sdfc_sim* s, const double* q, const double* qdot) {
     sdfc_context* ctx = s->ctx;
     int rc = use_device(ctx);
     if (rc) return rc;
-    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_q, q, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, ctx->stream));
-    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd, qdot, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice, ctx->stream));
+    const size_t bytes = sizeof(double) * s->nd * s->n;
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_q, q, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd, qdot, bytes, cudaMemcpyHostToDevice, ctx->stream));
     if (s->record_cap > 0) {  // a new initial state restarts the recording
         s->recorded = 0;
-        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis, s->d_q, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
-                                           ctx->stream));
-        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd0rec, s->d_qd, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
-                                           ctx->stream));
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis, s->d_q, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qd0rec, s->d_qd, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     }
     SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return SDFC_OK;
@@ -686,8 +803,9 @@ int sdfc_sim_get_state(sdfc_sim* s, double* q, double* qdot) {
     sdfc_context* ctx = s->ctx;
     int rc = use_device(ctx);
     if (rc) return rc;
-    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(q, s->d_q, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost, ctx->stream));
-    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(qdot, s->d_qd, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(q, s->d_q, sizeof(double) * s->nd * s->n, cudaMemcpyDeviceToHost, ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(qdot, s->d_qd, sizeof(double) * s->nd * s->n, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
     SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return SDFC_OK;
 }
@@ -757,15 +875,17 @@ int capture_backward(sdfc_sim* s) {
     SDFC_CUDA_TRY(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc = SDFC_OK;
     if (np > 0) {
-        adj_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, n, s->d_pair_inst, s->d_role, s->d_Efixed, s->d_mover,
-                                                          s->d_qhis, s->d_t, s->d_EA, s->d_phiA, s->d_EB, s->d_phiB);
+        adj_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, n, s->nd, s->d_pair_inst, s->d_role, s->d_Efixed,
+                                                          s->d_mover, s->d_qhis, s->d_t, s->d_EA, s->d_phiA, s->d_EB,
+                                                          s->d_phiB);
         sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
         sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
         rc = sdfc_impl::run_batch(s->batch, in, true, out, st);
     }
     if (!rc) {
-        adj_step_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_Km, s->d_Dm,
-                                                         s->d_qhis, s->d_dfdq, s->d_t, s->d_adj, s->d_gout);
+        adj_step_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
+                                                         s->d_fm, s->d_Km, s->d_Dm, s->d_qhis, s->d_qd0rec, s->d_dfdq,
+                                                         s->d_t, s->d_adj, s->d_gout);
         adj_advance_kernel<<<1, 1, 0, st>>>(s->d_t);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
@@ -801,7 +921,7 @@ int sdfc_sim_record(sdfc_sim* s, int max_steps) {
     s->d_qhis = s->d_qd0rec = nullptr;
     s->record_cap = s->recorded = 0;
     if (max_steps == 0) return SDFC_OK;
-    const size_t n3 = 3 * (size_t)s->n;
+    const size_t n3 = (size_t)s->nd * s->n;
     if ((rc = dev_alloc(ctx, (void**)&s->d_qhis, sizeof(double) * n3 * ((size_t)max_steps + 1))) ||
         (rc = dev_alloc(ctx, (void**)&s->d_qd0rec, sizeof(double) * n3))) {
         cudaFree(s->d_qhis);
@@ -823,14 +943,14 @@ int sdfc_sim_history(sdfc_sim* s, int* steps, double* q_his) {
     if (s->record_cap == 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_history: recording is off");
     *steps = s->recorded;
     if (!q_his) return SDFC_OK;
-    const int n = s->n, T1 = s->recorded + 1;
-    std::vector<double> h(3 * (size_t)n * T1);
+    const int n = s->n, T1 = s->recorded + 1, nd = s->nd;
+    std::vector<double> h((size_t)nd * n * T1);
     SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), s->d_qhis, sizeof(double) * h.size(), cudaMemcpyDeviceToHost,
                                        ctx->stream));
     SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     for (int t = 0; t < T1; ++t)  // step-major on the device, scene-major for the caller
         for (int i = 0; i < n; ++i)
-            for (int c = 0; c < 3; ++c) q_his[(3 * ((size_t)i * T1 + t)) + c] = h[3 * ((size_t)t * n + i) + c];
+            for (int c = 0; c < nd; ++c) q_his[(nd * ((size_t)i * T1 + t)) + c] = h[nd * ((size_t)t * n + i) + c];
     return SDFC_OK;
 }
 
@@ -841,11 +961,11 @@ int sdfc_sim_backward(sdfc_sim* s, const double* df_dq, double* df_dq0, double* 
     if (s->record_cap == 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_backward: recording is off");
     int rc = use_device(ctx);
     if (rc) return rc;
-    const int n = s->n, T = s->recorded, tb = 128;
+    const int n = s->n, T = s->recorded, tb = 128, nd = s->nd;
     cudaStream_t st = ctx->stream;
-    std::vector<double> g(12 * (size_t)n, 0.0);
+    std::vector<double> g(18 * (size_t)n, 0.0);
     if (T > 0) {
-        const size_t need = 3 * (size_t)n * T;
+        const size_t need = (size_t)nd * n * T;
         if (need > s->dfdq_cap) {
             if (s->back_exec) {  // its kernels hold the old dL/dq pointer
                 cudaGraphExecDestroy(s->back_exec);
@@ -866,10 +986,10 @@ int sdfc_sim_backward(sdfc_sim* s, const double* df_dq, double* df_dq0, double* 
         SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     }
     for (int i = 0; i < n; ++i) {
-        const double* gi = &g[12 * (size_t)i];
-        if (df_dq0) std::memcpy(df_dq0 + 3 * (size_t)i, gi, sizeof(double) * 3);
-        if (df_dqdot0) std::memcpy(df_dqdot0 + 3 * (size_t)i, gi + 3, sizeof(double) * 3);
-        if (df_dfext) std::memcpy(df_dfext + 6 * (size_t)i, gi + 6, sizeof(double) * 6);
+        const double* gi = &g[18 * (size_t)i];
+        if (df_dq0) std::memcpy(df_dq0 + (size_t)nd * i, gi, sizeof(double) * nd);
+        if (df_dqdot0) std::memcpy(df_dqdot0 + (size_t)nd * i, gi + 6, sizeof(double) * nd);
+        if (df_dfext) std::memcpy(df_dfext + 6 * (size_t)i, gi + 12, sizeof(double) * 6);
     }
     return SDFC_OK;
 }
@@ -888,7 +1008,8 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
     const int max_rounds = 100 * (1 + kMaxLineSearch) + 1;
     const int per_check = 2;  // rounds enqueued between completion checks
     for (int step = 0; step < num_steps; ++step) {
-        sim_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_mover, s->d_q, s->d_qd, s->d_state, s->d_remaining);
+        sim_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_mover, s->d_q, s->d_qd, s->d_state,
+                                                          s->d_remaining);
         int active = n;
         for (int r = 0; r < max_rounds && active > 0; r += per_check) {
             for (int k = 0; k < per_check; ++k) SDFC_CUDA_TRY(ctx, cudaGraphLaunch(s->round_exec, st));
@@ -898,11 +1019,11 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
             active = *s->h_remaining;
             if (active == 0) break;
         }
-        sim_end_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_mover, s->d_state, s->d_q, s->d_qd, s->d_conv);
+        sim_end_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_mover, s->d_state, s->d_q, s->d_qd, s->d_conv);
         if (s->record_cap > 0) {
             ++s->recorded;
-            SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis + 3 * (size_t)n * s->recorded, s->d_q, sizeof(double) * 3 * n,
-                                               cudaMemcpyDeviceToDevice, st));
+            SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis + (size_t)s->nd * n * s->recorded, s->d_q,
+                                               sizeof(double) * s->nd * n, cudaMemcpyDeviceToDevice, st));
         }
     }
     SDFC_CUDA_TRY(ctx, cudaGetLastError());

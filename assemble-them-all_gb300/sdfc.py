@@ -29,6 +29,7 @@ EXPORTS = (
     "sdfc_sim_step", "sdfc_sim_stats", "sdfc_sim_record", "sdfc_sim_history", "sdfc_sim_backward",
 )
 JOINT_TRANSLATIONAL = 3
+JOINT_FREE3D_EXP = 6
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 DERIV_ANALYTIC = 0
@@ -320,6 +321,7 @@ class Sim:
     def __init__(self, ctx: Context, movers, pairs):
         self.ctx = ctx
         self.n = len(movers)
+        self.ndof = 6 if movers[0].joint == JOINT_FREE3D_EXP else 3
         marr = (Mover * self.n)(*movers)
         parr = (ScenePair * max(1, len(pairs)))(*pairs)
         self._h = ctypes.c_void_p()
@@ -337,13 +339,13 @@ class Sim:
 
     def set_state(self, q, qdot):
         self.generation += 1
-        self.ctx._check(lib().sdfc_sim_set_state(self._h, _dp(_f64(q, 3 * self.n)), _dp(_f64(qdot, 3 * self.n))),
-                        "sdfc_sim_set_state")
+        k = self.ndof * self.n
+        self.ctx._check(lib().sdfc_sim_set_state(self._h, _dp(_f64(q, k)), _dp(_f64(qdot, k))), "sdfc_sim_set_state")
 
     def get_state(self):
-        q, qd = np.zeros(3 * self.n), np.zeros(3 * self.n)
+        q, qd = np.zeros(self.ndof * self.n), np.zeros(self.ndof * self.n)
         self.ctx._check(lib().sdfc_sim_get_state(self._h, _dp(q), _dp(qd)), "sdfc_sim_get_state")
-        return q.reshape(self.n, 3), qd.reshape(self.n, 3)
+        return q.reshape(self.n, self.ndof), qd.reshape(self.n, self.ndof)
 
     def set_external_force(self, f):
         self.generation += 1
@@ -368,23 +370,23 @@ class Sim:
         self.ctx._check(lib().sdfc_sim_record(self._h, int(max_steps)), "sdfc_sim_record")
 
     def history(self):
-        """Recorded joint trajectory, shape (n, T+1, 3), q_0 first."""
+        """Recorded joint trajectory, shape (n, T+1, ndof), q_0 first."""
         T = ctypes.c_int()
         self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), None), "sdfc_sim_history")
-        q = np.zeros((self.n, T.value + 1, 3))
+        q = np.zeros((self.n, T.value + 1, self.ndof))
         self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), _dp(q)), "sdfc_sim_history")
         return q
 
     def backward(self, df_dq):
-        """Simulation::backward_BDF1 over the recorded steps for dL/dq_k (n, T, 3):
-        returns dL/dq0 (n, 3), dL/dqdot0 (n, 3), dL/d(external force) (n, 6)."""
+        """Simulation::backward_BDF1 over the recorded steps for dL/dq_k (n, T, ndof):
+        returns dL/dq0 (n, ndof), dL/dqdot0 (n, ndof), dL/d(external force) (n, 6)."""
         df_dq = np.ascontiguousarray(df_dq, dtype=np.float64)
-        if df_dq.ndim != 3 or df_dq.shape[0] != self.n or df_dq.shape[2] != 3:
-            raise ValueError("df_dq must have shape (n, T, 3)")
+        if df_dq.ndim != 3 or df_dq.shape[0] != self.n or df_dq.shape[2] != self.ndof:
+            raise ValueError(f"df_dq must have shape (n, T, {self.ndof})")
         T = ctypes.c_int()
         self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), None), "sdfc_sim_history")
         if df_dq.shape[1] != T.value:
             raise ValueError(f"df_dq covers {df_dq.shape[1]} steps, {T.value} recorded")
-        g0, gd0, gf = np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros((self.n, 6))
+        g0, gd0, gf = np.zeros((self.n, self.ndof)), np.zeros((self.n, self.ndof)), np.zeros((self.n, 6))
         self.ctx._check(lib().sdfc_sim_backward(self._h, _dp(df_dq), _dp(g0), _dp(gd0), _dp(gf)), "sdfc_sim_backward")
         return g0, gd0, gf

@@ -189,8 +189,12 @@ int sdfc_batch_recheck_count(sdfc_batch* batch, unsigned long long* count, int r
  * most max(20 ndof, 100) Newton iterations, backtracking line search halving
  * the step up to 20 times, 3 consecutive line-search failures stop.  Every
  * force evaluation of every scene of one Newton round runs as one batched
- * evaluation on the GPU; the 3x3 solves run in FP64 on the GPU. */
+ * evaluation on the GPU; the reduced systems and their solves run in FP64 on the GPU.
+ * All movers of one sim share one joint type; q, qdot arrays are n x ndof. */
 #define SDFC_JOINT_TRANSLATIONAL 3 /* JointTranslational: q = position (3 dof) */
+#define SDFC_JOINT_FREE3D_EXP 6    /* JointFree3DExp: q = (position, exponential rotation
+                                      coordinates) (6 dof); rotation vectors longer than 1.5 pi
+                                      are reparameterised after each step like the reference */
 
 /* The moving part: Body::_mass, Body::_Inertia (Ixx, Iyy, Izz, m, m, m),
  * Joint::_E_pj_0 (row-major 4x4), Body::_E_ji, the options gravity and
@@ -236,16 +240,17 @@ int sdfc_sim_stats(sdfc_sim* sim, long long* rounds, long long* evaluations);
  * simulation/redmax/Simulation.cpp:1512-1634, integrator BDF1).
  * sdfc_sim_record starts recording at the current state (q_0, qdot_0) for at most
  * max_steps steps (sdfc_sim_step fails with SDFC_ERR_CAPACITY beyond it; 0 stops
- * recording).  Only the joint trajectory is kept (n x 3 doubles per step) where the
+ * recording).  Only the joint trajectory is kept (n x ndof doubles per step) where the
  * reference stores H_lu, M, D per step (BackwardData.h); the backward pass recomputes
- * each step's H and D from it.  sdfc_sim_set_state restarts the recording. */
+ * each step's H and D from it.  sdfc_sim_set_state restarts the recording.  Like the
+ * reference, the adjoint does not differentiate the free joint's reparameterisation. */
 int sdfc_sim_record(sdfc_sim* sim, int max_steps);
-/* Recorded steps T and, if q_his is not NULL, the trajectory (host, n x (T+1) x 3,
+/* Recorded steps T and, if q_his is not NULL, the trajectory (host, n x (T+1) x ndof,
  * q_0 first): Simulation::get_q_his. */
 int sdfc_sim_history(sdfc_sim* sim, int* steps, double* q_his);
 /* Simulation::backward_BDF1 for every scene over the T recorded steps.
- * df_dq (host, n x T x 3): dL/dq_k for k = 1..T (BackwardInfo::_df_dq).
- * Outputs (host, may be NULL): df_dq0 (n x 3) and df_dqdot0 (n x 3), the reference's
+ * df_dq (host, n x T x ndof): dL/dq_k for k = 1..T (BackwardInfo::_df_dq).
+ * Outputs (host, may be NULL): df_dq0 (n x ndof) and df_dqdot0 (n x ndof), the reference's
  * BackwardResults::_df_dq0/_df_dqdot0 with zero direct terms, and df_dfext (n x 6,
  * world frame, torque then force like sdfc_sim_set_external_force), which the
  * reference does not compute: dL/d(external force), the force held constant over the

@@ -20,10 +20,11 @@ def sdfc():
     return submodule("sdfc")
 
 
-def make_sim(sdfc, ctx, fx, n=1, f_ext=None, q0=None, qd0=None, precision=0):
+def make_sim(sdfc, ctx, fx, n=1, f_ext=None, q0=None, qd0=None, precision=0, joint=3):
     g = ctx.upload_grid(fx["grid"], fx["min_box"], fx["max_box"], fx["dx"], float(fx["col_th"]), 1)
     p = ctx.upload_points(fx["points"], 1)
-    mover = sdfc.Mover.make(float(fx["mass"]), fx["inertia"], fx["E_ji"], float(fx["h"]), tuple(fx["gravity"]))
+    mover = sdfc.Mover.make(float(fx["mass"]), fx["inertia"], fx["E_ji"], float(fx["h"]), tuple(fx["gravity"]),
+                            joint=joint)
     prm = sdfc.Params(*[float(x) for x in fx["params"]])
     pairs = [sdfc.ScenePair.make(i, p, g, True, fx["E_fixed"], prm) for i in range(n)]
     sim = ctx.sim([mover] * n, pairs)
