@@ -28,8 +28,16 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
-                   "-I", CSRC]
+    f = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
+                "-I", CSRC]
+    # force_kernel's resident CTAs per SM on the FP32 path (a tuning knob; see sdfc_kernels.cu)
+    mb = os.environ.get("SDFC_FORCE_MIN_BLOCKS")
+    if mb:
+        f.append(f"-DSDFC_FORCE_MIN_BLOCKS={int(mb)}")
+    # further compile-time variants, e.g. SDFC_DEFINES="SDFC_COLD=inline" (measurement only)
+    for d in os.environ.get("SDFC_DEFINES", "").split():
+        f.append("-D" + d)
+    return f
 
 
 def _stale(target, deps):

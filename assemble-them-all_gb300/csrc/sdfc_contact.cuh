@@ -275,8 +275,14 @@ struct SdfJet {
 
 constexpr double kFdEps = 1e-5;  // BodySDFObj.cpp:178,191
 
+// Rarely executed exact paths (the 19-query FP64 stencil) are kept out of line so that
+// the force kernel's hot loop stays compact in the instruction cache.
+#ifndef SDFC_COLD
+#define SDFC_COLD static __noinline__
+#endif
+
 // The reference's stencil (BodySDFObj.cpp:176-205), bit-identical in FP64.
-__device__ inline void sdf_stencil(const GridDesc& g, V3 x, V3& grad, double* hess, bool want_hessian) {
+__device__ SDFC_COLD void sdf_stencil(const GridDesc& g, V3 x, V3& grad, double* hess, bool want_hessian) {
     const double e = kFdEps, h = kFdEps / 2;
     double gp[3], gm[3];
 #pragma unroll
@@ -316,7 +322,7 @@ __device__ inline void sdf_stencil(const GridDesc& g, V3 x, V3& grad, double* he
 // lanes active).  Lane l < 19 evaluates one query point, the values are
 // exchanged by shuffles and every lane combines them in sdf_stencil's operation
 // order, so the results are bit-identical to sdf_stencil's.
-__device__ inline void sdf_stencil_warp(const GridDesc& g, V3 x, V3& grad, double* hess, bool want_hessian,
+__device__ SDFC_COLD void sdf_stencil_warp(const GridDesc& g, V3 x, V3& grad, double* hess, bool want_hessian,
                                         double& centre) {
     const int lane = threadIdx.x & 31;
     const double e = kFdEps, h = kFdEps / 2;

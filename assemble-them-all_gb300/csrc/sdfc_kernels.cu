@@ -336,11 +336,14 @@ struct WarpSink {
     }
 };
 
-// The FP32 path fits 128 registers, so four CTAs (16 warps) share an SM; the
-// FP64 path is left its full register budget.
+// CTAs of the FP32 path resident per SM (its register budget is 65536 / (this x 128));
+// the FP64 path is left its full register budget.
+#ifndef SDFC_FORCE_MIN_BLOCKS
+#define SDFC_FORCE_MIN_BLOCKS 4
+#endif
 template <typename T>
 constexpr int force_min_blocks() {
-    return std::is_same<T, float>::value ? 4 : 1;
+    return std::is_same<T, float>::value ? SDFC_FORCE_MIN_BLOCKS : 1;
 }
 
 template <bool DERIV, bool STENCIL, typename T>
