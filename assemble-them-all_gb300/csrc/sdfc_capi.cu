@@ -1,4 +1,5 @@
 // C ABI of libsdfcontact (include/sdfc.h): contexts, uploads, batches.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -263,7 +264,7 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     if (!values || !min_box || !max_box || !dxyz || !grid)
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: null argument");
     if (ni < 2 || nj < 2 || nk < 2) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: each extent must be >= 2");
-    if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32)
+    if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32 && storage != SDFC_STORAGE_F16_BRICKS)
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: unknown storage");
     const int nn[3] = {ni, nj, nk};
     for (int a = 0; a < 3; ++a) {
@@ -280,12 +281,25 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     int rc = use_device(ctx);
     if (rc) return rc;
 
-    std::vector<float> v32(n);
-    double vmax = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        v32[i] = (float)values[i];
-        vmax = std::max(vmax, std::fabs(values[i]));
+    // the values every evaluation sees: the caller's, or the FP32-rounded / FP16-decoded ones
+    std::vector<double> seen;
+    std::vector<unsigned short> codes;
+    std::vector<float> so;
+    const int nbx = (ni + 7) / 8, nby = (nj + 7) / 8, nbz = (nk + 7) / 8;
+    if (storage == SDFC_STORAGE_F16_BRICKS) {
+        const size_t nb = (size_t)nbx * nby * nbz;
+        codes.resize(nb * 512);
+        so.resize(2 * nb);
+        seen.resize(n);
+        sdfc_f16_brick_encode(values, ni, nj, nk, codes.data(), so.data());
+        sdfc_f16_brick_decode(codes.data(), so.data(), ni, nj, nk, seen.data());
+    } else if (storage == SDFC_STORAGE_F32) {
+        seen.resize(n);
+        for (size_t i = 0; i < n; ++i) seen[i] = (double)(float)values[i];
     }
+    const double* vals = seen.empty() ? values : seen.data();
+    double vmax = 0.0;
+    for (size_t i = 0; i < n; ++i) vmax = std::max(vmax, std::fabs(vals[i]));
     // Lipschitz bound of the trilinear interpolant: per axis the largest
     // neighbour difference over the spacing.
     double lip2 = 0.0;
@@ -298,7 +312,7 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
                     int c[3] = {i, j, k};
                     if (c[a] + 1 >= nn[a]) continue;
                     size_t idx = i + st[1] * j + st[2] * k;
-                    m = std::max(m, std::fabs(values[idx + st[a]] - values[idx]));
+                    m = std::max(m, std::fabs(vals[idx + st[a]] - vals[idx]));
                 }
         lip2 += (m / dxyz[a]) * (m / dxyz[a]);
     }
@@ -321,7 +335,23 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     g.col_th = col_th;
     g.lip = (float)(std::sqrt(lip2) * 1.0001);
     g.vmax = (float)(vmax * 1.0001);
-    {
+    auto upload = [&](const void* src, size_t bytes, void** dst) -> int {
+        int r = dev_alloc(ctx, dst, bytes);
+        if (r) return r;
+        ctx->allocations.push_back(*dst);
+        CUDA_TRY(ctx, cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+        return SDFC_OK;
+    };
+    if (storage == SDFC_STORAGE_F16_BRICKS) {
+        void *pb = nullptr, *ps = nullptr;
+        if ((rc = upload(codes.data(), codes.size() * sizeof(unsigned short), &pb)) ||
+            (rc = upload(so.data(), so.size() * sizeof(float), &ps)))
+            return rc;
+        g.b16 = (const unsigned short*)pb;
+        g.bso = (const float2*)ps;
+        g.nbx = nbx;
+        g.nby = nby;
+    } else {
         // cell-corner array: per cell its 8 FP32 corners (GridDesc::cells32)
         const size_t ci = (size_t)ni - 1, cj = (size_t)nj - 1, ck = (size_t)nk - 1;
         std::vector<float> cells(8 * ci * cj * ck);
@@ -330,34 +360,14 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
                 for (size_t i = 0; i < ci; ++i) {
                     float* c = &cells[8 * (i + ci * (j + cj * k))];
                     const size_t b = i + (size_t)ni * (j + (size_t)nj * k), sj = (size_t)ni, sk = (size_t)ni * nj;
-                    c[0] = v32[b];
-                    c[1] = v32[b + 1];
-                    c[2] = v32[b + sj];
-                    c[3] = v32[b + sj + 1];
-                    c[4] = v32[b + sk];
-                    c[5] = v32[b + sk + 1];
-                    c[6] = v32[b + sk + sj];
-                    c[7] = v32[b + sk + sj + 1];
+                    const size_t at[8] = {b, b + 1, b + sj, b + sj + 1, b + sk, b + sk + 1, b + sk + sj, b + sk + sj + 1};
+                    for (int q = 0; q < 8; ++q) c[q] = (float)vals[at[q]];
                 }
-        void* pc = nullptr;
-        if ((rc = dev_alloc(ctx, &pc, cells.size() * sizeof(float)))) return rc;
-        ctx->allocations.push_back(pc);
-        CUDA_TRY(ctx, cudaMemcpy(pc, cells.data(), cells.size() * sizeof(float), cudaMemcpyHostToDevice));
+        void *pc = nullptr, *p64 = nullptr;
+        if ((rc = upload(cells.data(), cells.size() * sizeof(float), &pc)) ||
+            (rc = upload(vals, n * sizeof(double), &p64)))
+            return rc;
         g.cells32 = (const float4*)pc;
-    }
-    {
-        // FP64 values of the grid as stored: the caller's doubles, or the FP32 values widened
-        std::vector<double> w64;
-        const double* src = values;
-        if (storage == SDFC_STORAGE_F32) {
-            w64.resize(n);
-            for (size_t i = 0; i < n; ++i) w64[i] = (double)v32[i];
-            src = w64.data();
-        }
-        void* p64 = nullptr;
-        if ((rc = dev_alloc(ctx, &p64, n * sizeof(double)))) return rc;
-        ctx->allocations.push_back(p64);
-        CUDA_TRY(ctx, cudaMemcpy(p64, src, n * sizeof(double), cudaMemcpyHostToDevice));
         g.v64 = (const double*)p64;
     }
     ctx->grids.push_back(g);
@@ -366,6 +376,84 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
         return rc;
     }
     *grid = (int)ctx->grids.size() - 1;
+    return SDFC_OK;
+}
+
+int sdfc_grid_values(sdfc_context* ctx, int grid, double* values) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (!values) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "grid_values: null argument");
+    if (grid < 0 || grid >= (int)ctx->grids.size()) return fail(ctx, SDFC_ERR_NOT_FOUND, "grid_values: unknown grid");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    const GridDesc& g = ctx->grids[grid];
+    const size_t n = (size_t)g.ni * g.nj * g.nk;
+    if (!g.b16) {
+        CUDA_TRY(ctx, cudaMemcpy(values, g.v64, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return SDFC_OK;
+    }
+    const size_t nb = (size_t)g.nbx * g.nby * ((g.nk + 7) / 8);
+    std::vector<unsigned short> codes(nb * 512);
+    std::vector<float> so(2 * nb);
+    CUDA_TRY(ctx, cudaMemcpy(codes.data(), g.b16, codes.size() * sizeof(unsigned short), cudaMemcpyDeviceToHost));
+    CUDA_TRY(ctx, cudaMemcpy(so.data(), g.bso, so.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    return sdfc_f16_brick_decode(codes.data(), so.data(), g.ni, g.nj, g.nk, values);
+}
+
+static inline unsigned short half_bits(float x) {
+    const __half_raw r = __half(__float2half_rn(x));
+    return r.x;
+}
+static inline float half_value(unsigned short bits) {
+    __half_raw r;
+    r.x = bits;
+    return __half2float(__half(r));
+}
+
+int sdfc_f16_brick_encode(const double* values, int ni, int nj, int nk, unsigned short* codes, float* so) {
+    if (!values || !codes || !so || ni < 1 || nj < 1 || nk < 1) return SDFC_ERR_INVALID_ARGUMENT;
+    const int nbx = (ni + 7) / 8, nby = (nj + 7) / 8, nbz = (nk + 7) / 8;
+    for (int bz = 0; bz < nbz; ++bz)
+        for (int by = 0; by < nby; ++by)
+            for (int bx = 0; bx < nbx; ++bx) {
+                const size_t b = (size_t)bx + (size_t)nbx * ((size_t)by + (size_t)nby * bz);
+                auto at = [&](int ii, int jj, int kk) {  // node of the brick, the last node repeated past the end
+                    const int i = std::min(8 * bx + ii, ni - 1), j = std::min(8 * by + jj, nj - 1),
+                              k = std::min(8 * bz + kk, nk - 1);
+                    return values[(size_t)i + (size_t)ni * ((size_t)j + (size_t)nj * k)];
+                };
+                double lo = INFINITY, hi = -INFINITY;
+                for (int kk = 0; kk < 8; ++kk)
+                    for (int jj = 0; jj < 8; ++jj)
+                        for (int ii = 0; ii < 8; ++ii) {
+                            const double v = at(ii, jj, kk);
+                            lo = std::min(lo, v);
+                            hi = std::max(hi, v);
+                        }
+                const float off = (lo <= 0.0 && hi >= 0.0) ? 0.0f : (float)(lo > 0.0 ? lo : hi);
+                const double amax = std::max(std::fabs(hi - (double)off), std::fabs(lo - (double)off));
+                const float scale = amax > 0.0 ? (float)(amax / 32768.0) : 1.0f;
+                so[2 * b] = scale;
+                so[2 * b + 1] = off;
+                for (int kk = 0; kk < 8; ++kk)
+                    for (int jj = 0; jj < 8; ++jj)
+                        for (int ii = 0; ii < 8; ++ii)
+                            codes[b * 512 + ii + 8 * jj + 64 * kk] =
+                                half_bits((float)((at(ii, jj, kk) - (double)off) / (double)scale));
+            }
+    return SDFC_OK;
+}
+
+int sdfc_f16_brick_decode(const unsigned short* codes, const float* so, int ni, int nj, int nk, double* values) {
+    if (!values || !codes || !so || ni < 1 || nj < 1 || nk < 1) return SDFC_ERR_INVALID_ARGUMENT;
+    const int nbx = (ni + 7) / 8, nby = (nj + 7) / 8;
+    for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < ni; ++i) {
+                const size_t b = (size_t)(i >> 3) + (size_t)nbx * ((size_t)(j >> 3) + (size_t)nby * (k >> 3));
+                const double h = (double)half_value(codes[b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7)]);
+                values[(size_t)i + (size_t)ni * ((size_t)j + (size_t)nj * k)] =
+                    std::fma((double)so[2 * b], h, (double)so[2 * b + 1]);
+            }
     return SDFC_OK;
 }
 

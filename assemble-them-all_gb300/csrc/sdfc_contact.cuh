@@ -25,6 +25,8 @@
 //     sink, so a thread never holds a 12x12 block.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cfloat>
 #include <cstdint>
 #include <type_traits>
@@ -129,11 +131,17 @@ __device__ __forceinline__ Mat3<T> transpose(const Mat3<T>& A) {
 // indexed [i + ni*(j + nj*k)] (simulation/externals/sdfgen/array3.h:70-79).
 struct GridDesc {
     int ni, nj, nk;
-    int storage;  // 0 = FP64 values, 1 = FP32 values
+    int storage;  // 0 = FP64 values, 1 = FP32 values, 2 = FP16 bricks
     double min_box[3], max_box[3], dx[3], inv_dx[3];
     double org[3];  // min_box / dx (cell coordinate of the origin), for the fast depth path
     double col_th;
     const double* v64;   // FP64 values (storage 1: the FP32 values widened), read for active contacts
+    // storage 2: FP16 codes in 8^3-node bricks (brick b = bx + nbx (by + nby bz), node
+    // (i&7) + 8 (j&7) + 64 (k&7) within it) and per brick (scale, offset); value =
+    // fma(scale, code, offset), in FP64 for the exact paths and FP32 for the others
+    const unsigned short* b16;
+    const float2* bso;
+    int nbx, nby;
     // per cell (ni-1)(nj-1)(nk-1), i fastest: its 8 FP32 corner values in two float4,
     // (c000, c100, c010, c110) and (c001, c101, c011, c111); read by detection and the
     // FP32 derivatives with two 16-byte loads instead of eight scattered gathers
@@ -171,8 +179,53 @@ __device__ __forceinline__ Pose load_pose(const double* E) {
     return P;
 }
 
+__device__ __forceinline__ size_t brick_of(const GridDesc& g, int i, int j, int k) {
+    return (size_t)(i >> 3) + (size_t)g.nbx * ((size_t)(j >> 3) + (size_t)g.nby * (size_t)(k >> 3));
+}
+__device__ __forceinline__ float brick_code(const GridDesc& g, size_t b, int i, int j, int k) {
+    return __half2float(__ushort_as_half(__ldg(g.b16 + b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7))));
+}
+__device__ __forceinline__ double brick_value64(const GridDesc& g, int i, int j, int k) {
+    const size_t b = brick_of(g, i, j, k);
+    const float2 so = __ldg(g.bso + b);
+    return fma((double)so.x, (double)brick_code(g, b, i, j, k), (double)so.y);
+}
+__device__ __forceinline__ float brick_value32(const GridDesc& g, int i, int j, int k) {
+    const size_t b = brick_of(g, i, j, k);
+    const float2 so = __ldg(g.bso + b);
+    return fmaf(so.x, brick_code(g, b, i, j, k), so.y);
+}
+
 __device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, int k) {
+    if (g.b16) return brick_value64(g, i, j, k);
     return __ldg(g.v64 + (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k));
+}
+
+// The 8 corner values of cell (i, j, k), ordered c000, c100, c010, c110, c001, c101,
+// c011, c111: FP32 (from the cell-corner array or the bricks) and FP64.
+__device__ __forceinline__ void cell_corners32(const GridDesc& g, int i, int j, int k, float* c) {
+    if (g.b16) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) c[q] = brick_value32(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+        return;
+    }
+    const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
+    const float4 lo = __ldg(cq), hi = __ldg(cq + 1);
+    c[0] = lo.x; c[1] = lo.y; c[2] = lo.z; c[3] = lo.w;
+    c[4] = hi.x; c[5] = hi.y; c[6] = hi.z; c[7] = hi.w;
+}
+__device__ __forceinline__ void cell_corners64(const GridDesc& g, int i, int j, int k, double* c) {
+    if (g.b16) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) c[q] = brick_value64(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+        return;
+    }
+    const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
+    const size_t b = (size_t)i + sj * (size_t)j + sk * (size_t)k;
+    c[0] = __ldg(g.v64 + b);           c[1] = __ldg(g.v64 + b + 1);
+    c[2] = __ldg(g.v64 + b + sj);      c[3] = __ldg(g.v64 + b + sj + 1);
+    c[4] = __ldg(g.v64 + b + sk);      c[5] = __ldg(g.v64 + b + sk + 1);
+    c[6] = __ldg(g.v64 + b + sk + sj); c[7] = __ldg(g.v64 + b + sk + sj + 1);
 }
 
 // FP64 arithmetic in the reference's operation order without FMA contraction.
@@ -584,13 +637,11 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
     if constexpr (std::is_same<T, float>::value) {
         if (fc && fc->ok && !stencil_only) {
             const int i = fc->i, j = fc->j, k = fc->k;
-            const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
-            const size_t b = (size_t)i + sj * (size_t)j + sk * (size_t)k;
             const double ud = fc->ud, vd = fc->vd, wd = fc->wd;
-            const double e000 = __ldg(g.v64 + b), e100 = __ldg(g.v64 + b + 1);
-            const double e010 = __ldg(g.v64 + b + sj), e110 = __ldg(g.v64 + b + sj + 1);
-            const double e001 = __ldg(g.v64 + b + sk), e101 = __ldg(g.v64 + b + sk + 1);
-            const double e011 = __ldg(g.v64 + b + sk + sj), e111 = __ldg(g.v64 + b + sk + sj + 1);
+            double e[8];
+            cell_corners64(g, i, j, k, e);
+            const double e000 = e[0], e100 = e[1], e010 = e[2], e110 = e[3];
+            const double e001 = e[4], e101 = e[5], e011 = e[6], e111 = e[7];
             const double q0 = fma(ud, e100 - e000, e000), q1 = fma(ud, e110 - e010, e010);
             const double q2 = fma(ud, e101 - e001, e001), q3 = fma(ud, e111 - e011, e011);
             const double r0 = fma(vd, q1 - q0, q0), r1 = fma(vd, q3 - q2, q2);
@@ -599,10 +650,10 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             d = J.v + g.col_th;
             // FP32 analytic derivatives of the cell's interpolant
             const float u = (float)ud, v = (float)vd, w = (float)wd;
-            const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
-            const float4 lo = __ldg(cq), hi = __ldg(cq + 1);
-            const float c000 = lo.x, c100 = lo.y, c010 = lo.z, c110 = lo.w;
-            const float c001 = hi.x, c101 = hi.y, c011 = hi.z, c111 = hi.w;
+            float cc[8];
+            cell_corners32(g, i, j, k, cc);
+            const float c000 = cc[0], c100 = cc[1], c010 = cc[2], c110 = cc[3];
+            const float c001 = cc[4], c101 = cc[5], c011 = cc[6], c111 = cc[7];
             const float a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;
             const float b0 = fmaf(u, a00, c000), b1 = fmaf(u, a10, c010);
             const float b2 = fmaf(u, a01, c001), b3 = fmaf(u, a11, c011);

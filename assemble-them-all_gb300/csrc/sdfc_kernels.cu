@@ -59,9 +59,9 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
 }
 
 // FP32 trilinear interpolation for a point certainly inside the box, from the
-// cell-corner array (GridDesc::cells32).
-__device__ __forceinline__ float trilinear32(const float4* __restrict__ cells, int ni, int nj, int nk,
-                                             const Prefilter& f, float x, float y, float z) {
+// cell-corner array (GridDesc::cells32) or, with `g` non-null, from FP16 bricks.
+__device__ __forceinline__ float trilinear32(const float4* __restrict__ cells, const GridDesc* g, int ni, int nj,
+                                             int nk, const Prefilter& f, float x, float y, float z) {
     float cx = (x - f.gmin[0]) * f.ginv[0];
     float cy = (y - f.gmin[1]) * f.ginv[1];
     float cz = (z - f.gmin[2]) * f.ginv[2];
@@ -69,10 +69,18 @@ __device__ __forceinline__ float trilinear32(const float4* __restrict__ cells, i
     int j = min(max((int)floorf(cy), 0), nj - 2);
     int k = min(max((int)floorf(cz), 0), nk - 2);
     float u = cx - (float)i, w1 = cy - (float)j, w2 = cz - (float)k;
-    const float4* q = cells + 2 * ((size_t)i + (size_t)(ni - 1) * ((size_t)j + (size_t)(nj - 1) * k));
-    const float4 lo = __ldg(q), hi = __ldg(q + 1);
-    float c000 = lo.x, c100 = lo.y, c010 = lo.z, c110 = lo.w;
-    float c001 = hi.x, c101 = hi.y, c011 = hi.z, c111 = hi.w;
+    float c000, c100, c010, c110, c001, c101, c011, c111;
+    if (g) {
+        float c[8];
+        cell_corners32(*g, i, j, k, c);
+        c000 = c[0]; c100 = c[1]; c010 = c[2]; c110 = c[3];
+        c001 = c[4]; c101 = c[5]; c011 = c[6]; c111 = c[7];
+    } else {
+        const float4* q = cells + 2 * ((size_t)i + (size_t)(ni - 1) * ((size_t)j + (size_t)(nj - 1) * k));
+        const float4 lo = __ldg(q), hi = __ldg(q + 1);
+        c000 = lo.x; c100 = lo.y; c010 = lo.z; c110 = lo.w;
+        c001 = hi.x; c101 = hi.y; c011 = hi.z; c111 = hi.w;
+    }
     float a0 = fmaf(u, c100 - c000, c000), a1 = fmaf(u, c110 - c010, c010);
     float a2 = fmaf(u, c101 - c001, c001), a3 = fmaf(u, c111 - c011, c011);
     float b0 = fmaf(w1, a1 - a0, a0), b1 = fmaf(w1, a3 - a2, a2);
@@ -100,6 +108,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                                                                 int* __restrict__ tile_queue,
                                                                 const int* __restrict__ mode) {
     __shared__ Prefilter f;
+    __shared__ GridDesc gd;
     __shared__ const float4* gv;
     __shared__ const float* px;
     __shared__ int gn[3], pn;
@@ -120,6 +129,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         reinterpret_cast<float*>(&f)[tid] = reinterpret_cast<const float*>(pref + i)[tid];
     if (tid == 0) {
         const GridDesc& g = grids[I.grid];
+        gd = g;
         gv = g.cells32;
         gn[0] = g.ni;
         gn[1] = g.nj;
@@ -150,7 +160,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                 const bool surely_in = x >= f.lo_in[0] && x <= f.hi_in[0] && y >= f.lo_in[1] && y <= f.hi_in[1] &&
                                        z >= f.lo_in[2] && z <= f.hi_in[2];
                 if (surely_in) {
-                    const float d32 = trilinear32(gv, gn[0], gn[1], gn[2], f, x, y, z) + f.col_th;
+                    const float d32 = trilinear32(gv, gd.b16 ? &gd : nullptr, gn[0], gn[1], gn[2], f, x, y, z) + f.col_th;
                     if (fabsf(d32) <= f.guard)
                         queue = true;
                     else

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libsdfcontact.so")
 SDFC_OK = 0
 STORAGE_F64 = 0
 STORAGE_F32 = 1
+STORAGE_F16_BRICKS = 2
 
 # every symbol include/sdfc.h declares
 EXPORTS = (
@@ -27,6 +28,7 @@ EXPORTS = (
     "sdfc_batch_set_precision", "sdfc_evaluate_noalloc", "sdfc_sim_create", "sdfc_sim_destroy",
     "sdfc_sim_set_precision", "sdfc_sim_set_state", "sdfc_sim_get_state", "sdfc_sim_set_external_force",
     "sdfc_sim_step", "sdfc_sim_stats", "sdfc_sim_record", "sdfc_sim_history", "sdfc_sim_backward",
+    "sdfc_grid_values", "sdfc_f16_brick_encode", "sdfc_f16_brick_decode",
 )
 JOINT_TRANSLATIONAL = 3
 JOINT_FREE3D_EXP = 6
@@ -121,6 +123,9 @@ def lib():
         L.sdfc_sim_step.argtypes = [v, i, P(i)]
         L.sdfc_sim_stats.argtypes = [v, P(ctypes.c_longlong), P(ctypes.c_longlong)]
         L.sdfc_sim_record.argtypes = [v, i]
+        L.sdfc_grid_values.argtypes = [v, i, d]
+        L.sdfc_f16_brick_encode.argtypes = [d, i, i, i, v, v]
+        L.sdfc_f16_brick_decode.argtypes = [v, v, i, i, i, d]
         L.sdfc_sim_history.argtypes = [v, P(i), d]
         L.sdfc_sim_backward.argtypes = [v, d, d, d, d]
         L.sdfc_evaluate_noalloc.argtypes = [v, i, i, i, d, d, d, ctypes.c_double, v, i, v, v, v, v, v, i, v, v, v,
@@ -156,6 +161,7 @@ class Context:
             raise SdfcError(f"sdfc_create failed ({rc}): no usable CUDA device {device}")
         self.device = device
         self._npoints = {}
+        self._grid_shapes = {}
         self._batches = []
 
     def _check(self, rc, what):
@@ -181,7 +187,14 @@ class Context:
         self._check(lib().sdfc_upload_grid(self._h, _dp(v), ni, nj, nk, _dp(_f64(min_box, 3)), _dp(_f64(max_box, 3)),
                                            _dp(_f64(dx, 3)), float(col_th), int(storage), ctypes.byref(h)),
                     "sdfc_upload_grid")
+        self._grid_shapes[h.value] = (nk, nj, ni)
         return h.value
+
+    def grid_values(self, grid: int) -> np.ndarray:
+        """The grid as the evaluations see it, (nk, nj, ni) (sdfc_grid_values)."""
+        out = np.zeros(self._grid_shapes[grid])
+        self._check(lib().sdfc_grid_values(self._h, int(grid), _dp(out)), "sdfc_grid_values")
+        return out
 
     def upload_points(self, xyz, storage=STORAGE_F32) -> int:
         p = _f64(xyz).reshape(-1, 3)
@@ -390,3 +403,28 @@ class Sim:
         g0, gd0, gf = np.zeros((self.n, self.ndof)), np.zeros((self.n, self.ndof)), np.zeros((self.n, 6))
         self.ctx._check(lib().sdfc_sim_backward(self._h, _dp(df_dq), _dp(g0), _dp(gd0), _dp(gf)), "sdfc_sim_backward")
         return g0, gd0, gf
+
+
+def f16_brick_encode(values):
+    """sdfc_f16_brick_encode (host only): values (nk, nj, ni) -> (codes uint16 [nb*512], so float32 [nb, 2])."""
+    v = _f64(values)
+    nk, nj, ni = v.shape
+    nb = ((ni + 7) // 8) * ((nj + 7) // 8) * ((nk + 7) // 8)
+    codes = np.zeros(nb * 512, dtype=np.uint16)
+    so = np.zeros((nb, 2), dtype=np.float32)
+    rc = lib().sdfc_f16_brick_encode(_dp(v), ni, nj, nk, codes.ctypes.data, so.ctypes.data)
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_f16_brick_encode failed ({rc})")
+    return codes, so
+
+
+def f16_brick_decode(codes, so, shape):
+    """sdfc_f16_brick_decode (host only): the FP64 grid (nk, nj, ni) the codes stand for."""
+    nk, nj, ni = shape
+    codes = np.ascontiguousarray(codes, dtype=np.uint16)
+    so = np.ascontiguousarray(so, dtype=np.float32)
+    out = np.zeros(shape)
+    rc = lib().sdfc_f16_brick_decode(codes.ctypes.data, so.ctypes.data, ni, nj, nk, _dp(out))
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_f16_brick_decode failed ({rc})")
+    return out

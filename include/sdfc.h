@@ -46,6 +46,12 @@ extern "C" {
 /* storage of grid values / contact points on the device */
 #define SDFC_STORAGE_F64 0
 #define SDFC_STORAGE_F32 1
+/* Grid values as FP16 codes in bricks of 8x8x8 nodes, each brick with an FP32 scale and
+ * offset: value = offset + scale * code (see sdfc_f16_brick_encode).  A quarter of the
+ * FP64 grid's memory; its values keep about 11 significant bits (the brick's offset is 0
+ * where the SDF changes sign, so the values near the surface keep FP16's relative
+ * precision). */
+#define SDFC_STORAGE_F16_BRICKS 2
 
 /* How the SDF gradient and Hessian of an active contact are evaluated.
  * The reference takes central differences of the trilinear interpolant with
@@ -97,12 +103,29 @@ int sdfc_set_precision(sdfc_context* ctx, int precision);
  * BodySDFObj.h:13-16; filled by BodySDFObj::precompute_SDF / load_SDF,
  * BodySDFObj.cpp:38-116).  `values` holds ni*nj*nk doubles, i fastest.
  * storage = SDFC_STORAGE_F32 keeps FP32 values (exact for grids made by sdfgen,
- * which computes in FP32); SDFC_STORAGE_F64 keeps FP64 values.  Rejects
+ * which computes in FP32); SDFC_STORAGE_F64 keeps FP64 values;
+ * SDFC_STORAGE_F16_BRICKS keeps FP16 bricks, and every evaluation then uses the decoded
+ * values (sdfc_grid_values) as the grid.  Rejects
  * grids on which the reference's cell index could leave the array
  * ((max_box - min_box)/dx >= n on some axis), non-finite values, n < 2.
  * Writes a handle to *grid. */
 int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
                      const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid);
+
+/* The grid as the evaluations see it (host, ni*nj*nk doubles, i fastest): the FP64
+ * values, the FP32 values widened, or the decoded FP16 bricks. */
+int sdfc_grid_values(sdfc_context* ctx, int grid, double* values);
+
+/* Host-only FP16 brick codec of SDFC_STORAGE_F16_BRICKS (no device needed).  Bricks are
+ * nb = ceil(n/8) per axis, brick b = bx + nbx*(by + nby*bz); node (i, j, k) is code
+ * b*512 + (i&7) + 8*(j&7) + 64*(k&7) of brick (i>>3, j>>3, k>>3); nodes past the grid's
+ * end repeat its last node.  so[2b], so[2b+1] = scale, offset.  Encoding: offset 0 if the
+ * brick's values straddle 0, else the value nearest 0; scale = max|v - offset| / 32768;
+ * code = FP16(FP32((v - offset) / scale)).  Decoding: value = fma(scale, code, offset) in
+ * FP64 (the grid used by the exact paths; the FP32 paths use the same fma in FP32).
+ * codes holds nbx*nby*nbz*512 FP16 bit patterns, so 2*nbx*nby*nbz floats. */
+int sdfc_f16_brick_encode(const double* values, int ni, int nj, int nk, unsigned short* codes, float* so);
+int sdfc_f16_brick_decode(const unsigned short* codes, const float* so, int ni, int nj, int nk, double* values);
 
 /* Uploads a contact body's contact points (Body::_contact_points, body frame;
  * BodyMeshObj::precompute_contact_points, simulation/redmax/Body/BodyMeshObj.cpp:184-238).

@@ -9,7 +9,7 @@ from conftest import ROOT, submodule
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "sdfc.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(sdfc_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(sdfc_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_library_exports_header_symbols():

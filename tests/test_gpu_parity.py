@@ -317,3 +317,49 @@ def test_masked_requests(sdfc, ctx, workloads, precision):
         else:
             assert np.isnan(fm[k]).all() and np.isnan(Km[k]).all() and nact[k] == -7, k
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_f16_bricks_against_oracle(sdfc, ctx, oracle, workloads, precision):
+    """FP16-brick grids (SDFC_STORAGE_F16_BRICKS): the evaluations see the decoded grid
+    (sdfc_grid_values), so against the oracle on that grid they keep the bars of the other
+    storages (identical active sets; FP64 path fm 1e-10, Km/Dm 1e-6; mixed 1e-5).  Against the
+    original FP64 grid the error is FP16's; it is bounded loosely here and reported by the bench."""
+    rng = np.random.default_rng(21)
+    g = workloads.socket_grid(61, dtype=np.float64)  # 61 nodes per axis: partial bricks at the top
+    gh = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, sdfc.STORAGE_F16_BRICKS)
+    dec = ctx.grid_values(gh)
+    assert np.abs(dec - g.values).max() <= 2.0 ** -11 * np.abs(g.values).max()
+    pts = workloads.peg_points(8000, seed=11)
+    ph = ctx.upload_points(pts, 1)
+    n = 6
+    b = ctx.batch([ph] * n, [gh] * n)
+    b.set_precision(precision)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    rel = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.003),
+                                   [0.025 * np.cos(a), 0.025 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
+    EB = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.3), rng.normal(size=3))
+                   for _ in range(n)])
+    EA = EB @ rel
+    phiA = rng.normal(size=(n, 6)) * 0.2
+    phiB = rng.normal(size=(n, 6)) * 0.1
+    prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0) for _ in range(n)]
+    fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
+    assert not st.any()
+    og = oracle.Grid(dec, g.min_box, g.max_box, g.dx, 0.01)
+    og64 = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
+    op = oracle.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0)
+    for k in range(n):
+        rf, rK, rD, rids = oracle.pair_eval(og, pts, EA[k], phiA[k], EB[k], phiB[k], op, True)
+        assert nact[k] == len(rids) > 0
+        if precision == 0:
+            assert_close(f"inst {k} fm", fm[k], rf, rel=FM_REL)
+            assert_close(f"inst {k} Km", Km[k], rK, rel=JAC_REL)
+            assert_close(f"inst {k} Dm", Dm[k], rD, rel=JAC_REL)
+        else:
+            assert_close(f"inst {k} fm", fm[k], rf, rel=MIXED_REL, abs_=1e-9)
+            assert_close(f"inst {k} Km", Km[k], rK, rel=MIXED_REL, abs_=1e-9)
+            assert_close(f"inst {k} Dm", Dm[k], rD, rel=MIXED_REL, abs_=1e-9)
+        f64, _, _, _ = oracle.pair_eval(og64, pts, EA[k], phiA[k], EB[k], phiB[k], op, False)
+        assert np.linalg.norm(fm[k] - f64) <= 0.05 * np.linalg.norm(f64)  # FP16 quantisation
+    b.close()
