@@ -56,8 +56,20 @@ def sample_grid(fn, lo, hi, n: int, pad: float = 0.1, dtype=np.float64) -> GridS
     dx = (mx - mn) / (n - 1)
     mx = mn + (n - 1) * dx
     ax = [mn[a] + dx[a] * np.arange(n) for a in range(3)]
-    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
-    vals = fn(np.stack([X, Y, Z], axis=-1))
+    vals = np.empty((n, n, n))
+    Y, X = np.meshgrid(ax[1], ax[0], indexing="ij")
+
+    def slab(k):  # one z slab at a time bounds the memory of large grids
+        vals[k] = fn(np.stack([X, Y, np.full_like(X, ax[2][k])], axis=-1))
+
+    if n >= 128:  # NumPy releases the GIL inside its kernels: slabs in threads
+        import concurrent.futures as cf
+        import os
+        with cf.ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 1)) as ex:
+            list(ex.map(slab, range(n)))
+    else:
+        for k in range(n):
+            slab(k)
     vals = vals.astype(dtype).astype(np.float64)
     return GridSpec(np.ascontiguousarray(vals), mn, mx, dx)
 

@@ -378,6 +378,7 @@ def run_gpu(args, world, rank):
     d2h = n * (300 * 8 + 2 * 4)
 
     sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 else None
+    c5_res = run_c5(args, sdfc, ctx, torch) if args.c5_points > 0 and rank == 0 else None
     if sim_res is not None:
         plain = run_sim_plain(args, sdfc, ctx, g, p, n)
         plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
@@ -433,6 +434,8 @@ def run_gpu(args, world, rank):
         pool.close()
     if sim_res is not None:
         line["sim"] = sim_res
+    if c5_res is not None:
+        line["fp16_bricks"] = c5_res
     print(json.dumps(line), flush=True)
 
 
@@ -511,6 +514,119 @@ def run_sim_plain(args, sdfc, ctx, g, p, n_dirs, instances=4):
             "precision": "fp64", "scenes_per_sim": 1}
 
 
+def run_c5(args, sdfc, ctx, torch):
+    """Precision scaling: a two-part tab-in-slot assembly whose slotted part is a 512^3 SDF stored
+    as FP16 bricks (8^3 nodes, FP32 scale/offset per brick), the other part's 1M surface points
+    against it, 256 pull directions.  Batched derivative evaluations (mixed precision) are timed;
+    then 200 BDF1 steps of all directions.  Errors are reported against the same scenes on the
+    FP64 grid with FP64 evaluations: forces on a sample of instances, poses after the steps on a
+    sample of scenes, and the grid values themselves."""
+    asm = W.procedural_assembly(5, n_parts=2, points=(args.c5_points, args.c5_points), grids=(args.c5_grid,))
+    mover, still = 0, 1  # part 0's tab sits in part 1's slot
+    t = time.perf_counter()
+    grid = asm.parts[still].grid(args.c5_grid)
+    gen_s = time.perf_counter() - t
+    pts = asm.parts[mover].surface_points(args.c5_points, 55).astype(np.float32).astype(np.float64)
+    t = time.perf_counter()
+    g16 = ctx.upload_grid(grid.values, grid.min_box, grid.max_box, grid.dx, 0.0, sdfc.STORAGE_F16_BRICKS)
+    up_s = time.perf_counter() - t
+    g64 = ctx.upload_grid(grid.values, grid.min_box, grid.max_box, grid.dx, 0.0, sdfc.STORAGE_F64)
+    dec = ctx.grid_values(g16)
+    near = np.abs(grid.values) < 0.05
+    dist_err = {"max_abs": float(np.abs(dec - grid.values).max()),
+                "max_abs_within_0.05_of_surface": float(np.abs(dec - grid.values)[near].max()),
+                "max_rel": float((np.abs(dec - grid.values) / np.maximum(np.abs(grid.values), 1e-12)).max())}
+    ph = ctx.upload_points(pts, sdfc.STORAGE_F32)
+    n = args.c5_dirs
+    dirs = W.fibonacci_directions(n)
+    E_still = W.pose(None, asm.parts[still].position)
+    EA = np.stack([W.pose(None, asm.parts[mover].position + 0.0105 * d) for d in dirs])
+    EB = np.broadcast_to(E_still, (n, 4, 4)).copy()
+    phiA = np.zeros((n, 6))
+    phiA[:, 3:] = 0.01 * dirs
+    phiB = np.zeros((n, 6))
+    prm = [sdfc.Params(*PARAMS)] * n
+    b16 = ctx.batch([ph] * n, [g16] * n)
+    b16.set_precision(sdfc.PRECISION_MIXED)
+    cuda = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()  # noqa: E731
+    dEA, dphiA, dEB, dphiB = cuda(EA), cuda(phiA), cuda(EB), cuda(phiB)
+    dprm = cuda(np.tile(np.array(PARAMS), (n, 1)))
+    fm = torch.zeros(n, 12, dtype=torch.float64, device="cuda")
+    Km = torch.zeros(n, 144, dtype=torch.float64, device="cuda")
+    Dm = torch.zeros(n, 144, dtype=torch.float64, device="cuda")
+    nact = torch.zeros(n, dtype=torch.int32, device="cuda")
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+
+    def step():
+        b16.evaluate_device(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
+                            fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
+                            want_deriv=True, stream=stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            step()
+        stream.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    act = nact.cpu().numpy()
+    n_active = int(act.sum())
+    m = min(n, args.c5_check)
+    idx = np.sort(np.argsort(-act, kind="stable")[:m])  # the instances with the most contacts
+    f16 = (fm.cpu().numpy()[idx], Km.cpu().numpy()[idx].reshape(m, 12, 12), Dm.cpu().numpy()[idx].reshape(m, 12, 12))
+    b64 = ctx.batch([ph] * m, [g64] * m)
+    b64.set_precision(sdfc.PRECISION_FP64)
+    r = b64.evaluate(EA[idx], phiA[idx], EB[idx], phiB[idx], prm[:m], want_deriv=True)
+    force_err = {"fm": rel_err(f16[0], r[0]), "Km": rel_err(f16[1], r[1]), "Dm": rel_err(f16[2], r[2]),
+                 "fm_norm_rel": float(np.max(np.linalg.norm(f16[0] - r[0], axis=1) /
+                                             np.maximum(np.linalg.norm(r[0], axis=1), 1e-12))),
+                 "instances": m, "active_contacts_checked": int(act[idx].sum())}
+    b16.close()
+    b64.close()
+    out = {"grid": f"{args.c5_grid}^3 fp16 bricks", "grid_bytes": int(((args.c5_grid + 7) // 8) ** 3 * (512 * 2 + 8)),
+           "fp64_grid_bytes": int(args.c5_grid ** 3 * 8), "points": args.c5_points, "instances": n,
+           "ms_per_eval": ms, "contact_pts_per_s": n * args.c5_points / (ms / 1e3),
+           "active_contacts_per_eval": n_active, "grid_sample_s": gen_s, "grid_encode_upload_s": up_s,
+           "distance_error_vs_fp64_grid": dist_err, "force_error_vs_fp64_grid": force_err}
+    if args.c5_steps > 0:
+        m_, inertia = asm.parts[mover].mass_props()
+        E_pj0 = W.pose(None, asm.parts[mover].position)
+        mv = sdfc.Mover.make(m_, inertia, np.eye(4), SIM_H, SIM_GRAVITY, E_pj0=E_pj0)
+        F = np.zeros((n, 6))
+        F[:, 3:] = SIM_PULL * dirs
+
+        def sim_run(grid_h, which, precision):
+            scenes = len(which)
+            sim = ctx.sim([mv] * scenes, [sdfc.ScenePair.make(i, ph, grid_h, True, E_still, sdfc.Params(*PARAMS))
+                                          for i in range(scenes)])
+            sim.set_precision(precision)
+            sim.set_state(np.zeros((scenes, 3)), np.zeros((scenes, 3)))
+            sim.set_external_force(F[which])
+            t0 = time.perf_counter()
+            conv = sim.step(args.c5_steps)
+            wall = time.perf_counter() - t0
+            q, _ = sim.get_state()
+            r_, e_ = sim.stats()
+            sim.close()
+            return q, wall, conv, r_, e_
+
+        q16, wall, conv, rounds, evals = sim_run(g16, np.arange(n), sdfc.PRECISION_MIXED)
+        q64, _, _, _, _ = sim_run(g64, idx, sdfc.PRECISION_FP64)
+        out["sim"] = {"scenes": n, "steps": args.c5_steps, "wall_s": wall, "scene_steps_per_s": n * args.c5_steps / wall,
+                      "rounds": rounds, "scene_evaluations": evals, "converged_last_step": float(np.mean(conv)),
+                      "pose_error_vs_fp64_grid": {"max_abs": float(np.abs(q16[idx] - q64).max()),
+                                                   "max_displacement": float(np.abs(q64).max()), "scenes": m}}
+    return out
+
+
 def cpu_sim_rate(pool, n_scenes, steps, procs):
     dirs = W.fibonacci_directions(1024)
     idx = np.linspace(0, len(dirs) - 1, n_scenes).astype(int)
@@ -542,6 +658,11 @@ def main():
     ap.add_argument("--sim-steps", type=int, default=500, help="BDF1 steps of the direction sweep (0: skip)")
     ap.add_argument("--sim-early", type=int, default=25, help="steps also timed alone (compared with the CPU)")
     ap.add_argument("--cpu-sim-scenes", type=int, default=32, help="scenes stepped by the CPU baseline")
+    ap.add_argument("--c5-grid", type=int, default=512, help="FP16-brick leg: grid nodes per axis")
+    ap.add_argument("--c5-points", type=int, default=1000000, help="FP16-brick leg: points (0: skip the leg)")
+    ap.add_argument("--c5-dirs", type=int, default=256, help="FP16-brick leg: pull directions")
+    ap.add_argument("--c5-steps", type=int, default=200, help="FP16-brick leg: BDF1 steps (0: skip)")
+    ap.add_argument("--c5-check", type=int, default=8, help="FP16-brick leg: instances checked on the FP64 grid")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank = dist_setup()
