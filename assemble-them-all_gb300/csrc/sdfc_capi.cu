@@ -91,6 +91,18 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
     return SDFC_OK;
 }
 
+int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, double* dE, cudaStream_t stream) {
+    sdfc_context* ctx = b->ctx;
+    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck};
+    const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
+    const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
+    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream);
+    sdfc::launch_energy(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, stencil, prec, stream);
+    sdfc::launch_energy_finalize(b->n, sc, energy, dE, in.mode, stream);
+    CUDA_TRY(ctx, cudaGetLastError());
+    return SDFC_OK;
+}
+
 }  // namespace sdfc_impl
 
 namespace {
@@ -590,6 +602,53 @@ int sdfc_batch_evaluate_masked_device(sdfc_batch* b, const double* E_A, const do
     in.mode = request;
     sdfc::BatchOutputs out{fm, Km, Dm, n_active, status};
     return sdfc_impl::run_batch(b, in, true, out, (cudaStream_t)stream);
+}
+
+int sdfc_batch_energy_device(sdfc_batch* b, const double* E_A, const double* phi_A, const double* E_B,
+                             const double* phi_B, const double* params, double* energy, double* dE, void* stream) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!E_A || !phi_A || !E_B || !phi_B || !params || !energy || !dE)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_energy_device: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    sdfc::BatchInputs in{E_A, phi_A, E_B, phi_B, params};
+    return sdfc_impl::run_energy(b, in, energy, dE, (cudaStream_t)stream);
+}
+
+int sdfc_batch_energy(sdfc_batch* b, const double* E_A, const double* E_B, const sdfc_params* params, double* energy,
+                      double* dE) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!E_A || !E_B || !params || !energy || !dE) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_energy: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    const size_t n = (size_t)b->n;
+    double* h = b->h_in;
+    std::memcpy(h, E_A, sizeof(double) * 16 * n);
+    std::memset(h + 16 * n, 0, sizeof(double) * 6 * n);
+    std::memcpy(h + 22 * n, E_B, sizeof(double) * 16 * n);
+    std::memset(h + 38 * n, 0, sizeof(double) * 6 * n);
+    for (size_t k = 0; k < n; ++k) {
+        double* p = h + 44 * n + 6 * k;
+        p[0] = params[k].kn;
+        p[1] = params[k].kt;
+        p[2] = params[k].mu;
+        p[3] = params[k].damping;
+        p[4] = params[k].scale;
+        p[5] = params[k].contact_scale;
+    }
+    cudaStream_t st = ctx->stream;
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->d_in, h, sizeof(double) * 50 * n, cudaMemcpyHostToDevice, st));
+    double* d = b->d_in;
+    sdfc::BatchInputs in{d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n};
+    double* dout = b->d_out;  // energy [n] then dE [12 n]
+    if ((rc = sdfc_impl::run_energy(b, in, dout, dout + n, st))) return rc;
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->h_out, dout, sizeof(double) * 13 * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    std::memcpy(energy, b->h_out, sizeof(double) * n);
+    std::memcpy(dE, b->h_out + n, sizeof(double) * 12 * n);
+    return SDFC_OK;
 }
 
 int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, const double* E_B, const double* phi_B,

@@ -676,6 +676,39 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
     d = J.v + g.col_th;
 }
 
+// Penetration energy of one contact, e = kn d^2 / 2 with kn scaled as in the force law
+// (ForceGeneralSDFContact.cpp:155-156) and d = SDF + col_th < 0 its depth, and its derivatives
+// kn d dd/dq wrt the twist coordinates of body A (contact points) and body B (SDF), from the
+// same jet as the force path: dd/dxw = R_B g, so for body A
+//   w-rows: xi1 x (R_A^T R_B g),  v-rows: R_A^T R_B g,
+// and for body B (dx/dq_B = [skew(x) | -I]):  w-rows: g x x,  v-rows: -g.
+template <typename T>
+struct ContactEnergy {
+    double e;
+    Vec3<T> aw, av, bw, bv;
+};
+
+template <typename T>
+__device__ inline ContactEnergy<T> contact_energy(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
+                                                  bool valid, bool stencil_only, const ExactJet<T>* ej = nullptr) {
+    V3 xd;
+    double dd;
+    SdfJet<T> J;
+    contact_geometry(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
+    ContactEnergy<T> E;
+    const double kn = S.cp.kn;
+    E.e = valid ? 0.5 * kn * dd * dd : 0.0;
+    const T s = valid ? (T)(kn * dd) : T(0);
+    const Vec3<T> gr = J.g;
+    const Vec3<T> x = cast<T>(xd), xi1 = cast<T>(xi1d);
+    const Vec3<T> ga = mulT(S.R1, mul(S.R2, gr));
+    E.av = s * ga;
+    E.aw = s * cross(xi1, ga);
+    E.bw = s * cross(gr, x);
+    E.bv = -s * gr;
+    return E;
+}
+
 // The force-law scalars s1 = -kn d + kd ddot d and sK = kn d - kd ddot d
 // (ForceGeneralSDFContact.cpp:300, 328): in the reference's expression for the
 // FP64 path, from the FP64 depth rounded once for the FP32 path.

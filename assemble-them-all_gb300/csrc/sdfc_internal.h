@@ -64,6 +64,8 @@ void free_batch(sdfc_batch* b);
 void free_sim(sdfc_sim* s);
 // One evaluation of every instance (in.mode null) with `deriv`, or, with
 // in.mode set, each instance as it requests (0 skip, 1 value, 2 derivatives).
+// Penetration energy of every requested instance (in.mode: 0 skips): energy[n], dE[n x 12].
+int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, double* dE, cudaStream_t stream);
 int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
               cudaStream_t stream);
 

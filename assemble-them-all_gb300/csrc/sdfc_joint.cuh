@@ -328,6 +328,22 @@ __device__ inline void free_pose(const double* E_pj0, const double* E_ji, const 
     mv6(A, pj, phi);
 }
 
+// J = Ad(E_ij) S_j (6 x 6, row-major) of the free body at q: body twist = J qdot.
+__device__ inline void free_jacobian(const double* E_ji, const double* q, double* J) {
+    const double zero3[3] = {0.0, 0.0, 0.0};
+    Rot o;
+    rot_update(q + 3, zero3, false, o);
+    double A[36], S[36];
+    adjoint_inverse(E_ji, A);
+    zero(S, 36);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            S[6 * r + 3 + c] = o.T[3 * r + c];
+            S[6 * (r + 3) + c] = o.R[3 * c + r];
+        }
+    mul6(A, S, J);
+}
+
 // The reduced system of the free body at (q1, qd1) from the summed mover blocks of the
 // contacts (fmc[6], Kmc[36], Dmc[36], wrt the body twist).  Outputs g (with q0, qdot0) and,
 // with `deriv`, H and D; always M; J and R_0i for the adjoint if asked.

@@ -448,6 +448,114 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     }
 }
 
+// Penetration energy of every instance (sum over its active contacts of kn d^2 / 2) and its
+// gradient wrt both bodies' twist coordinates; one CTA per (instance, slot) like force_kernel,
+// partial row = [e, dE/dq_A (w, v), dE/dq_B (w, v)] (kOutEnergy values).
+template <bool STENCIL, typename T>
+__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(const InstanceDesc* __restrict__ inst,
+                                                        BatchInputs in, const GridDesc* __restrict__ grids,
+                                                        const PointsDesc* __restrict__ points,
+                                                        const int* __restrict__ ids,
+                                                        const int* __restrict__ tile_count,
+                                                        double* __restrict__ partial) {
+    constexpr int NW = kChunk / 32;
+    constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
+    __shared__ Accum<T> acc[NW * 12];
+    __shared__ double eacc[NW];
+    __shared__ int prefix[kMaxTilesPerInstance + 1];
+    __shared__ GridDesc g;
+    __shared__ PointsDesc P;
+    __shared__ PairState<T> S;
+    const int i = blockIdx.y, s = blockIdx.x;
+    if (in.mode && in.mode[i] == 0) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const InstanceDesc I = inst[i];
+    if (warp == 0) {
+        int run = 0;
+        if (lane == 0) prefix[0] = 0;
+        for (int k0 = 0; k0 < I.ntiles; k0 += 32) {
+            const int k = k0 + lane;
+            int v = k < I.ntiles ? tile_count[I.tile0 + k] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(kFull, v, o);
+                if (lane >= o) v += u;
+            }
+            if (k < I.ntiles) prefix[k + 1] = run + v;
+            run += __shfl_sync(kFull, v, 31);
+        }
+    } else if (tid == 32) {
+        g = grids[I.grid];
+        P = points[I.points];
+        make_pair_state(in.EA + 16 * (size_t)i, in.phiA + 6 * (size_t)i, in.EB + 16 * (size_t)i,
+                        in.phiB + 6 * (size_t)i, in.prm + 6 * (size_t)i, S);
+    }
+    for (int k = tid; k < NW * 12; k += kChunk) acc[k].zero();
+    if (tid < NW) eacc[tid] = 0.0;
+    __syncthreads();
+    const int total = prefix[I.ntiles];
+    const int nchunks = (total + kChunk - 1) / kChunk;
+    for (int chunk = s; chunk < nchunks; chunk += kSlots) {
+        const int c = chunk * kChunk + tid;
+        const bool valid = c < total;
+        V3 xi = v3(0, 0, 0);
+        if (valid) {
+            int lo = 0, hi = I.ntiles;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (prefix[mid] <= c)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            xi = load_point(P, ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])]);
+        }
+        FastCell fc;
+        const FastCell* fcp = nullptr;
+        ExactJet<T> ej;
+        const ExactJet<T>* ejp = nullptr;
+        if constexpr (kWarpExact) {
+            fc = fast_cell<T>(g, S.RT, S.pT, xi);
+            fcp = &fc;
+            warp_exact_jets<T>(g, S, xi, valid && !fc.ok, false, ej);
+            ejp = &ej;
+        }
+        const ContactEnergy<T> E = contact_energy<T>(g, xi, S, fcp, valid, STENCIL, ejp);
+        WarpSink<12, T> sink{acc + warp * 12, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
+        T v[12] = {E.aw.x, E.aw.y, E.aw.z, E.av.x, E.av.y, E.av.z, E.bw.x, E.bw.y, E.bw.z, E.bv.x, E.bv.y, E.bv.z};
+        sink.add12(v, 0, 1);
+        double e = E.e;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
+        if (lane == 0) eacc[warp] += e;
+    }
+    __syncthreads();
+    double* row = partial + ((size_t)i * kSlots + s) * kOutDeriv;
+    for (int k = tid; k < kOutEnergy; k += kChunk) {
+        double v = 0.0;
+        if (k == 0)
+            for (int w = 0; w < NW; ++w) v += eacc[w];
+        else
+            for (int w = 0; w < NW; ++w) v += acc[w * 12 + k - 1].value();
+        row[k] = v;
+    }
+}
+
+__global__ void energy_finalize_kernel(int n_inst, const double* __restrict__ partial, double* __restrict__ energy,
+                                       double* __restrict__ dE, const int* __restrict__ mode) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)n_inst * kOutEnergy) return;
+    const int i = (int)(idx / kOutEnergy), k = (int)(idx % kOutEnergy);
+    if (mode && mode[i] == 0) return;
+    const double* p = partial + (size_t)i * kSlots * kOutDeriv + k;
+    double v = 0.0;
+    for (int s = 0; s < kSlots; ++s) v += p[(size_t)s * kOutDeriv];
+    if (k == 0)
+        energy[i] = v;
+    else
+        dE[12 * (size_t)i + k - 1] = v;
+}
+
 // Column j of Ad(E_A^{-1} E_B) (twists ordered (w, v)): the map that turns the
 // dq1 columns of Km into its dq2 columns.  Every contact's force in the bodies'
 // frames is unchanged when both bodies move together, so for a world twist eps,
@@ -587,5 +695,33 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
 }
 
 bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !stencil && precision == kMixed; }
+
+void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
+                   const PointsDesc* d_points, BatchScratch s, bool stencil, int precision, cudaStream_t stream) {
+    if (n_inst <= 0) return;
+    dim3 grid(kSlots, n_inst);
+    if (precision == kMixed) {
+        if (stencil)
+            energy_kernel<true, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids, s.tile_count,
+                                                                     s.partial);
+        else
+            energy_kernel<false, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
+                                                                      s.tile_count, s.partial);
+    } else {
+        if (stencil)
+            energy_kernel<true, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
+                                                                      s.tile_count, s.partial);
+        else
+            energy_kernel<false, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
+                                                                       s.tile_count, s.partial);
+    }
+}
+
+void launch_energy_finalize(int n_inst, BatchScratch s, double* energy, double* dE, const int* mode,
+                            cudaStream_t stream) {
+    if (n_inst <= 0) return;
+    const size_t total = (size_t)n_inst * kOutEnergy;
+    energy_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(n_inst, s.partial, energy, dE, mode);
+}
 
 }  // namespace sdfc

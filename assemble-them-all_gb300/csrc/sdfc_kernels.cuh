@@ -49,6 +49,7 @@ constexpr int kSlots = 8;            // partial rows per instance
 constexpr int kMaxTilesPerInstance = 4096;
 constexpr int kOutDeriv = 300;       // fm (12) + Km (144) + Dm (144)
 constexpr int kOutValue = 12;
+constexpr int kOutEnergy = 13;      // penetration energy + its 12 twist derivatives
 
 // Fixed topology of one batch instance.
 struct InstanceDesc {
@@ -115,6 +116,12 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
                      cudaStream_t stream, const int* mode = nullptr, bool zero_status = true,
                      const BatchInputs* derive_q2 = nullptr);
+// Penetration energy (sum of kn d^2 / 2 over the active contacts) and its gradient wrt
+// both bodies' twists, after launch_detect: energy[n], dE[n x 12] (A: w, v; B: w, v).
+void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
+                   const PointsDesc* d_points, BatchScratch s, bool stencil, int precision, cudaStream_t stream);
+void launch_energy_finalize(int n_inst, BatchScratch s, double* energy, double* dE, const int* mode,
+                            cudaStream_t stream);
 // Whether launch_force's derivative pass leaves the dq2 columns of Km to finalize
 // (the FP32-algebra path outside the stencil mode).
 bool force_skips_q2(bool deriv, bool stencil, int precision);

@@ -34,7 +34,7 @@ using sdfc_impl::use_device;
 
 namespace {
 
-constexpr double kTol = 1e-8;     // Simulation.cpp:1008
+constexpr double kTol = 1e-8;     // Simulation.cpp:1008 (default of MoverDev::tol)
 constexpr int kMaxLineSearch = 20;  // :1011
 constexpr int kMaxStrike = 3;     // :1014
 
@@ -44,6 +44,7 @@ constexpr int kMaxDof = 6;
 
 struct MoverDev {
     double mass, inertia[6], E_pj0[16], E_ji[16], gravity[3], h, Kr, Dr;
+    double tol;  // Newton tolerance on |g| (the reference's 1e-8 unless set)
     int max_iter;
     int ndof;  // 3: translational, 6: free3d-exp
 };
@@ -326,7 +327,7 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
         }
         if (step_done) {
             ++s.iter;
-            if (gn < kTol) {
+            if (gn < m.tol) {
                 s.converged = 1;
                 done = true;
             } else if (s.iter >= m.max_iter) {
@@ -473,6 +474,7 @@ __global__ void adj_step_kernel(int n, int nd, const int* __restrict__ pair_begi
                                 const double* __restrict__ fm, const double* __restrict__ Km,
                                 const double* __restrict__ Dm, const double* __restrict__ q_his,
                                 const double* __restrict__ qd0_rec, const double* __restrict__ df_dq,
+                                const double* __restrict__ gE_his, const double* __restrict__ df_dE,
                                 const int* __restrict__ t_dev, AdjState* __restrict__ adj, double* __restrict__ gout) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int t = t_dev[0], T = t_dev[1];
@@ -529,6 +531,8 @@ __global__ void adj_step_kernel(int n, int nd, const int* __restrict__ pair_begi
     AdjState a = adj[i];
     double y[kMaxDof];
     for (int c = 0; c < nd; ++c) y[c] = df_dq[((size_t)i * T + (t - 1)) * nd + c];
+    if (gE_his)  // dL/dE_total times dE_t/dq_t (step t's energy at its end state)
+        for (int c = 0; c < nd; ++c) y[c] += df_dE[i] * gE_his[((size_t)(t - 1) * n + i) * nd + c];
     if (t < T)  // step t + 1: dg/dq_t = -2 M_{t+1} + h D_{t+1}
         for (int c = 0; c < nd; ++c)
             for (int r = 0; r < nd; ++r) y[c] -= (-2.0 * a.M1[nd * r + c] + h * a.D1[nd * r + c]) * a.z1[r];
@@ -578,6 +582,64 @@ __global__ void adj_step_kernel(int n, int nd, const int* __restrict__ pair_begi
 
 __global__ void adj_advance_kernel(int* t_dev) { t_dev[0] -= 1; }
 
+// ---------------------------------------------------------------- penetration energy of the steps
+//
+// With energy recording on, every recorded step also evaluates each pair's penetration energy
+// at the step's end state (sdfc_batch_energy) and reduces it per scene: E_t and its gradient
+// wrt the joint coordinates, J^T dE/dq_m (the mover's twist block of each pair).
+
+__global__ void energy_pose_kernel(int n_pairs, int nd, const int* __restrict__ pair_inst,
+                                   const int* __restrict__ role, const double* __restrict__ E_fixed,
+                                   const MoverDev* __restrict__ mover, const double* __restrict__ q,
+                                   const double* __restrict__ qd, double* __restrict__ EA, double* __restrict__ phiA,
+                                   double* __restrict__ EB, double* __restrict__ phiB) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pairs) return;
+    const int i = pair_inst[k];
+    double E0i[16], phi[6];
+    mover_pose(mover[i], q + (size_t)nd * i, qd + (size_t)nd * i, E0i, phi);
+    double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
+    double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
+    double *Ef = role[k] ? EB + 16 * (size_t)k : EA + 16 * (size_t)k;
+    double *pf = role[k] ? phiB + 6 * (size_t)k : phiA + 6 * (size_t)k;
+    for (int c = 0; c < 16; ++c) {
+        Em[c] = E0i[c];
+        Ef[c] = E_fixed[16 * (size_t)k + c];
+    }
+    for (int c = 0; c < 6; ++c) {
+        pm[c] = phi[c];
+        pf[c] = 0.0;
+    }
+}
+
+__global__ void energy_reduce_kernel(int n, int nd, const int* __restrict__ pair_begin, const int* __restrict__ role,
+                                     const MoverDev* __restrict__ mover, const double* __restrict__ q,
+                                     const double* __restrict__ e_pair, const double* __restrict__ dE_pair,
+                                     double* __restrict__ E_out, double* __restrict__ g_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const MoverDev& m = mover[i];
+    double e = 0.0, dm[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = pair_begin[i]; k < pair_begin[i + 1]; ++k) {
+        e += e_pair[k];
+        const int o = role[k] ? 0 : 6;
+        for (int c = 0; c < 6; ++c) dm[c] += dE_pair[12 * (size_t)k + o + c];
+    }
+    E_out[i] = e;
+    double* g = g_out + (size_t)nd * i;
+    if (nd == 6) {
+        double J[36];
+        sdfc_joint::free_jacobian(m.E_ji, q + 6 * (size_t)i, J);
+        for (int c = 0; c < 6; ++c) {
+            double v = 0.0;
+            for (int r = 0; r < 6; ++r) v += J[6 * r + c] * dm[r];
+            g[c] = v;
+        }
+    } else {  // J = [0; R_ji^T]: g = R_ji dE/dv
+        for (int r = 0; r < 3; ++r) g[r] = m.E_ji[4 * r] * dm[3] + m.E_ji[4 * r + 1] * dm[4] + m.E_ji[4 * r + 2] * dm[5];
+    }
+}
+
 }  // namespace
 
 struct sdfc_sim {
@@ -612,6 +674,11 @@ struct sdfc_sim {
     double* d_gout = nullptr;
     int* d_t = nullptr;
     cudaGraphExec_t back_exec = nullptr;
+    // penetration energy per recorded step (step-major, record_cap x n) and its joint-space
+    // gradient (record_cap x n x nd); per-pair energies of one evaluation; dL/dE per scene
+    int energy_on = 0;
+    double *d_Ehis = nullptr, *d_gEhis = nullptr, *d_epair = nullptr, *d_dEpair = nullptr, *d_dfdE = nullptr;
+    std::vector<MoverDev> movers;  // host copy (tolerance updates)
 };
 
 namespace sdfc_impl {
@@ -624,6 +691,8 @@ void free_sim(sdfc_sim* s) {
     cudaFree(s->d_qhis);
     cudaFree(s->d_qd0rec);
     cudaFree(s->d_dfdq);
+    cudaFree(s->d_Ehis);
+    cudaFree(s->d_gEhis);
     for (void* p : s->allocations) cudaFree(p);
     if (s->h_remaining) cudaFreeHost(s->h_remaining);
     if (s->batch) sdfc_impl::free_batch(s->batch);
@@ -707,6 +776,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         d.Dr = m.joint_damping;
         d.max_iter = std::max(20 * nd, 100);  // Simulation.cpp:1009
         d.ndof = nd;
+        d.tol = kTol;
         md[i] = d;
     }
     if (n_pairs > 0 && (rc = sdfc_impl::batch_create(ctx, n_pairs, pts.data(), grd.data(), &s->batch))) {
@@ -724,7 +794,9 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         (rc = alloc(s, &s->d_Dm, 144 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_nact, n_pairs)) ||
         (rc = alloc(s, &s->d_status, n_pairs)) || (rc = alloc(s, &s->d_conv, n)) ||
         (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, 1)) || (rc = alloc(s, &s->d_adj, n)) ||
-        (rc = alloc(s, &s->d_gout, 18 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2))) {
+        (rc = alloc(s, &s->d_gout, 18 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2)) ||
+        (rc = alloc(s, &s->d_epair, n_pairs)) || (rc = alloc(s, &s->d_dEpair, 12 * (size_t)n_pairs)) ||
+        (rc = alloc(s, &s->d_dfdE, n))) {
         free_sim(s);
         return rc;
     }
@@ -732,6 +804,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         free_sim(s);
         return fail(ctx, SDFC_ERR_CUDA, "sim_create: cudaMallocHost failed");
     }
+    s->movers = md;
     cudaError_t e = cudaMemcpy(s->d_mover, md.data(), sizeof(MoverDev) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n_pairs > 0) {
         e = cudaMemcpy(s->d_pair_inst, inst.data(), sizeof(int) * n_pairs, cudaMemcpyHostToDevice);
@@ -885,7 +958,8 @@ int capture_backward(sdfc_sim* s) {
     if (!rc) {
         adj_step_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
                                                          s->d_fm, s->d_Km, s->d_Dm, s->d_qhis, s->d_qd0rec, s->d_dfdq,
-                                                         s->d_t, s->d_adj, s->d_gout);
+                                                         s->energy_on ? s->d_gEhis : nullptr, s->d_dfdE, s->d_t,
+                                                         s->d_adj, s->d_gout);
         adj_advance_kernel<<<1, 1, 0, st>>>(s->d_t);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
@@ -903,7 +977,71 @@ int capture_backward(sdfc_sim* s) {
 
 }  // namespace
 
+// Penetration energy at the end state of the step just recorded (recorded >= 1).
+int record_energy_step(sdfc_sim* s, cudaStream_t st) {
+    const int n = s->n, np = s->n_pairs, nd = s->nd, tb = 128;
+    double* E_out = s->d_Ehis + (size_t)n * (s->recorded - 1);
+    double* g_out = s->d_gEhis + (size_t)nd * n * (s->recorded - 1);
+    if (np > 0) {
+        energy_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, nd, s->d_pair_inst, s->d_role, s->d_Efixed,
+                                                             s->d_mover, s->d_q, s->d_qd, s->d_EA, s->d_phiA, s->d_EB,
+                                                             s->d_phiB);
+        sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
+        int rc = sdfc_impl::run_energy(s->batch, in, s->d_epair, s->d_dEpair, st);
+        if (rc) return rc;
+    }
+    energy_reduce_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, nd, s->d_pair_begin, s->d_role, s->d_mover, s->d_q,
+                                                          s->d_epair, s->d_dEpair, E_out, g_out);
+    return SDFC_OK;
+}
+
 extern "C" {
+
+int sdfc_sim_record_energy(sdfc_sim* s, int on) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    int rc = sdfc_sim_record(s, 0);  // a recording kept so far has no energies: stop it
+    if (rc) return rc;
+    s->energy_on = on ? 1 : 0;
+    return SDFC_OK;
+}
+
+int sdfc_sim_energy(sdfc_sim* s, double* per_step, double* total) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    if (!s->energy_on || s->record_cap == 0)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_energy: energy recording is off");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    const int n = s->n, T = s->recorded;
+    std::vector<double> h((size_t)n * std::max(T, 1), 0.0);
+    if (T > 0) {
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), s->d_Ehis, sizeof(double) * n * T, cudaMemcpyDeviceToHost,
+                                           ctx->stream));
+        SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    for (int i = 0; i < n; ++i) {
+        double acc = 0.0;
+        for (int t = 0; t < T; ++t) {
+            const double e = h[(size_t)t * n + i];
+            if (per_step) per_step[(size_t)i * T + t] = e;
+            acc += e;
+        }
+        if (total) total[i] = acc;
+    }
+    return SDFC_OK;
+}
+
+int sdfc_sim_set_tolerance(sdfc_sim* s, double tol) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    if (!(tol > 0.0)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_tolerance: tolerance must be > 0");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    for (auto& m : s->movers) m.tol = tol;
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpy(s->d_mover, s->movers.data(), sizeof(MoverDev) * s->n, cudaMemcpyHostToDevice));
+    return SDFC_OK;
+}
 
 int sdfc_sim_record(sdfc_sim* s, int max_steps) {
     if (!s) return SDFC_ERR_INVALID_ARGUMENT;
@@ -918,14 +1056,20 @@ int sdfc_sim_record(sdfc_sim* s, int max_steps) {
     }
     cudaFree(s->d_qhis);
     cudaFree(s->d_qd0rec);
-    s->d_qhis = s->d_qd0rec = nullptr;
+    cudaFree(s->d_Ehis);
+    cudaFree(s->d_gEhis);
+    s->d_qhis = s->d_qd0rec = s->d_Ehis = s->d_gEhis = nullptr;
     s->record_cap = s->recorded = 0;
     if (max_steps == 0) return SDFC_OK;
     const size_t n3 = (size_t)s->nd * s->n;
     if ((rc = dev_alloc(ctx, (void**)&s->d_qhis, sizeof(double) * n3 * ((size_t)max_steps + 1))) ||
-        (rc = dev_alloc(ctx, (void**)&s->d_qd0rec, sizeof(double) * n3))) {
+        (rc = dev_alloc(ctx, (void**)&s->d_qd0rec, sizeof(double) * n3)) ||
+        (s->energy_on && ((rc = dev_alloc(ctx, (void**)&s->d_Ehis, sizeof(double) * s->n * (size_t)max_steps)) ||
+                          (rc = dev_alloc(ctx, (void**)&s->d_gEhis, sizeof(double) * n3 * (size_t)max_steps))))) {
         cudaFree(s->d_qhis);
-        s->d_qhis = nullptr;
+        cudaFree(s->d_qd0rec);
+        cudaFree(s->d_Ehis);
+        s->d_qhis = s->d_qd0rec = s->d_Ehis = nullptr;
         return rc;
     }
     SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis, s->d_q, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -955,9 +1099,16 @@ int sdfc_sim_history(sdfc_sim* s, int* steps, double* q_his) {
 }
 
 int sdfc_sim_backward(sdfc_sim* s, const double* df_dq, double* df_dq0, double* df_dqdot0, double* df_dfext) {
+    return sdfc_sim_backward_energy(s, df_dq, nullptr, df_dq0, df_dqdot0, df_dfext);
+}
+
+int sdfc_sim_backward_energy(sdfc_sim* s, const double* df_dq, const double* df_dE, double* df_dq0,
+                             double* df_dqdot0, double* df_dfext) {
     if (!s) return SDFC_ERR_INVALID_ARGUMENT;
     sdfc_context* ctx = s->ctx;
     if (!df_dq) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_backward: null df_dq");
+    if (df_dE && !s->energy_on)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_backward: energy recording is off (sdfc_sim_record_energy)");
     if (s->record_cap == 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_backward: recording is off");
     int rc = use_device(ctx);
     if (rc) return rc;
@@ -978,6 +1129,10 @@ int sdfc_sim_backward(sdfc_sim* s, const double* df_dq, double* df_dq0, double* 
             s->dfdq_cap = need;
         }
         SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_dfdq, df_dq, sizeof(double) * need, cudaMemcpyHostToDevice, st));
+        if (df_dE)
+            SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_dfdE, df_dE, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        else
+            SDFC_CUDA_TRY(ctx, cudaMemsetAsync(s->d_dfdE, 0, sizeof(double) * n, st));
         adj_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, T, s->d_adj, s->d_t);
         SDFC_CUDA_TRY(ctx, cudaGetLastError());
         if (!s->back_exec && (rc = capture_backward(s))) return rc;
@@ -1024,6 +1179,7 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
             ++s->recorded;
             SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis + (size_t)s->nd * n * s->recorded, s->d_q,
                                                sizeof(double) * s->nd * n, cudaMemcpyDeviceToDevice, st));
+            if (s->energy_on && (rc = record_energy_step(s, st))) return rc;
         }
     }
     SDFC_CUDA_TRY(ctx, cudaGetLastError());

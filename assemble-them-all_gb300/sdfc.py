@@ -28,7 +28,9 @@ EXPORTS = (
     "sdfc_batch_set_precision", "sdfc_evaluate_noalloc", "sdfc_sim_create", "sdfc_sim_destroy",
     "sdfc_sim_set_precision", "sdfc_sim_set_state", "sdfc_sim_get_state", "sdfc_sim_set_external_force",
     "sdfc_sim_step", "sdfc_sim_stats", "sdfc_sim_record", "sdfc_sim_history", "sdfc_sim_backward",
-    "sdfc_grid_values", "sdfc_f16_brick_encode", "sdfc_f16_brick_decode",
+    "sdfc_grid_values", "sdfc_f16_brick_encode", "sdfc_f16_brick_decode", "sdfc_batch_energy",
+    "sdfc_batch_energy_device", "sdfc_sim_record_energy", "sdfc_sim_energy", "sdfc_sim_backward_energy",
+    "sdfc_sim_set_tolerance",
 )
 JOINT_TRANSLATIONAL = 3
 JOINT_FREE3D_EXP = 6
@@ -124,6 +126,12 @@ def lib():
         L.sdfc_sim_stats.argtypes = [v, P(ctypes.c_longlong), P(ctypes.c_longlong)]
         L.sdfc_sim_record.argtypes = [v, i]
         L.sdfc_grid_values.argtypes = [v, i, d]
+        L.sdfc_batch_energy.argtypes = [v, d, d, P(Params), d, d]
+        L.sdfc_sim_record_energy.argtypes = [v, i]
+        L.sdfc_sim_energy.argtypes = [v, d, d]
+        L.sdfc_sim_backward_energy.argtypes = [v, d, d, d, d, d]
+        L.sdfc_sim_set_tolerance.argtypes = [v, ctypes.c_double]
+        L.sdfc_batch_energy_device.argtypes = [v, v, v, v, v, v, v, v, v]
         L.sdfc_f16_brick_encode.argtypes = [d, i, i, i, v, v]
         L.sdfc_f16_brick_decode.argtypes = [v, v, i, i, i, d]
         L.sdfc_sim_history.argtypes = [v, P(i), d]
@@ -289,6 +297,17 @@ class Batch:
                                                          int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active,
                                                          status, stream), "sdfc_batch_evaluate_device")
 
+    def energy(self, E_A, E_B, params):
+        """Penetration energy per instance (n,) and its gradient wrt both bodies' twists (n, 12)."""
+        n = self.n
+        pa = (Params * n)()
+        for k in range(n):
+            pa[k] = params[k] if isinstance(params, (list, tuple)) else params
+        e, dE = np.zeros(n), np.zeros((n, 12))
+        self.ctx._check(lib().sdfc_batch_energy(self._h, _dp(_f64(E_A, 16 * n)), _dp(_f64(E_B, 16 * n)), pa, _dp(e),
+                                                _dp(dE)), "sdfc_batch_energy")
+        return e, dE
+
     def evaluate_masked_device(self, E_A, phi_A, E_B, phi_B, params, request, fm, Km, Dm, n_active, status,
                                stream=0):
         """Device pointers; request (device int32[n]): 0 skip, 1 fm only, 2 fm, Km, Dm."""
@@ -390,8 +409,26 @@ class Sim:
         self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), _dp(q)), "sdfc_sim_history")
         return q
 
-    def backward(self, df_dq):
-        """Simulation::backward_BDF1 over the recorded steps for dL/dq_k (n, T, ndof):
+    def record_energy(self, on=True):
+        """Also record each step's penetration energy (call before record(); stops a recording)."""
+        self.generation += 1
+        self.ctx._check(lib().sdfc_sim_record_energy(self._h, int(bool(on))), "sdfc_sim_record_energy")
+
+    def energy(self):
+        """Recorded penetration energies: per step (n, T) and their sum (n,)."""
+        T = ctypes.c_int()
+        self.ctx._check(lib().sdfc_sim_history(self._h, ctypes.byref(T), None), "sdfc_sim_history")
+        per, tot = np.zeros((self.n, T.value)), np.zeros(self.n)
+        self.ctx._check(lib().sdfc_sim_energy(self._h, _dp(per), _dp(tot)), "sdfc_sim_energy")
+        return per, tot
+
+    def set_tolerance(self, tol: float):
+        """Newton tolerance on |g| (the reference's 1e-8 by default)."""
+        self.ctx._check(lib().sdfc_sim_set_tolerance(self._h, float(tol)), "sdfc_sim_set_tolerance")
+
+    def backward(self, df_dq, df_dE=None):
+        """Simulation::backward_BDF1 over the recorded steps for dL/dq_k (n, T, ndof) and, with
+        energy recording, dL/d(sum of the steps' penetration energies) df_dE (n,):
         returns dL/dq0 (n, ndof), dL/dqdot0 (n, ndof), dL/d(external force) (n, 6)."""
         df_dq = np.ascontiguousarray(df_dq, dtype=np.float64)
         if df_dq.ndim != 3 or df_dq.shape[0] != self.n or df_dq.shape[2] != self.ndof:
@@ -401,7 +438,9 @@ class Sim:
         if df_dq.shape[1] != T.value:
             raise ValueError(f"df_dq covers {df_dq.shape[1]} steps, {T.value} recorded")
         g0, gd0, gf = np.zeros((self.n, self.ndof)), np.zeros((self.n, self.ndof)), np.zeros((self.n, 6))
-        self.ctx._check(lib().sdfc_sim_backward(self._h, _dp(df_dq), _dp(g0), _dp(gd0), _dp(gf)), "sdfc_sim_backward")
+        dfE = None if df_dE is None else _f64(df_dE, self.n)
+        self.ctx._check(lib().sdfc_sim_backward_energy(self._h, _dp(df_dq), None if dfE is None else _dp(dfE), _dp(g0),
+                                                       _dp(gd0), _dp(gf)), "sdfc_sim_backward_energy")
         return g0, gd0, gf
 
 

@@ -178,6 +178,19 @@ int sdfc_batch_evaluate_device(sdfc_batch* batch, const double* E_A, const doubl
                                const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
                                double* Dm, int* n_active, int* status, void* stream);
 
+/* Penetration energy of every instance: energy[i] = sum over its active contacts of
+ * kn d^2 / 2 (d = SDF + col_th < 0 the contact's depth, kn scaled by scale * contact_scale as
+ * in the force law) and dE[12 i ..] its gradient wrt the twist coordinates of body A then B
+ * (w then v, body frames, like the rows of fm): kn d dd/dq.  No counterpart in the reference,
+ * which has no energy; it serves losses on penetration (the rollout adjoint).  Host arrays
+ * (E_A, E_B [n*16], params [n], energy [n], dE [n*12]); velocities play no part. */
+int sdfc_batch_energy(sdfc_batch* batch, const double* E_A, const double* E_B, const sdfc_params* params,
+                      double* energy, double* dE);
+/* Same with DEVICE arrays (phi_A, phi_B [n*6] are read but do not change the result; params
+ * n x 6) on `stream`. */
+int sdfc_batch_energy_device(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
+                             const double* phi_B, const double* params, double* energy, double* dE, void* stream);
+
 /* sdfc_batch_evaluate_device with a per-instance request (DEVICE int[n]): 0 skips the
  * instance (its outputs are left as they are), 1 evaluates fm only
  * (ForceGeneralSDFContact::computeForce), 2 fm, Km and Dm (computeForceWithDerivative).
@@ -279,6 +292,21 @@ int sdfc_sim_history(sdfc_sim* sim, int* steps, double* q_his);
  * reference does not compute: dL/d(external force), the force held constant over the
  * T steps. */
 int sdfc_sim_backward(sdfc_sim* sim, const double* df_dq, double* df_dq0, double* df_dqdot0, double* df_dfext);
+
+/* Penetration energy of the rollout (no counterpart in the reference).  With energy recording
+ * on (call before sdfc_sim_record; switching it stops a recording), every recorded step also
+ * evaluates the penetration energy E_t of each scene at the step's end state (the sum over the
+ * scene's pairs of sdfc_batch_energy) and its gradient wrt the joint coordinates.
+ * sdfc_sim_energy: per_step (host, n x T, may be NULL) and total (host, n, may be NULL) = sum_t E_t.
+ * sdfc_sim_backward_energy: sdfc_sim_backward for L(q_1..q_T, sum_t E_t) given also
+ * df_dE (host, n) = dL/d(sum_t E_t) per scene (NULL: 0). */
+int sdfc_sim_record_energy(sdfc_sim* sim, int on);
+int sdfc_sim_energy(sdfc_sim* sim, double* per_step, double* total);
+int sdfc_sim_backward_energy(sdfc_sim* sim, const double* df_dq, const double* df_dE, double* df_dq0,
+                             double* df_dqdot0, double* df_dfext);
+/* Newton tolerance on |g| of every scene (the reference's 1e-8, Simulation.cpp:1008, by default).
+ * A tighter tolerance lets finite differences of a rollout resolve its adjoint. */
+int sdfc_sim_set_tolerance(sdfc_sim* sim, double tol);
 
 /* ---------------------------------------------------------------- allocation-free evaluation */
 

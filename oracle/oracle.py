@@ -328,3 +328,20 @@ def bdf1_backward(mover: Mover, pairs, q_his, qdot0, df_dq):
     L.orc_bdf1_backward(ctypes.byref(m), arr, len(pairs), _dp(q_his), _dp(_f64(qdot0)), T, _dp(df_dq), _dp(g0),
                         _dp(gd0), _dp(gf))
     return g0, gd0, gf
+
+
+def pair_energy(grid: Grid, pts, E_A, E_B, params: Params):
+    """Penetration energy of a pair and its gradient (12) wrt the twists of A then B."""
+    L = lib()
+    if not hasattr(L, "_energy_ready"):
+        L.orc_pair_energy.restype = ctypes.c_double
+        L.orc_pair_energy.argtypes = [ctypes.POINTER(_Grid), ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(_Params), ctypes.POINTER(ctypes.c_double)]
+        L._energy_ready = True
+    g = grid._c()
+    p = _f64(pts).reshape(-1, 3)
+    dE = np.zeros(12)
+    prm = params._c()
+    e = L.orc_pair_energy(ctypes.byref(g), _dp(p), len(p), _dp(_f64(E_A)), _dp(_f64(E_B)), ctypes.byref(prm), _dp(dE))
+    return e, dE

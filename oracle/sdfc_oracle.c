@@ -803,6 +803,51 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
     return n_active;
 }
 
+/* ------------------------------------------------------------------ penetration energy */
+
+/* Penetration energy of a pair: the sum over its active contacts (orc_detect) of kn d^2 / 2,
+ * kn scaled as in the force law (ForceGeneralSDFContact.cpp:155-156), and its gradient wrt the
+ * twists of A then B (w, v each): kn d dd/dq with dd/dxw = R_B g (g = query_dSDF at the
+ * grid-frame point, BodySDFObj.cpp:176-187), dxw/dq_A = [-R_A skew(xi) | R_A],
+ * dx/dq_B = [skew(x) | -I].  The reference has no energy; this is the definition the GPU's
+ * energy mode computes, on the reference's own distance and gradient. */
+double orc_pair_energy(const orc_grid* g, const double* pts, int n_pts, const double* E_A, const double* E_B,
+                       const orc_params* prm, double* dE) {
+    int* ids = (int*)malloc(sizeof(int) * (size_t)(n_pts > 0 ? n_pts : 1));
+    double* dist = (double*)malloc(sizeof(double) * (size_t)(n_pts > 0 ? n_pts : 1));
+    const int na = orc_detect(g, E_A, E_B, pts, n_pts, ids, dist);
+    const double kn = prm->kn * prm->scale * prm->contact_scale;
+    double RA[9], pA[3], RB[9], pB[3];
+    pose_split(E_A, RA, pA);
+    pose_split(E_B, RB, pB);
+    double e = 0.0;
+    for (int k = 0; k < 12; ++k) dE[k] = 0.0;
+    for (int c = 0; c < na; ++c) {
+        const double* xi = pts + 3 * (size_t)ids[c];
+        double xw[3], t[3], x[3], gr[3], w[3], ga[3], aw[3], bw[3];
+        m3_vec(RA, xi, xw);
+        for (int k = 0; k < 3; ++k) t[k] = xw[k] + pA[k] - pB[k];
+        m3t_vec(RB, t, x);
+        const double d = dist[ids[c]]; /* orc_detect writes distances by point index */
+        orc_query_dsdf(g, x, gr);
+        m3_vec(RB, gr, w);
+        m3t_vec(RA, w, ga);
+        cross3(xi, ga, aw);
+        cross3(gr, x, bw);
+        const double s = kn * d;
+        e += 0.5 * kn * d * d;
+        for (int k = 0; k < 3; ++k) {
+            dE[k] += s * aw[k];
+            dE[3 + k] += s * ga[k];
+            dE[6 + k] += s * bw[k];
+            dE[9 + k] -= s * gr[k];
+        }
+    }
+    free(ids);
+    free(dist);
+    return e;
+}
+
 /* ------------------------------------------------------------------ BDF1 of one moving part */
 
 /* ---- translational joint (3 dof) */

@@ -55,6 +55,11 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
                   const double* E_B, const double* phi_B, const orc_params* prm, int want_deriv, double* fm,
                   double* Km, double* Dm, int* ids);
 
+/* Penetration energy of a pair (sum of kn d^2 / 2 over the active contacts) and its gradient
+ * dE[12] wrt the twists of A then B (w, v each). */
+double orc_pair_energy(const orc_grid* g, const double* pts, int n_pts, const double* E_A, const double* E_B,
+                       const orc_params* prm, double* dE);
+
 /* ---------------------------------------------------------------- one moving body, BDF1 */
 
 /* The moving part of the planner's scene (examples/run_joint_plan.py:140-178): one

@@ -363,3 +363,33 @@ def test_f16_bricks_against_oracle(sdfc, ctx, oracle, workloads, precision):
         f64, _, _, _ = oracle.pair_eval(og64, pts, EA[k], phiA[k], EB[k], phiB[k], op, False)
         assert np.linalg.norm(fm[k] - f64) <= 0.05 * np.linalg.norm(f64)  # FP16 quantisation
     b.close()
+
+
+@pytest.mark.parametrize("precision,bar", [(0, 1e-10), (1, 1e-5)])
+def test_energy_against_oracle(sdfc, ctx, oracle, workloads, precision, bar):
+    """Penetration energy (sdfc_batch_energy) and its twist gradient against the oracle's
+    definition on the same inputs (the oracle's gradient is itself checked against central
+    differences of the energy in the CPU tests)."""
+    rng = np.random.default_rng(31)
+    g = workloads.socket_grid(64, dtype=np.float32)
+    gh = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+    pts = workloads.peg_points(6000, seed=12)
+    ph = ctx.upload_points(pts, 1)
+    n = 6
+    b = ctx.batch([ph] * n, [gh] * n)
+    b.set_precision(precision)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    rel = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.004),
+                                   [0.026 * np.cos(a), 0.026 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
+    EB = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.3), rng.normal(size=3))
+                   for _ in range(n)])
+    EA = EB @ rel
+    prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 2.0, 0.5) for _ in range(n)]
+    e, dE = b.energy(EA, EB, prm)
+    og = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
+    for k in range(n):
+        re, rdE = oracle.pair_energy(og, pts, EA[k], EB[k], oracle.Params(1e5, 1e3, 0.3, 1e3, 2.0, 0.5))
+        assert re > 0
+        assert abs(e[k] - re) <= bar * re, (k, e[k], re)
+        assert np.linalg.norm(dE[k] - rdE) <= bar * np.linalg.norm(rdE), (k, dE[k], rdE)
+    b.close()
