@@ -42,6 +42,14 @@ enum Phase : int { kNewton = 0, kLine = 1, kDone = 2 };
 
 constexpr int kMaxDof = 6;
 
+// Threads per block of the per-scene kernels (Newton update, adjoint step).  Each scene's
+// FP64 work runs on one thread; small blocks spread the scenes over all SMs so that no SM's
+// FP64 pipe carries more than a few of them.
+#ifndef SDFC_SCENE_THREADS
+#define SDFC_SCENE_THREADS 32
+#endif
+constexpr int kSceneThreads = SDFC_SCENE_THREADS;
+
 struct MoverDev {
     double mass, inertia[6], E_pj0[16], E_ji[16], gravity[3], h, Kr, Dr;
     double tol;  // Newton tolerance on |g| (the reference's 1e-8 unless set)
@@ -910,7 +918,8 @@ int enqueue_round(sdfc_sim* s, cudaStream_t st) {
         int rc = sdfc_impl::run_batch(s->batch, in, true, out, st);
         if (rc) return rc;
     }
-    sim_newton_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext, s->d_fm,
+    constexpr int ts = kSceneThreads;
+    sim_newton_kernel<<<(n + ts - 1) / ts, ts, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext, s->d_fm,
                                                        s->d_Km, s->d_Dm, s->d_state, s->d_remaining, s->d_evals);
     return SDFC_OK;
 }
@@ -956,7 +965,8 @@ int capture_backward(sdfc_sim* s) {
         rc = sdfc_impl::run_batch(s->batch, in, true, out, st);
     }
     if (!rc) {
-        adj_step_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
+        constexpr int ts = kSceneThreads;
+        adj_step_kernel<<<(n + ts - 1) / ts, ts, 0, st>>>(n, s->nd, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
                                                          s->d_fm, s->d_Km, s->d_Dm, s->d_qhis, s->d_qd0rec, s->d_dfdq,
                                                          s->energy_on ? s->d_gEhis : nullptr, s->d_dfdE, s->d_t,
                                                          s->d_adj, s->d_gout);

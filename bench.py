@@ -379,6 +379,7 @@ def run_gpu(args, world, rank):
 
     sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 else None
     c5_res = run_c5(args, sdfc, ctx, torch) if args.c5_points > 0 and rank == 0 else None
+    c4_res = run_c4(args, sdfc, ctx, g, torch) if args.c4_instances > 0 and rank == 0 else None
     if sim_res is not None:
         plain = run_sim_plain(args, sdfc, ctx, g, p, n)
         plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
@@ -436,6 +437,8 @@ def run_gpu(args, world, rank):
         line["sim"] = sim_res
     if c5_res is not None:
         line["fp16_bricks"] = c5_res
+    if c4_res is not None:
+        line["differentiable_rollout"] = c4_res
     print(json.dumps(line), flush=True)
 
 
@@ -627,6 +630,67 @@ def run_c5(args, sdfc, ctx, torch):
     return out
 
 
+def run_c4(args, sdfc, ctx, g, torch):
+    """Differentiable rollout: args.c4_instances pegs on free3d-exp joints in the socket, initial
+    pose perturbed (sigma 0.01 translation, sigma 1 degree rotation), pulled along directions in a
+    30 degree cone about +z, args.c4_steps BDF1 steps.  Loss per instance: the steps' summed
+    penetration energy plus |q_T - target|^2 (target: the peg extracted 0.25 along +z).  The
+    gradients wrt the initial pose and the pull direction come from the adjoint
+    (sdfc_sim_backward_energy); the joint trajectory, recorded every step, is the checkpoint from
+    which each step's matrices are recomputed."""
+    n, T = args.c4_instances, args.c4_steps
+    rng = np.random.default_rng(4)
+    pts = W.peg_points(args.c4_points, seed=9)
+    ph = ctx.upload_points(pts, sdfc.STORAGE_F32)
+    dirs = W.cone_directions(n, 30.0, seed=4)
+    m, inertia = W.cylinder_mass_props()
+    mv = sdfc.Mover.make(m, inertia, np.eye(4), SIM_H, SIM_GRAVITY, joint=sdfc.JOINT_FREE3D_EXP)
+    sim = ctx.sim([mv] * n, [sdfc.ScenePair.make(i, ph, g, True, np.eye(4), sdfc.Params(*PARAMS)) for i in range(n)])
+    sim.set_precision(sdfc.PRECISION_MIXED if args.c4_precision == "mixed" else sdfc.PRECISION_FP64)
+    q0 = np.zeros((n, 6))
+    q0[:, :3] = rng.normal(size=(n, 3)) * 0.01
+    q0[:, 3:] = rng.normal(size=(n, 3)) * np.deg2rad(1.0)
+    F = np.zeros((n, 6))
+    F[:, 3:] = SIM_PULL * dirs
+    target = np.array([0.0, 0.0, 0.25, 0.0, 0.0, 0.0])
+    # warm-up (graph capture of the rounds and the reverse step)
+    sim.record_energy(True)
+    sim.set_state(q0, np.zeros((n, 6)))
+    sim.set_external_force(F)
+    sim.record(2)
+    sim.step(2)
+    sim.backward(np.zeros((n, 2, 6)), np.ones(n))
+    sim.record(T)
+    sim.set_state(q0, np.zeros((n, 6)))
+    torch.cuda.synchronize()
+    r0, e0 = sim.stats()
+    t0 = time.perf_counter()
+    conv = sim.step(T)
+    qh = sim.history()
+    _, E = sim.energy()
+    t_fwd = time.perf_counter() - t0
+    r1, e1 = sim.stats()
+    L = E + ((qh[:, T] - target) ** 2).sum(1)
+    df_dq = np.zeros((n, T, 6))
+    df_dq[:, T - 1] = 2.0 * (qh[:, T] - target)
+    t1 = time.perf_counter()
+    g0, gd0, gf = sim.backward(df_dq, np.ones(n))
+    t_bwd = time.perf_counter() - t1
+    r, e = sim.stats()
+    sim.close()
+    g_dir = SIM_PULL * gf[:, 3:]  # F = pull * direction
+    return {"instances": n, "steps": T, "points": args.c4_points, "joint": "free3d-exp",
+            "precision": args.c4_precision, "rounds": r1 - r0, "scene_evaluations": e1 - e0,
+            "converged_last_step": float(np.mean(conv)),
+            "forward_wall_s": t_fwd, "backward_wall_s": t_bwd,
+            "forward_scene_steps_per_s": n * T / t_fwd, "backward_scene_steps_per_s": n * T / t_bwd,
+            "loss_mean": float(L.mean()), "penetration_energy_mean": float(E.mean()),
+            "grad_q0_norm_mean": float(np.linalg.norm(g0, axis=1).mean()),
+            "grad_direction_norm_mean": float(np.linalg.norm(g_dir, axis=1).mean()),
+            "finite": bool(np.isfinite(g0).all() and np.isfinite(gf).all()),
+            "checkpoint": "joint trajectory every step (48 B per scene-step); step matrices recomputed in reverse"}
+
+
 def cpu_sim_rate(pool, n_scenes, steps, procs):
     dirs = W.fibonacci_directions(1024)
     idx = np.linspace(0, len(dirs) - 1, n_scenes).astype(int)
@@ -658,6 +722,11 @@ def main():
     ap.add_argument("--sim-steps", type=int, default=500, help="BDF1 steps of the direction sweep (0: skip)")
     ap.add_argument("--sim-early", type=int, default=25, help="steps also timed alone (compared with the CPU)")
     ap.add_argument("--cpu-sim-scenes", type=int, default=32, help="scenes stepped by the CPU baseline")
+    ap.add_argument("--c4-instances", type=int, default=4096, help="differentiable-rollout leg: instances (0: skip)")
+    ap.add_argument("--c4-steps", type=int, default=200, help="differentiable-rollout leg: BDF1 steps")
+    ap.add_argument("--c4-points", type=int, default=10000, help="differentiable-rollout leg: peg points")
+    ap.add_argument("--c4-precision", choices=("mixed", "fp64"), default="mixed",
+                    help="differentiable-rollout leg: precision of the force evaluations")
     ap.add_argument("--c5-grid", type=int, default=512, help="FP16-brick leg: grid nodes per axis")
     ap.add_argument("--c5-points", type=int, default=1000000, help="FP16-brick leg: points (0: skip the leg)")
     ap.add_argument("--c5-dirs", type=int, default=256, help="FP16-brick leg: pull directions")

@@ -159,8 +159,8 @@ def test_torch_autograd(sdfc):
         q0 = torch.tensor(np.tile(fx["q0"], (n, 1)), requires_grad=True)
         qd0 = torch.tensor(np.tile(fx["qdot0"], (n, 1)), requires_grad=True)
         fe = torch.tensor(np.tile(fx["f_ext"], (n, 1)) * np.array([[1, 1, 1, 1, 0.5, 2]]), requires_grad=True)
-        q = ag.rollout(sim, q0, qd0, fe, T)
-        assert q.shape == (n, T, 3)
+        q, E = ag.rollout(sim, q0, qd0, fe, T)
+        assert q.shape == (n, T, 3) and not E.any()
         loss = (q * w).sum()
         loss.backward()
         g0, gd0, gf = sim.backward(w.numpy())
@@ -168,7 +168,7 @@ def test_torch_autograd(sdfc):
         np.testing.assert_array_equal(qd0.grad.numpy(), gd0)
         np.testing.assert_array_equal(fe.grad.numpy(), gf)
         # a stepped simulation no longer holds the rollout's trajectory
-        q = ag.rollout(sim, q0, qd0, fe, T)
+        q, _ = ag.rollout(sim, q0, qd0, fe, T)
         sim.step(0)
         with pytest.raises(RuntimeError):
             (q * w).sum().backward()

@@ -86,3 +86,27 @@ def test_energy_loss_adjoint_against_central_differences(sdfc):
     fd = (L[1::2] - L[2::2]) / (2 * eps)
     for got, want in ((g0[0], fd[0:6]), (gd0[0], fd[6:12]), (gf[0], fd[12:18])):
         assert np.linalg.norm(got - want) <= 1e-4 * np.linalg.norm(got), (got, want)
+
+
+def test_torch_rollout_with_energy(sdfc):
+    """autograd.rollout's energy output backpropagates through sdfc_sim_backward_energy."""
+    torch = pytest.importorskip("torch")
+    ag = submodule("autograd")
+    fx = load("sim_free.npz")
+    T, n = 5, 2
+    ctx = sdfc.Context(0)
+    try:
+        sim = make_sim(sdfc, ctx, fx, n=n, joint=sdfc.JOINT_FREE3D_EXP)
+        q0 = torch.tensor(np.tile(fx["q0"], (n, 1)), requires_grad=True)
+        qd0 = torch.tensor(np.tile(fx["qdot0"], (n, 1)), requires_grad=True)
+        fe = torch.tensor(np.tile(fx["f_ext"], (n, 1)), requires_grad=True)
+        q, E = ag.rollout(sim, q0, qd0, fe, T, energy=True)
+        assert (E > 0).all()
+        (E.sum() + (q[:, -1] ** 2).sum()).backward()
+        df_dq = np.zeros((n, T, 6))
+        df_dq[:, -1] = 2.0 * q[:, -1].detach().numpy()
+        g0, gd0, gf = sim.backward(df_dq, np.ones(n))
+        np.testing.assert_array_equal(q0.grad.numpy(), g0)
+        np.testing.assert_array_equal(fe.grad.numpy(), gf)
+    finally:
+        ctx.close()
