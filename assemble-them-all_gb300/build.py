@@ -40,6 +40,11 @@ def _flags():
     return f
 
 
+# Per-file flags.  The level-set builder reproduces the reference's FP32 distances bit for bit;
+# the reference is compiled without contraction, so no multiply-add may be fused there.
+FILE_FLAGS = {"sdfc_levelset.cu": ["-fmad=false"]}
+
+
 def _stale(target, deps):
     if not os.path.exists(target):
         return True
@@ -57,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(OUT_DIR, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc()] + _flags() + ["-c", s, "-o", o])
+            jobs.append([nvcc()] + _flags() + FILE_FLAGS.get(os.path.basename(s), []) + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

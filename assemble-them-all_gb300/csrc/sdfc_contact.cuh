@@ -201,12 +201,18 @@ __device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, in
     return __ldg(g.v64 + (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k));
 }
 
+// FP16-brick corners, kept out of line so that the FP32 cell-corner path of the hot
+// kernels stays small.
+__device__ __noinline__ static void brick_corners32(const GridDesc& g, int i, int j, int k, float* c) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) c[q] = brick_value32(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+}
+
 // The 8 corner values of cell (i, j, k), ordered c000, c100, c010, c110, c001, c101,
 // c011, c111: FP32 (from the cell-corner array or the bricks) and FP64.
 __device__ __forceinline__ void cell_corners32(const GridDesc& g, int i, int j, int k, float* c) {
     if (g.b16) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) c[q] = brick_value32(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+        brick_corners32(g, i, j, k, c);
         return;
     }
     const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));

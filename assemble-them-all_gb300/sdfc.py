@@ -30,7 +30,7 @@ EXPORTS = (
     "sdfc_sim_step", "sdfc_sim_stats", "sdfc_sim_record", "sdfc_sim_history", "sdfc_sim_backward",
     "sdfc_grid_values", "sdfc_f16_brick_encode", "sdfc_f16_brick_decode", "sdfc_batch_energy",
     "sdfc_batch_energy_device", "sdfc_sim_record_energy", "sdfc_sim_energy", "sdfc_sim_backward_energy",
-    "sdfc_sim_set_tolerance",
+    "sdfc_sim_set_tolerance", "sdfc_make_level_set3", "sdfc_make_level_set3_device", "sdfc_sdf_grid_layout",
 )
 JOINT_TRANSLATIONAL = 3
 JOINT_FREE3D_EXP = 6
@@ -140,6 +140,10 @@ def lib():
                                             v, v]
         L.sdfc_batch_set_precision.argtypes = [v, i]
         L.sdfc_batch_last_timing.argtypes = [v, P(ctypes.c_float)]
+        f, f32 = P(ctypes.c_float), ctypes.c_float
+        L.sdfc_make_level_set3.argtypes = [v, f, i, P(ctypes.c_uint), i, f, f32, f32, f32, i, i, i, i, f]
+        L.sdfc_make_level_set3_device.argtypes = [v, v, i, v, i, f, f32, f32, f32, i, i, i, i, v, v]
+        L.sdfc_sdf_grid_layout.argtypes = [d, i, ctypes.c_double, i, P(i), d, d, d, f]
         _lib = L
     return _lib
 
@@ -240,6 +244,53 @@ class Context:
     def set_precision(self, precision: int):
         """PRECISION_FP64 or PRECISION_MIXED for sdfc_evaluate and later batches."""
         self._check(lib().sdfc_set_precision(self._h, int(precision)), "sdfc_set_precision")
+
+    def make_level_set3(self, verts, tris, origin, dx, shape, exact_band=1) -> np.ndarray:
+        """sdfgen::make_level_set3 on the GPU (sdfc_make_level_set3): phi (nk, nj, ni) float32 of
+        the closed mesh (verts (nv, 3) float32, tris (nt, 3)) on the grid with node (i, j, k) at
+        origin + (i dx, j dy, k dz), shape = (ni, nj, nk)."""
+        V = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        T = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+        o = np.ascontiguousarray(origin, np.float32).reshape(3)
+        d = np.broadcast_to(np.asarray(dx, np.float32), (3,))
+        ni, nj, nk = (int(x) for x in shape)
+        phi = np.empty((nk, nj, ni), np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(lib().sdfc_make_level_set3(self._h, V.ctypes.data_as(fp), len(V),
+                                               T.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), len(T),
+                                               o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni, nj,
+                                               nk, int(exact_band), phi.ctypes.data_as(fp)), "sdfc_make_level_set3")
+        return phi
+
+    def make_level_set3_device(self, verts, tris, origin, dx, shape, exact_band=1, stream=None):
+        """sdfc_make_level_set3_device on torch CUDA tensors: verts (nv, 3) float32, tris (nt, 3)
+        int32 (read as unsigned); returns phi (nk, nj, ni) float32 on the same device, queued on
+        `stream` (default: torch's current stream)."""
+        import torch
+        V = verts.contiguous()
+        T = tris.contiguous()
+        if V.dtype != torch.float32 or T.dtype != torch.int32 or not V.is_cuda or not T.is_cuda:
+            raise ValueError("verts: CUDA float32 (nv, 3); tris: CUDA int32 (nt, 3)")
+        o = np.ascontiguousarray(origin, np.float32).reshape(3)
+        d = np.broadcast_to(np.asarray(dx, np.float32), (3,))
+        ni, nj, nk = (int(x) for x in shape)
+        phi = torch.empty((nk, nj, ni), dtype=torch.float32, device=V.device)
+        st = (stream or torch.cuda.current_stream(V.device)).cuda_stream
+        fp = ctypes.POINTER(ctypes.c_float)
+        self._check(lib().sdfc_make_level_set3_device(self._h, V.data_ptr(), V.shape[0], T.data_ptr(), T.shape[0],
+                                                      o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni,
+                                                      nj, nk, int(exact_band), phi.data_ptr(), st),
+                    "sdfc_make_level_set3_device")
+        return phi
+
+    def precompute_sdf(self, V, F, dx, res):
+        """BodySDFObj::precompute_SDF (simulation/redmax/Body/BodySDFObj.cpp:38-84) with the level set
+        built on the GPU: the body-frame mesh (V (nv, 3), F (nt, 3)) with the body's dx and res ->
+        (values (nk, nj, ni) float64, min_box, max_box, spacing), the arguments of upload_grid."""
+        shape, min_box, max_box, spacing, origin = sdf_grid_layout(V, dx, res)
+        phi = self.make_level_set3(np.asarray(V, np.float64).astype(np.float32), F, origin,
+                                   spacing.astype(np.float32), shape)
+        return phi.astype(np.float64), min_box, max_box, spacing
 
     def batch(self, points, grids) -> "Batch":
         return Batch(self, points, grids)
@@ -467,3 +518,17 @@ def f16_brick_decode(codes, so, shape):
     if rc != SDFC_OK:
         raise SdfcError(f"sdfc_f16_brick_decode failed ({rc})")
     return out
+
+
+def sdf_grid_layout(V, dx, res):
+    """sdfc_sdf_grid_layout (host only): BodySDFObj::precompute_SDF's grid for the body-frame
+    vertices V (nv, 3) -> (shape (ni, nj, nk), min_box, max_box, spacing, origin float32)."""
+    v = _f64(V).reshape(-1, 3)
+    shape = (ctypes.c_int * 3)()
+    mn, mx, sp = np.zeros(3), np.zeros(3), np.zeros(3)
+    org = np.zeros(3, np.float32)
+    rc = lib().sdfc_sdf_grid_layout(_dp(v), len(v), float(dx), int(res), shape, _dp(mn), _dp(mx), _dp(sp),
+                                    org.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_grid_layout failed ({rc})")
+    return tuple(shape), mn, mx, sp, org

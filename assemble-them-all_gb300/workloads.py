@@ -333,3 +333,72 @@ def procedural_assembly(seed: int, n_parts: int = None, points=(2000, 200000), g
     d = np.zeros(3)
     d[axis] = 1.0 if g.uniform() < 0.5 else -1.0
     return Assembly(parts, n_pts, grid_n, mover, d)
+
+
+# ----------------------------------------------------------------------------- triangle meshes
+# Closed triangle meshes for building SDF grids (BodySDFObj::precompute_SDF): the parts of an
+# assembly arrive as OBJ meshes; these procedural ones stand in for them.  Vertices (nv, 3)
+# float64, faces (nt, 3) int32, outward-facing.
+
+def box_mesh(half=(0.5, 0.5, 0.5), center=(0.0, 0.0, 0.0)):
+    h = np.asarray(half, float)
+    c = np.asarray(center, float)
+    V = np.array([[sx, sy, sz] for sz in (-1, 1) for sy in (-1, 1) for sx in (-1, 1)], float) * h + c
+    F = np.array([[0, 2, 1], [1, 2, 3], [4, 5, 6], [5, 7, 6], [0, 1, 4], [1, 5, 4],
+                  [2, 6, 3], [3, 6, 7], [0, 4, 2], [2, 4, 6], [1, 3, 5], [3, 7, 5]], np.int32)
+    return V, F
+
+
+def cylinder_mesh(radius=0.4, half_len=0.5, segments=24):
+    """A z-axis cylinder: `segments` side quads and two fans."""
+    n = segments
+    t = 2 * np.pi * np.arange(n) / n
+    ring = np.stack([radius * np.cos(t), radius * np.sin(t)], 1)
+    V = np.concatenate([np.c_[ring, np.full(n, -half_len)], np.c_[ring, np.full(n, half_len)],
+                        [[0, 0, -half_len], [0, 0, half_len]]])
+    F = []
+    for a in range(n):
+        b = (a + 1) % n
+        F += [(a, b, n + b), (a, n + b, n + a), (2 * n, b, a), (2 * n + 1, n + a, n + b)]
+    return V, np.array(F, np.int32)
+
+
+def torus_mesh(R=0.6, r=0.25, n=32, m=16):
+    """A torus about z: n segments around the axis, m around the tube."""
+    u = 2 * np.pi * np.arange(n) / n
+    v = 2 * np.pi * np.arange(m) / m
+    U, Vv = np.meshgrid(u, v, indexing="ij")
+    V = np.stack([(R + r * np.cos(Vv)) * np.cos(U), (R + r * np.cos(Vv)) * np.sin(U), r * np.sin(Vv)], -1)
+    F = []
+    for a in range(n):
+        for b in range(m):
+            i, j = a * m + b, ((a + 1) % n) * m + b
+            k, l = ((a + 1) % n) * m + (b + 1) % m, a * m + (b + 1) % m
+            F += [(i, j, k), (i, k, l)]
+    return V.reshape(-1, 3), np.array(F, np.int32)
+
+
+def socket_mesh(outer=1.0, inner=0.5, half_len=1.0):
+    """A square socket: the box [-outer, outer]^2 x [-half_len, half_len] minus a square z-bore
+    of half-width `inner` (32 large triangles)."""
+    sq = np.array([[-1, -1], [1, -1], [1, 1], [-1, 1]], float)
+    rings = [np.c_[sq * s, np.full(4, z)] for s in (outer, inner) for z in (-half_len, half_len)]
+    V = np.concatenate(rings)  # outer bottom 0-3, outer top 4-7, inner bottom 8-11, inner top 12-15
+    F = []
+    for c in range(4):
+        d = (c + 1) % 4
+        F += [(c, d, 4 + d), (c, 4 + d, 4 + c)]                  # outer side
+        F += [(8 + d, 8 + c, 12 + c), (8 + d, 12 + c, 12 + d)]    # bore side
+        F += [(4 + c, 4 + d, 12 + d), (4 + c, 12 + d, 12 + c)]    # top ring
+        F += [(d, c, 8 + c), (d, 8 + c, 8 + d)]                   # bottom ring
+    return V, np.array(F, np.int32)
+
+
+def level_set_grid(V, dx, pad=2):
+    """A grid covering the mesh with `pad` cells of margin: (origin float32, shape (ni, nj, nk))."""
+    V = np.asarray(V, np.float32)
+    h = np.float32(dx)
+    lo, hi = V.min(0), V.max(0)
+    origin = (lo - pad * h).astype(np.float32)
+    shape = tuple(int(np.ceil((hi[a] - lo[a]) / h)) + 2 * pad + 1 for a in range(3))
+    return origin, shape

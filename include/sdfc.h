@@ -338,6 +338,30 @@ int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, int nk, con
                           const double* params, int want_deriv, double* fm, double* Km, double* Dm, int* n_active,
                           void* stream);
 
+/* ---------------------------------------------------------------- SDF grids from meshes */
+
+/* sdfgen::make_level_set3 (simulation/externals/sdfgen/makelevelset3.h:14-16,
+ * makelevelset3.cpp:161-227) on the GPU: the signed distance phi of the closed triangle
+ * mesh (verts: nv x 3 floats; tris: nt x 3 vertex indices) at the nodes origin + (i dx,
+ * j dy, k dz), phi[i + ni*(j + nj*k)], exact distances within exact_band cells of the
+ * mesh, fast sweeping elsewhere, negative inside (crossing parity along +i).
+ * Bit-identical to the reference's FP32 result.  Host arrays in and out. */
+int sdfc_make_level_set3(sdfc_context* ctx, const float* verts, int nv, const unsigned* tris, int nt,
+                         const float origin[3], float dx, float dy, float dz, int ni, int nj, int nk, int exact_band,
+                         float* phi);
+/* The same from device arrays (d_tris entries must be < nv: not checked here), on
+ * `stream` (null: the context's stream); returns after the work is queued. */
+int sdfc_make_level_set3_device(sdfc_context* ctx, const float* d_verts, int nv, const unsigned* d_tris, int nt,
+                                const float origin[3], float dx, float dy, float dz, int ni, int nj, int nk,
+                                int exact_band, float* d_phi, void* stream);
+/* The grid of BodySDFObj::precompute_SDF (simulation/redmax/Body/BodySDFObj.cpp:38-70) for the
+ * body-frame mesh vertices V (nv x 3 doubles, the body's _V) with the body's dx and res:
+ * node counts shape = (ni, nj, nk), _min_box, _max_box, the spacing (_dx, _dy, _dz), and
+ * (if origin_f is not null) the FP32 origin and spacing handed to make_level_set3 are
+ * origin_f and (float)spacing.  Host-only arithmetic in the reference's order. */
+int sdfc_sdf_grid_layout(const double* V, int nv, double dx, int res, int shape[3], double min_box[3],
+                         double max_box[3], double spacing[3], float origin_f[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -345,3 +345,25 @@ def pair_energy(grid: Grid, pts, E_A, E_B, params: Params):
     prm = params._c()
     e = L.orc_pair_energy(ctypes.byref(g), _dp(p), len(p), _dp(_f64(E_A)), _dp(_f64(E_B)), ctypes.byref(prm), _dp(dE))
     return e, dE
+
+
+def make_level_set3(verts, tris, origin, dx, shape, exact_band=1) -> np.ndarray:
+    """sdfgen::make_level_set3 (simulation/externals/sdfgen/makelevelset3.cpp:161-227):
+    phi[k, j, i] of the closed mesh (verts (nv, 3), tris (nt, 3)) on the grid with
+    node (i, j, k) at origin + (i dx, j dy, k dz), shape = (ni, nj, nk)."""
+    L = lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.orc_make_level_set3.restype = None
+    L.orc_make_level_set3.argtypes = [fp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint), ctypes.c_int, fp,
+                                      ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, fp]
+    V = np.ascontiguousarray(verts, np.float32)
+    T = np.ascontiguousarray(tris, np.uint32)
+    o = np.ascontiguousarray(origin, np.float32)
+    d = np.broadcast_to(np.asarray(dx, np.float32), (3,))
+    ni, nj, nk = (int(s) for s in shape)
+    phi = np.empty((nk, nj, ni), np.float32)
+    L.orc_make_level_set3(V.ctypes.data_as(fp), len(V), T.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), len(T),
+                          o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni, nj, nk, int(exact_band),
+                          phi.ctypes.data_as(fp))
+    return phi

@@ -17,6 +17,7 @@
 #include "Force/ForceGeneralSDFContact.h"
 #include "CollisionDetection/CollisionDetection.h"
 #include "CollisionDetection/Contact.h"
+#include "makelevelset3.h"
 
 using namespace redmax;
 
@@ -144,6 +145,24 @@ int ref_body_get_sdf_shape(void* sim, const char* name, int* nijk, double* min_b
     dxyz[1] = b->_dy;
     dxyz[2] = b->_dz;
     *col_th = b->_col_th;
+    return 0;
+}
+
+// The body-frame mesh BodySDFObj::precompute_SDF was given (BodyMeshObj::_V, _F): sizes when
+// V or F is null, else copies (V: nv x 3, F: nt x 3).
+int ref_body_mesh(void* sim, const char* name, int* nv, int* nt, double* V, int* F) {
+    auto* b = dynamic_cast<BodySDFObj*>(body_of(sim, name));
+    if (!b) return -1;
+    const Matrix3X Vb = b->get_vertices();
+    const Matrix3Xi Fb = b->get_faces();
+    *nv = (int)Vb.cols();
+    *nt = (int)Fb.cols();
+    if (V && F) {
+        for (int c = 0; c < Vb.cols(); ++c)
+            for (int r = 0; r < 3; ++r) V[3 * c + r] = Vb(r, c);
+        for (int c = 0; c < Fb.cols(); ++c)
+            for (int r = 0; r < 3; ++r) F[3 * c + r] = Fb(r, c);
+    }
     return 0;
 }
 
@@ -343,6 +362,25 @@ int ref_sim_backward(void* sim, const double* df_dq, int T, double* df_dq0, doub
         df_dq0[i] = s->_backward_results._df_dq0(i);
         df_dqdot0[i] = s->_backward_results._df_dqdot0(i);
     }
+    return 0;
+    HARNESS_CATCH
+}
+
+/* sdfgen::make_level_set3 as the reference builds its grids (BodySDFObj::precompute_SDF):
+ * phi (ni*nj*nk floats, i fastest). */
+int ref_make_level_set3(const float* verts, int nv, const unsigned* tris, int nt, const float* origin, float dx,
+                        float dy, float dz, int ni, int nj, int nk, int exact_band, float* phi) {
+    HARNESS_TRY
+    std::vector<sdfgen::Vec3f> x(nv);
+    for (int k = 0; k < nv; ++k) x[k] = sdfgen::Vec3f(verts[3 * k], verts[3 * k + 1], verts[3 * k + 2]);
+    std::vector<sdfgen::Vec3ui> t(nt);
+    for (int k = 0; k < nt; ++k) t[k] = sdfgen::Vec3ui(tris[3 * k], tris[3 * k + 1], tris[3 * k + 2]);
+    sdfgen::Array3f out;
+    sdfgen::make_level_set3(t, x, sdfgen::Vec3f(origin[0], origin[1], origin[2]), dx, dy, dz, ni, nj, nk, out,
+                            exact_band);
+    for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < ni; ++i) phi[i + ni * (j + nj * k)] = out(i, j, k);
     return 0;
     HARNESS_CATCH
 }

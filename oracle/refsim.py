@@ -66,6 +66,10 @@ def lib():
         L.ref_sim_is_converged.argtypes = [v]
         L.ref_sim_get_state.argtypes = [v, d, d]
         L.ref_sim_backward.argtypes = [v, d, i, d, d]
+        L.ref_body_mesh.argtypes = [v, c, ctypes.POINTER(i), ctypes.POINTER(i), d, ctypes.POINTER(i)]
+        f = ctypes.POINTER(ctypes.c_float)
+        L.ref_make_level_set3.argtypes = [f, i, ctypes.POINTER(ctypes.c_uint), i, f, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_float, i, i, i, i, f]
         _lib = L
     return _lib
 
@@ -194,6 +198,16 @@ class RefSim:
         lib().ref_body_get_sdf_values(self._h, name.encode(), _dp(v))
         return v, mn, mx, dx, float(ct[0])
 
+    def mesh(self, name):
+        """The body-frame vertices (nv, 3) and faces (nt, 3) the body's SDF was built from."""
+        nv, nt = ctypes.c_int(), ctypes.c_int()
+        _check(lib().ref_body_mesh(self._h, name.encode(), ctypes.byref(nv), ctypes.byref(nt), None, None), "mesh")
+        V = np.zeros((nv.value, 3))
+        F = np.zeros((nt.value, 3), np.int32)
+        _check(lib().ref_body_mesh(self._h, name.encode(), ctypes.byref(nv), ctypes.byref(nt), _dp(V),
+                                   F.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), "mesh")
+        return V, F
+
     def set_pose(self, name, E, phi):
         _check(lib().ref_body_set_pose(self._h, name.encode(), _dp(_f64(E)), _dp(_f64(phi))), "set_pose")
 
@@ -259,3 +273,19 @@ def make_pair_sim(joint_a="free3d-exp", half_a=(0.3, 0.3, 0.3), half_b=(0.5, 0.5
     write_obj(os.path.join(workdir, "b.obj"), Vb, Fb)
     xml = two_body_xml("a.obj", "b.obj", joint_a=joint_a, **kw)
     return RefSim(xml, workdir), workdir
+
+
+def make_level_set3(verts, tris, origin, dx, shape, exact_band=1) -> np.ndarray:
+    """The reference's own sdfgen::make_level_set3 (FP32 inputs, phi[k, j, i])."""
+    L = lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    V = np.ascontiguousarray(verts, np.float32)
+    T = np.ascontiguousarray(tris, np.uint32)
+    o = np.ascontiguousarray(origin, np.float32)
+    d = np.broadcast_to(np.asarray(dx, np.float32), (3,))
+    ni, nj, nk = (int(s) for s in shape)
+    phi = np.empty((nk, nj, ni), np.float32)
+    _check(L.ref_make_level_set3(V.ctypes.data_as(fp), len(V), T.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
+                                 len(T), o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni, nj, nk,
+                                 int(exact_band), phi.ctypes.data_as(fp)), "make_level_set3")
+    return phi

@@ -1747,3 +1747,202 @@ void orc_bdf1_backward(const orc_mover* m, const orc_pair* pairs, int n_pairs, c
     free(Js);
     free(Rs);
 }
+
+/* ------------------------------------------------------------------ mesh -> SDF grid */
+
+/* sdfgen::make_level_set3 (simulation/externals/sdfgen/makelevelset3.cpp:161-227), the grid
+ * builder of BodySDFObj::precompute_SDF (rm/Body/BodySDFObj.cpp:38-84), in FP32 with its operation
+ * order (vec.h: sums in index order; compiled without contraction).  Sequential, like the
+ * reference; the GPU runs the same arithmetic with the sweeps as diagonal wavefronts. */
+typedef struct {
+    float v[3];
+} ov3;
+
+static ov3 ov_sub(ov3 a, ov3 b) {
+    ov3 r = {{a.v[0] - b.v[0], a.v[1] - b.v[1], a.v[2] - b.v[2]}};
+    return r;
+}
+static ov3 ov_scale(float s, ov3 a) {
+    ov3 r = {{s * a.v[0], s * a.v[1], s * a.v[2]}};
+    return r;
+}
+static ov3 ov_add(ov3 a, ov3 b) {
+    ov3 r = {{a.v[0] + b.v[0], a.v[1] + b.v[1], a.v[2] + b.v[2]}};
+    return r;
+}
+static float ov_dot(ov3 a, ov3 b) {
+    float d = a.v[0] * b.v[0];
+    d += a.v[1] * b.v[1];
+    d += a.v[2] * b.v[2];
+    return d;
+}
+static float ov_mag2(ov3 a) { return ov_dot(a, a); }
+static float ov_dist(ov3 a, ov3 b) {
+    float d = (a.v[0] - b.v[0]) * (a.v[0] - b.v[0]);
+    d += (a.v[1] - b.v[1]) * (a.v[1] - b.v[1]);
+    d += (a.v[2] - b.v[2]) * (a.v[2] - b.v[2]);
+    return sqrtf(d);
+}
+static float ofmin(float a, float b) { return b < a ? b : a; }  /* std::min */
+
+static float seg_dist(ov3 x0, ov3 x1, ov3 x2) { /* point_segment_distance */
+    ov3 dx = ov_sub(x2, x1);
+    double m2 = (double)ov_mag2(dx);
+    float s12 = (float)((double)ov_dot(ov_sub(x2, x0), dx) / m2);
+    if (s12 < 0)
+        s12 = 0;
+    else if (s12 > 1)
+        s12 = 1;
+    return ov_dist(x0, ov_add(ov_scale(s12, x1), ov_scale(1 - s12, x2)));
+}
+
+static float tri_dist(ov3 x0, ov3 x1, ov3 x2, ov3 x3) { /* point_triangle_distance */
+    ov3 x13 = ov_sub(x1, x3), x23 = ov_sub(x2, x3), x03 = ov_sub(x0, x3);
+    float m13 = ov_mag2(x13), m23 = ov_mag2(x23), d = ov_dot(x13, x23);
+    float den = m13 * m23 - d * d;
+    float invdet = 1.f / (den < 1e-30f ? 1e-30f : den); /* max(den, 1e-30f) */
+    float a = ov_dot(x13, x03), b = ov_dot(x23, x03);
+    float w23 = invdet * (m23 * a - d * b);
+    float w31 = invdet * (m13 * b - d * a);
+    float w12 = 1 - w23 - w31;
+    if (w23 >= 0 && w31 >= 0 && w12 >= 0)
+        return ov_dist(x0, ov_add(ov_add(ov_scale(w23, x1), ov_scale(w31, x2)), ov_scale(w12, x3)));
+    if (w23 > 0) return ofmin(seg_dist(x0, x1, x2), seg_dist(x0, x1, x3));
+    if (w31 > 0) return ofmin(seg_dist(x0, x1, x2), seg_dist(x0, x2, x3));
+    return ofmin(seg_dist(x0, x1, x3), seg_dist(x0, x2, x3));
+}
+
+static int orient2(double x1, double y1, double x2, double y2, double* area) { /* orientation, SOS */
+    *area = y1 * x2 - x1 * y2;
+    if (*area > 0) return 1;
+    if (*area < 0) return -1;
+    if (y2 > y1) return 1;
+    if (y2 < y1) return -1;
+    if (x1 > x2) return 1;
+    if (x1 < x2) return -1;
+    return 0;
+}
+
+static int in_tri_2d(double x0, double y0, double x1, double y1, double x2, double y2, double x3, double y3,
+                     double* a, double* b, double* c) { /* point_in_triangle_2d */
+    x1 -= x0; x2 -= x0; x3 -= x0;
+    y1 -= y0; y2 -= y0; y3 -= y0;
+    int sa = orient2(x2, y2, x3, y3, a);
+    if (sa == 0) return 0;
+    int sb = orient2(x3, y3, x1, y1, b);
+    if (sb != sa) return 0;
+    int sc = orient2(x1, y1, x2, y2, c);
+    if (sc != sa) return 0;
+    double sum = *a + *b + *c;
+    *a /= sum;
+    *b /= sum;
+    *c /= sum;
+    return 1;
+}
+
+static int oclampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
+/* sdfgen::min / max of three: min(a1, min(a2, a3)) with std::min(a, b) = b < a ? b : a and
+ * std::max(a, b) = a < b ? b : a */
+static double omin3(double a, double b, double c) { double m = c < b ? c : b; return m < a ? m : a; }
+static double omax3(double a, double b, double c) { double m = b < c ? c : b; return a < m ? m : a; }
+
+void orc_make_level_set3(const float* verts, int nv, const unsigned* tris, int nt, const float* origin, float dx,
+                         float dy, float dz, int ni, int nj, int nk, int band, float* phi) {
+    (void)nv;
+    const size_t n = (size_t)ni * nj * nk;
+    int* closest = (int*)malloc(sizeof(int) * n);
+    int* count = (int*)calloc(n, sizeof(int));
+    const float init = (float)(ni + nj + nk) * (dx + dy + dz);
+#define OIX(i, j, k) ((size_t)(i) + (size_t)ni * ((size_t)(j) + (size_t)nj * (size_t)(k)))
+    for (size_t q = 0; q < n; ++q) {
+        phi[q] = init;
+        closest[q] = -1;
+    }
+    ov3 o = {{origin[0], origin[1], origin[2]}};
+    for (int t = 0; t < nt; ++t) {
+        unsigned p = tris[3 * t], q = tris[3 * t + 1], r = tris[3 * t + 2];
+        ov3 xp = {{verts[3 * p], verts[3 * p + 1], verts[3 * p + 2]}};
+        ov3 xq = {{verts[3 * q], verts[3 * q + 1], verts[3 * q + 2]}};
+        ov3 xr = {{verts[3 * r], verts[3 * r + 1], verts[3 * r + 2]}};
+        double fip = ((double)xp.v[0] - o.v[0]) / dx, fjp = ((double)xp.v[1] - o.v[1]) / dy,
+               fkp = ((double)xp.v[2] - o.v[2]) / dz;
+        double fiq = ((double)xq.v[0] - o.v[0]) / dx, fjq = ((double)xq.v[1] - o.v[1]) / dy,
+               fkq = ((double)xq.v[2] - o.v[2]) / dz;
+        double fir = ((double)xr.v[0] - o.v[0]) / dx, fjr = ((double)xr.v[1] - o.v[1]) / dy,
+               fkr = ((double)xr.v[2] - o.v[2]) / dz;
+        int i0 = oclampi((int)omin3(fip, fiq, fir) - band, 0, ni - 1),
+            i1 = oclampi((int)omax3(fip, fiq, fir) + band + 1, 0, ni - 1);
+        int j0 = oclampi((int)omin3(fjp, fjq, fjr) - band, 0, nj - 1),
+            j1 = oclampi((int)omax3(fjp, fjq, fjr) + band + 1, 0, nj - 1);
+        int k0 = oclampi((int)omin3(fkp, fkq, fkr) - band, 0, nk - 1),
+            k1 = oclampi((int)omax3(fkp, fkq, fkr) + band + 1, 0, nk - 1);
+        for (int k = k0; k <= k1; ++k)
+            for (int j = j0; j <= j1; ++j)
+                for (int i = i0; i <= i1; ++i) {
+                    ov3 gx = {{(float)i * dx + o.v[0], (float)j * dy + o.v[1], (float)k * dz + o.v[2]}};
+                    float d = tri_dist(gx, xp, xq, xr);
+                    if (d < phi[OIX(i, j, k)]) {
+                        phi[OIX(i, j, k)] = d;
+                        closest[OIX(i, j, k)] = t;
+                    }
+                }
+        j0 = oclampi((int)ceil(omin3(fjp, fjq, fjr)), 0, nj - 1);
+        j1 = oclampi((int)floor(omax3(fjp, fjq, fjr)), 0, nj - 1);
+        k0 = oclampi((int)ceil(omin3(fkp, fkq, fkr)), 0, nk - 1);
+        k1 = oclampi((int)floor(omax3(fkp, fkq, fkr)), 0, nk - 1);
+        for (int k = k0; k <= k1; ++k)
+            for (int j = j0; j <= j1; ++j) {
+                double a, b, c;
+                if (in_tri_2d(j, k, fjp, fkp, fjq, fkq, fjr, fkr, &a, &b, &c)) {
+                    double fi = a * fip + b * fiq + c * fir;
+                    int iv = (int)ceil(fi);
+                    if (iv < 0)
+                        ++count[OIX(0, j, k)];
+                    else if (iv < ni)
+                        ++count[OIX(iv, j, k)];
+                }
+            }
+    }
+    static const int dirs[8][3] = {{1, 1, 1}, {-1, -1, -1}, {1, 1, -1}, {-1, -1, 1},
+                                   {1, -1, 1}, {-1, 1, -1}, {1, -1, -1}, {-1, 1, 1}};
+    for (int pass = 0; pass < 2; ++pass)
+        for (int s = 0; s < 8; ++s) {
+            const int di = dirs[s][0], dj = dirs[s][1], dk = dirs[s][2];
+            const int ia = di > 0 ? 1 : ni - 2, ib = di > 0 ? ni : -1;
+            const int ja = dj > 0 ? 1 : nj - 2, jb = dj > 0 ? nj : -1;
+            const int ka = dk > 0 ? 1 : nk - 2, kb = dk > 0 ? nk : -1;
+            for (int k = ka; k != kb; k += dk)
+                for (int j = ja; j != jb; j += dj)
+                    for (int i = ia; i != ib; i += di) {
+                        ov3 gx = {{(float)i * dx + o.v[0], (float)j * dy + o.v[1], (float)k * dz + o.v[2]}};
+                        const int nb[7][3] = {{i - di, j, k},      {i, j - dj, k},      {i - di, j - dj, k},
+                                              {i, j, k - dk},      {i - di, j, k - dk}, {i, j - dj, k - dk},
+                                              {i - di, j - dj, k - dk}};
+                        for (int m = 0; m < 7; ++m) { /* check_neighbour */
+                            const int ct = closest[OIX(nb[m][0], nb[m][1], nb[m][2])];
+                            if (ct >= 0) {
+                                unsigned p = tris[3 * ct], q = tris[3 * ct + 1], r = tris[3 * ct + 2];
+                                ov3 xp = {{verts[3 * p], verts[3 * p + 1], verts[3 * p + 2]}};
+                                ov3 xq = {{verts[3 * q], verts[3 * q + 1], verts[3 * q + 2]}};
+                                ov3 xr = {{verts[3 * r], verts[3 * r + 1], verts[3 * r + 2]}};
+                                float d = tri_dist(gx, xp, xq, xr);
+                                if (d < phi[OIX(i, j, k)]) {
+                                    phi[OIX(i, j, k)] = d;
+                                    closest[OIX(i, j, k)] = ct;
+                                }
+                            }
+                        }
+                    }
+        }
+    for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < nj; ++j) {
+            int total = 0;
+            for (int i = 0; i < ni; ++i) {
+                total += count[OIX(i, j, k)];
+                if (total % 2 == 1) phi[OIX(i, j, k)] = -phi[OIX(i, j, k)];
+            }
+        }
+#undef OIX
+    free(closest);
+    free(count);
+}

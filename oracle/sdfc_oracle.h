@@ -60,6 +60,11 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
 double orc_pair_energy(const orc_grid* g, const double* pts, int n_pts, const double* E_A, const double* E_B,
                        const orc_params* prm, double* dE);
 
+/* sdfgen::make_level_set3: the signed distance grid phi (ni*nj*nk floats, i fastest) of a closed
+ * triangle mesh (verts: nv x 3 floats, tris: nt x 3 indices), grid origin and spacing, exact band. */
+void orc_make_level_set3(const float* verts, int nv, const unsigned* tris, int nt, const float* origin, float dx,
+                         float dy, float dz, int ni, int nj, int nk, int band, float* phi);
+
 /* ---------------------------------------------------------------- one moving body, BDF1 */
 
 /* The moving part of the planner's scene (examples/run_joint_plan.py:140-178): one
