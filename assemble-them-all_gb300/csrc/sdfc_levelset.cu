@@ -13,14 +13,16 @@
 //              node keeps min over the packed key (distance bits << 32 | triangle): a
 //              non-negative float's bits order like the float.  The same triangles count
 //              their crossings of the grid's +i rays (one atomic add per crossing; sums are
-//              order-free).  Work is cut into chunks of kLsChunk pairs so that one large
-//              triangle spreads over many CTAs.
+//              order-free).  Work is cut into chunks of kLsChunk pairs, one warp each, so
+//              that one large triangle spreads over many warps and small ones fill theirs.
 //   sweeps     two passes of eight fast-sweeping orders.  In one order the node (i, j, k)
 //              reads the closest triangle of its seven upwind neighbours, all of which come
-//              earlier in the reference's loop and lie on lower diagonals a + b + c of the
-//              sweep-relative indices (a, b, c).  One launch per diagonal runs every node of
-//              it in parallel; each node sees exactly the neighbour values the sequential
-//              loop would have shown it, so the result is the sequential one.
+//              earlier in the reference's loop.  One cooperative launch per order: a CTA per
+//              k-plane walks the plane's diagonals, each diagonal's nodes in parallel, and
+//              starts a diagonal only once the plane before it has passed that diagonal (a
+//              bounded wait on a progress counter).  Each node sees exactly the neighbour
+//              values the sequential loop would have shown it, so the result is the
+//              sequential one.
 //   sign       per grid row (j, k) the running crossing count's parity flips the sign
 //              (one warp per row, parity prefix by ballot).
 //
@@ -32,7 +34,9 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <climits>
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -41,8 +45,10 @@
 
 namespace {
 
-constexpr int kLsThreads = 128;   // threads per CTA of the band and sweep kernels
-constexpr int kLsChunk = 1024;    // (node, triangle) pairs per band CTA
+constexpr int kLsThreads = 128;   // threads per CTA of the band kernel
+constexpr int kLsChunk = 256;     // (node, triangle) pairs per band warp
+constexpr int kLsSweepThreads = 1024;  // 128 nodes of a diagonal per pass
+constexpr int kLsMinSlab = 1;     // planes per sweep slab, at least
 constexpr unsigned kNoTri = 0xffffffffu;
 
 struct LsGrid {
@@ -86,11 +92,15 @@ __device__ __forceinline__ float f3dist(float3 a, float3 b) {
 }
 __device__ __forceinline__ float fmin_std(float a, float b) { return b < a ? b : a; }  // std::min
 
-// point_segment_distance (makelevelset3.cpp:8-20)
+// point_segment_distance (makelevelset3.cpp:8-20).  The reference divides the float dot
+// product by the float squared length in FP64 and rounds the quotient to float.  Double
+// rounding of a quotient of floats through a format of p' >= 2p + 2 bits is innocuous
+// (Figueroa, "When is double rounding innocuous?", 1995): the result is the correctly rounded
+// float quotient, so one IEEE FP32 division gives the same bits without the FP64 unit.
 __device__ float ls_seg(float3 x0, float3 x1, float3 x2) {
     const float3 dx = f3sub(x2, x1);
-    const double m2 = (double)f3dot(dx, dx);
-    float s12 = (float)((double)f3dot(f3sub(x2, x0), dx) / m2);
+    const float m2 = f3dot(dx, dx);
+    float s12 = __fdiv_rn(f3dot(f3sub(x2, x0), dx), m2);
     if (s12 < 0)
         s12 = 0;
     else if (s12 > 1)
@@ -119,12 +129,6 @@ __device__ float ls_tri(float3 x0, float3 x1, float3 x2, float3 x3) {
     if (w23 > 0) return fmin_std(ls_seg(x0, x1, x2), ls_seg(x0, x1, x3));
     if (w31 > 0) return fmin_std(ls_seg(x0, x1, x2), ls_seg(x0, x2, x3));
     return fmin_std(ls_seg(x0, x1, x3), ls_seg(x0, x2, x3));
-}
-
-__device__ __forceinline__ float ls_tri_index(const float* __restrict__ verts, const unsigned* __restrict__ tris,
-                                              unsigned t, float3 x0) {
-    const unsigned p = tris[3 * (size_t)t], q = tris[3 * (size_t)t + 1], r = tris[3 * (size_t)t + 2];
-    return ls_tri(x0, ld_vert(verts, p), ld_vert(verts, q), ld_vert(verts, r));
 }
 
 // orientation (makelevelset3.cpp:97-113): sign of the doubled area, ties broken by
@@ -199,8 +203,9 @@ __global__ void ls_init_kernel(unsigned long long* __restrict__ key, int* __rest
 __global__ void ls_plan_kernel(const float* __restrict__ verts, const unsigned* __restrict__ tris, int nt, LsGrid g,
                                int band, LsPlan* __restrict__ plan, unsigned long long* __restrict__ total) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nt) return;
-    const TriGrid c = tri_grid(verts, tris, (unsigned)t, g);
+    const int lane = threadIdx.x & 31;
+    const bool valid = t < nt;
+    const TriGrid c = tri_grid(verts, tris, valid ? (unsigned)t : 0u, g);
     LsPlan p;
     const int i0 = clampi((int)min3d(c.fi[0], c.fi[1], c.fi[2]) - band, 0, g.ni - 1);
     const int i1 = clampi((int)max3d(c.fi[0], c.fi[1], c.fi[2]) + band + 1, 0, g.ni - 1);
@@ -224,9 +229,19 @@ __global__ void ls_plan_kernel(const float* __restrict__ verts, const unsigned* 
     p.cnk = ck1 >= ck0 ? ck1 - ck0 + 1 : 0;
     // with i0 <= i1 etc. always (clamped), the band box is never empty
     const long long work = (long long)p.ni * p.nj * p.nk + (long long)p.cnj * p.cnk;
-    p.chunks = (int)((work + kLsChunk - 1) / kLsChunk);
-    p.first_chunk = (long long)atomicAdd(total, (unsigned long long)p.chunks);
-    plan[t] = p;
+    p.chunks = valid ? (int)((work + kLsChunk - 1) / kLsChunk) : 0;
+    // the warp's chunk ranges: one atomic per warp, inclusive scan over the lanes
+    long long incl = p.chunks;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    unsigned long long base = 0;
+    if (lane == 31) base = atomicAdd(total, (unsigned long long)incl);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    p.first_chunk = (long long)base + incl - p.chunks;
+    if (valid) plan[t] = p;
 }
 
 // chunk -> triangle map (one thread per triangle writes its chunks)
@@ -237,22 +252,25 @@ __global__ void ls_chunk_map_kernel(const LsPlan* __restrict__ plan, int nt, int
     for (int c = 0; c < p.chunks; ++c) chunk_tri[p.first_chunk + c] = t;
 }
 
-// One CTA per chunk of (node, triangle) pairs: band distances (makelevelset3.cpp:180-189) and
-// crossing counts (makelevelset3.cpp:191-207).
+// One warp per chunk of kLsChunk (node, triangle) pairs, kLsThreads / 32 chunks per CTA: band
+// distances (makelevelset3.cpp:180-189) and crossing counts (makelevelset3.cpp:191-207).
 __global__ void __launch_bounds__(kLsThreads) ls_band_kernel(const float* __restrict__ verts,
                                                              const unsigned* __restrict__ tris, LsGrid g,
                                                              const LsPlan* __restrict__ plan,
                                                              const int* __restrict__ chunk_tri,
                                                              unsigned long long* __restrict__ key,
-                                                             int* __restrict__ count, float init) {
-    const int t = chunk_tri[blockIdx.x];
+                                                             int* __restrict__ count, float init,
+                                                             long long chunks) {
+    const long long chunk = (long long)blockIdx.x * (kLsThreads / 32) + (threadIdx.x >> 5);
+    if (chunk >= chunks) return;
+    const int t = chunk_tri[chunk];
     const LsPlan p = plan[t];
-    const long long base = ((long long)blockIdx.x - p.first_chunk) * kLsChunk;
+    const long long base = (chunk - p.first_chunk) * kLsChunk;
     const long long vol = (long long)p.ni * p.nj * p.nk;
     const long long work = vol + (long long)p.cnj * p.cnk;
     const unsigned q0 = tris[3 * (size_t)t], q1 = tris[3 * (size_t)t + 1], q2 = tris[3 * (size_t)t + 2];
     const float3 xp = ld_vert(verts, q0), xq = ld_vert(verts, q1), xr = ld_vert(verts, q2);
-    for (int u = threadIdx.x; u < kLsChunk; u += kLsThreads) {
+    for (int u = threadIdx.x & 31; u < kLsChunk; u += 32) {
         const long long w = base + u;
         if (w >= work) break;
         if (w < vol) {
@@ -296,65 +314,175 @@ __global__ void ls_unpack_kernel(const unsigned long long* __restrict__ key, flo
     }
 }
 
-// One diagonal L of one sweep order (makelevelset3.cpp:75-94): the nodes with sweep-relative
-// a + b + c = L, threads over (b, c) with c in [c_lo, c_lo + nc).
-__global__ void __launch_bounds__(kLsThreads) ls_sweep_kernel(const float* __restrict__ verts,
-                                                              const unsigned* __restrict__ tris, LsGrid g,
-                                                              float* __restrict__ phi, int* __restrict__ closest,
-                                                              int di, int dj, int dk, int L, int c_lo, int nc) {
-    const int nb = g.nj - 1;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= nb * nc) return;
-    const int b = tid % nb, c = c_lo + tid / nb;
-    const int a = L - b - c;
-    if (a < 0 || a > g.ni - 2) return;
-    const int i = di > 0 ? a + 1 : g.ni - 2 - a;
-    const int j = dj > 0 ? b + 1 : g.nj - 2 - b;
-    const int k = dk > 0 ? c + 1 : g.nk - 2 - c;
-    // check_neighbour order of sweep(): (i-di,j,k) (i,j-dj,k) (i-di,j-dj,k) (i,j,k-dk)
-    // (i-di,j,k-dk) (i,j-dj,k-dk) (i-di,j-dj,k-dk)
-    int ct[7];
-    ct[0] = closest[g.at(i - di, j, k)];
-    ct[1] = closest[g.at(i, j - dj, k)];
-    ct[2] = closest[g.at(i - di, j - dj, k)];
-    ct[3] = closest[g.at(i, j, k - dk)];
-    ct[4] = closest[g.at(i - di, j, k - dk)];
-    ct[5] = closest[g.at(i, j - dj, k - dk)];
-    ct[6] = closest[g.at(i - di, j - dj, k - dk)];
-    const size_t self = g.at(i, j, k);
-    const int own = closest[self];
-    // A candidate equal to the node's own triangle or to an earlier candidate cannot pass
-    // `d < phi`: phi already is at most that triangle's distance (phi of a node with a closest
-    // triangle is that triangle's distance from the same node position, the same bits).
-    // The distances do not depend on phi, so they are evaluated first, the comparisons after,
-    // in the reference's order.
-    bool use[7];
-#pragma unroll
-    for (int m = 0; m < 7; ++m) {
-        bool u = ct[m] >= 0 && ct[m] != own;
-#pragma unroll
-        for (int e = 0; e < m; ++e) u = u && ct[e] != ct[m];
-        use[m] = u;
+// Triangle vertices gathered per triangle, three float4 each: x1 y1 z1 x2 | y2 z2 x3 y3 | z3 - - -
+__global__ void ls_soup_kernel(const float* __restrict__ verts, const unsigned* __restrict__ tris, int nt,
+                               float4* __restrict__ soup) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const float3 a = ld_vert(verts, tris[3 * (size_t)t]), b = ld_vert(verts, tris[3 * (size_t)t + 1]),
+                 c = ld_vert(verts, tris[3 * (size_t)t + 2]);
+    soup[3 * (size_t)t] = make_float4(a.x, a.y, a.z, b.x);
+    soup[3 * (size_t)t + 1] = make_float4(b.y, b.z, c.x, c.y);
+    soup[3 * (size_t)t + 2] = make_float4(c.z, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ float ls_tri_soup(const float4* __restrict__ soup, int t, float3 x0) {
+    const float4 a = __ldg(soup + 3 * (size_t)t), b = __ldg(soup + 3 * (size_t)t + 1),
+                 c = __ldg(soup + 3 * (size_t)t + 2);
+    return ls_tri(x0, make_float3(a.x, a.y, a.z), make_float3(a.w, b.x, b.y), make_float3(b.z, b.w, c.x));
+}
+
+// The sweep step of node (i, j, k) in order (di, dj, dk) (makelevelset3.cpp:75-94 with
+// check_neighbour, :56-71), by a group of 8 lanes: lane e < 7 takes the reference's e-th
+// neighbour, (i-di,j,k) (i,j-dj,k) (i-di,j-dj,k) (i,j,k-dk) (i-di,j,k-dk) (i,j-dj,k-dk)
+// (i-di,j-dj,k-dk), i.e. offsets by the bits of e + 1.  The candidates' distances do not depend
+// on phi, so the lanes evaluate them at once; the comparisons then run in the reference's
+// order over shuffles.  A candidate equal to the node's own triangle or to an earlier
+// candidate cannot pass `d < phi` (phi is at most that triangle's distance from the same
+// node position, the same bits) and is not evaluated.
+//
+// Plane k and, unless prev_remote, plane k - dk belong to the calling CTA's slab: only it
+// writes them during the launch, so plain (L1-cached) loads see its own stores.  A plane
+// k - dk of another slab is read through L2 (ld.global.cg): its lines may sit in this SM's L1
+// from before that slab finished them.  All 32 lanes of the warp call this (valid = false for
+// lanes without a node).
+__device__ __forceinline__ void ls_sweep_node8(const float4* __restrict__ soup, const LsGrid& g, float* phi,
+                                               int* closest, bool valid, int i, int j, int k, int di, int dj,
+                                               int dk, bool prev_remote) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, e = lane & 7, gbase = lane & ~7;
+    const int f = e + 1;
+    int ct = -1, own = -1;
+    float phi0 = 0.f;
+    size_t self = 0;
+    if (valid) {
+        self = g.at(i, j, k);
+        own = closest[self];
+        phi0 = phi[self];
+        if (e < 7) {
+            const size_t q = g.at(i - ((f & 1) ? di : 0), j - ((f & 2) ? dj : 0), k - ((f & 4) ? dk : 0));
+            ct = (prev_remote && (f & 4)) ? __ldcg(closest + q) : closest[q];
+        }
     }
-    bool any = false;
+    bool use = ct >= 0 && ct != own;
 #pragma unroll
-    for (int m = 0; m < 7; ++m) any = any || use[m];
-    if (!any) return;
-    const float3 x0 = g.node(i, j, k);
-    float d[7];
-#pragma unroll
-    for (int m = 0; m < 7; ++m) d[m] = use[m] ? ls_tri_index(verts, tris, (unsigned)ct[m], x0) : 0.f;
-    float p = phi[self];
+    for (int e2 = 0; e2 < 7; ++e2) {
+        const int v = __shfl_sync(full, ct, gbase + e2);
+        if (e2 < e && v == ct) use = false;
+    }
+    float d = 0.f;
+    if (use) d = ls_tri_soup(soup, ct, g.node(i, j, k));
+    float p = phi0;
     int best = own;
 #pragma unroll
-    for (int m = 0; m < 7; ++m)
-        if (use[m] && d[m] < p) {
-            p = d[m];
-            best = ct[m];
+    for (int e2 = 0; e2 < 7; ++e2) {
+        const float de = __shfl_sync(full, d, gbase + e2);
+        const int ce = __shfl_sync(full, ct, gbase + e2);
+        const unsigned ue = __shfl_sync(full, (unsigned)use, gbase + e2);
+        if (ue && de < p) {
+            p = de;
+            best = ce;
         }
-    if (best != own) {
+    }
+    if (valid && e == 0 && best != own) {
         phi[self] = p;
         closest[self] = best;
+    }
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bound on the polls of one wait (each at least ~0.3 us): about a second.
+constexpr long kLsSpinLimit = 1L << 22;
+
+// One sweep order over slabs of planes.  With sweep-relative indices (a, b, c) (a = i - 1 for
+// di > 0, ni - 2 - i for di < 0, likewise b, c), CTA s owns the planes c in [s P, s P + P) and
+// walks the slab's diagonals M = a + b + (c - s P) in order, each diagonal's nodes in parallel,
+// a __syncthreads between diagonals.  Node (a, b, c) reads nodes of plane c on diagonals M - 1,
+// M - 2 and of plane c - 1 on M - 1, M - 2, M - 3: for the slab's first plane those lie in slab
+// s - 1, on its diagonals up to M + P - 1, so the slab starts diagonal M once progress[s - 1]
+// (slab s - 1's finished diagonals) reaches M + P.  Every node therefore reads what the
+// reference's loop (c, b, a ascending) would have shown it.  Needs all CTAs resident
+// (cooperative launch); every wait is bounded: on timeout the CTA sets *err and returns, and
+// the others see *err and return.
+__global__ void __launch_bounds__(kLsSweepThreads, 1) ls_sweep_slabs_kernel(const float4* __restrict__ soup,
+                                                                       LsGrid g, float* phi, int* closest, int di,
+                                                                       int dj, int dk, int P, int* progress,
+                                                                       int* err) {
+    __shared__ int s_seen;
+    const int A = g.ni - 2, B = g.nj - 2, planes = g.nk - 1;
+    const int s = blockIdx.x;
+    const int c0 = s * P;
+    if (c0 >= planes) return;
+    const int np = min(P, planes - c0);
+    const int steps = A + B + np;       // diagonals of this slab
+    const int prev_steps = A + B + P;   // diagonals of slab s - 1 (always a full slab)
+    const bool signal = c0 + np < planes;
+    int seen = s == 0 ? INT_MAX : 0;
+    for (int M = 0; M < steps; ++M) {
+        const int need = min(M + P, prev_steps);
+        if (seen < need) {  // uniform over the CTA
+            if (threadIdx.x == 0) {
+                int v;
+                long it = 0;
+                while ((v = ld_acquire_gpu(progress + s - 1)) < need) {
+                    if (ld_acquire_gpu(err) != 0) {
+                        v = -1;
+                        break;
+                    }
+                    if (++it > kLsSpinLimit) {
+                        atomicExch(err, 1);
+                        v = -1;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+                s_seen = v;
+            }
+            __syncthreads();
+            seen = s_seen;
+            if (seen < 0) return;
+        }
+        // nodes of diagonal M: planes cl in [cl_lo, cl_hi], in each a in [a_lo, a_hi]; a group
+        // of 8 lanes per node, kLsSweepThreads / 8 nodes per pass
+        const int cl_lo = max(0, M - A - B), cl_hi = min(np - 1, M);
+        int total = 0;
+        for (int cl = cl_lo; cl <= cl_hi; ++cl) {
+            const int m = M - cl;
+            total += min(A, m) - max(0, m - B) + 1;
+        }
+        for (int base = 0; base < total; base += kLsSweepThreads / 8) {
+            const int t = base + (int)(threadIdx.x >> 3);
+            int cl = cl_lo, a = -1;
+            if (t < total) {
+                int rest = t;
+                for (; cl <= cl_hi; ++cl) {
+                    const int m = M - cl;
+                    const int a_lo = max(0, m - B), cnt = min(A, m) - a_lo + 1;
+                    if (rest < cnt) {
+                        a = a_lo + rest;
+                        break;
+                    }
+                    rest -= cnt;
+                }
+            }
+            const bool valid = a >= 0;
+            const int b = M - cl - a;
+            const int c = c0 + cl;
+            const int i = di > 0 ? a + 1 : g.ni - 2 - a;
+            const int j = dj > 0 ? b + 1 : g.nj - 2 - b;
+            const int k = dk > 0 ? c + 1 : g.nk - 2 - c;
+            ls_sweep_node8(soup, g, phi, closest, valid, i, j, k, di, dj, dk, cl == 0 && s > 0);
+        }
+        __syncthreads();
+        if (signal && threadIdx.x == 0) st_release_gpu(progress + s, M + 1);
     }
 }
 
@@ -404,10 +532,12 @@ int ls_run(sdfc_context* ctx, const float* d_verts, const unsigned* d_tris, int 
     LsPlan* d_plan = nullptr;
     unsigned long long* d_total = nullptr;
     int* d_chunk_tri = nullptr;
+    float4* d_soup = nullptr;
+    int* d_progress = nullptr;
     int rc = SDFC_OK;
     auto cleanup = [&]() {
         for (void* p : {(void*)d_key, (void*)d_count, (void*)d_closest, (void*)d_plan, (void*)d_total,
-                        (void*)d_chunk_tri})
+                        (void*)d_chunk_tri, (void*)d_soup, (void*)d_progress})
             if (p) cudaFreeAsync(p, st);
     };
 #define LS_TRY(call)                                                                                          \
@@ -442,26 +572,57 @@ int ls_run(sdfc_context* ctx, const float* d_verts, const unsigned* d_tris, int 
         LS_TRY(cudaMallocAsync((void**)&d_chunk_tri, sizeof(int) * total, st));
         ls_chunk_map_kernel<<<(nt + 127) / 128, 128, 0, st>>>(d_plan, nt, d_chunk_tri);
         LS_TRY(cudaGetLastError());
-        ls_band_kernel<<<(unsigned)total, kLsThreads, 0, st>>>(d_verts, d_tris, g, d_plan, d_chunk_tri, d_key,
-                                                               d_count, init);
+        const unsigned band_blocks = (unsigned)((total + kLsThreads / 32 - 1) / (kLsThreads / 32));
+        ls_band_kernel<<<band_blocks, kLsThreads, 0, st>>>(d_verts, d_tris, g, d_plan, d_chunk_tri, d_key,
+                                                           d_count, init, (long long)total);
         LS_TRY(cudaGetLastError());
     }
     ls_unpack_kernel<<<fill_blocks, 256, 0, st>>>(d_key, d_phi, d_closest, n, init);
     LS_TRY(cudaGetLastError());
-    if (ni >= 2 && nj >= 2 && nk >= 2) {
+    if (ni >= 2 && nj >= 2 && nk >= 2 && nt > 0) {
         static const int dirs[8][3] = {{1, 1, 1},  {-1, -1, -1}, {1, 1, -1},  {-1, -1, 1},
                                        {1, -1, 1}, {-1, 1, -1},  {1, -1, -1}, {-1, 1, 1}};
-        const int A = ni - 2, B = nj - 2, C = nk - 2;
-        for (int pass = 0; pass < 2; ++pass)
-            for (int s = 0; s < 8; ++s)
-                for (int L = 0; L <= A + B + C; ++L) {
-                    const int c_lo = std::max(0, L - A - B), c_hi = std::min(C, L);
-                    const int nc = c_hi - c_lo + 1;
-                    const int threads = (B + 1) * nc;
-                    ls_sweep_kernel<<<(threads + kLsThreads - 1) / kLsThreads, kLsThreads, 0, st>>>(
-                        d_verts, d_tris, g, d_phi, d_closest, dirs[s][0], dirs[s][1], dirs[s][2], L, c_lo, nc);
-                }
+        const int planes = nk - 1;
+        LS_TRY(cudaMallocAsync((void**)&d_soup, sizeof(float4) * 3 * (size_t)nt, st));
+        LS_TRY(cudaMallocAsync((void**)&d_progress, sizeof(int) * ((size_t)planes + 1), st));
+        int* d_err = d_progress + planes;
+        LS_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+        ls_soup_kernel<<<(nt + 127) / 128, 128, 0, st>>>(d_verts, d_tris, nt, d_soup);
         LS_TRY(cudaGetLastError());
+        int dev = 0, sms = 0, per_sm = 0;
+        LS_TRY(cudaGetDevice(&dev));
+        LS_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        LS_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ls_sweep_slabs_kernel, kLsSweepThreads, 0));
+        if (per_sm < 1) {
+            cleanup();
+            return sdfc_impl::fail(ctx, SDFC_ERR_CUDA, "make_level_set3: sweep kernel cannot be resident");
+        }
+        // slabs of P planes, one CTA each, all resident
+        const int capacity = sms * per_sm;
+        const char* slab_env = std::getenv("SDFC_LS_SLAB");  // tuning knob: planes per slab
+        const int min_slab = slab_env ? std::max(1, std::atoi(slab_env)) : kLsMinSlab;
+        const int P = std::max(min_slab, (planes + capacity - 1) / capacity);
+        const int slabs = (planes + P - 1) / P;
+        LsGrid gg = g;
+        float* a_phi = d_phi;
+        int* a_closest = d_closest;
+        int aP = P;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int s = 0; s < 8; ++s) {
+                int di = dirs[s][0], dj = dirs[s][1], dk = dirs[s][2];
+                LS_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * planes, st));
+                void* args[] = {(void*)&d_soup, (void*)&gg, (void*)&a_phi, (void*)&a_closest, (void*)&di,
+                                (void*)&dj, (void*)&dk, (void*)&aP, (void*)&d_progress, (void*)&d_err};
+                LS_TRY(cudaLaunchCooperativeKernel((const void*)ls_sweep_slabs_kernel, dim3(slabs),
+                                                   dim3(kLsSweepThreads), args, 0, st));
+            }
+        int h_err = 0;
+        LS_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        LS_TRY(cudaStreamSynchronize(st));
+        if (h_err) {
+            cleanup();
+            return sdfc_impl::fail(ctx, SDFC_ERR_CUDA, "make_level_set3: a sweep wait timed out");
+        }
     }
     const int rows = nj * nk;
     ls_sign_kernel<<<(rows + 7) / 8, 256, 0, st>>>(d_phi, d_count, g, rows);

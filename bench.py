@@ -380,6 +380,7 @@ def run_gpu(args, world, rank):
     sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 else None
     c5_res = run_c5(args, sdfc, ctx, torch) if args.c5_points > 0 and rank == 0 else None
     c4_res = run_c4(args, sdfc, ctx, g, torch) if args.c4_instances > 0 and rank == 0 else None
+    ls_res = run_levelset(args, sdfc, ctx, torch) if args.ls_segments > 0 and rank == 0 else None
     if sim_res is not None:
         plain = run_sim_plain(args, sdfc, ctx, g, p, n)
         plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
@@ -439,6 +440,8 @@ def run_gpu(args, world, rank):
         line["fp16_bricks"] = c5_res
     if c4_res is not None:
         line["differentiable_rollout"] = c4_res
+    if ls_res is not None:
+        line["sdf_construction"] = ls_res
     print(json.dumps(line), flush=True)
 
 
@@ -630,6 +633,54 @@ def run_c5(args, sdfc, ctx, torch):
     return out
 
 
+def run_levelset(args, sdfc, ctx, torch):
+    """Mesh -> SDF grid (sdfgen::make_level_set3, the work of BodySDFObj::precompute_SDF): a seeded
+    bumpy torus of args.ls_segments x args.ls_segments/2 quads (2 triangles each) on a grid of
+    spacing args.ls_dx with 2 cells of margin, exact band 1.  Device arrays in and out (value) and
+    host arrays through sdfc_make_level_set3 (e2e); the oracle's sequential restatement of the
+    reference times a smaller grid of the same mesh on one host core.  The GPU result on that
+    grid is compared bit for bit with the oracle's."""
+    from oracle import oracle
+    n, m = args.ls_segments, args.ls_segments // 2
+    V, F = W.torus_mesh(0.6, 0.25, n, m)
+    V = V * (1 + 0.03 * np.random.default_rng(n).standard_normal((len(V), 1)))
+    origin, shape = W.level_set_grid(V, args.ls_dx)
+    nodes = int(np.prod(shape))
+    Vd = torch.tensor(np.asarray(V, np.float32), device="cuda")
+    Fd = torch.tensor(np.asarray(F, np.int32), device="cuda")
+    st = torch.cuda.current_stream()
+    ctx.make_level_set3_device(Vd, Fd, origin, args.ls_dx, shape)  # warm-up
+    times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        ctx.make_level_set3_device(Vd, Fd, origin, args.ls_dx, shape)
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    t = time.perf_counter()
+    ctx.make_level_set3(V, F, origin, args.ls_dx, shape)
+    e2e_ms = (time.perf_counter() - t) * 1e3
+    A, B, C = shape[0] - 2, shape[1] - 2, shape[2] - 2
+    out = {"mesh": f"bumpy torus, {len(F)} triangles", "grid": list(shape), "nodes": nodes, "exact_band": 1,
+           "ms": ms, "nodes_per_s": nodes / (ms / 1e3),
+           "e2e": {"ms": e2e_ms, "nodes_per_s": nodes / (e2e_ms / 1e3),
+                   "h2d_bytes": int(V.size * 4 + F.size * 4), "d2h_bytes": nodes * 4},
+           "sweep_diagonals": 16 * (A + B + C + 1), "us_per_sweep_diagonal": ms * 1e3 / (16 * (A + B + C + 1))}
+    if args.ls_cpu_dx > 0:
+        o2, s2 = W.level_set_grid(V, args.ls_cpu_dx)
+        t = time.perf_counter()
+        want = oracle.make_level_set3(V, F, o2, args.ls_cpu_dx, s2)
+        ct = time.perf_counter() - t
+        got = ctx.make_level_set3(V, F, o2, args.ls_cpu_dx, s2)
+        out["bit_exact_vs_oracle"] = bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))
+        out["cpu_baseline"] = {"value": int(np.prod(s2)) / ct, "unit": "nodes/s", "cores": 1, "kind": "port",
+                               "sample": f"same mesh on a {s2[0]}x{s2[1]}x{s2[2]} grid (spacing {args.ls_cpu_dx})"}
+        out["speedup_vs_cpu"] = out["nodes_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
 def run_c4(args, sdfc, ctx, g, torch):
     """Differentiable rollout: args.c4_instances pegs on free3d-exp joints in the socket, initial
     pose perturbed (sigma 0.01 translation, sigma 1 degree rotation), pulled along directions in a
@@ -727,6 +778,10 @@ def main():
     ap.add_argument("--c4-points", type=int, default=10000, help="differentiable-rollout leg: peg points")
     ap.add_argument("--c4-precision", choices=("mixed", "fp64"), default="mixed",
                     help="differentiable-rollout leg: precision of the force evaluations")
+    ap.add_argument("--ls-segments", type=int, default=512,
+                    help="SDF-construction leg: torus segments (x segments/2 quads; 0: skip the leg)")
+    ap.add_argument("--ls-dx", type=float, default=0.0068, help="SDF-construction leg: grid spacing")
+    ap.add_argument("--ls-cpu-dx", type=float, default=0.02, help="SDF-construction leg: spacing of the CPU sample")
     ap.add_argument("--c5-grid", type=int, default=512, help="FP16-brick leg: grid nodes per axis")
     ap.add_argument("--c5-points", type=int, default=1000000, help="FP16-brick leg: points (0: skip the leg)")
     ap.add_argument("--c5-dirs", type=int, default=256, help="FP16-brick leg: pull directions")

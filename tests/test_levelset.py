@@ -50,3 +50,18 @@ def test_layout_rules():
     assert shape == (23, 13, 13)
     with pytest.raises(sdfc.SdfcError):
         sdfc.sdf_grid_layout(V, 0.05, 0)
+
+
+def test_float_quotient_identity():
+    """The GPU level set divides in FP32 where the reference divides float operands in FP64
+    and rounds to float (point_segment_distance); the two agree bit for bit.  Checked on
+    random, tiny, huge and tie-prone operands."""
+    r = np.random.default_rng(3)
+    a = np.concatenate([r.standard_normal(200000), r.uniform(-1, 1, 50000) * 1e-38, r.uniform(1, 2, 50000) * 1e38,
+                        np.arange(1, 50001), [0.0, -0.0, 1.0, 3.0]]).astype(np.float32)
+    b = np.concatenate([r.standard_normal(200000), r.uniform(0.5, 2, 50000) * 1e5, r.uniform(1e-3, 1e-2, 50000),
+                        np.full(50000, 3.0), [0.0, 1.0, 0.0, 7.0]]).astype(np.float32)
+    with np.errstate(all="ignore"):
+        via_double = (a.astype(np.float64) / b.astype(np.float64)).astype(np.float32)
+        direct = a / b
+    assert np.array_equal(via_double.view(np.uint32), direct.view(np.uint32))
