@@ -52,6 +52,7 @@ void free_batch(sdfc_batch* b) {
     cudaFree(b->d_prefilter);
     cudaFree(b->d_partial);
     cudaFree(b->d_recheck);
+    cudaFree(b->d_point_offset);
     cudaFree(b->d_in);
     cudaFree(b->d_out);
     cudaFree(b->d_int);
@@ -151,6 +152,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     b->precision = ctx->precision;
     b->inst.resize(n);
     std::vector<int> tile_inst;
+    std::vector<long long> point_offset(n);
     int tiles = 0;
     for (int k = 0; k < n; ++k) {
         if (points[k] < 0 || points[k] >= (int)ctx->points.size() || grids[k] < 0 || grids[k] >= (int)ctx->grids.size()) {
@@ -164,6 +166,8 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
             return fail(ctx, SDFC_ERR_CAPACITY, "batch_create: point set larger than kTile*kMaxTilesPerInstance");
         }
         b->inst[k] = InstanceDesc{points[k], grids[k], tiles, nt};
+        point_offset[k] = b->total_points;
+        b->total_points += np;
         for (int t = 0; t < nt; ++t) tile_inst.push_back(k);
         tiles += nt;
     }
@@ -177,6 +181,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
+        (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||
         (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
         (rc = alloc((void**)&b->d_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_int, sizeof(int) * (size_t)n * 2))) {
@@ -192,6 +197,8 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     cudaError_t e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && tiles > 0)
         e = cudaMemcpy(b->d_tile_inst, tile_inst.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_point_offset, point_offset.data(), sizeof(long long) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_recheck, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(b->d_tile_count, 0, sizeof(int) * std::max(tiles, 1));
     if (e == cudaSuccess) e = cudaMemset(b->d_tile_queue, 0, sizeof(int) * std::max(tiles, 1));
@@ -270,10 +277,14 @@ int sdfc_batch_set_derivative_mode(sdfc_batch* b, int mode) {
     return SDFC_OK;
 }
 
-int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
-                     const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
+}  // extern "C"
+
+// values (FP64 grid) or, for SDFC_STORAGE_F16_BRICKS, already encoded bricks (codes_in, so_in)
+static int upload_grid_impl(sdfc_context* ctx, const double* values, const unsigned short* codes_in,
+                            const float* so_in, int ni, int nj, int nk, const double min_box[3],
+                            const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
     if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
-    if (!values || !min_box || !max_box || !dxyz || !grid)
+    if ((!values && !(codes_in && so_in)) || !min_box || !max_box || !dxyz || !grid)
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: null argument");
     if (ni < 2 || nj < 2 || nk < 2) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: each extent must be >= 2");
     if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32 && storage != SDFC_STORAGE_F16_BRICKS)
@@ -289,7 +300,7 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     }
     if (!std::isfinite(col_th)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite col_th");
     const size_t n = (size_t)ni * nj * nk;
-    if (!all_finite(values, n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite value");
+    if (values && !all_finite(values, n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite value");
     int rc = use_device(ctx);
     if (rc) return rc;
 
@@ -303,8 +314,15 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
         codes.resize(nb * 512);
         so.resize(2 * nb);
         seen.resize(n);
-        sdfc_f16_brick_encode(values, ni, nj, nk, codes.data(), so.data());
+        if (codes_in) {
+            std::copy(codes_in, codes_in + codes.size(), codes.begin());
+            std::copy(so_in, so_in + so.size(), so.begin());
+        } else {
+            sdfc_f16_brick_encode(values, ni, nj, nk, codes.data(), so.data());
+        }
         sdfc_f16_brick_decode(codes.data(), so.data(), ni, nj, nk, seen.data());
+        if (codes_in && !all_finite(seen.data(), n))
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite brick value");
     } else if (storage == SDFC_STORAGE_F32) {
         seen.resize(n);
         for (size_t i = 0; i < n; ++i) seen[i] = (double)(float)values[i];
@@ -389,6 +407,22 @@ int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, in
     }
     *grid = (int)ctx->grids.size() - 1;
     return SDFC_OK;
+}
+
+extern "C" {
+
+int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
+                     const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
+    return upload_grid_impl(ctx, values, nullptr, nullptr, ni, nj, nk, min_box, max_box, dxyz, col_th, storage, grid);
+}
+
+int sdfc_upload_grid_bricks(sdfc_context* ctx, const unsigned short* codes, const float* so, int ni, int nj, int nk,
+                            const double min_box[3], const double max_box[3], const double dxyz[3], double col_th,
+                            int* grid) {
+    if (!codes || !so) return ctx ? fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid_bricks: null argument")
+                                  : SDFC_ERR_INVALID_ARGUMENT;
+    return upload_grid_impl(ctx, nullptr, codes, so, ni, nj, nk, min_box, max_box, dxyz, col_th,
+                            SDFC_STORAGE_F16_BRICKS, grid);
 }
 
 int sdfc_grid_values(sdfc_context* ctx, int grid, double* values) {
@@ -693,6 +727,83 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
     }
     if (n_active) std::memcpy(n_active, b->h_int, sizeof(int) * n);
     if (status) std::memcpy(status, b->h_int + n, sizeof(int) * n);
+    return SDFC_OK;
+}
+
+int sdfc_batch_distance_device(sdfc_batch* b, const double* d_EA, const double* d_EB, double* d_min, double* d_d,
+                               void* stream) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!d_EA || !d_EB || !d_min) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_distance: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    sdfc::BatchInputs in{d_EA, nullptr, d_EB, nullptr, nullptr};
+    // d_out (n x 300 doubles) holds the minimum keys
+    sdfc::launch_distance(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points,
+                          b->d_point_offset, (unsigned long long*)b->d_out, d_min, d_d, s);
+    CUDA_TRY(ctx, cudaGetLastError());
+    return SDFC_OK;
+}
+
+int sdfc_batch_distance(sdfc_batch* b, const double* E_A, const double* E_B, double* min_d, double* d) {
+    if (!b) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = b->ctx;
+    if (!E_A || !E_B || !min_d) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "batch_distance: null argument");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    const size_t n = (size_t)b->n;
+    cudaStream_t s = ctx->stream;
+    double* h = b->h_in;
+    std::memcpy(h, E_A, sizeof(double) * 16 * n);
+    std::memcpy(h + 16 * n, E_B, sizeof(double) * 16 * n);
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->d_in, h, sizeof(double) * 32 * n, cudaMemcpyHostToDevice, s));
+    double* dd = nullptr;
+    if (d && b->total_points > 0) CUDA_TRY(ctx, cudaMallocAsync((void**)&dd, sizeof(double) * b->total_points, s));
+    double* dmin = b->d_in + 32 * n;  // n doubles after the poses
+    rc = sdfc_batch_distance_device(b, b->d_in, b->d_in + 16 * n, dmin, dd, s);
+    if (rc == SDFC_OK) {
+        cudaError_t e = cudaMemcpyAsync(b->h_out, dmin, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && dd)
+            e = cudaMemcpyAsync(d, dd, sizeof(double) * b->total_points, cudaMemcpyDeviceToHost, s);
+        if (dd) cudaFreeAsync(dd, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("batch_distance: ") + cudaGetErrorString(e));
+        std::memcpy(min_d, b->h_out, sizeof(double) * n);
+    } else if (dd) {
+        cudaFreeAsync(dd, s);
+        cudaStreamSynchronize(s);
+    }
+    return rc;
+}
+
+int sdfc_grid_distance(sdfc_context* ctx, int grid, const double* X, int n, double* d, double* min_d) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (n < 0 || (n > 0 && !X)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "grid_distance: bad argument");
+    if (grid < 0 || grid >= (int)ctx->grids.size()) return fail(ctx, SDFC_ERR_NOT_FOUND, "grid_distance: unknown grid");
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    if (!d && !min_d) return SDFC_OK;
+    cudaStream_t s = ctx->stream;
+    // X (n x 3), d (n), the minimum and its key, in one allocation
+    const size_t words = 3 * (size_t)n + (size_t)n + 2;
+    double* buf = nullptr;
+    CUDA_TRY(ctx, cudaMallocAsync((void**)&buf, sizeof(double) * words, s));
+    double* dX = buf;
+    double* dd = buf + 3 * (size_t)n;
+    double* dmin = dd + n;
+    cudaError_t e = n > 0 ? cudaMemcpyAsync(dX, X, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    if (e == cudaSuccess) {
+        sdfc::launch_grid_query(ctx->d_grids, grid, dX, n, d ? dd : nullptr, (unsigned long long*)(dmin + 1),
+                                min_d ? dmin : nullptr, s);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && d && n > 0) e = cudaMemcpyAsync(d, dd, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && min_d) e = cudaMemcpyAsync(min_d, dmin, sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(buf, s);
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("grid_distance: ") + cudaGetErrorString(e));
     return SDFC_OK;
 }
 

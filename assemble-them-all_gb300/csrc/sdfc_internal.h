@@ -43,6 +43,8 @@ struct sdfc_batch {
     sdfc::Prefilter* d_prefilter = nullptr;
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
+    long long* d_point_offset = nullptr;  // n: first output row of each instance's per-point distances
+    long long total_points = 0;
     // staging of the host-array entry points
     double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
     double* d_out = nullptr;  // n x 300: fm | Km | Dm

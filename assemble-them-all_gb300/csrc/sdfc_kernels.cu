@@ -1,4 +1,6 @@
 // Kernels of the batched point-vs-SDF contact evaluation; see sdfc_kernels.cuh.
+#include <algorithm>
+#include <math_constants.h>
 #include <cstdint>
 
 #include "sdfc_kernels.cuh"
@@ -244,6 +246,84 @@ __global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restr
         tile_count[t] = base;
         if (recheck) atomicAdd(recheck, (unsigned long long)q);
     }
+}
+
+// ------------------------------------------------------------------ distances
+// Order-preserving key of a double for an unsigned atomic minimum (NaN aside).
+__device__ __forceinline__ unsigned long long dist_key(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dist_unkey(unsigned long long k) {
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+__global__ void distance_init_kernel(unsigned long long* __restrict__ key, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) key[i] = dist_key(CUDART_INF);
+}
+
+// A body-frame mesh vertex in world as Simulation::get_body_vertices computes it
+// (rm/Simulation.cpp:252-264, (R2 * v + p2).eval() with a Matrix3 R2): in the reference's
+// x86-64 build Eigen sums rows 0 and 1 as one SSE2 packet, (r0 v0 + r1 v1) + r2 v2, and row 2
+// by its unrolled scalar reduction, r0 v0 + (r1 v1 + r2 v2).
+__device__ __forceinline__ V3 vertex_world(const M3& R, V3 p, V3 v) {
+    const double x = add_rn(add_rn(mul_rn(R.m[0], v.x), mul_rn(R.m[1], v.y)), mul_rn(R.m[2], v.z));
+    const double y = add_rn(add_rn(mul_rn(R.m[3], v.x), mul_rn(R.m[4], v.y)), mul_rn(R.m[5], v.z));
+    const double z = add_rn(mul_rn(R.m[6], v.x), add_rn(mul_rn(R.m[7], v.y), mul_rn(R.m[8], v.z)));
+    return v3(add_rn(x, p.x), add_rn(y, p.y), add_rn(z, p.z));
+}
+
+// One CTA per detection tile: every vertex's FP64 distance as Simulation::get_body_distance
+// computes it (rm/Simulation.cpp:276-296: get_body_vertices, then BodySDFObj::distance), the
+// tile's minimum (exact: a selection) folded into the instance's by an atomic minimum.
+__global__ void __launch_bounds__(kDetectThreads) distance_kernel(const InstanceDesc* __restrict__ inst,
+                                                                  const int* __restrict__ tile_inst, BatchInputs in,
+                                                                  const GridDesc* __restrict__ grids,
+                                                                  const PointsDesc* __restrict__ points,
+                                                                  const long long* __restrict__ point_offset,
+                                                                  unsigned long long* __restrict__ key,
+                                                                  double* __restrict__ d) {
+    const int t = blockIdx.x;
+    const int i = tile_inst[t];
+    const InstanceDesc I = inst[i];
+    const GridDesc& g = grids[I.grid];
+    const PointsDesc& P = points[I.points];
+    const Pose A = load_pose(in.EA + 16 * (size_t)i), B = load_pose(in.EB + 16 * (size_t)i);
+    const int base = (t - I.tile0) * kTile;
+    const int n = P.n;
+    double m = CUDART_INF;
+    for (int k = threadIdx.x; k < kTile; k += kDetectThreads) {
+        const int sid = base + k;
+        if (sid >= n) break;
+        const double v = query_sdf(g, grid_point(B.R, B.p, vertex_world(A.R, A.p, load_point(P, sid))), false) +
+                         g.col_th;
+        if (d) d[point_offset[i] + __ldg(P.orig + sid)] = v;
+        m = fmin(m, v);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fmin(m, __shfl_xor_sync(kFull, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMin(key + i, dist_key(m));
+}
+
+// SDFMesh::query_SDF at caller points already in the grid frame (n x 3, AoS), no col_th.
+__global__ void grid_query_kernel(const GridDesc* __restrict__ grids, int grid, const double* __restrict__ X, int n,
+                                  double* __restrict__ d, unsigned long long* __restrict__ key) {
+    const GridDesc& g = grids[grid];
+    double m = CUDART_INF;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const double v = query_sdf(g, v3(X[3 * (size_t)q], X[3 * (size_t)q + 1], X[3 * (size_t)q + 2]), false);
+        if (d) d[q] = v;
+        m = fmin(m, v);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fmin(m, __shfl_xor_sync(kFull, m, o));
+    if (key && (threadIdx.x & 31) == 0) atomicMin(key, dist_key(m));
+}
+
+__global__ void distance_finalize_kernel(const unsigned long long* __restrict__ key, double* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = dist_unkey(key[i]);
 }
 
 // ------------------------------------------------------------------ forces
@@ -656,6 +736,27 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
                                                               s.ids, s.tile_count, s.tile_queue, in.mode);
     recheck_kernel<<<total_tiles, 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points, s.ids, s.tile_count,
                                                    s.tile_queue, s.recheck);
+}
+
+void launch_distance(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
+                     const GridDesc* d_grids, const PointsDesc* d_points, const long long* point_offset,
+                     unsigned long long* key_scratch, double* min_d, double* d, cudaStream_t stream) {
+    if (n_inst <= 0) return;
+    distance_init_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(key_scratch, n_inst);
+    if (total_tiles > 0)
+        distance_kernel<<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points,
+                                                                     point_offset, key_scratch, d);
+    distance_finalize_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(key_scratch, min_d, n_inst);
+}
+
+void launch_grid_query(const GridDesc* d_grids, int grid, const double* X, int n, double* d,
+                       unsigned long long* key_scratch, double* min_d, cudaStream_t stream) {
+    if (min_d) distance_init_kernel<<<1, 32, 0, stream>>>(key_scratch, 1);
+    if (n > 0) {
+        const int blocks = std::min((n + 255) / 256, 152 * 8);
+        grid_query_kernel<<<blocks, 256, 0, stream>>>(d_grids, grid, X, n, d, min_d ? key_scratch : nullptr);
+    }
+    if (min_d) distance_finalize_kernel<<<1, 32, 0, stream>>>(key_scratch, min_d, 1);
 }
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,

@@ -122,6 +122,16 @@ void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const
                    const PointsDesc* d_points, BatchScratch s, bool stencil, int precision, cudaStream_t stream);
 void launch_energy_finalize(int n_inst, BatchScratch s, double* energy, double* dE, const int* mode,
                             cudaStream_t stream);
+// The reference's distance (BodySDFObj::distance) of every point of every instance, FP64,
+// bit-identical: min_d[n] the per-instance minimum (+inf for an empty point set) and, with d
+// non-null, d[point_offset[i] + caller's index] every point's distance.
+void launch_distance(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
+                     const GridDesc* d_grids, const PointsDesc* d_points, const long long* point_offset,
+                     unsigned long long* key_scratch, double* min_d, double* d, cudaStream_t stream);
+// SDFMesh::query_SDF at n points X (n x 3, grid frame): d[n] (may be null) and the minimum
+// min_d[0] (may be null; key_scratch: one word).
+void launch_grid_query(const GridDesc* d_grids, int grid, const double* X, int n, double* d,
+                       unsigned long long* key_scratch, double* min_d, cudaStream_t stream);
 // Whether launch_force's derivative pass leaves the dq2 columns of Km to finalize
 // (the FP32-algebra path outside the stencil mode).
 bool force_skips_q2(bool deriv, bool stencil, int precision);

@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsdfcontact.so")
 
 SDFC_OK = 0
+SDFC_ERR_NOT_FOUND = -3
 STORAGE_F64 = 0
 STORAGE_F32 = 1
 STORAGE_F16_BRICKS = 2
@@ -31,6 +32,8 @@ EXPORTS = (
     "sdfc_grid_values", "sdfc_f16_brick_encode", "sdfc_f16_brick_decode", "sdfc_batch_energy",
     "sdfc_batch_energy_device", "sdfc_sim_record_energy", "sdfc_sim_energy", "sdfc_sim_backward_energy",
     "sdfc_sim_set_tolerance", "sdfc_make_level_set3", "sdfc_make_level_set3_device", "sdfc_sdf_grid_layout",
+    "sdfc_batch_distance", "sdfc_batch_distance_device", "sdfc_grid_distance", "sdfc_sdf_save_text",
+    "sdfc_sdf_load_text", "sdfc_sdf_save_bricks", "sdfc_sdf_load_bricks", "sdfc_upload_grid_bricks",
 )
 JOINT_TRANSLATIONAL = 3
 JOINT_FREE3D_EXP = 6
@@ -144,6 +147,15 @@ def lib():
         L.sdfc_make_level_set3.argtypes = [v, f, i, P(ctypes.c_uint), i, f, f32, f32, f32, i, i, i, i, f]
         L.sdfc_make_level_set3_device.argtypes = [v, v, i, v, i, f, f32, f32, f32, i, i, i, i, v, v]
         L.sdfc_sdf_grid_layout.argtypes = [d, i, ctypes.c_double, i, P(i), d, d, d, f]
+        L.sdfc_batch_distance.argtypes = [v, d, d, d, d]
+        L.sdfc_batch_distance_device.argtypes = [v, v, v, v, v, v]
+        L.sdfc_grid_distance.argtypes = [v, i, d, i, d, d]
+        cp = ctypes.c_char_p
+        L.sdfc_sdf_save_text.argtypes = [cp, d, i, i, i, d, d, d]
+        L.sdfc_sdf_load_text.argtypes = [cp, P(i), d, d, d, d, ctypes.c_longlong]
+        L.sdfc_sdf_save_bricks.argtypes = [cp, d, i, i, i, d, d, d]
+        L.sdfc_sdf_load_bricks.argtypes = [cp, P(i), d, d, d, v, v]
+        L.sdfc_upload_grid_bricks.argtypes = [v, v, v, i, i, i, d, d, d, ctypes.c_double, P(i)]
         _lib = L
     return _lib
 
@@ -201,6 +213,32 @@ class Context:
                     "sdfc_upload_grid")
         self._grid_shapes[h.value] = (nk, nj, ni)
         return h.value
+
+    def upload_grid_bricks(self, codes, so, shape, min_box, max_box, dx, col_th) -> int:
+        """sdfc_upload_grid_bricks: an FP16-brick grid from its codes and (scale, offset) pairs
+        (as f16_brick_encode / load_sdf_bricks give them); shape = (nk, nj, ni)."""
+        nk, nj, ni = shape
+        codes = np.ascontiguousarray(codes, np.uint16)
+        so = np.ascontiguousarray(so, np.float32)
+        nb = ((ni + 7) // 8) * ((nj + 7) // 8) * ((nk + 7) // 8)
+        if codes.size != nb * 512 or so.size != 2 * nb:
+            raise ValueError("codes / so do not match the grid's bricks")
+        h = ctypes.c_int()
+        self._check(lib().sdfc_upload_grid_bricks(self._h, codes.ctypes.data, so.ctypes.data, ni, nj, nk,
+                                                  _dp(_f64(min_box, 3)), _dp(_f64(max_box, 3)), _dp(_f64(dx, 3)),
+                                                  float(col_th), ctypes.byref(h)), "sdfc_upload_grid_bricks")
+        self._grid_shapes[h.value] = (nk, nj, ni)
+        return h.value
+
+    def grid_distance(self, grid: int, X, want_values=True):
+        """sdfc_grid_distance: SDFMesh::query_SDF at X (n, 3) in the grid's frame ->
+        (d (n,) or None, minimum)."""
+        Xc = _f64(X).reshape(-1, 3)
+        d = np.zeros(len(Xc)) if want_values else None
+        m = np.zeros(1)
+        self._check(lib().sdfc_grid_distance(self._h, int(grid), _dp(Xc), len(Xc), None if d is None else _dp(d),
+                                             _dp(m)), "sdfc_grid_distance")
+        return d, float(m[0])
 
     def grid_values(self, grid: int) -> np.ndarray:
         """The grid as the evaluations see it, (nk, nj, ni) (sdfc_grid_values)."""
@@ -309,6 +347,7 @@ class Batch:
             raise ValueError("points and grids must be equal-length 1-D handle arrays")
         self.ctx = ctx
         self.n = len(pts)
+        self._points = [int(x) for x in pts]
         self._h = ctypes.c_void_p()
         ctx._check(lib().sdfc_batch_create(ctx._h, self.n, _ip(pts), _ip(grd), ctypes.byref(self._h)),
                    "sdfc_batch_create")
@@ -320,6 +359,20 @@ class Batch:
 
     def set_derivative_mode(self, mode: int):
         self.ctx._check(lib().sdfc_batch_set_derivative_mode(self._h, int(mode)), "sdfc_batch_set_derivative_mode")
+
+    def distance(self, E_A, E_B, per_point=False):
+        """sdfc_batch_distance: each instance's minimum distance of A's points to B's grid (n,);
+        with per_point, also every point's distance (a list of n arrays, caller order)."""
+        n = self.n
+        mn = np.zeros(n)
+        counts = [self.ctx._npoints[p] for p in self._points]
+        d = np.zeros(max(1, sum(counts))) if per_point else None
+        self.ctx._check(lib().sdfc_batch_distance(self._h, _dp(_f64(E_A, 16 * n)), _dp(_f64(E_B, 16 * n)), _dp(mn),
+                                                  None if d is None else _dp(d)), "sdfc_batch_distance")
+        if not per_point:
+            return mn
+        off = np.concatenate([[0], np.cumsum(counts)])
+        return mn, [d[off[k]:off[k + 1]].copy() for k in range(n)]
 
     def evaluate(self, E_A, phi_A, E_B, phi_B, params, want_deriv=True):
         """Host arrays in, host arrays out: (fm[n,12], Km[n,12,12], Dm[n,12,12], n_active[n], status[n])."""
@@ -532,3 +585,62 @@ def sdf_grid_layout(V, dx, res):
     if rc != SDFC_OK:
         raise SdfcError(f"sdfc_sdf_grid_layout failed ({rc})")
     return tuple(shape), mn, mx, sp, org
+
+
+def save_sdf_text(path, values, min_box, max_box, dx):
+    """sdfc_sdf_save_text: the reference's .sdf text cache of a grid (values (nk, nj, ni))."""
+    v = _f64(values)
+    nk, nj, ni = v.shape
+    rc = lib().sdfc_sdf_save_text(str(path).encode(), _dp(v), ni, nj, nk, _dp(_f64(min_box, 3)),
+                                  _dp(_f64(max_box, 3)), _dp(_f64(dx, 3)))
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_save_text failed ({rc}): {path}")
+
+
+def load_sdf_text(path):
+    """sdfc_sdf_load_text: (values (nk, nj, ni), min_box, max_box, dx) of a .sdf text cache,
+    or None when the file does not open (as the reference's load_SDF reports)."""
+    shape = (ctypes.c_int * 3)()
+    mn, mx, dx = np.zeros(3), np.zeros(3), np.zeros(3)
+    rc = lib().sdfc_sdf_load_text(str(path).encode(), shape, _dp(mn), _dp(mx), _dp(dx), None, 0)
+    if rc == SDFC_ERR_NOT_FOUND:
+        return None
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_load_text failed ({rc}): {path}")
+    ni, nj, nk = shape
+    v = np.zeros((nk, nj, ni))
+    rc = lib().sdfc_sdf_load_text(str(path).encode(), shape, _dp(mn), _dp(mx), _dp(dx), _dp(v), v.size)
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_load_text failed ({rc}): {path}")
+    return v, mn, mx, dx
+
+
+def save_sdf_bricks(path, values, min_box, max_box, dx):
+    """sdfc_sdf_save_bricks: the binary FP16-brick cache of a grid (values (nk, nj, ni))."""
+    v = _f64(values)
+    nk, nj, ni = v.shape
+    rc = lib().sdfc_sdf_save_bricks(str(path).encode(), _dp(v), ni, nj, nk, _dp(_f64(min_box, 3)),
+                                    _dp(_f64(max_box, 3)), _dp(_f64(dx, 3)))
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_save_bricks failed ({rc}): {path}")
+
+
+def load_sdf_bricks(path):
+    """sdfc_sdf_load_bricks: (codes, so, shape (nk, nj, ni), min_box, max_box, dx), or None when the
+    file does not open."""
+    shape = (ctypes.c_int * 3)()
+    mn, mx, dx = np.zeros(3), np.zeros(3), np.zeros(3)
+    rc = lib().sdfc_sdf_load_bricks(str(path).encode(), shape, _dp(mn), _dp(mx), _dp(dx), None, None)
+    if rc == SDFC_ERR_NOT_FOUND:
+        return None
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_load_bricks failed ({rc}): {path}")
+    ni, nj, nk = shape
+    nb = ((ni + 7) // 8) * ((nj + 7) // 8) * ((nk + 7) // 8)
+    codes = np.zeros(nb * 512, np.uint16)
+    so = np.zeros((nb, 2), np.float32)
+    rc = lib().sdfc_sdf_load_bricks(str(path).encode(), shape, _dp(mn), _dp(mx), _dp(dx), codes.ctypes.data,
+                                    so.ctypes.data)
+    if rc != SDFC_OK:
+        raise SdfcError(f"sdfc_sdf_load_bricks failed ({rc}): {path}")
+    return codes, so, (nk, nj, ni), mn, mx, dx

@@ -338,6 +338,55 @@ int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, int nk, con
                           const double* params, int want_deriv, double* fm, double* Km, double* Dm, int* n_active,
                           void* stream);
 
+/* ---------------------------------------------------------------- distances */
+
+/* Per instance of the batch, the reference's distance of each of body A's points (the
+ * instance's point set, body frame, posed by E_A as Simulation::get_body_vertices poses mesh
+ * vertices, rm/Simulation.cpp:252-264) to body B's grid (posed by E_B), BodySDFObj::distance
+ * (rm/Body/BodySDFObj.cpp:207-213): the trilinear value at the point in B's frame plus B's
+ * col_th, FLT_MAX + col_th outside B's box; FP64, bit-identical.
+ * min_d (n doubles): each instance's minimum, +inf for an empty point set.  With A's mesh
+ * vertices as the point set this is Simulation::get_body_distance (rm/Simulation.cpp:276-296);
+ * two calls make body_in_contact (:298-303).  SDFMesh::distance / min_distance (rm/Mesh.cpp:
+ * 18-20, 143-198) are the case of identity poses and a grid uploaded with col_th = 0.
+ * d (may be NULL): every point's distance, instance after instance, each instance's points in
+ * the caller's order.  E_A, E_B: n row-major 4x4 poses each. */
+int sdfc_batch_distance(sdfc_batch* b, const double* E_A, const double* E_B, double* min_d, double* d);
+/* The same on device arrays, queued on `stream` (null: the context's stream). */
+int sdfc_batch_distance_device(sdfc_batch* b, const double* d_EA, const double* d_EB, double* d_min, double* d_d,
+                               void* stream);
+
+/* SDFMesh::distance (rm/Mesh.cpp:190-198) and min_distance (:18-20) on an uploaded grid: the
+ * trilinear value of SDFMesh::query_SDF (:143-188; FLT_MAX outside the box) at each of the n
+ * points X (n x 3 doubles, grid frame), FP64, bit-identical; the grid's col_th is not added.
+ * d (may be NULL): n values; min_d (may be NULL): their minimum (+inf for n = 0). */
+int sdfc_grid_distance(sdfc_context* ctx, int grid, const double* X, int n, double* d, double* min_d);
+
+/* ---------------------------------------------------------------- grid files */
+
+/* The reference's .sdf text cache (BodySDFObj::save_SDF / load_SDF, rm/Body/BodySDFObj.cpp:
+ * 86-116; SDFMesh::save_SDF / load_SDF, rm/Mesh.cpp:103-135): the same text, byte for byte
+ * (std::ostream's default 6-significant-digit doubles, so the cache is lossy), and the same
+ * values on reading.  Host only.  load: with values NULL only the header (shape, boxes,
+ * spacing); else also capacity >= ni*nj*nk values.  SDFC_ERR_NOT_FOUND when the file does not
+ * open (the reference then builds the grid), SDFC_ERR_INVALID_ARGUMENT when it is malformed. */
+int sdfc_sdf_save_text(const char* path, const double* values, int ni, int nj, int nk, const double min_box[3],
+                       const double max_box[3], const double dxyz[3]);
+int sdfc_sdf_load_text(const char* path, int shape[3], double min_box[3], double max_box[3], double dxyz[3],
+                       double* values, long long capacity);
+/* A binary cache of FP16-brick grids (no reference counterpart; for SDFC_STORAGE_F16_BRICKS):
+ * save encodes the FP64 values with sdfc_f16_brick_encode; load returns the header and, if
+ * codes and so are not NULL, the codes and per-brick (scale, offset) exactly as saved (sized as
+ * for sdfc_f16_brick_encode), which sdfc_upload_grid_bricks uploads without re-encoding. */
+int sdfc_sdf_save_bricks(const char* path, const double* values, int ni, int nj, int nk, const double min_box[3],
+                         const double max_box[3], const double dxyz[3]);
+int sdfc_sdf_load_bricks(const char* path, int shape[3], double min_box[3], double max_box[3], double dxyz[3],
+                         unsigned short* codes, float* so);
+/* sdfc_upload_grid with SDFC_STORAGE_F16_BRICKS from already encoded bricks. */
+int sdfc_upload_grid_bricks(sdfc_context* ctx, const unsigned short* codes, const float* so, int ni, int nj, int nk,
+                            const double min_box[3], const double max_box[3], const double dxyz[3], double col_th,
+                            int* grid);
+
 /* ---------------------------------------------------------------- SDF grids from meshes */
 
 /* sdfgen::make_level_set3 (simulation/externals/sdfgen/makelevelset3.h:14-16,

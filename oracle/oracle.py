@@ -367,3 +367,18 @@ def make_level_set3(verts, tris, origin, dx, shape, exact_band=1) -> np.ndarray:
                           o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni, nj, nk, int(exact_band),
                           phi.ctypes.data_as(fp))
     return phi
+
+
+def body_distance(grid: Grid, E_from, E_to, V, per_point=False):
+    """Simulation::get_body_distance (rm/Simulation.cpp:276-296): the `to` body's grid, both
+    poses, the `from` body's vertices (n, 3) -> minimum (and every vertex's distance)."""
+    L = lib()
+    L.orc_body_distance.restype = ctypes.c_double
+    L.orc_body_distance.argtypes = [ctypes.POINTER(_Grid), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_double)]
+    g = grid._c()
+    v = _f64(V).reshape(-1, 3)
+    d = np.zeros(len(v))
+    m = L.orc_body_distance(ctypes.byref(g), _dp(_f64(E_from)), _dp(_f64(E_to)), _dp(v), len(v), _dp(d))
+    return (m, d) if per_point else m

@@ -18,6 +18,7 @@
 #include "CollisionDetection/CollisionDetection.h"
 #include "CollisionDetection/Contact.h"
 #include "makelevelset3.h"
+#include "Mesh.h"
 
 using namespace redmax;
 
@@ -383,6 +384,75 @@ int ref_make_level_set3(const float* verts, int nv, const unsigned* tris, int nt
             for (int i = 0; i < ni; ++i) phi[i + ni * (j + nj * k)] = out(i, j, k);
     return 0;
     HARNESS_CATCH
+}
+
+// redmax::SDFMesh (rm/Mesh.cpp:41-198): V nv x 3, F nt x 3 (the reference takes 3 x n).
+void* ref_sdfmesh_create(const double* V, int nv, const int* F, int nt, double dx, const char* load_path,
+                         const char* save_path) {
+    try {
+        Matrix3X Vm(3, nv);
+        Matrix3Xi Fm(3, nt);
+        for (int c = 0; c < nv; ++c)
+            for (int r = 0; r < 3; ++r) Vm(r, c) = V[3 * c + r];
+        for (int c = 0; c < nt; ++c)
+            for (int r = 0; r < 3; ++r) Fm(r, c) = F[3 * c + r];
+        return new SDFMesh(Vm, Fm, dx, load_path ? load_path : "", save_path ? save_path : "");
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void ref_sdfmesh_destroy(void* m) { delete static_cast<SDFMesh*>(m); }
+
+int ref_sdfmesh_shape(void* m, int* nijk, double* min_box, double* max_box, double* dxyz) {
+    auto* s = static_cast<SDFMesh*>(m);
+    nijk[0] = s->_SDF.ni;
+    nijk[1] = s->_SDF.nj;
+    nijk[2] = s->_SDF.nk;
+    for (int k = 0; k < 3; ++k) {
+        min_box[k] = s->_min_box[k];
+        max_box[k] = s->_max_box[k];
+    }
+    dxyz[0] = s->_dx;
+    dxyz[1] = s->_dy;
+    dxyz[2] = s->_dz;
+    return 0;
+}
+
+int ref_sdfmesh_values(void* m, double* values) {
+    auto* s = static_cast<SDFMesh*>(m);
+    std::memcpy(values, s->_SDF.a.data(), sizeof(double) * s->_SDF.a.size());
+    return 0;
+}
+
+// SDFMesh::distance of n points (n x 3) and min_distance
+int ref_sdfmesh_distance(void* m, const double* X, int n, double* d, double* min_d) {
+    HARNESS_TRY
+    auto* s = static_cast<SDFMesh*>(m);
+    Matrix3X Xm(3, n);
+    for (int c = 0; c < n; ++c)
+        for (int r = 0; r < 3; ++r) Xm(r, c) = X[3 * c + r];
+    VectorX dv = s->distance(Xm);
+    for (int c = 0; c < n; ++c) d[c] = dv(c);
+    *min_d = s->min_distance(Xm);
+    return 0;
+    HARNESS_CATCH
+}
+
+// Simulation::get_body_distance / body_in_contact (rm/Simulation.cpp:276-303)
+int ref_body_distance(void* sim, const char* from, const char* to, double* d) {
+    HARNESS_TRY
+    *d = static_cast<Simulation*>(sim)->get_body_distance(from, to);
+    return 0;
+    HARNESS_CATCH
+}
+
+int ref_body_in_contact(void* sim, const char* a, const char* b, double eps) {
+    try {
+        return static_cast<Simulation*>(sim)->body_in_contact(a, b, eps) ? 1 : 0;
+    } catch (...) {
+        return -1;
+    }
 }
 
 }  // extern "C"

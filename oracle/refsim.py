@@ -67,6 +67,14 @@ def lib():
         L.ref_sim_get_state.argtypes = [v, d, d]
         L.ref_sim_backward.argtypes = [v, d, i, d, d]
         L.ref_body_mesh.argtypes = [v, c, ctypes.POINTER(i), ctypes.POINTER(i), d, ctypes.POINTER(i)]
+        L.ref_sdfmesh_create.restype = v
+        L.ref_sdfmesh_create.argtypes = [d, i, ctypes.POINTER(i), i, ctypes.c_double, c, c]
+        L.ref_sdfmesh_destroy.argtypes = [v]
+        L.ref_sdfmesh_shape.argtypes = [v, ctypes.POINTER(i), d, d, d]
+        L.ref_sdfmesh_values.argtypes = [v, d]
+        L.ref_sdfmesh_distance.argtypes = [v, d, i, d, d]
+        L.ref_body_distance.argtypes = [v, c, c, d]
+        L.ref_body_in_contact.argtypes = [v, c, c, ctypes.c_double]
         f = ctypes.POINTER(ctypes.c_float)
         L.ref_make_level_set3.argtypes = [f, i, ctypes.POINTER(ctypes.c_uint), i, f, ctypes.c_float,
                                           ctypes.c_float, ctypes.c_float, i, i, i, i, f]
@@ -208,6 +216,18 @@ class RefSim:
                                    F.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), "mesh")
         return V, F
 
+    def body_distance(self, name_from, name_to):
+        """Simulation::get_body_distance (rm/Simulation.cpp:276-296)."""
+        out = np.zeros(1)
+        _check(lib().ref_body_distance(self._h, name_from.encode(), name_to.encode(), _dp(out)), "body_distance")
+        return float(out[0])
+
+    def body_in_contact(self, a, b, eps):
+        r = lib().ref_body_in_contact(self._h, a.encode(), b.encode(), float(eps))
+        if r < 0:
+            raise RuntimeError("reference harness: body_in_contact failed")
+        return bool(r)
+
     def set_pose(self, name, E, phi):
         _check(lib().ref_body_set_pose(self._h, name.encode(), _dp(_f64(E)), _dp(_f64(phi))), "set_pose")
 
@@ -289,3 +309,43 @@ def make_level_set3(verts, tris, origin, dx, shape, exact_band=1) -> np.ndarray:
                                  len(T), o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni, nj, nk,
                                  int(exact_band), phi.ctypes.data_as(fp)), "make_level_set3")
     return phi
+
+
+class RefSDFMesh:
+    """The reference's redmax::SDFMesh (rm/Mesh.cpp:41-198): V (nv, 3), F (nt, 3)."""
+
+    def __init__(self, V, F, dx, load_path="", save_path=""):
+        V = _f64(V).reshape(-1, 3)
+        F = np.ascontiguousarray(F, np.int32).reshape(-1, 3)
+        self._h = lib().ref_sdfmesh_create(_dp(V), len(V), F.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(F),
+                                           float(dx), load_path.encode(), save_path.encode())
+        if not self._h:
+            raise RuntimeError("reference SDFMesh construction failed")
+
+    def close(self):
+        if self._h:
+            lib().ref_sdfmesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def grid(self):
+        nijk = (ctypes.c_int * 3)()
+        mn, mx, dx = np.zeros(3), np.zeros(3), np.zeros(3)
+        lib().ref_sdfmesh_shape(self._h, nijk, _dp(mn), _dp(mx), _dp(dx))
+        ni, nj, nk = nijk
+        v = np.zeros((nk, nj, ni))
+        lib().ref_sdfmesh_values(self._h, _dp(v))
+        return v, mn, mx, dx
+
+    def distance(self, X):
+        """SDFMesh::distance and min_distance of X (n, 3)."""
+        X = _f64(X).reshape(-1, 3)
+        d = np.zeros(len(X))
+        m = np.zeros(1)
+        _check(lib().ref_sdfmesh_distance(self._h, _dp(X), len(X), _dp(d), _dp(m)), "sdfmesh_distance")
+        return d, float(m[0])

@@ -424,6 +424,31 @@ int orc_detect(const orc_grid* g, const double* E_A, const double* E_B, const do
     return cnt;
 }
 
+/* Simulation::get_body_distance (rm/Simulation.cpp:276-296): the `from` body's mesh vertices to
+ * world by get_body_vertices (:252-264), then the `to` body's distance() (BodySDFObj.cpp:207-213),
+ * minimised.  get_body_vertices evaluates (R2 * v + p2).eval() with a Matrix3 R2; in the reference's
+ * x86-64 build Eigen computes rows 0 and 1 of R2 * v as one SSE2 packet, ((r0 v0 + r1 v1) + r2 v2),
+ * and row 2 by its unrolled scalar reduction, r0 v0 + (r1 v1 + r2 v2); both are kept.  d_out
+ * (optional) receives every vertex's distance. */
+double orc_body_distance(const orc_grid* g, const double* E_from, const double* E_to, const double* V, int n,
+                         double* d_out) {
+    double R[9], p[3];
+    pose_split(E_from, R, p);
+    double m = INFINITY;
+    for (int i = 0; i < n; ++i) {
+        const double* v = V + 3 * i;
+        double xw[3];
+        xw[0] = (R[0] * v[0] + R[1] * v[1]) + R[2] * v[2];
+        xw[1] = (R[3] * v[0] + R[4] * v[1]) + R[5] * v[2];
+        xw[2] = R[6] * v[0] + (R[7] * v[1] + R[8] * v[2]);
+        for (int k = 0; k < 3; ++k) xw[k] += p[k];
+        const double d = orc_distance(g, E_to, xw);
+        if (d_out) d_out[i] = d;
+        if (d < m) m = d;
+    }
+    return m;
+}
+
 /* ------------------------------------------------------------------ forces */
 
 static void contact_kinematics(const double* E_A, const double* phi_A, const double* xi1, double* xw1,

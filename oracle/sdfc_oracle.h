@@ -60,6 +60,11 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
 double orc_pair_energy(const orc_grid* g, const double* pts, int n_pts, const double* E_A, const double* E_B,
                        const orc_params* prm, double* dE);
 
+/* Simulation::get_body_distance: min over the `from` body's vertices V (n x 3, body frame) of the
+ * `to` body's distance(), vertices posed as get_body_vertices computes them. */
+double orc_body_distance(const orc_grid* g, const double* E_from, const double* E_to, const double* V, int n,
+                         double* d_out);
+
 /* sdfgen::make_level_set3: the signed distance grid phi (ni*nj*nk floats, i fastest) of a closed
  * triangle mesh (verts: nv x 3 floats, tris: nt x 3 indices), grid origin and spacing, exact band. */
 void orc_make_level_set3(const float* verts, int nv, const unsigned* tris, int nt, const float* origin, float dx,
