@@ -15,6 +15,7 @@ struct sdfc_context {
     std::string err;
     std::vector<sdfc::GridDesc> grids;  // host copies of the descriptors
     std::vector<sdfc::PointsDesc> points;
+    std::vector<sdfc::HullDesc> hulls;  // convex hulls of the disassembly check
     std::vector<void*> allocations;  // every device allocation owned by the context
     sdfc::GridDesc* d_grids = nullptr;
     sdfc::PointsDesc* d_points = nullptr;

@@ -51,6 +51,15 @@ constexpr int kOutDeriv = 300;       // fm (12) + Km (144) + Dm (144)
 constexpr int kOutValue = 12;
 constexpr int kOutEnergy = 13;      // penetration energy + its 12 twist derivatives
 
+// A convex hull on the device (the planner's disassembly check): vertices (nv x 3) and facet
+// planes (nf x 4, n . x + offset <= 0 inside), with the vertices' bounds.
+struct HullDesc {
+    int nv, nf;
+    const double* v;
+    const double* planes;
+    double lo[3], hi[3];
+};
+
 // Fixed topology of one batch instance.
 struct InstanceDesc {
     int points;  // point-set handle (contact body A)

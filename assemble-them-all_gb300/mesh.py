@@ -90,3 +90,20 @@ class BodyDistance:
 def body_in_contact(d_ab, d_ba, eps) -> np.ndarray:
     """Simulation::body_in_contact (rm/Simulation.cpp:298-303) from the two directions' distances."""
     return np.minimum(d_ab, d_ba) < eps
+
+
+class DisassemblyCheck:
+    """PhysicsPlanner.is_disassembled (examples/run_joint_plan.py:291-302) for many poses at once.
+
+    ``vertices_move``: the moving part's mesh vertices in its body frame (get_body_vertices,
+    (n, 3)); ``vertices_still``: every still part's vertices in world (stacked, (m, 3)).  Both
+    hulls are built once, as the planner builds them in its constructor (:225-228);
+    ``__call__(E0i)`` takes poses (k, 4, 4) of the moving part and returns k booleans."""
+
+    def __init__(self, ctx, vertices_move, vertices_still):
+        self.ctx = ctx
+        self.hull_move = ctx.upload_hull(vertices_move)
+        self.hull_still = ctx.upload_hull(vertices_still)
+
+    def __call__(self, E0i, with_flags=False):
+        return self.ctx.disassembled(self.hull_move, self.hull_still, E0i, with_flags)

@@ -34,6 +34,7 @@ EXPORTS = (
     "sdfc_sim_set_tolerance", "sdfc_make_level_set3", "sdfc_make_level_set3_device", "sdfc_sdf_grid_layout",
     "sdfc_batch_distance", "sdfc_batch_distance_device", "sdfc_grid_distance", "sdfc_sdf_save_text",
     "sdfc_sdf_load_text", "sdfc_sdf_save_bricks", "sdfc_sdf_load_bricks", "sdfc_upload_grid_bricks",
+    "sdfc_upload_hull", "sdfc_disassembled", "sdfc_disassembled_device",
 )
 JOINT_TRANSLATIONAL = 3
 JOINT_FREE3D_EXP = 6
@@ -156,6 +157,9 @@ def lib():
         L.sdfc_sdf_save_bricks.argtypes = [cp, d, i, i, i, d, d, d]
         L.sdfc_sdf_load_bricks.argtypes = [cp, P(i), d, d, d, v, v]
         L.sdfc_upload_grid_bricks.argtypes = [v, v, v, i, i, i, d, d, d, ctypes.c_double, P(i)]
+        L.sdfc_upload_hull.argtypes = [v, d, i, d, i, P(i)]
+        L.sdfc_disassembled.argtypes = [v, i, i, d, i, P(i), P(i)]
+        L.sdfc_disassembled_device.argtypes = [v, i, i, v, i, v, v, v]
         _lib = L
     return _lib
 
@@ -239,6 +243,29 @@ class Context:
         self._check(lib().sdfc_grid_distance(self._h, int(grid), _dp(Xc), len(Xc), None if d is None else _dp(d),
                                              _dp(m)), "sdfc_grid_distance")
         return d, float(m[0])
+
+    def upload_hull(self, points) -> int:
+        """The convex hull of points (n, 3) for the disassembly check (sdfc_upload_hull): its
+        vertices and facet planes from qhull, as trimesh.convex.convex_hull builds it."""
+        from scipy.spatial import ConvexHull
+        pts = _f64(points).reshape(-1, 3)
+        hull = ConvexHull(pts)
+        verts = np.ascontiguousarray(pts[hull.vertices])
+        planes = np.ascontiguousarray(hull.equations, dtype=np.float64)
+        h = ctypes.c_int()
+        self._check(lib().sdfc_upload_hull(self._h, _dp(verts), len(verts), _dp(planes), len(planes),
+                                           ctypes.byref(h)), "sdfc_upload_hull")
+        return h.value
+
+    def disassembled(self, hull_move: int, hull_still: int, E, with_flags=False):
+        """sdfc_disassembled for poses E (n, 4, 4) of the moving part -> bool (n,) [, flags]."""
+        Ec = _f64(E).reshape(-1, 16)
+        n = len(Ec)
+        out = np.zeros(n, np.int32)
+        flags = np.zeros(n, np.int32)
+        self._check(lib().sdfc_disassembled(self._h, int(hull_move), int(hull_still), _dp(Ec), n, _ip(out),
+                                            _ip(flags)), "sdfc_disassembled")
+        return (out.astype(bool), flags) if with_flags else out.astype(bool)
 
     def grid_values(self, grid: int) -> np.ndarray:
         """The grid as the evaluations see it, (nk, nj, ni) (sdfc_grid_values)."""

@@ -362,6 +362,24 @@ int sdfc_batch_distance_device(sdfc_batch* b, const double* d_EA, const double* 
  * d (may be NULL): n values; min_d (may be NULL): their minimum (+inf for n = 0). */
 int sdfc_grid_distance(sdfc_context* ctx, int grid, const double* X, int n, double* d, double* min_d);
 
+/* ---------------------------------------------------------------- disassembly check */
+
+/* A convex hull for the planner's disassembly check: its vertices (nv x 3 doubles, the
+ * part's frame) and facet planes (nf x 4: unit normal n and offset o, n . x + o <= 0 inside,
+ * as qhull reports them; trimesh.convex.convex_hull in the reference).  Writes a handle. */
+int sdfc_upload_hull(sdfc_context* ctx, const double* verts, int nv, const double* planes, int nf, int* hull);
+/* PhysicsPlanner.is_disassembled (examples/run_joint_plan.py:291-302) for n poses E (n x 16,
+ * row-major E_0i) of the moving part: out[q] = 1 when the moving hull, posed, and the still hull
+ * (world frame) have no surface point in common (the reference's FCL mesh-mesh collision of
+ * the two hulls; for convex hulls: the solids meet and neither lies inside the other) and
+ * neither hull's axis-aligned box contains the other's.  FP64 GJK per pose; flags (may be
+ * NULL): bit 0 solids meet, bit 1 moving hull inside the still hull, bit 2 the reverse, bit 3
+ * box containment, bits 8.. GJK iterations. */
+int sdfc_disassembled(sdfc_context* ctx, int hull_move, int hull_still, const double* E, int n, int* out, int* flags);
+/* The same on device arrays, queued on `stream` (null: the context's stream). */
+int sdfc_disassembled_device(sdfc_context* ctx, int hull_move, int hull_still, const double* d_E, int n, int* d_out,
+                             int* d_flags, void* stream);
+
 /* ---------------------------------------------------------------- grid files */
 
 /* The reference's .sdf text cache (BodySDFObj::save_SDF / load_SDF, rm/Body/BodySDFObj.cpp:
