@@ -164,6 +164,16 @@ def lib():
     return _lib
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream named explicitly
+
+
+def torch_stream_handle(stream) -> int:
+    """The handle to pass for a torch stream.  torch's default stream has handle 0, which the
+    library reads as "the context's own stream"; name the legacy default stream instead."""
+    h = int(stream.cuda_stream)
+    return h if h else CUDA_STREAM_LEGACY
+
+
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
@@ -340,7 +350,7 @@ class Context:
         d = np.broadcast_to(np.asarray(dx, np.float32), (3,))
         ni, nj, nk = (int(x) for x in shape)
         phi = torch.empty((nk, nj, ni), dtype=torch.float32, device=V.device)
-        st = (stream or torch.cuda.current_stream(V.device)).cuda_stream
+        st = torch_stream_handle(stream or torch.cuda.current_stream(V.device))
         fp = ctypes.POINTER(ctypes.c_float)
         self._check(lib().sdfc_make_level_set3_device(self._h, V.data_ptr(), V.shape[0], T.data_ptr(), T.shape[0],
                                                       o.ctypes.data_as(fp), float(d[0]), float(d[1]), float(d[2]), ni,

@@ -381,6 +381,7 @@ def run_gpu(args, world, rank):
     c5_res = run_c5(args, sdfc, ctx, torch) if args.c5_points > 0 and rank == 0 else None
     c4_res = run_c4(args, sdfc, ctx, g, torch) if args.c4_instances > 0 and rank == 0 else None
     ls_res = run_levelset(args, sdfc, ctx, torch) if args.ls_segments > 0 and rank == 0 else None
+    pl_res = run_planner(args, sdfc, ctx, torch) if args.planner_states > 0 and rank == 0 else None
     if sim_res is not None:
         plain = run_sim_plain(args, sdfc, ctx, g, p, n)
         plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
@@ -442,6 +443,8 @@ def run_gpu(args, world, rank):
         line["differentiable_rollout"] = c4_res
     if ls_res is not None:
         line["sdf_construction"] = ls_res
+    if pl_res is not None:
+        line["planner_queries"] = pl_res
     print(json.dumps(line), flush=True)
 
 
@@ -648,13 +651,14 @@ def run_levelset(args, sdfc, ctx, torch):
     nodes = int(np.prod(shape))
     Vd = torch.tensor(np.asarray(V, np.float32), device="cuda")
     Fd = torch.tensor(np.asarray(F, np.int32), device="cuda")
-    st = torch.cuda.current_stream()
-    ctx.make_level_set3_device(Vd, Fd, origin, args.ls_dx, shape)  # warm-up
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    ctx.make_level_set3_device(Vd, Fd, origin, args.ls_dx, shape, stream=st)  # warm-up
     times = []
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        ctx.make_level_set3_device(Vd, Fd, origin, args.ls_dx, shape)
+        ctx.make_level_set3_device(Vd, Fd, origin, args.ls_dx, shape, stream=st)
         e1.record(st)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
@@ -679,6 +683,90 @@ def run_levelset(args, sdfc, ctx, torch):
                                "sample": f"same mesh on a {s2[0]}x{s2[1]}x{s2[2]} grid (spacing {args.ls_cpu_dx})"}
         out["speedup_vs_cpu"] = out["nodes_per_s"] / out["cpu_baseline"]["value"]
     return out
+
+
+def run_planner(args, sdfc, ctx, torch):
+    """Planner-side queries, batched: get_body_distance of a moving part's mesh vertices against a
+    still part's grid (the planner's collision_th set-up and body_in_contact) and the disassembly
+    check, for args.planner_states poses of a procedural assembly's mover.  Device arrays in and
+    out, CUDA events; the oracle's restatements timed on one core on a sample of poses."""
+    from oracle import disassembly as D
+    from oracle import oracle
+    mesh = importlib.import_module(f"{PKG}.mesh")
+    n = args.planner_states
+    asm = W.procedural_assembly(11, n_parts=6, points=(args.planner_vertices, args.planner_vertices), grids=(128,))
+    mover, still = asm.parts[0], asm.parts[1]
+    verts = mover.surface_points(args.planner_vertices, 21)
+    grid = still.grid(128)
+    gB = ctx.upload_grid(grid.values, grid.min_box, grid.max_box, grid.dx, 0.01, sdfc.STORAGE_F32)
+    rng = np.random.default_rng(12)
+    E = np.zeros((n, 4, 4))
+    for k in range(n):
+        # the mover around its assembled place (the parts' frames are translations)
+        E[k] = W.pose(W.rotvec_to_matrix(rng.normal(size=3) * 0.05), mover.position + rng.normal(size=3) * 0.3)
+    EB = np.tile(W.pose(np.eye(3), still.position), (n, 1, 1))
+    bd = mesh.BodyDistance(ctx, verts, gB, n)
+    dE = torch.tensor(E.reshape(n, 16), device="cuda")
+    dEB = torch.tensor(EB.reshape(n, 16), device="cuda")
+    dmin = torch.empty(n, dtype=torch.float64, device="cuda")
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    L = sdfc.lib()
+
+    def dist_call():
+        rc = L.sdfc_batch_distance_device(bd.batch._h, dE.data_ptr(), dEB.data_ptr(), dmin.data_ptr(), None,
+                                          st.cuda_stream)
+        assert rc == 0
+
+    still_verts = np.concatenate([p.surface_points(args.planner_vertices // 2, 30 + k) + p.position
+                                  for k, p in enumerate(asm.parts[1:])])
+    chk = mesh.DisassemblyCheck(ctx, verts, still_verts)
+    dout = torch.empty(n, dtype=torch.int32, device="cuda")
+    Ew = E
+    dEw = dE
+
+    def dis_call():
+        rc = L.sdfc_disassembled_device(ctx._h, chk.hull_move, chk.hull_still, dEw.data_ptr(), n, dout.data_ptr(),
+                                        None, st.cuda_stream)
+        assert rc == 0
+
+    def timed(fn, reps=5):
+        fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    dist_ms, dis_ms = timed(dist_call), timed(dis_call)
+    # the oracle on a sample of poses, one core
+    og = oracle.Grid(grid.values.astype(np.float32).astype(np.float64), grid.min_box, grid.max_box, grid.dx, 0.01)
+    m = min(n, args.planner_cpu_sample)
+    t = time.perf_counter()
+    ref_min = np.array([oracle.body_distance(og, E[k], EB[k], verts) for k in range(m)])
+    cpu_dist = m / (time.perf_counter() - t)
+    got_min = dmin.cpu().numpy()
+    oc = D.Checker(verts, still_verts)
+    md = min(n, max(8, args.planner_cpu_sample // 8))
+    t = time.perf_counter()
+    want = np.array([oc(Ew[k]) for k in range(md)])
+    cpu_dis = md / (time.perf_counter() - t)
+    got = dout.cpu().numpy().astype(bool)
+    return {"states": n, "mover_vertices": len(verts), "grid": "128^3 fp32",
+            "hull_vertices": {"move": int(len(oc.VA0)), "still": int(len(oc.VB))},
+            "body_distance": {"ms": dist_ms, "states_per_s": n / (dist_ms / 1e3),
+                              "vertex_queries_per_s": n * len(verts) / (dist_ms / 1e3),
+                              "bit_exact_vs_oracle_sample": bool(np.array_equal(got_min[:m], ref_min)),
+                              "cpu_baseline": {"value": cpu_dist, "unit": "states/s", "cores": 1, "kind": "port",
+                                               "sample": f"{m} poses"}},
+            "disassembly_check": {"ms": dis_ms, "states_per_s": n / (dis_ms / 1e3), "disassembled": int(got.sum()),
+                                  "agree_with_oracle_sample": int((got[:md] == want).sum()), "sample": md,
+                                  "cpu_baseline": {"value": cpu_dis, "unit": "states/s", "cores": 1, "kind": "port",
+                                                   "sample": f"{md} poses, LP feasibility (HiGHS)"}}}
 
 
 def run_c4(args, sdfc, ctx, g, torch):
@@ -778,6 +866,9 @@ def main():
     ap.add_argument("--c4-points", type=int, default=10000, help="differentiable-rollout leg: peg points")
     ap.add_argument("--c4-precision", choices=("mixed", "fp64"), default="mixed",
                     help="differentiable-rollout leg: precision of the force evaluations")
+    ap.add_argument("--planner-states", type=int, default=4096, help="planner-query leg: poses (0: skip the leg)")
+    ap.add_argument("--planner-vertices", type=int, default=20000, help="planner-query leg: mover mesh vertices")
+    ap.add_argument("--planner-cpu-sample", type=int, default=64, help="planner-query leg: poses timed on the CPU")
     ap.add_argument("--ls-segments", type=int, default=512,
                     help="SDF-construction leg: torus segments (x segments/2 quads; 0: skip the leg)")
     ap.add_argument("--ls-dx", type=float, default=0.0068, help="SDF-construction leg: grid spacing")
