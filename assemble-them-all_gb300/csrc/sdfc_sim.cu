@@ -20,6 +20,8 @@
 //                      bookkeeping, convergence.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -27,6 +29,7 @@
 
 #include "sdfc_internal.h"
 #include "sdfc_joint.cuh"
+#include "sdfc_joint_warp.cuh"
 
 using sdfc_impl::dev_alloc;
 using sdfc_impl::fail;
@@ -126,16 +129,15 @@ __global__ void sim_begin_kernel(int n, int nd, const MoverDev* __restrict__ mov
     st[i] = s;
 }
 
-__global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, const int* __restrict__ role,
-                                const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
-                                const SceneState* __restrict__ st, double* __restrict__ EA, double* __restrict__ phiA,
-                                double* __restrict__ EB, double* __restrict__ phiB, int* __restrict__ mode) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_pairs) return;
+// Poses of pair k (mover posed by its scene's current iterate) into evaluation slot j.
+__device__ inline void pose_pair(int k, int j, const int* __restrict__ pair_inst, const int* __restrict__ role,
+                                 const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
+                                 const SceneState* __restrict__ st, double* __restrict__ EA, double* __restrict__ phiA,
+                                 double* __restrict__ EB, double* __restrict__ phiB, int* __restrict__ mode) {
     const int i = pair_inst[k];
     const SceneState& s = st[i];
     if (s.phase == kDone) {
-        mode[k] = 0;
+        mode[j] = 0;
         return;
     }
     const MoverDev& m = mover[i];
@@ -143,10 +145,10 @@ __global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, 
     double qd[kMaxDof], E0i[16], phi[6];
     for (int c = 0; c < m.ndof; ++c) qd[c] = (p[c] - s.q0[c]) / m.h;
     mover_pose(m, p, qd, E0i, phi);
-    double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
-    double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
-    double *Ef = role[k] ? EB + 16 * (size_t)k : EA + 16 * (size_t)k;
-    double *pf = role[k] ? phiB + 6 * (size_t)k : phiA + 6 * (size_t)k;
+    double *Em = role[k] ? EA + 16 * (size_t)j : EB + 16 * (size_t)j;
+    double *pm = role[k] ? phiA + 6 * (size_t)j : phiB + 6 * (size_t)j;
+    double *Ef = role[k] ? EB + 16 * (size_t)j : EA + 16 * (size_t)j;
+    double *pf = role[k] ? phiB + 6 * (size_t)j : phiA + 6 * (size_t)j;
     for (int c = 0; c < 16; ++c) {
         Em[c] = E0i[c];
         Ef[c] = E_fixed[16 * (size_t)k + c];
@@ -155,7 +157,104 @@ __global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, 
         pm[c] = phi[c];
         pf[c] = 0.0;
     }
-    mode[k] = s.phase == kNewton ? 2 : 1;
+    mode[j] = s.phase == kNewton ? 2 : 1;
+}
+
+__global__ void sim_pose_kernel(int n_pairs, const int* __restrict__ pair_inst, const int* __restrict__ role,
+                                const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
+                                const SceneState* __restrict__ st, double* __restrict__ EA, double* __restrict__ phiA,
+                                double* __restrict__ EB, double* __restrict__ phiB, int* __restrict__ mode) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pairs) return;
+    pose_pair(k, k, pair_inst, role, E_fixed, mover, st, EA, phiA, EB, phiB, mode);
+}
+
+// ---------------------------------------------------------------- compacted rounds
+//
+// A batched Newton round waits for its slowest scene, and late in a step only a few scenes
+// still iterate.  The Newton kernels append every scene that stays active, its pairs and their
+// detection tiles to the next round's lists (double-buffered by round parity; order does not
+// matter: every pair is evaluated on its own).  A compacted round evaluates only the listed
+// pairs, in slots j = 0..count-1 of arrays sized for a capacity bucket chosen on the host from
+// the active count it reads between rounds (the count only falls within a step); slots past the
+// count are masked (mode 0), and tiles past the tile count point at the last slot, which is
+// always masked.
+
+struct CompactLists {
+    int* cnt;  // scenes, pairs, tiles
+    int* scene;
+    int* pair;
+    sdfc::InstanceDesc* inst;
+    int* tile;
+};
+
+// Appends scene i (still iterating) to the next round's lists.
+__device__ inline void append_active(int i, const int* __restrict__ pair_begin,
+                                     const sdfc::InstanceDesc* __restrict__ inst_full, CompactLists nx) {
+    const int k0 = pair_begin[i], k1 = pair_begin[i + 1];
+    int nt = 0;
+    for (int k = k0; k < k1; ++k) nt += inst_full[k].ntiles;
+    const int js = atomicAdd(nx.cnt + 0, 1);
+    nx.scene[js] = i;
+    int jp = atomicAdd(nx.cnt + 1, k1 - k0);
+    int tb = atomicAdd(nx.cnt + 2, nt);
+    for (int k = k0; k < k1; ++k, ++jp) {
+        sdfc::InstanceDesc d = inst_full[k];
+        d.tile0 = tb;
+        nx.pair[jp] = k;
+        nx.inst[jp] = d;
+        for (int t = 0; t < d.ntiles; ++t) nx.tile[tb + t] = jp;
+        tb += d.ntiles;
+    }
+}
+
+// Slots 0..Bp-1 of a compacted round: the listed pairs' poses and coefficients, masked slots
+// past the count; tiles past the tile count mapped to the masked last slot.
+__global__ void sim_pose_compact_kernel(int Bp, int Bt, const int* __restrict__ cnt, const int* __restrict__ pair_list,
+                                        int* __restrict__ tile_c, const int* __restrict__ pair_inst,
+                                        const int* __restrict__ role, const double* __restrict__ E_fixed,
+                                        const double* __restrict__ prm, const MoverDev* __restrict__ mover,
+                                        const SceneState* __restrict__ st, double* __restrict__ EA,
+                                        double* __restrict__ phiA, double* __restrict__ EB, double* __restrict__ phiB,
+                                        double* __restrict__ prm_c, int* __restrict__ mode) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < Bp) {
+        if (t >= cnt[1]) {
+            mode[t] = 0;
+            return;
+        }
+        const int k = pair_list[t];
+        for (int c = 0; c < 6; ++c) prm_c[6 * (size_t)t + c] = prm[6 * (size_t)k + c];
+        pose_pair(k, t, pair_inst, role, E_fixed, mover, st, EA, phiA, EB, phiB, mode);
+    } else if (t < Bp + Bt) {
+        const int tt = t - Bp;
+        if (tt >= cnt[2]) tile_c[tt] = Bp - 1;
+    }
+}
+
+// The compacted round's results back to the pairs' rows (fm always; Km, Dm where requested).
+__global__ void sim_scatter_kernel(const int* __restrict__ cnt, const int* __restrict__ pair_list,
+                                   const int* __restrict__ mode_c, const double* __restrict__ fm_c,
+                                   const double* __restrict__ Km_c, const double* __restrict__ Dm_c,
+                                   const int* __restrict__ nact_c, const int* __restrict__ status_c,
+                                   double* __restrict__ fm, double* __restrict__ Km, double* __restrict__ Dm,
+                                   int* __restrict__ nact, int* __restrict__ status) {
+    const int j = blockIdx.x;
+    if (j >= cnt[1]) return;
+    const int k = pair_list[j];
+    const bool deriv = mode_c[j] == 2;
+    for (int e = threadIdx.x; e < 300; e += blockDim.x) {
+        if (e < 12)
+            fm[12 * (size_t)k + e] = fm_c[12 * (size_t)j + e];
+        else if (deriv && e < 156)
+            Km[144 * (size_t)k + e - 12] = Km_c[144 * (size_t)j + e - 12];
+        else if (deriv)
+            Dm[144 * (size_t)k + e - 156] = Dm_c[144 * (size_t)j + e - 156];
+    }
+    if (threadIdx.x == 0) {
+        nact[k] = nact_c[j];
+        status[k] = status_c[j];
+    }
 }
 
 // n x n solve (n <= 6) by Gaussian elimination with partial pivoting (the algorithm of
@@ -284,9 +383,16 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
                                   const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
                                   const double* __restrict__ fm, const double* __restrict__ Km,
                                   const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining,
-                                  unsigned long long* evaluations) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                                  unsigned long long* evaluations, const int* __restrict__ scene_list,
+                                  const int* __restrict__ scene_cnt, const sdfc::InstanceDesc* __restrict__ inst_full,
+                                  CompactLists nx) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (scene_list) {
+        if (i >= *scene_cnt) return;
+        i = scene_list[i];
+    } else if (i >= n) {
+        return;
+    }
     SceneState s = st[i];
     if (s.phase == kDone) return;
     atomicAdd(evaluations, 1ull);
@@ -348,6 +454,111 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
     if (done) {
         s.phase = kDone;
         atomicSub(remaining, 1);
+    } else if (nx.cnt) {
+        append_active(i, pair_begin, inst_full, nx);
+    }
+    st[i] = s;
+}
+
+// sim_newton_kernel for free3d-exp movers with one warp per scene (one scene per CTA): the
+// contact sums and the reduced system are spread over the lanes (sdfc_joint_warp.cuh), lane 0
+// runs the 6x6 solve and the line-search bookkeeping as sim_newton_kernel does.
+__global__ void __launch_bounds__(32) sim_newton_free_warp_kernel(
+    int n, const int* __restrict__ pair_begin, const int* __restrict__ role, const MoverDev* __restrict__ mover,
+    const double* __restrict__ f_ext, const double* __restrict__ fm, const double* __restrict__ Km,
+    const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining, unsigned long long* evaluations,
+    const int* __restrict__ scene_list, const int* __restrict__ scene_cnt,
+    const sdfc::InstanceDesc* __restrict__ inst_full, CompactLists nx) {
+    __shared__ sdfc_joint::FreeWarp w;
+    int i = blockIdx.x;
+    const int lane = threadIdx.x;
+    if (scene_list) {
+        if (i >= *scene_cnt) return;
+        i = scene_list[i];
+    } else if (i >= n) {
+        return;
+    }
+    SceneState s = st[i];
+    if (s.phase == kDone) return;  // uniform over the warp
+    if (lane == 0) atomicAdd(evaluations, 1ull);
+    const MoverDev& m = mover[i];
+    const bool newton = s.phase == kNewton;
+    const double* p = newton ? s.x : s.xt;
+    // contact sums: the mover's 6-row block of every pair's fm, Km, Dm
+    const int k0 = pair_begin[i], k1 = pair_begin[i + 1];
+    for (int t = lane; t < 78; t += 32) {
+        if (t >= 6 && !newton) break;
+        double v = 0.0;
+        for (int k = k0; k < k1; ++k) {
+            const int o = role[k] ? 0 : 6;
+            if (t < 6) {
+                v += fm[12 * (size_t)k + o + t];
+            } else {
+                const int e = (t - 6) % 36, r = e / 6, c = e % 6;
+                const double* src = t < 42 ? Km : Dm;
+                v += src[144 * (size_t)k + (o + r) * 12 + o + c];
+            }
+        }
+        if (t < 6)
+            w.fmc[t] = v;
+        else if (t < 42)
+            w.Kmc[t - 6] = v;
+        else
+            w.Dmc[t - 42] = v;
+    }
+    __syncwarp();
+    sdfc_joint::free_system_w(free_body(m), f_ext + 6 * (size_t)i, s.q0, s.qd0, p, newton, w);
+    if (lane != 0) return;
+    const int nd = 6;
+    double g[6];
+    for (int k = 0; k < 6; ++k) g[k] = w.g[k];
+    bool done = false;
+    if (newton) {
+        double mg[kMaxDof], H[36];
+        for (int k = 0; k < 36; ++k) H[k] = w.H[k];
+        for (int k = 0; k < nd; ++k) mg[k] = -g[k];
+        solve_n(H, mg, nd, s.dx);
+        s.gnorm = norm_n(g, nd);
+        s.alpha = 1.0;
+        s.trial = 0;
+        for (int k = 0; k < nd; ++k) s.xt[k] = s.x[k] + s.dx[k];
+        s.phase = kLine;
+    } else {
+        const double gn = norm_n(g, nd);
+        bool step_done = false;
+        if (gn < s.gnorm) {
+            s.strike = 0;
+            for (int k = 0; k < nd; ++k) s.x[k] = s.xt[k];
+            step_done = true;
+        } else if (++s.trial < kMaxLineSearch) {
+            s.alpha *= 0.5;
+            for (int k = 0; k < nd; ++k) s.xt[k] = s.x[k] + s.alpha * s.dx[k];
+        } else {
+            s.alpha *= 0.5;
+            if (++s.strike >= kMaxStrike) {
+                done = true;
+            } else {
+                for (int k = 0; k < nd; ++k) s.x[k] = s.x[k] + s.alpha * s.dx[k];
+                step_done = true;
+            }
+        }
+        if (step_done) {
+            ++s.iter;
+            if (gn < m.tol) {
+                s.converged = 1;
+                done = true;
+            } else if (s.iter >= m.max_iter) {
+                done = true;
+            } else {
+                s.phase = kNewton;
+            }
+        }
+    }
+    if (done) {
+        s.phase = kDone;
+        atomicSub(remaining, 1);
+    } else if (nx.cnt) {
+        append_active(i, pair_begin, inst_full, nx);
     }
     st[i] = s;
 }
@@ -654,6 +865,9 @@ struct sdfc_sim {
     sdfc_context* ctx = nullptr;
     int n = 0, n_pairs = 0;
     int nd = 3;  // joint dofs of every mover (3 translational, 6 free3d-exp)
+    // free3d-exp Newton updates on one thread per scene instead of one warp (SDFC_FREE_NEWTON_THREAD
+    // set when the simulation is created; for comparing the two)
+    bool free_thread = false;
     sdfc_batch* batch = nullptr;
     std::vector<int> order;  // sorted pair k -> caller's pair index
     MoverDev* d_mover = nullptr;
@@ -669,9 +883,25 @@ struct sdfc_sim {
     int* h_remaining = nullptr;
     long long rounds = 0;
     std::vector<void*> allocations;
-    // one Newton round (pose, batched evaluation, Newton update) as a CUDA graph,
-    // captured at the first step and after a precision change
-    cudaGraphExec_t round_exec = nullptr;
+    // one Newton round (pose, batched evaluation, Newton update) as a CUDA graph per round
+    // parity, captured at the first step and after a precision change
+    cudaGraphExec_t round_exec[2] = {nullptr, nullptr};
+    // compacted rounds: the next round's lists ([2] by parity; counts d_cnt[3 parity + 0..2]:
+    // scenes, pairs, tiles), compact evaluation arrays, and one graph per capacity bucket and parity
+    int parity = 0;
+    int max_pairs_scene = 0, max_tiles_scene = 0;
+    int* d_cnt = nullptr;
+    int* d_scene_list[2] = {nullptr, nullptr};
+    int* d_pair_list[2] = {nullptr, nullptr};
+    sdfc::InstanceDesc* d_inst_c[2] = {nullptr, nullptr};
+    int* d_tile_c[2] = {nullptr, nullptr};
+    double *d_EA_c = nullptr, *d_phiA_c = nullptr, *d_EB_c = nullptr, *d_phiB_c = nullptr, *d_prm_c = nullptr;
+    int* d_mode_c = nullptr;
+    double *d_fm_c = nullptr, *d_Km_c = nullptr, *d_Dm_c = nullptr;
+    int *d_nact_c = nullptr, *d_status_c = nullptr;
+    std::vector<int> buckets;  // scene capacities, decreasing
+    std::vector<cudaGraphExec_t> compact_exec;  // [2 b + parity]
+    long long compact_rounds = 0;
     cudaStream_t capture_stream = nullptr;
     // adjoint: the recorded trajectory (step-major, (record_cap + 1) x n x 3), qdot_0,
     // dL/dq (n x T x 3), per-scene recursion state, gradients, reverse step counter
@@ -693,7 +923,10 @@ namespace sdfc_impl {
 
 void free_sim(sdfc_sim* s) {
     if (!s) return;
-    if (s->round_exec) cudaGraphExecDestroy(s->round_exec);
+    for (cudaGraphExec_t& g : s->round_exec)
+        if (g) cudaGraphExecDestroy(g);
+    for (cudaGraphExec_t g : s->compact_exec)
+        if (g) cudaGraphExecDestroy(g);
     if (s->back_exec) cudaGraphExecDestroy(s->back_exec);
     if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
     cudaFree(s->d_qhis);
@@ -750,6 +983,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     s->n = n;
     s->n_pairs = n_pairs;
     s->nd = nd;
+    s->free_thread = std::getenv("SDFC_FREE_NEWTON_THREAD") != nullptr;
     // pairs grouped by scene (stable), so each scene's pairs are contiguous
     s->order.resize(n_pairs);
     std::iota(s->order.begin(), s->order.end(), 0);
@@ -812,6 +1046,52 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         free_sim(s);
         return fail(ctx, SDFC_ERR_CUDA, "sim_create: cudaMallocHost failed");
     }
+    // compacted rounds: per-scene maxima of pairs and tiles, capacity buckets n/4, n/16, ...
+    if (n_pairs > 0) {
+        for (int i = 0; i < n; ++i) {
+            int tiles = 0;
+            for (int k = begin[i]; k < begin[i + 1]; ++k) tiles += s->batch->inst[k].ntiles;
+            s->max_pairs_scene = std::max(s->max_pairs_scene, begin[i + 1] - begin[i]);
+            s->max_tiles_scene = std::max(s->max_tiles_scene, tiles);
+        }
+        // SDFC_SIM_NO_COMPACT set at creation: full rounds only (for comparing the two)
+        const bool compact = std::getenv("SDFC_SIM_NO_COMPACT") == nullptr;
+        for (int b = n / 4; compact && b >= 1; b /= 4) {
+            const long long Bp = (long long)b * s->max_pairs_scene + 1, Bt = (long long)b * s->max_tiles_scene;
+            if (Bp <= n_pairs && Bt <= s->batch->total_tiles) s->buckets.push_back(b);
+            if (b < 8) break;
+        }
+        s->compact_exec.assign(2 * s->buckets.size(), nullptr);
+        const int tt = std::max(s->batch->total_tiles, 1);
+        if ((rc = alloc(s, &s->d_cnt, 6)) || (rc = alloc(s, &s->d_scene_list[0], n)) ||
+            (rc = alloc(s, &s->d_scene_list[1], n)) || (rc = alloc(s, &s->d_pair_list[0], n_pairs)) ||
+            (rc = alloc(s, &s->d_pair_list[1], n_pairs)) || (rc = alloc(s, &s->d_inst_c[0], n_pairs + 1)) ||
+            (rc = alloc(s, &s->d_inst_c[1], n_pairs + 1)) || (rc = alloc(s, &s->d_tile_c[0], tt)) ||
+            (rc = alloc(s, &s->d_tile_c[1], tt)) || (rc = alloc(s, &s->d_EA_c, 16 * (size_t)(n_pairs + 1))) ||
+            (rc = alloc(s, &s->d_phiA_c, 6 * (size_t)(n_pairs + 1))) ||
+            (rc = alloc(s, &s->d_EB_c, 16 * (size_t)(n_pairs + 1))) ||
+            (rc = alloc(s, &s->d_phiB_c, 6 * (size_t)(n_pairs + 1))) ||
+            (rc = alloc(s, &s->d_prm_c, 6 * (size_t)(n_pairs + 1))) || (rc = alloc(s, &s->d_mode_c, n_pairs + 1)) ||
+            (rc = alloc(s, &s->d_fm_c, 12 * (size_t)(n_pairs + 1))) ||
+            (rc = alloc(s, &s->d_Km_c, 144 * (size_t)(n_pairs + 1))) ||
+            (rc = alloc(s, &s->d_Dm_c, 144 * (size_t)(n_pairs + 1))) || (rc = alloc(s, &s->d_nact_c, n_pairs + 1)) ||
+            (rc = alloc(s, &s->d_status_c, n_pairs + 1))) {
+            free_sim(s);
+            return rc;
+        }
+        cudaError_t e0 = cudaMemset(s->d_cnt, 0, sizeof(int) * 6);
+        // the masked last slot of every bucket reads valid descriptors
+        for (int p = 0; p < 2 && e0 == cudaSuccess; ++p) {
+            std::vector<sdfc::InstanceDesc> fill(n_pairs + 1, s->batch->inst[0]);
+            for (auto& d : fill) d.ntiles = 0;
+            e0 = cudaMemcpy(s->d_inst_c[p], fill.data(), sizeof(sdfc::InstanceDesc) * fill.size(),
+                            cudaMemcpyHostToDevice);
+        }
+        if (e0 != cudaSuccess) {
+            free_sim(s);
+            return fail(ctx, SDFC_ERR_CUDA, std::string("sim_create: ") + cudaGetErrorString(e0));
+        }
+    }
     s->movers = md;
     cudaError_t e = cudaMemcpy(s->d_mover, md.data(), sizeof(MoverDev) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n_pairs > 0) {
@@ -851,9 +1131,18 @@ int sdfc_sim_set_precision(sdfc_sim* s, int precision) {
     if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
         return fail(s->ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_precision: unknown precision");
     if (s->batch) s->batch->precision = precision;
-    if (s->round_exec) {  // the captured rounds launch the old precision's kernels
-        cudaGraphExecDestroy(s->round_exec);
-        s->round_exec = nullptr;
+    if (s->round_exec[0] || s->round_exec[1] || !s->compact_exec.empty()) {
+        // the captured rounds launch the old precision's kernels
+        for (cudaGraphExec_t& g : s->round_exec)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+        for (cudaGraphExec_t& g : s->compact_exec)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
     }
     if (s->back_exec) {
         cudaGraphExecDestroy(s->back_exec);
@@ -905,12 +1194,35 @@ int sdfc_sim_set_external_force(sdfc_sim* s, const double* f) {
 
 namespace {
 
-// Enqueues one Newton round on `st`.
-int enqueue_round(sdfc_sim* s, cudaStream_t st) {
+CompactLists lists_of(sdfc_sim* s, int parity) {
+    if (!s->d_cnt) return CompactLists{nullptr, nullptr, nullptr, nullptr, nullptr};
+    return CompactLists{s->d_cnt + 3 * parity, s->d_scene_list[parity], s->d_pair_list[parity], s->d_inst_c[parity],
+                        s->d_tile_c[parity]};
+}
+
+void launch_newton(sdfc_sim* s, cudaStream_t st, int grid_scenes, const int* scene_list, const int* scene_cnt,
+                   CompactLists nx) {
+    const sdfc::InstanceDesc* inst_full = s->batch ? s->batch->d_inst : nullptr;
+    if (s->nd == 6 && !s->free_thread) {
+        sim_newton_free_warp_kernel<<<grid_scenes, 32, 0, st>>>(s->n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
+                                                                 s->d_fm, s->d_Km, s->d_Dm, s->d_state, s->d_remaining,
+                                                                 s->d_evals, scene_list, scene_cnt, inst_full, nx);
+    } else {
+        constexpr int ts = kSceneThreads;
+        sim_newton_kernel<<<(grid_scenes + ts - 1) / ts, ts, 0, st>>>(
+            s->n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext, s->d_fm, s->d_Km, s->d_Dm, s->d_state,
+            s->d_remaining, s->d_evals, scene_list, scene_cnt, inst_full, nx);
+    }
+}
+
+// Enqueues one Newton round over every scene on `st`; the still-active scenes are listed for
+// the next round (parity 1 - parity).
+int enqueue_round(sdfc_sim* s, cudaStream_t st, int parity) {
     const int n = s->n, np = s->n_pairs, tb = 128;
     sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
     in.mode = s->d_mode;
     sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
+    if (s->d_cnt) SDFC_CUDA_TRY(s->ctx, cudaMemsetAsync(s->d_cnt + 3 * (1 - parity), 0, 3 * sizeof(int), st));
     if (np > 0) {
         sim_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, s->d_pair_inst, s->d_role, s->d_Efixed, s->d_mover,
                                                           s->d_state, s->d_EA, s->d_phiA, s->d_EB, s->d_phiB,
@@ -918,30 +1230,70 @@ int enqueue_round(sdfc_sim* s, cudaStream_t st) {
         int rc = sdfc_impl::run_batch(s->batch, in, true, out, st);
         if (rc) return rc;
     }
-    constexpr int ts = kSceneThreads;
-    sim_newton_kernel<<<(n + ts - 1) / ts, ts, 0, st>>>(n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext, s->d_fm,
-                                                       s->d_Km, s->d_Dm, s->d_state, s->d_remaining, s->d_evals);
+    launch_newton(s, st, n, nullptr, nullptr, lists_of(s, 1 - parity));
     return SDFC_OK;
 }
 
-// Captures one round into a graph (replayed every round: its kernels skip the
-// scenes that are done, so replaying it is always correct).
-int capture_round(sdfc_sim* s) {
+// Enqueues one compacted round of capacity `cap` scenes reading the lists of `parity`.
+int enqueue_compact(sdfc_sim* s, cudaStream_t st, int parity, int cap) {
+    const int Bp = cap * s->max_pairs_scene + 1, Bt = cap * s->max_tiles_scene, tb = 128;
+    const int* cnt = s->d_cnt + 3 * parity;
+    SDFC_CUDA_TRY(s->ctx, cudaMemsetAsync(s->d_cnt + 3 * (1 - parity), 0, 3 * sizeof(int), st));
+    sim_pose_compact_kernel<<<(Bp + Bt + tb - 1) / tb, tb, 0, st>>>(
+        Bp, Bt, cnt, s->d_pair_list[parity], s->d_tile_c[parity], s->d_pair_inst, s->d_role, s->d_Efixed, s->d_prm,
+        s->d_mover, s->d_state, s->d_EA_c, s->d_phiA_c, s->d_EB_c, s->d_phiB_c, s->d_prm_c, s->d_mode_c);
+    sdfc_batch view = *s->batch;  // the batch's scratch, the compact instance and tile tables
+    view.d_inst = s->d_inst_c[parity];
+    view.d_tile_inst = s->d_tile_c[parity];
+    view.n = Bp;
+    view.total_tiles = Bt;
+    view.timing = false;
+    sdfc::BatchInputs in{s->d_EA_c, s->d_phiA_c, s->d_EB_c, s->d_phiB_c, s->d_prm_c};
+    in.mode = s->d_mode_c;
+    sdfc::BatchOutputs out{s->d_fm_c, s->d_Km_c, s->d_Dm_c, s->d_nact_c, s->d_status_c};
+    int rc = sdfc_impl::run_batch(&view, in, true, out, st);
+    if (rc) return rc;
+    sim_scatter_kernel<<<Bp, 128, 0, st>>>(cnt, s->d_pair_list[parity], s->d_mode_c, s->d_fm_c, s->d_Km_c, s->d_Dm_c,
+                                           s->d_nact_c, s->d_status_c, s->d_fm, s->d_Km, s->d_Dm, s->d_nact,
+                                           s->d_status);
+    launch_newton(s, st, cap, s->d_scene_list[parity], cnt, lists_of(s, 1 - parity));
+    return SDFC_OK;
+}
+
+// Captures a round into a graph (replayed every round of its kind: its kernels skip the
+// scenes that are done, so replaying it is always correct).  cap < 0: a full round.
+int capture_round(sdfc_sim* s, int parity, int cap, cudaGraphExec_t* exec) {
     sdfc_context* ctx = s->ctx;
     if (!s->capture_stream)
         SDFC_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;
     SDFC_CUDA_TRY(ctx, cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_round(s, s->capture_stream);
+    int rc = cap < 0 ? enqueue_round(s, s->capture_stream, parity) : enqueue_compact(s, s->capture_stream, parity, cap);
     cudaError_t e = cudaStreamEndCapture(s->capture_stream, &graph);
     if (rc) {
         if (graph) cudaGraphDestroy(graph);
         return rc;
     }
     if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("sim capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&s->round_exec, graph, 0);
+    e = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail(ctx, SDFC_ERR_CUDA, std::string("sim instantiate: ") + cudaGetErrorString(e));
+    return SDFC_OK;
+}
+
+// The graph of the next round: compacted to the smallest bucket that holds `active` scenes.
+int round_graph(sdfc_sim* s, int active, cudaGraphExec_t* out) {
+    const int p = s->parity;
+    int b = -1;
+    for (int k = 0; k < (int)s->buckets.size(); ++k)
+        if (s->buckets[k] >= active) b = k;
+    cudaGraphExec_t* slot = b < 0 ? &s->round_exec[p] : &s->compact_exec[2 * b + p];
+    if (!*slot) {
+        int rc = capture_round(s, p, b < 0 ? -1 : s->buckets[b], slot);
+        if (rc) return rc;
+    }
+    if (b >= 0) ++s->compact_rounds;
+    *out = *slot;
     return SDFC_OK;
 }
 
@@ -1166,7 +1518,6 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
     if (rc) return rc;
     if (s->record_cap > 0 && s->recorded + num_steps > s->record_cap)
         return fail(ctx, SDFC_ERR_CAPACITY, "sim_step: more steps than sdfc_sim_record's max_steps");
-    if (!s->round_exec && (rc = capture_round(s))) return rc;
     cudaStream_t st = ctx->stream;
     const int n = s->n;
     const int tb = 128;
@@ -1177,7 +1528,12 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
                                                           s->d_remaining);
         int active = n;
         for (int r = 0; r < max_rounds && active > 0; r += per_check) {
-            for (int k = 0; k < per_check; ++k) SDFC_CUDA_TRY(ctx, cudaGraphLaunch(s->round_exec, st));
+            for (int k = 0; k < per_check; ++k) {
+                cudaGraphExec_t g = nullptr;
+                if ((rc = round_graph(s, active, &g))) return rc;
+                SDFC_CUDA_TRY(ctx, cudaGraphLaunch(g, st));
+                s->parity ^= 1;
+            }
             SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_remaining, s->d_remaining, sizeof(int), cudaMemcpyDeviceToHost, st));
             SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
             s->rounds += per_check;

@@ -111,3 +111,72 @@ def test_mixed_joint_types_rejected(sdfc):
             ctx.sim([sdfc.Mover.make(1.0, np.ones(6), np.eye(4), 1e-3, joint=4)], pairs[:1])
     finally:
         ctx.close()
+
+
+def test_warp_newton_matches_thread_newton(sdfc, monkeypatch):
+    """The free-joint Newton update runs on one warp per scene (sdfc_joint_warp.cuh); the one-
+    thread version (selected by SDFC_FREE_NEWTON_THREAD at creation) computes the same entries
+    in the same order.  Both drive the same rollout: trajectories agree to round-off and the
+    Newton counts are identical."""
+    fx = load("sim_free.npz")
+    rng = np.random.default_rng(23)
+    n, T = 16, 12
+    F = np.zeros((n, 6))
+    F[:, :3] = rng.normal(size=(n, 3)) * 0.1
+    F[:, 3:] = rng.normal(size=(n, 3)) * 3.0
+    q0 = np.tile(fx["q0"], (n, 1)) + rng.normal(size=(n, 6)) * [0.004, 0.004, 0.05, 0.01, 0.01, 0.3]
+    q0[0, 3:] = 0.0  # the small-rotation branch of the exponential map
+    qd0 = rng.normal(size=(n, 6)) * [0.3, 0.3, 0.3, 0.5, 0.5, 0.5]
+    out = []
+    for thread in (False, True):
+        if thread:
+            monkeypatch.setenv("SDFC_FREE_NEWTON_THREAD", "1")
+        else:
+            monkeypatch.delenv("SDFC_FREE_NEWTON_THREAD", raising=False)
+        ctx = sdfc.Context(0)
+        try:
+            sim = make_sim(sdfc, ctx, fx, n=n, f_ext=F, q0=q0, qd0=qd0, joint=sdfc.JOINT_FREE3D_EXP)
+            sim.record(T)
+            conv = sim.step(T)
+            out.append((sim.history(), conv, sim.stats()))
+        finally:
+            ctx.close()
+    (qa, ca, sa), (qb, cb, sb) = out
+    np.testing.assert_allclose(qa, qb, rtol=0, atol=1e-12)
+    assert np.array_equal(ca, cb)
+    assert sa == sb
+
+
+@pytest.mark.parametrize("joint", ["free", "trans"])
+def test_compacted_rounds_match_full_rounds(sdfc, monkeypatch, joint):
+    """Late Newton rounds evaluate only the scenes still iterating (compacted rounds, sized by
+    capacity buckets).  Every pair's evaluation is independent of the others, so a rollout with
+    compaction is bit-identical to one with full rounds only (SDFC_SIM_NO_COMPACT)."""
+    fx = load("sim_free.npz" if joint == "free" else "sim_trans.npz")
+    nd = 6 if joint == "free" else 3
+    rng = np.random.default_rng(29)
+    n, T = 64, 8
+    F = np.zeros((n, 6))
+    F[:, 3:] = rng.normal(size=(n, 3)) * 3.0
+    q0 = np.tile(fx["q0"], (n, 1)) + rng.normal(size=(n, nd)) * 0.004
+    qd0 = rng.normal(size=(n, nd)) * 0.3
+    out = []
+    for compact in (True, False):
+        if compact:
+            monkeypatch.delenv("SDFC_SIM_NO_COMPACT", raising=False)
+        else:
+            monkeypatch.setenv("SDFC_SIM_NO_COMPACT", "1")
+        ctx = sdfc.Context(0)
+        try:
+            sim = make_sim(sdfc, ctx, fx, n=n, f_ext=F, q0=q0, qd0=qd0,
+                           joint=sdfc.JOINT_FREE3D_EXP if joint == "free" else sdfc.JOINT_TRANSLATIONAL)
+            sim.set_precision(sdfc.PRECISION_MIXED)
+            sim.record(T)
+            conv = sim.step(T)
+            out.append((sim.history(), conv, sim.stats()))
+        finally:
+            ctx.close()
+    (qa, ca, sa), (qb, cb, sb) = out
+    assert np.array_equal(qa, qb)
+    assert np.array_equal(ca, cb)
+    assert sa == sb
