@@ -71,13 +71,17 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     if (b->timing) cudaEventRecord(b->ev[0], stream);
-    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream);
+    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
+                        b->has_plain, b->has_bricks);
     if (b->timing) cudaEventRecord(b->ev[1], stream);
     if (in.mode) {
-        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, true, stencil, prec, stream);
-        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, false, stencil, prec, stream);
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, true, stencil, prec, stream,
+                           b->has_plain, b->has_bricks);
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, false, stencil, prec, stream,
+                           b->has_plain, b->has_bricks);
     } else {
-        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, deriv, stencil, prec, stream);
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, deriv, stencil, prec, stream,
+                           b->has_plain, b->has_bricks);
     }
     if (b->timing) cudaEventRecord(b->ev[2], stream);
     const sdfc::BatchInputs* q2 = sdfc::force_skips_q2(true, stencil, prec) ? &in : nullptr;
@@ -97,7 +101,8 @@ int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, doubl
     sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck};
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
-    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream);
+    sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
+                        b->has_plain, b->has_bricks);
     sdfc::launch_energy(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, stencil, prec, stream);
     sdfc::launch_energy_finalize(b->n, sc, energy, dE, in.mode, stream);
     CUDA_TRY(ctx, cudaGetLastError());
@@ -172,6 +177,8 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         tiles += nt;
     }
     b->total_tiles = tiles;
+    b->has_plain = b->has_bricks = false;
+    for (int k = 0; k < n; ++k) (ctx->grids[grids[k]].b16 ? b->has_bricks : b->has_plain) = true;
     auto alloc = [&](void** p, size_t bytes) { return dev_alloc(ctx, p, bytes); };
     if ((rc = alloc((void**)&b->d_inst, sizeof(InstanceDesc) * n)) ||
         (rc = alloc((void**)&b->d_tile_inst, sizeof(int) * std::max(tiles, 1))) ||

@@ -196,23 +196,33 @@ __device__ __forceinline__ float brick_value32(const GridDesc& g, int i, int j, 
     return fmaf(so.x, brick_code(g, b, i, j, k), so.y);
 }
 
-__device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, int k) {
-    if (g.b16) return brick_value64(g, i, j, k);
-    return __ldg(g.v64 + (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k));
+// The brick reads are kept out of line (results returned by value, in registers) so that the
+// hot loops over the FP64 array and the FP32 cell-corner array stay as small as without bricks.
+struct Corners32 {
+    float c[8];
+};
+static __device__ __noinline__ Corners32 brick_corners32(const GridDesc& g, int i, int j, int k) {
+    Corners32 r;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) r.c[q] = brick_value32(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+    return r;
+}
+static __device__ __noinline__ double brick_value64_cold(const GridDesc& g, int i, int j, int k) {
+    return brick_value64(g, i, j, k);
 }
 
-// FP16-brick corners, kept out of line so that the FP32 cell-corner path of the hot
-// kernels stays small.
-__device__ __noinline__ static void brick_corners32(const GridDesc& g, int i, int j, int k, float* c) {
-#pragma unroll
-    for (int q = 0; q < 8; ++q) c[q] = brick_value32(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+__device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, int k) {
+    if (g.b16) return brick_value64_cold(g, i, j, k);
+    return __ldg(g.v64 + (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k));
 }
 
 // The 8 corner values of cell (i, j, k), ordered c000, c100, c010, c110, c001, c101,
 // c011, c111: FP32 (from the cell-corner array or the bricks) and FP64.
 __device__ __forceinline__ void cell_corners32(const GridDesc& g, int i, int j, int k, float* c) {
     if (g.b16) {
-        brick_corners32(g, i, j, k, c);
+        const Corners32 r = brick_corners32(g, i, j, k);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) c[q] = r.c[q];
         return;
     }
     const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
@@ -220,10 +230,26 @@ __device__ __forceinline__ void cell_corners32(const GridDesc& g, int i, int j, 
     c[0] = lo.x; c[1] = lo.y; c[2] = lo.z; c[3] = lo.w;
     c[4] = hi.x; c[5] = hi.y; c[6] = hi.z; c[7] = hi.w;
 }
+// The cell-corner reads of FP64 / FP32 grids alone (no brick test), for code specialised on
+// grids without bricks.
+__device__ __forceinline__ void plain_corners32(const GridDesc& g, int i, int j, int k, float* c) {
+    const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
+    const float4 lo = __ldg(cq), hi = __ldg(cq + 1);
+    c[0] = lo.x; c[1] = lo.y; c[2] = lo.z; c[3] = lo.w;
+    c[4] = hi.x; c[5] = hi.y; c[6] = hi.z; c[7] = hi.w;
+}
+__device__ __forceinline__ void plain_corners64(const GridDesc& g, int i, int j, int k, double* c) {
+    const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
+    const size_t b = (size_t)i + sj * (size_t)j + sk * (size_t)k;
+    c[0] = __ldg(g.v64 + b);           c[1] = __ldg(g.v64 + b + 1);
+    c[2] = __ldg(g.v64 + b + sj);      c[3] = __ldg(g.v64 + b + sj + 1);
+    c[4] = __ldg(g.v64 + b + sk);      c[5] = __ldg(g.v64 + b + sk + 1);
+    c[6] = __ldg(g.v64 + b + sk + sj); c[7] = __ldg(g.v64 + b + sk + sj + 1);
+}
 __device__ __forceinline__ void cell_corners64(const GridDesc& g, int i, int j, int k, double* c) {
     if (g.b16) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) c[q] = brick_value64(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+        for (int q = 0; q < 8; ++q) c[q] = brick_value64_cold(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
         return;
     }
     const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
@@ -622,7 +648,8 @@ __device__ inline void warp_exact_jets(const GridDesc& g, const PairState<T>& S,
 // `valid == false` marks a padding lane: the grid is not read and the result
 // is discarded by the caller, but the lane still walks the same code so that
 // warp collectives downstream see every lane.
-template <typename T>
+// BR = false: specialised for grids without FP16 bricks (the caller guarantees it).
+template <typename T, bool BR = true>
 __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S, V3 xi, const FastCell* fc,
                                         bool want_hessian, bool valid, bool stencil_only, V3& x, double& d,
                                         SdfJet<T>& J, const ExactJet<T>* ej = nullptr) {
@@ -645,7 +672,10 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             const int i = fc->i, j = fc->j, k = fc->k;
             const double ud = fc->ud, vd = fc->vd, wd = fc->wd;
             double e[8];
-            cell_corners64(g, i, j, k, e);
+            if constexpr (BR)
+                cell_corners64(g, i, j, k, e);
+            else
+                plain_corners64(g, i, j, k, e);
             const double e000 = e[0], e100 = e[1], e010 = e[2], e110 = e[3];
             const double e001 = e[4], e101 = e[5], e011 = e[6], e111 = e[7];
             const double q0 = fma(ud, e100 - e000, e000), q1 = fma(ud, e110 - e010, e010);
@@ -657,7 +687,10 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             // FP32 analytic derivatives of the cell's interpolant
             const float u = (float)ud, v = (float)vd, w = (float)wd;
             float cc[8];
-            cell_corners32(g, i, j, k, cc);
+            if constexpr (BR)
+                cell_corners32(g, i, j, k, cc);
+            else
+                plain_corners32(g, i, j, k, cc);
             const float c000 = cc[0], c100 = cc[1], c010 = cc[2], c110 = cc[3];
             const float c001 = cc[4], c101 = cc[5], c011 = cc[6], c111 = cc[7];
             const float a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;
@@ -694,13 +727,13 @@ struct ContactEnergy {
     Vec3<T> aw, av, bw, bv;
 };
 
-template <typename T>
+template <typename T, bool BR = true>
 __device__ inline ContactEnergy<T> contact_energy(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
                                                   bool valid, bool stencil_only, const ExactJet<T>* ej = nullptr) {
     V3 xd;
     double dd;
     SdfJet<T> J;
-    contact_geometry(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
+    contact_geometry<T, BR>(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
     ContactEnergy<T> E;
     const double kn = S.cp.kn;
     E.e = valid ? 0.5 * kn * dd * dd : 0.0;
@@ -747,13 +780,13 @@ struct ContactForce {
     Vec3<T> xi1, xi2, f1, f2;
 };
 
-template <typename T>
+template <typename T, bool BR = true>
 __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
                                                 bool valid, bool stencil_only, const ExactJet<T>* ej = nullptr) {
     V3 xd;
     double dd;
     SdfJet<T> J;
-    contact_geometry(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
+    contact_geometry<T, BR>(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;
@@ -802,7 +835,7 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
 // sink.force(xi1, f1, xi2, f2) receives the force; then, for each of the 24
 // columns c (0-5: dq1, 6-11: dq2 -> Km columns; 12-17: dphi1, 18-23: dphi2 ->
 // Dm columns), sink.column(c, N1, N2, T2) receives the column's factors.
-template <typename T, class Sink>
+template <typename T, class Sink, bool BR = true>
 __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
                                               Sink& sink, bool valid, bool stencil_only,
                                               const ExactJet<T>* ej = nullptr, bool skip_q2 = false) {
@@ -810,7 +843,7 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     V3 xd;
     double dd;
     SdfJet<T> J;
-    contact_geometry(g, S, xi1d, fc, true, valid, stencil_only, xd, dd, J, ej);
+    contact_geometry<T, BR>(g, S, xi1d, fc, true, valid, stencil_only, xd, dd, J, ej);
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;

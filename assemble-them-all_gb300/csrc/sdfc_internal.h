@@ -45,6 +45,7 @@ struct sdfc_batch {
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
     long long* d_point_offset = nullptr;  // n: first output row of each instance's per-point distances
+    bool has_plain = true, has_bricks = false;  // instances on FP64/FP32 grids, on FP16-brick grids
     long long total_points = 0;
     // staging of the host-array entry points
     double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm

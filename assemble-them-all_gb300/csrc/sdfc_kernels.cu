@@ -101,6 +101,25 @@ __device__ __forceinline__ double exact_distance(const GridDesc& g, const Pose& 
 }
 
 // ------------------------------------------------------------------ detection
+// One instantiation per grid storage: BRICKS = false reads the FP32 cell-corner array,
+// BRICKS = true the FP16 bricks (with the grid descriptor in shared memory).  A batch launches
+// the ones its grids need; each leaves the other kind's tiles alone, so the plain kernel keeps
+// the registers and shared memory of a brick-free build.
+template <bool BRICKS>
+struct DetectGrid;
+template <>
+struct DetectGrid<false> {
+    __device__ __forceinline__ void set(const GridDesc&) {}
+    __device__ __forceinline__ const GridDesc* get() { return nullptr; }
+};
+template <>
+struct DetectGrid<true> {
+    GridDesc gd;
+    __device__ __forceinline__ void set(const GridDesc& g) { gd = g; }
+    __device__ __forceinline__ const GridDesc* get() { return &gd; }
+};
+
+template <bool BRICKS>
 __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDesc* __restrict__ inst,
                                                                 const int* __restrict__ tile_inst,
                                                                 const Prefilter* __restrict__ pref,
@@ -110,7 +129,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                                                                 int* __restrict__ tile_queue,
                                                                 const int* __restrict__ mode) {
     __shared__ Prefilter f;
-    __shared__ GridDesc gd;
+    __shared__ DetectGrid<BRICKS> dg;
     __shared__ const float4* gv;
     __shared__ const float* px;
     __shared__ int gn[3], pn;
@@ -127,11 +146,12 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         return;
     }
     const InstanceDesc I = inst[i];
+    if ((grids[I.grid].b16 != nullptr) != BRICKS) return;  // the other storage's kernel handles this tile
     if (tid < (int)(sizeof(Prefilter) / sizeof(float)))
         reinterpret_cast<float*>(&f)[tid] = reinterpret_cast<const float*>(pref + i)[tid];
     if (tid == 0) {
         const GridDesc& g = grids[I.grid];
-        gd = g;
+        dg.set(g);
         gv = g.cells32;
         gn[0] = g.ni;
         gn[1] = g.nj;
@@ -162,7 +182,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                 const bool surely_in = x >= f.lo_in[0] && x <= f.hi_in[0] && y >= f.lo_in[1] && y <= f.hi_in[1] &&
                                        z >= f.lo_in[2] && z <= f.hi_in[2];
                 if (surely_in) {
-                    const float d32 = trilinear32(gv, gd.b16 ? &gd : nullptr, gn[0], gn[1], gn[2], f, x, y, z) + f.col_th;
+                    const float d32 = trilinear32(gv, dg.get(), gn[0], gn[1], gn[2], f, x, y, z) + f.col_th;
                     if (fabsf(d32) <= f.guard)
                         queue = true;
                     else
@@ -436,13 +456,16 @@ constexpr int force_min_blocks() {
     return std::is_same<T, float>::value ? SDFC_FORCE_MIN_BLOCKS : 1;
 }
 
-template <bool DERIV, bool STENCIL, typename T>
+// BR = false: the FP32 fast path specialised for grids without FP16 bricks.  skip: 0 none,
+// 1 instances on brick grids, 2 instances on other grids (when a batch has both kinds, the two
+// instantiations split its instances).
+template <bool DERIV, bool STENCIL, typename T, bool BR = true>
 __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(const InstanceDesc* __restrict__ inst, BatchInputs in,
                                                        const GridDesc* __restrict__ grids,
                                                        const PointsDesc* __restrict__ points,
                                                        const int* __restrict__ ids,
                                                        const int* __restrict__ tile_count,
-                                                       double* __restrict__ partial) {
+                                                       double* __restrict__ partial, int skip) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     constexpr int NW = kChunk / 32;
     // FP32 algebra: contacts whose derivative stencil leaves the cell take the
@@ -457,6 +480,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const InstanceDesc I = inst[i];
+    if (skip && (grids[I.grid].b16 != nullptr) == (skip == 1)) return;  // the other instantiation's instance
     if (warp == 0) {
         // inclusive prefix of the instance's tile counts, 32 tiles at a time
         int run = 0;
@@ -512,9 +536,9 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             }
             WarpSink<NV, T> sink{acc + warp * NV, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
             if constexpr (DERIV) {
-                contact_force_jacobian<T>(g, xi, S, fcp, sink, valid, STENCIL, ejp, kWarpExact);
+                contact_force_jacobian<T, WarpSink<NV, T>, BR>(g, xi, S, fcp, sink, valid, STENCIL, ejp, kWarpExact);
             } else {
-                ContactForce<T> F = contact_force<T>(g, xi, S, fcp, valid, STENCIL, ejp);
+                ContactForce<T> F = contact_force<T, BR>(g, xi, S, fcp, valid, STENCIL, ejp);
                 sink.force(F.xi1, F.f1, F.xi2, F.f2);
             }
         }
@@ -716,24 +740,40 @@ __global__ void zero_status_kernel(int* status, int n) {
 
 template <bool DERIV, bool STENCIL>
 void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, const InstanceDesc* d_inst,
-                    BatchInputs in, const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s) {
-    if (precision == kMixed)
+                    BatchInputs in, const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s,
+                    bool plain, bool bricks) {
+    if (precision == kMixed && !STENCIL) {  // the FP32 fast path: specialised for brick-free grids
+        if (plain)
+            force_kernel<DERIV, STENCIL, float, false><<<grid, kChunk, 0, stream>>>(
+                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, bricks ? 1 : 0);
+        if (bricks)
+            force_kernel<DERIV, STENCIL, float, true><<<grid, kChunk, 0, stream>>>(
+                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, plain ? 2 : 0);
+    } else if (precision == kMixed) {
         force_kernel<DERIV, STENCIL, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                         s.tile_count, s.partial);
-    else
+                                                                         s.tile_count, s.partial, 0);
+    } else {
         force_kernel<DERIV, STENCIL, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                          s.tile_count, s.partial);
+                                                                          s.tile_count, s.partial, 0);
+    }
 }
 
 }  // namespace
 
 void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
-                   const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream) {
+                   const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream,
+                   bool plain, bool bricks) {
     if (n_inst <= 0) return;
     prep_kernel<<<(n_inst + 127) / 128, 128, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter);
     if (total_tiles <= 0) return;
-    detect_kernel<<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids, d_points,
-                                                              s.ids, s.tile_count, s.tile_queue, in.mode);
+    if (plain)
+        detect_kernel<false><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
+                                                                         d_points, s.ids, s.tile_count, s.tile_queue,
+                                                                         in.mode);
+    if (bricks)
+        detect_kernel<true><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
+                                                                        d_points, s.ids, s.tile_count, s.tile_queue,
+                                                                        in.mode);
     recheck_kernel<<<total_tiles, 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points, s.ids, s.tile_count,
                                                    s.tile_queue, s.recheck);
 }
@@ -761,19 +801,22 @@ void launch_grid_query(const GridDesc* d_grids, int grid, const double* X, int n
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, bool plain, bool bricks) {
     if (n_inst <= 0) return;
     dim3 grid(kSlots, n_inst);
     if (deriv) {
         if (stencil)
-            launch_force_t<true, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+            launch_force_t<true, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain, bricks);
         else
-            launch_force_t<true, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+            launch_force_t<true, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain,
+                                        bricks);
     } else {
         if (stencil)
-            launch_force_t<false, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+            launch_force_t<false, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain,
+                                        bricks);
         else
-            launch_force_t<false, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s);
+            launch_force_t<false, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain,
+                                         bricks);
     }
 }
 

@@ -110,12 +110,14 @@ struct BatchScratch {
 
 enum Precision { kFP64 = 0, kMixed = 1 };
 
+// plain / bricks: whether the batch has instances on FP64-or-FP32 grids / on FP16-brick grids.
 void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
-                   const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream);
+                   const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream,
+                   bool plain = true, bool bricks = true);
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
-                  cudaStream_t stream);
+                  cudaStream_t stream, bool plain = true, bool bricks = true);
 
 // Zeroes the status words, then finalizes.  With in.mode set, only the
 // instances whose request matches `deriv` are finalized (zero_status = false

@@ -365,6 +365,43 @@ def test_f16_bricks_against_oracle(sdfc, ctx, oracle, workloads, precision):
     b.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("stencil", [0, 1])
+def test_mixed_storage_batch(sdfc, ctx, workloads, precision, stencil):
+    """One batch over an FP32 grid, an FP64 grid and an FP16-brick grid: the kernels specialised
+    on brick-free grids and the general ones split the instances; every instance equals its
+    evaluation in a batch of its own storage alone (bit for bit)."""
+    rng = np.random.default_rng(31)
+    g = workloads.socket_grid(40, dtype=np.float64)
+    hs = [ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, st) for st in (1, 0, sdfc.STORAGE_F16_BRICKS)]
+    ph = ctx.upload_points(workloads.peg_points(4000, seed=13), 1)
+    n = 9
+    grids = [hs[k % 3] for k in range(n)]
+    ang = rng.uniform(0, 2 * np.pi, n)
+    EA = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.003),
+                                  [0.025 * np.cos(a), 0.025 * np.sin(a), 0.3 * rng.normal()]) for a in ang])
+    EB = np.tile(np.eye(4), (n, 1, 1))
+    phiA = rng.normal(size=(n, 6)) * 0.2
+    phiB = np.zeros((n, 6))
+    prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0) for _ in range(n)]
+
+    def run(idx):
+        b = ctx.batch([ph] * len(idx), [grids[k] for k in idx])
+        b.set_precision(precision)
+        b.set_derivative_mode(stencil)
+        out = b.evaluate(EA[idx], phiA[idx], EB[idx], phiB[idx], [prm[k] for k in idx], want_deriv=True)
+        b.close()
+        return out
+
+    fm, Km, Dm, nact, _ = run(list(range(n)))
+    assert (nact > 0).all()
+    for kind in range(3):
+        idx = [k for k in range(n) if k % 3 == kind]
+        f1, K1, D1, n1, _ = run(idx)
+        assert np.array_equal(fm[idx], f1) and np.array_equal(Km[idx], K1) and np.array_equal(Dm[idx], D1)
+        assert np.array_equal(nact[idx], n1)
+
+
 @pytest.mark.parametrize("precision,bar", [(0, 1e-10), (1, 1e-5)])
 def test_energy_against_oracle(sdfc, ctx, oracle, workloads, precision, bar):
     """Penetration energy (sdfc_batch_energy) and its twist gradient against the oracle's
