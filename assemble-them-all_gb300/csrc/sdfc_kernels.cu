@@ -133,8 +133,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
     __shared__ const float4* gv;
     __shared__ const float* px;
     __shared__ int gn[3], pn;
-    __shared__ int warp_act[kDetectThreads / 32], warp_q[kDetectThreads / 32];
-    __shared__ int base_act, base_q;
+    __shared__ int cnt_a[kTile / 32], cnt_q[kTile / 32];  // per (round, warp): counts, then offsets
     const int t = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int i = tile_inst[t];
@@ -158,8 +157,6 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         gn[2] = g.nk;
         px = points[I.points].x32;
         pn = points[I.points].n;
-        base_act = 0;
-        base_q = 0;
     }
     __syncthreads();
     const int n = pn;
@@ -167,8 +164,15 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
     const int count = min(kTile, n - first);
     int* out = ids + (size_t)t * kTile;
     const float* __restrict__ xs = px;
-    for (int r0 = 0; r0 < count; r0 += kDetectThreads) {
-        const int local = r0 + tid;
+    // classification of the tile's kRounds rounds of kDetectThreads points (several rounds' loads
+    // in flight), kept as per-thread bit masks; then the ordered compaction of all rounds
+    constexpr int kRounds = kTile / kDetectThreads;
+    constexpr int kWarps = kDetectThreads / 32;
+    static_assert(kRounds * kWarps == 64, "the compaction scan takes two (round, warp) counts per lane");
+    unsigned am = 0, qm = 0;
+#pragma unroll 4
+    for (int r = 0; r < kRounds; ++r) {
+        const int local = r * kDetectThreads + tid;
         const int sid = first + local;
         bool active = false, queue = false;
         if (local < count) {
@@ -192,37 +196,50 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                 }
             }
         }
-        // ordered compaction: ascending active stored indices from the start of
-        // the tile's slots, queued ones from the end (descending positions)
-        const unsigned ma = __ballot_sync(kFull, active), mq = __ballot_sync(kFull, queue);
-        if (lane == 0) {
-            warp_act[warp] = __popc(ma);
-            warp_q[warp] = __popc(mq);
-        }
-        __syncthreads();
-        int oa = base_act, oq = base_q;
-        for (int w = 0; w < warp; ++w) {
-            oa += warp_act[w];
-            oq += warp_q[w];
-        }
-        const unsigned below = (1u << lane) - 1u;
-        if (active) out[oa + __popc(ma & below)] = sid;
-        if (queue) out[kTile - 1 - (oq + __popc(mq & below))] = sid;
-        __syncthreads();
-        if (tid == 0) {
-            int sa = 0, sq = 0;
-            for (int w = 0; w < kDetectThreads / 32; ++w) {
-                sa += warp_act[w];
-                sq += warp_q[w];
-            }
-            base_act += sa;
-            base_q += sq;
-        }
-        __syncthreads();
+        am |= (unsigned)active << r;
+        qm |= (unsigned)queue << r;
     }
-    if (tid == 0) {
-        tile_count[t] = base_act;
-        tile_queue[t] = base_q;
+    // ordered compaction: ascending active stored indices from the start of the tile's slots,
+    // queued ones from the end (descending positions); order = round, warp, lane
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const unsigned ma = __ballot_sync(kFull, (am >> r) & 1u), mq = __ballot_sync(kFull, (qm >> r) & 1u);
+        if (lane == 0) {
+            cnt_a[r * kWarps + warp] = __popc(ma);
+            cnt_q[r * kWarps + warp] = __popc(mq);
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive prefix over the 64 (round, warp) counts, two per lane
+        const int a0 = cnt_a[2 * lane], a1 = cnt_a[2 * lane + 1];
+        const int q0 = cnt_q[2 * lane], q1 = cnt_q[2 * lane + 1];
+        int ia = a0 + a1, iq = q0 + q1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ua = __shfl_up_sync(kFull, ia, o), uq = __shfl_up_sync(kFull, iq, o);
+            if (lane >= o) {
+                ia += ua;
+                iq += uq;
+            }
+        }
+        const int ea = ia - (a0 + a1), eq = iq - (q0 + q1);
+        cnt_a[2 * lane] = ea;
+        cnt_a[2 * lane + 1] = ea + a0;
+        cnt_q[2 * lane] = eq;
+        cnt_q[2 * lane + 1] = eq + q0;
+        if (lane == 31) {
+            tile_count[t] = ia;
+            tile_queue[t] = iq;
+        }
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const unsigned ma = __ballot_sync(kFull, (am >> r) & 1u), mq = __ballot_sync(kFull, (qm >> r) & 1u);
+        const int sid = first + r * kDetectThreads + tid;
+        if ((am >> r) & 1u) out[cnt_a[r * kWarps + warp] + __popc(ma & below)] = sid;
+        if ((qm >> r) & 1u) out[kTile - 1 - (cnt_q[r * kWarps + warp] + __popc(mq & below))] = sid;
     }
 }
 
