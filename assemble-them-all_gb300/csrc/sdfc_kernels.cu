@@ -101,6 +101,11 @@ __device__ __forceinline__ double exact_distance(const GridDesc& g, const Pose& 
 }
 
 // ------------------------------------------------------------------ detection
+// rounds of a detection tile classified with their loads in flight together
+#ifndef SDFC_DETECT_UNROLL
+#define SDFC_DETECT_UNROLL 8
+#endif
+constexpr int kDetectUnroll = SDFC_DETECT_UNROLL;
 // One instantiation per grid storage: BRICKS = false reads the FP32 cell-corner array,
 // BRICKS = true the FP16 bricks (with the grid descriptor in shared memory).  A batch launches
 // the ones its grids need; each leaves the other kind's tiles alone, so the plain kernel keeps
@@ -170,7 +175,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
     constexpr int kWarps = kDetectThreads / 32;
     static_assert(kRounds * kWarps == 64, "the compaction scan takes two (round, warp) counts per lane");
     unsigned am = 0, qm = 0;
-#pragma unroll 4
+#pragma unroll kDetectUnroll
     for (int r = 0; r < kRounds; ++r) {
         const int local = r * kDetectThreads + tid;
         const int sid = first + local;
