@@ -56,6 +56,11 @@ struct sdfc_batch {
     int* h_int = nullptr;     // pinned
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // sdfc_batch_evaluate's device work (H2D of the staged inputs, the evaluation, D2H of the
+    // results) as a graph per derivative flag, with the modes it was captured under
+    cudaGraphExec_t eval_exec[2] = {nullptr, nullptr};
+    int eval_key[2] = {-1, -1};
+    cudaStream_t eval_stream = nullptr;
 };
 
 namespace sdfc_impl {

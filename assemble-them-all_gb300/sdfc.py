@@ -412,12 +412,18 @@ class Batch:
         return mn, [d[off[k]:off[k + 1]].copy() for k in range(n)]
 
     def evaluate(self, E_A, phi_A, E_B, phi_B, params, want_deriv=True):
-        """Host arrays in, host arrays out: (fm[n,12], Km[n,12,12], Dm[n,12,12], n_active[n], status[n])."""
+        """Host arrays in, host arrays out: (fm[n,12], Km[n,12,12], Dm[n,12,12], n_active[n], status[n]).
+        params: one Params for every instance, a sequence of n Params, or an (n, 6) array of
+        (kn, kt, mu, damping, scale, contact_scale) rows (sdfc_params' layout)."""
         n = self.n
-        prm = (Params * n)()
-        for k in range(n):
-            p = params[k] if isinstance(params, (list, tuple)) else params
-            prm[k] = p
+        if isinstance(params, Params):
+            rows = np.tile(params.as_row(), (n, 1))
+        elif isinstance(params, np.ndarray):
+            rows = params
+        else:
+            rows = np.array([p.as_row() for p in params])
+        rows = _f64(rows, (n, 6))
+        prm = rows.ctypes.data_as(ctypes.POINTER(Params))
         fm = np.zeros(12 * n)
         Km = np.zeros(144 * n) if want_deriv else np.zeros(1)
         Dm = np.zeros(144 * n) if want_deriv else np.zeros(1)

@@ -348,6 +348,7 @@ def run_gpu(args, world, rank):
     plain = ctx.batch([p], [g])
     plain.set_precision(sdfc.PRECISION_FP64)
     params_c = [sdfc.Params(*PARAMS)] * n
+    params_rows = np.tile(np.array(PARAMS, dtype=np.float64), (n, 1))  # sdfc_params rows, as a C caller holds them
     ref = [np.zeros((n, 12)), np.zeros((n, 12, 12)), np.zeros((n, 12, 12))]
     sample = min(n, args.plain_sample)
     plain_t = []
@@ -370,7 +371,7 @@ def run_gpu(args, world, rank):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        batch.evaluate(EA, phiA, EB, phiB, params_c, want_deriv=True)
+        batch.evaluate(EA, phiA, EB, phiB, params_rows, want_deriv=True)
         if k:
             e2e_t.append(time.perf_counter() - t)
     e2e_s = dist_max(float(np.mean(e2e_t)), world)
