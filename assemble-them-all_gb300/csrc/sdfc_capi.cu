@@ -70,7 +70,8 @@ void free_batch(sdfc_batch* b) {
 int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
               cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
-    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck};
+    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
+                         b->slots};
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     if (b->timing) cudaEventRecord(b->ev[0], stream);
@@ -101,7 +102,8 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
 
 int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, double* dE, cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
-    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck};
+    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
+                         b->slots};
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
@@ -157,6 +159,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     b->ctx = ctx;
     b->n = n;
     b->deriv_mode = ctx->deriv_mode;
+    b->slots = sdfc::slots_for(n);
     b->precision = ctx->precision;
     b->inst.resize(n);
     std::vector<int> tile_inst;
@@ -189,7 +192,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_tile_count, sizeof(int) * std::max(tiles, 1))) ||
         (rc = alloc((void**)&b->d_tile_queue, sizeof(int) * std::max(tiles, 1))) ||
         (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
-        (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * sdfc::kSlots * sdfc::kOutDeriv)) ||
+        (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * b->slots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||
         (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||

@@ -33,6 +33,7 @@ struct sdfc_batch {
     sdfc_context* ctx = nullptr;
     int n = 0;
     int total_tiles = 0;
+    int slots = 8;  // force CTAs (partial rows) per instance
     int deriv_mode = SDFC_DERIV_ANALYTIC;
     int precision = SDFC_PRECISION_FP64;
     std::vector<sdfc::InstanceDesc> inst;

@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
                                                        const PointsDesc* __restrict__ points,
                                                        const int* __restrict__ ids,
                                                        const int* __restrict__ tile_count,
-                                                       double* __restrict__ partial, int skip) {
+                                                       double* __restrict__ partial, int skip, int slots) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     constexpr int NW = kChunk / 32;
     // FP32 algebra: contacts whose derivative stencil leaves the cell take the
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     const int total = prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
     if (s < nchunks) {
-        for (int chunk = s; chunk < nchunks; chunk += kSlots) {
+        for (int chunk = s; chunk < nchunks; chunk += slots) {
             const int c = chunk * kChunk + tid;
             const bool valid = c < total;
             V3 xi = v3(0, 0, 0);
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
         }
     }
     __syncthreads();
-    double* row = partial + ((size_t)i * kSlots + s) * kOutDeriv;  // one row stride for both passes
+    double* row = partial + ((size_t)i * slots + s) * kOutDeriv;  // one row stride for both passes
     for (int k = tid; k < NV; k += kChunk) {
         double v = 0.0;
         for (int w = 0; w < NW; ++w) v += acc[w * NV + k].value();
@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
                                                         const PointsDesc* __restrict__ points,
                                                         const int* __restrict__ ids,
                                                         const int* __restrict__ tile_count,
-                                                        double* __restrict__ partial) {
+                                                        double* __restrict__ partial, int slots) {
     constexpr int NW = kChunk / 32;
     constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
     __shared__ Accum<T> acc[NW * 12];
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
     __syncthreads();
     const int total = prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
-    for (int chunk = s; chunk < nchunks; chunk += kSlots) {
+    for (int chunk = s; chunk < nchunks; chunk += slots) {
         const int c = chunk * kChunk + tid;
         const bool valid = c < total;
         V3 xi = v3(0, 0, 0);
@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
         if (lane == 0) eacc[warp] += e;
     }
     __syncthreads();
-    double* row = partial + ((size_t)i * kSlots + s) * kOutDeriv;
+    double* row = partial + ((size_t)i * slots + s) * kOutDeriv;
     for (int k = tid; k < kOutEnergy; k += kChunk) {
         double v = 0.0;
         if (k == 0)
@@ -668,14 +668,14 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
 }
 
 __global__ void energy_finalize_kernel(int n_inst, const double* __restrict__ partial, double* __restrict__ energy,
-                                       double* __restrict__ dE, const int* __restrict__ mode) {
+                                       double* __restrict__ dE, const int* __restrict__ mode, int slots) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)n_inst * kOutEnergy) return;
     const int i = (int)(idx / kOutEnergy), k = (int)(idx % kOutEnergy);
     if (mode && mode[i] == 0) return;
-    const double* p = partial + (size_t)i * kSlots * kOutDeriv + k;
+    const double* p = partial + (size_t)i * slots * kOutDeriv + k;
     double v = 0.0;
-    for (int s = 0; s < kSlots; ++s) v += p[(size_t)s * kOutDeriv];
+    for (int s = 0; s < slots; ++s) v += p[(size_t)s * kOutDeriv];
     if (k == 0)
         energy[i] = v;
     else
@@ -718,27 +718,27 @@ __device__ inline void adjoint_column(const double* EA, const double* EB, int j,
 template <bool DERIV>
 __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
                                 const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode,
-                                const double* __restrict__ EA, const double* __restrict__ EB) {
+                                const double* __restrict__ EA, const double* __restrict__ EB, int slots) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)n_inst * NV) return;
     const int i = (int)(idx / NV), k = (int)(idx % NV);
     if (mode && mode[i] != (DERIV ? 2 : 1)) return;
-    const double* p = partial + (size_t)i * kSlots * kOutDeriv + k;
+    const double* p = partial + (size_t)i * slots * kOutDeriv + k;
     double v = 0.0;
     if (DERIV && EA && k >= 12 && k < 156 && (k - 12) % 12 >= 6) {
         const int r = (k - 12) / 12, j = (k - 12) % 12 - 6;
-        const double* row = partial + (size_t)i * kSlots * kOutDeriv + 12 + 12 * r;  // Km row r, dq1 columns
+        const double* row = partial + (size_t)i * slots * kOutDeriv + 12 + 12 * r;  // Km row r, dq1 columns
         double km[6];
         for (int c = 0; c < 6; ++c) {
             km[c] = 0.0;
-            for (int s = 0; s < kSlots; ++s) km[c] += row[(size_t)s * kOutDeriv + c];
+            for (int s = 0; s < slots; ++s) km[c] += row[(size_t)s * kOutDeriv + c];
         }
         double top[3], bot[3];
         adjoint_column(EA + 16 * (size_t)i, EB + 16 * (size_t)i, j, top, bot);
         for (int c = 0; c < 3; ++c) v -= km[c] * top[c] + km[3 + c] * bot[c];
     } else {
-        for (int s = 0; s < kSlots; ++s) v += p[(size_t)s * kOutDeriv];
+        for (int s = 0; s < slots; ++s) v += p[(size_t)s * kOutDeriv];
     }
     if (k < 12)
         out.fm[12 * (size_t)i + k] = v;
@@ -767,16 +767,16 @@ void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, c
     if (precision == kMixed && !STENCIL) {  // the FP32 fast path: specialised for brick-free grids
         if (plain)
             force_kernel<DERIV, STENCIL, float, false><<<grid, kChunk, 0, stream>>>(
-                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, bricks ? 1 : 0);
+                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, bricks ? 1 : 0, s.slots);
         if (bricks)
             force_kernel<DERIV, STENCIL, float, true><<<grid, kChunk, 0, stream>>>(
-                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, plain ? 2 : 0);
+                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, plain ? 2 : 0, s.slots);
     } else if (precision == kMixed) {
         force_kernel<DERIV, STENCIL, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                         s.tile_count, s.partial, 0);
+                                                                         s.tile_count, s.partial, 0, s.slots);
     } else {
         force_kernel<DERIV, STENCIL, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                          s.tile_count, s.partial, 0);
+                                                                          s.tile_count, s.partial, 0, s.slots);
     }
 }
 
@@ -825,7 +825,7 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
                   cudaStream_t stream, bool plain, bool bricks) {
     if (n_inst <= 0) return;
-    dim3 grid(kSlots, n_inst);
+    dim3 grid(s.slots, n_inst);
     if (deriv) {
         if (stencil)
             launch_force_t<true, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain, bricks);
@@ -854,10 +854,10 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
     const double* EB = derive_q2 ? derive_q2->EB : nullptr;
     if (deriv)
         finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA,
-                                                              EB);
+                                                              EB, s.slots);
     else
         finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
-                                                               nullptr, nullptr);
+                                                               nullptr, nullptr, s.slots);
 }
 
 bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !stencil && precision == kMixed; }
@@ -865,21 +865,21 @@ bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !
 void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                    const PointsDesc* d_points, BatchScratch s, bool stencil, int precision, cudaStream_t stream) {
     if (n_inst <= 0) return;
-    dim3 grid(kSlots, n_inst);
+    dim3 grid(s.slots, n_inst);
     if (precision == kMixed) {
         if (stencil)
             energy_kernel<true, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids, s.tile_count,
-                                                                     s.partial);
+                                                                     s.partial, s.slots);
         else
             energy_kernel<false, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                      s.tile_count, s.partial);
+                                                                      s.tile_count, s.partial, s.slots);
     } else {
         if (stencil)
             energy_kernel<true, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                      s.tile_count, s.partial);
+                                                                      s.tile_count, s.partial, s.slots);
         else
             energy_kernel<false, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                       s.tile_count, s.partial);
+                                                                       s.tile_count, s.partial, s.slots);
     }
 }
 
@@ -887,7 +887,8 @@ void launch_energy_finalize(int n_inst, BatchScratch s, double* energy, double* 
                             cudaStream_t stream) {
     if (n_inst <= 0) return;
     const size_t total = (size_t)n_inst * kOutEnergy;
-    energy_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(n_inst, s.partial, energy, dE, mode);
+    energy_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(n_inst, s.partial, energy, dE, mode,
+                                                                                s.slots);
 }
 
 }  // namespace sdfc

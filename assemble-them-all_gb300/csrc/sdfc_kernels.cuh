@@ -19,7 +19,7 @@
 //                    simulation/redmax/CollisionDetection/CollisionDetection.cpp:124-147.
 //   force_kernel     one CTA per (instance, slot).  The instance's active
 //                    contacts are cut into chunks of kChunk; slot s takes chunks
-//                    s, s+kSlots, ...  Each thread evaluates one contact; the
+//                    s, s+slots, ...  Each thread evaluates one contact; the
 //                    per-contact force (12 values) and, with derivatives, the 24
 //                    Jacobian columns (288 values) are summed over the warp with
 //                    shuffles and over the CTA in FP64 shared memory, in a fixed
@@ -30,7 +30,7 @@
 //                    queries together, one contact at a time across its lanes
 //                    (warp_exact_jets), so that no lane runs the long FP64
 //                    stencil alone while 31 wait.
-//   finalize_kernel  sums the kSlots partial rows of each instance in order and
+//   finalize_kernel  sums the slots partial rows of each instance in order and
 //                    scatters them into fm / Km / Dm.
 //
 // No atomics touch the results: the sums are deterministic run to run.
@@ -45,7 +45,15 @@ namespace sdfc {
 constexpr int kTile = 2048;          // points per detection tile
 constexpr int kDetectThreads = 256;  // threads per detection CTA
 constexpr int kChunk = 128;          // contacts per force chunk = threads per force CTA
-constexpr int kSlots = 8;            // partial rows per instance
+constexpr int kMaxSlots = 32;        // partial rows per instance (force CTAs per instance), at most
+// Slots of a batch of n instances: about six waves of force CTAs on 152 SMs at 4 CTAs each
+// (measured: 4 for 1024 instances of 50k points, 16 for 256 of 1M).
+inline int slots_for(int n) {
+    constexpr int kTargetCtas = 152 * 4 * 6;
+    int s = 1;
+    while (s < kMaxSlots && (long long)s * n < kTargetCtas) s *= 2;
+    return s;
+}
 constexpr int kMaxTilesPerInstance = 4096;
 constexpr int kOutDeriv = 300;       // fm (12) + Km (144) + Dm (144)
 constexpr int kOutValue = 12;
@@ -104,8 +112,9 @@ struct BatchScratch {
     int* ids;                   // total_tiles x kTile: active stored indices, queued rechecks at the tail
     int* tile_count;            // total_tiles: active count per tile
     int* tile_queue;            // total_tiles: queued recheck count per tile
-    double* partial;            // n x kSlots x kOutDeriv
+    double* partial;            // n x slots x kOutDeriv
     unsigned long long* recheck;  // diagnostic counter of FP64 rechecks
+    int slots;                  // force CTAs (partial rows) per instance
 };
 
 enum Precision { kFP64 = 0, kMixed = 1 };
