@@ -458,15 +458,24 @@ struct WarpSink {
         T v[12] = {t1.x, t1.y, t1.z, f1.x, f1.y, f1.z, t2.x, t2.y, t2.z, f2.x, f2.y, f2.z};
         add12(v, 0, 1);
     }
-    // column c of [Km | Dm]: rows [xi1 x N1; N1; xi2 x N2 + T2; N2]
+    // column c of [Km | Dm]: rows [xi1 x N1; N1; xi2 x N2 + T2; N2].  The accumulators of Km and
+    // Dm are column-major (acc_index), so a column's 12 rows are 12 adjacent accumulators (no
+    // shared-memory bank conflicts); the kernel's epilogue writes the partial row in row-major order.
     __device__ __forceinline__ void column(int c, Vec3<T> N1, Vec3<T> N2, Vec3<T> T2) {
         if constexpr (NV == kOutDeriv) {
             const Vec3<T> r0 = cross(xi1, N1), r2 = cross(xi2, N2) + T2;
             T v[12] = {r0.x, r0.y, r0.z, N1.x, N1.y, N1.z, r2.x, r2.y, r2.z, N2.x, N2.y, N2.z};
-            add12(v, c < 12 ? 12 + c : 156 + (c - 12), 12);
+            add12(v, c < 12 ? 12 + 12 * c : 156 + 12 * (c - 12), 1);
         }
     }
 };
+
+// Accumulator of output k (fm, then Km and Dm row-major) in WarpSink's layout (Km, Dm column-major).
+__device__ __forceinline__ int acc_index(int k) {
+    if (k < 12) return k;
+    const int b = k < 156 ? 12 : 156, e = k - b;
+    return b + 12 * (e % 12) + e / 12;
+}
 
 // CTAs of the FP32 path resident per SM (its register budget is 65536 / (this x 128));
 // the FP64 path is left its full register budget.
@@ -568,8 +577,9 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     __syncthreads();
     double* row = partial + ((size_t)i * slots + s) * kOutDeriv;  // one row stride for both passes
     for (int k = tid; k < NV; k += kChunk) {
+        const int a = acc_index(k);
         double v = 0.0;
-        for (int w = 0; w < NW; ++w) v += acc[w * NV + k].value();
+        for (int w = 0; w < NW; ++w) v += acc[w * NV + a].value();
         row[k] = v;
     }
 }
