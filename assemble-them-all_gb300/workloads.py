@@ -116,6 +116,27 @@ def fibonacci_directions(n: int) -> np.ndarray:
     return np.stack([np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)], axis=-1)
 
 
+def direction_sweep_states(n, rank=0):
+    """The direction sweep of the planner (one instance per pull direction): the peg fully inserted
+    in the socket, shifted 0.0201 toward the direction's lateral part (pressed 1e-4 into the bore
+    wall past col_th 0.01), tilted 0.002 rad about the perpendicular axis, raised 0.25 d_z, moving
+    at 0.01 d.  Returns (E_A, phi_A, E_B, phi_B) for n instances (rank r takes the r-th block of
+    n directions of a Fibonacci sphere of n (r + 1) points)."""
+    dirs = fibonacci_directions(n * max(1, rank + 1))[rank * n:(rank + 1) * n] if rank else fibonacci_directions(n)
+    EA = np.zeros((n, 4, 4))
+    phiA = np.zeros((n, 6))
+    for k, d in enumerate(dirs):
+        lat = np.array([d[0], d[1], 0.0])
+        ln = np.linalg.norm(lat)
+        lat = lat / ln if ln > 1e-6 else np.array([1.0, 0.0, 0.0])
+        R = rotvec_to_matrix(0.002 * np.array([-lat[1], lat[0], 0.0]))
+        EA[k] = pose(R, 0.0201 * lat + np.array([0.0, 0.0, 0.25 * d[2]]))
+        phiA[k, 3:] = 0.01 * d
+    EB = np.broadcast_to(np.eye(4), (n, 4, 4)).copy()
+    phiB = np.zeros((n, 6))
+    return EA, phiA, EB, phiB
+
+
 def cone_directions(n: int, half_angle_deg: float = 30.0, seed: int = 0) -> np.ndarray:
     """n unit vectors uniform in a cone about +z."""
     g = np.random.default_rng(seed)

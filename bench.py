@@ -52,20 +52,8 @@ SIM_PULL = 1.0  # pull force magnitude along each direction (scaled by the mass,
 
 
 def instance_states(n, rank=0):
-    """Pose / twist of each instance from its pull direction."""
-    dirs = W.fibonacci_directions(n * max(1, rank + 1))[rank * n:(rank + 1) * n] if rank else W.fibonacci_directions(n)
-    EA = np.zeros((n, 4, 4))
-    phiA = np.zeros((n, 6))
-    for k, d in enumerate(dirs):
-        lat = np.array([d[0], d[1], 0.0])
-        ln = np.linalg.norm(lat)
-        lat = lat / ln if ln > 1e-6 else np.array([1.0, 0.0, 0.0])
-        R = W.rotvec_to_matrix(0.002 * np.array([-lat[1], lat[0], 0.0]))
-        EA[k] = W.pose(R, 0.0201 * lat + np.array([0.0, 0.0, 0.25 * d[2]]))
-        phiA[k, 3:] = 0.01 * d
-    EB = np.broadcast_to(np.eye(4), (n, 4, 4)).copy()
-    phiB = np.zeros((n, 6))
-    return EA, phiA, EB, phiB
+    """Pose / twist of each instance from its pull direction (workloads.direction_sweep_states)."""
+    return W.direction_sweep_states(n, rank)
 
 
 def build_workload(n_inst, n_pts, grid_n, rank=0):
