@@ -370,23 +370,27 @@ __device__ __forceinline__ void ls_sweep_node8(const float4* __restrict__ soup, 
         const int v = __shfl_sync(full, ct, gbase + e2);
         if (e2 < e && v == ct) use = false;
     }
-    float d = 0.f;
-    if (use) d = ls_tri_soup(soup, ct, g.node(i, j, k));
-    float p = phi0;
-    int best = own;
+    float d = use ? ls_tri_soup(soup, ct, g.node(i, j, k)) : INFINITY;
+    // The reference's comparisons in order (replace when d < phi) keep the smallest distance and,
+    // among equal ones, the earliest candidate, and keep the node's own only if no candidate is
+    // strictly smaller: an arg-min over the 8 lanes ordered by (distance, lane), then one test.
+    // Unused candidates carry +inf (a used NaN distance never passes `d < phi`: it is dropped
+    // too, as the ordered tree below would otherwise rank it).
+    if (d != d) d = INFINITY;
+    int at = e;
 #pragma unroll
-    for (int e2 = 0; e2 < 7; ++e2) {
-        const float de = __shfl_sync(full, d, gbase + e2);
-        const int ce = __shfl_sync(full, ct, gbase + e2);
-        const unsigned ue = __shfl_sync(full, (unsigned)use, gbase + e2);
-        if (ue && de < p) {
-            p = de;
-            best = ce;
+    for (int o = 1; o < 8; o <<= 1) {
+        const float d2 = __shfl_xor_sync(full, d, o);
+        const int a2 = __shfl_xor_sync(full, at, o);
+        if (d2 < d || (d2 == d && a2 < at)) {
+            d = d2;
+            at = a2;
         }
     }
-    if (valid && e == 0 && best != own) {
-        phi[self] = p;
-        closest[self] = best;
+    const int best_ct = __shfl_sync(full, ct, gbase + at);
+    if (valid && e == 0 && d < phi0) {
+        phi[self] = d;
+        closest[self] = best_ct;
     }
 }
 
