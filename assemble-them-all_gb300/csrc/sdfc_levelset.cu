@@ -405,6 +405,8 @@ __device__ __forceinline__ void st_release_gpu(int* p, int v) {
 
 // Bound on the polls of one wait (each at least ~0.3 us): about a second.
 constexpr long kLsSpinLimit = 1L << 22;
+// Polls without sleeping first (a plane usually waits for one diagonal of its neighbour).
+constexpr long kLsSpinFast = 1L << 12;
 
 // One sweep order over slabs of planes.  With sweep-relative indices (a, b, c) (a = i - 1 for
 // di > 0, ni - 2 - i for di < 0, likewise b, c), CTA s owns the planes c in [s P, s P + P) and
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(kLsSweepThreads, 1) ls_sweep_slabs_kernel(cons
                         v = -1;
                         break;
                     }
-                    __nanosleep(64);
+                    if (it > kLsSpinFast) __nanosleep(64);  // back off only on long waits
                 }
                 s_seen = v;
             }
