@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -236,6 +237,10 @@ int sdfc_create(sdfc_context** out, int device) {
         delete ctx;
         return SDFC_ERR_CUDA;
     }
+    int direct = 0;
+    if (cudaDeviceGetAttribute(&direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess)
+        direct = 0;
+    ctx->pageable_direct = direct != 0 && std::getenv("SDFC_STAGED_COPIES") == nullptr;
     *out = ctx;
     return SDFC_OK;
 }
@@ -708,34 +713,33 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
     int rc = use_device(ctx);
     if (rc) return rc;
     const size_t n = (size_t)b->n;
-    double* h = b->h_in;
-    std::memcpy(h, E_A, sizeof(double) * 16 * n);
-    std::memcpy(h + 16 * n, phi_A, sizeof(double) * 6 * n);
-    std::memcpy(h + 22 * n, E_B, sizeof(double) * 16 * n);
-    std::memcpy(h + 38 * n, phi_B, sizeof(double) * 6 * n);
-    for (size_t k = 0; k < n; ++k) {
-        double* p = h + 44 * n + 6 * k;
-        p[0] = params[k].kn;
-        p[1] = params[k].kt;
-        p[2] = params[k].mu;
-        p[3] = params[k].damping;
-        p[4] = params[k].scale;
-        p[5] = params[k].contact_scale;
-    }
     cudaStream_t s = ctx->stream;
     const int dv = want_deriv ? 1 : 0;
-    // the staged H2D, the evaluation and the D2H, captured once per (derivative flag, modes)
+    double* d = b->d_in;
+    double* o = b->d_out;
+    const size_t nout = dv ? 300 * n : 12 * n;
+    static_assert(sizeof(sdfc_params) == 6 * sizeof(double), "sdfc_params rows are the kernels' 6 doubles");
+    // Inputs: where the device reads pageable memory through the host page tables (Grace: the
+    // C2C link), straight from the caller's arrays; elsewhere staged through pinned buffers.
+    if (ctx->pageable_direct) {
+        CUDA_TRY(ctx, cudaMemcpyAsync(d, E_A, sizeof(double) * 16 * n, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(ctx, cudaMemcpyAsync(d + 16 * n, phi_A, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(ctx, cudaMemcpyAsync(d + 22 * n, E_B, sizeof(double) * 16 * n, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(ctx, cudaMemcpyAsync(d + 38 * n, phi_B, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(ctx, cudaMemcpyAsync(d + 44 * n, params, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s));
+    } else {
+        double* h = b->h_in;
+        std::memcpy(h, E_A, sizeof(double) * 16 * n);
+        std::memcpy(h + 16 * n, phi_A, sizeof(double) * 6 * n);
+        std::memcpy(h + 22 * n, E_B, sizeof(double) * 16 * n);
+        std::memcpy(h + 38 * n, phi_B, sizeof(double) * 6 * n);
+        std::memcpy(h + 44 * n, params, sizeof(double) * 6 * n);
+        CUDA_TRY(ctx, cudaMemcpyAsync(d, h, sizeof(double) * 50 * n, cudaMemcpyHostToDevice, s));
+    }
+    // the evaluation's kernels, captured once per (derivative flag, modes)
     auto enqueue = [&](cudaStream_t st) -> int {
-        CUDA_TRY(ctx, cudaMemcpyAsync(b->d_in, b->h_in, sizeof(double) * 50 * n, cudaMemcpyHostToDevice, st));
-        double* d = b->d_in;
-        double* o = b->d_out;
-        int r = run_batch(b, d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n, dv != 0, o, o + 12 * n, o + 156 * n,
-                          b->d_int, b->d_int + n, st);
-        if (r) return r;
-        const size_t nout = dv ? 300 * n : 12 * n;
-        CUDA_TRY(ctx, cudaMemcpyAsync(b->h_out, o, sizeof(double) * nout, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(ctx, cudaMemcpyAsync(b->h_int, b->d_int, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, st));
-        return SDFC_OK;
+        return run_batch(b, d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n, dv != 0, o, o + 12 * n, o + 156 * n,
+                         b->d_int, b->d_int + n, st);
     };
     const int key = b->precision * 2 + b->deriv_mode;
     if (b->timing) {  // the phase events need the kernels launched one by one
@@ -762,6 +766,19 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
         }
         CUDA_TRY(ctx, cudaGraphLaunch(b->eval_exec[dv], s));
     }
+    if (ctx->pageable_direct) {
+        CUDA_TRY(ctx, cudaMemcpyAsync(fm, o, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, s));
+        if (dv) {
+            CUDA_TRY(ctx, cudaMemcpyAsync(Km, o + 12 * n, sizeof(double) * 144 * n, cudaMemcpyDeviceToHost, s));
+            CUDA_TRY(ctx, cudaMemcpyAsync(Dm, o + 156 * n, sizeof(double) * 144 * n, cudaMemcpyDeviceToHost, s));
+        }
+        if (n_active) CUDA_TRY(ctx, cudaMemcpyAsync(n_active, b->d_int, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+        if (status) CUDA_TRY(ctx, cudaMemcpyAsync(status, b->d_int + n, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        return SDFC_OK;
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->h_out, o, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(ctx, cudaMemcpyAsync(b->h_int, b->d_int, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(ctx, cudaStreamSynchronize(s));
     std::memcpy(fm, b->h_out, sizeof(double) * 12 * n);
     if (want_deriv) {

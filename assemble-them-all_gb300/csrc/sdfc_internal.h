@@ -12,6 +12,10 @@
 struct sdfc_context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // host-array calls copy straight between the caller's pageable arrays and the device (the
+    // device reads pageable memory through the host page tables, as over Grace's C2C link);
+    // otherwise they stage through pinned buffers (SDFC_STAGED_COPIES forces staging)
+    bool pageable_direct = false;
     std::string err;
     std::vector<sdfc::GridDesc> grids;  // host copies of the descriptors
     std::vector<sdfc::PointsDesc> points;

@@ -411,11 +411,21 @@ class Batch:
         off = np.concatenate([[0], np.cumsum(counts)])
         return mn, [d[off[k]:off[k + 1]].copy() for k in range(n)]
 
-    def evaluate(self, E_A, phi_A, E_B, phi_B, params, want_deriv=True):
+    def evaluate(self, E_A, phi_A, E_B, phi_B, params, want_deriv=True, out=None):
         """Host arrays in, host arrays out: (fm[n,12], Km[n,12,12], Dm[n,12,12], n_active[n], status[n]).
         params: one Params for every instance, a sequence of n Params, or an (n, 6) array of
-        (kn, kt, mu, damping, scale, contact_scale) rows (sdfc_params' layout)."""
+        (kn, kt, mu, damping, scale, contact_scale) rows (sdfc_params' layout).  out: optional
+        (fm, Km, Dm, n_active, status) arrays of those shapes (float64 / int32, C-contiguous) to
+        write into and return, for callers that keep their result buffers across calls."""
         n = self.n
+        if out is not None:
+            fm, Km, Dm, nact, st = out
+            ok = (fm.dtype == np.float64 and fm.shape == (n, 12) and fm.flags.c_contiguous and
+                  nact.dtype == np.int32 and nact.shape == (n,) and st.dtype == np.int32 and st.shape == (n,) and
+                  (not want_deriv or all(a.dtype == np.float64 and a.shape == (n, 12, 12) and a.flags.c_contiguous
+                                         for a in (Km, Dm))))
+            if not ok:
+                raise ValueError("out: fm (n, 12), Km and Dm (n, 12, 12) float64, n_active and status (n,) int32")
         if isinstance(params, Params):
             rows = np.tile(params.as_row(), (n, 1))
         elif isinstance(params, np.ndarray):
@@ -424,18 +434,20 @@ class Batch:
             rows = np.array([p.as_row() for p in params])
         rows = _f64(rows, (n, 6))
         prm = rows.ctypes.data_as(ctypes.POINTER(Params))
-        fm = np.zeros(12 * n)
-        Km = np.zeros(144 * n) if want_deriv else np.zeros(1)
-        Dm = np.zeros(144 * n) if want_deriv else np.zeros(1)
-        nact = np.zeros(n, dtype=np.int32)
-        st = np.zeros(n, dtype=np.int32)
+        if out is None:
+            fm = np.zeros((n, 12))
+            Km = np.zeros((n, 12, 12)) if want_deriv else np.zeros(1)
+            Dm = np.zeros((n, 12, 12)) if want_deriv else np.zeros(1)
+            nact = np.zeros(n, dtype=np.int32)
+            st = np.zeros(n, dtype=np.int32)
         self.ctx._check(lib().sdfc_batch_evaluate(self._h, _dp(_f64(E_A, 16 * n)), _dp(_f64(phi_A, 6 * n)),
                                                   _dp(_f64(E_B, 16 * n)), _dp(_f64(phi_B, 6 * n)), prm,
-                                                  int(bool(want_deriv)), _dp(fm), _dp(Km), _dp(Dm), _ip(nact),
-                                                  _ip(st)), "sdfc_batch_evaluate")
+                                                  int(bool(want_deriv)), _dp(fm), _dp(Km) if want_deriv else None,
+                                                  _dp(Dm) if want_deriv else None, _ip(nact), _ip(st)),
+                        "sdfc_batch_evaluate")
         if want_deriv:
-            return fm.reshape(n, 12), Km.reshape(n, 12, 12), Dm.reshape(n, 12, 12), nact, st
-        return fm.reshape(n, 12), None, None, nact, st
+            return fm, Km, Dm, nact, st
+        return fm, None, None, nact, st
 
     def evaluate_device(self, E_A, phi_A, E_B, phi_B, params, fm, Km, Dm, n_active, status, want_deriv=True,
                         stream=0):

@@ -353,13 +353,16 @@ def run_gpu(args, world, rank):
            "Dm": rel_err(out_fast[2][:m], ref[2][:m]), "instances": m}
     plain_rate = args.points / float(np.mean(plain_t[1:] if len(plain_t) > 1 else plain_t))
 
-    # e2e through the C ABI with host buffers (H2D of the instance states, D2H of fm/Km/Dm)
+    # e2e through the C ABI with host buffers (H2D of the instance states, D2H of fm/Km/Dm into
+    # result arrays the caller keeps across calls, as a simulator's force assembly does)
+    e2e_out = (np.zeros((n, 12)), np.zeros((n, 12, 12)), np.zeros((n, 12, 12)), np.zeros(n, np.int32),
+               np.zeros(n, np.int32))
     e2e_t = []
     for k in range(max(3, args.steps // 2) + 1):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        batch.evaluate(EA, phiA, EB, phiB, params_rows, want_deriv=True)
+        batch.evaluate(EA, phiA, EB, phiB, params_rows, want_deriv=True, out=e2e_out)
         if k:
             e2e_t.append(time.perf_counter() - t)
     e2e_s = dist_max(float(np.mean(e2e_t)), world)
