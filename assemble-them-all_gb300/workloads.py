@@ -116,13 +116,16 @@ def fibonacci_directions(n: int) -> np.ndarray:
     return np.stack([np.cos(theta) * np.sin(phi), np.sin(theta) * np.sin(phi), np.cos(phi)], axis=-1)
 
 
-def direction_sweep_states(n, rank=0):
+def direction_sweep_states(n, rank=0, world=1):
     """The direction sweep of the planner (one instance per pull direction): the peg fully inserted
     in the socket, shifted 0.0201 toward the direction's lateral part (pressed 1e-4 into the bore
     wall past col_th 0.01), tilted 0.002 rad about the perpendicular axis, raised 0.25 d_z, moving
-    at 0.01 d.  Returns (E_A, phi_A, E_B, phi_B) for n instances (rank r takes the r-th block of
-    n directions of a Fibonacci sphere of n (r + 1) points)."""
-    dirs = fibonacci_directions(n * max(1, rank + 1))[rank * n:(rank + 1) * n] if rank else fibonacci_directions(n)
+    at 0.01 d.  Returns (E_A, phi_A, E_B, phi_B) for n instances.  With `world` replicas the sweep
+    is one Fibonacci sphere of n * world directions and replica `rank` takes its rank-th block of
+    n, so the replicas' instances are disjoint and together cover the sphere."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    dirs = fibonacci_directions(n * world)[rank * n:(rank + 1) * n]
     EA = np.zeros((n, 4, 4))
     phiA = np.zeros((n, 6))
     for k, d in enumerate(dirs):

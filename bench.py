@@ -51,15 +51,16 @@ SIM_GRAVITY = (0.0, 0.0, -9.8)
 SIM_PULL = 1.0  # pull force magnitude along each direction (scaled by the mass, Body.cpp:267-268)
 
 
-def instance_states(n, rank=0):
-    """Pose / twist of each instance from its pull direction (workloads.direction_sweep_states)."""
-    return W.direction_sweep_states(n, rank)
+def instance_states(n, rank=0, world=1):
+    """Pose / twist of each instance from its pull direction (workloads.direction_sweep_states):
+    replica `rank` of `world` takes its own block of n directions of one shared sweep."""
+    return W.direction_sweep_states(n, rank, world)
 
 
-def build_workload(n_inst, n_pts, grid_n, rank=0):
+def build_workload(n_inst, n_pts, grid_n, rank=0, world=1):
     grid = W.socket_grid(grid_n, dtype=np.float32)
     pts = W.peg_points(n_pts, seed=0)
-    return grid, pts, instance_states(n_inst, rank)
+    return grid, pts, instance_states(n_inst, rank, world)
 
 
 # --------------------------------------------------------------------------- CPU baseline (oracle)
@@ -131,6 +132,13 @@ def dist_max(x, world):
     t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(units_per_rank, seconds, world):
+    """Weak-scaling aggregate: every replica processes `units_per_rank` units; the job's time is
+    the slowest replica's.  Returns (units per second over all replicas, the max-over-ranks time)."""
+    s = dist_max(seconds, world)
+    return world * units_per_rank / s, s
 
 
 def dist_barrier(world):
@@ -257,7 +265,7 @@ def rel_err(a, b):
 
 
 def run_gpu(args, world, rank):
-    grid, pts, states = build_workload(args.instances, args.points, args.grid, rank)
+    grid, pts, states = build_workload(args.instances, args.points, args.grid, rank, world)
     pool = None
     if rank == 0 and not args.no_cpu_baseline:
         pool = cpu_pool(grid, pts, os.cpu_count() or 1)  # spawned before the first CUDA call
@@ -313,10 +321,9 @@ def run_gpu(args, world, rank):
         wall = time.perf_counter() - t0
         clk = clocks.stop()
         dist_barrier(world)
-        step_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-        step_ms = dist_max(step_ms, world)
         pts_per_step = n * args.points
-        value = world * pts_per_step / (step_ms / 1e3)
+        value, step_s = whole_job_rate(pts_per_step, float(np.mean([a.elapsed_time(b) for a, b in ev])) / 1e3, world)
+        step_ms = step_s * 1e3
 
         # per-phase device times (separate pass with events between the launches)
         batch.set_timing(True)
@@ -365,11 +372,11 @@ def run_gpu(args, world, rank):
         batch.evaluate(EA, phiA, EB, phiB, params_rows, want_deriv=True, out=e2e_out)
         if k:
             e2e_t.append(time.perf_counter() - t)
-    e2e_s = dist_max(float(np.mean(e2e_t)), world)
+    e2e_value, e2e_s = whole_job_rate(pts_per_step, float(np.mean(e2e_t)), world)
     h2d = n * 50 * 8
     d2h = n * (300 * 8 + 2 * 4)
 
-    sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 else None
+    sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 and rank == 0 else None
     c5_res = run_c5(args, sdfc, ctx, torch) if args.c5_points > 0 and rank == 0 else None
     c4_res = run_c4(args, sdfc, ctx, g, torch) if args.c4_instances > 0 and rank == 0 else None
     ls_res = run_levelset(args, sdfc, ctx, torch) if args.ls_segments > 0 and rank == 0 else None
@@ -402,7 +409,7 @@ def run_gpu(args, world, rank):
         "dtype": "f64 depth/sums, f32 per-contact algebra" if args.precision == "mixed" else "f64",
         "data": "synthetic",
         "config": workload_config(args),
-        "e2e": {"value": world * pts_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": ach / hbm_peak, "traffic": traffic,
