@@ -943,64 +943,12 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     }
     sink.force(xi1, f1, xi2, f2);
 
-    const Vec3<T> rxd = mulT(R2, xw1d);
-
-    // skip_q2: the dq2 columns of Km are left to the caller, which derives them
-    // from the summed dq1 columns (finalize_kernel)
-#pragma unroll 1
-    for (int ci = 0; ci < (skip_q2 ? 18 : 24); ++ci) {
-        const int c = (skip_q2 && ci >= 6) ? ci + 6 : ci;
-        const int blk = c / 6, j = c % 6;
+    // One column's factors from its derivatives (dd_j, dddot_j, dn_j, dt_j, dxi2_j of the depth,
+    // its rate, the normal, the tangential velocity and the body-B contact point along column c);
+    // blk = c / 6 (0: dq1, 1: dq2 -> Km; 2: dphi1, 3: dphi2 -> Dm), j = c % 6.
+    auto emit = [&](int c, int blk, int j, T dd_j, T dddot_j, const Vec3<T>& dn_j, const Vec3<T>& dt_j,
+                    const Vec3<T>& dxi2_j) {
         const bool kcol = blk < 2;  // Km column (dq) vs Dm column (dphi)
-        T dd_j = 0, dddot_j = 0;
-        Vec3<T> dn_j = vec3<T>(0, 0, 0), dt_j = vec3<T>(0, 0, 0), dxi2_j = vec3<T>(0, 0, 0);
-        if (blk == 0 || blk == 2) {
-            // through the contact point: dxw1/dq1 = [-R1 skew(xi1) | R1] = dxw1dot/dphi1,
-            // dxw1dot/dq1 = [-R1 skew(u1) | 0]
-            Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
-            if (blk == 0) {
-                Vec3<T> b = (j < 3) ? mul(R1, cross(unit<T>(j), u1)) : vec3<T>(0, 0, 0);
-                dd_j = dot(dd_dxw, a);
-                dddot_j = dot(dddot_dxw, a) + dot(dddot_dxwd, b);
-                dn_j = mul(dn_dxw, a);
-                dt_j = mul(dt_dxw, a) + (b - dot(n, b) * n);
-                dxi2_j = mul(dxi2_dxw, a);
-            } else {
-                dddot_j = dot(dddot_dxwd, a);
-                dt_j = a - dot(n, a) * n;
-            }
-        } else if (blk == 1) {
-            // dx/dq2 = [skew(x) | -I]
-            Vec3<T> dxj = (j < 3) ? cross(x, unit<T>(j)) : -unit<T>(j - 3);
-            dd_j = dot(gr, dxj);
-            Vec3<T> de_j = mul(de_dx, dxj);
-            dn_j = mul(R2, de_j);
-            if (j < 3) dn_j = dn_j + mul(R2, cross(unit<T>(j), e));
-            dxi2_j = dxj - dd_j * e - d * de_j;
-            if (j < 3) {
-                // g^T(-Sw Sx + skew(R2^T xw_dot)) e_j + (H xdot)^T Sx e_j
-                Vec3<T> sxe = cross(x, unit<T>(j));
-                dddot_j = dot(gr, -cross(w2, sxe) + cross(rxd, unit<T>(j))) + dot(Hxdot, sxe);
-            } else {
-                dddot_j = dot(gr, cross(w2, unit<T>(j - 3))) - comp(Hxdot, j - 3);
-            }
-            // dxw2dot/dq2 = [-R2 skew(w2 x xi2 + v2) + R2 Sw dxi2_dq2.left | R2 Sw dxi2_dq2.right]
-            Vec3<T> dxw2d_j = mul(R2Sw, dxi2_j);
-            if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit<T>(j)));
-            // dtdot/dq2 = -dxw2d - nvw dn - n (vw.dn - n.dxw2d)
-            dt_j = -dxw2d_j - nvw * dn_j - (dot(vw, dn_j) - dot(n, dxw2d_j)) * n;
-        } else {  // blk == 3: dphi2
-            Vec3<T> q;
-            if (j < 3) {
-                dddot_j = dot(gr, cross(x, unit<T>(j)));
-                q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
-            } else {
-                dddot_j = -comp(gr, j - 3);
-                q = col(R2, j - 3);
-            }
-            dt_j = -(q - dot(n, q) * n);
-        }
-
         // normal-force columns
         Vec3<T> N1, N2, T2 = vec3<T>(0, 0, 0);
         if (kcol) {
@@ -1036,6 +984,64 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
             }
         }
         sink.column(c, N1, N2, T2);
+    };
+    const Vec3<T> zero3 = vec3<T>(0, 0, 0);
+
+    // The four column blocks run as separate loops, so that each block's intermediate matrices
+    // die with its loop.  dq1 and dphi1 go through the contact point: dxw1/dq1 =
+    // [-R1 skew(xi1) | R1] = dxw1dot/dphi1, dxw1dot/dq1 = [-R1 skew(u1) | 0].
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dq1
+        const Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
+        const Vec3<T> b = (j < 3) ? mul(R1, cross(unit<T>(j), u1)) : vec3<T>(0, 0, 0);
+        emit(j, 0, j, dot(dd_dxw, a), dot(dddot_dxw, a) + dot(dddot_dxwd, b), mul(dn_dxw, a),
+             mul(dt_dxw, a) + (b - dot(n, b) * n), mul(dxi2_dxw, a));
+    }
+    // skip_q2: the dq2 columns of Km are left to the caller, which derives them
+    // from the summed dq1 columns (finalize_kernel)
+    if (!skip_q2) {
+        const Vec3<T> rxd = mulT(R2, xw1d);
+#pragma unroll 1
+        for (int j = 0; j < 6; ++j) {  // dq2: dx/dq2 = [skew(x) | -I]
+            Vec3<T> dxj = (j < 3) ? cross(x, unit<T>(j)) : -unit<T>(j - 3);
+            const T dd_j = dot(gr, dxj);
+            Vec3<T> de_j = mul(de_dx, dxj);
+            Vec3<T> dn_j = mul(R2, de_j);
+            if (j < 3) dn_j = dn_j + mul(R2, cross(unit<T>(j), e));
+            const Vec3<T> dxi2_j = dxj - dd_j * e - d * de_j;
+            T dddot_j;
+            if (j < 3) {
+                // g^T(-Sw Sx + skew(R2^T xw_dot)) e_j + (H xdot)^T Sx e_j
+                Vec3<T> sxe = cross(x, unit<T>(j));
+                dddot_j = dot(gr, -cross(w2, sxe) + cross(rxd, unit<T>(j))) + dot(Hxdot, sxe);
+            } else {
+                dddot_j = dot(gr, cross(w2, unit<T>(j - 3))) - comp(Hxdot, j - 3);
+            }
+            // dxw2dot/dq2 = [-R2 skew(w2 x xi2 + v2) + R2 Sw dxi2_dq2.left | R2 Sw dxi2_dq2.right]
+            Vec3<T> dxw2d_j = mul(R2Sw, dxi2_j);
+            if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit<T>(j)));
+            // dtdot/dq2 = -dxw2d - nvw dn - n (vw.dn - n.dxw2d)
+            const Vec3<T> dt_j = -dxw2d_j - nvw * dn_j - (dot(vw, dn_j) - dot(n, dxw2d_j)) * n;
+            emit(6 + j, 1, j, dd_j, dddot_j, dn_j, dt_j, dxi2_j);
+        }
+    }
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dphi1
+        const Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
+        emit(12 + j, 2, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
+    }
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dphi2
+        T dddot_j;
+        Vec3<T> q;
+        if (j < 3) {
+            dddot_j = dot(gr, cross(x, unit<T>(j)));
+            q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
+        } else {
+            dddot_j = -comp(gr, j - 3);
+            q = col(R2, j - 3);
+        }
+        emit(18 + j, 3, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
     }
 }
 
