@@ -942,11 +942,18 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
         }
     }
     sink.force(xi1, f1, xi2, f2);
+    // FP32 path: the friction columns' per-contact factors.  Sliding: al = cm (dfn - ratio dtn)
+    // with cm = mu / tn, dfn = s1 (xr1.(xi1 x N1) + rho1.N1) / fc_norm, dtn = t.dt_j / tn, i.e.
+    // al = fa (xr1.(xi1 x N1) + rho1.N1) - fb t.dt_j; static: al = 0, be = ga = kt.
+    constexpr bool kFusedFriction = std::is_same<T, float>::value;
+    const T cm = mu / tn;
+    const T fa = stat ? T(0) : cm * s1 / fc_norm, fb = stat ? T(0) : cm * ratio / tn;
+    const T be = stat ? kt : cm * fc_norm, ga = stat ? kt : mu * ratio;
 
     // One column's factors from its derivatives (dd_j, dddot_j, dn_j, dt_j, dxi2_j of the depth,
     // its rate, the normal, the tangential velocity and the body-B contact point along column c);
-    // blk = c / 6 (0: dq1, 1: dq2 -> Km; 2: dphi1, 3: dphi2 -> Dm), j = c % 6.
-    auto emit = [&](int c, int blk, int j, T dd_j, T dddot_j, const Vec3<T>& dn_j, const Vec3<T>& dt_j,
+    // blk = c / 6 (0: dq1, 1: dq2 -> Km; 2: dphi1, 3: dphi2 -> Dm), j = c % 6, rot = j < 3.
+    auto emit = [&](int c, int blk, bool rot, int j, T dd_j, T dddot_j, const Vec3<T>& dn_j, const Vec3<T>& dt_j,
                     const Vec3<T>& dxi2_j) {
         const bool kcol = blk < 2;  // Km column (dq) vs Dm column (dphi)
         // normal-force columns
@@ -955,31 +962,41 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
             T r = kn * dd_j - kd * dddot_j * d - kd * ddot * dd_j;
             N1 = -r * rho1 - sK * mulT(R1, dn_j);
             N2 = r * rho2 + sK * mulT(R2, dn_j);
-            if (blk == 0 && j < 3) N1 = N1 - sK * cross(rho1, unit<T>(j));
-            if (blk == 1 && j < 3) N2 = N2 + sK * cross(rho2, unit<T>(j));
+            if (blk == 0 && rot) N1 = N1 - sK * cross(rho1, unit<T>(j));
+            if (blk == 1 && rot) N2 = N2 + sK * cross(rho2, unit<T>(j));
             T2 = -sK * cross(rho2, dxi2_j);
         } else {
             T r = kd * dddot_j * d;
             N1 = r * rho1;
             N2 = -r * rho2;
         }
-        if (friction) {
+        if (friction && kFusedFriction) {
+            // both regimes in one form, N1 -= al tau1 + be R1^T dt_j (+ ga tau1 x e_j), so that
+            // the static and sliding contacts of a warp do not diverge (the sliding terms of
+            // the reference form below, with cm = mu / tn distributed over the sum)
+            const T al = fa * (dot(xr1, cross(xi1, N1)) + dot(rho1, N1)) - fb * dot(t, dt_j);
+            N1 = N1 - (al * tau1 + be * mulT(R1, dt_j));
+            N2 = N2 + (al * tau2 + be * mulT(R2, dt_j));
+            if (blk == 0 && rot) N1 = N1 - ga * cross(tau1, unit<T>(j));
+            if (blk == 1 && rot) N2 = N2 + ga * cross(tau2, unit<T>(j));
+            if (kcol) T2 = T2 - ga * cross(tau2, dxi2_j);
+        } else if (friction) {
             // dfc_norm = fc1^T dfc1 / |fc1|, with dfc1 = Gamma1^T N1 and fc1 = s1 Gamma1^T rho1
             T dfn = s1 * (dot(xr1, cross(xi1, N1)) + dot(rho1, N1)) / fc_norm;
             T dtn = dot(t, dt_j) / tn;
             if (stat) {
                 N1 = N1 - kt * mulT(R1, dt_j);
                 N2 = N2 + kt * mulT(R2, dt_j);
-                if (blk == 0 && j < 3) N1 = N1 - kt * cross(tau1, unit<T>(j));
-                if (blk == 1 && j < 3) N2 = N2 + kt * cross(tau2, unit<T>(j));
+                if (blk == 0 && rot) N1 = N1 - kt * cross(tau1, unit<T>(j));
+                if (blk == 1 && rot) N2 = N2 + kt * cross(tau2, unit<T>(j));
                 if (kcol) T2 = T2 - kt * cross(tau2, dxi2_j);
             } else {
                 T cm = mu / tn;
                 T s = dfn - ratio * dtn;
                 N1 = N1 - cm * (s * tau1 + fc_norm * mulT(R1, dt_j));
                 N2 = N2 + cm * (s * tau2 + fc_norm * mulT(R2, dt_j));
-                if (blk == 0 && j < 3) N1 = N1 - (mu * ratio) * cross(tau1, unit<T>(j));
-                if (blk == 1 && j < 3) N2 = N2 + (mu * ratio) * cross(tau2, unit<T>(j));
+                if (blk == 0 && rot) N1 = N1 - (mu * ratio) * cross(tau1, unit<T>(j));
+                if (blk == 1 && rot) N2 = N2 + (mu * ratio) * cross(tau2, unit<T>(j));
                 if (kcol) T2 = T2 - (mu * ratio) * cross(tau2, dxi2_j);
             }
         }
@@ -987,15 +1004,21 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     };
     const Vec3<T> zero3 = vec3<T>(0, 0, 0);
 
-    // The four column blocks run as separate loops, so that each block's intermediate matrices
-    // die with its loop.  dq1 and dphi1 go through the contact point: dxw1/dq1 =
-    // [-R1 skew(xi1) | R1] = dxw1dot/dphi1, dxw1dot/dq1 = [-R1 skew(u1) | 0].
+    // The column blocks run as separate loops, each split into its rotational (j < 3) and
+    // translational (j >= 3) halves, so that each block's intermediate matrices die with its
+    // loops and the j < 3 cases are resolved at compile time.  dq1 and dphi1 go through the
+    // contact point: dxw1/dq1 = [-R1 skew(xi1) | R1] = dxw1dot/dphi1, dxw1dot/dq1 = [-R1 skew(u1) | 0].
 #pragma unroll 1
-    for (int j = 0; j < 6; ++j) {  // dq1
-        const Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
-        const Vec3<T> b = (j < 3) ? mul(R1, cross(unit<T>(j), u1)) : vec3<T>(0, 0, 0);
-        emit(j, 0, j, dot(dd_dxw, a), dot(dddot_dxw, a) + dot(dddot_dxwd, b), mul(dn_dxw, a),
+    for (int j = 0; j < 3; ++j) {  // dq1, rotational
+        const Vec3<T> a = mul(R1, cross(unit<T>(j), xi1));
+        const Vec3<T> b = mul(R1, cross(unit<T>(j), u1));
+        emit(j, 0, true, j, dot(dd_dxw, a), dot(dddot_dxw, a) + dot(dddot_dxwd, b), mul(dn_dxw, a),
              mul(dt_dxw, a) + (b - dot(n, b) * n), mul(dxi2_dxw, a));
+    }
+#pragma unroll 1
+    for (int j = 3; j < 6; ++j) {  // dq1, translational (b = 0)
+        const Vec3<T> a = col(R1, j - 3);
+        emit(j, 0, false, j, dot(dd_dxw, a), dot(dddot_dxw, a), mul(dn_dxw, a), mul(dt_dxw, a), mul(dxi2_dxw, a));
     }
     // skip_q2: the dq2 columns of Km are left to the caller, which derives them
     // from the summed dq1 columns (finalize_kernel)
@@ -1022,26 +1045,30 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
             if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit<T>(j)));
             // dtdot/dq2 = -dxw2d - nvw dn - n (vw.dn - n.dxw2d)
             const Vec3<T> dt_j = -dxw2d_j - nvw * dn_j - (dot(vw, dn_j) - dot(n, dxw2d_j)) * n;
-            emit(6 + j, 1, j, dd_j, dddot_j, dn_j, dt_j, dxi2_j);
+            emit(6 + j, 1, j < 3, j, dd_j, dddot_j, dn_j, dt_j, dxi2_j);
         }
     }
 #pragma unroll 1
-    for (int j = 0; j < 6; ++j) {  // dphi1
-        const Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
-        emit(12 + j, 2, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
+    for (int j = 0; j < 3; ++j) {  // dphi1, rotational
+        const Vec3<T> a = mul(R1, cross(unit<T>(j), xi1));
+        emit(12 + j, 2, true, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
     }
 #pragma unroll 1
-    for (int j = 0; j < 6; ++j) {  // dphi2
-        T dddot_j;
-        Vec3<T> q;
-        if (j < 3) {
-            dddot_j = dot(gr, cross(x, unit<T>(j)));
-            q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
-        } else {
-            dddot_j = -comp(gr, j - 3);
-            q = col(R2, j - 3);
-        }
-        emit(18 + j, 3, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
+    for (int j = 3; j < 6; ++j) {  // dphi1, translational
+        const Vec3<T> a = col(R1, j - 3);
+        emit(12 + j, 2, false, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
+    }
+#pragma unroll 1
+    for (int j = 0; j < 3; ++j) {  // dphi2, rotational
+        const T dddot_j = dot(gr, cross(x, unit<T>(j)));
+        const Vec3<T> q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
+        emit(18 + j, 3, true, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
+    }
+#pragma unroll 1
+    for (int j = 3; j < 6; ++j) {  // dphi2, translational
+        const T dddot_j = -comp(gr, j - 3);
+        const Vec3<T> q = col(R2, j - 3);
+        emit(18 + j, 3, false, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
     }
 }
 
