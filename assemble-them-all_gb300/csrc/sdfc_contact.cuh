@@ -1058,6 +1058,20 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
         const Vec3<T> a = col(R1, j - 3);
         emit(12 + j, 2, false, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
     }
+    if (skip_q2) {
+        // The dphi2 columns of Dm are derived by the caller as well: the force depends on the
+        // velocities through ddot and the relative velocity vw, and for a common world twist
+        // (rotation w about the origin) of both bodies ddot is unchanged while vw gains
+        // w x (xw1 - xw2) = w x (d n).  Hence Dm2 = -Dm1 Ad(E_A^{-1} E_B) + [C | 0], where column
+        // j of C is the response to vw = d R2 (e_j x e) with ddot fixed (w = R2 e_j).  C's three
+        // columns go to the (unused) dq2 accumulators of Km.
+#pragma unroll 1
+        for (int j = 0; j < 3; ++j) {
+            const Vec3<T> dv = d * mul(R2, cross(unit<T>(j), e));
+            emit(6 + j, 2, false, j, T(0), T(0), zero3, dv - dot(n, dv) * n, zero3);
+        }
+        return;
+    }
 #pragma unroll 1
     for (int j = 0; j < 3; ++j) {  // dphi2, rotational
         const T dddot_j = dot(gr, cross(x, unit<T>(j)));

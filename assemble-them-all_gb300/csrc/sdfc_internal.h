@@ -47,6 +47,8 @@ struct sdfc_batch {
     int* d_tile_count = nullptr;
     int* d_tile_queue = nullptr;
     sdfc::Prefilter* d_prefilter = nullptr;
+    sdfc::PairState<float>* d_pair32 = nullptr;
+    sdfc::PairState<double>* d_pair64 = nullptr;
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
     long long* d_point_offset = nullptr;  // n: first output row of each instance's per-point distances

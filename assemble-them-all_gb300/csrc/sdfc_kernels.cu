@@ -50,14 +50,33 @@ __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pos
 
 __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchInputs in,
                             const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
-                            Prefilter* __restrict__ pref) {
+                            Prefilter* __restrict__ pref, PairState<float>* __restrict__ pair32,
+                            PairState<double>* __restrict__ pair64) {
+    // blockIdx.y: 0 the prefilter, 1 / 2 the FP32 / FP64 pair state every force or energy CTA of
+    // the instance starts from (once per instance here, spread over three warps per 32 instances:
+    // all three are FP64 arithmetic)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (in.mode && in.mode[i] == 0)) return;
-    const InstanceDesc I = inst[i];
-    Prefilter f;
-    make_prefilter(grids[I.grid], points[I.points], load_pose(in.EA + 16 * (size_t)i), load_pose(in.EB + 16 * (size_t)i),
-                   f);
-    pref[i] = f;
+    const size_t o = (size_t)i;
+    if (blockIdx.y == 0) {
+        const InstanceDesc I = inst[i];
+        Prefilter f;
+        make_prefilter(grids[I.grid], points[I.points], load_pose(in.EA + 16 * o), load_pose(in.EB + 16 * o), f);
+        pref[i] = f;
+    } else if (blockIdx.y == 1) {
+        make_pair_state(in.EA + 16 * o, in.phiA + 6 * o, in.EB + 16 * o, in.phiB + 6 * o, in.prm + 6 * o, pair32[i]);
+    } else {
+        make_pair_state(in.EA + 16 * o, in.phiA + 6 * o, in.EB + 16 * o, in.phiB + 6 * o, in.prm + 6 * o, pair64[i]);
+    }
+}
+
+// dst = src by the 32 lanes of a warp, 8 bytes per lane and step
+template <typename S>
+__device__ __forceinline__ void warp_copy(S& dst, const S& src, int lane) {
+    static_assert(sizeof(S) % 8 == 0 && alignof(S) >= 8, "8-byte words");
+    const long long* a = reinterpret_cast<const long long*>(&src);
+    long long* b = reinterpret_cast<long long*>(&dst);
+    for (int k = lane; k < (int)(sizeof(S) / 8); k += 32) b[k] = a[k];
 }
 
 // FP32 trilinear interpolation for a point certainly inside the box, from the
@@ -394,6 +413,12 @@ struct Accum<float> {
         lo += err;
     }
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+    // this + o as an FP32 pair (TwoSum of the leading parts, trailing parts added)
+    __device__ __forceinline__ void merge(const Accum<float>& o) {
+        const float lo0 = lo + o.lo;
+        lo = lo0;
+        add(o.hi);
+    }
 };
 
 // Sum over the 32 lanes of 12 values per lane by recursive halving: at each
@@ -496,6 +521,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
                                                        const PointsDesc* __restrict__ points,
                                                        const int* __restrict__ ids,
                                                        const int* __restrict__ tile_count,
+                                                       const PairState<T>* __restrict__ pairs,
                                                        double* __restrict__ partial, int skip, int slots) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     constexpr int NW = kChunk / 32;
@@ -527,11 +553,10 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             if (k < I.ntiles) prefix[k + 1] = run + v;
             run += __shfl_sync(kFull, v, 31);
         }
-    } else if (tid == 32) {
-        g = grids[I.grid];
-        P = points[I.points];
-        make_pair_state(in.EA + 16 * (size_t)i, in.phiA + 6 * (size_t)i, in.EB + 16 * (size_t)i,
-                        in.phiB + 6 * (size_t)i, in.prm + 6 * (size_t)i, S);
+    } else if (warp == 1) {
+        warp_copy(g, grids[I.grid], lane);
+        warp_copy(P, points[I.points], lane);
+        warp_copy(S, pairs[i], lane);
     }
     for (int k = tid; k < NW * NV; k += kChunk) acc[k].zero();
     __syncthreads();
@@ -578,8 +603,16 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     double* row = partial + ((size_t)i * slots + s) * kOutDeriv;  // one row stride for both passes
     for (int k = tid; k < NV; k += kChunk) {
         const int a = acc_index(k);
-        double v = 0.0;
-        for (int w = 0; w < NW; ++w) v += acc[w * NV + a].value();
+        double v;
+        if constexpr (std::is_same<T, float>::value) {
+            // the warps' pairs merged in FP32 (one conversion per value on the FP64 pipe)
+            Accum<float> m = acc[a];
+            for (int w = 1; w < NW; ++w) m.merge(acc[w * NV + a]);
+            v = m.value();
+        } else {
+            v = 0.0;
+            for (int w = 0; w < NW; ++w) v += acc[w * NV + a].value();
+        }
         row[k] = v;
     }
 }
@@ -593,6 +626,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
                                                         const PointsDesc* __restrict__ points,
                                                         const int* __restrict__ ids,
                                                         const int* __restrict__ tile_count,
+                                                        const PairState<T>* __restrict__ pairs,
                                                         double* __restrict__ partial, int slots) {
     constexpr int NW = kChunk / 32;
     constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
@@ -620,11 +654,10 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
             if (k < I.ntiles) prefix[k + 1] = run + v;
             run += __shfl_sync(kFull, v, 31);
         }
-    } else if (tid == 32) {
-        g = grids[I.grid];
-        P = points[I.points];
-        make_pair_state(in.EA + 16 * (size_t)i, in.phiA + 6 * (size_t)i, in.EB + 16 * (size_t)i,
-                        in.phiB + 6 * (size_t)i, in.prm + 6 * (size_t)i, S);
+    } else if (warp == 1) {
+        warp_copy(g, grids[I.grid], lane);
+        warp_copy(P, points[I.points], lane);
+        warp_copy(S, pairs[i], lane);
     }
     for (int k = tid; k < NW * 12; k += kChunk) acc[k].zero();
     if (tid < NW) eacc[tid] = 0.0;
@@ -692,63 +725,64 @@ __global__ void energy_finalize_kernel(int n_inst, const double* __restrict__ pa
         dE[12 * (size_t)i + k - 1] = v;
 }
 
-// Column j of Ad(E_A^{-1} E_B) (twists ordered (w, v)): the map that turns the
-// dq1 columns of Km into its dq2 columns.  Every contact's force in the bodies'
-// frames is unchanged when both bodies move together, so for a world twist eps,
-// Km1 Ad(E_A^{-1}) eps + Km2 Ad(E_B^{-1}) eps = 0, i.e. Km2 = -Km1 Ad(E_A^{-1} E_B).
-// (Dm has no such identity in the reference: its friction damping is not a function
-// of the relative velocity alone.)
-__device__ inline void adjoint_column(const double* EA, const double* EB, int j, double* top, double* bot) {
-    double R[9], p[3];
-    for (int r = 0; r < 3; ++r) {
-        p[r] = 0.0;
-        for (int c = 0; c < 3; ++c) {
-            double v = 0.0;
-            for (int k = 0; k < 3; ++k) v += EA[4 * k + r] * EB[4 * k + c];  // R_A^T R_B
-            R[3 * r + c] = v;
-        }
-        for (int k = 0; k < 3; ++k) p[r] += EA[4 * k + r] * (EB[4 * k + 3] - EA[4 * k + 3]);  // R_A^T (p_B - p_A)
+// Every contact's force in the bodies' frames is unchanged when both bodies move
+// together, so for a world twist eps, Km1 Ad(E_A^{-1}) eps + Km2 Ad(E_B^{-1}) eps = 0,
+// i.e. Km2 = -Km1 Ad(E_A^{-1} E_B).  Dm's friction damping sees, under a common
+// rotation w, the relative velocity w x (d n) of the two contact points, so
+// Dm2 = -Dm1 Ad(E_A^{-1} E_B) + [C | 0] with C accumulated by force_kernel
+// (contact_force_jacobian's skip_q2).
+// Entry (r, c) of Ad(E_A^{-1} E_B) (6 x 6, twists ordered (w, v)):
+//   [Q, 0; [t] Q, Q] with Q = R_A^T R_B and t = R_A^T (p_B - p_A).
+__device__ inline double adjoint_entry(const double* EA, const double* EB, int r, int c) {
+    auto q = [&](int a, int b) {
+        double v = 0.0;
+        for (int k = 0; k < 3; ++k) v += EA[4 * k + a] * EB[4 * k + b];  // (R_A^T R_B)_ab
+        return v;
+    };
+    if (r < 3) return c < 3 ? q(r, c) : 0.0;
+    if (c >= 3) return q(r - 3, c - 3);
+    double t[3];
+    for (int a = 0; a < 3; ++a) {
+        t[a] = 0.0;
+        for (int k = 0; k < 3; ++k) t[a] += EA[4 * k + a] * (EB[4 * k + 3] - EA[4 * k + 3]);  // R_A^T (p_B - p_A)
     }
-    if (j < 3) {
-        const double a[3] = {R[j], R[3 + j], R[6 + j]};
-        for (int r = 0; r < 3; ++r) top[r] = a[r];
-        bot[0] = p[1] * a[2] - p[2] * a[1];
-        bot[1] = p[2] * a[0] - p[0] * a[2];
-        bot[2] = p[0] * a[1] - p[1] * a[0];
-    } else {
-        for (int r = 0; r < 3; ++r) {
-            top[r] = 0.0;
-            bot[r] = R[3 * r + (j - 3)];
-        }
-    }
+    const int a1 = (r - 3 + 1) % 3, a2 = (r - 3 + 2) % 3;  // (t x Q e_c) component r - 3
+    return t[a1] * q(a2, c) - t[a2] * q(a1, c);
 }
 
-// EA / EB not null: the dq2 columns of Km were not accumulated (force_kernel's
-// skip_q2) and are derived here from the summed dq1 columns.
+// One CTA per instance: the instance's slots partial rows summed in order into shared
+// memory, then written out.  EA / EB not null: the dq2 columns of Km and the dphi2 columns
+// of Dm were not accumulated (force_kernel's skip_q2) and are derived here from the summed
+// dq1 / dphi1 columns; the partial rows' dq2 slots of Km then hold C (Dm's correction).
 template <bool DERIV>
 __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
                                 const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode,
                                 const double* __restrict__ EA, const double* __restrict__ EB, int slots) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (size_t)n_inst * NV) return;
-    const int i = (int)(idx / NV), k = (int)(idx % NV);
-    if (mode && mode[i] != (DERIV ? 2 : 1)) return;
-    const double* p = partial + (size_t)i * slots * kOutDeriv + k;
-    double v = 0.0;
-    if (DERIV && EA && k >= 12 && k < 156 && (k - 12) % 12 >= 6) {
-        const int r = (k - 12) / 12, j = (k - 12) % 12 - 6;
-        const double* row = partial + (size_t)i * slots * kOutDeriv + 12 + 12 * r;  // Km row r, dq1 columns
-        double km[6];
-        for (int c = 0; c < 6; ++c) {
-            km[c] = 0.0;
-            for (int s = 0; s < slots; ++s) km[c] += row[(size_t)s * kOutDeriv + c];
+    __shared__ double tot[NV];
+    __shared__ double ad[36];  // Ad(E_A^{-1} E_B), ad[6 c + r] = entry (r, c)
+    const int i = blockIdx.x, k = threadIdx.x;
+    if (i >= n_inst || (mode && mode[i] != (DERIV ? 2 : 1))) return;  // uniform over the CTA
+    const double* p = partial + (size_t)i * slots * kOutDeriv;
+    if (k < NV) {
+        double v = 0.0;
+        for (int s = 0; s < slots; ++s) v += p[(size_t)s * kOutDeriv + k];
+        tot[k] = v;
+    }
+    const bool derive = DERIV && EA != nullptr;
+    if (derive && k < 36) ad[k] = adjoint_entry(EA + 16 * (size_t)i, EB + 16 * (size_t)i, k % 6, k / 6);
+    __syncthreads();
+    if (k >= NV) return;
+    double v = tot[k];
+    if (derive && k >= 12) {
+        const int b = k < 156 ? 12 : 156, r = (k - b) / 12, j = (k - b) % 12;
+        if (j >= 6) {  // column j of Km / Dm = -(columns 0-5) Ad e_{j-6} (+ C)
+            const double* m1 = tot + b + 12 * r;
+            const double* a = ad + 6 * (j - 6);
+            v = 0.0;
+            for (int c = 0; c < 3; ++c) v -= m1[c] * a[c] + m1[3 + c] * a[3 + c];
+            if (b == 156 && j < 9) v += tot[12 + 12 * r + j];  // C column j - 6, in Km's slot (r, j)
         }
-        double top[3], bot[3];
-        adjoint_column(EA + 16 * (size_t)i, EB + 16 * (size_t)i, j, top, bot);
-        for (int c = 0; c < 3; ++c) v -= km[c] * top[c] + km[3 + c] * bot[c];
-    } else {
-        for (int s = 0; s < slots; ++s) v += p[(size_t)s * kOutDeriv];
     }
     if (k < 12)
         out.fm[12 * (size_t)i + k] = v;
@@ -777,16 +811,18 @@ void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, c
     if (precision == kMixed && !STENCIL) {  // the FP32 fast path: specialised for brick-free grids
         if (plain)
             force_kernel<DERIV, STENCIL, float, false><<<grid, kChunk, 0, stream>>>(
-                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, bricks ? 1 : 0, s.slots);
+                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.pair32, s.partial, bricks ? 1 : 0, s.slots);
         if (bricks)
             force_kernel<DERIV, STENCIL, float, true><<<grid, kChunk, 0, stream>>>(
-                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.partial, plain ? 2 : 0, s.slots);
+                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.pair32, s.partial, plain ? 2 : 0, s.slots);
     } else if (precision == kMixed) {
         force_kernel<DERIV, STENCIL, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                         s.tile_count, s.partial, 0, s.slots);
+                                                                         s.tile_count, s.pair32, s.partial, 0,
+                                                                         s.slots);
     } else {
         force_kernel<DERIV, STENCIL, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                          s.tile_count, s.partial, 0, s.slots);
+                                                                          s.tile_count, s.pair64, s.partial, 0,
+                                                                          s.slots);
     }
 }
 
@@ -796,7 +832,8 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
                    const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream,
                    bool plain, bool bricks) {
     if (n_inst <= 0) return;
-    prep_kernel<<<(n_inst + 127) / 128, 128, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter);
+    prep_kernel<<<dim3((n_inst + 31) / 32, 3), 32, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter,
+                                                                s.pair32, s.pair64);
     if (total_tiles <= 0) return;
     if (plain)
         detect_kernel<false><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
@@ -856,18 +893,14 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
                      cudaStream_t stream, const int* mode, bool zero_status, const BatchInputs* derive_q2) {
     if (n_inst <= 0) return;
     if (zero_status) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out.status, n_inst);
-    const int NV = deriv ? kOutDeriv : kOutValue;
-    const size_t total = (size_t)n_inst * NV;
-    const int threads = 256;
-    const unsigned blocks = (unsigned)((total + threads - 1) / threads);
     const double* EA = derive_q2 ? derive_q2->EA : nullptr;
     const double* EB = derive_q2 ? derive_q2->EB : nullptr;
     if (deriv)
-        finalize_kernel<true><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA,
-                                                              EB, s.slots);
+        finalize_kernel<true><<<n_inst, 320, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA, EB,
+                                                          s.slots);
     else
-        finalize_kernel<false><<<blocks, threads, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
-                                                               nullptr, nullptr, s.slots);
+        finalize_kernel<false><<<n_inst, 64, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
+                                                          nullptr, nullptr, s.slots);
 }
 
 bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !stencil && precision == kMixed; }
@@ -879,17 +912,17 @@ void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const
     if (precision == kMixed) {
         if (stencil)
             energy_kernel<true, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids, s.tile_count,
-                                                                     s.partial, s.slots);
+                                                                     s.pair32, s.partial, s.slots);
         else
             energy_kernel<false, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                      s.tile_count, s.partial, s.slots);
+                                                                      s.tile_count, s.pair32, s.partial, s.slots);
     } else {
         if (stencil)
             energy_kernel<true, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                      s.tile_count, s.partial, s.slots);
+                                                                      s.tile_count, s.pair64, s.partial, s.slots);
         else
             energy_kernel<false, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                       s.tile_count, s.partial, s.slots);
+                                                                       s.tile_count, s.pair64, s.partial, s.slots);
     }
 }
 

@@ -115,6 +115,8 @@ struct BatchScratch {
     double* partial;            // n x slots x kOutDeriv
     unsigned long long* recheck;  // diagnostic counter of FP64 rechecks
     int slots;                  // force CTAs (partial rows) per instance
+    PairState<float>* pair32;   // n: each instance's pair state for the FP32 kernels (written by prep_kernel)
+    PairState<double>* pair64;  // n: the same for the FP64 kernels
 };
 
 enum Precision { kFP64 = 0, kMixed = 1 };
