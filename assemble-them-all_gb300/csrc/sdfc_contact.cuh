@@ -828,6 +828,13 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
     return F;
 }
 
+// Unrolling of the Jacobian's three-column loops (1: rolled; 3: unrolled, every unit
+// vector e_j a constant) — a compile-time tuning knob.
+#ifndef SDFC_COLUMN_UNROLL
+#define SDFC_COLUMN_UNROLL 1
+#endif
+constexpr int kColumnUnroll = SDFC_COLUMN_UNROLL;
+
 // Force plus Jacobian columns of one active contact
 // (ForceGeneralSDFContact::computeForceWithDerivative, :221-447, with
 // BodySDFObj::collision derivative form :278-377).
@@ -859,7 +866,10 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     const Vec3<T> xw1d = mul(R1, u1);
     const Vec3<T> gr = J.g;
     const T gn = norm(gr);
-    const Vec3<T> e = vec3<T>(gr.x / gn, gr.y / gn, gr.z / gn);
+    // FP32 path: the unit normal and de/dg through one reciprocal of |g|
+    constexpr bool kRecip = std::is_same<T, float>::value;
+    const T inv_gn = kRecip ? T(1) / gn : T(0);
+    const Vec3<T> e = kRecip ? inv_gn * gr : vec3<T>(gr.x / gn, gr.y / gn, gr.z / gn);
     const Vec3<T> n = mul(R2, e);
     const Vec3<T> xi2 = x - d * e;
     const Vec3<T> xdot = cross(x, w2) + mulT(R2, xw1d) - v2;
@@ -874,12 +884,13 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     Hm.m[0] = J.h[0]; Hm.m[1] = J.h[3]; Hm.m[2] = J.h[4];
     Hm.m[3] = J.h[3]; Hm.m[4] = J.h[1]; Hm.m[5] = J.h[5];
     Hm.m[6] = J.h[4]; Hm.m[7] = J.h[5]; Hm.m[8] = J.h[2];
-    Mat3<T> De;  // de/dg = (|g| I - g g^T / |g|) / |g|^2
+    Mat3<T> De;  // de/dg = (|g| I - g g^T / |g|) / |g|^2  (FP32 path: (I - e e^T) / |g|)
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            De.m[3 * r + c] = (gn * (r == c ? T(1) : T(0)) - comp(gr, r) * comp(gr, c) / gn) / (gn * gn);
+            De.m[3 * r + c] = kRecip ? ((r == c ? T(1) : T(0)) - comp(e, r) * comp(e, c)) * inv_gn
+                                     : (gn * (r == c ? T(1) : T(0)) - comp(gr, r) * comp(gr, c) / gn) / (gn * gn);
     const Mat3<T> de_dx = mul(De, Hm);
     const Mat3<T> R2T = transpose(R2);
     const Mat3<T> de_dxw = mul(de_dx, R2T);
@@ -1008,14 +1019,14 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     // translational (j >= 3) halves, so that each block's intermediate matrices die with its
     // loops and the j < 3 cases are resolved at compile time.  dq1 and dphi1 go through the
     // contact point: dxw1/dq1 = [-R1 skew(xi1) | R1] = dxw1dot/dphi1, dxw1dot/dq1 = [-R1 skew(u1) | 0].
-#pragma unroll 1
+#pragma unroll kColumnUnroll
     for (int j = 0; j < 3; ++j) {  // dq1, rotational
         const Vec3<T> a = mul(R1, cross(unit<T>(j), xi1));
         const Vec3<T> b = mul(R1, cross(unit<T>(j), u1));
         emit(j, 0, true, j, dot(dd_dxw, a), dot(dddot_dxw, a) + dot(dddot_dxwd, b), mul(dn_dxw, a),
              mul(dt_dxw, a) + (b - dot(n, b) * n), mul(dxi2_dxw, a));
     }
-#pragma unroll 1
+#pragma unroll kColumnUnroll
     for (int j = 3; j < 6; ++j) {  // dq1, translational (b = 0)
         const Vec3<T> a = col(R1, j - 3);
         emit(j, 0, false, j, dot(dd_dxw, a), dot(dddot_dxw, a), mul(dn_dxw, a), mul(dt_dxw, a), mul(dxi2_dxw, a));
@@ -1048,12 +1059,12 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
             emit(6 + j, 1, j < 3, j, dd_j, dddot_j, dn_j, dt_j, dxi2_j);
         }
     }
-#pragma unroll 1
+#pragma unroll kColumnUnroll
     for (int j = 0; j < 3; ++j) {  // dphi1, rotational
         const Vec3<T> a = mul(R1, cross(unit<T>(j), xi1));
         emit(12 + j, 2, true, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
     }
-#pragma unroll 1
+#pragma unroll kColumnUnroll
     for (int j = 3; j < 6; ++j) {  // dphi1, translational
         const Vec3<T> a = col(R1, j - 3);
         emit(12 + j, 2, false, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
@@ -1065,20 +1076,20 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
         // w x (xw1 - xw2) = w x (d n).  Hence Dm2 = -Dm1 Ad(E_A^{-1} E_B) + [C | 0], where column
         // j of C is the response to vw = d R2 (e_j x e) with ddot fixed (w = R2 e_j).  C's three
         // columns go to the (unused) dq2 accumulators of Km.
-#pragma unroll 1
+#pragma unroll kColumnUnroll
         for (int j = 0; j < 3; ++j) {
             const Vec3<T> dv = d * mul(R2, cross(unit<T>(j), e));
             emit(6 + j, 2, false, j, T(0), T(0), zero3, dv - dot(n, dv) * n, zero3);
         }
         return;
     }
-#pragma unroll 1
+#pragma unroll kColumnUnroll
     for (int j = 0; j < 3; ++j) {  // dphi2, rotational
         const T dddot_j = dot(gr, cross(x, unit<T>(j)));
         const Vec3<T> q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
         emit(18 + j, 3, true, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
     }
-#pragma unroll 1
+#pragma unroll kColumnUnroll
     for (int j = 3; j < 6; ++j) {  // dphi2, translational
         const T dddot_j = -comp(gr, j - 3);
         const Vec3<T> q = col(R2, j - 3);

@@ -564,6 +564,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     const int nchunks = (total + kChunk - 1) / kChunk;
     if (s < nchunks) {
         for (int chunk = s; chunk < nchunks; chunk += slots) {
+            if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
             const int c = chunk * kChunk + tid;
             const bool valid = c < total;
             V3 xi = v3(0, 0, 0);
@@ -665,6 +666,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
     const int total = prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
     for (int chunk = s; chunk < nchunks; chunk += slots) {
+        if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
         const int c = chunk * kChunk + tid;
         const bool valid = c < total;
         V3 xi = v3(0, 0, 0);
