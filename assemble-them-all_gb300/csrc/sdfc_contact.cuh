@@ -828,13 +828,6 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
     return F;
 }
 
-// Unrolling of the Jacobian's three-column loops (1: rolled; 3: unrolled, every unit
-// vector e_j a constant) — a compile-time tuning knob.
-#ifndef SDFC_COLUMN_UNROLL
-#define SDFC_COLUMN_UNROLL 1
-#endif
-constexpr int kColumnUnroll = SDFC_COLUMN_UNROLL;
-
 // Force plus Jacobian columns of one active contact
 // (ForceGeneralSDFContact::computeForceWithDerivative, :221-447, with
 // BodySDFObj::collision derivative form :278-377).
@@ -1015,85 +1008,82 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     };
     const Vec3<T> zero3 = vec3<T>(0, 0, 0);
 
-    // The column blocks run as separate loops, each split into its rotational (j < 3) and
-    // translational (j >= 3) halves, so that each block's intermediate matrices die with its
-    // loops and the j < 3 cases are resolved at compile time.  dq1 and dphi1 go through the
-    // contact point: dxw1/dq1 = [-R1 skew(xi1) | R1] = dxw1dot/dphi1, dxw1dot/dq1 = [-R1 skew(u1) | 0].
-#pragma unroll kColumnUnroll
-    for (int j = 0; j < 3; ++j) {  // dq1, rotational
-        const Vec3<T> a = mul(R1, cross(unit<T>(j), xi1));
-        const Vec3<T> b = mul(R1, cross(unit<T>(j), u1));
-        emit(j, 0, true, j, dot(dd_dxw, a), dot(dddot_dxw, a) + dot(dddot_dxwd, b), mul(dn_dxw, a),
+    // The column blocks run as separate loops, so that each block's intermediate matrices
+    // die with its loop; each loop holds one copy of emit and of the sink's warp sums (the
+    // kernel is sensitive to its code size).  dq1 and dphi1 go through the contact point:
+    // dxw1/dq1 = [-R1 skew(xi1) | R1] = dxw1dot/dphi1, dxw1dot/dq1 = [-R1 skew(u1) | 0].
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dq1
+        const Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
+        const Vec3<T> b = (j < 3) ? mul(R1, cross(unit<T>(j), u1)) : vec3<T>(0, 0, 0);
+        emit(j, 0, j < 3, j, dot(dd_dxw, a), dot(dddot_dxw, a) + dot(dddot_dxwd, b), mul(dn_dxw, a),
              mul(dt_dxw, a) + (b - dot(n, b) * n), mul(dxi2_dxw, a));
     }
-#pragma unroll kColumnUnroll
-    for (int j = 3; j < 6; ++j) {  // dq1, translational (b = 0)
-        const Vec3<T> a = col(R1, j - 3);
-        emit(j, 0, false, j, dot(dd_dxw, a), dot(dddot_dxw, a), mul(dn_dxw, a), mul(dt_dxw, a), mul(dxi2_dxw, a));
-    }
-    // skip_q2: the dq2 columns of Km are left to the caller, which derives them
-    // from the summed dq1 columns (finalize_kernel)
-    if (!skip_q2) {
-        const Vec3<T> rxd = mulT(R2, xw1d);
-#pragma unroll 1
-        for (int j = 0; j < 6; ++j) {  // dq2: dx/dq2 = [skew(x) | -I]
-            Vec3<T> dxj = (j < 3) ? cross(x, unit<T>(j)) : -unit<T>(j - 3);
-            const T dd_j = dot(gr, dxj);
-            Vec3<T> de_j = mul(de_dx, dxj);
-            Vec3<T> dn_j = mul(R2, de_j);
-            if (j < 3) dn_j = dn_j + mul(R2, cross(unit<T>(j), e));
-            const Vec3<T> dxi2_j = dxj - dd_j * e - d * de_j;
-            T dddot_j;
-            if (j < 3) {
-                // g^T(-Sw Sx + skew(R2^T xw_dot)) e_j + (H xdot)^T Sx e_j
-                Vec3<T> sxe = cross(x, unit<T>(j));
-                dddot_j = dot(gr, -cross(w2, sxe) + cross(rxd, unit<T>(j))) + dot(Hxdot, sxe);
-            } else {
-                dddot_j = dot(gr, cross(w2, unit<T>(j - 3))) - comp(Hxdot, j - 3);
-            }
-            // dxw2dot/dq2 = [-R2 skew(w2 x xi2 + v2) + R2 Sw dxi2_dq2.left | R2 Sw dxi2_dq2.right]
-            Vec3<T> dxw2d_j = mul(R2Sw, dxi2_j);
-            if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit<T>(j)));
-            // dtdot/dq2 = -dxw2d - nvw dn - n (vw.dn - n.dxw2d)
-            const Vec3<T> dt_j = -dxw2d_j - nvw * dn_j - (dot(vw, dn_j) - dot(n, dxw2d_j)) * n;
-            emit(6 + j, 1, j < 3, j, dd_j, dddot_j, dn_j, dt_j, dxi2_j);
-        }
-    }
-#pragma unroll kColumnUnroll
-    for (int j = 0; j < 3; ++j) {  // dphi1, rotational
-        const Vec3<T> a = mul(R1, cross(unit<T>(j), xi1));
-        emit(12 + j, 2, true, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
-    }
-#pragma unroll kColumnUnroll
-    for (int j = 3; j < 6; ++j) {  // dphi1, translational
-        const Vec3<T> a = col(R1, j - 3);
-        emit(12 + j, 2, false, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
-    }
     if (skip_q2) {
-        // The dphi2 columns of Dm are derived by the caller as well: the force depends on the
-        // velocities through ddot and the relative velocity vw, and for a common world twist
-        // (rotation w about the origin) of both bodies ddot is unchanged while vw gains
-        // w x (xw1 - xw2) = w x (d n).  Hence Dm2 = -Dm1 Ad(E_A^{-1} E_B) + [C | 0], where column
-        // j of C is the response to vw = d R2 (e_j x e) with ddot fixed (w = R2 e_j).  C's three
-        // columns go to the (unused) dq2 accumulators of Km.
-#pragma unroll kColumnUnroll
-        for (int j = 0; j < 3; ++j) {
-            const Vec3<T> dv = d * mul(R2, cross(unit<T>(j), e));
-            emit(6 + j, 2, false, j, T(0), T(0), zero3, dv - dot(n, dv) * n, zero3);
+        // The dq2 columns of Km are derived by the caller (finalize_kernel) from the summed dq1
+        // columns, and so are the dphi2 columns of Dm: the force depends on the velocities
+        // through ddot and the relative velocity vw, and for a common world twist (rotation w
+        // about the origin) of both bodies ddot is unchanged while vw gains
+        // w x (xw1 - xw2) = w x (d n).  Hence Dm2 = -Dm1 Ad(E_A^{-1} E_B) + [C | 0], where
+        // column j of C is the response to vw = d R2 (e_j x e) with ddot fixed (w = R2 e_j).
+        // Iterations 0-5: the dphi1 columns; 6-8: C's columns, into the (unused) dq2
+        // accumulators of Km.
+#pragma unroll 1
+        for (int j = 0; j < 9; ++j) {
+            Vec3<T> dv;
+            T dq;
+            if (j < 6) {
+                dv = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
+                dq = dot(dddot_dxwd, dv);
+            } else {
+                dv = d * mul(R2, cross(unit<T>(j - 6), e));
+                dq = T(0);
+            }
+            emit(j < 6 ? 12 + j : j, 2, false, j, T(0), dq, zero3, dv - dot(n, dv) * n, zero3);
         }
         return;
     }
-#pragma unroll kColumnUnroll
-    for (int j = 0; j < 3; ++j) {  // dphi2, rotational
-        const T dddot_j = dot(gr, cross(x, unit<T>(j)));
-        const Vec3<T> q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
-        emit(18 + j, 3, true, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
+    const Vec3<T> rxd = mulT(R2, xw1d);
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dq2: dx/dq2 = [skew(x) | -I]
+        Vec3<T> dxj = (j < 3) ? cross(x, unit<T>(j)) : -unit<T>(j - 3);
+        const T dd_j = dot(gr, dxj);
+        Vec3<T> de_j = mul(de_dx, dxj);
+        Vec3<T> dn_j = mul(R2, de_j);
+        if (j < 3) dn_j = dn_j + mul(R2, cross(unit<T>(j), e));
+        const Vec3<T> dxi2_j = dxj - dd_j * e - d * de_j;
+        T dddot_j;
+        if (j < 3) {
+            // g^T(-Sw Sx + skew(R2^T xw_dot)) e_j + (H xdot)^T Sx e_j
+            Vec3<T> sxe = cross(x, unit<T>(j));
+            dddot_j = dot(gr, -cross(w2, sxe) + cross(rxd, unit<T>(j))) + dot(Hxdot, sxe);
+        } else {
+            dddot_j = dot(gr, cross(w2, unit<T>(j - 3))) - comp(Hxdot, j - 3);
+        }
+        // dxw2dot/dq2 = [-R2 skew(w2 x xi2 + v2) + R2 Sw dxi2_dq2.left | R2 Sw dxi2_dq2.right]
+        Vec3<T> dxw2d_j = mul(R2Sw, dxi2_j);
+        if (j < 3) dxw2d_j = dxw2d_j - mul(R2, cross(wxi, unit<T>(j)));
+        // dtdot/dq2 = -dxw2d - nvw dn - n (vw.dn - n.dxw2d)
+        const Vec3<T> dt_j = -dxw2d_j - nvw * dn_j - (dot(vw, dn_j) - dot(n, dxw2d_j)) * n;
+        emit(6 + j, 1, j < 3, j, dd_j, dddot_j, dn_j, dt_j, dxi2_j);
     }
-#pragma unroll kColumnUnroll
-    for (int j = 3; j < 6; ++j) {  // dphi2, translational
-        const T dddot_j = -comp(gr, j - 3);
-        const Vec3<T> q = col(R2, j - 3);
-        emit(18 + j, 3, false, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dphi1
+        const Vec3<T> a = (j < 3) ? mul(R1, cross(unit<T>(j), xi1)) : col(R1, j - 3);
+        emit(12 + j, 2, j < 3, j, T(0), dot(dddot_dxwd, a), zero3, a - dot(n, a) * n, zero3);
+    }
+#pragma unroll 1
+    for (int j = 0; j < 6; ++j) {  // dphi2
+        T dddot_j;
+        Vec3<T> q;
+        if (j < 3) {
+            dddot_j = dot(gr, cross(x, unit<T>(j)));
+            q = mul(R2, cross(unit<T>(j), xi2));  // dxw2dot/dphi2 column R2 (e_j x xi2)
+        } else {
+            dddot_j = -comp(gr, j - 3);
+            q = col(R2, j - 3);
+        }
+        emit(18 + j, 3, j < 3, j, T(0), dddot_j, zero3, -(q - dot(n, q) * n), zero3);
     }
 }
 
