@@ -509,6 +509,8 @@ __device__ __forceinline__ Vec3<T> hess_mul(const T* h, Vec3<T> v) {
 // ---------------------------------------------------------------- per-contact force
 struct ContactParams {
     double kn, kt, mu, kd;  // kn, kt already scaled by scale * contact_scale (ForceGeneralSDFContact.cpp:155-156)
+    float kn32, kt32, mu32, kd32;  // the same rounded to FP32 (the FP32 path's coefficients)
+    bool friction;          // mu > eps (ForceGeneralSDFContact.cpp:199, 341)
 };
 
 constexpr double kFrictionEps = 1e-8;  // constants::eps, simulation/redmax/Utils.h:9
@@ -516,6 +518,16 @@ constexpr double kFrictionEps = 1e-8;  // constants::eps, simulation/redmax/Util
 struct BodyState {
     Pose P;
     V3 w, v;  // phi = (w, v), body frame
+};
+
+// The FP32 fast path's map from the contact body's frame to the SDF grid:
+// cell coordinates c = Rc xi + pc in FP64 (Rc = diag(1/dx) R_B^T R_A,
+// pc = diag(1/dx) R_B^T (p_A - p_B) - org) and the grid-frame point in FP32.
+struct CellMap {
+    M3 Rc;
+    V3 pc;
+    Mat3<float> Rf;
+    Vec3<float> pf;
 };
 
 // Per-instance state of a pair as a force thread holds it: the FP64 poses and
@@ -529,6 +541,7 @@ struct PairState {
     ContactParams cp;
     M3 RT;  // R_B^T R_A
     V3 pT;  // R_B^T (p_A - p_B)
+    CellMap cm;  // set by make_cell_map
 };
 
 template <typename T>
@@ -550,8 +563,26 @@ __device__ __forceinline__ void make_pair_state(const double* EA, const double* 
     S.cp.kt = prm[1] * prm[4] * prm[5];
     S.cp.mu = prm[2];
     S.cp.kd = prm[3];
+    S.cp.kn32 = (float)S.cp.kn;
+    S.cp.kt32 = (float)S.cp.kt;
+    S.cp.mu32 = (float)S.cp.mu;
+    S.cp.kd32 = (float)S.cp.kd;
+    S.cp.friction = S.cp.mu > kFrictionEps;
     S.RT = mul(transpose(S.B.P.R), S.A.P.R);
     S.pT = mulT(S.B.P.R, S.A.P.p - S.B.P.p);
+}
+
+// The pair's CellMap on grid g (after make_pair_state).
+template <typename T>
+__device__ __forceinline__ void make_cell_map(const GridDesc& g, PairState<T>& S) {
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) S.cm.Rc.m[3 * r + c] = S.RT.m[3 * r + c] * g.inv_dx[r];
+        const double p = r == 0 ? S.pT.x : (r == 1 ? S.pT.y : S.pT.z);
+        const double q = fma(p, g.inv_dx[r], -g.org[r]);
+        if (r == 0) S.cm.pc.x = q; else if (r == 1) S.cm.pc.y = q; else S.cm.pc.z = q;
+    }
+    S.cm.Rf = cast<float>(S.RT);
+    S.cm.pf = cast<float>(S.pT);
 }
 
 // Cell of an active contact for the FP32 throughput path: the grid-frame point
@@ -563,21 +594,21 @@ __device__ __forceinline__ void make_pair_state(const double* EA, const double* 
 // within FP32 round-off of a face, which `ok` rejects.  Active contacts lie
 // inside the grid box (detection guarantees it), so no box test is needed.
 struct FastCell {
-    V3 y;
+    Vec3<float> y;  // grid-frame point (FP32)
     double ud, vd, wd;
     int i, j, k;
     bool ok;
 };
 
 template <typename T>
-__device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const M3& RT, V3 pT, V3 xi) {
+__device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const CellMap& cm, V3 xi) {
     FastCell c;
-    c.y = v3(fma(RT.m[0], xi.x, fma(RT.m[1], xi.y, fma(RT.m[2], xi.z, pT.x))),
-             fma(RT.m[3], xi.x, fma(RT.m[4], xi.y, fma(RT.m[5], xi.z, pT.y))),
-             fma(RT.m[6], xi.x, fma(RT.m[7], xi.y, fma(RT.m[8], xi.z, pT.z))));
-    const double cx = fma(c.y.x, g.inv_dx[0], -g.org[0]);
-    const double cy = fma(c.y.y, g.inv_dx[1], -g.org[1]);
-    const double cz = fma(c.y.z, g.inv_dx[2], -g.org[2]);
+    const M3& R = cm.Rc;
+    const double cx = fma(R.m[0], xi.x, fma(R.m[1], xi.y, fma(R.m[2], xi.z, cm.pc.x)));
+    const double cy = fma(R.m[3], xi.x, fma(R.m[4], xi.y, fma(R.m[5], xi.z, cm.pc.y)));
+    const double cz = fma(R.m[6], xi.x, fma(R.m[7], xi.y, fma(R.m[8], xi.z, cm.pc.z)));
+    const Vec3<float> xf = vec3<float>((float)xi.x, (float)xi.y, (float)xi.z);
+    c.y = mul(cm.Rf, xf) + cm.pf;
     c.i = (int)floorf((float)cx);
     c.j = (int)floorf((float)cy);
     c.k = (int)floorf((float)cz);
@@ -645,16 +676,17 @@ __device__ inline void warp_exact_jets(const GridDesc& g, const PairState<T>& S,
 //   Fast path (T = float with a FastCell `fc` whose `ok` is set): the depth by
 //   FP64 trilinear interpolation at the FastCell, the gradient / Hessian in
 //   FP32; the depth then differs from the reference's by FP64 round-off only.
+// x: the grid-frame point in the algebra type (on the fast path computed in FP32).
 // `valid == false` marks a padding lane: the grid is not read and the result
 // is discarded by the caller, but the lane still walks the same code so that
 // warp collectives downstream see every lane.
 // BR = false: specialised for grids without FP16 bricks (the caller guarantees it).
 template <typename T, bool BR = true>
 __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S, V3 xi, const FastCell* fc,
-                                        bool want_hessian, bool valid, bool stencil_only, V3& x, double& d,
+                                        bool want_hessian, bool valid, bool stencil_only, Vec3<T>& x, double& d,
                                         SdfJet<T>& J, const ExactJet<T>* ej = nullptr) {
     if (!valid) {
-        x = xi;
+        x = cast<T>(xi);
         d = -1.0;
         J.v = -1.0;
         J.g = vec3<T>(1, 0, 0);
@@ -662,7 +694,7 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
         return;
     }
     if (ej && ej->set) {  // computed by the warp (warp_exact_jets)
-        x = ej->x;
+        x = cast<T>(ej->x);
         J = ej->J;
         d = J.v + g.col_th;
         return;
@@ -710,8 +742,9 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             return;
         }
     }
-    x = grid_point(S.B.P.R, S.B.P.p, world_point(S.A.P.R, S.A.P.p, xi));
-    sdf_jet(g, x, J, want_hessian, stencil_only);
+    const V3 xe = grid_point(S.B.P.R, S.B.P.p, world_point(S.A.P.R, S.A.P.p, xi));
+    sdf_jet(g, xe, J, want_hessian, stencil_only);
+    x = cast<T>(xe);
     d = J.v + g.col_th;
 }
 
@@ -730,22 +763,31 @@ struct ContactEnergy {
 template <typename T, bool BR = true>
 __device__ inline ContactEnergy<T> contact_energy(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
                                                   bool valid, bool stencil_only, const ExactJet<T>* ej = nullptr) {
-    V3 xd;
+    Vec3<T> x;
     double dd;
     SdfJet<T> J;
-    contact_geometry<T, BR>(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
+    contact_geometry<T, BR>(g, S, xi1d, fc, false, valid, stencil_only, x, dd, J, ej);
     ContactEnergy<T> E;
     const double kn = S.cp.kn;
     E.e = valid ? 0.5 * kn * dd * dd : 0.0;
     const T s = valid ? (T)(kn * dd) : T(0);
     const Vec3<T> gr = J.g;
-    const Vec3<T> x = cast<T>(xd), xi1 = cast<T>(xi1d);
+    const Vec3<T> xi1 = cast<T>(xi1d);
     const Vec3<T> ga = mulT(S.R1, mul(S.R2, gr));
     E.av = s * ga;
     E.aw = s * cross(xi1, ga);
     E.bw = s * cross(gr, x);
     E.bv = -s * gr;
     return E;
+}
+
+// A coefficient in the algebra type: the FP64 value, or its FP32 rounding kept in ContactParams.
+template <typename T>
+__device__ __forceinline__ T fp_coef(double v, float v32) {
+    if constexpr (std::is_same<T, float>::value)
+        return v32;
+    else
+        return v;
 }
 
 // The force-law scalars s1 = -kn d + kd ddot d and sK = kn d - kd ddot d
@@ -755,7 +797,7 @@ template <typename T>
 __device__ __forceinline__ void force_scalars(const ContactParams& cp, double dd, T ddot, T& s1, T& sK) {
     if constexpr (std::is_same<T, float>::value) {
         const float df = (float)dd;
-        const float k = (float)cp.kd * ddot - (float)cp.kn;
+        const float k = cp.kd32 * ddot - cp.kn32;
         s1 = df * k;
         sK = -s1;
     } else {
@@ -768,7 +810,7 @@ __device__ __forceinline__ void force_scalars(const ContactParams& cp, double dd
 template <typename T>
 __device__ __forceinline__ bool static_friction(const ContactParams& cp, T fc_norm, T tn) {
     if constexpr (std::is_same<T, float>::value)
-        return (float)cp.mu * fc_norm >= (float)cp.kt * tn - (float)kFrictionEps;
+        return cp.mu32 * fc_norm >= cp.kt32 * tn - (float)kFrictionEps;
     else
         return cp.mu * fc_norm >= cp.kt * tn - kFrictionEps;
 }
@@ -783,15 +825,14 @@ struct ContactForce {
 template <typename T, bool BR = true>
 __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, const PairState<T>& S, const FastCell* fc,
                                                 bool valid, bool stencil_only, const ExactJet<T>* ej = nullptr) {
-    V3 xd;
+    Vec3<T> x;
     double dd;
     SdfJet<T> J;
-    contact_geometry<T, BR>(g, S, xi1d, fc, false, valid, stencil_only, xd, dd, J, ej);
+    contact_geometry<T, BR>(g, S, xi1d, fc, false, valid, stencil_only, x, dd, J, ej);
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;
     const Vec3<T> xi1 = cast<T>(xi1d);
-    const Vec3<T> x = cast<T>(xd);
     const Vec3<T> xw1d = mul(R1, cross(S.w1, xi1) + S.v1);  // R1 (skew(xi1)^T w1 + v1)
     const T gn = norm(J.g);
     const Vec3<T> e = vec3<T>(J.g.x / gn, J.g.y / gn, J.g.z / gn);
@@ -810,12 +851,12 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
     F.xi2 = xi2;
     F.f1 = s1 * rho1;
     F.f2 = sK * rho2;
-    if (cp.mu > kFrictionEps) {
+    if (cp.friction) {
         const Vec3<T> c1 = cross(xi1, rho1);
         const T fc_norm = fabs(s1) * sqrt(dot(c1, c1) + dot(rho1, rho1));
         const T tn = norm(t);
         const Vec3<T> tau1 = mulT(R1, t), tau2 = mulT(R2, t);
-        const T mu = (T)cp.mu, kt = (T)cp.kt;
+        const T mu = fp_coef<T>(cp.mu, cp.mu32), kt = fp_coef<T>(cp.kt, cp.kt32);
         if (static_friction(cp, fc_norm, tn)) {
             F.f1 = F.f1 - kt * tau1;
             F.f2 = F.f2 + kt * tau2;
@@ -840,10 +881,10 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
                                               Sink& sink, bool valid, bool stencil_only,
                                               const ExactJet<T>* ej = nullptr, bool skip_q2 = false) {
     // collision, :292-310
-    V3 xd;
+    Vec3<T> x;
     double dd;
     SdfJet<T> J;
-    contact_geometry<T, BR>(g, S, xi1d, fc, true, valid, stencil_only, xd, dd, J, ej);
+    contact_geometry<T, BR>(g, S, xi1d, fc, true, valid, stencil_only, x, dd, J, ej);
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;
@@ -852,7 +893,6 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     const Vec3<T>& w2 = S.w2;
     const Vec3<T>& v2 = S.v2;
     const Vec3<T> xi1 = cast<T>(xi1d);
-    const Vec3<T> x = cast<T>(xd);
     const T d = (T)dd;
     // kinematics of the contact point, :238-252
     const Vec3<T> u1 = cross(w1, xi1) + v1;  // skew(xi1)^T w1 + v1
@@ -918,7 +958,8 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     // dtdot/dxw_dot = I - n n^T (applied as P v = v - n (n.v))
 
     // force-law scalars, :300-328 (the depth-dependent magnitudes from the FP64 depth)
-    const T kn = (T)cp.kn, kt = (T)cp.kt, mu = (T)cp.mu, kd = (T)cp.kd;
+    const T kn = fp_coef<T>(cp.kn, cp.kn32), kt = fp_coef<T>(cp.kt, cp.kt32), mu = fp_coef<T>(cp.mu, cp.mu32),
+            kd = fp_coef<T>(cp.kd, cp.kd32);
     T s1, sK;
     force_scalars(cp, dd, ddot, s1, sK);
     const Vec3<T> rho1 = mulT(R1, n);
@@ -926,7 +967,7 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     const Vec3<T> xr1 = cross(xi1, rho1);
     Vec3<T> f1 = s1 * rho1, f2 = sK * rho2;
 
-    const bool friction = cp.mu > kFrictionEps;
+    const bool friction = cp.friction;
     T fc_norm = 0, tn = 0, ratio = 0;
     bool stat = true;
     Vec3<T> tau1 = vec3<T>(0, 0, 0), tau2 = vec3<T>(0, 0, 0);

@@ -65,8 +65,10 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
         pref[i] = f;
     } else if (blockIdx.y == 1) {
         make_pair_state(in.EA + 16 * o, in.phiA + 6 * o, in.EB + 16 * o, in.phiB + 6 * o, in.prm + 6 * o, pair32[i]);
+        make_cell_map(grids[inst[i].grid], pair32[i]);
     } else {
         make_pair_state(in.EA + 16 * o, in.phiA + 6 * o, in.EB + 16 * o, in.phiB + 6 * o, in.prm + 6 * o, pair64[i]);
+        make_cell_map(grids[inst[i].grid], pair64[i]);
     }
 }
 
@@ -586,7 +588,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             ExactJet<T> ej;
             const ExactJet<T>* ejp = nullptr;
             if constexpr (kWarpExact) {
-                fc = fast_cell<T>(g, S.RT, S.pT, xi);
+                fc = fast_cell<T>(g, S.cm, xi);
                 fcp = &fc;
                 warp_exact_jets<T>(g, S, xi, valid && !fc.ok, DERIV, ej);
                 ejp = &ej;
@@ -686,7 +688,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
         ExactJet<T> ej;
         const ExactJet<T>* ejp = nullptr;
         if constexpr (kWarpExact) {
-            fc = fast_cell<T>(g, S.RT, S.pT, xi);
+            fc = fast_cell<T>(g, S.cm, xi);
             fcp = &fc;
             warp_exact_jets<T>(g, S, xi, valid && !fc.ok, false, ej);
             ejp = &ej;
