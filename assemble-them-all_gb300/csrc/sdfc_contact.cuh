@@ -528,6 +528,7 @@ struct CellMap {
     V3 pc;
     Mat3<float> Rf;
     Vec3<float> pf;
+    Vec3<float> of;  // -org in FP32 (cell coordinate = y / dx - org)
 };
 
 // Per-instance state of a pair as a force thread holds it: the FP64 poses and
@@ -583,6 +584,7 @@ __device__ __forceinline__ void make_cell_map(const GridDesc& g, PairState<T>& S
     }
     S.cm.Rf = cast<float>(S.RT);
     S.cm.pf = cast<float>(S.pT);
+    S.cm.of = vec3<float>((float)-g.org[0], (float)-g.org[1], (float)-g.org[2]);
 }
 
 // Cell of an active contact for the FP32 throughput path: the grid-frame point
@@ -594,6 +596,7 @@ __device__ __forceinline__ void make_cell_map(const GridDesc& g, PairState<T>& S
 // within FP32 round-off of a face, which `ok` rejects.  Active contacts lie
 // inside the grid box (detection guarantees it), so no box test is needed.
 struct FastCell {
+    Vec3<float> xi32;  // the contact point in its body's frame (FP32)
     Vec3<float> y;  // grid-frame point (FP32)
     double ud, vd, wd;
     int i, j, k;
@@ -601,17 +604,20 @@ struct FastCell {
 };
 
 template <typename T>
-__device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const CellMap& cm, V3 xi) {
+__device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const CellMap& cm, V3 xi, Vec3<float> xf) {
     FastCell c;
     const M3& R = cm.Rc;
     const double cx = fma(R.m[0], xi.x, fma(R.m[1], xi.y, fma(R.m[2], xi.z, cm.pc.x)));
     const double cy = fma(R.m[3], xi.x, fma(R.m[4], xi.y, fma(R.m[5], xi.z, cm.pc.y)));
     const double cz = fma(R.m[6], xi.x, fma(R.m[7], xi.y, fma(R.m[8], xi.z, cm.pc.z)));
-    const Vec3<float> xf = vec3<float>((float)xi.x, (float)xi.y, (float)xi.z);
+    c.xi32 = xf;
     c.y = mul(cm.Rf, xf) + cm.pf;
-    c.i = (int)floorf((float)cx);
-    c.j = (int)floorf((float)cy);
-    c.k = (int)floorf((float)cz);
+    // the cell from the FP32 point (any cell within FP32 round-off of the true one; where it
+    // is not the FP64 coordinate's own cell the FP64 fraction below leaves [eps, 1 - eps] and
+    // `ok` rejects the contact)
+    c.i = (int)floorf(fmaf(c.y.x, g.finv_dx[0], cm.of.x));
+    c.j = (int)floorf(fmaf(c.y.y, g.finv_dx[1], cm.of.y));
+    c.k = (int)floorf(fmaf(c.y.z, g.finv_dx[2], cm.of.z));
     c.ud = cx - (double)c.i;
     c.vd = cy - (double)c.j;
     c.wd = cz - (double)c.k;
@@ -668,6 +674,15 @@ __device__ inline void warp_exact_jets(const GridDesc& g, const PairState<T>& S,
             for (int k = 0; k < 6; ++k) ej.J.h[k] = want_hessian ? (T)hs[k] : T(0);
         }
     }
+}
+
+// The contact point in the algebra type (from the FastCell's FP32 copy on the fast path).
+template <typename T>
+__device__ __forceinline__ Vec3<T> point_in(V3 xi, const FastCell* fc) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (fc) return fc->xi32;
+    }
+    return cast<T>(xi);
 }
 
 // Grid-frame point, depth and SDF jet of one contact.
@@ -772,7 +787,7 @@ __device__ inline ContactEnergy<T> contact_energy(const GridDesc& g, V3 xi1d, co
     E.e = valid ? 0.5 * kn * dd * dd : 0.0;
     const T s = valid ? (T)(kn * dd) : T(0);
     const Vec3<T> gr = J.g;
-    const Vec3<T> xi1 = cast<T>(xi1d);
+    const Vec3<T> xi1 = point_in<T>(xi1d, fc);
     const Vec3<T> ga = mulT(S.R1, mul(S.R2, gr));
     E.av = s * ga;
     E.aw = s * cross(xi1, ga);
@@ -832,7 +847,7 @@ __device__ inline ContactForce<T> contact_force(const GridDesc& g, V3 xi1d, cons
     const ContactParams& cp = S.cp;
     const Mat3<T>& R1 = S.R1;
     const Mat3<T>& R2 = S.R2;
-    const Vec3<T> xi1 = cast<T>(xi1d);
+    const Vec3<T> xi1 = point_in<T>(xi1d, fc);
     const Vec3<T> xw1d = mul(R1, cross(S.w1, xi1) + S.v1);  // R1 (skew(xi1)^T w1 + v1)
     const T gn = norm(J.g);
     const Vec3<T> e = vec3<T>(J.g.x / gn, J.g.y / gn, J.g.z / gn);
@@ -892,7 +907,7 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     const Vec3<T>& v1 = S.v1;
     const Vec3<T>& w2 = S.w2;
     const Vec3<T>& v2 = S.v2;
-    const Vec3<T> xi1 = cast<T>(xi1d);
+    const Vec3<T> xi1 = point_in<T>(xi1d, fc);
     const T d = (T)dd;
     // kinematics of the contact point, :238-252
     const Vec3<T> u1 = cross(w1, xi1) + v1;  // skew(xi1)^T w1 + v1

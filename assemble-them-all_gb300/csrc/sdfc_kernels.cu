@@ -113,6 +113,10 @@ __device__ __forceinline__ float trilinear32(const float4* __restrict__ cells, c
 __device__ __forceinline__ V3 load_point(const PointsDesc& P, int id) {
     return v3(__ldg(P.x64 + id), __ldg(P.x64 + P.n + id), __ldg(P.x64 + 2 * (size_t)P.n + id));
 }
+// The same point rounded to FP32 (exactly the stored point for FP32 storage).
+__device__ __forceinline__ Vec3<float> load_point32(const PointsDesc& P, int id) {
+    return vec3<float>(__ldg(P.x32 + id), __ldg(P.x32 + P.n + id), __ldg(P.x32 + 2 * (size_t)P.n + id));
+}
 
 // distance() of the reference on the FP64 path (BodySDFObj.cpp:207-213 after
 // CollisionDetection.cpp:136): xw = R_A xi + p_A, x = R_B^T (xw - p_B).
@@ -570,6 +574,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             const int c = chunk * kChunk + tid;
             const bool valid = c < total;
             V3 xi = v3(0, 0, 0);
+            Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
             int sid = 0;
             if (valid) {
                 int lo = 0, hi = I.ntiles;  // largest k with prefix[k] <= c
@@ -582,13 +587,14 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
                 }
                 sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
                 xi = load_point(P, sid);
+                if constexpr (kWarpExact) xf = load_point32(P, sid);
             }
             FastCell fc;
             const FastCell* fcp = nullptr;
             ExactJet<T> ej;
             const ExactJet<T>* ejp = nullptr;
             if constexpr (kWarpExact) {
-                fc = fast_cell<T>(g, S.cm, xi);
+                fc = fast_cell<T>(g, S.cm, xi, xf);
                 fcp = &fc;
                 warp_exact_jets<T>(g, S, xi, valid && !fc.ok, DERIV, ej);
                 ejp = &ej;
@@ -672,6 +678,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
         const int c = chunk * kChunk + tid;
         const bool valid = c < total;
         V3 xi = v3(0, 0, 0);
+        Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
         if (valid) {
             int lo = 0, hi = I.ntiles;
             while (hi - lo > 1) {
@@ -681,14 +688,16 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
                 else
                     hi = mid;
             }
-            xi = load_point(P, ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])]);
+            const int sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
+            xi = load_point(P, sid);
+            if constexpr (kWarpExact) xf = load_point32(P, sid);
         }
         FastCell fc;
         const FastCell* fcp = nullptr;
         ExactJet<T> ej;
         const ExactJet<T>* ejp = nullptr;
         if constexpr (kWarpExact) {
-            fc = fast_cell<T>(g, S.cm, xi);
+            fc = fast_cell<T>(g, S.cm, xi, xf);
             fcp = &fc;
             warp_exact_jets<T>(g, S, xi, valid && !fc.ok, false, ej);
             ejp = &ej;
