@@ -393,11 +393,16 @@ def run_gpu(args, world, rank):
     # algorithmic bytes: detection reads 12 B per point and 8 FP32 corners (32 B) per query
     det_bytes = pts_per_step * (12 + 8 * 4)
     # forces: per active contact its id (4 B), point (12 B) and 8 FP32 corners; per instance-slot 300 FP64 partials
-    frc_bytes = n_active * (4 + 12 + 32) + n * 8 * 300 * 8
+    # per instance-slot 300 FP64 partials (the library's slots per instance: about six waves of
+    # force CTAs, slots_for in csrc/sdfc_kernels.cuh)
+    slots = 1
+    while slots < 32 and slots * n < 152 * 4 * 6:
+        slots *= 2
+    frc_bytes = n_active * (4 + 12 + 32) + n * slots * 300 * 8
     kernels = {
         "detect": {"ms": det_ms, "bytes": det_bytes},
         "force_kernel": {"ms": frc_ms, "bytes": frc_bytes},
-        "finalize_kernel": {"ms": red_ms, "bytes": n * 8 * 300 * 8 + n * 300 * 8},
+        "finalize_kernel": {"ms": red_ms, "bytes": n * slots * 300 * 8 + n * 300 * 8},
     }
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     ach = kernels[dom]["bytes"] / (kernels[dom]["ms"] / 1e3) / 1e9
