@@ -62,6 +62,8 @@ void free_batch(sdfc_batch* b) {
     cudaFreeHost(b->h_in);
     cudaFreeHost(b->h_out);
     cudaFreeHost(b->h_int);
+    cudaFreeHost(b->h_io);
+    cudaFree(b->d_io);
     for (cudaEvent_t e : b->ev)
         if (e) cudaEventDestroy(e);
     for (cudaGraphExec_t g : b->eval_exec)
@@ -202,13 +204,15 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||
         (rc = alloc((void**)&b->d_in, sizeof(double) * (size_t)n * 50)) ||
         (rc = alloc((void**)&b->d_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv)) ||
-        (rc = alloc((void**)&b->d_int, sizeof(int) * (size_t)n * 2))) {
+        (rc = alloc((void**)&b->d_int, sizeof(int) * (size_t)n * 2)) ||
+        (rc = alloc((void**)&b->d_io, sizeof(sdfc::HostIO)))) {
         free_batch(b);
         return rc;
     }
     if (cudaMallocHost((void**)&b->h_in, sizeof(double) * (size_t)n * 50) != cudaSuccess ||
         cudaMallocHost((void**)&b->h_out, sizeof(double) * (size_t)n * sdfc::kOutDeriv) != cudaSuccess ||
-        cudaMallocHost((void**)&b->h_int, sizeof(int) * (size_t)n * 2) != cudaSuccess) {
+        cudaMallocHost((void**)&b->h_int, sizeof(int) * (size_t)n * 2) != cudaSuccess ||
+        cudaMallocHost((void**)&b->h_io, sizeof(sdfc::HostIO)) != cudaSuccess) {
         free_batch(b);
         return fail(ctx, SDFC_ERR_CUDA, "batch_create: cudaMallocHost failed");
     }
@@ -723,14 +727,22 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
     double* o = b->d_out;
     const size_t nout = dv ? 300 * n : 12 * n;
     static_assert(sizeof(sdfc_params) == 6 * sizeof(double), "sdfc_params rows are the kernels' 6 doubles");
-    // Inputs: where the device reads pageable memory through the host page tables (Grace: the
-    // C2C link), straight from the caller's arrays; elsewhere staged through pinned buffers.
-    if (ctx->pageable_direct) {
-        CUDA_TRY(ctx, cudaMemcpyAsync(d, E_A, sizeof(double) * 16 * n, cudaMemcpyHostToDevice, s));
-        CUDA_TRY(ctx, cudaMemcpyAsync(d + 16 * n, phi_A, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s));
-        CUDA_TRY(ctx, cudaMemcpyAsync(d + 22 * n, E_B, sizeof(double) * 16 * n, cudaMemcpyHostToDevice, s));
-        CUDA_TRY(ctx, cudaMemcpyAsync(d + 38 * n, phi_B, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s));
-        CUDA_TRY(ctx, cudaMemcpyAsync(d + 44 * n, params, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s));
+    // Where the device reads pageable memory through the host page tables (Grace: the C2C
+    // link), the evaluation's kernels read the caller's input arrays and write its output
+    // arrays themselves (gather_inputs_kernel; finalize_kernel's indirect outputs): per call only
+    // the arrays' addresses go to the device.  Elsewhere inputs and outputs are staged through
+    // pinned buffers.
+    const bool direct = ctx->pageable_direct;
+    if (direct) {
+        sdfc::HostIO* io = b->h_io;
+        io->in[0] = E_A;
+        io->in[1] = phi_A;
+        io->in[2] = E_B;
+        io->in[3] = phi_B;
+        io->in[4] = reinterpret_cast<const double*>(params);
+        io->out = sdfc::BatchOutputs{fm, dv ? Km : nullptr, dv ? Dm : nullptr, n_active ? n_active : b->d_int,
+                                     status ? status : b->d_int + n};
+        CUDA_TRY(ctx, cudaMemcpyAsync(b->d_io, io, sizeof(sdfc::HostIO), cudaMemcpyHostToDevice, s));
     } else {
         double* h = b->h_in;
         std::memcpy(h, E_A, sizeof(double) * 16 * n);
@@ -742,8 +754,13 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
     }
     // the evaluation's kernels, captured once per (derivative flag, modes)
     auto enqueue = [&](cudaStream_t st) -> int {
-        return run_batch(b, d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n, dv != 0, o, o + 12 * n, o + 156 * n,
-                         b->d_int, b->d_int + n, st);
+        if (!direct)
+            return run_batch(b, d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n, dv != 0, o, o + 12 * n,
+                             o + 156 * n, b->d_int, b->d_int + n, st);
+        sdfc::launch_gather_inputs(b->d_io, d, (int)n, st);
+        sdfc::BatchInputs in{d, d + 16 * n, d + 22 * n, d + 38 * n, d + 44 * n};
+        sdfc::BatchOutputs out{nullptr, nullptr, nullptr, nullptr, nullptr, &b->d_io->out};
+        return sdfc_impl::run_batch(b, in, dv != 0, out, st);
     };
     const int key = b->precision * 2 + b->deriv_mode;
     if (b->timing) {  // the phase events need the kernels launched one by one
@@ -770,14 +787,7 @@ int sdfc_batch_evaluate(sdfc_batch* b, const double* E_A, const double* phi_A, c
         }
         CUDA_TRY(ctx, cudaGraphLaunch(b->eval_exec[dv], s));
     }
-    if (ctx->pageable_direct) {
-        CUDA_TRY(ctx, cudaMemcpyAsync(fm, o, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, s));
-        if (dv) {
-            CUDA_TRY(ctx, cudaMemcpyAsync(Km, o + 12 * n, sizeof(double) * 144 * n, cudaMemcpyDeviceToHost, s));
-            CUDA_TRY(ctx, cudaMemcpyAsync(Dm, o + 156 * n, sizeof(double) * 144 * n, cudaMemcpyDeviceToHost, s));
-        }
-        if (n_active) CUDA_TRY(ctx, cudaMemcpyAsync(n_active, b->d_int, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-        if (status) CUDA_TRY(ctx, cudaMemcpyAsync(status, b->d_int + n, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    if (direct) {
         CUDA_TRY(ctx, cudaStreamSynchronize(s));
         return SDFC_OK;
     }

@@ -61,6 +61,10 @@ struct sdfc_batch {
     double* h_in = nullptr;   // pinned
     double* h_out = nullptr;  // pinned
     int* h_int = nullptr;     // pinned
+    // the direct host-array path (the device reads pageable memory): the call's array pointers,
+    // written to the pinned copy and sent to the device copy before each graph launch
+    sdfc::HostIO* h_io = nullptr;
+    sdfc::HostIO* d_io = nullptr;
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // sdfc_batch_evaluate's device work (H2D of the staged inputs, the evaluation, D2H of the

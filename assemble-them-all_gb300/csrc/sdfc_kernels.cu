@@ -776,6 +776,7 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
     __shared__ double ad[36];  // Ad(E_A^{-1} E_B), ad[6 c + r] = entry (r, c)
     const int i = blockIdx.x, k = threadIdx.x;
     if (i >= n_inst || (mode && mode[i] != (DERIV ? 2 : 1))) return;  // uniform over the CTA
+    if (out.dev) out = *out.dev;
     const double* p = partial + (size_t)i * slots * kOutDeriv;
     if (k < NV) {
         double v = 0.0;
@@ -785,9 +786,8 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
     const bool derive = DERIV && EA != nullptr;
     if (derive && k < 36) ad[k] = adjoint_entry(EA + 16 * (size_t)i, EB + 16 * (size_t)i, k % 6, k / 6);
     __syncthreads();
-    if (k >= NV) return;
-    double v = tot[k];
-    if (derive && k >= 12) {
+    double v = k < NV ? tot[k] : 0.0;
+    if (derive && k >= 12 && k < NV) {
         const int b = k < 156 ? 12 : 156, r = (k - b) / 12, j = (k - b) % 12;
         if (j >= 6) {  // column j of Km / Dm = -(columns 0-5) Ad e_{j-6} (+ C)
             const double* m1 = tot + b + 12 * r;
@@ -797,14 +797,18 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
             if (b == 156 && j < 9) v += tot[12 + 12 * r + j];  // C column j - 6, in Km's slot (r, j)
         }
     }
-    if (k < 12)
-        out.fm[12 * (size_t)i + k] = v;
-    else if (k < 156)
-        out.Km[144 * (size_t)i + (k - 12)] = v;
-    else
-        out.Dm[144 * (size_t)i + (k - 156)] = v;
-    if (!isfinite(v)) atomicOr(out.status + i, 1);
+    if (k < NV) {
+        if (k < 12)
+            out.fm[12 * (size_t)i + k] = v;
+        else if (k < 156)
+            out.Km[144 * (size_t)i + (k - 12)] = v;
+        else
+            out.Dm[144 * (size_t)i + (k - 156)] = v;
+    }
+    // plain stores only (the outputs may be the caller's host memory)
+    const int bad = __syncthreads_or(k < NV && !isfinite(v));
     if (k == 0) {
+        if (bad) out.status[i] = 1;
         const InstanceDesc I = inst[i];
         int n = 0;
         for (int t = 0; t < I.ntiles; ++t) n += tile_count[I.tile0 + t];
@@ -812,9 +816,21 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
     }
 }
 
-__global__ void zero_status_kernel(int* status, int n) {
+__global__ void zero_status_kernel(BatchOutputs out, int n) {
+    if (out.dev) out = *out.dev;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) status[i] = 0;
+    if (i < n) out.status[i] = 0;
+}
+
+__global__ void gather_inputs_kernel(const HostIO* __restrict__ io, double* __restrict__ d, int n) {
+    const size_t nn = (size_t)n, total = 50 * nn;
+    const size_t end[5] = {16 * nn, 22 * nn, 38 * nn, 44 * nn, 50 * nn};
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+        int seg = 0;
+        while (k >= end[seg]) ++seg;
+        const size_t start = seg ? end[seg - 1] : 0;
+        d[k] = io->in[seg][k - start];
+    }
 }
 
 template <bool DERIV, bool STENCIL>
@@ -905,7 +921,7 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
                      cudaStream_t stream, const int* mode, bool zero_status, const BatchInputs* derive_q2) {
     if (n_inst <= 0) return;
-    if (zero_status) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out.status, n_inst);
+    if (zero_status) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out, n_inst);
     const double* EA = derive_q2 ? derive_q2->EA : nullptr;
     const double* EB = derive_q2 ? derive_q2->EB : nullptr;
     if (deriv)
@@ -914,6 +930,12 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
     else
         finalize_kernel<false><<<n_inst, 64, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
                                                           nullptr, nullptr, s.slots);
+}
+
+void launch_gather_inputs(const HostIO* io, double* d, int n, cudaStream_t stream) {
+    if (n <= 0) return;
+    const int blocks = (int)std::min<size_t>((50 * (size_t)n + 255) / 256, 152 * 4);
+    gather_inputs_kernel<<<blocks, 256, 0, stream>>>(io, d, n);
 }
 
 bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !stencil && precision == kMixed; }

@@ -104,7 +104,21 @@ struct BatchOutputs {
     double* Dm;      // n x 144
     int* n_active;   // n
     int* status;     // n: bit 0 = non-finite output
+    // not null: the kernels take the five pointers from this device copy instead, which the
+    // host rewrites per call (a captured graph then writes wherever the call asks, e.g. into
+    // the caller's own host arrays where the device reads pageable memory)
+    const BatchOutputs* dev = nullptr;
 };
+
+// One host-array evaluation as the device sees it: the caller's five input arrays
+// (E_A n x 16, phi_A n x 6, E_B n x 16, phi_B n x 6, params n x 6) and its outputs.
+struct HostIO {
+    const double* in[5];
+    BatchOutputs out;
+};
+
+// d (n x 50, the BatchInputs block) <- the arrays io->in point to (read by the device).
+void launch_gather_inputs(const HostIO* io, double* d, int n, cudaStream_t stream);
 
 // Scratch of a batch: device buffers sized at batch creation.
 struct BatchScratch {

@@ -430,3 +430,43 @@ def test_energy_against_oracle(sdfc, ctx, oracle, workloads, precision, bar):
         assert abs(e[k] - re) <= bar * re, (k, e[k], re)
         assert np.linalg.norm(dE[k] - rdE) <= bar * np.linalg.norm(rdE), (k, dE[k], rdE)
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_host_array_paths_agree(sdfc, workloads, precision):
+    """sdfc_batch_evaluate's two host-array paths give the same bits: kernels that read the
+    caller's arrays and write its result arrays themselves (where the device reads pageable
+    memory), and inputs / results staged through pinned buffers (SDFC_STAGED_COPIES)."""
+    import os
+    g = workloads.socket_grid(64, dtype=np.float32)
+    pts = workloads.peg_points(20000, seed=3)
+    n = 16
+    EA, phiA, EB, phiB = workloads.direction_sweep_states(n)
+    prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0)] * n
+    outs = []
+    for staged in (False, True):
+        if staged:
+            os.environ["SDFC_STAGED_COPIES"] = "1"
+        try:
+            c = sdfc.Context(0)
+        finally:
+            os.environ.pop("SDFC_STAGED_COPIES", None)
+        gh = c.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+        ph = c.upload_points(pts, 1)
+        b = c.batch([ph] * n, [gh] * n)
+        b.set_precision(sdfc.PRECISION_MIXED if precision == "mixed" else sdfc.PRECISION_FP64)
+        r = []
+        for _ in range(2):  # the second call replays the captured graph
+            r.append(b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True))
+        r.append(b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=False))
+        outs.append(r)
+        b.close()
+        c.close()
+    (d1, d2, dv), (s1, s2, sv) = outs
+    assert d1[3].sum() > 0
+    for a, b_ in ((d1, s1), (d2, s2), (d1, d2)):
+        for x, y in zip(a, b_):
+            np.testing.assert_array_equal(x, y)
+    for x, y in zip((dv[0], dv[3], dv[4]), (sv[0], sv[3], sv[4])):
+        np.testing.assert_array_equal(x, y)
+    np.testing.assert_array_equal(dv[3], d1[3])
