@@ -53,6 +53,8 @@ void free_batch(sdfc_batch* b) {
     cudaFree(b->d_prefilter);
     cudaFree(b->d_pair32);
     cudaFree(b->d_pair64);
+    cudaFree(b->d_recheck_list);
+    cudaFree(b->d_recheck_n);
     cudaFree(b->d_partial);
     cudaFree(b->d_recheck);
     cudaFree(b->d_point_offset);
@@ -76,7 +78,7 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
               cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
     sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
-                         b->slots, b->d_pair32, b->d_pair64};
+                         b->slots, b->d_pair32, b->d_pair64, b->d_recheck_list, b->d_recheck_n};
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     if (b->timing) cudaEventRecord(b->ev[0], stream);
@@ -108,7 +110,7 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
 int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, double* dE, cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
     sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
-                         b->slots, b->d_pair32, b->d_pair64};
+                         b->slots, b->d_pair32, b->d_pair64, b->d_recheck_list, b->d_recheck_n};
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
@@ -199,6 +201,8 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_prefilter, sizeof(sdfc::Prefilter) * n)) ||
         (rc = alloc((void**)&b->d_pair32, sizeof(sdfc::PairState<float>) * n)) ||
         (rc = alloc((void**)&b->d_pair64, sizeof(sdfc::PairState<double>) * n)) ||
+        (rc = alloc((void**)&b->d_recheck_list, sizeof(int) * std::max(tiles, 1))) ||
+        (rc = alloc((void**)&b->d_recheck_n, sizeof(int))) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * b->slots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||

@@ -51,11 +51,12 @@ __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pos
 __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchInputs in,
                             const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
                             Prefilter* __restrict__ pref, PairState<float>* __restrict__ pair32,
-                            PairState<double>* __restrict__ pair64) {
+                            PairState<double>* __restrict__ pair64, int* __restrict__ recheck_n) {
     // blockIdx.y: 0 the prefilter, 1 / 2 the FP32 / FP64 pair state every force or energy CTA of
     // the instance starts from (once per instance here, spread over three warps per 32 instances:
     // all three are FP64 arithmetic)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && blockIdx.y == 0) *recheck_n = 0;  // detection's list of tiles to recheck starts empty
     if (i >= n || (in.mode && in.mode[i] == 0)) return;
     const size_t o = (size_t)i;
     if (blockIdx.y == 0) {
@@ -157,7 +158,9 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                                                                 const PointsDesc* __restrict__ points,
                                                                 int* __restrict__ ids, int* __restrict__ tile_count,
                                                                 int* __restrict__ tile_queue,
-                                                                const int* __restrict__ mode) {
+                                                                const int* __restrict__ mode,
+                                                                int* __restrict__ recheck_list,
+                                                                int* __restrict__ recheck_n) {
     __shared__ Prefilter f;
     __shared__ DetectGrid<BRICKS> dg;
     __shared__ const float4* gv;
@@ -260,6 +263,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         if (lane == 31) {
             tile_count[t] = ia;
             tile_queue[t] = iq;
+            if (iq > 0) recheck_list[atomicAdd(recheck_n, 1)] = t;  // any order: tiles are independent
         }
     }
     __syncthreads();
@@ -273,18 +277,14 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
     }
 }
 
-// One warp per tile: the reference's FP64 distance for the queued points,
-// appended (ascending) after the tile's FP32-classified actives.
-__global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restrict__ inst,
-                                                     const int* __restrict__ tile_inst, BatchInputs in,
-                                                     const GridDesc* __restrict__ grids,
-                                                     const PointsDesc* __restrict__ points, int* __restrict__ ids,
-                                                     int* __restrict__ tile_count, const int* __restrict__ tile_queue,
-                                                     unsigned long long* __restrict__ recheck) {
-    __shared__ int qs[kTile];
-    const int t = blockIdx.x;
+// One tile with queued points, by one warp: the reference's FP64 distance for the
+// queued points, appended (ascending) after the tile's FP32-classified actives.
+__device__ void recheck_tile(const InstanceDesc* __restrict__ inst, const int* __restrict__ tile_inst,
+                             const BatchInputs& in, const GridDesc* __restrict__ grids,
+                             const PointsDesc* __restrict__ points, int* __restrict__ ids,
+                             int* __restrict__ tile_count, const int* __restrict__ tile_queue,
+                             unsigned long long* __restrict__ recheck, int t, int* qs) {
     const int q = tile_queue[t];
-    if (q == 0) return;
     const int lane = threadIdx.x;
     const int i = tile_inst[t];
     const InstanceDesc I = inst[i];
@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restr
     int* out = ids + (size_t)t * kTile;
     // queued stored indices sit at descending positions from the end: read them
     // back in ascending order before any write can reach those slots
+    __syncwarp();
     for (int k = lane; k < q; k += 32) qs[k] = out[kTile - 1 - k];
     __syncwarp();
     int base = tile_count[t];
@@ -313,6 +314,22 @@ __global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restr
         tile_count[t] = base;
         if (recheck) atomicAdd(recheck, (unsigned long long)q);
     }
+}
+
+// The warps walk the list of tiles with queued points (appended by detect_kernel in any
+// order: each tile's recheck touches only that tile).
+__global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restrict__ inst,
+                                                     const int* __restrict__ tile_inst, BatchInputs in,
+                                                     const GridDesc* __restrict__ grids,
+                                                     const PointsDesc* __restrict__ points, int* __restrict__ ids,
+                                                     int* __restrict__ tile_count, const int* __restrict__ tile_queue,
+                                                     unsigned long long* __restrict__ recheck,
+                                                     const int* __restrict__ recheck_list,
+                                                     const int* __restrict__ recheck_n) {
+    __shared__ int qs[kTile];
+    const int nl = *recheck_n;
+    for (int w = blockIdx.x; w < nl; w += gridDim.x)
+        recheck_tile(inst, tile_inst, in, grids, points, ids, tile_count, tile_queue, recheck, recheck_list[w], qs);
 }
 
 // ------------------------------------------------------------------ distances
@@ -862,18 +879,20 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
                    bool plain, bool bricks) {
     if (n_inst <= 0) return;
     prep_kernel<<<dim3((n_inst + 31) / 32, 3), 32, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter,
-                                                                s.pair32, s.pair64);
+                                                                s.pair32, s.pair64, s.recheck_n);
     if (total_tiles <= 0) return;
     if (plain)
         detect_kernel<false><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
                                                                          d_points, s.ids, s.tile_count, s.tile_queue,
-                                                                         in.mode);
+                                                                         in.mode, s.recheck_list, s.recheck_n);
     if (bricks)
         detect_kernel<true><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
                                                                         d_points, s.ids, s.tile_count, s.tile_queue,
-                                                                        in.mode);
-    recheck_kernel<<<total_tiles, 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points, s.ids, s.tile_count,
-                                                   s.tile_queue, s.recheck);
+                                                                        in.mode, s.recheck_list, s.recheck_n);
+    // one warp per listed tile, up to 16 warps per SM (the list is only known on the device)
+    recheck_kernel<<<std::min(total_tiles, 152 * 16), 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points,
+                                                                       s.ids, s.tile_count, s.tile_queue, s.recheck,
+                                                                       s.recheck_list, s.recheck_n);
 }
 
 void launch_distance(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,

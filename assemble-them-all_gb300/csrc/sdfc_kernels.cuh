@@ -131,6 +131,8 @@ struct BatchScratch {
     int slots;                  // force CTAs (partial rows) per instance
     PairState<float>* pair32;   // n: each instance's pair state for the FP32 kernels (written by prep_kernel)
     PairState<double>* pair64;  // n: the same for the FP64 kernels
+    int* recheck_list;          // total_tiles: the tiles with queued points (appended by detect_kernel)
+    int* recheck_n;             // 1: their count (reset by prep_kernel)
 };
 
 enum Precision { kFP64 = 0, kMixed = 1 };
