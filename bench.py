@@ -419,6 +419,14 @@ def run_gpu(args, world, rank):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": ach / hbm_peak, "traffic": traffic,
                      "peak_source": "measured" if peaks else "fallback"},
+        # the whole evaluation against the same peak, with the per-point algorithmic bytes of a
+        # contact-point evaluation (12 B point + 8 FP32 corners), plus the active contacts' force
+        # reads and the partial rows
+        "roofline_evaluation": {"bound": "hbm", "bytes_per_step": det_bytes + frc_bytes,
+                                "achieved": (det_bytes + frc_bytes) / (step_ms / 1e3) / 1e9, "peak": hbm_peak,
+                                "unit": "GB/s", "frac": (det_bytes + frc_bytes) / (step_ms / 1e3) / 1e9 / hbm_peak,
+                                "note": "points and grid are shared by all instances, so these bytes are L2 reads; "
+                                        "DRAM traffic per step is ~23 MB (profiles/)"},
         "phases_ms": {"detect": det_ms, "force": frc_ms, "reduce": red_ms},
         "plain_fp64_per_instance": {"value": plain_rate, "unit": UNIT, "instances_timed": len(plain_t),
                                     "speedup_of_batched": value / plain_rate},
