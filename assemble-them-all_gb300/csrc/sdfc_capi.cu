@@ -71,6 +71,9 @@ void free_batch(sdfc_batch* b) {
     for (cudaGraphExec_t g : b->eval_exec)
         if (g) cudaGraphExecDestroy(g);
     if (b->eval_stream) cudaStreamDestroy(b->eval_stream);
+    if (b->aux_stream) cudaStreamDestroy(b->aux_stream);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->join_ev) cudaEventDestroy(b->join_ev);
     delete b;
 }
 
@@ -85,6 +88,24 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
                         b->has_plain, b->has_bricks);
     if (b->timing) cudaEventRecord(b->ev[1], stream);
+    const sdfc::BatchInputs* q2 = sdfc::force_skips_q2(true, stencil, prec) ? &in : nullptr;
+    if (in.mode && !b->timing && b->aux_stream) {
+        // masked evaluation: the derivative and value passes touch disjoint instances (and
+        // partial rows), so the value pass runs on a forked stream beside the derivative pass
+        sdfc::launch_zero_status(out, b->n, stream);
+        CUDA_TRY(ctx, cudaEventRecord(b->fork_ev, stream));
+        CUDA_TRY(ctx, cudaStreamWaitEvent(b->aux_stream, b->fork_ev, 0));
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, false, stencil, prec, b->aux_stream,
+                           b->has_plain, b->has_bricks);
+        sdfc::launch_finalize(b->d_inst, b->n, sc, false, out, b->aux_stream, in.mode, false);
+        sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, true, stencil, prec, stream,
+                           b->has_plain, b->has_bricks);
+        sdfc::launch_finalize(b->d_inst, b->n, sc, true, out, stream, in.mode, false, q2);
+        CUDA_TRY(ctx, cudaEventRecord(b->join_ev, b->aux_stream));
+        CUDA_TRY(ctx, cudaStreamWaitEvent(stream, b->join_ev, 0));
+        CUDA_TRY(ctx, cudaGetLastError());
+        return SDFC_OK;
+    }
     if (in.mode) {
         sdfc::launch_force(b->d_inst, b->n, in, ctx->d_grids, ctx->d_points, sc, true, stencil, prec, stream,
                            b->has_plain, b->has_bricks);
@@ -95,7 +116,6 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
                            b->has_plain, b->has_bricks);
     }
     if (b->timing) cudaEventRecord(b->ev[2], stream);
-    const sdfc::BatchInputs* q2 = sdfc::force_skips_q2(true, stencil, prec) ? &in : nullptr;
     if (in.mode) {
         sdfc::launch_finalize(b->d_inst, b->n, sc, true, out, stream, in.mode, true, q2);
         sdfc::launch_finalize(b->d_inst, b->n, sc, false, out, stream, in.mode, false);
@@ -220,7 +240,10 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         free_batch(b);
         return fail(ctx, SDFC_ERR_CUDA, "batch_create: cudaMallocHost failed");
     }
-    cudaError_t e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->aux_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_inst, b->inst.data(), sizeof(InstanceDesc) * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && tiles > 0)
         e = cudaMemcpy(b->d_tile_inst, tile_inst.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)

@@ -74,6 +74,9 @@ struct sdfc_batch {
     cudaGraphExec_t eval_exec[2] = {nullptr, nullptr};
     int eval_key[2] = {-1, -1};
     cudaStream_t eval_stream = nullptr;
+    // masked evaluations: the value pass runs on this stream beside the derivative pass
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 };
 
 namespace sdfc_impl {

@@ -951,6 +951,10 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
                                                           nullptr, nullptr, s.slots);
 }
 
+void launch_zero_status(BatchOutputs out, int n_inst, cudaStream_t stream) {
+    if (n_inst > 0) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out, n_inst);
+}
+
 void launch_gather_inputs(const HostIO* io, double* d, int n, cudaStream_t stream) {
     if (n <= 0) return;
     const int blocks = (int)std::min<size_t>((50 * (size_t)n + 255) / 256, 152 * 4);

@@ -117,6 +117,9 @@ struct HostIO {
     BatchOutputs out;
 };
 
+// status[i] = 0 for every instance (launch_finalize does it itself with zero_status).
+void launch_zero_status(BatchOutputs out, int n_inst, cudaStream_t stream);
+
 // d (n x 50, the BatchInputs block) <- the arrays io->in point to (read by the device).
 void launch_gather_inputs(const HostIO* io, double* d, int n, cudaStream_t stream);
 
