@@ -542,6 +542,7 @@ struct PairState {
     ContactParams cp;
     M3 RT;  // R_B^T R_A
     V3 pT;  // R_B^T (p_A - p_B)
+    Mat3<T> Q;   // R_A^T R_B: body A's frame -> body B's, for body B's Jacobian columns
     CellMap cm;  // set by make_cell_map
 };
 
@@ -571,6 +572,7 @@ __device__ __forceinline__ void make_pair_state(const double* EA, const double* 
     S.cp.friction = S.cp.mu > kFrictionEps;
     S.RT = mul(transpose(S.B.P.R), S.A.P.R);
     S.pT = mulT(S.B.P.R, S.A.P.p - S.B.P.p);
+    S.Q = cast<T>(transpose(S.RT));
 }
 
 // The pair's CellMap on grid g (after make_pair_state).
@@ -1009,6 +1011,8 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     const T cm = mu / tn;
     const T fa = stat ? T(0) : cm * s1 / fc_norm, fb = stat ? T(0) : cm * ratio / tn;
     const T be = stat ? kt : cm * fc_norm, ga = stat ? kt : mu * ratio;
+    const T fr = fa * (dot(xr1, xr1) + dot(rho1, rho1));  // a Dm column's al per unit r
+    const Mat3<T>& Q = S.Q;
 
     // One column's factors from its derivatives (dd_j, dddot_j, dn_j, dt_j, dxi2_j of the depth,
     // its rate, the normal, the tangential velocity and the body-B contact point along column c);
@@ -1016,8 +1020,46 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
     auto emit = [&](int c, int blk, bool rot, int j, T dd_j, T dddot_j, const Vec3<T>& dn_j, const Vec3<T>& dt_j,
                     const Vec3<T>& dxi2_j) {
         const bool kcol = blk < 2;  // Km column (dq) vs Dm column (dphi)
-        // normal-force columns
         Vec3<T> N1, N2, T2 = vec3<T>(0, 0, 0);
+        if constexpr (kFusedFriction) {  // the FP32 path
+            // body A's column first (without the terms of its own frame's rotation, N1p)
+            Vec3<T> N1p;
+            T r;
+            if (kcol) {
+                r = kn * dd_j - kd * dddot_j * d - kd * ddot * dd_j;
+                N1p = -r * rho1 - sK * mulT(R1, dn_j);
+                T2 = -sK * cross(rho2, dxi2_j);
+            } else {
+                r = kd * dddot_j * d;
+                N1p = r * rho1;
+            }
+            if (friction) {
+                // both regimes in one form, N1 -= al tau1 + be R1^T dt_j (+ ga tau1 x e_j), so that the
+                // static and sliding contacts of a warp do not diverge (the sliding terms of the
+                // reference form below, with cm = mu / tn distributed over the sum).  A Dm column
+                // has N1 = r rho1, so there xr1.(xi1 x N1) + rho1.N1 = r (|xr1|^2 + |rho1|^2).
+                T al;
+                if (kcol) {
+                    const Vec3<T> N1n = (blk == 0 && rot) ? N1p - sK * cross(rho1, unit<T>(j)) : N1p;
+                    al = fa * (dot(xr1, cross(xi1, N1n)) + dot(rho1, N1n));
+                } else {
+                    al = fr * r;
+                }
+                al = al - fb * dot(t, dt_j);
+                N1p = N1p - (al * tau1 + be * mulT(R1, dt_j));
+                if (kcol) T2 = T2 - ga * cross(tau2, dxi2_j);
+            }
+            // the two bodies' world forces are opposite (R1 N1p = -R2 N2p): N2p = -Q^T N1p; then
+            // each body's frame-rotation terms, (sK rho + ga tau) x e_j on body A's rotational
+            // dq1 columns (subtracted) and body B's rotational dq2 columns (added)
+            N2 = -mulT(Q, N1p);
+            N1 = N1p;
+            if (blk == 0 && rot) N1 = N1 - cross(sK * rho1 + ga * tau1, unit<T>(j));
+            if (blk == 1 && rot) N2 = N2 + cross(sK * rho2 + ga * tau2, unit<T>(j));
+            sink.column(c, N1, N2, T2);
+            return;
+        }
+        // normal-force columns
         if (kcol) {
             T r = kn * dd_j - kd * dddot_j * d - kd * ddot * dd_j;
             N1 = -r * rho1 - sK * mulT(R1, dn_j);
@@ -1030,17 +1072,7 @@ __device__ inline void contact_force_jacobian(const GridDesc& g, V3 xi1d, const 
             N1 = r * rho1;
             N2 = -r * rho2;
         }
-        if (friction && kFusedFriction) {
-            // both regimes in one form, N1 -= al tau1 + be R1^T dt_j (+ ga tau1 x e_j), so that
-            // the static and sliding contacts of a warp do not diverge (the sliding terms of
-            // the reference form below, with cm = mu / tn distributed over the sum)
-            const T al = fa * (dot(xr1, cross(xi1, N1)) + dot(rho1, N1)) - fb * dot(t, dt_j);
-            N1 = N1 - (al * tau1 + be * mulT(R1, dt_j));
-            N2 = N2 + (al * tau2 + be * mulT(R2, dt_j));
-            if (blk == 0 && rot) N1 = N1 - ga * cross(tau1, unit<T>(j));
-            if (blk == 1 && rot) N2 = N2 + ga * cross(tau2, unit<T>(j));
-            if (kcol) T2 = T2 - ga * cross(tau2, dxi2_j);
-        } else if (friction) {
+        if (friction) {
             // dfc_norm = fc1^T dfc1 / |fc1|, with dfc1 = Gamma1^T N1 and fc1 = s1 Gamma1^T rho1
             T dfn = s1 * (dot(xr1, cross(xi1, N1)) + dot(rho1, N1)) / fc_norm;
             T dtn = dot(t, dt_j) / tn;
