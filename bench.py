@@ -426,7 +426,7 @@ def run_gpu(args, world, rank):
                                 "achieved": (det_bytes + frc_bytes) / (step_ms / 1e3) / 1e9, "peak": hbm_peak,
                                 "unit": "GB/s", "frac": (det_bytes + frc_bytes) / (step_ms / 1e3) / 1e9 / hbm_peak,
                                 "note": "points and grid are shared by all instances, so these bytes are L2 reads; "
-                                        "DRAM traffic per step is ~23 MB (profiles/)"},
+                                        "DRAM traffic per step is ~35 MB (profiles/)"},
         "phases_ms": {"detect": det_ms, "force": frc_ms, "reduce": red_ms},
         "plain_fp64_per_instance": {"value": plain_rate, "unit": UNIT, "instances_timed": len(plain_t),
                                     "speedup_of_batched": value / plain_rate},
