@@ -165,8 +165,13 @@ int sdfc_batch_set_precision(sdfc_batch* batch, int precision);
 
 /* Evaluates every instance.  Arrays are per instance, row-major, HOST memory:
  * E_A, E_B [n*16]; phi_A, phi_B [n*6]; params [n]; fm [n*12]; Km, Dm [n*144]
- * (want_deriv only); n_active [n]; status [n] (bit 0: a non-finite output).
- * Host<->device copies are part of the call. */
+ * (want_deriv only); n_active [n]; status [n] (bit 0: a non-finite output;
+ * n_active and status may be null).  Host<->device transfers are part of the
+ * call, which returns when the results are in the caller's arrays.  Where the
+ * device reads pageable host memory through the host's page tables (Grace's
+ * C2C link) the kernels read the input arrays and write the result arrays
+ * themselves; elsewhere (or with SDFC_STAGED_COPIES set in the environment when
+ * the context is created) they are staged through pinned buffers. */
 int sdfc_batch_evaluate(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
                         const double* phi_B, const sdfc_params* params, int want_deriv, double* fm, double* Km,
                         double* Dm, int* n_active, int* status);
