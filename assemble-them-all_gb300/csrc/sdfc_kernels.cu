@@ -787,7 +787,8 @@ __device__ inline double adjoint_entry(const double* EA, const double* EB, int r
 template <bool DERIV>
 __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
                                 const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode,
-                                const double* __restrict__ EA, const double* __restrict__ EB, int slots) {
+                                const double* __restrict__ EA, const double* __restrict__ EB, int slots,
+                                bool set_status) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     __shared__ double tot[NV];
     __shared__ double ad[36];  // Ad(E_A^{-1} E_B), ad[6 c + r] = entry (r, c)
@@ -825,7 +826,10 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
     // plain stores only (the outputs may be the caller's host memory)
     const int bad = __syncthreads_or(k < NV && !isfinite(v));
     if (k == 0) {
-        if (bad) out.status[i] = 1;
+        if (set_status)  // every instance passes through this launch: status written outright
+            out.status[i] = bad ? 1 : 0;
+        else if (bad)
+            out.status[i] = 1;
         const InstanceDesc I = inst[i];
         int n = 0;
         for (int t = 0; t < I.ntiles; ++t) n += tile_count[I.tile0 + t];
@@ -940,15 +944,18 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
                      cudaStream_t stream, const int* mode, bool zero_status, const BatchInputs* derive_q2) {
     if (n_inst <= 0) return;
-    if (zero_status) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out, n_inst);
+    // without a request mask every instance is finalized here, which then sets each status
+    // outright; with one, the statuses are cleared first and each pass sets its instances' flags
+    const bool set_status = zero_status && !mode;
+    if (zero_status && mode) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out, n_inst);
     const double* EA = derive_q2 ? derive_q2->EA : nullptr;
     const double* EB = derive_q2 ? derive_q2->EB : nullptr;
     if (deriv)
         finalize_kernel<true><<<n_inst, 320, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA, EB,
-                                                          s.slots);
+                                                          s.slots, set_status);
     else
         finalize_kernel<false><<<n_inst, 64, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
-                                                          nullptr, nullptr, s.slots);
+                                                          nullptr, nullptr, s.slots, set_status);
 }
 
 void launch_zero_status(BatchOutputs out, int n_inst, cudaStream_t stream) {

@@ -149,9 +149,10 @@ void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const 
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
                   cudaStream_t stream, bool plain = true, bool bricks = true);
 
-// Zeroes the status words, then finalizes.  With in.mode set, only the
-// instances whose request matches `deriv` are finalized (zero_status = false
-// lets a second, value-only pass keep the first pass's status bits).
+// Finalizes the status words too: without a mask every instance's status is
+// written outright; with one (in.mode), zero_status clears them all first, and
+// only the instances whose request matches `deriv` are finalized (zero_status =
+// false lets a second, value-only pass keep the first pass's status bits).
 // derive_q2: the inputs of the evaluation whose force pass skipped the dq2 columns
 // of Km (force_skips_q2); finalize derives them from the dq1 columns.
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,

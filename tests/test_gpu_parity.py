@@ -470,3 +470,29 @@ def test_host_array_paths_agree(sdfc, workloads, precision):
     for x, y in zip((dv[0], dv[3], dv[4]), (sv[0], sv[3], sv[4])):
         np.testing.assert_array_equal(x, y)
     np.testing.assert_array_equal(dv[3], d1[3])
+
+
+def test_host_array_optional_outputs(sdfc, ctx, workloads):
+    """sdfc_batch_evaluate with n_active and status left null (both optional in the ABI): the
+    forces are the same as with them."""
+    import ctypes
+    g = workloads.socket_grid(64, dtype=np.float32)
+    gh = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+    ph = ctx.upload_points(workloads.peg_points(8000, seed=5), 1)
+    n = 8
+    EA, phiA, EB, phiB = workloads.direction_sweep_states(n)
+    b = ctx.batch([ph] * n, [gh] * n)
+    rows = np.tile(sdfc.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0).as_row(), (n, 1))
+    fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, rows, want_deriv=True)
+    assert nact.sum() > 0 and not st.any()
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    ins = [f64(EA), f64(phiA), f64(EB), f64(phiB)]
+    prm = f64(rows)
+    fm2, Km2, Dm2 = np.zeros((n, 12)), np.zeros((n, 12, 12)), np.zeros((n, 12, 12))
+    rc = sdfc.lib().sdfc_batch_evaluate(b._h, *(dp(a) for a in ins), prm.ctypes.data_as(ctypes.POINTER(sdfc.Params)),
+                                        1, dp(fm2), dp(Km2), dp(Dm2), None, None)
+    assert rc == 0
+    for x, y in ((fm, fm2), (Km, Km2), (Dm, Dm2)):
+        np.testing.assert_array_equal(x, y)
+    b.close()
