@@ -525,14 +525,11 @@ __device__ __forceinline__ int acc_index(int k) {
     return b + 12 * (e % 12) + e / 12;
 }
 
-// CTAs of the FP32 path resident per SM (its register budget is 65536 / (this x 128));
-// the FP64 path is left its full register budget.
-#ifndef SDFC_FORCE_MIN_BLOCKS
-#define SDFC_FORCE_MIN_BLOCKS 4
-#endif
+// CTAs of the FP32 path resident per SM (kForceCtasPerSm); the FP64 path is left its full
+// register budget.
 template <typename T>
 constexpr int force_min_blocks() {
-    return std::is_same<T, float>::value ? SDFC_FORCE_MIN_BLOCKS : 1;
+    return std::is_same<T, float>::value ? kForceCtasPerSm : 1;
 }
 
 // BR = false: the FP32 fast path specialised for grids without FP16 bricks.  skip: 0 none,

@@ -44,12 +44,21 @@ namespace sdfc {
 
 constexpr int kTile = 2048;          // points per detection tile
 constexpr int kDetectThreads = 256;  // threads per detection CTA
-constexpr int kChunk = 128;          // contacts per force chunk = threads per force CTA
+// contacts per force chunk = threads per force CTA, and the FP32 force CTAs resident per SM
+// (their register budget is 65536 / (this x kChunk)): compile-time tuning knobs
+#ifndef SDFC_FORCE_CHUNK
+#define SDFC_FORCE_CHUNK 128
+#endif
+#ifndef SDFC_FORCE_MIN_BLOCKS
+#define SDFC_FORCE_MIN_BLOCKS 4
+#endif
+constexpr int kChunk = SDFC_FORCE_CHUNK;
+constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
 constexpr int kMaxSlots = 32;        // partial rows per instance (force CTAs per instance), at most
-// Slots of a batch of n instances: about six waves of force CTAs on 152 SMs at 4 CTAs each
+// Slots of a batch of n instances: about six waves of force CTAs on 152 SMs
 // (measured: 4 for 1024 instances of 50k points, 16 for 256 of 1M).
 inline int slots_for(int n) {
-    constexpr int kTargetCtas = 152 * 4 * 6;
+    constexpr int kTargetCtas = 152 * kForceCtasPerSm * 6;
     int s = 1;
     while (s < kMaxSlots && (long long)s * n < kTargetCtas) s *= 2;
     return s;
