@@ -30,7 +30,7 @@ def nvcc() -> str:
 def _flags():
     f = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
                 "-I", CSRC]
-    # force_kernel's resident CTAs per SM on the FP32 path (a tuning knob; see sdfc_kernels.cu)
+    # force_kernel's resident CTAs per SM on the FP32 path (a tuning knob; see sdfc_kernels.cuh)
     mb = os.environ.get("SDFC_FORCE_MIN_BLOCKS")
     if mb:
         f.append(f"-DSDFC_FORCE_MIN_BLOCKS={int(mb)}")
