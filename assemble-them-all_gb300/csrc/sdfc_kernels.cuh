@@ -12,26 +12,30 @@
 //                    the others (and points near the box faces) are queued in
 //                    the tile for an exact FP64 recheck.  Active stored indices
 //                    are compacted in ascending order (ballot + CTA scan).
-//   recheck_kernel   one warp per tile with queued points: the reference's FP64
-//                    distance (BodySDFObj::distance, bit-identical), appending
-//                    the active ones to the tile's list in ascending order.
+//   recheck_kernel   one warp per tile with queued points (detect_kernel lists
+//                    those tiles): the reference's FP64 distance
+//                    (BodySDFObj::distance, bit-identical), appending the active
+//                    ones to the tile's list in ascending order.
 //                    Detection as a whole restates
 //                    simulation/redmax/CollisionDetection/CollisionDetection.cpp:124-147.
 //   force_kernel     one CTA per (instance, slot).  The instance's active
 //                    contacts are cut into chunks of kChunk; slot s takes chunks
 //                    s, s+slots, ...  Each thread evaluates one contact; the
-//                    per-contact force (12 values) and, with derivatives, the 24
-//                    Jacobian columns (288 values) are summed over the warp with
-//                    shuffles and over the CTA in FP64 shared memory, in a fixed
-//                    order, into one partial row per (instance, slot).
+//                    per-contact force (12 values) and, with derivatives, the
+//                    Jacobian columns (24 on the FP64 path; 15 on the FP32 path,
+//                    which leaves body B's twist columns to finalize_kernel) are
+//                    summed over the warp with shuffles and over the CTA's warps
+//                    in shared memory, in a fixed order, into one partial row per
+//                    (instance, slot).
 //                    On the FP32 path a contact whose derivative stencil could
 //                    leave its cell takes the exact path (the reference's FP64
 //                    stencil); the warp evaluates such contacts' 19 stencil
 //                    queries together, one contact at a time across its lanes
 //                    (warp_exact_jets), so that no lane runs the long FP64
 //                    stencil alone while 31 wait.
-//   finalize_kernel  sums the slots partial rows of each instance in order and
-//                    scatters them into fm / Km / Dm.
+//   finalize_kernel  one CTA per instance: sums its slots partial rows in order,
+//                    derives the FP32 path's body-B columns (Km: -Km1 Ad; Dm:
+//                    -Dm1 Ad + C) and writes fm / Km / Dm, n_active and status.
 //
 // No atomics touch the results: the sums are deterministic run to run.
 #pragma once
