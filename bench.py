@@ -155,7 +155,9 @@ class ClockSampler:
 
     def __init__(self, device_index=0):
         self.proc = None
-        self.out = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples (the JSON line carries their summary); SDFC_CLOCKS_DIR keeps them elsewhere
+        import tempfile
+        self.out = os.path.join(os.environ.get("SDFC_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_{os.getpid()}.csv")
         try:
             os.makedirs(os.path.dirname(self.out), exist_ok=True)
             self.fh = open(self.out, "w")
