@@ -148,13 +148,25 @@ def dist_barrier(world):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region: read-only
+    NVML queries every 2 ms from a thread, or nvidia-smi every 100 ms where NVML cannot be
+    loaded."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits (nvml.h: nvmlClocksEventReason*)
+    REASON_BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                   0x40: "hw_thermal_slowdown"}
 
-    def __init__(self, device_index=0):
+    def __init__(self, device_index=0, uuid=None):
         self.proc = None
+        self.thread = None
+        self.samples, self.mask, self.mx = [], 0, 0.0
+        try:
+            self._start_nvml(device_index, uuid)
+            return
+        except Exception:
+            self.thread = None
         # raw samples (the JSON line carries their summary); SDFC_CLOCKS_DIR keeps them elsewhere
         import tempfile
         self.out = os.path.join(os.environ.get("SDFC_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_{os.getpid()}.csv")
@@ -167,7 +179,51 @@ class ClockSampler:
         except Exception:
             self.proc = None
 
+    def _start_nvml(self, device_index, uuid):
+        import ctypes
+        import threading
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit")
+        h = ctypes.c_void_p()
+        rc = 1
+        if uuid:
+            rc = lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(h))
+        if rc != 0:
+            rc = lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device_index), ctypes.byref(h))
+        if rc != 0:
+            raise OSError("nvml handle")
+        try:
+            reasons = lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            reasons = lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.mx = float(mx.value)
+        self.stop_flag = threading.Event()
+
+        def run():
+            c, r = ctypes.c_uint(), ctypes.c_ulonglong()
+            while not self.stop_flag.is_set():
+                if lib.nvmlDeviceGetClockInfo(h, ctypes.c_int(1), ctypes.byref(c)) == 0:
+                    self.samples.append(float(c.value))
+                if reasons(h, ctypes.byref(r)) == 0:
+                    self.mask |= r.value
+                time.sleep(0.002)
+
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+        time.sleep(0.01)  # the first samples precede the timed region
+
     def stop(self):
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=5)
+            if not self.samples:
+                return None
+            reasons = sorted(nm for bit, nm in self.REASON_BITS.items() if self.mask & bit)
+            return {"sm_mhz": float(np.median(self.samples)), "sm_max_mhz": self.mx, "reasons": reasons,
+                    "samples": len(self.samples), "source": "nvml"}
         if not self.proc:
             return None
         self.proc.terminate()
@@ -192,7 +248,8 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvidia-smi"}
 
 
 def load_peaks():
@@ -311,7 +368,11 @@ def run_gpu(args, world, rank):
         # timed region: K steps, each bracketed by CUDA events on the launching stream, L2 flushed between
         dist_barrier(world)
         torch.cuda.synchronize()
-        clocks = ClockSampler(dev)
+        try:
+            uuid = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+        except Exception:
+            uuid = None
+        clocks = ClockSampler(dev, uuid)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         t0 = time.perf_counter()
         for a, b in ev:
