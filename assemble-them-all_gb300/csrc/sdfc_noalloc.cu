@@ -177,7 +177,8 @@ extern "C" int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, 
                                      int n, const double* E_A, const double* phi_A, const double* E_B,
                                      const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
                                      double* Dm, int* n_active, void* stream) {
-    if (n < 0 || n > kNaMaxPoints) {
+    if (n < 0) return SDFC_ERR_INVALID_ARGUMENT;
+    if (n > kNaMaxPoints) {
         std::fprintf(stderr, "sdfc_evaluate_noalloc: %d points exceed the maximum of %d\n", n, kNaMaxPoints);
         return SDFC_ERR_CAPACITY;
     }
@@ -190,6 +191,9 @@ extern "C" int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, 
             std::floor((max_box[a] - min_box[a]) / dxyz[a]) > nn[a] - 1)
             return SDFC_ERR_INVALID_ARGUMENT;
 
+    // An error left pending by an earlier, unrelated runtime call stays with the caller: this
+    // call refuses to run rather than report that error as its own and clear it.
+    if (cudaPeekAtLastError() != cudaSuccess) return SDFC_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return SDFC_ERR_CUDA;
     // Set-up, once per device, on the current device: the host-side name of
@@ -236,5 +240,6 @@ extern "C" int sdfc_evaluate_noalloc(const double* grid_values, int ni, int nj, 
         na_finalize_kernel<true><<<1, 320, 0, s>>>(partial, rows, fm, Km, Dm, n_active);
     else
         na_finalize_kernel<false><<<1, 32, 0, s>>>(partial, rows, fm, Km, Dm, n_active);
+    // nothing was pending on entry, so an error now comes from these launches
     return cudaGetLastError() == cudaSuccess ? SDFC_OK : SDFC_ERR_CUDA;
 }

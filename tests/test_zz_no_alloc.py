@@ -58,10 +58,38 @@ def test_noalloc_matches_evaluate_on_consecutive_calls():
             if k in seen:
                 assert all(np.array_equal(a, b) for a, b in zip(got[:3], seen[k]))
             seen[k] = got[:3]
-        with pytest.raises(sdfc.SdfcError):
-            sdfc.evaluate_noalloc(g.data_ptr(), shape, fx["min_box"], fx["max_box"], fx["dx"], 0.01, p.data_ptr(),
-                                  131073, EA.data_ptr(), phiA.data_ptr(),
-                                  EB.data_ptr(), phiB.data_ptr(), prm.data_ptr(), fm.data_ptr(), Km.data_ptr(),
-                                  Dm.data_ptr(), nact.data_ptr(), want_deriv=True)
+        # value-only calls (Km, Dm not given) against the value form of sdfc_evaluate
+        for k in (4, 9):
+            EA, phiA, EB, phiB = (dev(fx[key][k]) for key in ("EA", "phiA", "EB", "phiB"))
+            prm = dev(fx["params"][k])
+            fm.fill_(np.nan)
+            sdfc.evaluate_noalloc(g.data_ptr(), shape, fx["min_box"], fx["max_box"], fx["dx"], float(fx["col_th"]),
+                                  p.data_ptr(), len(fx["points"]), EA.data_ptr(), phiA.data_ptr(), EB.data_ptr(),
+                                  phiB.data_ptr(), prm.data_ptr(), fm.data_ptr(), None, None, nact.data_ptr(),
+                                  want_deriv=False)
+            torch.cuda.synchronize()
+            ref = ctx.evaluate(pts, grid, fx["EA"][k], fx["phiA"][k], fx["EB"][k], fx["phiB"][k],
+                               sdfc.Params(*[float(x) for x in fx["params"][k]]), want_deriv=False)
+            assert int(nact.item()) == ref[3] == fx["n_active"][k]
+            assert_close(f"case {k} fm (value form)", fm.cpu().numpy(), ref[0], rel=FM_REL)
+        # an empty point set: no contact, zero force and Jacobians
+        fm.fill_(np.nan)
+        Km.fill_(np.nan)
+        Dm.fill_(np.nan)
+        nact.fill_(-1)
+        sdfc.evaluate_noalloc(g.data_ptr(), shape, fx["min_box"], fx["max_box"], fx["dx"], float(fx["col_th"]),
+                              p.data_ptr(), 0, EA.data_ptr(), phiA.data_ptr(), EB.data_ptr(), phiB.data_ptr(),
+                              prm.data_ptr(), fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(),
+                              want_deriv=True)
+        torch.cuda.synchronize()
+        assert int(nact.item()) == 0
+        assert not fm.cpu().numpy().any() and not Km.cpu().numpy().any() and not Dm.cpu().numpy().any()
+        # sizes beyond the maximum, and negative ones, are refused before any launch
+        for bad in (131073, -1):
+            with pytest.raises(sdfc.SdfcError):
+                sdfc.evaluate_noalloc(g.data_ptr(), shape, fx["min_box"], fx["max_box"], fx["dx"], 0.01,
+                                      p.data_ptr(), bad, EA.data_ptr(), phiA.data_ptr(), EB.data_ptr(),
+                                      phiB.data_ptr(), prm.data_ptr(), fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(),
+                                      nact.data_ptr(), want_deriv=True)
     finally:
         ctx.close()
