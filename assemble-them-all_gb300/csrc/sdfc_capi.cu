@@ -77,11 +77,30 @@ void free_batch(sdfc_batch* b) {
     delete b;
 }
 
+sdfc::BatchScratch scratch_of(const sdfc_batch* b) {
+    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
+                         b->slots, b->d_pair32, b->d_pair64, b->d_recheck_list, b->d_recheck_n};
+    sc.force_variant = b->force_variant;
+    sc.worker_ctas = b->worker_ctas;
+    sc.max_ntiles = b->max_ntiles;
+    return sc;
+}
+
+int ensure_partial(sdfc_batch* b, int slots) {
+    if (slots <= b->partial_slots) return SDFC_OK;
+    void* p = nullptr;
+    int rc = dev_alloc(b->ctx, &p, sizeof(double) * (size_t)b->n * slots * sdfc::kOutDeriv);
+    if (rc) return rc;
+    cudaFree(b->d_partial);
+    b->d_partial = (double*)p;
+    b->partial_slots = slots;
+    return SDFC_OK;
+}
+
 int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
               cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
-    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
-                         b->slots, b->d_pair32, b->d_pair64, b->d_recheck_list, b->d_recheck_n};
+    const sdfc::BatchScratch sc = scratch_of(b);
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     if (b->timing) cudaEventRecord(b->ev[0], stream);
@@ -129,8 +148,7 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
 
 int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, double* dE, cudaStream_t stream) {
     sdfc_context* ctx = b->ctx;
-    sdfc::BatchScratch sc{b->d_prefilter, b->d_ids, b->d_tile_count, b->d_tile_queue, b->d_partial, b->d_recheck,
-                         b->slots, b->d_pair32, b->d_pair64, b->d_recheck_list, b->d_recheck_n};
+    const sdfc::BatchScratch sc = scratch_of(b);
     const bool stencil = b->deriv_mode == SDFC_DERIV_STENCIL;
     const int prec = b->precision == SDFC_PRECISION_MIXED ? sdfc::kMixed : sdfc::kFP64;
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
@@ -186,7 +204,8 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     b->ctx = ctx;
     b->n = n;
     b->deriv_mode = ctx->deriv_mode;
-    b->slots = sdfc::slots_for(n);
+    b->slots = sdfc::slots_for(n, ctx->sm_count);
+    b->partial_slots = b->slots;
     b->precision = ctx->precision;
     b->inst.resize(n);
     std::vector<int> tile_inst;
@@ -204,6 +223,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
             return fail(ctx, SDFC_ERR_CAPACITY, "batch_create: point set larger than kTile*kMaxTilesPerInstance");
         }
         b->inst[k] = InstanceDesc{points[k], grids[k], tiles, nt};
+        b->max_ntiles = std::max(b->max_ntiles, nt);
         point_offset[k] = b->total_points;
         b->total_points += np;
         for (int t = 0; t < nt; ++t) tile_inst.push_back(k);
@@ -211,7 +231,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     }
     b->total_tiles = tiles;
     b->has_plain = b->has_bricks = false;
-    for (int k = 0; k < n; ++k) (ctx->grids[grids[k]].b16 ? b->has_bricks : b->has_plain) = true;
+    for (int k = 0; k < n; ++k) (ctx->grids[grids[k]].cells32 ? b->has_plain : b->has_bricks) = true;
     auto alloc = [&](void** p, size_t bytes) { return dev_alloc(ctx, p, bytes); };
     if ((rc = alloc((void**)&b->d_inst, sizeof(InstanceDesc) * n)) ||
         (rc = alloc((void**)&b->d_tile_inst, sizeof(int) * std::max(tiles, 1))) ||
@@ -222,7 +242,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_pair32, sizeof(sdfc::PairState<float>) * n)) ||
         (rc = alloc((void**)&b->d_pair64, sizeof(sdfc::PairState<double>) * n)) ||
         (rc = alloc((void**)&b->d_recheck_list, sizeof(int) * std::max(tiles, 1))) ||
-        (rc = alloc((void**)&b->d_recheck_n, sizeof(int))) ||
+        (rc = alloc((void**)&b->d_recheck_n, 5 * sizeof(int))) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * b->slots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||
@@ -276,6 +296,9 @@ int sdfc_create(sdfc_context** out, int device) {
     if (cudaDeviceGetAttribute(&direct, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess)
         direct = 0;
     ctx->pageable_direct = direct != 0 && std::getenv("SDFC_STAGED_COPIES") == nullptr;
+    if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        ctx->sm_count < 1)
+        ctx->sm_count = 1;
     *out = ctx;
     return SDFC_OK;
 }
@@ -332,15 +355,13 @@ int sdfc_batch_set_derivative_mode(sdfc_batch* b, int mode) {
 
 }  // extern "C"
 
-// values (FP64 grid) or, for SDFC_STORAGE_F16_BRICKS, already encoded bricks (codes_in, so_in)
-static int upload_grid_impl(sdfc_context* ctx, const double* values, const unsigned short* codes_in,
-                            const float* so_in, int ni, int nj, int nk, const double min_box[3],
-                            const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
-    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
-    if ((!values && !(codes_in && so_in)) || !min_box || !max_box || !dxyz || !grid)
-        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: null argument");
+// Shape, box and spacing checks shared by the grid uploads.
+static int check_grid(sdfc_context* ctx, int ni, int nj, int nk, const double min_box[3], const double max_box[3],
+                      const double dxyz[3], double col_th, int storage) {
+    if (!min_box || !max_box || !dxyz) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: null argument");
     if (ni < 2 || nj < 2 || nk < 2) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: each extent must be >= 2");
-    if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32 && storage != SDFC_STORAGE_F16_BRICKS)
+    if (storage != SDFC_STORAGE_F64 && storage != SDFC_STORAGE_F32 && storage != SDFC_STORAGE_F16_BRICKS &&
+        storage != SDFC_STORAGE_F32_NODES)
         return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: unknown storage");
     const int nn[3] = {ni, nj, nk};
     for (int a = 0; a < 3; ++a) {
@@ -352,53 +373,11 @@ static int upload_grid_impl(sdfc_context* ctx, const double* values, const unsig
             return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: box extends past the last grid node");
     }
     if (!std::isfinite(col_th)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite col_th");
-    const size_t n = (size_t)ni * nj * nk;
-    if (values && !all_finite(values, n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite value");
-    int rc = use_device(ctx);
-    if (rc) return rc;
+    return SDFC_OK;
+}
 
-    // the values every evaluation sees: the caller's, or the FP32-rounded / FP16-decoded ones
-    std::vector<double> seen;
-    std::vector<unsigned short> codes;
-    std::vector<float> so;
-    const int nbx = (ni + 7) / 8, nby = (nj + 7) / 8, nbz = (nk + 7) / 8;
-    if (storage == SDFC_STORAGE_F16_BRICKS) {
-        const size_t nb = (size_t)nbx * nby * nbz;
-        codes.resize(nb * 512);
-        so.resize(2 * nb);
-        seen.resize(n);
-        if (codes_in) {
-            std::copy(codes_in, codes_in + codes.size(), codes.begin());
-            std::copy(so_in, so_in + so.size(), so.begin());
-        } else {
-            sdfc_f16_brick_encode(values, ni, nj, nk, codes.data(), so.data());
-        }
-        sdfc_f16_brick_decode(codes.data(), so.data(), ni, nj, nk, seen.data());
-        if (codes_in && !all_finite(seen.data(), n))
-            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite brick value");
-    } else if (storage == SDFC_STORAGE_F32) {
-        seen.resize(n);
-        for (size_t i = 0; i < n; ++i) seen[i] = (double)(float)values[i];
-    }
-    const double* vals = seen.empty() ? values : seen.data();
-    double vmax = 0.0;
-    for (size_t i = 0; i < n; ++i) vmax = std::max(vmax, std::fabs(vals[i]));
-    // Lipschitz bound of the trilinear interpolant: per axis the largest
-    // neighbour difference over the spacing.
-    double lip2 = 0.0;
-    const size_t st[3] = {1, (size_t)ni, (size_t)ni * nj};
-    for (int a = 0; a < 3; ++a) {
-        double m = 0.0;
-        for (int k = 0; k < nk; ++k)
-            for (int j = 0; j < nj; ++j)
-                for (int i = 0; i < ni; ++i) {
-                    int c[3] = {i, j, k};
-                    if (c[a] + 1 >= nn[a]) continue;
-                    size_t idx = i + st[1] * j + st[2] * k;
-                    m = std::max(m, std::fabs(vals[idx + st[a]] - vals[idx]));
-                }
-        lip2 += (m / dxyz[a]) * (m / dxyz[a]);
-    }
+static sdfc::GridDesc grid_header(int ni, int nj, int nk, const double min_box[3], const double max_box[3],
+                                  const double dxyz[3], double col_th, int storage) {
     GridDesc g{};
     g.ni = ni;
     g.nj = nj;
@@ -416,8 +395,39 @@ static int upload_grid_impl(sdfc_context* ctx, const double* values, const unsig
         g.finv_dx[a] = (float)(1.0 / dxyz[a]);
     }
     g.col_th = col_th;
-    g.lip = (float)(std::sqrt(lip2) * 1.0001);
-    g.vmax = (float)(vmax * 1.0001);
+    return g;
+}
+
+// Adds a prepared grid to the context's table; on failure the grid's own allocations (those
+// made since `mark`) are released.
+static int register_grid(sdfc_context* ctx, const GridDesc& g, size_t mark, int rc, int* grid) {
+    if (rc == SDFC_OK) {
+        ctx->grids.push_back(g);
+        rc = sync_table(ctx, ctx->grids, &ctx->d_grids, &ctx->grid_cap);
+        if (rc == SDFC_OK) {
+            *grid = (int)ctx->grids.size() - 1;
+            return SDFC_OK;
+        }
+        ctx->grids.pop_back();
+    }
+    for (size_t q = mark; q < ctx->allocations.size(); ++q) cudaFree(ctx->allocations[q]);
+    ctx->allocations.resize(mark);
+    return rc;
+}
+
+// values (FP64 grid) or, for SDFC_STORAGE_F16_BRICKS, already encoded bricks (codes_in, so_in)
+static int upload_grid_impl(sdfc_context* ctx, const double* values, const unsigned short* codes_in,
+                            const float* so_in, int ni, int nj, int nk, const double min_box[3],
+                            const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if ((!values && !(codes_in && so_in)) || !grid) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: null argument");
+    int rc = check_grid(ctx, ni, nj, nk, min_box, max_box, dxyz, col_th, storage);
+    if (rc) return rc;
+    const size_t n = (size_t)ni * nj * nk;
+    if (values && !all_finite(values, n)) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite value");
+    if ((rc = use_device(ctx))) return rc;
+    GridDesc g = grid_header(ni, nj, nk, min_box, max_box, dxyz, col_th, storage);
+    const size_t mark = ctx->allocations.size();
     auto upload = [&](const void* src, size_t bytes, void** dst) -> int {
         int r = dev_alloc(ctx, dst, bytes);
         if (r) return r;
@@ -425,41 +435,76 @@ static int upload_grid_impl(sdfc_context* ctx, const double* values, const unsig
         CUDA_TRY(ctx, cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
         return SDFC_OK;
     };
+
     if (storage == SDFC_STORAGE_F16_BRICKS) {
+        // the values every evaluation sees are the decoded bricks; their bounds come from the host
+        const int nbx = (ni + 7) / 8, nby = (nj + 7) / 8, nbz = (nk + 7) / 8;
+        const size_t nb = (size_t)nbx * nby * nbz;
+        std::vector<unsigned short> codes(nb * 512);
+        std::vector<float> so(2 * nb);
+        std::vector<double> seen(n);
+        if (codes_in) {
+            std::copy(codes_in, codes_in + codes.size(), codes.begin());
+            std::copy(so_in, so_in + so.size(), so.begin());
+        } else {
+            sdfc_f16_brick_encode(values, ni, nj, nk, codes.data(), so.data());
+        }
+        sdfc_f16_brick_decode(codes.data(), so.data(), ni, nj, nk, seen.data());
+        if (codes_in && !all_finite(seen.data(), n))
+            return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid: non-finite brick value");
+        double vmax = 0.0;
+        for (size_t i = 0; i < n; ++i) vmax = std::max(vmax, std::fabs(seen[i]));
+        // Lipschitz bound of the trilinear interpolant: per axis the largest neighbour
+        // difference over the spacing
+        double lip2 = 0.0;
+        const size_t st[3] = {1, (size_t)ni, (size_t)ni * nj};
+        const int nn[3] = {ni, nj, nk};
+        for (int a = 0; a < 3; ++a) {
+            double m = 0.0;
+            for (int k = 0; k < nk; ++k)
+                for (int j = 0; j < nj; ++j)
+                    for (int i = 0; i < ni; ++i) {
+                        int c[3] = {i, j, k};
+                        if (c[a] + 1 >= nn[a]) continue;
+                        size_t idx = i + st[1] * j + st[2] * k;
+                        m = std::max(m, std::fabs(seen[idx + st[a]] - seen[idx]));
+                    }
+            lip2 += (m / dxyz[a]) * (m / dxyz[a]);
+        }
+        g.lip = (float)(std::sqrt(lip2) * 1.0001);
+        g.vmax = (float)(vmax * 1.0001);
         void *pb = nullptr, *ps = nullptr;
         if ((rc = upload(codes.data(), codes.size() * sizeof(unsigned short), &pb)) ||
             (rc = upload(so.data(), so.size() * sizeof(float), &ps)))
-            return rc;
+            return register_grid(ctx, g, mark, rc, grid);
         g.b16 = (const unsigned short*)pb;
         g.bso = (const float2*)ps;
         g.nbx = nbx;
         g.nby = nby;
-    } else {
-        // cell-corner array: per cell its 8 FP32 corners (GridDesc::cells32)
-        const size_t ci = (size_t)ni - 1, cj = (size_t)nj - 1, ck = (size_t)nk - 1;
-        std::vector<float> cells(8 * ci * cj * ck);
-        for (size_t k = 0; k < ck; ++k)
-            for (size_t j = 0; j < cj; ++j)
-                for (size_t i = 0; i < ci; ++i) {
-                    float* c = &cells[8 * (i + ci * (j + cj * k))];
-                    const size_t b = i + (size_t)ni * (j + (size_t)nj * k), sj = (size_t)ni, sk = (size_t)ni * nj;
-                    const size_t at[8] = {b, b + 1, b + sj, b + sj + 1, b + sk, b + sk + 1, b + sk + sj, b + sk + sj + 1};
-                    for (int q = 0; q < 8; ++q) c[q] = (float)vals[at[q]];
-                }
-        void *pc = nullptr, *p64 = nullptr;
-        if ((rc = upload(cells.data(), cells.size() * sizeof(float), &pc)) ||
-            (rc = upload(vals, n * sizeof(double), &p64)))
-            return rc;
-        g.cells32 = (const float4*)pc;
+        return register_grid(ctx, g, mark, SDFC_OK, grid);
+    }
+    if (storage == SDFC_STORAGE_F32_NODES) {
+        std::vector<float> v(n);
+        for (size_t i = 0; i < n; ++i) v[i] = (float)values[i];
+        void* p = nullptr;
+        if (!(rc = upload(v.data(), n * sizeof(float), &p))) {
+            g.v32 = (const float*)p;
+            rc = sdfc_impl::grid_finish_device(ctx, g, p, true, false);
+        }
+        return register_grid(ctx, g, mark, rc, grid);
+    }
+    // storages 0 and 1: the FP64 values (storage 1: rounded to FP32 first) and the cell-corner array
+    std::vector<double> rounded;
+    if (storage == SDFC_STORAGE_F32) {
+        rounded.resize(n);
+        for (size_t i = 0; i < n; ++i) rounded[i] = (double)(float)values[i];
+    }
+    void* p64 = nullptr;
+    if (!(rc = upload(rounded.empty() ? values : rounded.data(), n * sizeof(double), &p64))) {
         g.v64 = (const double*)p64;
+        rc = sdfc_impl::grid_finish_device(ctx, g, p64, false, true);
     }
-    ctx->grids.push_back(g);
-    if ((rc = sync_table(ctx, ctx->grids, &ctx->d_grids, &ctx->grid_cap))) {
-        ctx->grids.pop_back();
-        return rc;
-    }
-    *grid = (int)ctx->grids.size() - 1;
-    return SDFC_OK;
+    return register_grid(ctx, g, mark, rc, grid);
 }
 
 extern "C" {
@@ -467,6 +512,42 @@ extern "C" {
 int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
                      const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid) {
     return upload_grid_impl(ctx, values, nullptr, nullptr, ni, nj, nk, min_box, max_box, dxyz, col_th, storage, grid);
+}
+
+int sdfc_upload_grid_device(sdfc_context* ctx, const float* d_values, int ni, int nj, int nk,
+                            const double min_box[3], const double max_box[3], const double dxyz[3], double col_th,
+                            int storage, int* grid) {
+    if (!ctx) return SDFC_ERR_INVALID_ARGUMENT;
+    if (!d_values || !grid) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid_device: null argument");
+    if (storage != SDFC_STORAGE_F32 && storage != SDFC_STORAGE_F32_NODES)
+        return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "upload_grid_device: storage must be F32 or F32_NODES");
+    int rc = check_grid(ctx, ni, nj, nk, min_box, max_box, dxyz, col_th, storage);
+    if (rc) return rc;
+    if ((rc = use_device(ctx))) return rc;
+    const size_t n = (size_t)ni * nj * nk;
+    GridDesc g = grid_header(ni, nj, nk, min_box, max_box, dxyz, col_th, storage);
+    const size_t mark = ctx->allocations.size();
+    void* p = nullptr;
+    if (storage == SDFC_STORAGE_F32_NODES) {
+        if (!(rc = dev_alloc(ctx, &p, n * sizeof(float)))) {
+            ctx->allocations.push_back(p);
+            cudaError_t e = cudaMemcpyAsync(p, d_values, n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream);
+            if (e != cudaSuccess) {
+                rc = fail(ctx, SDFC_ERR_CUDA, std::string("upload_grid_device: ") + cudaGetErrorString(e));
+            } else {
+                g.v32 = (const float*)p;
+                rc = sdfc_impl::grid_finish_device(ctx, g, p, true, false);
+            }
+        }
+        return register_grid(ctx, g, mark, rc, grid);
+    }
+    if (!(rc = dev_alloc(ctx, &p, n * sizeof(double)))) {
+        ctx->allocations.push_back(p);
+        g.v64 = (const double*)p;
+        if (!(rc = sdfc_impl::widen_device(ctx, d_values, (double*)p, n)))
+            rc = sdfc_impl::grid_finish_device(ctx, g, d_values, true, true);
+    }
+    return register_grid(ctx, g, mark, rc, grid);
 }
 
 int sdfc_upload_grid_bricks(sdfc_context* ctx, const unsigned short* codes, const float* so, int ni, int nj, int nk,
@@ -486,6 +567,12 @@ int sdfc_grid_values(sdfc_context* ctx, int grid, double* values) {
     if (rc) return rc;
     const GridDesc& g = ctx->grids[grid];
     const size_t n = (size_t)g.ni * g.nj * g.nk;
+    if (g.v32) {
+        std::vector<float> v(n);
+        CUDA_TRY(ctx, cudaMemcpy(v.data(), g.v32, n * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; ++i) values[i] = (double)v[i];
+        return SDFC_OK;
+    }
     if (!g.b16) {
         CUDA_TRY(ctx, cudaMemcpy(values, g.v64, n * sizeof(double), cudaMemcpyDeviceToHost));
         return SDFC_OK;
@@ -588,8 +675,46 @@ static std::vector<int> morton_order(const double* xyz, int n) {
         }
         code[i] = spread(q[0]) | (spread(q[1]) << 1) | (spread(q[2]) << 2);
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+    // stable sort by the 30-bit code: three counting-sort passes of 10 bits each (least
+    // significant first), each stable, so equal codes keep the input order
+    std::vector<int> tmp(n);
+    std::vector<int> count(1025);
+    for (int pass = 0; pass < 3; ++pass) {
+        const int shift = 10 * pass;
+        std::fill(count.begin(), count.end(), 0);
+        for (int k = 0; k < n; ++k) ++count[((code[order[k]] >> shift) & 1023u) + 1];
+        for (int b = 0; b < 1024; ++b) count[b + 1] += count[b];
+        for (int k = 0; k < n; ++k) tmp[count[(code[order[k]] >> shift) & 1023u]++] = order[k];
+        order.swap(tmp);
+    }
     return order;
+}
+
+// Bounding sphere (x, y, z, r) of every detection tile of a stored point set (FP32 SoA),
+// r rounded up so that every FP32 point of the tile lies within it.
+static std::vector<float4> tile_spheres(const std::vector<float>& s32, int n) {
+    const int nt = (n + sdfc::kTile - 1) / sdfc::kTile;
+    std::vector<float4> out(std::max(nt, 1), make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int t = 0; t < nt; ++t) {
+        const int a = t * sdfc::kTile, b = std::min(n, a + sdfc::kTile);
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = a; k < b; ++k)
+            for (int c = 0; c < 3; ++c) {
+                const double v = s32[(size_t)c * n + k];
+                lo[c] = std::min(lo[c], v);
+                hi[c] = std::max(hi[c], v);
+            }
+        const float cx = (float)(0.5 * (lo[0] + hi[0])), cy = (float)(0.5 * (lo[1] + hi[1])),
+                    cz = (float)(0.5 * (lo[2] + hi[2]));
+        double r2 = 0.0;
+        for (int k = a; k < b; ++k) {
+            const double dx = s32[k] - (double)cx, dy = s32[(size_t)n + k] - (double)cy,
+                         dz = s32[2 * (size_t)n + k] - (double)cz;
+            r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+        }
+        out[t] = make_float4(cx, cy, cz, (float)(std::sqrt(r2) * (1.0 + 1e-6)) + 1e-30f);
+    }
+    return out;
 }
 
 int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage, int* points) {
@@ -621,6 +746,14 @@ int sdfc_upload_points(sdfc_context* ctx, const double* xyz, int n, int storage,
     ctx->allocations.push_back(p32);
     CUDA_TRY(ctx, cudaMemcpy(p32, s32.data(), s32.size() * sizeof(float), cudaMemcpyHostToDevice));
     P.x32 = (const float*)p32;
+    {
+        const std::vector<float4> sph = tile_spheres(s32, n);
+        void* psph = nullptr;
+        if ((rc = dev_alloc(ctx, &psph, sph.size() * sizeof(float4)))) return rc;
+        ctx->allocations.push_back(psph);
+        CUDA_TRY(ctx, cudaMemcpy(psph, sph.data(), sph.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        P.tiles = (const float4*)psph;
+    }
     void* pord = nullptr;
     if ((rc = dev_alloc(ctx, &pord, (size_t)n * sizeof(int)))) return rc;
     ctx->allocations.push_back(pord);

@@ -131,11 +131,14 @@ __device__ __forceinline__ Mat3<T> transpose(const Mat3<T>& A) {
 // indexed [i + ni*(j + nj*k)] (simulation/externals/sdfgen/array3.h:70-79).
 struct GridDesc {
     int ni, nj, nk;
-    int storage;  // 0 = FP64 values, 1 = FP32 values, 2 = FP16 bricks
+    int storage;  // 0 = FP64 values, 1 = FP32 values, 2 = FP16 bricks, 3 = FP32 node values only
     double min_box[3], max_box[3], dx[3], inv_dx[3];
     double org[3];  // min_box / dx (cell coordinate of the origin), for the fast depth path
     double col_th;
     const double* v64;   // FP64 values (storage 1: the FP32 values widened), read for active contacts
+    // storage 3: the FP32 node values alone (4 B per node, no FP64 copy, no cell-corner array);
+    // every read widens them, so the exact paths see the same doubles as storage 1
+    const float* v32;
     // storage 2: FP16 codes in 8^3-node bricks (brick b = bx + nbx (by + nby bz), node
     // (i&7) + 8 (j&7) + 64 (k&7) within it) and per brick (scale, offset); value =
     // fma(scale, code, offset), in FP64 for the exact paths and FP32 for the others
@@ -161,6 +164,9 @@ struct PointsDesc {
     const double* x64; // FP64 SoA (storage 1: the FP32 points widened)
     const int* orig;   // stored index -> caller's index
     float radius;      // max |xi|
+    // per detection tile (kTile consecutive stored points): a sphere (x, y, z, r) in the body frame
+    // holding the tile's FP32 points, so that detection can pass over tiles far from a grid box
+    const float4* tiles;
 };
 
 struct Pose {
@@ -213,7 +219,19 @@ static __device__ __noinline__ double brick_value64_cold(const GridDesc& g, int 
 
 __device__ __forceinline__ double grid_value(const GridDesc& g, int i, int j, int k) {
     if (g.b16) return brick_value64_cold(g, i, j, k);
-    return __ldg(g.v64 + (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k));
+    const size_t idx = (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k);
+    if (g.v32) return (double)__ldg(g.v32 + idx);
+    return __ldg(g.v64 + idx);
+}
+
+// The 8 corners of cell (i, j, k) from FP32 node values (storage 3), in cell-corner order.
+__device__ __forceinline__ void node_corners32(const GridDesc& g, int i, int j, int k, float* c) {
+    const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
+    const float* b = g.v32 + (size_t)i + sj * (size_t)j + sk * (size_t)k;
+    c[0] = __ldg(b);           c[1] = __ldg(b + 1);
+    c[2] = __ldg(b + sj);      c[3] = __ldg(b + sj + 1);
+    c[4] = __ldg(b + sk);      c[5] = __ldg(b + sk + 1);
+    c[6] = __ldg(b + sk + sj); c[7] = __ldg(b + sk + sj + 1);
 }
 
 // The 8 corner values of cell (i, j, k), ordered c000, c100, c010, c110, c001, c101,
@@ -223,6 +241,10 @@ __device__ __forceinline__ void cell_corners32(const GridDesc& g, int i, int j, 
         const Corners32 r = brick_corners32(g, i, j, k);
 #pragma unroll
         for (int q = 0; q < 8; ++q) c[q] = r.c[q];
+        return;
+    }
+    if (g.v32) {
+        node_corners32(g, i, j, k, c);
         return;
     }
     const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
@@ -250,6 +272,13 @@ __device__ __forceinline__ void cell_corners64(const GridDesc& g, int i, int j, 
     if (g.b16) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) c[q] = brick_value64_cold(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+        return;
+    }
+    if (g.v32) {
+        float f[8];
+        node_corners32(g, i, j, k, f);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) c[q] = (double)f[q];
         return;
     }
     const size_t sj = (size_t)g.ni, sk = (size_t)g.ni * (size_t)g.nj;
@@ -721,10 +750,20 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             const int i = fc->i, j = fc->j, k = fc->k;
             const double ud = fc->ud, vd = fc->vd, wd = fc->wd;
             double e[8];
-            if constexpr (BR)
-                cell_corners64(g, i, j, k, e);
-            else
+            float cc[8];
+            bool have32 = false;
+            if constexpr (BR) {
+                if (g.v32) {  // FP32 node values: one set of loads serves both the depth and the derivatives
+                    node_corners32(g, i, j, k, cc);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) e[q] = (double)cc[q];
+                    have32 = true;
+                } else {
+                    cell_corners64(g, i, j, k, e);
+                }
+            } else {
                 plain_corners64(g, i, j, k, e);
+            }
             const double e000 = e[0], e100 = e[1], e010 = e[2], e110 = e[3];
             const double e001 = e[4], e101 = e[5], e011 = e[6], e111 = e[7];
             const double q0 = fma(ud, e100 - e000, e000), q1 = fma(ud, e110 - e010, e010);
@@ -735,11 +774,11 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             d = J.v + g.col_th;
             // FP32 analytic derivatives of the cell's interpolant
             const float u = (float)ud, v = (float)vd, w = (float)wd;
-            float cc[8];
-            if constexpr (BR)
-                cell_corners32(g, i, j, k, cc);
-            else
+            if constexpr (BR) {
+                if (!have32) cell_corners32(g, i, j, k, cc);
+            } else {
                 plain_corners32(g, i, j, k, cc);
+            }
             const float c000 = cc[0], c100 = cc[1], c010 = cc[2], c110 = cc[3];
             const float c001 = cc[4], c101 = cc[5], c011 = cc[6], c111 = cc[7];
             const float a00 = c100 - c000, a10 = c110 - c010, a01 = c101 - c001, a11 = c111 - c011;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "sdfc.h"
@@ -11,6 +12,7 @@
 
 struct sdfc_context {
     int device = 0;
+    int sm_count = 1;  // the device's multiprocessors (cudaDevAttrMultiProcessorCount): launch shapes follow it
     cudaStream_t stream = nullptr;
     // host-array calls copy straight between the caller's pageable arrays and the device (the
     // device reads pageable memory through the host page tables, as over Grace's C2C link);
@@ -31,6 +33,8 @@ struct sdfc_context {
     int single_points = -1, single_grid = -1;
     std::vector<sdfc_batch*> batches;  // live batches, destroyed with the context
     std::vector<sdfc_sim*> sims;       // live simulations, destroyed with the context
+    // tunings found by sdfc_batch_autotune, by batch shape (sdfc_impl::tune_key)
+    std::vector<std::pair<std::vector<long long>, sdfc_tuning>> tunings;
 };
 
 struct sdfc_batch {
@@ -38,6 +42,11 @@ struct sdfc_batch {
     int n = 0;
     int total_tiles = 0;
     int slots = 8;  // force CTAs (partial rows) per instance
+    int partial_slots = 0;  // slots the partial-row buffer holds
+    int force_variant = sdfc::kForceCtas;
+    int worker_ctas = 0;  // one-warp force workers (0: the device's multiprocessors x resident workers)
+    int max_ntiles = 0;   // most detection tiles of one instance
+    float tuned_ms = 0.f;  // measured evaluation time of the configuration in use (0: not measured)
     int deriv_mode = SDFC_DERIV_ANALYTIC;
     int precision = SDFC_PRECISION_FP64;
     std::vector<sdfc::InstanceDesc> inst;
@@ -54,7 +63,8 @@ struct sdfc_batch {
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
     long long* d_point_offset = nullptr;  // n: first output row of each instance's per-point distances
-    bool has_plain = true, has_bricks = false;  // instances on FP64/FP32 grids, on FP16-brick grids
+    // instances on grids with the FP32 cell-corner array (storages 0, 1), on grids without it
+    bool has_plain = true, has_bricks = false;
     long long total_points = 0;
     // staging of the host-array entry points
     double* d_in = nullptr;   // n x 50: EA | phiA | EB | phiB | prm
@@ -93,6 +103,22 @@ void free_sim(sdfc_sim* s);
 int run_energy(sdfc_batch* b, const sdfc::BatchInputs& in, double* energy, double* dE, cudaStream_t stream);
 int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
               cudaStream_t stream);
+// The kernels' view of a batch's scratch and launch configuration.
+sdfc::BatchScratch scratch_of(const sdfc_batch* b);
+// Makes the batch's partial-row buffer hold `slots` rows per instance (reallocating it; not
+// during a stream capture).
+int ensure_partial(sdfc_batch* b, int slots);
+// Times the candidate launch configurations of the force pass on these inputs (each a whole
+// evaluation, CUDA events on `stream`), applies the fastest and remembers it in the context for
+// batches of the same shape; `chosen` (may be null) receives it.
+int autotune(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc::BatchOutputs& out,
+             cudaStream_t stream, sdfc_tuning* chosen);
+// Device-side grid preparation (sdfc_grid.cu) from the node values at d_values (FP32 or FP64,
+// ni*nj*nk, i fastest, on the device): g.lip and g.vmax, and with `cells` the FP32 cell-corner
+// array (owned by the context).  Fails with SDFC_ERR_INVALID_ARGUMENT on a non-finite value.
+int grid_finish_device(sdfc_context* ctx, sdfc::GridDesc& g, const void* d_values, bool fp32, bool cells);
+// b[0..n) = (double) a[0..n), both on the device, on the context's stream.
+int widen_device(sdfc_context* ctx, const float* a, double* b, size_t n);
 
 }  // namespace sdfc_impl
 

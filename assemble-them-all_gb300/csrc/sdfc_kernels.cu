@@ -56,7 +56,9 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
     // the instance starts from (once per instance here, spread over three warps per 32 instances:
     // all three are FP64 arithmetic)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0 && blockIdx.y == 0) *recheck_n = 0;  // detection's list of tiles to recheck starts empty
+    if (i == 0 && blockIdx.y == 0)  // detection's list of tiles to recheck starts empty, and so do the
+        for (int q = 0; q < 5; ++q) recheck_n[q] = 0;  // force workers' queues
+
     if (i >= n || (in.mode && in.mode[i] == 0)) return;
     const size_t o = (size_t)i;
     if (blockIdx.y == 0) {
@@ -132,10 +134,11 @@ __device__ __forceinline__ double exact_distance(const GridDesc& g, const Pose& 
 #define SDFC_DETECT_UNROLL 8
 #endif
 constexpr int kDetectUnroll = SDFC_DETECT_UNROLL;
-// One instantiation per grid storage: BRICKS = false reads the FP32 cell-corner array,
-// BRICKS = true the FP16 bricks (with the grid descriptor in shared memory).  A batch launches
-// the ones its grids need; each leaves the other kind's tiles alone, so the plain kernel keeps
-// the registers and shared memory of a brick-free build.
+// One instantiation per kind of grid storage: BRICKS = false reads the FP32 cell-corner array
+// (storages 0 and 1), BRICKS = true every grid without one, the FP16 bricks and the FP32 node
+// values (with the grid descriptor in shared memory).  A batch launches the ones its grids need;
+// each leaves the other kind's tiles alone, so the cell-corner kernel keeps the registers and
+// shared memory of a build without the other storages.
 template <bool BRICKS>
 struct DetectGrid;
 template <>
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         return;
     }
     const InstanceDesc I = inst[i];
-    if ((grids[I.grid].b16 != nullptr) != BRICKS) return;  // the other storage's kernel handles this tile
+    if ((grids[I.grid].cells32 == nullptr) != BRICKS) return;  // the other storage's kernel handles this tile
     if (tid < (int)(sizeof(Prefilter) / sizeof(float)))
         reinterpret_cast<float*>(&f)[tid] = reinterpret_cast<const float*>(pref + i)[tid];
     if (tid == 0) {
@@ -192,6 +195,29 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         pn = points[I.points].n;
     }
     __syncthreads();
+    {
+        // Broad phase: the tile's points lie in a sphere (body frame); where its image in the
+        // grid frame, grown by a margin well above the FP32 transform's error (a few ulps of
+        // |xi| + |p|), lies wholly outside the box test below on some axis, every point of the
+        // tile fails that test, so the tile is empty without reading its points.
+        const PointsDesc& P = points[I.points];
+        const float4 sp = __ldg(P.tiles + (t - I.tile0));
+        const float cx = fmaf(f.R[0], sp.x, fmaf(f.R[1], sp.y, fmaf(f.R[2], sp.z, f.p[0])));
+        const float cy = fmaf(f.R[3], sp.x, fmaf(f.R[4], sp.y, fmaf(f.R[5], sp.z, f.p[1])));
+        const float cz = fmaf(f.R[6], sp.x, fmaf(f.R[7], sp.y, fmaf(f.R[8], sp.z, f.p[2])));
+        const float r = sp.w * 1.00001f +
+                        1e-5f * (P.radius + fabsf(f.p[0]) + fabsf(f.p[1]) + fabsf(f.p[2]) + fabsf(cx) + fabsf(cy) +
+                                 fabsf(cz));
+        const bool away = cx + r < f.lo_out[0] || cx - r > f.hi_out[0] || cy + r < f.lo_out[1] ||
+                          cy - r > f.hi_out[1] || cz + r < f.lo_out[2] || cz - r > f.hi_out[2];
+        if (away) {  // uniform over the CTA
+            if (tid == 0) {
+                tile_count[t] = 0;
+                tile_queue[t] = 0;
+            }
+            return;
+        }
+    }
     const int n = pn;
     const int first = (t - I.tile0) * kTile;
     const int count = min(kTile, n - first);
@@ -532,9 +558,10 @@ constexpr int force_min_blocks() {
     return std::is_same<T, float>::value ? kForceCtasPerSm : 1;
 }
 
-// BR = false: the FP32 fast path specialised for grids without FP16 bricks.  skip: 0 none,
-// 1 instances on brick grids, 2 instances on other grids (when a batch has both kinds, the two
-// instantiations split its instances).
+// BR = false: the FP32 fast path specialised for grids with the FP32 cell-corner array
+// (storages 0 and 1); BR = true serves every storage.  skip: 0 none, 1 instances on grids
+// without the cell-corner array, 2 instances on grids with it (when a batch has both kinds,
+// the two instantiations split its instances).
 template <bool DERIV, bool STENCIL, typename T, bool BR = true>
 __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(const InstanceDesc* __restrict__ inst, BatchInputs in,
                                                        const GridDesc* __restrict__ grids,
@@ -557,7 +584,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
     if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const InstanceDesc I = inst[i];
-    if (skip && (grids[I.grid].b16 != nullptr) == (skip == 1)) return;  // the other instantiation's instance
+    if (skip && (grids[I.grid].cells32 == nullptr) == (skip == 1)) return;  // the other instantiation's instance
     if (warp == 0) {
         // inclusive prefix of the instance's tile counts, 32 tiles at a time
         int run = 0;
@@ -637,6 +664,106 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
             for (int w = 0; w < NW; ++w) v += acc[w * NV + a].value();
         }
         row[k] = v;
+    }
+}
+
+// Resident one-warp force workers per SM: the FP32 path within 128 registers, the FP64 path
+// within 255.
+template <typename T>
+constexpr int worker_min_blocks() {
+    return std::is_same<T, float>::value ? 16 : 8;
+}
+
+// Force pass by persistent one-warp workers (kForceWorkers).  Item q of the queue is (instance
+// q / slots, slot q % slots); the slot takes the instance's 32-contact chunks s, s + slots, ...
+// in order and writes its own partial row, so the sums do not depend on which worker took the
+// item.  queue: the pass's counter, zeroed by prep_kernel.  Dynamic shared memory: the prefix of
+// the instance's tile counts, max_ntiles + 1 ints.
+template <bool DERIV, bool STENCIL, typename T, bool BR = true>
+__global__ void __launch_bounds__(32, worker_min_blocks<T>()) force_worker_kernel(
+    const InstanceDesc* __restrict__ inst, int n_inst, BatchInputs in, const GridDesc* __restrict__ grids,
+    const PointsDesc* __restrict__ points, const int* __restrict__ ids, const int* __restrict__ tile_count,
+    const PairState<T>* __restrict__ pairs, double* __restrict__ partial, int skip, int slots, int* __restrict__ queue) {
+    constexpr int NV = DERIV ? kOutDeriv : kOutValue;
+    constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
+    __shared__ Accum<T> acc[NV];
+    __shared__ GridDesc g;
+    __shared__ PointsDesc P;
+    __shared__ PairState<T> S;
+    extern __shared__ int prefix[];
+    const int lane = threadIdx.x;
+    const int n_items = n_inst * slots;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(queue, 1);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= n_items) break;
+        const int i = item / slots, s = item - (item / slots) * slots;
+        if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) continue;  // not requested in this pass
+        const InstanceDesc I = inst[i];
+        if (skip && (grids[I.grid].cells32 == nullptr) == (skip == 1)) continue;  // the other instantiation's
+        __syncwarp();  // the previous item's reads of the shared state are done
+        {
+            int run = 0;
+            if (lane == 0) prefix[0] = 0;
+            for (int k0 = 0; k0 < I.ntiles; k0 += 32) {
+                const int k = k0 + lane;
+                int v = k < I.ntiles ? tile_count[I.tile0 + k] : 0;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(kFull, v, o);
+                    if (lane >= o) v += u;
+                }
+                if (k < I.ntiles) prefix[k + 1] = run + v;
+                run += __shfl_sync(kFull, v, 31);
+            }
+        }
+        warp_copy(g, grids[I.grid], lane);
+        warp_copy(P, points[I.points], lane);
+        warp_copy(S, pairs[i], lane);
+        for (int k = lane; k < NV; k += 32) acc[k].zero();
+        __syncwarp();
+        const int total = prefix[I.ntiles];
+        const int nchunks = (total + 31) >> 5;
+        for (int chunk = s; chunk < nchunks; chunk += slots) {
+            const int c = chunk * 32 + lane;
+            const bool valid = c < total;
+            V3 xi = v3(0, 0, 0);
+            Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
+            if (valid) {
+                int lo = 0, hi = I.ntiles;  // largest k with prefix[k] <= c
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (prefix[mid] <= c)
+                        lo = mid;
+                    else
+                        hi = mid;
+                }
+                const int sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
+                xi = load_point(P, sid);
+                if constexpr (kWarpExact) xf = load_point32(P, sid);
+            }
+            FastCell fc;
+            const FastCell* fcp = nullptr;
+            ExactJet<T> ej;
+            const ExactJet<T>* ejp = nullptr;
+            if constexpr (kWarpExact) {
+                fc = fast_cell<T>(g, S.cm, xi, xf);
+                fcp = &fc;
+                warp_exact_jets<T>(g, S, xi, valid && !fc.ok, DERIV, ej);
+                ejp = &ej;
+            }
+            WarpSink<NV, T> sink{acc, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
+            if constexpr (DERIV) {
+                contact_force_jacobian<T, WarpSink<NV, T>, BR>(g, xi, S, fcp, sink, valid, STENCIL, ejp, kWarpExact);
+            } else {
+                ContactForce<T> F = contact_force<T, BR>(g, xi, S, fcp, valid, STENCIL, ejp);
+                sink.force(F.xi1, F.f1, F.xi2, F.f2);
+            }
+        }
+        __syncwarp();
+        double* row = partial + ((size_t)i * slots + s) * kOutDeriv;
+        for (int k = lane; k < NV; k += 32) row[k] = acc[acc_index(k)].value();
     }
 }
 
@@ -851,10 +978,40 @@ __global__ void gather_inputs_kernel(const HostIO* __restrict__ io, double* __re
     }
 }
 
+// force_worker_kernel<DERIV, STENCIL, T, BR> on s.worker_ctas one-warp CTAs.  Each launch of an
+// evaluation has its own queue: recheck_n[1 + 2 (value pass) + (general-storage kernel)].
+template <bool DERIV, bool STENCIL, typename T, bool BR>
+void launch_workers(int n_inst, cudaStream_t stream, const InstanceDesc* d_inst, BatchInputs in,
+                    const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s,
+                    const PairState<T>* pairs, int skip) {
+    int* queue = s.recheck_n + 1 + (DERIV ? 0 : 2) + (BR ? 1 : 0);
+    const size_t smem = sizeof(int) * ((size_t)s.max_ntiles + 1);
+    const int ctas = s.worker_ctas > 0 ? s.worker_ctas : device_sm_count() * worker_min_blocks<T>();
+    force_worker_kernel<DERIV, STENCIL, T, BR><<<ctas, 32, smem, stream>>>(
+        d_inst, n_inst, in, d_grids, d_points, s.ids, s.tile_count, pairs, s.partial, skip, s.slots, queue);
+}
+
 template <bool DERIV, bool STENCIL>
 void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, const InstanceDesc* d_inst,
                     BatchInputs in, const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s,
                     bool plain, bool bricks) {
+    if (s.force_variant == kForceWorkers) {
+        if (precision == kMixed && !STENCIL) {
+            if (plain)
+                launch_workers<DERIV, STENCIL, float, false>(n_inst, stream, d_inst, in, d_grids, d_points, s,
+                                                             s.pair32, bricks ? 1 : 0);
+            if (bricks)
+                launch_workers<DERIV, STENCIL, float, true>(n_inst, stream, d_inst, in, d_grids, d_points, s,
+                                                            s.pair32, plain ? 2 : 0);
+        } else if (precision == kMixed) {
+            launch_workers<DERIV, STENCIL, float, true>(n_inst, stream, d_inst, in, d_grids, d_points, s, s.pair32,
+                                                        0);
+        } else {
+            launch_workers<DERIV, STENCIL, double, true>(n_inst, stream, d_inst, in, d_grids, d_points, s, s.pair64,
+                                                         0);
+        }
+        return;
+    }
     if (precision == kMixed && !STENCIL) {  // the FP32 fast path: specialised for brick-free grids
         if (plain)
             force_kernel<DERIV, STENCIL, float, false><<<grid, kChunk, 0, stream>>>(
@@ -875,6 +1032,17 @@ void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, c
 
 }  // namespace
 
+int device_sm_count() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64 && cache[dev] > 0) return cache[dev];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    if (dev < 64) cache[dev] = n;
+    return n;
+}
+
 void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
                    const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream,
                    bool plain, bool bricks) {
@@ -891,7 +1059,7 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
                                                                         d_points, s.ids, s.tile_count, s.tile_queue,
                                                                         in.mode, s.recheck_list, s.recheck_n);
     // one warp per listed tile, up to 16 warps per SM (the list is only known on the device)
-    recheck_kernel<<<std::min(total_tiles, 152 * 16), 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points,
+    recheck_kernel<<<std::min(total_tiles, device_sm_count() * 16), 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points,
                                                                        s.ids, s.tile_count, s.tile_queue, s.recheck,
                                                                        s.recheck_list, s.recheck_n);
 }
@@ -911,7 +1079,7 @@ void launch_grid_query(const GridDesc* d_grids, int grid, const double* X, int n
                        unsigned long long* key_scratch, double* min_d, cudaStream_t stream) {
     if (min_d) distance_init_kernel<<<1, 32, 0, stream>>>(key_scratch, 1);
     if (n > 0) {
-        const int blocks = std::min((n + 255) / 256, 152 * 8);
+        const int blocks = std::min((n + 255) / 256, device_sm_count() * 8);
         grid_query_kernel<<<blocks, 256, 0, stream>>>(d_grids, grid, X, n, d, min_d ? key_scratch : nullptr);
     }
     if (min_d) distance_finalize_kernel<<<1, 32, 0, stream>>>(key_scratch, min_d, 1);
@@ -961,7 +1129,7 @@ void launch_zero_status(BatchOutputs out, int n_inst, cudaStream_t stream) {
 
 void launch_gather_inputs(const HostIO* io, double* d, int n, cudaStream_t stream) {
     if (n <= 0) return;
-    const int blocks = (int)std::min<size_t>((50 * (size_t)n + 255) / 256, 152 * 4);
+    const int blocks = (int)std::min<size_t>((50 * (size_t)n + 255) / 256, (size_t)device_sm_count() * 4);
     gather_inputs_kernel<<<blocks, 256, 0, stream>>>(io, d, n);
 }
 

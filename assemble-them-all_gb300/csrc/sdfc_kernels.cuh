@@ -59,12 +59,16 @@ constexpr int kDetectThreads = 256;  // threads per detection CTA
 constexpr int kChunk = SDFC_FORCE_CHUNK;
 constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
 constexpr int kMaxSlots = 32;        // partial rows per instance (force CTAs per instance), at most
-// Slots of a batch of n instances: about six waves of force CTAs on 152 SMs
-// (measured: 4 for 1024 instances of 50k points, 16 for 256 of 1M).
-inline int slots_for(int n) {
-    constexpr int kTargetCtas = 152 * kForceCtasPerSm * 6;
+// Multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked up once per
+// device): launch shapes follow it.
+int device_sm_count();
+// Default slots of a batch of n instances on a device with `sms` multiprocessors: about six
+// waves of force CTAs (measured on GB300: 4 for 1024 instances of 50k points, 16 for 256 of 1M).
+// A batch's tuning (sdfc_batch_autotune) may replace it.
+inline int slots_for(int n, int sms) {
+    const long long target = (long long)sms * kForceCtasPerSm * 6;
     int s = 1;
-    while (s < kMaxSlots && (long long)s * n < kTargetCtas) s *= 2;
+    while (s < kMaxSlots && (long long)s * n < target) s *= 2;
     return s;
 }
 constexpr int kMaxTilesPerInstance = 4096;
@@ -80,6 +84,15 @@ struct HullDesc {
     const double* planes;
     double lo[3], hi[3];
 };
+
+// The two forms of the force pass (a batch's tuning picks one; both sum each instance's contacts
+// into `slots` partial rows in a fixed order, so each is deterministic):
+//   kForceCtas    force_kernel: one CTA of kChunk threads per (instance, slot), chunks of kChunk
+//                 contacts, the CTA's warps merged at the end;
+//   kForceWorkers force_worker_kernel: persistent one-warp CTAs, as many as the SMs hold, taking
+//                 (instance, slot) items from a queue, chunks of 32 contacts.  No CTA barrier: a
+//                 warp that finishes an item takes the next instead of waiting for its CTA.
+enum ForceVariant { kForceCtas = 0, kForceWorkers = 1 };
 
 // Fixed topology of one batch instance.
 struct InstanceDesc {
@@ -148,12 +161,19 @@ struct BatchScratch {
     PairState<float>* pair32;   // n: each instance's pair state for the FP32 kernels (written by prep_kernel)
     PairState<double>* pair64;  // n: the same for the FP64 kernels
     int* recheck_list;          // total_tiles: the tiles with queued points (appended by detect_kernel)
-    int* recheck_n;             // 1: their count (reset by prep_kernel)
+    // 5 counters, reset by prep_kernel: [0] the count of recheck_list, [1..4] the work queues of the
+    // force workers (force_worker_kernel): derivative pass on cell-corner grids, on other grids,
+    // value pass on cell-corner grids, on other grids
+    int* recheck_n;
+    int force_variant = kForceCtas;  // which force kernel runs (set by the batch's tuning)
+    int worker_ctas = 0;             // force workers launched (0: the device's multiprocessors x resident)
+    int max_ntiles = 0;              // most detection tiles of one instance (the workers' shared prefix)
 };
 
 enum Precision { kFP64 = 0, kMixed = 1 };
 
-// plain / bricks: whether the batch has instances on FP64-or-FP32 grids / on FP16-brick grids.
+// plain / bricks: whether the batch has instances on grids with the FP32 cell-corner array
+// (storages 0 and 1) / on grids without it (FP16 bricks, FP32 node values).
 void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
                    const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream,
                    bool plain = true, bool bricks = true);

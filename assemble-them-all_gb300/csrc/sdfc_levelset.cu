@@ -560,7 +560,7 @@ int ls_run(sdfc_context* ctx, const float* d_verts, const unsigned* d_tris, int 
     LS_TRY(cudaMallocAsync((void**)&d_plan, sizeof(LsPlan) * std::max(nt, 1), st));
     LS_TRY(cudaMallocAsync((void**)&d_total, sizeof(unsigned long long), st));
     LS_TRY(cudaMemsetAsync(d_total, 0, sizeof(unsigned long long), st));
-    const int fill_blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    const int fill_blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sdfc::device_sm_count() * 16);
     ls_init_kernel<<<fill_blocks, 256, 0, st>>>(d_key, d_count, n, init_key);
     LS_TRY(cudaGetLastError());
     unsigned long long total = 0;

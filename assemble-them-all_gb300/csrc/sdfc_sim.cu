@@ -395,7 +395,8 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
     }
     SceneState s = st[i];
     if (s.phase == kDone) return;
-    atomicAdd(evaluations, 1ull);
+    atomicAdd(evaluations, 1ull);  // [0]: all scenes; [1 + i]: scene i (this thread's alone)
+    evaluations[1 + i] += 1ull;
     const MoverDev& m = mover[i];
     const int nd = m.ndof;
     const bool newton = s.phase == kNewton;
@@ -480,7 +481,10 @@ __global__ void __launch_bounds__(32) sim_newton_free_warp_kernel(
     }
     SceneState s = st[i];
     if (s.phase == kDone) return;  // uniform over the warp
-    if (lane == 0) atomicAdd(evaluations, 1ull);
+    if (lane == 0) {
+        atomicAdd(evaluations, 1ull);
+        evaluations[1 + i] += 1ull;
+    }
     const MoverDev& m = mover[i];
     const bool newton = s.phase == kNewton;
     const double* p = newton ? s.x : s.xt;
@@ -1035,7 +1039,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         (rc = alloc(s, &s->d_fm, 12 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_Km, 144 * (size_t)n_pairs)) ||
         (rc = alloc(s, &s->d_Dm, 144 * (size_t)n_pairs)) || (rc = alloc(s, &s->d_nact, n_pairs)) ||
         (rc = alloc(s, &s->d_status, n_pairs)) || (rc = alloc(s, &s->d_conv, n)) ||
-        (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, 1)) || (rc = alloc(s, &s->d_adj, n)) ||
+        (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, (size_t)n + 1)) || (rc = alloc(s, &s->d_adj, n)) ||
         (rc = alloc(s, &s->d_gout, 18 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2)) ||
         (rc = alloc(s, &s->d_epair, n_pairs)) || (rc = alloc(s, &s->d_dEpair, 12 * (size_t)n_pairs)) ||
         (rc = alloc(s, &s->d_dfdE, n))) {
@@ -1106,7 +1110,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     if (e == cudaSuccess) e = cudaMemset(s->d_qd, 0, sizeof(double) * nd * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_fext, 0, sizeof(double) * 6 * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_conv, 0, sizeof(int) * n);
-    if (e == cudaSuccess) e = cudaMemset(s->d_evals, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(s->d_evals, 0, sizeof(unsigned long long) * ((size_t)n + 1));
     if (e != cudaSuccess) {
         free_sim(s);
         return fail(ctx, SDFC_ERR_CUDA, std::string("sim_create: ") + cudaGetErrorString(e));
@@ -1126,28 +1130,69 @@ void sdfc_sim_destroy(sdfc_sim* s) {
     free_sim(s);
 }
 
+// Drops the captured graphs (they launch the kernels of the configuration they were captured
+// under); the next step or backward pass captures them again.
+static void drop_graphs(sdfc_sim* s) {
+    for (cudaGraphExec_t& g : s->round_exec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    for (cudaGraphExec_t& g : s->compact_exec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    if (s->back_exec) {
+        cudaGraphExecDestroy(s->back_exec);
+        s->back_exec = nullptr;
+    }
+}
+
 int sdfc_sim_set_precision(sdfc_sim* s, int precision) {
     if (!s) return SDFC_ERR_INVALID_ARGUMENT;
     if (precision != SDFC_PRECISION_FP64 && precision != SDFC_PRECISION_MIXED)
         return fail(s->ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_precision: unknown precision");
     if (s->batch) s->batch->precision = precision;
-    if (s->round_exec[0] || s->round_exec[1] || !s->compact_exec.empty()) {
-        // the captured rounds launch the old precision's kernels
-        for (cudaGraphExec_t& g : s->round_exec)
-            if (g) {
-                cudaGraphExecDestroy(g);
-                g = nullptr;
-            }
-        for (cudaGraphExec_t& g : s->compact_exec)
-            if (g) {
-                cudaGraphExecDestroy(g);
-                g = nullptr;
-            }
-    }
-    if (s->back_exec) {
-        cudaGraphExecDestroy(s->back_exec);
-        s->back_exec = nullptr;
-    }
+    drop_graphs(s);
+    return SDFC_OK;
+}
+
+int sdfc_sim_set_tuning(sdfc_sim* s, const sdfc_tuning* t) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    if (!s->batch) return fail(s->ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_set_tuning: the sim has no contact pairs");
+    int rc = sdfc_batch_set_tuning(s->batch, t);
+    if (rc) return rc;
+    drop_graphs(s);
+    return SDFC_OK;
+}
+
+int sdfc_sim_get_tuning(sdfc_sim* s, sdfc_tuning* t) {
+    if (!s || !s->batch) return SDFC_ERR_INVALID_ARGUMENT;
+    return sdfc_batch_get_tuning(s->batch, t);
+}
+
+int sdfc_sim_autotune(sdfc_sim* s, sdfc_tuning* chosen) {
+    if (!s) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    if (s->n_pairs == 0) return fail(ctx, SDFC_ERR_INVALID_ARGUMENT, "sim_autotune: the sim has no contact pairs");
+    cudaStream_t st = ctx->stream;
+    const int n = s->n, np = s->n_pairs, tb = 128;
+    // the opening evaluation of a step from the current state: every scene at its Newton point
+    // (the state sim_begin_kernel writes is rewritten by the next step)
+    sim_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_mover, s->d_q, s->d_qd, s->d_state,
+                                                      s->d_remaining);
+    sim_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, s->d_pair_inst, s->d_role, s->d_Efixed, s->d_mover,
+                                                      s->d_state, s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_mode);
+    SDFC_CUDA_TRY(ctx, cudaGetLastError());
+    sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
+    in.mode = s->d_mode;
+    sdfc::BatchOutputs out{s->d_fm, s->d_Km, s->d_Dm, s->d_nact, s->d_status};
+    if ((rc = sdfc_impl::autotune(s->batch, in, true, out, st, chosen))) return rc;
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    drop_graphs(s);
     return SDFC_OK;
 }
 
@@ -1565,6 +1610,16 @@ int sdfc_sim_stats(sdfc_sim* s, long long* rounds, long long* evaluations) {
     SDFC_CUDA_TRY(ctx, cudaMemcpy(&e, s->d_evals, sizeof e, cudaMemcpyDeviceToHost));
     if (rounds) *rounds = s->rounds;
     if (evaluations) *evaluations = (long long)e;
+    return SDFC_OK;
+}
+
+int sdfc_sim_scene_evaluations(sdfc_sim* s, long long* evaluations) {
+    if (!s || !evaluations) return SDFC_ERR_INVALID_ARGUMENT;
+    sdfc_context* ctx = s->ctx;
+    int rc = use_device(ctx);
+    if (rc) return rc;
+    SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    SDFC_CUDA_TRY(ctx, cudaMemcpy(evaluations, s->d_evals + 1, sizeof(long long) * s->n, cudaMemcpyDeviceToHost));
     return SDFC_OK;
 }
 

@@ -1,10 +1,12 @@
 // See ForceGeneralSDFContactGPU.h.
 #include "ForceGeneralSDFContactGPU.h"
 
+#include <cstring>
 #include <string>
 #include <vector>
 
 #include "Body/Body.h"
+#include "Body/BodyCuboid.h"
 #include "Body/BodySDFObj.h"
 
 namespace redmax {
@@ -51,25 +53,38 @@ void ForceGeneralSDFContactGPU::set_stiffness(dtype kn, dtype kt) { _kn = kn; _k
 void ForceGeneralSDFContactGPU::set_friction(dtype mu) { _mu = mu; }
 void ForceGeneralSDFContactGPU::set_damping(dtype damping) { _damping = damping; }
 void ForceGeneralSDFContactGPU::set_scale(dtype scale) { _scale = scale; }
+void ForceGeneralSDFContactGPU::set_derivative_mode(int mode) {
+    if (mode != SDFC_DERIV_ANALYTIC && mode != SDFC_DERIV_STENCIL) throw_error("unknown derivative mode");
+    _deriv_mode = mode;
+}
 
 void ForceGeneralSDFContactGPU::upload_if_needed() {
     sdfc_context* ctx = shared_context();
-    const std::vector<Vector3>& pts = _contact_body->_contact_points;
-    if (_points < 0 || _points_n != pts.size()) {
-        std::vector<double> xyz(3 * pts.size());
-        for (size_t i = 0; i < pts.size(); ++i)
-            for (int k = 0; k < 3; ++k) xyz[3 * i + k] = pts[i](k);
+    // the contact points detection reads (CollisionDetection.cpp:126-131): a cuboid's
+    // general contact points, any other body's contact points
+    std::vector<Vector3> pts = _contact_body->get_contact_points();
+    if (BodyCuboid* cuboid = dynamic_cast<BodyCuboid*>(_contact_body)) pts = cuboid->get_general_contact_points();
+    std::vector<double> xyz(3 * pts.size());
+    for (size_t i = 0; i < pts.size(); ++i)
+        for (int k = 0; k < 3; ++k) xyz[3 * i + k] = pts[i](k);
+    if (_points < 0 || xyz != _points_seen) {
         check(sdfc_upload_points(ctx, xyz.data(), (int)pts.size(), SDFC_STORAGE_F64, &_points), "upload_points");
-        _points_n = pts.size();
+        _points_seen.swap(xyz);
     }
-    if (_grid < 0 || _grid_data != (const void*)_SDF_body->_SDF.a.data()) {
-        const double mn[3] = {_SDF_body->_min_box[0], _SDF_body->_min_box[1], _SDF_body->_min_box[2]};
-        const double mx[3] = {_SDF_body->_max_box[0], _SDF_body->_max_box[1], _SDF_body->_max_box[2]};
-        const double dx[3] = {_SDF_body->_dx, _SDF_body->_dy, _SDF_body->_dz};
-        check(sdfc_upload_grid(ctx, _SDF_body->_SDF.a.data(), _SDF_body->_SDF.ni, _SDF_body->_SDF.nj,
-                               _SDF_body->_SDF.nk, mn, mx, dx, _SDF_body->_col_th, SDFC_STORAGE_F64, &_grid),
+    const BodySDFObj* b = _SDF_body;
+    const size_t n = (size_t)b->_SDF.ni * b->_SDF.nj * b->_SDF.nk;
+    const double head[13] = {(double)b->_SDF.ni, (double)b->_SDF.nj, (double)b->_SDF.nk, b->_min_box[0], b->_min_box[1],
+                             b->_min_box[2], b->_max_box[0], b->_max_box[1], b->_max_box[2], b->_dx, b->_dy, b->_dz,
+                             b->_col_th};
+    const bool same = _grid >= 0 && _grid_seen.size() == 13 + n &&
+                      std::memcmp(_grid_seen.data(), head, sizeof head) == 0 &&
+                      std::memcmp(_grid_seen.data() + 13, b->_SDF.a.data(), n * sizeof(double)) == 0;
+    if (!same) {
+        check(sdfc_upload_grid(ctx, b->_SDF.a.data(), b->_SDF.ni, b->_SDF.nj, b->_SDF.nk, head + 3, head + 6, head + 9,
+                               b->_col_th, SDFC_STORAGE_F64, &_grid),
               "upload_grid");
-        _grid_data = _SDF_body->_SDF.a.data();
+        _grid_seen.assign(head, head + 13);
+        _grid_seen.insert(_grid_seen.end(), b->_SDF.a.data(), b->_SDF.a.data() + n);
     }
 }
 
@@ -80,6 +95,7 @@ int ForceGeneralSDFContactGPU::evaluate(bool deriv, double* fm12, double* Km144,
     pose_of(_SDF_body, EB, phiB);
     sdfc_params p{_kn, _kt, _mu, _damping, _scale, _contact_body->_contact_scale};
     int n_active = 0;
+    check(sdfc_set_derivative_mode(shared_context(), _deriv_mode), "set_derivative_mode");
     check(sdfc_evaluate(shared_context(), _points, _grid, EA, phiA, EB, phiB, &p, deriv ? 1 : 0, fm12, Km144, Dm144,
                         &n_active),
           "evaluate");

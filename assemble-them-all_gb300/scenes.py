@@ -32,6 +32,27 @@ class AssemblyScene:
         m, inertia = asm.parts[asm.mover].mass_props()
         return cls(asm, grids, pts, m, inertia)
 
+    @classmethod
+    def make_device(cls, ctx: "sdfc.Context", asm: W.Assembly, seed: int = 0, storage=sdfc.STORAGE_F32_NODES,
+                    col_th=0.0):
+        """The scene of a large assembly generated on the device: each part's FP32 grid is sampled
+        on the GPU and uploaded at once (kept only in the context, as grid handles), and its
+        contact points are drawn on the GPU (kept on the host for the point upload)."""
+        import torch
+        handles, boxes = [], []
+        for p, n in zip(asm.parts, asm.grid_n):
+            vals, mn, mx, dx = p.grid_device(n)
+            torch.cuda.current_stream().synchronize()  # the library reads the values on its own stream
+            handles.append(ctx.upload_grid_device(vals.data_ptr(), tuple(vals.shape), mn, mx, dx, col_th, storage))
+            boxes.append((mn, mx, dx))
+            del vals
+        pts = [p.surface_points_device(n, seed * 1000 + k) for k, (p, n) in enumerate(zip(asm.parts, asm.n_points))]
+        m, inertia = asm.parts[asm.mover].mass_props()
+        sc = cls(asm, None, pts, m, inertia)
+        sc.grid_handles = handles
+        sc.grid_boxes = boxes  # (min_box, max_box, dx) per part
+        return sc
+
     def placement(self, k):
         return W.pose(None, self.asm.parts[k].position)
 
@@ -51,8 +72,11 @@ def build_sim(ctx: "sdfc.Context", scenes, h, gravity, params: "sdfc.Params", co
     q = qdot = 0 with no external force."""
     movers, pairs = [], []
     for i, sc in enumerate(scenes):
-        gh = [ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, col_th, storage) for g in sc.grids]
-        ph = [ctx.upload_points(p, storage) for p in sc.points]
+        gh = getattr(sc, "grid_handles", None)  # grids generated and uploaded on the device
+        if gh is None:
+            gh = [ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, col_th, storage) for g in sc.grids]
+        ph = [ctx.upload_points(p, sdfc.STORAGE_F32 if storage == sdfc.STORAGE_F32_NODES else storage)
+              for p in sc.points]
         m = sc.asm.mover
         movers.append(sdfc.Mover.make(sc.mass, sc.inertia, np.eye(4), h, gravity, E_pj0=sc.placement(m)))
         for a, b in sc.contact_pairs():

@@ -19,6 +19,7 @@ SDFC_ERR_NOT_FOUND = -3
 STORAGE_F64 = 0
 STORAGE_F32 = 1
 STORAGE_F16_BRICKS = 2
+STORAGE_F32_NODES = 3
 
 # every symbol include/sdfc.h declares
 EXPORTS = (
@@ -34,7 +35,9 @@ EXPORTS = (
     "sdfc_sim_set_tolerance", "sdfc_make_level_set3", "sdfc_make_level_set3_device", "sdfc_sdf_grid_layout",
     "sdfc_batch_distance", "sdfc_batch_distance_device", "sdfc_grid_distance", "sdfc_sdf_save_text",
     "sdfc_sdf_load_text", "sdfc_sdf_save_bricks", "sdfc_sdf_load_bricks", "sdfc_upload_grid_bricks",
-    "sdfc_upload_hull", "sdfc_disassembled", "sdfc_disassembled_device",
+    "sdfc_upload_hull", "sdfc_disassembled", "sdfc_disassembled_device", "sdfc_upload_grid_device",
+    "sdfc_sim_scene_evaluations", "sdfc_batch_autotune", "sdfc_batch_get_tuning", "sdfc_batch_set_tuning",
+    "sdfc_sim_autotune", "sdfc_sim_get_tuning", "sdfc_sim_set_tuning",
 )
 JOINT_TRANSLATIONAL = 3
 JOINT_FREE3D_EXP = 6
@@ -62,6 +65,20 @@ class Mover(ctypes.Structure):
                    (ctypes.c_double * 16)(*E_pj0.ravel()),
                    (ctypes.c_double * 16)(*np.asarray(E_ji, dtype=np.float64).ravel()),
                    (ctypes.c_double * 3)(*gravity), float(h), float(joint_stiffness), float(joint_damping))
+
+
+FORCE_CTAS = 0
+FORCE_WORKERS = 1
+
+
+class Tuning(ctypes.Structure):
+    """sdfc_tuning: the launch configuration of a batch's force pass."""
+    _fields_ = [("slots", ctypes.c_int), ("force_variant", ctypes.c_int), ("worker_ctas", ctypes.c_int),
+                ("ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {"slots": self.slots, "force_variant": ("ctas", "workers")[self.force_variant],
+                "worker_ctas": self.worker_ctas, "ms": float(self.ms)}
 
 
 class Params(ctypes.Structure):
@@ -105,6 +122,7 @@ def lib():
         L.sdfc_last_error.argtypes = [v]
         L.sdfc_last_error.restype = ctypes.c_char_p
         L.sdfc_upload_grid.argtypes = [v, d, i, i, i, d, d, d, ctypes.c_double, i, P(i)]
+        L.sdfc_upload_grid_device.argtypes = [v, v, i, i, i, d, d, d, ctypes.c_double, i, P(i)]
         L.sdfc_upload_points.argtypes = [v, d, i, i, P(i)]
         L.sdfc_evaluate.argtypes = [v, i, i, d, d, d, d, P(Params), i, d, d, d, P(i)]
         L.sdfc_active_ids.argtypes = [v, P(i), i, P(i)]
@@ -128,6 +146,13 @@ def lib():
         L.sdfc_sim_set_external_force.argtypes = [v, d]
         L.sdfc_sim_step.argtypes = [v, i, P(i)]
         L.sdfc_sim_stats.argtypes = [v, P(ctypes.c_longlong), P(ctypes.c_longlong)]
+        L.sdfc_sim_scene_evaluations.argtypes = [v, P(ctypes.c_longlong)]
+        L.sdfc_batch_autotune.argtypes = [v, v, v, v, v, v, i, v, v, v, v, v, v, P(Tuning)]
+        L.sdfc_batch_get_tuning.argtypes = [v, P(Tuning)]
+        L.sdfc_batch_set_tuning.argtypes = [v, P(Tuning)]
+        L.sdfc_sim_autotune.argtypes = [v, P(Tuning)]
+        L.sdfc_sim_get_tuning.argtypes = [v, P(Tuning)]
+        L.sdfc_sim_set_tuning.argtypes = [v, P(Tuning)]
         L.sdfc_sim_record.argtypes = [v, i]
         L.sdfc_grid_values.argtypes = [v, i, d]
         L.sdfc_batch_energy.argtypes = [v, d, d, P(Params), d, d]
@@ -225,6 +250,17 @@ class Context:
         self._check(lib().sdfc_upload_grid(self._h, _dp(v), ni, nj, nk, _dp(_f64(min_box, 3)), _dp(_f64(max_box, 3)),
                                            _dp(_f64(dx, 3)), float(col_th), int(storage), ctypes.byref(h)),
                     "sdfc_upload_grid")
+        self._grid_shapes[h.value] = (nk, nj, ni)
+        return h.value
+
+    def upload_grid_device(self, values_ptr, shape, min_box, max_box, dx, col_th, storage=STORAGE_F32_NODES) -> int:
+        """sdfc_upload_grid_device: FP32 node values already on the device (values_ptr, an int
+        address of (nk, nj, ni) floats, i fastest); shape = (nk, nj, ni)."""
+        nk, nj, ni = shape
+        h = ctypes.c_int()
+        self._check(lib().sdfc_upload_grid_device(self._h, int(values_ptr), ni, nj, nk, _dp(_f64(min_box, 3)),
+                                                  _dp(_f64(max_box, 3)), _dp(_f64(dx, 3)), float(col_th),
+                                                  int(storage), ctypes.byref(h)), "sdfc_upload_grid_device")
         self._grid_shapes[h.value] = (nk, nj, ni)
         return h.value
 
@@ -456,6 +492,25 @@ class Batch:
                                                          int(bool(want_deriv)), fm, Km or 0, Dm or 0, n_active,
                                                          status, stream), "sdfc_batch_evaluate_device")
 
+    def autotune(self, E_A, phi_A, E_B, phi_B, params, fm, Km, Dm, n_active, status, want_deriv=True,
+                 stream=0) -> dict:
+        """sdfc_batch_autotune on device inputs (pointers as for evaluate_device); returns the
+        chosen launch configuration, which the batch keeps."""
+        t = Tuning()
+        self.ctx._check(lib().sdfc_batch_autotune(self._h, E_A, phi_A, E_B, phi_B, params, int(bool(want_deriv)), fm,
+                                                  Km or 0, Dm or 0, n_active, status, stream, ctypes.byref(t)),
+                        "sdfc_batch_autotune")
+        return t.as_dict()
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        self.ctx._check(lib().sdfc_batch_get_tuning(self._h, ctypes.byref(t)), "sdfc_batch_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, slots: int, force_variant: int, worker_ctas: int = 0):
+        t = Tuning(int(slots), int(force_variant), int(worker_ctas), 0.0)
+        self.ctx._check(lib().sdfc_batch_set_tuning(self._h, ctypes.byref(t)), "sdfc_batch_set_tuning")
+
     def energy(self, E_A, E_B, params):
         """Penetration energy per instance (n,) and its gradient wrt both bodies' twists (n, 12)."""
         n = self.n
@@ -528,6 +583,21 @@ class Sim:
     def set_precision(self, precision: int):
         self.ctx._check(lib().sdfc_sim_set_precision(self._h, int(precision)), "sdfc_sim_set_precision")
 
+    def autotune(self) -> dict:
+        """sdfc_sim_autotune: the fastest launch configuration for the sim's batch of pairs."""
+        t = Tuning()
+        self.ctx._check(lib().sdfc_sim_autotune(self._h, ctypes.byref(t)), "sdfc_sim_autotune")
+        return t.as_dict()
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        self.ctx._check(lib().sdfc_sim_get_tuning(self._h, ctypes.byref(t)), "sdfc_sim_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, slots: int, force_variant: int, worker_ctas: int = 0):
+        t = Tuning(int(slots), int(force_variant), int(worker_ctas), 0.0)
+        self.ctx._check(lib().sdfc_sim_set_tuning(self._h, ctypes.byref(t)), "sdfc_sim_set_tuning")
+
     def set_state(self, q, qdot):
         self.generation += 1
         k = self.ndof * self.n
@@ -553,6 +623,13 @@ class Sim:
         r, e = ctypes.c_longlong(), ctypes.c_longlong()
         self.ctx._check(lib().sdfc_sim_stats(self._h, ctypes.byref(r), ctypes.byref(e)), "sdfc_sim_stats")
         return r.value, e.value
+
+    def scene_evaluations(self) -> np.ndarray:
+        """Force evaluations of each scene since creation (sdfc_sim_scene_evaluations)."""
+        out = np.zeros(self.n, dtype=np.int64)
+        self.ctx._check(lib().sdfc_sim_scene_evaluations(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))),
+                        "sdfc_sim_scene_evaluations")
+        return out
 
     # adjoint (Simulation::reset(backward_flag=True) / get_q_his / backward)
     def record(self, max_steps: int):

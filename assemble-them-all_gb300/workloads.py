@@ -303,6 +303,106 @@ class Part:
         lo, hi = self.bounds()
         return sample_grid(self.sdf, lo, hi, n, pad=pad, dtype=dtype)
 
+    # ---- the same definitions evaluated on the GPU (torch, FP64), for workloads too large to
+    # generate on the host (hundreds of 256^3 grids, tens of millions of surface points)
+    def sdf_device(self, p):
+        """sdf() of (..., 3) FP64 points on the device."""
+        d = None
+        for pr in self.prims:
+            if pr.sign > 0:
+                s = _prim_sdf_t(pr, p)
+                d = s if d is None else _torch().minimum(d, s)
+        for pr in self.prims:
+            if pr.sign < 0:
+                d = _torch().maximum(d, -_prim_sdf_t(pr, p))
+        return d
+
+    def grid_device(self, n, pad=0.1):
+        """grid(n, FP32) sampled on the device: (FP32 values (nk, nj, ni) on the device, min_box,
+        max_box, dx), the box and spacing computed as sample_grid computes them."""
+        torch = _torch()
+        lo, hi = self.bounds()
+        ext = hi - lo
+        mn = lo - pad * ext / 2.0
+        mx = hi + pad * ext / 2.0
+        dx = (mx - mn) / (n - 1)
+        mx = mn + (n - 1) * dx
+        ax = [torch.tensor(mn[a] + dx[a] * np.arange(n), dtype=torch.float64, device="cuda") for a in range(3)]
+        Y, X = torch.meshgrid(ax[1], ax[0], indexing="ij")
+        vals = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+        for k0 in range(0, n, 32):  # slabs of 32 planes bound the temporaries
+            k1 = min(n, k0 + 32)
+            Z = ax[2][k0:k1].view(-1, 1, 1).expand(k1 - k0, n, n)
+            P = torch.stack([X.expand(k1 - k0, n, n), Y.expand(k1 - k0, n, n), Z], dim=-1)
+            vals[k0:k1] = self.sdf_device(P).to(torch.float32)
+        return vals, mn, mx, dx
+
+    def surface_points_device(self, n, seed, tol=1e-9):
+        """surface_points(n) drawn on the device (its own seeded stream): n points uniform
+        (area-weighted) on the part's surface, rounded to FP32, returned as a host (n, 3) FP64 array."""
+        torch = _torch()
+        g = torch.Generator(device="cuda")
+        g.manual_seed(int(seed))
+        areas = torch.tensor([pr.area() for pr in self.prims], dtype=torch.float64, device="cuda")
+        out, have = [], 0
+        while have < n:
+            m = max(2 * (n - have), 256)
+            which = torch.multinomial(areas / areas.sum(), m, replacement=True, generator=g)
+            counts = torch.bincount(which, minlength=len(self.prims)).tolist()
+            cand = torch.cat([_prim_sample_t(pr, g, c) for pr, c in zip(self.prims, counts) if c > 0])
+            keep = cand[self.sdf_device(cand).abs() <= tol]
+            out.append(keep)
+            have += len(keep)
+        pts = torch.cat(out)[:n]
+        pts = pts[torch.randperm(len(pts), generator=g, device="cuda")]
+        return pts.to(torch.float32).to(torch.float64).cpu().numpy()
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _prim_sdf_t(pr, p):
+    torch = _torch()
+    c = torch.tensor(pr.c, dtype=torch.float64, device=p.device)
+    if pr.kind == "box":
+        q = (p - c).abs() - torch.tensor(pr.size, dtype=torch.float64, device=p.device)
+        return q.clamp_min(0.0).norm(dim=-1) + q.amax(dim=-1).clamp_max(0.0)
+    r, hl = pr.size
+    d = p - c
+    rr = torch.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2)
+    e = torch.stack([rr - r, d[..., 2].abs() - hl], dim=-1)
+    return e.amax(dim=-1).clamp_max(0.0) + e.clamp_min(0.0).norm(dim=-1)
+
+
+def _prim_sample_t(pr, g, n):
+    """Primitive.sample_surface on the device."""
+    torch = _torch()
+    dev = "cuda"
+    c = torch.tensor(pr.c, dtype=torch.float64, device=dev)
+    if pr.kind == "box":
+        h = torch.tensor(pr.size, dtype=torch.float64, device=dev)
+        areas = torch.stack([h[1] * h[2], h[1] * h[2], h[0] * h[2], h[0] * h[2], h[0] * h[1], h[0] * h[1]])
+        face = torch.multinomial(areas / areas.sum(), n, replacement=True, generator=g)
+        u = (torch.rand((n, 3), dtype=torch.float64, device=dev, generator=g) * 2.0 - 1.0) * h
+        ax = face // 2
+        idx = torch.arange(n, device=dev)
+        u[idx, ax] = torch.where(face % 2 == 0, -h[ax], h[ax])
+        return c + u
+    r, hl = pr.size
+    side, cap = 2 * np.pi * r * 2 * hl, np.pi * r * r
+    rnd = lambda: torch.rand(n, dtype=torch.float64, device=dev, generator=g)  # noqa: E731
+    which = rnd() * (side + 2 * cap)
+    th = rnd() * (2 * np.pi)
+    z = rnd() * (2 * hl) - hl
+    rr = r * torch.sqrt(rnd())
+    zc = torch.where(which < side + cap, torch.full_like(z, -hl), torch.full_like(z, hl))
+    lat = (which < side).unsqueeze(-1)
+    a = torch.stack([r * torch.cos(th), r * torch.sin(th), z], dim=-1)
+    b = torch.stack([rr * torch.cos(th), rr * torch.sin(th), zc], dim=-1)
+    return c + torch.where(lat, a, b)
+
 
 @dataclass
 class Assembly:

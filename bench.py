@@ -357,6 +357,12 @@ def run_gpu(args, world, rank):
                           fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
                           want_deriv=True, stream=stream.cuda_stream)
 
+    tuning = None
+    if not args.no_autotune:  # the batch's launch configuration, timed once on these inputs
+        tuning = batch.autotune(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
+                                fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
+                                want_deriv=True, stream=stream.cuda_stream)
+    tuning_used = batch.tuning()
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step()
@@ -444,6 +450,7 @@ def run_gpu(args, world, rank):
     c4_res = run_c4(args, sdfc, ctx, g, torch) if args.c4_instances > 0 and rank == 0 else None
     ls_res = run_levelset(args, sdfc, ctx, torch) if args.ls_segments > 0 and rank == 0 else None
     pl_res = run_planner(args, sdfc, ctx, torch) if args.planner_states > 0 and rank == 0 else None
+    c3_res = run_c3(args, sdfc, ctx, torch) if args.c3_assemblies > 0 and rank == 0 else None
     if sim_res is not None:
         plain = run_sim_plain(args, sdfc, ctx, g, p, n)
         plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
@@ -456,11 +463,8 @@ def run_gpu(args, world, rank):
     # algorithmic bytes: detection reads 12 B per point and 8 FP32 corners (32 B) per query
     det_bytes = pts_per_step * (12 + 8 * 4)
     # forces: per active contact its id (4 B), point (12 B) and 8 FP32 corners; per instance-slot 300 FP64 partials
-    # per instance-slot 300 FP64 partials (the library's slots per instance: about six waves of
-    # force CTAs, slots_for in csrc/sdfc_kernels.cuh)
-    slots = 1
-    while slots < 32 and slots * n < 152 * 4 * 6:
-        slots *= 2
+    # per instance-slot 300 FP64 partials (the batch's slots per instance, as tuned)
+    slots = tuning_used["slots"]
     frc_bytes = n_active * (4 + 12 + 32) + n * slots * 300 * 8
     kernels = {
         "detect": {"ms": det_ms, "bytes": det_bytes},
@@ -494,6 +498,9 @@ def run_gpu(args, world, rank):
         "plain_fp64_per_instance": {"value": plain_rate, "unit": UNIT, "instances_timed": len(plain_t),
                                     "speedup_of_batched": value / plain_rate},
         "error_vs_fp64_path": err,
+        "tuning": {"chosen": tuning_used, "autotuned": tuning is not None,
+                   "candidates": "force pass as CTAs per (instance, slot) or persistent one-warp workers, "
+                                 "x 1-32 partial sums per instance; each timed on one evaluation"},
         "active_contacts_per_step": n_active, "fp64_rechecked_points_per_step": rechecked,
         "gpu_launches": 5 * args.steps,  # prep, detect, recheck, force, finalize
         "clocks": clk,
@@ -520,6 +527,8 @@ def run_gpu(args, world, rank):
         line["sdf_construction"] = ls_res
     if pl_res is not None:
         line["planner_queries"] = pl_res
+    if c3_res is not None:
+        line["uneven_assemblies"] = c3_res
     print(json.dumps(line), flush=True)
 
 
@@ -905,6 +914,121 @@ def run_c4(args, sdfc, ctx, g, torch):
             "checkpoint": "joint trajectory every step (48 B per scene-step); step matrices recomputed in reverse"}
 
 
+# --------------------------------------------------------------------------- uneven multi-part batch
+# The planner's scene parameters (examples/run_joint_plan.py:147-153, 192-216): h = 1e-3 (read as
+# FP32), gravity 1e-12 along +z, kn = 1e6, kt = 1e3, mu = 0, damping = 0, pull 100, and
+# col_th = max(-min distance, 0) + 0.01 = 0.01 for these assemblies (parts 0.005 apart).
+C3_H = float(np.float32(1e-3))
+C3_GRAVITY = (0.0, 0.0, 1e-12)
+C3_PULL = 100.0
+C3_PRM = (1e6, 1e3, 0.0, 0.0, 1.0, 1.0)
+C3_COL_TH = 0.01
+
+
+def _c3_cpu_scene(args):
+    """Steps of one assembly scene by the oracle (spawned worker): (seconds, scene evaluations)."""
+    from oracle import oracle as O
+    mover, pairs, steps = args
+    grids, opairs = {}, []
+    for (gkey, gv, mn, mx, dx), pts, is_contact, E_fixed in pairs:
+        if gkey not in grids:
+            grids[gkey] = O.Grid(gv, mn, mx, dx, C3_COL_TH)
+        opairs.append(O.ScenePair(grids[gkey], pts, is_contact, E_fixed, O.Params(*C3_PRM)))
+    t = time.perf_counter()
+    _, _, _, _, evs = O.bdf1_steps(O.Mover(*mover), opairs, np.zeros(3), np.zeros(3), steps)
+    return time.perf_counter() - t, int(evs.sum())
+
+
+def run_c3(args, sdfc, ctx, torch):
+    """Uneven multi-part batch: args.c3_assemblies seeded procedural assemblies (2-12 parts, per
+    part log-uniform 2k-200k contact points and a grid of 64^3, 128^3 or 256^3 FP32 nodes), one
+    part of each pulled along a random axis for args.c3_steps BDF1 steps, all scenes in one
+    sdfc_sim (the pulled part against every other part both ways, as the planner declares it).
+    Grids are sampled on the GPU and kept as FP32 node values (4 B per node)."""
+    S = importlib.import_module(f"{PKG}.scenes")
+    t0 = time.perf_counter()
+    asms = [W.procedural_assembly(s) for s in range(args.c3_assemblies)]
+    scenes = [S.AssemblyScene.make_device(ctx, a, s, col_th=C3_COL_TH) for s, a in enumerate(asms)]
+    sim = S.build_sim(ctx, scenes, C3_H, C3_GRAVITY, sdfc.Params(*C3_PRM), col_th=C3_COL_TH,
+                      storage=sdfc.STORAGE_F32_NODES)
+    setup_s = time.perf_counter() - t0
+    sim.set_precision(sdfc.PRECISION_MIXED if args.precision == "mixed" else sdfc.PRECISION_FP64)
+    n = len(scenes)
+    F = S.pull_forces(scenes, C3_PULL)
+    zero = np.zeros((n, 3))
+    sim.set_state(zero, zero)
+    sim.set_external_force(F)
+    tuning = sim.autotune() if not args.no_autotune else sim.tuning()
+    sim.step(1)  # warm-up: the round graphs are captured here
+    sim.set_state(zero, zero)
+    e0 = sim.scene_evaluations()
+    r0, _ = sim.stats()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    conv = sim.step(args.c3_steps)
+    wall = time.perf_counter() - t
+    r1, _ = sim.stats()
+    evals = sim.scene_evaluations() - e0
+    q, _ = sim.get_state()
+    # contact points one evaluation of a scene evaluates: its pairs' contact-body points
+    pts_scene = np.array([sum(len(sc.points[a]) for a, _ in sc.contact_pairs()) for sc in scenes], dtype=np.int64)
+    cpe = int((evals * pts_scene).sum())
+    disp = np.linalg.norm(q, axis=1)
+    parts = [len(a.parts) for a in asms]
+    grid_n = [g for a in asms for g in a.grid_n]
+    out = {
+        "assemblies": n, "parts": int(sum(parts)), "parts_per_assembly": [int(min(parts)), int(max(parts))],
+        "pairs": int(sum(2 * (k - 1) for k in parts)), "contact_points_total": int(sum(sum(a.n_points) for a in asms)),
+        "points_per_part": [int(min(min(a.n_points) for a in asms)), int(max(max(a.n_points) for a in asms))],
+        "grids": {f"{g}^3": int(sum(1 for x in grid_n if x == g)) for g in (64, 128, 256)},
+        "grid_storage": "fp32 nodes", "grid_bytes": int(sum(4 * g ** 3 for g in grid_n)),
+        "grid_bytes_cell_corner_layout": int(sum(40 * g ** 3 for g in grid_n)),
+        "precision": args.precision, "tuning": tuning, "setup_s": setup_s, "steps": args.c3_steps, "wall_s": wall,
+        "scene_steps_per_s": n * args.c3_steps / wall, "rounds": r1 - r0,
+        "scene_evaluations": int(evals.sum()),
+        "evaluations_per_scene_step": float(evals.sum()) / (n * args.c3_steps),
+        "contact_point_evaluations": cpe, "contact_pts_per_s": cpe / wall,
+        "work_spread": {
+            "points_per_scene_evaluation": {"min": int(pts_scene.min()), "median": float(np.median(pts_scene)),
+                                            "max": int(pts_scene.max())},
+            "evaluations_per_scene": {"min": int(evals.min()), "median": float(np.median(evals)),
+                                      "max": int(evals.max())},
+            "contact_points_per_scene": {"min": int((evals * pts_scene).min()),
+                                         "median": float(np.median(evals * pts_scene)),
+                                         "max": int((evals * pts_scene).max())}},
+        "converged_last_step": float(np.mean(conv)),
+        "displacement": {"escaped_over_1": int((disp > 1.0).sum()), "held_under_0.1": int((disp < 0.1).sum())},
+    }
+    if args.c3_cpu_scenes > 0:
+        # the oracle on the first scenes, a few steps each, one process per scene
+        k = min(args.c3_cpu_scenes, n)
+        jobs = []
+        for sc in scenes[:k]:
+            m = sc.asm.mover
+            Fm = np.zeros(6)
+            Fm[3:] = C3_PULL * sc.asm.direction
+            mover = (sc.mass, sc.inertia, np.eye(4), sc.placement(m), C3_GRAVITY, C3_H, Fm)
+            pairs = []
+            for a, b in sc.contact_pairs():
+                lo, hi, dx = sc.grid_boxes[b]
+                pairs.append(((b, ctx.grid_values(sc.grid_handles[b]), lo, hi, dx), sc.points[a], a == m,
+                              sc.placement(b if a == m else a)))
+            jobs.append((mover, pairs, args.c3_cpu_steps))
+        procs = min(k, os.cpu_count() or 1)
+        t = time.perf_counter()
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_c3_cpu_scene, jobs, chunksize=1)
+        cwall = time.perf_counter() - t
+        ev = np.array([r[1] for r in res])
+        out["cpu_baseline"] = {
+            "value": k * args.c3_cpu_steps / cwall, "unit": "scene-steps/s", "cores": procs, "kind": "port",
+            "contact_pts_per_s": float((ev * pts_scene[:k]).sum()) / cwall,
+            "sample": f"scenes 0-{k - 1}, {args.c3_cpu_steps} steps each from rest, one process per scene "
+                      "(wall time includes sending each scene's grids to its process)"}
+    sim.close()
+    return out
+
+
 def cpu_sim_rate(pool, n_scenes, steps, procs):
     dirs = W.fibonacci_directions(1024)
     idx = np.linspace(0, len(dirs) - 1, n_scenes).astype(int)
@@ -930,6 +1054,7 @@ def main():
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=512, help="instances per CPU-baseline step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the batches' default launch configuration")
     ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
     ap.add_argument("--plain-sample", type=int, default=64, help="instances timed on the per-instance FP64 path")
     ap.add_argument("--full-error", action="store_true", help="compare every instance against the FP64 path")
@@ -953,6 +1078,11 @@ def main():
     ap.add_argument("--c5-dirs", type=int, default=256, help="FP16-brick leg: pull directions")
     ap.add_argument("--c5-steps", type=int, default=200, help="FP16-brick leg: BDF1 steps (0: skip)")
     ap.add_argument("--c5-check", type=int, default=8, help="FP16-brick leg: instances checked on the FP64 grid")
+    ap.add_argument("--c3-assemblies", type=int, default=256,
+                    help="uneven multi-part leg: procedural assemblies (0: skip the leg)")
+    ap.add_argument("--c3-steps", type=int, default=300, help="uneven multi-part leg: BDF1 steps")
+    ap.add_argument("--c3-cpu-scenes", type=int, default=8, help="uneven multi-part leg: scenes stepped on the CPU")
+    ap.add_argument("--c3-cpu-steps", type=int, default=3, help="uneven multi-part leg: CPU steps per scene")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank = dist_setup()

@@ -52,6 +52,13 @@ extern "C" {
  * where the SDF changes sign, so the values near the surface keep FP16's relative
  * precision). */
 #define SDFC_STORAGE_F16_BRICKS 2
+/* Grid values as FP32 node values alone: 4 bytes per node, where SDFC_STORAGE_F32 also keeps an
+ * FP64 copy and a per-cell array of the 8 FP32 corners (40 bytes per node in all, which speeds
+ * detection on grids that many instances share).  Every evaluation sees the same values as
+ * with SDFC_STORAGE_F32 (the FP32 values, widened where FP64 is read), so results are
+ * identical; this storage is for batches of many distinct large grids (256^3 grids of hundreds
+ * of parts), whose 40-byte layout would not fit in device memory. */
+#define SDFC_STORAGE_F32_NODES 3
 
 /* How the SDF gradient and Hessian of an active contact are evaluated.
  * The reference takes central differences of the trilinear interpolant with
@@ -111,6 +118,17 @@ int sdfc_set_precision(sdfc_context* ctx, int precision);
  * Writes a handle to *grid. */
 int sdfc_upload_grid(sdfc_context* ctx, const double* values, int ni, int nj, int nk, const double min_box[3],
                      const double max_box[3], const double dxyz[3], double col_th, int storage, int* grid);
+
+/* sdfc_upload_grid for node values already on the device: d_values holds ni*nj*nk FP32 values
+ * (i fastest) in device memory of the context's device, e.g. a grid generated on the GPU.  storage
+ * is SDFC_STORAGE_F32 or SDFC_STORAGE_F32_NODES.  The values are copied (the caller keeps its
+ * array); the grid's bounds and cell-corner array are computed on the device.  The call reads
+ * the values on the context's own stream, which does not wait for work on other streams: the
+ * values must be complete when it is made.  It returns once the grid is ready.  Non-finite
+ * values are rejected as by sdfc_upload_grid.  Same counterpart in the reference (BodySDFObj::_SDF). */
+int sdfc_upload_grid_device(sdfc_context* ctx, const float* d_values, int ni, int nj, int nk,
+                            const double min_box[3], const double max_box[3], const double dxyz[3], double col_th,
+                            int storage, int* grid);
 
 /* The grid as the evaluations see it (host, ni*nj*nk doubles, i fastest): the FP64
  * values, the FP32 values widened, or the decoded FP16 bricks. */
@@ -214,6 +232,41 @@ int sdfc_batch_evaluate_masked_device(sdfc_batch* batch, const double* E_A, cons
 int sdfc_batch_set_timing(sdfc_batch* batch, int enable);
 int sdfc_batch_last_timing(sdfc_batch* batch, float* ms);
 
+/* ---------------------------------------------------------------- launch tuning */
+
+/* How a batch's force pass is launched.  No counterpart in the reference (its only
+ * parallelism knob is the process count of utils/parallel.py:10).
+ *   slots          partial sums per instance: each instance's active contacts are split into
+ *                  `slots` interleaved shares, each summed on its own and the shares summed in
+ *                  order at the end (1..32, a power of two);
+ *   force_variant  SDFC_FORCE_CTAS: one CTA of 128 threads per (instance, slot);
+ *                  SDFC_FORCE_WORKERS: persistent one-warp CTAs, as many as the multiprocessors
+ *                  hold, taking (instance, slot) items from a queue;
+ *   worker_ctas    one-warp CTAs launched by SDFC_FORCE_WORKERS (0: multiprocessors x resident);
+ *   ms             measured time of one evaluation with this configuration (0 if not measured).
+ * Every configuration sums each share in a fixed order, so results are reproducible run to run
+ * for a given configuration; different configurations group the sums differently and may
+ * differ in the last bits. */
+#define SDFC_FORCE_CTAS 0
+#define SDFC_FORCE_WORKERS 1
+typedef struct {
+    int slots, force_variant, worker_ctas;
+    float ms;
+} sdfc_tuning;
+
+/* Times the candidate configurations (force_variant x slots) on one evaluation of these DEVICE
+ * inputs (as sdfc_batch_evaluate_device; want_deriv as there), keeps the fastest for the batch
+ * and for later batches of the same shape in this context (instances, tiles, points, grid
+ * storages, precision, derivative mode), and writes it to *chosen (may be NULL).  A batch whose
+ * shape was tuned before takes that tuning without timing.  The outputs are overwritten.  Not
+ * during a stream capture (it synchronises and may reallocate the batch's scratch). */
+int sdfc_batch_autotune(sdfc_batch* batch, const double* E_A, const double* phi_A, const double* E_B,
+                        const double* phi_B, const double* params, int want_deriv, double* fm, double* Km,
+                        double* Dm, int* n_active, int* status, void* stream, sdfc_tuning* chosen);
+/* The batch's launch configuration (set by sdfc_batch_autotune, or the default one). */
+int sdfc_batch_get_tuning(sdfc_batch* batch, sdfc_tuning* tuning);
+int sdfc_batch_set_tuning(sdfc_batch* batch, const sdfc_tuning* tuning);
+
 /* Number of points the last evaluations of this batch re-checked in FP64
  * because their FP32 distance fell inside the guard band (diagnostic; the
  * counter accumulates until reset with reset != 0). */
@@ -276,6 +329,17 @@ int sdfc_sim_step(sdfc_sim* sim, int num_steps, int* converged);
 /* Totals since creation: Newton rounds (batched force evaluations) and scene
  * force evaluations (diagnostic). */
 int sdfc_sim_stats(sdfc_sim* sim, long long* rounds, long long* evaluations);
+/* sdfc_batch_autotune for the sim's batch of contact pairs, on the evaluation that opens the
+ * next step at the current state (every scene's pairs with derivatives).  Call between steps;
+ * the sim's captured rounds are rebuilt with the chosen configuration. */
+int sdfc_sim_autotune(sdfc_sim* sim, sdfc_tuning* chosen);
+/* The sim's launch configuration: read, or set directly (as sdfc_batch_set_tuning). */
+int sdfc_sim_get_tuning(sdfc_sim* sim, sdfc_tuning* tuning);
+int sdfc_sim_set_tuning(sdfc_sim* sim, const sdfc_tuning* tuning);
+/* Force evaluations of each scene since creation (host, n): a scene's evaluation evaluates
+ * every contact pair of the scene once (diagnostic, e.g. contact points per second of scenes
+ * with uneven point counts). */
+int sdfc_sim_scene_evaluations(sdfc_sim* sim, long long* evaluations);
 
 /* Adjoint of the rollout (Simulation::reset(backward_flag = true) + Simulation::backward,
  * simulation/redmax/Simulation.cpp:1512-1634, integrator BDF1).
@@ -331,7 +395,10 @@ int sdfc_sim_set_tolerance(sdfc_sim* sim, double tol);
  *
  * Its working memory is a file-scope device array of about 2.6 MB that every
  * GPU loading the library holds until exit; n may not exceed
- * SDFC_NOALLOC_MAX_POINTS (larger n returns SDFC_ERR_CAPACITY).  The first
+ * SDFC_NOALLOC_MAX_POINTS (larger n returns SDFC_ERR_CAPACITY, negative n
+ * SDFC_ERR_INVALID_ARGUMENT).  A CUDA error already pending on the calling
+ * thread when the call starts is left there and the call returns
+ * SDFC_ERR_CUDA without launching anything.  The first
  * call on a device looks up that array's device address; make that first call
  * before any stream capture begins.  All calls share the array: calls whose
  * work may overlap on the GPU (other streams, other host threads) race and

@@ -17,28 +17,73 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_ref", "libredmax_ref.so")
-REFERENCE_ROOT = os.environ.get("SDFC_REFERENCE_ROOT", "/root/reference")
+PLUGIN_LIB_PATH = os.path.join(_HERE, "_ref", "libredmax_gpu_plugin.so")
+# The reference project's root: SDFC_REFERENCE_ROOT, else the copy of its sources that
+# `make -C oracle/ref stage` puts under baseline/_ref/src (git-ignored); None where neither exists.
+_STAGED = os.path.join(os.path.dirname(_HERE), "baseline", "_ref", "src")
+
+
+def reference_root():
+    for root in (os.environ.get("SDFC_REFERENCE_ROOT"), _STAGED):
+        if root and os.path.isdir(os.path.join(root, "simulation", "redmax")):
+            return root
+    return None
 
 
 def available() -> bool:
     return os.path.exists(LIB_PATH)
 
 
-def build(jobs: int = 8) -> bool:
+def build(jobs: int = None) -> bool:
     """Compile the reference + harness if the reference sources are present."""
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "simulation", "redmax")):
+    root = reference_root()
+    if root is None:
         return False
-    subprocess.check_call(["make", "-s", "-C", os.path.join(_HERE, "ref"), f"REF={REFERENCE_ROOT}", f"-j{jobs}"])
+    jobs = jobs or max(1, min(16, os.cpu_count() or 1))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(_HERE, "ref"), f"REF={root}", f"-j{jobs}"])
     return available()
+
+
+def build_plugin(jobs: int = None) -> bool:
+    """Compile the reference objects with the GPU Force plugin and its swap hook
+    (oracle/_ref/libredmax_gpu_plugin.so; libsdfcontact must be built)."""
+    root = reference_root()
+    if root is None:
+        return False
+    jobs = jobs or max(1, min(16, os.cpu_count() or 1))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(_HERE, "ref"), f"REF={root}", f"-j{jobs}",
+                           "plugin-check"])
+    return os.path.exists(PLUGIN_LIB_PATH)
 
 
 _lib = None
 
 
+def use_plugin_library():
+    """Makes this module drive libredmax_gpu_plugin.so (the reference objects, the harness and the
+    GPU plugin in one library) instead of libredmax_ref.so; the two are never loaded together.
+    Afterwards RefSim.use_gpu_contacts is available."""
+    global _lib
+    if _lib is not None and getattr(_lib, "_path", None) == PLUGIN_LIB_PATH:
+        return _lib
+    if _lib is not None:
+        raise RuntimeError("the reference library is already loaded in this process")
+    L = _declare(ctypes.CDLL(PLUGIN_LIB_PATH))
+    L.ref_sim_use_gpu_contacts.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L._path = PLUGIN_LIB_PATH
+    _lib = L
+    return L
+
+
 def lib():
     global _lib
     if _lib is None:
-        L = ctypes.CDLL(LIB_PATH)
+        _lib = _declare(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+def _declare(L):
+    if True:
         d, i, c = ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_char_p
         v = ctypes.c_void_p
         L.ref_sim_create.restype = v
@@ -78,8 +123,7 @@ def lib():
         f = ctypes.POINTER(ctypes.c_float)
         L.ref_make_level_set3.argtypes = [f, i, ctypes.POINTER(ctypes.c_uint), i, f, ctypes.c_float,
                                           ctypes.c_float, ctypes.c_float, i, i, i, i, f]
-        _lib = L
-    return _lib
+    return L
 
 
 def _dp(a):
@@ -277,6 +321,14 @@ class RefSim:
         q, qd = np.zeros(self.ndof_r), np.zeros(self.ndof_r)
         _check(lib().ref_sim_get_state(self._h, _dp(q), _dp(qd)), "get_state")
         return q, qd
+
+    def use_gpu_contacts(self, deriv_mode=0):
+        """Puts ForceGeneralSDFContactGPU in place of every ForceGeneralSDFContact of this
+        simulation (use_plugin_library first); returns how many were replaced."""
+        n = lib().ref_sim_use_gpu_contacts(self._h, int(deriv_mode))
+        if n < 0:
+            raise RuntimeError("reference harness: use_gpu_contacts failed")
+        return n
 
     def backward(self, df_dq, T):
         g0, gd0 = np.zeros(self.ndof_r), np.zeros(self.ndof_r)

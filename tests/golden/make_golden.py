@@ -15,7 +15,7 @@ and stores inputs and outputs as compressed .npz files:
                   reference's joint trajectory and Newton convergence flags
 
 Usage (where the reference sources are present):
-    make -C oracle/ref -j8 && python tests/golden/make_golden.py
+    make -C oracle/ref REF=<reference root> -j8 && python tests/golden/make_golden.py
 """
 import importlib
 import os
@@ -63,7 +63,7 @@ def cases(rng):
 
 def main():
     if not refsim.available():
-        raise SystemExit("oracle/_ref/libredmax_ref.so missing: build it with make -C oracle/ref")
+        raise SystemExit("oracle/_ref/libredmax_ref.so missing: build it with make -C oracle/ref REF=<reference root>")
     rng = np.random.default_rng(20261203)
     grid = W.socket_grid(GRID_N, dtype=np.float32)
     pts = W.peg_points(N_POINTS, seed=7)

@@ -10,7 +10,7 @@ oracle/ref/Makefile (oracle/_ref/libredmax_ref.so), on procedural meshes:
                  dx and res, and the reference's grid (shape, min_box, max_box, spacing, values)
 
 Usage (where the reference sources are present):
-    make -C oracle/ref -j8 && python tests/golden/make_levelset_golden.py
+    make -C oracle/ref REF=<reference root> -j8 && python tests/golden/make_levelset_golden.py
 """
 import importlib
 import os
@@ -58,7 +58,7 @@ def cases():
 
 def main():
     if not refsim.available():
-        raise SystemExit("oracle/_ref/libredmax_ref.so missing: build it with make -C oracle/ref")
+        raise SystemExit("oracle/_ref/libredmax_ref.so missing: build it with make -C oracle/ref REF=<reference root>")
     blob = {}
     names = []
     for name, V, F, o, d, shape, band in cases():

@@ -13,7 +13,7 @@ sources by oracle/ref/Makefile):
               124-135) as bytes, and the grid the reference reads back from it (load_SDF)
 
 Usage (where the reference sources are present):
-    make -C oracle/ref -j8 && python tests/golden/make_mesh_distance_golden.py
+    make -C oracle/ref REF=<reference root> -j8 && python tests/golden/make_mesh_distance_golden.py
 """
 import importlib
 import os
@@ -33,7 +33,7 @@ W = importlib.import_module("assemble-them-all_gb300.workloads")
 
 def main():
     if not refsim.available():
-        raise SystemExit("oracle/_ref/libredmax_ref.so missing: build it with make -C oracle/ref")
+        raise SystemExit("oracle/_ref/libredmax_ref.so missing: build it with make -C oracle/ref REF=<reference root>")
     rng = np.random.default_rng(20261204)
     blob = {}
 
