@@ -55,6 +55,7 @@ void free_batch(sdfc_batch* b) {
     cudaFree(b->d_pair64);
     cudaFree(b->d_recheck_list);
     cudaFree(b->d_recheck_n);
+    cudaFree(b->d_badin);
     cudaFree(b->d_partial);
     cudaFree(b->d_recheck);
     cudaFree(b->d_point_offset);
@@ -83,6 +84,7 @@ sdfc::BatchScratch scratch_of(const sdfc_batch* b) {
     sc.force_variant = b->force_variant;
     sc.worker_ctas = b->worker_ctas;
     sc.max_ntiles = b->max_ntiles;
+    sc.badin = b->d_badin;
     return sc;
 }
 
@@ -243,6 +245,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_pair64, sizeof(sdfc::PairState<double>) * n)) ||
         (rc = alloc((void**)&b->d_recheck_list, sizeof(int) * std::max(tiles, 1))) ||
         (rc = alloc((void**)&b->d_recheck_n, 5 * sizeof(int))) ||
+        (rc = alloc((void**)&b->d_badin, sizeof(int) * (size_t)n)) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * b->slots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||

@@ -59,7 +59,8 @@ struct sdfc_batch {
     sdfc::PairState<float>* d_pair32 = nullptr;
     sdfc::PairState<double>* d_pair64 = nullptr;
     int* d_recheck_list = nullptr;  // total_tiles
-    int* d_recheck_n = nullptr;     // 1
+    int* d_recheck_n = nullptr;     // 5 counters (BatchScratch::recheck_n)
+    int* d_badin = nullptr;         // n: non-finite inputs (BatchScratch::badin)
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
     long long* d_point_offset = nullptr;  // n: first output row of each instance's per-point distances

@@ -51,7 +51,8 @@ __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pos
 __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchInputs in,
                             const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
                             Prefilter* __restrict__ pref, PairState<float>* __restrict__ pair32,
-                            PairState<double>* __restrict__ pair64, int* __restrict__ recheck_n) {
+                            PairState<double>* __restrict__ pair64, int* __restrict__ recheck_n,
+                            int* __restrict__ badin) {
     // blockIdx.y: 0 the prefilter, 1 / 2 the FP32 / FP64 pair state every force or energy CTA of
     // the instance starts from (once per instance here, spread over three warps per 32 instances:
     // all three are FP64 arithmetic)
@@ -62,6 +63,14 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
     if (i >= n || (in.mode && in.mode[i] == 0)) return;
     const size_t o = (size_t)i;
     if (blockIdx.y == 0) {
+        // an instance whose poses, twists or coefficients are not all finite is flagged (its
+        // points then classify as outside the grid, as the reference's distance query has them)
+        bool finite = true;
+        const double* rows[5] = {in.EA + 16 * o, in.phiA + 6 * o, in.EB + 16 * o, in.phiB + 6 * o, in.prm + 6 * o};
+        const int widths[5] = {16, 6, 16, 6, 6};
+        for (int r = 0; r < 5; ++r)
+            for (int c = 0; c < widths[r]; ++c) finite = finite && isfinite(rows[r][c]);
+        badin[i] = finite ? 0 : 1;
         const InstanceDesc I = inst[i];
         Prefilter f;
         make_prefilter(grids[I.grid], points[I.points], load_pose(in.EA + 16 * o), load_pose(in.EB + 16 * o), f);
@@ -912,7 +921,7 @@ template <bool DERIV>
 __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
                                 const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode,
                                 const double* __restrict__ EA, const double* __restrict__ EB, int slots,
-                                bool set_status) {
+                                bool set_status, const int* __restrict__ badin) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     __shared__ double tot[NV];
     __shared__ double ad[36];  // Ad(E_A^{-1} E_B), ad[6 c + r] = entry (r, c)
@@ -950,10 +959,12 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
     // plain stores only (the outputs may be the caller's host memory)
     const int bad = __syncthreads_or(k < NV && !isfinite(v));
     if (k == 0) {
+        // bit 0: a non-finite output; bit 1: a non-finite input (prep_kernel)
+        const int st = (bad ? 1 : 0) | (badin[i] ? 2 : 0);
         if (set_status)  // every instance passes through this launch: status written outright
-            out.status[i] = bad ? 1 : 0;
-        else if (bad)
-            out.status[i] = 1;
+            out.status[i] = st;
+        else if (st)
+            out.status[i] = st;
         const InstanceDesc I = inst[i];
         int n = 0;
         for (int t = 0; t < I.ntiles; ++t) n += tile_count[I.tile0 + t];
@@ -1048,7 +1059,7 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
                    bool plain, bool bricks) {
     if (n_inst <= 0) return;
     prep_kernel<<<dim3((n_inst + 31) / 32, 3), 32, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter,
-                                                                s.pair32, s.pair64, s.recheck_n);
+                                                                s.pair32, s.pair64, s.recheck_n, s.badin);
     if (total_tiles <= 0) return;
     if (plain)
         detect_kernel<false><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
@@ -1117,10 +1128,10 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
     const double* EB = derive_q2 ? derive_q2->EB : nullptr;
     if (deriv)
         finalize_kernel<true><<<n_inst, 320, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA, EB,
-                                                          s.slots, set_status);
+                                                          s.slots, set_status, s.badin);
     else
         finalize_kernel<false><<<n_inst, 64, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
-                                                          nullptr, nullptr, s.slots, set_status);
+                                                          nullptr, nullptr, s.slots, set_status, s.badin);
 }
 
 void launch_zero_status(BatchOutputs out, int n_inst, cudaStream_t stream) {

@@ -129,7 +129,7 @@ struct BatchOutputs {
     double* Km;      // n x 144 (may be null for value-only evaluations)
     double* Dm;      // n x 144
     int* n_active;   // n
-    int* status;     // n: bit 0 = non-finite output
+    int* status;     // n: bit 0 = non-finite output, bit 1 = non-finite input
     // not null: the kernels take the five pointers from this device copy instead, which the
     // host rewrites per call (a captured graph then writes wherever the call asks, e.g. into
     // the caller's own host arrays where the device reads pageable memory)
@@ -165,6 +165,7 @@ struct BatchScratch {
     // force workers (force_worker_kernel): derivative pass on cell-corner grids, on other grids,
     // value pass on cell-corner grids, on other grids
     int* recheck_n;
+    int* badin = nullptr;            // n: 1 where the instance's inputs are not all finite (prep_kernel)
     int force_variant = kForceCtas;  // which force kernel runs (set by the batch's tuning)
     int worker_ctas = 0;             // force workers launched (0: the device's multiprocessors x resident)
     int max_ntiles = 0;              // most detection tiles of one instance (the workers' shared prefix)

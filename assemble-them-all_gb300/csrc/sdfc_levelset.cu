@@ -416,12 +416,13 @@ constexpr long kLsSpinFast = 1L << 12;
 // s - 1, on its diagonals up to M + P - 1, so the slab starts diagonal M once progress[s - 1]
 // (slab s - 1's finished diagonals) reaches M + P.  Every node therefore reads what the
 // reference's loop (c, b, a ascending) would have shown it.  Needs all CTAs resident
-// (cooperative launch); every wait is bounded: on timeout the CTA sets *err and returns, and
-// the others see *err and return.
+// (cooperative launch); every wait is bounded: after spin_limit polls the CTA sets *err and
+// returns, and the others see *err and return.  need_extra (0 in use) is added to every awaited
+// progress value: a test sets it beyond any slab's diagonals so that every wait runs out.
 __global__ void __launch_bounds__(kLsSweepThreads, 1) ls_sweep_slabs_kernel(const float4* __restrict__ soup,
                                                                        LsGrid g, float* phi, int* closest, int di,
                                                                        int dj, int dk, int P, int* progress,
-                                                                       int* err) {
+                                                                       int* err, long spin_limit, int need_extra) {
     __shared__ int s_seen;
     const int A = g.ni - 2, B = g.nj - 2, planes = g.nk - 1;
     const int s = blockIdx.x;
@@ -433,7 +434,7 @@ __global__ void __launch_bounds__(kLsSweepThreads, 1) ls_sweep_slabs_kernel(cons
     const bool signal = c0 + np < planes;
     int seen = s == 0 ? INT_MAX : 0;
     for (int M = 0; M < steps; ++M) {
-        const int need = min(M + P, prev_steps);
+        const int need = min(M + P, prev_steps) + need_extra;
         if (seen < need) {  // uniform over the CTA
             if (threadIdx.x == 0) {
                 int v;
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(kLsSweepThreads, 1) ls_sweep_slabs_kernel(cons
                         v = -1;
                         break;
                     }
-                    if (++it > kLsSpinLimit) {
+                    if (++it > spin_limit) {
                         atomicExch(err, 1);
                         v = -1;
                         break;
@@ -613,12 +614,21 @@ int ls_run(sdfc_context* ctx, const float* d_verts, const unsigned* d_tris, int 
         float* a_phi = d_phi;
         int* a_closest = d_closest;
         int aP = P;
+        // SDFC_TEST_EXPIRE_SWEEP_WAITS (tests of the failure path only): every wait awaits a
+        // progress no slab reaches and gives up after a short spin, so the call must report it
+        long spin_limit = kLsSpinLimit;
+        int need_extra = 0;
+        if (std::getenv("SDFC_TEST_EXPIRE_SWEEP_WAITS")) {
+            spin_limit = 1000;
+            need_extra = 1 << 30;
+        }
         for (int pass = 0; pass < 2; ++pass)
             for (int s = 0; s < 8; ++s) {
                 int di = dirs[s][0], dj = dirs[s][1], dk = dirs[s][2];
                 LS_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * planes, st));
-                void* args[] = {(void*)&d_soup, (void*)&gg, (void*)&a_phi, (void*)&a_closest, (void*)&di,
-                                (void*)&dj, (void*)&dk, (void*)&aP, (void*)&d_progress, (void*)&d_err};
+                void* args[] = {(void*)&d_soup, (void*)&gg, (void*)&a_phi,  (void*)&a_closest,
+                                (void*)&di,     (void*)&dj, (void*)&dk,     (void*)&aP,
+                                (void*)&d_progress, (void*)&d_err, (void*)&spin_limit, (void*)&need_extra};
                 LS_TRY(cudaLaunchCooperativeKernel((const void*)ls_sweep_slabs_kernel, dim3(slabs),
                                                    dim3(kLsSweepThreads), args, 0, st));
             }

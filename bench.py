@@ -83,6 +83,13 @@ def _cpu_eval(args):
     return time.perf_counter() - t
 
 
+def _cpu_norm_sum(args):
+    """Sum of |fm_i| over one instance's active contacts (the error scale of fm where the contacts'
+    forces cancel), by the oracle."""
+    EA, phiA, EB, phiB = args
+    return _G["O"].pair_force_norm_sum(_G["grid"], _G["pts"], EA, phiA, EB, phiB, _G["prm"])
+
+
 def _cpu_sim(args):
     """One scene of the direction sweep stepped by the oracle's BDF1 restatement."""
     d, steps = args
@@ -134,11 +141,37 @@ def dist_max(x, world):
     return float(t.item())
 
 
+def dist_sum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def whole_job_rate(units_per_rank, seconds, world):
     """Weak-scaling aggregate: every replica processes `units_per_rank` units; the job's time is
     the slowest replica's.  Returns (units per second over all replicas, the max-over-ranks time)."""
     s = dist_max(seconds, world)
     return world * units_per_rank / s, s
+
+
+def gather_rows(x, world):
+    """Per-instance results of every rank, in rank order, on every rank (a host-side gather of
+    the replicas' results; no device collective)."""
+    if world == 1:
+        return np.asarray(x)
+    import torch.distributed as dist
+    out = [None] * world
+    dist.all_gather_object(out, np.asarray(x))
+    return np.concatenate(out)
+
+
+def rank_block(total, n, rank, world):
+    """Replica `rank`'s block of n items of a workload of n * world items (`total` gives them all)."""
+    return total[rank * n:(rank + 1) * n]
 
 
 def dist_barrier(world):
@@ -408,26 +441,54 @@ def run_gpu(args, world, rank):
         det_ms, frc_ms, red_ms = (float(np.mean([x[i] for x in phases])) for i in range(3))
         rechecked = batch.recheck_count(reset=True) / (args.warmup + args.steps + len(phases))
 
-    # plain per-instance FP64 GPU path on the same inputs: one FP64 evaluation per instance
+    # the plain per-instance FP64 GPU path on the same inputs: a one-instance FP64 batch evaluated
+    # once per instance on device arrays, the instances' launches back to back on the stream (no
+    # host round trip per instance), CUDA events around the run
     plain = ctx.batch([p], [g])
     plain.set_precision(sdfc.PRECISION_FP64)
-    params_c = [sdfc.Params(*PARAMS)] * n
     params_rows = np.tile(np.array(PARAMS, dtype=np.float64), (n, 1))  # sdfc_params rows, as a C caller holds them
-    ref = [np.zeros((n, 12)), np.zeros((n, 12, 12)), np.zeros((n, 12, 12))]
-    sample = min(n, args.plain_sample)
-    plain_t = []
-    for k in range(n):
-        t = time.perf_counter()
-        f_, K_, D_, _, _ = plain.evaluate(EA[k:k + 1], phiA[k:k + 1], EB[k:k + 1], phiB[k:k + 1], params_c[:1])
-        if k < sample:
-            plain_t.append(time.perf_counter() - t)
-        ref[0][k], ref[1][k], ref[2][k] = f_[0], K_[0], D_[0]
-        if k + 1 >= sample and not args.full_error:
-            break
-    m = n if args.full_error else sample
-    err = {"fm": rel_err(out_fast[0][:m], ref[0][:m]), "Km": rel_err(out_fast[1][:m], ref[1][:m]),
-           "Dm": rel_err(out_fast[2][:m], ref[2][:m]), "instances": m}
-    plain_rate = args.points / float(np.mean(plain_t[1:] if len(plain_t) > 1 else plain_t))
+    m = n if args.full_error else min(n, args.plain_sample)
+    pfm = torch.zeros(n, 12, dtype=torch.float64, device="cuda")
+    pKm = torch.zeros(n, 144, dtype=torch.float64, device="cuda")
+    pDm = torch.zeros(n, 144, dtype=torch.float64, device="cuda")
+    off = lambda t, k, w: t.data_ptr() + 8 * w * k  # noqa: E731  (row k of an FP64 tensor of width w)
+    ioff = lambda t, k: t.data_ptr() + 4 * k  # noqa: E731
+
+    def plain_eval(k):
+        plain.evaluate_device(off(dEA, k, 16), off(dphiA, k, 6), off(dEB, k, 16), off(dphiB, k, 6), off(dprm, k, 6),
+                              off(pfm, k, 12), off(pKm, k, 144), off(pDm, k, 144), ioff(nact, k), ioff(st, k),
+                              want_deriv=True, stream=stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for k in range(3):  # warm-up
+            plain_eval(k)
+        flush.zero_()
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pa.record(stream)
+        for k in range(m):
+            plain_eval(k)
+        pb.record(stream)
+        stream.synchronize()
+    plain_rate = m * args.points / (pa.elapsed_time(pb) / 1e3)
+    ref = (pfm.cpu().numpy()[:m], pKm.cpu().numpy().reshape(n, 12, 12)[:m], pDm.cpu().numpy().reshape(n, 12, 12)[:m])
+    err = {"fm": rel_err(out_fast[0][:m], ref[0]), "Km": rel_err(out_fast[1][:m], ref[1]),
+           "Dm": rel_err(out_fast[2][:m], ref[2]), "instances": m}
+
+    # the batched path with FP64 per-contact algebra on the same batch (same launches, FP64 kernels)
+    batch.set_precision(sdfc.PRECISION_FP64)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            step()
+        f64_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(max(3, args.steps // 2))]
+        for a, b in f64_ev:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+        stream.synchronize()
+    f64_ms = float(np.mean([a.elapsed_time(b) for a, b in f64_ev]))
+    batch.set_precision(sdfc.PRECISION_MIXED if args.precision == "mixed" else sdfc.PRECISION_FP64)
 
     # e2e through the C ABI with host buffers (H2D of the instance states, D2H of fm/Km/Dm into
     # result arrays the caller keeps across calls, as a simulator's force assembly does)
@@ -445,15 +506,18 @@ def run_gpu(args, world, rank):
     h2d = n * 50 * 8
     d2h = n * (300 * 8 + 2 * 4)
 
-    sim_res = run_sim(args, sdfc, ctx, g, p, n) if args.sim_steps > 0 and rank == 0 else None
+    # the simulation, rollout and multi-part legs shard their scenes over the replicas too; the
+    # single-GPU studies (FP16 bricks, SDF construction, planner queries) run on rank 0
+    sim_res = run_sim(args, sdfc, ctx, g, p, n, world, rank) if args.sim_steps > 0 else None
     c5_res = run_c5(args, sdfc, ctx, torch) if args.c5_points > 0 and rank == 0 else None
-    c4_res = run_c4(args, sdfc, ctx, g, torch) if args.c4_instances > 0 and rank == 0 else None
+    c4_res = run_c4(args, sdfc, ctx, g, torch, world, rank) if args.c4_instances > 0 else None
     ls_res = run_levelset(args, sdfc, ctx, torch) if args.ls_segments > 0 and rank == 0 else None
     pl_res = run_planner(args, sdfc, ctx, torch) if args.planner_states > 0 and rank == 0 else None
-    c3_res = run_c3(args, sdfc, ctx, torch) if args.c3_assemblies > 0 and rank == 0 else None
-    if sim_res is not None:
+    c3_res = run_c3(args, sdfc, ctx, torch, world, rank) if args.c3_assemblies > 0 else None
+    if sim_res is not None and rank == 0:
         plain = run_sim_plain(args, sdfc, ctx, g, p, n)
-        plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / plain["scene_steps_per_s"]
+        # per GPU: the batched rate of one replica against the per-instance path on one GPU
+        plain["speedup_of_batched"] = sim_res["first_steps"]["scene_steps_per_s"] / world / plain["scene_steps_per_s"]
         sim_res["plain_fp64_per_instance"] = plain
 
     if rank != 0:
@@ -478,7 +542,8 @@ def run_gpu(args, world, rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 depth/sums, f32 per-contact algebra" if args.precision == "mixed" else "f64",
+        "dtype": ("f32 per-contact algebra and 32-contact warp sums; f64 depth; warp totals TwoSum-compensated "
+                  "f32 within a force CTA, f64 across CTAs") if args.precision == "mixed" else "f64",
         "data": "synthetic",
         "config": workload_config(args),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -495,8 +560,13 @@ def run_gpu(args, world, rank):
                                 "note": "points and grid are shared by all instances, so these bytes are L2 reads; "
                                         "DRAM traffic per step is ~35 MB (profiles/)"},
         "phases_ms": {"detect": det_ms, "force": frc_ms, "reduce": red_ms},
-        "plain_fp64_per_instance": {"value": plain_rate, "unit": UNIT, "instances_timed": len(plain_t),
+        "plain_fp64_per_instance": {"value": plain_rate, "unit": UNIT, "instances_timed": m,
+                                    "how": "one-instance FP64 batch per instance, device arrays, launches back to "
+                                           "back on one stream, CUDA events",
                                     "speedup_of_batched": value / plain_rate},
+        "batched_fp64": {"value": n * args.points / (f64_ms / 1e3), "unit": UNIT, "ms_per_step": f64_ms,
+                         "how": "the same batch and launch configuration with FP64 per-contact algebra",
+                         "speedup_of_mixed": f64_ms / step_ms},
         "error_vs_fp64_path": err,
         "tuning": {"chosen": tuning_used, "autotuned": tuning is not None,
                    "candidates": "force pass as CTAs per (instance, slot) or persistent one-warp workers, "
@@ -514,6 +584,12 @@ def run_gpu(args, world, rank):
         ct = cpu_time(pool, states, rng.choice(n, sample, replace=False))
         line["cpu_baseline"] = {"value": sample * args.points / ct, "unit": UNIT, "cores": procs, "kind": "port",
                                 "sample": f"{sample} of {n} instances, derivative evaluation, one process per core"}
+        # the error of fm relative to the sum of the contacts' own force norms (where radial forces
+        # cancel, |fm| understates the scale of the sum)
+        m_err = err["instances"]
+        sums = np.array(pool.map(_cpu_norm_sum, [(EA[k], phiA[k], EB[k], phiB[k]) for k in range(m_err)]))
+        dev_fm = np.linalg.norm(out_fast[0][:m_err] - ref[0][:m_err], axis=1)
+        line["error_vs_fp64_path"]["fm_over_sum_of_contact_norms"] = float(np.max(dev_fm / sums))
         if sim_res is not None:
             line["cpu_baseline"]["sim"] = cpu_sim_rate(pool, args.cpu_sim_scenes, min(args.sim_early, 25), procs)
         pool.close()
@@ -532,10 +608,12 @@ def run_gpu(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_sim(args, sdfc, ctx, g, p, n):
+def run_sim(args, sdfc, ctx, g, p, n, world=1, rank=0):
     """The direction sweep stepped: n scenes (peg on a translational joint, fixed socket), each pulled along
-    its Fibonacci direction, args.sim_steps BDF1 steps through sdfc_sim_step (host state in and out)."""
-    dirs = W.fibonacci_directions(n)
+    its Fibonacci direction, args.sim_steps BDF1 steps through sdfc_sim_step (host state in and out).
+    With world replicas the sweep has n * world directions and replica rank steps its block; rates are
+    over all replicas' scenes and the slowest replica's time, and the final states are gathered."""
+    dirs = rank_block(W.fibonacci_directions(n * world), n, rank, world)
     m, inertia = W.cylinder_mass_props()
     mover = sdfc.Mover.make(m, inertia, np.eye(4), SIM_H, SIM_GRAVITY)
     prm = sdfc.Params(*PARAMS)
@@ -550,6 +628,7 @@ def run_sim(args, sdfc, ctx, g, p, n):
     sim.set_state(np.zeros((n, 3)), np.zeros((n, 3)))
     sim.record(args.sim_steps)  # the trajectory for the adjoint (one device copy per step)
     r0, e0 = sim.stats()
+    dist_barrier(world)
     t0 = time.perf_counter()
     early = min(args.sim_steps, args.sim_early)
     conv = sim.step(early)
@@ -564,20 +643,28 @@ def run_sim(args, sdfc, ctx, g, p, n):
     # dL/dq0, dL/dqdot0 and dL/d(pull force) of every scene
     w = np.zeros((n, args.sim_steps, 3))
     w[:, -1] = dirs
+    dist_barrier(world)
     t1 = time.perf_counter()
     g0, gd0, gf = sim.backward(w)
     t_bwd = time.perf_counter() - t1
     sim.close()
-    return {"scenes": n, "steps": args.sim_steps, "wall_s": wall,
-            "scene_steps_per_s": n * args.sim_steps / wall,
-            "contact_pts_per_s": (e2 - e0) * args.points / wall,
-            "rounds": r2 - r0, "scene_evaluations": e2 - e0,
-            "first_steps": {"steps": early, "wall_s": t_early, "scene_steps_per_s": n * early / t_early,
-                            "scene_evaluations": e1 - e0},
-            "converged_last_step": float(np.mean(conv)),
-            "final_z_mean": float(q[:, 2].mean()),
-            "adjoint": {"steps": args.sim_steps, "wall_s": t_bwd, "scene_steps_per_s": n * args.sim_steps / t_bwd,
-                        "finite": bool(np.isfinite(gf).all() and np.isfinite(g0).all())}}
+    rate, wall_job = whole_job_rate(n * args.sim_steps, wall, world)
+    early_rate, _ = whole_job_rate(n * early, t_early, world)
+    bwd_rate, t_bwd_job = whole_job_rate(n * args.sim_steps, t_bwd, world)
+    evals = int(dist_sum(e2 - e0, world))
+    q_all = gather_rows(q, world)  # every replica's final states, on every rank
+    conv_all = gather_rows(conv, world)
+    finite = bool(gather_rows([np.isfinite(gf).all() and np.isfinite(g0).all()], world).all())
+    return {"scenes": n * world, "steps": args.sim_steps, "wall_s": wall_job,
+            "scene_steps_per_s": rate,
+            "contact_pts_per_s": evals * args.points / wall_job,
+            "rounds": r2 - r0, "scene_evaluations": evals,
+            "first_steps": {"steps": early, "wall_s": t_early, "scene_steps_per_s": early_rate,
+                            "scene_evaluations": int(dist_sum(e1 - e0, world))},
+            "converged_last_step": float(np.mean(conv_all)),
+            "final_z_mean": float(q_all[:, 2].mean()),
+            "adjoint": {"steps": args.sim_steps, "wall_s": t_bwd_job, "scene_steps_per_s": bwd_rate,
+                        "finite": finite}}
 
 
 def run_sim_plain(args, sdfc, ctx, g, p, n_dirs, instances=4):
@@ -853,7 +940,7 @@ def run_planner(args, sdfc, ctx, torch):
                                                    "sample": f"{md} poses, LP feasibility (HiGHS)"}}}
 
 
-def run_c4(args, sdfc, ctx, g, torch):
+def run_c4(args, sdfc, ctx, g, torch, world=1, rank=0):
     """Differentiable rollout: args.c4_instances pegs on free3d-exp joints in the socket, initial
     pose perturbed (sigma 0.01 translation, sigma 1 degree rotation), pulled along directions in a
     30 degree cone about +z, args.c4_steps BDF1 steps.  Loss per instance: the steps' summed
@@ -865,14 +952,16 @@ def run_c4(args, sdfc, ctx, g, torch):
     rng = np.random.default_rng(4)
     pts = W.peg_points(args.c4_points, seed=9)
     ph = ctx.upload_points(pts, sdfc.STORAGE_F32)
-    dirs = W.cone_directions(n, 30.0, seed=4)
+    # with world replicas: n * world instances, replica rank takes its block
+    dirs = rank_block(W.cone_directions(n * world, 30.0, seed=4), n, rank, world)
     m, inertia = W.cylinder_mass_props()
     mv = sdfc.Mover.make(m, inertia, np.eye(4), SIM_H, SIM_GRAVITY, joint=sdfc.JOINT_FREE3D_EXP)
     sim = ctx.sim([mv] * n, [sdfc.ScenePair.make(i, ph, g, True, np.eye(4), sdfc.Params(*PARAMS)) for i in range(n)])
     sim.set_precision(sdfc.PRECISION_MIXED if args.c4_precision == "mixed" else sdfc.PRECISION_FP64)
-    q0 = np.zeros((n, 6))
-    q0[:, :3] = rng.normal(size=(n, 3)) * 0.01
-    q0[:, 3:] = rng.normal(size=(n, 3)) * np.deg2rad(1.0)
+    q0_all = np.zeros((n * world, 6))
+    q0_all[:, :3] = rng.normal(size=(n * world, 3)) * 0.01
+    q0_all[:, 3:] = rng.normal(size=(n * world, 3)) * np.deg2rad(1.0)
+    q0 = rank_block(q0_all, n, rank, world)
     F = np.zeros((n, 6))
     F[:, 3:] = SIM_PULL * dirs
     target = np.array([0.0, 0.0, 0.25, 0.0, 0.0, 0.0])
@@ -887,6 +976,7 @@ def run_c4(args, sdfc, ctx, g, torch):
     sim.set_state(q0, np.zeros((n, 6)))
     torch.cuda.synchronize()
     r0, e0 = sim.stats()
+    dist_barrier(world)
     t0 = time.perf_counter()
     conv = sim.step(T)
     qh = sim.history()
@@ -896,22 +986,96 @@ def run_c4(args, sdfc, ctx, g, torch):
     L = E + ((qh[:, T] - target) ** 2).sum(1)
     df_dq = np.zeros((n, T, 6))
     df_dq[:, T - 1] = 2.0 * (qh[:, T] - target)
+    dist_barrier(world)
     t1 = time.perf_counter()
     g0, gd0, gf = sim.backward(df_dq, np.ones(n))
     t_bwd = time.perf_counter() - t1
     r, e = sim.stats()
     sim.close()
+    check = None
+    if args.c4_check > 0 and rank == 0:
+        check = c4_gradient_check(sdfc, ctx, g, ph, mv, q0, dirs, T, target, g0, gf, args.c4_check)
+    fwd_rate, t_fwd_job = whole_job_rate(n * T, t_fwd, world)
+    bwd_rate, t_bwd_job = whole_job_rate(n * T, t_bwd, world)
+    # every replica's per-instance results, gathered
+    L, E, conv = gather_rows(L, world), gather_rows(E, world), gather_rows(conv, world)
+    g0, gf = gather_rows(g0, world), gather_rows(gf, world)
     g_dir = SIM_PULL * gf[:, 3:]  # F = pull * direction
-    return {"instances": n, "steps": T, "points": args.c4_points, "joint": "free3d-exp",
-            "precision": args.c4_precision, "rounds": r1 - r0, "scene_evaluations": e1 - e0,
+    out = {"instances": n * world, "steps": T, "points": args.c4_points, "joint": "free3d-exp",
+            "precision": args.c4_precision, "rounds": r1 - r0, "scene_evaluations": int(dist_sum(e1 - e0, world)),
             "converged_last_step": float(np.mean(conv)),
-            "forward_wall_s": t_fwd, "backward_wall_s": t_bwd,
-            "forward_scene_steps_per_s": n * T / t_fwd, "backward_scene_steps_per_s": n * T / t_bwd,
+            "forward_wall_s": t_fwd_job, "backward_wall_s": t_bwd_job,
+            "forward_scene_steps_per_s": fwd_rate, "backward_scene_steps_per_s": bwd_rate,
             "loss_mean": float(L.mean()), "penetration_energy_mean": float(E.mean()),
             "grad_q0_norm_mean": float(np.linalg.norm(g0, axis=1).mean()),
             "grad_direction_norm_mean": float(np.linalg.norm(g_dir, axis=1).mean()),
             "finite": bool(np.isfinite(g0).all() and np.isfinite(gf).all()),
             "checkpoint": "joint trajectory every step (48 B per scene-step); step matrices recomputed in reverse"}
+    if check is not None:
+        out["gradient_check"] = check
+    return out
+
+
+def c4_gradient_check(sdfc, ctx, g, ph, mv, q0, dirs, T, target, g0_mixed, gf_mixed, k):
+    """Adjoint gradients of k instances spread over the rollout against central differences
+    (step 1e-6) of rollouts with FP64 evaluations and Newton solved to |g| < 1e-13: dL/dq0 (6) and
+    dL/d(direction) on the tangent plane of the unit sphere at the direction (2).  The FP64
+    adjoint comes from the same tightly solved sim; the mixed one is the timed rollout's."""
+    n = len(q0)
+    idx = np.linspace(0, n - 1, k).astype(int)
+    eps = 1e-6
+    q0s, Fs, bases = [], [], []
+    for i in idx:
+        a = np.array([1.0, 0.0, 0.0]) if abs(dirs[i][0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        t1 = np.cross(dirs[i], a)
+        t1 /= np.linalg.norm(t1)
+        t2 = np.cross(dirs[i], t1)
+        bases.append((t1, t2))
+        var = [(q0[i], dirs[i])]
+        for j in range(6):
+            for sgn in (1.0, -1.0):
+                q = q0[i].copy()
+                q[j] += sgn * eps
+                var.append((q, dirs[i]))
+        for t in (t1, t2):
+            for sgn in (1.0, -1.0):
+                var.append((q0[i], dirs[i] + sgn * eps * t))
+        for q, d in var:
+            q0s.append(q)
+            Fs.append(np.concatenate([np.zeros(3), SIM_PULL * d]))
+    m = len(q0s)
+    sim = ctx.sim([mv] * m, [sdfc.ScenePair.make(j, ph, g, True, np.eye(4), sdfc.Params(*PARAMS)) for j in range(m)])
+    sim.set_precision(sdfc.PRECISION_FP64)
+    sim.set_tolerance(1e-13)
+    sim.record_energy(True)
+    sim.set_state(np.array(q0s), np.zeros((m, 6)))
+    sim.set_external_force(np.array(Fs))
+    sim.record(T)
+    t0 = time.perf_counter()
+    conv = sim.step(T)
+    qh = sim.history()
+    _, E = sim.energy()
+    L = E + ((qh[:, T] - target) ** 2).sum(1)
+    df_dq = np.zeros((m, T, 6))
+    df_dq[:, T - 1] = 2.0 * (qh[:, T] - target)
+    g0, _, gf = sim.backward(df_dq, np.ones(m))
+    wall = time.perf_counter() - t0
+    sim.close()
+    rel64, relmx = [], []
+    for s_, i in enumerate(idx):
+        r = L[17 * s_:17 * (s_ + 1)]
+        t1, t2 = bases[s_]
+        fd = np.concatenate([(r[1:13:2] - r[2:13:2]) / (2 * eps), (r[13::2] - r[14::2]) / (2 * eps)])
+        gd = SIM_PULL * gf[17 * s_, 3:]
+        a64 = np.concatenate([g0[17 * s_], [gd @ t1, gd @ t2]])
+        gm = SIM_PULL * gf_mixed[i, 3:]
+        amx = np.concatenate([g0_mixed[i], [gm @ t1, gm @ t2]])
+        rel64.append(float(np.linalg.norm(a64 - fd) / np.linalg.norm(fd)))
+        relmx.append(float(np.linalg.norm(amx - fd) / np.linalg.norm(fd)))
+    return {"instances": [int(i) for i in idx], "fd_step": eps, "newton_tol": 1e-13,
+            "rel_err_fp64_adjoint": rel64, "rel_err_mixed_adjoint": relmx,
+            "converged": bool(np.all(conv)), "scenes": m, "wall_s": wall,
+            "components": "dL/dq0 (6) and dL/d(direction) along two tangent directions (2)"}
 
 
 # --------------------------------------------------------------------------- uneven multi-part batch
@@ -939,7 +1103,7 @@ def _c3_cpu_scene(args):
     return time.perf_counter() - t, int(evs.sum())
 
 
-def run_c3(args, sdfc, ctx, torch):
+def run_c3(args, sdfc, ctx, torch, world=1, rank=0):
     """Uneven multi-part batch: args.c3_assemblies seeded procedural assemblies (2-12 parts, per
     part log-uniform 2k-200k contact points and a grid of 64^3, 128^3 or 256^3 FP32 nodes), one
     part of each pulled along a random axis for args.c3_steps BDF1 steps, all scenes in one
@@ -947,8 +1111,10 @@ def run_c3(args, sdfc, ctx, torch):
     Grids are sampled on the GPU and kept as FP32 node values (4 B per node)."""
     S = importlib.import_module(f"{PKG}.scenes")
     t0 = time.perf_counter()
-    asms = [W.procedural_assembly(s) for s in range(args.c3_assemblies)]
-    scenes = [S.AssemblyScene.make_device(ctx, a, s, col_th=C3_COL_TH) for s, a in enumerate(asms)]
+    # with world replicas: assemblies (seeds) rank * n .. (rank + 1) * n - 1
+    seeds = list(range(rank * args.c3_assemblies, (rank + 1) * args.c3_assemblies))
+    asms = [W.procedural_assembly(s) for s in seeds]
+    scenes = [S.AssemblyScene.make_device(ctx, a, s, col_th=C3_COL_TH) for s, a in zip(seeds, asms)]
     sim = S.build_sim(ctx, scenes, C3_H, C3_GRAVITY, sdfc.Params(*C3_PRM), col_th=C3_COL_TH,
                       storage=sdfc.STORAGE_F32_NODES)
     setup_s = time.perf_counter() - t0
@@ -964,22 +1130,29 @@ def run_c3(args, sdfc, ctx, torch):
     e0 = sim.scene_evaluations()
     r0, _ = sim.stats()
     torch.cuda.synchronize()
+    dist_barrier(world)
     t = time.perf_counter()
     conv = sim.step(args.c3_steps)
-    wall = time.perf_counter() - t
+    wall_rank = time.perf_counter() - t
     r1, _ = sim.stats()
     evals = sim.scene_evaluations() - e0
     q, _ = sim.get_state()
     # contact points one evaluation of a scene evaluates: its pairs' contact-body points
     pts_scene = np.array([sum(len(sc.points[a]) for a, _ in sc.contact_pairs()) for sc in scenes], dtype=np.int64)
+    _, wall = whole_job_rate(1, wall_rank, world)
+    # every replica's per-scene results, gathered
+    evals, pts_scene = gather_rows(evals, world), gather_rows(pts_scene, world)
+    q, conv = gather_rows(q, world), gather_rows(conv, world)
+    n = len(evals)
     cpe = int((evals * pts_scene).sum())
     disp = np.linalg.norm(q, axis=1)
-    parts = [len(a.parts) for a in asms]
-    grid_n = [g for a in asms for g in a.grid_n]
+    parts = gather_rows([len(a.parts) for a in asms], world).tolist()
+    grid_n = gather_rows([g for a in asms for g in a.grid_n], world).tolist()
+    npts = gather_rows([x for a in asms for x in a.n_points], world)
     out = {
         "assemblies": n, "parts": int(sum(parts)), "parts_per_assembly": [int(min(parts)), int(max(parts))],
-        "pairs": int(sum(2 * (k - 1) for k in parts)), "contact_points_total": int(sum(sum(a.n_points) for a in asms)),
-        "points_per_part": [int(min(min(a.n_points) for a in asms)), int(max(max(a.n_points) for a in asms))],
+        "pairs": int(sum(2 * (k - 1) for k in parts)), "contact_points_total": int(npts.sum()),
+        "points_per_part": [int(npts.min()), int(npts.max())],
         "grids": {f"{g}^3": int(sum(1 for x in grid_n if x == g)) for g in (64, 128, 256)},
         "grid_storage": "fp32 nodes", "grid_bytes": int(sum(4 * g ** 3 for g in grid_n)),
         "grid_bytes_cell_corner_layout": int(sum(40 * g ** 3 for g in grid_n)),
@@ -999,9 +1172,9 @@ def run_c3(args, sdfc, ctx, torch):
         "converged_last_step": float(np.mean(conv)),
         "displacement": {"escaped_over_1": int((disp > 1.0).sum()), "held_under_0.1": int((disp < 0.1).sum())},
     }
-    if args.c3_cpu_scenes > 0:
+    if args.c3_cpu_scenes > 0 and rank == 0:
         # the oracle on the first scenes, a few steps each, one process per scene
-        k = min(args.c3_cpu_scenes, n)
+        k = min(args.c3_cpu_scenes, len(scenes))
         jobs = []
         for sc in scenes[:k]:
             m = sc.asm.mover
@@ -1064,6 +1237,8 @@ def main():
     ap.add_argument("--c4-instances", type=int, default=4096, help="differentiable-rollout leg: instances (0: skip)")
     ap.add_argument("--c4-steps", type=int, default=200, help="differentiable-rollout leg: BDF1 steps")
     ap.add_argument("--c4-points", type=int, default=10000, help="differentiable-rollout leg: peg points")
+    ap.add_argument("--c4-check", type=int, default=8,
+                    help="differentiable-rollout leg: instances whose gradients are checked by central differences")
     ap.add_argument("--c4-precision", choices=("mixed", "fp64"), default="mixed",
                     help="differentiable-rollout leg: precision of the force evaluations")
     ap.add_argument("--planner-states", type=int, default=4096, help="planner-query leg: poses (0: skip the leg)")

@@ -183,8 +183,10 @@ int sdfc_batch_set_precision(sdfc_batch* batch, int precision);
 
 /* Evaluates every instance.  Arrays are per instance, row-major, HOST memory:
  * E_A, E_B [n*16]; phi_A, phi_B [n*6]; params [n]; fm [n*12]; Km, Dm [n*144]
- * (want_deriv only); n_active [n]; status [n] (bit 0: a non-finite output;
- * n_active and status may be null).  Host<->device transfers are part of the
+ * (want_deriv only); n_active [n]; status [n] (bit 0: a non-finite output; bit 1: a
+ * non-finite pose, twist or coefficient, whose instance then finds no contact, as the
+ * reference's distance query puts non-finite points outside the grid; n_active and status may
+ * be null).  Host<->device transfers are part of the
  * call, which returns when the results are in the caller's arrays.  Where the
  * device reads pageable host memory through the host's page tables (Grace's
  * C2C link) the kernels read the input arrays and write the result arrays

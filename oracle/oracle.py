@@ -186,6 +186,23 @@ def pair_eval(grid: Grid, pts, E_A, phi_A, E_B, phi_B, params: Params, want_deri
     return fm, Km.reshape(12, 12), Dm.reshape(12, 12), ids[:n].copy()
 
 
+def pair_force_norm_sum(grid: Grid, pts, E_A, phi_A, E_B, phi_B, params: Params) -> float:
+    """Sum over the active contacts of |fm_i|, each contact's own 12-vector term of fm
+    (rm/Force/ForceGeneralSDFContact.cpp:147-219 for one contact): the error scale of fm where
+    contact forces cancel."""
+    L = lib()
+    if not hasattr(L, "_norm_ready"):
+        L.orc_pair_force_norm_sum.restype = ctypes.c_double
+        L.orc_pair_force_norm_sum.argtypes = [ctypes.POINTER(_Grid), ctypes.POINTER(ctypes.c_double), ctypes.c_int] + \
+            [ctypes.POINTER(ctypes.c_double)] * 4 + [ctypes.POINTER(_Params)]
+        L._norm_ready = True
+    g = grid._c()
+    p = _f64(pts).reshape(-1, 3)
+    prm = params._c()
+    return L.orc_pair_force_norm_sum(ctypes.byref(g), _dp(p), len(p), _dp(_f64(E_A)), _dp(_f64(phi_A)),
+                                     _dp(_f64(E_B)), _dp(_f64(phi_B)), ctypes.byref(prm))
+
+
 # --------------------------------------------------------------------------- BDF1 of one translational mover
 
 class _Mover(ctypes.Structure):

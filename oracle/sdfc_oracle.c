@@ -828,6 +828,25 @@ int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double*
     return n_active;
 }
 
+/* Sum over the pair's active contacts of the norm of each contact's own 12-vector (its term of
+ * fm, ForceGeneralSDFContact::computeForce(contacts), ForceGeneralSDFContact.cpp:147-219, for the
+ * contact alone).  Where the contacts' forces cancel in fm (a peg pressed all round into a bore),
+ * this is the scale against which the error of fm is meaningful.  Not in the reference. */
+double orc_pair_force_norm_sum(const orc_grid* g, const double* pts, int n_pts, const double* E_A,
+                               const double* phi_A, const double* E_B, const double* phi_B, const orc_params* prm) {
+    int* ids = (int*)malloc(sizeof(int) * (size_t)(n_pts > 0 ? n_pts : 1));
+    const int n_active = orc_detect(g, E_A, E_B, pts, n_pts, ids, NULL);
+    double total = 0.0, f[12];
+    for (int c = 0; c < n_active; ++c) {
+        force_value(g, E_A, phi_A, E_B, phi_B, prm, pts, ids + c, 1, f);
+        double s = 0.0;
+        for (int k = 0; k < 12; ++k) s += f[k] * f[k];
+        total += sqrt(s);
+    }
+    free(ids);
+    return total;
+}
+
 /* ------------------------------------------------------------------ penetration energy */
 
 /* Penetration energy of a pair: the sum over its active contacts (orc_detect) of kn d^2 / 2,

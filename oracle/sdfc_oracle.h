@@ -54,6 +54,10 @@ int orc_detect(const orc_grid* g, const double* E_A, const double* E_B, const do
 int orc_pair_eval(const orc_grid* g, const double* pts, int n_pts, const double* E_A, const double* phi_A,
                   const double* E_B, const double* phi_B, const orc_params* prm, int want_deriv, double* fm,
                   double* Km, double* Dm, int* ids);
+/* Sum over the active contacts of the norm of each contact's own 12-vector term of fm (the
+ * error scale of fm where contact forces cancel); not in the reference. */
+double orc_pair_force_norm_sum(const orc_grid* g, const double* pts, int n_pts, const double* E_A,
+                               const double* phi_A, const double* E_B, const double* phi_B, const orc_params* prm);
 
 /* Penetration energy of a pair (sum of kn d^2 / 2 over the active contacts) and its gradient
  * dE[12] wrt the twists of A then B (w, v each). */

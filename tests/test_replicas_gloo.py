@@ -43,6 +43,13 @@ def _rank_main(rank, world, port, out_dir):
     dirs = phiA[:, 3:] / 0.01
     gathered = [None] * w
     dist.all_gather_object(gathered, dirs.tolist())
+    # the sharded legs: each rank's block of a shared workload, its per-instance results gathered
+    # in rank order on every rank, sums over ranks
+    blk = bench.rank_block(np.arange(8 * w), 8, r, w)
+    rows = bench.gather_rows(np.stack([blk, 10 * blk], 1), w)
+    total = bench.dist_sum(r + 1, w)
+    c4_dirs = bench.rank_block(bench.W.cone_directions(4 * w, 30.0, seed=4), 4, r, w)
+    c4_all = bench.gather_rows(c4_dirs, w)
     # max over ranks of a per-rank time, and the weak-scaling aggregate built on it
     t_max = bench.dist_max(0.5 + r, w)
     rate, t_job = bench.whole_job_rate(1000, 0.5 + r, w)
@@ -52,6 +59,7 @@ def _rank_main(rank, world, port, out_dir):
     with contextlib.redirect_stdout(buf):
         ret = bench.run_reference(None, w, r) if r != 0 else None
     res = {"rank": r, "gathered": gathered, "t_max": t_max, "rate": rate, "t_job": t_job,
+           "blk": blk.tolist(), "rows": rows.tolist(), "total": total, "c4_all": c4_all.tolist(),
            "ref_stdout": buf.getvalue(), "ref_ret": ret, "EB_eye": bool(np.allclose(EB, np.eye(4))),
            "phiB_zero": bool(not phiB.any()), "EA_rot_ok": bool(np.allclose(EA[:, 3], [0, 0, 0, 1]))}
     with open(os.path.join(out_dir, f"rank{r}.json"), "w") as f:
@@ -80,6 +88,16 @@ def test_ranks_take_disjoint_blocks_of_one_sweep(two_ranks, workloads):
     np.testing.assert_allclose(phiA[:, 3:] / 0.01, workloads.fibonacci_directions(16), atol=1e-12)
     for r in two_ranks:
         assert r["EB_eye"] and r["phiB_zero"] and r["EA_rot_ok"]
+
+
+def test_sharded_legs_split_and_gather(two_ranks, workloads):
+    """Simulation, rollout and multi-part legs: disjoint blocks of one workload per rank, per-instance
+    results gathered in rank order (the whole workload), counts summed over ranks."""
+    assert two_ranks[0]["blk"] == list(range(8)) and two_ranks[1]["blk"] == list(range(8, 16))
+    for r in two_ranks:
+        assert r["rows"] == [[k, 10 * k] for k in range(16)]
+        assert r["total"] == 3.0
+        np.testing.assert_allclose(r["c4_all"], workloads.cone_directions(8, 30.0, seed=4), atol=0)
 
 
 def test_max_over_ranks_and_whole_job_rate(two_ranks):
