@@ -761,6 +761,14 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
                 } else {
                     cell_corners64(g, i, j, k, e);
                 }
+            } else if (g.storage == 1) {
+                // FP32 values: the FP64 copy holds them widened, so the cell-corner array's two
+                // 16-byte loads serve the depth too (bit-identical, instead of 8 FP64 gathers);
+                // the derivatives below load the corners again (L1 hits) rather than keep them live
+                const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
+                const float4 lo = __ldg(cq), hi = __ldg(cq + 1);
+                e[0] = lo.x; e[1] = lo.y; e[2] = lo.z; e[3] = lo.w;
+                e[4] = hi.x; e[5] = hi.y; e[6] = hi.z; e[7] = hi.w;
             } else {
                 plain_corners64(g, i, j, k, e);
             }
@@ -774,10 +782,11 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             d = J.v + g.col_th;
             // FP32 analytic derivatives of the cell's interpolant
             const float u = (float)ud, v = (float)vd, w = (float)wd;
-            if constexpr (BR) {
-                if (!have32) cell_corners32(g, i, j, k, cc);
-            } else {
-                plain_corners32(g, i, j, k, cc);
+            if (!have32) {
+                if constexpr (BR)
+                    cell_corners32(g, i, j, k, cc);
+                else
+                    plain_corners32(g, i, j, k, cc);
             }
             const float c000 = cc[0], c100 = cc[1], c010 = cc[2], c110 = cc[3];
             const float c001 = cc[4], c101 = cc[5], c011 = cc[6], c111 = cc[7];

@@ -110,6 +110,7 @@ struct Prefilter {
     float lo_out[3], hi_out[3];  // certainly outside beyond these
     float col_th;
     float guard;                 // bound on |d32 - d64|, times a safety factor
+    float lip;                   // Lipschitz bound of the grid's interpolant (GridDesc::lip)
 };
 
 // Per-evaluation inputs, device pointers (row-major 4x4 poses, body twists).
