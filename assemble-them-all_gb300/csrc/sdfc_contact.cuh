@@ -207,10 +207,58 @@ __device__ __forceinline__ float brick_value32(const GridDesc& g, int i, int j, 
 struct Corners32 {
     float c[8];
 };
+// Node offsets of a cell's 8 corners within one brick (corner order c000, c100, c010, c110, ...).
+__device__ __forceinline__ int brick_corner_offset(int q) { return (q & 1) + 8 * ((q >> 1) & 1) + 64 * (q >> 2); }
+// Whether cell (i, j, k)'s corners all lie in the brick of node (i, j, k) (about 2/3 of cells).
+__device__ __forceinline__ bool cell_in_one_brick(int i, int j, int k) {
+    return (i & 7) != 7 && (j & 7) != 7 && (k & 7) != 7;
+}
+
 static __device__ __noinline__ Corners32 brick_corners32(const GridDesc& g, int i, int j, int k) {
     Corners32 r;
+    if (cell_in_one_brick(i, j, k)) {  // one scale/offset and eight codes of one brick
+        const size_t b = brick_of(g, i, j, k);
+        const float2 so = __ldg(g.bso + b);
+        const unsigned short* cb = g.b16 + b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            r.c[q] = fmaf(so.x, __half2float(__ushort_as_half(__ldg(cb + brick_corner_offset(q)))), so.y);
+        return r;
+    }
 #pragma unroll
     for (int q = 0; q < 8; ++q) r.c[q] = brick_value32(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+    return r;
+}
+
+// A brick cell's corners decoded both ways from one set of loads: FP32 (as brick_value32) and
+// FP64 (as brick_value64).
+struct Corners3264 {
+    float c[8];
+    double e[8];
+};
+static __device__ __noinline__ Corners3264 brick_corners3264(const GridDesc& g, int i, int j, int k) {
+    Corners3264 r;
+    if (cell_in_one_brick(i, j, k)) {
+        const size_t b = brick_of(g, i, j, k);
+        const float2 so = __ldg(g.bso + b);
+        const unsigned short* cb = g.b16 + b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float h = __half2float(__ushort_as_half(__ldg(cb + brick_corner_offset(q))));
+            r.c[q] = fmaf(so.x, h, so.y);
+            r.e[q] = fma((double)so.x, (double)h, (double)so.y);
+        }
+        return r;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int ii = i + (q & 1), jj = j + ((q >> 1) & 1), kk = k + (q >> 2);
+        const size_t b = brick_of(g, ii, jj, kk);
+        const float2 so = __ldg(g.bso + b);
+        const float h = brick_code(g, b, ii, jj, kk);
+        r.c[q] = fmaf(so.x, h, so.y);
+        r.e[q] = fma((double)so.x, (double)h, (double)so.y);
+    }
     return r;
 }
 static __device__ __noinline__ double brick_value64_cold(const GridDesc& g, int i, int j, int k) {
@@ -753,7 +801,15 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             float cc[8];
             bool have32 = false;
             if constexpr (BR) {
-                if (g.v32) {  // FP32 node values: one set of loads serves both the depth and the derivatives
+                if (g.b16) {  // FP16 bricks: the codes loaded once, decoded in FP64 and in FP32
+                    const Corners3264 r = brick_corners3264(g, i, j, k);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        e[q] = r.e[q];
+                        cc[q] = r.c[q];
+                    }
+                    have32 = true;
+                } else if (g.v32) {  // FP32 node values: one set of loads serves both the depth and the derivatives
                     node_corners32(g, i, j, k, cc);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) e[q] = (double)cc[q];
