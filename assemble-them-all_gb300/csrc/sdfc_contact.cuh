@@ -817,15 +817,10 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
                 } else {
                     cell_corners64(g, i, j, k, e);
                 }
-            } else if (g.storage == 1) {
-                // FP32 values: the FP64 copy holds them widened, so the cell-corner array's two
-                // 16-byte loads serve the depth too (bit-identical, instead of 8 FP64 gathers);
-                // the derivatives below load the corners again (L1 hits) rather than keep them live
-                const float4* cq = g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k));
-                const float4 lo = __ldg(cq), hi = __ldg(cq + 1);
-                e[0] = lo.x; e[1] = lo.y; e[2] = lo.z; e[3] = lo.w;
-                e[4] = hi.x; e[5] = hi.y; e[6] = hi.z; e[7] = hi.w;
             } else {
+                // (FP32 grids keep an FP64 copy: widening the FP32 corners here instead would put
+                // eight conversions per contact on GB300's FP64 pipe, measured slower than the
+                // eight FP64 gathers)
                 plain_corners64(g, i, j, k, e);
             }
             const double e000 = e[0], e100 = e[1], e010 = e[2], e110 = e[3];

@@ -46,7 +46,6 @@ __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pos
     f.col_th = (float)g.col_th;
     double bound = (double)g.lip * eps_pos + 12.0 * kU * (double)g.vmax + 2.0 * kU * fabs(g.col_th);
     f.guard = (float)(4.0 * bound) + 1e-30f;
-    f.lip = g.lip;
 }
 
 __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchInputs in,
@@ -218,18 +217,8 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         const float r = sp.w * 1.00001f +
                         1e-5f * (P.radius + fabsf(f.p[0]) + fabsf(f.p[1]) + fabsf(f.p[2]) + fabsf(cx) + fabsf(cy) +
                                  fabsf(cz));
-        bool away = cx + r < f.lo_out[0] || cx - r > f.hi_out[0] || cy + r < f.lo_out[1] || cy - r > f.hi_out[1] ||
-                    cz + r < f.lo_out[2] || cz - r > f.hi_out[2];
-        // Depth bound: with the sphere's centre inside the box, every point x of the tile within
-        // the box has d(x) >= d32(centre) - guard - lip r (the interpolant is lip-Lipschitz, the
-        // FP32 value is within guard of the exact one, the segment to x stays in the box), and
-        // points outside the box have no depth; when that bound is positive no point of the
-        // tile can be active, and none needs the FP64 recheck.
-        if (!away && cx >= f.lo_in[0] && cx <= f.hi_in[0] && cy >= f.lo_in[1] && cy <= f.hi_in[1] &&
-            cz >= f.lo_in[2] && cz <= f.hi_in[2]) {
-            const float dc = trilinear32(gv, dg.get(), gn[0], gn[1], gn[2], f, cx, cy, cz) + f.col_th;
-            away = dc > 1.0001f * (f.guard + f.lip * r);
-        }
+        const bool away = cx + r < f.lo_out[0] || cx - r > f.hi_out[0] || cy + r < f.lo_out[1] ||
+                          cy - r > f.hi_out[1] || cz + r < f.lo_out[2] || cz - r > f.hi_out[2];
         if (away) {  // uniform over the CTA
             if (tid == 0) {
                 tile_count[t] = 0;

@@ -54,7 +54,7 @@ constexpr int kDetectThreads = 256;  // threads per detection CTA
 #define SDFC_FORCE_CHUNK 128
 #endif
 #ifndef SDFC_FORCE_MIN_BLOCKS
-#define SDFC_FORCE_MIN_BLOCKS 4
+#define SDFC_FORCE_MIN_BLOCKS 5
 #endif
 constexpr int kChunk = SDFC_FORCE_CHUNK;
 constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
@@ -110,7 +110,6 @@ struct Prefilter {
     float lo_out[3], hi_out[3];  // certainly outside beyond these
     float col_th;
     float guard;                 // bound on |d32 - d64|, times a safety factor
-    float lip;                   // Lipschitz bound of the grid's interpolant (GridDesc::lip)
 };
 
 // Per-evaluation inputs, device pointers (row-major 4x4 poses, body twists).

@@ -800,10 +800,24 @@ def run_c5(args, sdfc, ctx, torch):
 
         q16, wall, conv, rounds, evals = sim_run(g16, np.arange(n), sdfc.PRECISION_MIXED)
         q64, _, _, _, _ = sim_run(g64, idx, sdfc.PRECISION_FP64)
+        # the planner's decision per direction (PhysicsPlanner.is_disassembled,
+        # examples/run_joint_plan.py:291-302) after the steps, on the FP16-brick grid and on the
+        # FP64 grid (both with the same mixed-precision evaluations): does the storage change it?
+        q64m, _, _, _, _ = sim_run(g64, np.arange(n), sdfc.PRECISION_MIXED)
+        M = importlib.import_module(f"{PKG}.mesh")
+        still_pts = asm.parts[still].surface_points(20000, 56) + asm.parts[still].position
+        check = M.DisassemblyCheck(ctx, pts[::max(1, len(pts) // 20000)], still_pts)
+        at = lambda q: np.stack([W.pose(None, asm.parts[mover].position + x) for x in q])  # noqa: E731
+        d16, d64 = check(at(q16)), check(at(q64m))
         out["sim"] = {"scenes": n, "steps": args.c5_steps, "wall_s": wall, "scene_steps_per_s": n * args.c5_steps / wall,
                       "rounds": rounds, "scene_evaluations": evals, "converged_last_step": float(np.mean(conv)),
                       "pose_error_vs_fp64_grid": {"max_abs": float(np.abs(q16[idx] - q64).max()),
-                                                   "max_displacement": float(np.abs(q64).max()), "scenes": m}}
+                                                   "max_displacement": float(np.abs(q64).max()), "scenes": m},
+                      "planner_decision_vs_fp64_grid": {
+                          "directions": n, "disassembled_fp16_bricks": int(d16.sum()),
+                          "disassembled_fp64_grid": int(d64.sum()), "same_decision": int((d16 == d64).sum()),
+                          "rule": "is_disassembled after the steps (convex hulls of 20k surface points each), "
+                                  "mixed-precision evaluations on both grids"}}
     return out
 
 

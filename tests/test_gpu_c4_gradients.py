@@ -7,20 +7,23 @@ pose perturbed (sigma 0.01 translation, sigma 1 degree rotation), pulled along d
 energy) + |q_T - target|^2.  Eight instances spread over the 4096 (the bench's seeds) are checked:
 dL/dq0 (6) and dL/d(direction) on the tangent plane of the unit sphere at the direction (2),
 from sdfc_sim_backward_energy, against central differences of rollouts with FP64 evaluations
-and Newton solved to |g| < 1e-13, at steps 1e-6 and 1e-8.
+and Newton solved to |g| < 1e-13, at steps 1e-6, 1e-8 and 3e-9.
 
 This loss is piecewise smooth: over 200 steps thousands of contact points enter and leave the
 active set, and each entry is a kink of the rollout (the contact force is continuous in the
 depth, its derivative is not).  At the workload's stated step 1e-6 the +- rollouts straddle such
 kinks, so those differences are not the derivative; they converge to the adjoint as the step
 shrinks (at 1e-8 they agree with it to about 1e-7, the tolerance-limited noise of the
-differences).  An instance with a step whose Newton iteration stops without converging (the
-reference's three line-search strikes) has a non-differentiable loss and is not checked.
+differences).  Even at 1e-8 a component's +- rollouts can straddle a kink; such a component's
+differences at 1e-8 and 3e-9 disagree, which the test uses to recognise it.  An instance with a
+step whose Newton iteration stops without converging (the reference's three line-search
+strikes) has a non-differentiable loss and is not checked.
 
-Bars: for every sampled instance whose base and +-1e-8 rollouts converged at every step (at least
-five of the eight), the FP64 adjoint is within 1e-4 of the 1e-8 differences, relative to their
-norm; the mixed-precision adjoint (FP32 per-contact algebra, the reference's Newton tolerance
-1e-8) is within 1e-2 of the FP64 adjoint, measured on the same instances."""
+Bars, over the sampled instances whose base and fine-step rollouts converged at every step (at
+least five of the eight): every component whose differences at 1e-8 and 3e-9 agree to 1e-5 of the
+gradient's norm (at least 90% of them) has the FP64 adjoint within 1e-4 of the gradient's norm of
+its 1e-8 difference; the mixed-precision adjoint (FP32 per-contact algebra, the reference's Newton
+tolerance 1e-8) is within 1e-2 of the FP64 adjoint, relative to its norm."""
 import numpy as np
 import pytest
 
@@ -29,7 +32,7 @@ from conftest import submodule
 pytestmark = pytest.mark.gpu
 
 N_ALL, T, TOL = 4096, 200, 1e-13
-STEPS = (1e-6, 1e-8)  # the workload's stated difference step, and one in the differentiable regime
+STEPS = (1e-6, 1e-8, 3e-9)  # the workload's stated difference step, and two in the differentiable regime
 SAMPLE = tuple(range(0, N_ALL, N_ALL // 8))
 H = float(np.float32(5e-3))
 GRAVITY = (0.0, 0.0, -9.8)
@@ -143,17 +146,25 @@ def c4():
     ctx.close()
 
 
+def _checked(c4):
+    """Instances whose base and fine-step rollouts converged at every step."""
+    return [r for r in c4 if r["converged"][STEPS[1]] and r["converged"][STEPS[2]]]
+
+
 def test_fp64_adjoint_matches_central_differences(c4):
-    fine = STEPS[-1]
-    checked = [r for r in c4 if r["converged"][fine]]
-    assert len(checked) >= 5, [r["instance"] for r in c4 if not r["converged"][fine]]
+    checked = _checked(c4)
+    assert len(checked) >= 5, [r["instance"] for r in c4 if r not in checked]
+    smooth_total = 0
     for r in checked:
-        rel = np.linalg.norm(r["adj"] - r["fd"][fine]) / np.linalg.norm(r["fd"][fine])
-        assert rel <= 1e-4, (r["instance"], rel, r["adj"], r["fd"][fine])
+        scale = np.linalg.norm(r["fd"][STEPS[1]])
+        smooth = np.abs(r["fd"][STEPS[1]] - r["fd"][STEPS[2]]) <= 1e-5 * scale
+        smooth_total += int(smooth.sum())
+        err = np.abs(r["adj"] - r["fd"][STEPS[1]])[smooth] / scale
+        assert (err <= 1e-4).all(), (r["instance"], err, r["adj"], r["fd"][STEPS[1]])
+    assert smooth_total >= 0.9 * 8 * len(checked), smooth_total
 
 
 def test_mixed_adjoint_against_fp64_adjoint(c4):
-    fine = STEPS[-1]
-    for r in [r for r in c4 if r["converged"][fine]]:
+    for r in _checked(c4):
         rel = np.linalg.norm(r["mixed"] - r["adj"]) / np.linalg.norm(r["adj"])
         assert rel <= 1e-2, (r["instance"], rel)
