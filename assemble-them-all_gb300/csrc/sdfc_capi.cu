@@ -56,6 +56,8 @@ void free_batch(sdfc_batch* b) {
     cudaFree(b->d_recheck_list);
     cudaFree(b->d_recheck_n);
     cudaFree(b->d_badin);
+    cudaFree(b->d_inst_total);
+    cudaFree(b->d_items);
     cudaFree(b->d_partial);
     cudaFree(b->d_recheck);
     cudaFree(b->d_point_offset);
@@ -85,6 +87,9 @@ sdfc::BatchScratch scratch_of(const sdfc_batch* b) {
     sc.worker_ctas = b->worker_ctas;
     sc.max_ntiles = b->max_ntiles;
     sc.badin = b->d_badin;
+    sc.chunks_per_slot = b->chunks_per_slot;
+    sc.inst_total = b->d_inst_total;
+    sc.items = b->d_items;
     return sc;
 }
 
@@ -109,6 +114,8 @@ int run_batch(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc
     sdfc::launch_detect(b->d_inst, b->d_tile_inst, b->n, b->total_tiles, in, ctx->d_grids, ctx->d_points, sc, stream,
                         b->has_plain, b->has_bricks);
     if (b->timing) cudaEventRecord(b->ev[1], stream);
+    sdfc::launch_plan(b->d_inst, b->n, in, ctx->d_grids, sc, deriv, stencil, prec, stream, b->has_plain,
+                      b->has_bricks);
     const sdfc::BatchInputs* q2 = sdfc::force_skips_q2(true, stencil, prec) ? &in : nullptr;
     if (in.mode && !b->timing && b->aux_stream) {
         // masked evaluation: the derivative and value passes touch disjoint instances (and
@@ -206,7 +213,7 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
     b->ctx = ctx;
     b->n = n;
     b->deriv_mode = ctx->deriv_mode;
-    b->slots = sdfc::slots_for(n, ctx->sm_count);
+    b->slots = sdfc::slots_for(n);
     b->partial_slots = b->slots;
     b->precision = ctx->precision;
     b->inst.resize(n);
@@ -244,8 +251,10 @@ int sdfc_impl::batch_create(sdfc_context* ctx, int n, const int* points, const i
         (rc = alloc((void**)&b->d_pair32, sizeof(sdfc::PairState<float>) * n)) ||
         (rc = alloc((void**)&b->d_pair64, sizeof(sdfc::PairState<double>) * n)) ||
         (rc = alloc((void**)&b->d_recheck_list, sizeof(int) * std::max(tiles, 1))) ||
-        (rc = alloc((void**)&b->d_recheck_n, 5 * sizeof(int))) ||
+        (rc = alloc((void**)&b->d_recheck_n, sdfc::kCounters * sizeof(int))) ||
         (rc = alloc((void**)&b->d_badin, sizeof(int) * (size_t)n)) ||
+        (rc = alloc((void**)&b->d_inst_total, sizeof(int) * (size_t)n)) ||
+        (rc = alloc((void**)&b->d_items, sizeof(int) * 4 * (size_t)n * sdfc::kMaxSlots)) ||
         (rc = alloc((void**)&b->d_partial, sizeof(double) * (size_t)n * b->slots * sdfc::kOutDeriv)) ||
         (rc = alloc((void**)&b->d_recheck, sizeof(unsigned long long))) ||
         (rc = alloc((void**)&b->d_point_offset, sizeof(long long) * n)) ||

@@ -41,8 +41,9 @@ struct sdfc_batch {
     sdfc_context* ctx = nullptr;
     int n = 0;
     int total_tiles = 0;
-    int slots = 8;  // force CTAs (partial rows) per instance
+    int slots = sdfc::kMaxSlots;  // partial rows per instance, at most (the spread's cap)
     int partial_slots = 0;  // slots the partial-row buffer holds
+    int chunks_per_slot = sdfc::kDefaultChunksPerSlot;  // chunks of active contacts per share, at least
     int force_variant = sdfc::kForceCtas;
     int worker_ctas = 0;  // one-warp force workers (0: the device's multiprocessors x resident workers)
     int max_ntiles = 0;   // most detection tiles of one instance
@@ -59,8 +60,10 @@ struct sdfc_batch {
     sdfc::PairState<float>* d_pair32 = nullptr;
     sdfc::PairState<double>* d_pair64 = nullptr;
     int* d_recheck_list = nullptr;  // total_tiles
-    int* d_recheck_n = nullptr;     // 5 counters (BatchScratch::recheck_n)
+    int* d_recheck_n = nullptr;     // sdfc::kCounters counters (BatchScratch::recheck_n)
     int* d_badin = nullptr;         // n: non-finite inputs (BatchScratch::badin)
+    int* d_inst_total = nullptr;    // n: active contacts per instance (BatchScratch::inst_total)
+    int* d_items = nullptr;         // 4 x n x kMaxSlots: the force passes' item lists
     double* d_partial = nullptr;
     unsigned long long* d_recheck = nullptr;
     long long* d_point_offset = nullptr;  // n: first output row of each instance's per-point distances

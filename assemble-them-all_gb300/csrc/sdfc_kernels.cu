@@ -1,5 +1,6 @@
 // Kernels of the batched point-vs-SDF contact evaluation; see sdfc_kernels.cuh.
 #include <algorithm>
+#include <atomic>
 #include <math_constants.h>
 #include <cstdint>
 
@@ -52,13 +53,14 @@ __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchI
                             const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
                             Prefilter* __restrict__ pref, PairState<float>* __restrict__ pair32,
                             PairState<double>* __restrict__ pair64, int* __restrict__ recheck_n,
-                            int* __restrict__ badin) {
+                            int* __restrict__ badin, int* __restrict__ inst_total) {
     // blockIdx.y: 0 the prefilter, 1 / 2 the FP32 / FP64 pair state every force or energy CTA of
     // the instance starts from (once per instance here, spread over three warps per 32 instances:
     // all three are FP64 arithmetic)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0 && blockIdx.y == 0)  // detection's list of tiles to recheck starts empty, and so do the
-        for (int q = 0; q < 5; ++q) recheck_n[q] = 0;  // force workers' queues
+        for (int q = 0; q < kCounters; ++q) recheck_n[q] = 0;  // force launches' queues and item lists
+    if (i < n && blockIdx.y == 0) inst_total[i] = 0;  // detection adds each tile's active count
 
     if (i >= n || (in.mode && in.mode[i] == 0)) return;
     const size_t o = (size_t)i;
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                                                                 int* __restrict__ tile_queue,
                                                                 const int* __restrict__ mode,
                                                                 int* __restrict__ recheck_list,
-                                                                int* __restrict__ recheck_n) {
+                                                                int* __restrict__ recheck_n,
+                                                                int* __restrict__ inst_total) {
     __shared__ Prefilter f;
     __shared__ DetectGrid<BRICKS> dg;
     __shared__ const float4* gv;
@@ -299,6 +302,7 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
             tile_count[t] = ia;
             tile_queue[t] = iq;
             if (iq > 0) recheck_list[atomicAdd(recheck_n, 1)] = t;  // any order: tiles are independent
+            if (ia > 0) atomicAdd(inst_total + i, ia);                // integer sums: exact in any order
         }
     }
     __syncthreads();
@@ -318,7 +322,7 @@ __device__ void recheck_tile(const InstanceDesc* __restrict__ inst, const int* _
                              const BatchInputs& in, const GridDesc* __restrict__ grids,
                              const PointsDesc* __restrict__ points, int* __restrict__ ids,
                              int* __restrict__ tile_count, const int* __restrict__ tile_queue,
-                             unsigned long long* __restrict__ recheck, int t, int* qs) {
+                             unsigned long long* __restrict__ recheck, int* __restrict__ inst_total, int t, int* qs) {
     const int q = tile_queue[t];
     const int lane = threadIdx.x;
     const int i = tile_inst[t];
@@ -332,7 +336,8 @@ __device__ void recheck_tile(const InstanceDesc* __restrict__ inst, const int* _
     __syncwarp();
     for (int k = lane; k < q; k += 32) qs[k] = out[kTile - 1 - k];
     __syncwarp();
-    int base = tile_count[t];
+    const int base0 = tile_count[t];
+    int base = base0;
     for (int r0 = 0; r0 < q; r0 += 32) {
         const int k = r0 + lane;
         bool active = false;
@@ -347,6 +352,7 @@ __device__ void recheck_tile(const InstanceDesc* __restrict__ inst, const int* _
     }
     if (lane == 0) {
         tile_count[t] = base;
+        if (base > base0) atomicAdd(inst_total + i, base - base0);
         if (recheck) atomicAdd(recheck, (unsigned long long)q);
     }
 }
@@ -360,11 +366,13 @@ __global__ void __launch_bounds__(32) recheck_kernel(const InstanceDesc* __restr
                                                      int* __restrict__ tile_count, const int* __restrict__ tile_queue,
                                                      unsigned long long* __restrict__ recheck,
                                                      const int* __restrict__ recheck_list,
-                                                     const int* __restrict__ recheck_n) {
+                                                     const int* __restrict__ recheck_n,
+                                                     int* __restrict__ inst_total) {
     __shared__ int qs[kTile];
     const int nl = *recheck_n;
     for (int w = blockIdx.x; w < nl; w += gridDim.x)
-        recheck_tile(inst, tile_inst, in, grids, points, ids, tile_count, tile_queue, recheck, recheck_list[w], qs);
+        recheck_tile(inst, tile_inst, in, grids, points, ids, tile_count, tile_queue, recheck, inst_total,
+                     recheck_list[w], qs);
 }
 
 // ------------------------------------------------------------------ distances
@@ -567,37 +575,74 @@ constexpr int force_min_blocks() {
     return std::is_same<T, float>::value ? kForceCtasPerSm : 1;
 }
 
-// BR = false: the FP32 fast path specialised for grids with the FP32 cell-corner array
-// (storages 0 and 1); BR = true serves every storage.  skip: 0 none, 1 instances on grids
-// without the cell-corner array, 2 instances on grids with it (when a batch has both kinds,
-// the two instantiations split its instances).
-template <bool DERIV, bool STENCIL, typename T, bool BR = true>
-__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(const InstanceDesc* __restrict__ inst, BatchInputs in,
-                                                       const GridDesc* __restrict__ grids,
-                                                       const PointsDesc* __restrict__ points,
-                                                       const int* __restrict__ ids,
-                                                       const int* __restrict__ tile_count,
-                                                       const PairState<T>* __restrict__ pairs,
-                                                       double* __restrict__ partial, int skip, int slots) {
-    constexpr int NV = DERIV ? kOutDeriv : kOutValue;
-    constexpr int NW = kChunk / 32;
-    // FP32 algebra: contacts whose derivative stencil leaves the cell take the
-    // exact path with the warp's help (warp_exact_jets)
-    constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
-    __shared__ Accum<T> acc[NW * NV];
-    __shared__ int prefix[kMaxTilesPerInstance + 1];
-    __shared__ GridDesc g;
-    __shared__ PointsDesc P;
-    __shared__ PairState<T> S;
-    const int i = blockIdx.y, s = blockIdx.x;
-    if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const InstanceDesc I = inst[i];
-    if (skip && (grids[I.grid].cells32 == nullptr) == (skip == 1)) return;  // the other instantiation's instance
+// Shares of an instance with `total` active contacts in chunks of `chunk` contacts, at least
+// `per` chunks a share, at most `cap` shares (none without contacts).  The force kernels, the
+// plan and finalize_kernel each compute it from detection's count, so they agree.
+__host__ __device__ __forceinline__ int spread_of(int total, int chunk, int per, int cap) {
+    const int chunks = (total + chunk - 1) / chunk;
+    const int sh = (chunks + per - 1) / per;
+    return sh < cap ? sh : cap;
+}
+
+// One thread per instance: its items (instance x kMaxSlots + share, one per share), appended to
+// the list of the force launch that evaluates it (list l of n x cap entries at items + l n cap;
+// lengths in counters[5 + l]), one atomic per (warp, list).  Which instances land where in a list
+// depends on the atomics' order; no sum does.
+__global__ void plan_kernel(const InstanceDesc* __restrict__ inst, int n, const int* __restrict__ mode, int deriv,
+                            const GridDesc* __restrict__ grids, int split, int chunk, int per, int cap,
+                            const int* __restrict__ inst_total, int* __restrict__ items,
+                            int* __restrict__ counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    int S = 0, L = 0;
+    if (i < n) {
+        const int m = mode ? mode[i] : (deriv ? 2 : 1);
+        if (m != 0) {
+            S = spread_of(inst_total[i], chunk, per, cap);
+            L = (m == 2 ? 0 : 2) + (split && grids[inst[i].grid].cells32 == nullptr ? 1 : 0);
+        }
+    }
+    for (int l = 0; l < 4; ++l) {
+        const int v = L == l ? S : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += u;
+        }
+        const int tot = __shfl_sync(kFull, incl, 31);
+        if (tot == 0) continue;  // uniform over the warp
+        int base = 0;
+        if (lane == 31) base = atomicAdd(counters + 5 + l, tot);
+        base = __shfl_sync(kFull, base, 31);
+        int* out = items + (size_t)l * n * cap + base + (incl - v);
+        for (int k = 0; k < v; ++k) out[k] = i * kMaxSlots + k;
+    }
+}
+
+// Shared state of a force CTA of kChunk threads: the warps' accumulators, the prefix of the
+// instance's tile counts and its grid, point-set and pair descriptors.
+template <bool DERIV, typename T>
+struct ForceSmem {
+    static constexpr int NV = DERIV ? kOutDeriv : kOutValue;
+    static constexpr int NW = kChunk / 32;
+    Accum<T> acc[NW * NV];
+    int prefix[kMaxTilesPerInstance + 1];
+    GridDesc g;
+    PointsDesc P;
+    PairState<T> S;
+};
+
+// An item's set-up: warp 0 the inclusive prefix of the instance's tile counts (32 tiles at a
+// time), warp 1 the descriptors.  The caller's barrier follows.
+template <bool DERIV, typename T>
+__device__ __forceinline__ void force_item_setup(ForceSmem<DERIV, T>& sm, const InstanceDesc& I, int i,
+                                                 const GridDesc* __restrict__ grids,
+                                                 const PointsDesc* __restrict__ points,
+                                                 const int* __restrict__ tile_count,
+                                                 const PairState<T>* __restrict__ pairs, int warp, int lane) {
     if (warp == 0) {
-        // inclusive prefix of the instance's tile counts, 32 tiles at a time
         int run = 0;
-        if (lane == 0) prefix[0] = 0;
+        if (lane == 0) sm.prefix[0] = 0;
         for (int k0 = 0; k0 < I.ntiles; k0 += 32) {
             const int k = k0 + lane;
             int v = k < I.ntiles ? tile_count[I.tile0 + k] : 0;
@@ -606,93 +651,191 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(co
                 const int u = __shfl_up_sync(kFull, v, o);
                 if (lane >= o) v += u;
             }
-            if (k < I.ntiles) prefix[k + 1] = run + v;
+            if (k < I.ntiles) sm.prefix[k + 1] = run + v;
             run += __shfl_sync(kFull, v, 31);
         }
     } else if (warp == 1) {
-        warp_copy(g, grids[I.grid], lane);
-        warp_copy(P, points[I.points], lane);
-        warp_copy(S, pairs[i], lane);
+        warp_copy(sm.g, grids[I.grid], lane);
+        warp_copy(sm.P, points[I.points], lane);
+        warp_copy(sm.S, pairs[i], lane);
     }
-    for (int k = tid; k < NW * NV; k += kChunk) acc[k].zero();
-    __syncthreads();
-    const int total = prefix[I.ntiles];
+}
+
+// An item's contacts: chunks s, s + shares, ... of kChunk contacts, one per thread, each warp's
+// sums into its accumulators.
+template <bool DERIV, bool STENCIL, typename T, bool BR>
+__device__ __forceinline__ void force_item_chunks(ForceSmem<DERIV, T>& sm, const InstanceDesc& I, int s, int shares,
+                                                  const int* __restrict__ ids, int tid, int lane, int warp) {
+    constexpr int NV = ForceSmem<DERIV, T>::NV;
+    // FP32 algebra: contacts whose derivative stencil leaves the cell take the
+    // exact path with the warp's help (warp_exact_jets)
+    constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
+    const int total = sm.prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
-    if (s < nchunks) {
-        for (int chunk = s; chunk < nchunks; chunk += slots) {
-            if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
-            const int c = chunk * kChunk + tid;
-            const bool valid = c < total;
-            V3 xi = v3(0, 0, 0);
-            Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
-            int sid = 0;
-            if (valid) {
-                int lo = 0, hi = I.ntiles;  // largest k with prefix[k] <= c
-                while (hi - lo > 1) {
-                    int mid = (lo + hi) >> 1;
-                    if (prefix[mid] <= c)
-                        lo = mid;
-                    else
-                        hi = mid;
-                }
-                sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
-                xi = load_point(P, sid);
-                if constexpr (kWarpExact) xf = load_point32(P, sid);
+    for (int chunk = s; chunk < nchunks; chunk += shares) {
+        if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
+        const int c = chunk * kChunk + tid;
+        const bool valid = c < total;
+        V3 xi = v3(0, 0, 0);
+        Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
+        int sid = 0;
+        if (valid) {
+            int lo = 0, hi = I.ntiles;  // largest k with prefix[k] <= c
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (sm.prefix[mid] <= c)
+                    lo = mid;
+                else
+                    hi = mid;
             }
-            FastCell fc;
-            const FastCell* fcp = nullptr;
-            ExactJet<T> ej;
-            const ExactJet<T>* ejp = nullptr;
-            if constexpr (kWarpExact) {
-                fc = fast_cell<T>(g, S.cm, xi, xf);
-                fcp = &fc;
-                warp_exact_jets<T>(g, S, xi, valid && !fc.ok, DERIV, ej);
-                ejp = &ej;
-            }
-            WarpSink<NV, T> sink{acc + warp * NV, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
-            if constexpr (DERIV) {
-                contact_force_jacobian<T, WarpSink<NV, T>, BR>(g, xi, S, fcp, sink, valid, STENCIL, ejp, kWarpExact);
-            } else {
-                ContactForce<T> F = contact_force<T, BR>(g, xi, S, fcp, valid, STENCIL, ejp);
-                sink.force(F.xi1, F.f1, F.xi2, F.f2);
-            }
+            sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - sm.prefix[lo])];
+            xi = load_point(sm.P, sid);
+            if constexpr (kWarpExact) xf = load_point32(sm.P, sid);
+        }
+        FastCell fc;
+        const FastCell* fcp = nullptr;
+        ExactJet<T> ej;
+        const ExactJet<T>* ejp = nullptr;
+        if constexpr (kWarpExact) {
+            fc = fast_cell<T>(sm.g, sm.S.cm, xi, xf);
+            fcp = &fc;
+            warp_exact_jets<T>(sm.g, sm.S, xi, valid && !fc.ok, DERIV, ej);
+            ejp = &ej;
+        }
+        WarpSink<NV, T> sink{sm.acc + warp * NV, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
+        if constexpr (DERIV) {
+            contact_force_jacobian<T, WarpSink<NV, T>, BR>(sm.g, xi, sm.S, fcp, sink, valid, STENCIL, ejp,
+                                                           kWarpExact);
+        } else {
+            ContactForce<T> F = contact_force<T, BR>(sm.g, xi, sm.S, fcp, valid, STENCIL, ejp);
+            sink.force(F.xi1, F.f1, F.xi2, F.f2);
         }
     }
-    __syncthreads();
-    double* row = partial + ((size_t)i * slots + s) * kOutDeriv;  // one row stride for both passes
+}
+
+// An item's partial row (one row stride for both passes) from the warps' accumulators, merged in
+// a fixed order.  CLEAR: each accumulator is read by one thread, which clears it for the next
+// item.
+template <bool DERIV, typename T, bool CLEAR>
+__device__ __forceinline__ void force_item_row(ForceSmem<DERIV, T>& sm, double* __restrict__ row, int tid) {
+    constexpr int NV = ForceSmem<DERIV, T>::NV, NW = ForceSmem<DERIV, T>::NW;
     for (int k = tid; k < NV; k += kChunk) {
         const int a = acc_index(k);
         double v;
         if constexpr (std::is_same<T, float>::value) {
             // the warps' pairs merged in FP32 (one conversion per value on the FP64 pipe)
-            Accum<float> m = acc[a];
-            for (int w = 1; w < NW; ++w) m.merge(acc[w * NV + a]);
+            Accum<float> m = sm.acc[a];
+            if (CLEAR) sm.acc[a].zero();
+            for (int w = 1; w < NW; ++w) {
+                m.merge(sm.acc[w * NV + a]);
+                if (CLEAR) sm.acc[w * NV + a].zero();
+            }
             v = m.value();
         } else {
             v = 0.0;
-            for (int w = 0; w < NW; ++w) v += acc[w * NV + a].value();
+            for (int w = 0; w < NW; ++w) {
+                v += sm.acc[w * NV + a].value();
+                if (CLEAR) sm.acc[w * NV + a].zero();
+            }
         }
         row[k] = v;
     }
 }
 
-// Resident one-warp force workers per SM: the FP32 path within 128 registers, the FP64 path
-// within 255.
-template <typename T>
-constexpr int worker_min_blocks() {
-    return std::is_same<T, float>::value ? 16 : 8;
+// The grid form (kForceGrid): CTA (s, i) = (blockIdx.x, blockIdx.y) sums share s of instance i
+// (chunks s, s + S, ..., S its spread) into the share's partial row; CTAs past the spread return
+// at once.  BR = false: the FP32 fast path specialised for grids with the FP32 cell-corner array
+// (storages 0 and 1); BR = true serves every storage.  skip: 0 none, 1 instances on grids
+// without the cell-corner array, 2 instances on grids with it (when a batch has both kinds,
+// the two instantiations split its instances).
+template <bool DERIV, bool STENCIL, typename T, bool BR = true>
+__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(
+    const InstanceDesc* __restrict__ inst, const int* __restrict__ mode, const GridDesc* __restrict__ grids,
+    const PointsDesc* __restrict__ points, const int* __restrict__ ids, const int* __restrict__ tile_count,
+    const int* __restrict__ inst_total, const PairState<T>* __restrict__ pairs, double* __restrict__ partial, int skip,
+    int slots, int per) {
+    constexpr int NV = ForceSmem<DERIV, T>::NV, NW = ForceSmem<DERIV, T>::NW;
+    __shared__ ForceSmem<DERIV, T> sm;
+    const int i = blockIdx.y, s = blockIdx.x;
+    if (mode && mode[i] != (DERIV ? 2 : 1)) return;  // not requested in this pass
+    const int shares = spread_of(inst_total[i], kChunk, per, slots);
+    if (s >= shares) return;  // uniform over the CTA
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const InstanceDesc I = inst[i];
+    if (skip && (grids[I.grid].cells32 == nullptr) == (skip == 1)) return;  // the other instantiation's instance
+    force_item_setup<DERIV, T>(sm, I, i, grids, points, tile_count, pairs, warp, lane);
+    for (int k = tid; k < NW * NV; k += kChunk) sm.acc[k].zero();
+    __syncthreads();
+    force_item_chunks<DERIV, STENCIL, T, BR>(sm, I, s, shares, ids, tid, lane, warp);
+    __syncthreads();
+    force_item_row<DERIV, T, false>(sm, partial + ((size_t)i * slots + s) * kOutDeriv, tid);
 }
 
-// Force pass by persistent one-warp workers (kForceWorkers).  Item q of the queue is (instance
-// q / slots, slot q % slots); the slot takes the instance's 32-contact chunks s, s + slots, ...
-// in order and writes its own partial row, so the sums do not depend on which worker took the
-// item.  queue: the pass's counter, zeroed by prep_kernel.  Dynamic shared memory: the prefix of
-// the instance's tile counts, max_ntiles + 1 ints.
+// The queue form (kForceCtas): persistent CTAs, each taking the next item of its launch's list
+// (queue: the launch's counter, list_n: the list's length) until the list is exhausted.  The
+// next item is fetched while the current one runs (two item slots), and the row epilogue clears
+// the accumulators, so an item costs two CTA barriers.
+template <bool DERIV, bool STENCIL, typename T, bool BR = true>
+__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_queue_kernel(
+    const InstanceDesc* __restrict__ inst, const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
+    const int* __restrict__ ids, const int* __restrict__ tile_count, const int* __restrict__ inst_total,
+    const PairState<T>* __restrict__ pairs, double* __restrict__ partial, int slots, int per,
+    const int* __restrict__ items, const int* __restrict__ list_n, int* __restrict__ queue) {
+    constexpr int NV = ForceSmem<DERIV, T>::NV, NW = ForceSmem<DERIV, T>::NW;
+    static_assert(kChunk >= 64 && kChunk % 32 == 0, "warps 0 and 1 set an item up");
+    constexpr int kFetcher = kChunk > 64 ? 64 : 0;  // the thread that fetches items (warp 2's first)
+    __shared__ ForceSmem<DERIV, T> sm;
+    __shared__ int item[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n_items = *list_n;
+    auto fetch = [&]() {
+        const int q = atomicAdd(queue, 1);
+        return q < n_items ? items[q] : -1;
+    };
+    if (tid == 0) item[0] = fetch();
+    for (int k = tid; k < NW * NV; k += kChunk) sm.acc[k].zero();
+    __syncthreads();
+    for (int it = 0;; it ^= 1) {
+        // item[it] was written before the previous item's second barrier (or the one above)
+        const int e = item[it];
+        if (e < 0) break;  // uniform over the CTA
+        const int i = e / kMaxSlots, s = e % kMaxSlots;
+        const int shares = spread_of(inst_total[i], kChunk, per, slots);
+        const InstanceDesc I = inst[i];
+        // the next item, fetched now and stored before this item's second barrier (item[it ^ 1]
+        // was last read before the previous item's first barrier)
+        int pending = -1;
+        if (tid == kFetcher) pending = fetch();
+        // the prefix and the descriptors were last read before the previous item's second barrier
+        force_item_setup<DERIV, T>(sm, I, i, grids, points, tile_count, pairs, warp, lane);
+        __syncthreads();
+        force_item_chunks<DERIV, STENCIL, T, BR>(sm, I, s, shares, ids, tid, lane, warp);
+        if (tid == kFetcher) item[it ^ 1] = pending;
+        __syncthreads();
+        force_item_row<DERIV, T, true>(sm, partial + ((size_t)i * slots + s) * kOutDeriv, tid);
+    }
+}
+
+// Resident one-warp force workers per SM: the FP32 path within 65536 / (32 x this) registers
+// (a compile-time tuning knob, 16: 128 registers), the FP64 path within 255.
+#ifndef SDFC_WORKER_MIN_BLOCKS
+#define SDFC_WORKER_MIN_BLOCKS 16
+#endif
+template <typename T>
+constexpr int worker_min_blocks() {
+    return std::is_same<T, float>::value ? SDFC_WORKER_MIN_BLOCKS : 8;
+}
+
+// Force pass by persistent one-warp workers (kForceWorkers), over the same item lists as
+// force_queue_kernel: item (i, s) takes instance i's 32-contact chunks s, s + S, ... in order and
+// writes its own partial row, so the sums do not depend on which worker took the item.
+// Dynamic shared memory: the prefix of the instance's tile counts, max_ntiles + 1 ints.
 template <bool DERIV, bool STENCIL, typename T, bool BR = true>
 __global__ void __launch_bounds__(32, worker_min_blocks<T>()) force_worker_kernel(
-    const InstanceDesc* __restrict__ inst, int n_inst, BatchInputs in, const GridDesc* __restrict__ grids,
+    const InstanceDesc* __restrict__ inst, const GridDesc* __restrict__ grids,
     const PointsDesc* __restrict__ points, const int* __restrict__ ids, const int* __restrict__ tile_count,
-    const PairState<T>* __restrict__ pairs, double* __restrict__ partial, int skip, int slots, int* __restrict__ queue) {
+    const int* __restrict__ inst_total, const PairState<T>* __restrict__ pairs, double* __restrict__ partial,
+    int slots, int per, const int* __restrict__ items, const int* __restrict__ list_n, int* __restrict__ queue) {
     constexpr int NV = DERIV ? kOutDeriv : kOutValue;
     constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
     __shared__ Accum<T> acc[NV];
@@ -701,16 +844,25 @@ __global__ void __launch_bounds__(32, worker_min_blocks<T>()) force_worker_kerne
     __shared__ PairState<T> S;
     extern __shared__ int prefix[];
     const int lane = threadIdx.x;
-    const int n_items = n_inst * slots;
+    const int n_items = *list_n;
+    // lane 0 fetches the next item while the warp runs the current one; the warp reads it at
+    // the top of the next round
+    auto fetch = [&]() {
+        int e = -1;
+        if (lane == 0) {
+            const int q = atomicAdd(queue, 1);
+            if (q < n_items) e = items[q];
+        }
+        return e;
+    };
+    int pending = fetch();
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(queue, 1);
-        item = __shfl_sync(kFull, item, 0);
-        if (item >= n_items) break;
-        const int i = item / slots, s = item - (item / slots) * slots;
-        if (in.mode && in.mode[i] != (DERIV ? 2 : 1)) continue;  // not requested in this pass
+        const int e = __shfl_sync(kFull, pending, 0);
+        if (e < 0) break;
+        pending = fetch();
+        const int i = e / kMaxSlots, s = e % kMaxSlots;
+        const int shares = spread_of(inst_total[i], 32, per, slots);
         const InstanceDesc I = inst[i];
-        if (skip && (grids[I.grid].cells32 == nullptr) == (skip == 1)) continue;  // the other instantiation's
         __syncwarp();  // the previous item's reads of the shared state are done
         {
             int run = 0;
@@ -734,7 +886,7 @@ __global__ void __launch_bounds__(32, worker_min_blocks<T>()) force_worker_kerne
         __syncwarp();
         const int total = prefix[I.ntiles];
         const int nchunks = (total + 31) >> 5;
-        for (int chunk = s; chunk < nchunks; chunk += slots) {
+        for (int chunk = s; chunk < nchunks; chunk += shares) {
             const int c = chunk * 32 + lane;
             const bool valid = c < total;
             V3 xi = v3(0, 0, 0);
@@ -777,8 +929,9 @@ __global__ void __launch_bounds__(32, worker_min_blocks<T>()) force_worker_kerne
 }
 
 // Penetration energy of every instance (sum over its active contacts of kn d^2 / 2) and its
-// gradient wrt both bodies' twist coordinates; one CTA per (instance, slot) like force_kernel,
-// partial row = [e, dE/dq_A (w, v), dE/dq_B (w, v)] (kOutEnergy values).
+// gradient wrt both bodies' twist coordinates; one CTA per (instance, share) for every share up
+// to the cap (the CTAs past the instance's spread, from spread_of with chunks of kChunk, return
+// at once), partial row = [e, dE/dq_A (w, v), dE/dq_B (w, v)] (kOutEnergy values).
 template <bool STENCIL, typename T>
 __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(const InstanceDesc* __restrict__ inst,
                                                         BatchInputs in, const GridDesc* __restrict__ grids,
@@ -786,7 +939,8 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
                                                         const int* __restrict__ ids,
                                                         const int* __restrict__ tile_count,
                                                         const PairState<T>* __restrict__ pairs,
-                                                        double* __restrict__ partial, int slots) {
+                                                        double* __restrict__ partial, int slots, int per,
+                                                        const int* __restrict__ inst_total) {
     constexpr int NW = kChunk / 32;
     constexpr bool kWarpExact = std::is_same<T, float>::value && !STENCIL;
     __shared__ Accum<T> acc[NW * 12];
@@ -797,6 +951,8 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
     __shared__ PairState<T> S;
     const int i = blockIdx.y, s = blockIdx.x;
     if (in.mode && in.mode[i] == 0) return;
+    const int shares = spread_of(inst_total[i], kChunk, per, slots);
+    if (s >= shares) return;  // uniform over the CTA
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const InstanceDesc I = inst[i];
     if (warp == 0) {
@@ -823,7 +979,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
     __syncthreads();
     const int total = prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
-    for (int chunk = s; chunk < nchunks; chunk += slots) {
+    for (int chunk = s; chunk < nchunks; chunk += shares) {
         if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
         const int c = chunk * kChunk + tid;
         const bool valid = c < total;
@@ -874,14 +1030,16 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
 }
 
 __global__ void energy_finalize_kernel(int n_inst, const double* __restrict__ partial, double* __restrict__ energy,
-                                       double* __restrict__ dE, const int* __restrict__ mode, int slots) {
+                                       double* __restrict__ dE, const int* __restrict__ mode, int slots, int per,
+                                       const int* __restrict__ inst_total) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)n_inst * kOutEnergy) return;
     const int i = (int)(idx / kOutEnergy), k = (int)(idx % kOutEnergy);
     if (mode && mode[i] == 0) return;
     const double* p = partial + (size_t)i * slots * kOutDeriv + k;
+    const int shares = spread_of(inst_total[i], kChunk, per, slots);
     double v = 0.0;
-    for (int s = 0; s < slots; ++s) v += p[(size_t)s * kOutDeriv];
+    for (int s = 0; s < shares; ++s) v += p[(size_t)s * kOutDeriv];
     if (k == 0)
         energy[i] = v;
     else
@@ -913,12 +1071,12 @@ __device__ inline double adjoint_entry(const double* EA, const double* EB, int r
     return t[a1] * q(a2, c) - t[a2] * q(a1, c);
 }
 
-// One CTA per instance: the instance's slots partial rows summed in order into shared
-// memory, then written out.  EA / EB not null: the dq2 columns of Km and the dphi2 columns
+// One CTA per instance: the instance's partial rows (one per share: spread_of with the force
+// pass's chunk, chunks per share and cap) summed in order into shared memory, then written out.  EA / EB not null: the dq2 columns of Km and the dphi2 columns
 // of Dm were not accumulated (force_kernel's skip_q2) and are derived here from the summed
 // dq1 / dphi1 columns; the partial rows' dq2 slots of Km then hold C (Dm's correction).
 template <bool DERIV>
-__global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_inst, const int* __restrict__ tile_count,
+__global__ void finalize_kernel(int n_inst, const int* __restrict__ inst_total, int chunk, int per,
                                 const double* __restrict__ partial, BatchOutputs out, const int* __restrict__ mode,
                                 const double* __restrict__ EA, const double* __restrict__ EB, int slots,
                                 bool set_status, const int* __restrict__ badin) {
@@ -929,9 +1087,10 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
     if (i >= n_inst || (mode && mode[i] != (DERIV ? 2 : 1))) return;  // uniform over the CTA
     if (out.dev) out = *out.dev;
     const double* p = partial + (size_t)i * slots * kOutDeriv;
+    const int shares = spread_of(inst_total[i], chunk, per, slots);
     if (k < NV) {
         double v = 0.0;
-        for (int s = 0; s < slots; ++s) v += p[(size_t)s * kOutDeriv + k];
+        for (int s = 0; s < shares; ++s) v += p[(size_t)s * kOutDeriv + k];
         tot[k] = v;
     }
     const bool derive = DERIV && EA != nullptr;
@@ -965,10 +1124,7 @@ __global__ void finalize_kernel(const InstanceDesc* __restrict__ inst, int n_ins
             out.status[i] = st;
         else if (st)
             out.status[i] = st;
-        const InstanceDesc I = inst[i];
-        int n = 0;
-        for (int t = 0; t < I.ntiles; ++t) n += tile_count[I.tile0 + t];
-        out.n_active[i] = n;
+        out.n_active[i] = inst_total[i];
     }
 }
 
@@ -989,55 +1145,80 @@ __global__ void gather_inputs_kernel(const HostIO* __restrict__ io, double* __re
     }
 }
 
-// force_worker_kernel<DERIV, STENCIL, T, BR> on s.worker_ctas one-warp CTAs.  Each launch of an
-// evaluation has its own queue: recheck_n[1 + 2 (value pass) + (general-storage kernel)].
+// CTAs of `kernel` (block `threads`, dynamic shared memory `smem`) resident on the device at
+// once: the persistent force passes launch this many (looked up once per kernel).
+template <typename K>
+int resident_ctas(K kernel, int threads, size_t smem, std::atomic<int>& cache) {
+    int c = cache.load(std::memory_order_relaxed);
+    if (c > 0) return c;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    c = per_sm * device_sm_count();
+    cache.store(c, std::memory_order_relaxed);
+    return c;
+}
+
+// Contacts per chunk of the batch's force-pass form.
+int chunk_of(const BatchScratch& s) { return s.force_variant == kForceWorkers ? 32 : kChunk; }
+
+// One force launch: for the queue forms over list `l` (BatchScratch::recheck_n),
+// force_queue_kernel on persistent CTAs (as many as the SMs hold) or force_worker_kernel on
+// s.worker_ctas one-warp CTAs (0: as many as the SMs hold); for the grid form force_kernel on
+// (slots, n) CTAs with `skip` (force_kernel).
 template <bool DERIV, bool STENCIL, typename T, bool BR>
-void launch_workers(int n_inst, cudaStream_t stream, const InstanceDesc* d_inst, BatchInputs in,
-                    const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s,
-                    const PairState<T>* pairs, int skip) {
-    int* queue = s.recheck_n + 1 + (DERIV ? 0 : 2) + (BR ? 1 : 0);
-    const size_t smem = sizeof(int) * ((size_t)s.max_ntiles + 1);
-    const int ctas = s.worker_ctas > 0 ? s.worker_ctas : device_sm_count() * worker_min_blocks<T>();
-    force_worker_kernel<DERIV, STENCIL, T, BR><<<ctas, 32, smem, stream>>>(
-        d_inst, n_inst, in, d_grids, d_points, s.ids, s.tile_count, pairs, s.partial, skip, s.slots, queue);
+void launch_list(int n_inst, int l, int skip, cudaStream_t stream, const InstanceDesc* d_inst, const int* mode,
+                 const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s,
+                 const PairState<T>* pairs) {
+    const int per = std::max(s.chunks_per_slot, 1);
+    if (s.force_variant == kForceGrid) {
+        force_kernel<DERIV, STENCIL, T, BR><<<dim3(s.slots, n_inst), kChunk, 0, stream>>>(
+            d_inst, mode, d_grids, d_points, s.ids, s.tile_count, s.inst_total, pairs, s.partial, skip, s.slots, per);
+        return;
+    }
+    int* queue = s.recheck_n + 1 + l;
+    const int* list_n = s.recheck_n + 5 + l;
+    const int* items = s.items + (size_t)l * n_inst * s.slots;
+    const long long most = (long long)n_inst * s.slots;  // items in the list, at most
+    if (s.force_variant == kForceWorkers) {
+        const size_t smem = sizeof(int) * ((size_t)s.max_ntiles + 1);
+        int ctas = s.worker_ctas > 0 ? s.worker_ctas : device_sm_count() * worker_min_blocks<T>();
+        ctas = (int)std::min<long long>(ctas, most);
+        force_worker_kernel<DERIV, STENCIL, T, BR><<<ctas, 32, smem, stream>>>(
+            d_inst, d_grids, d_points, s.ids, s.tile_count, s.inst_total, pairs, s.partial, s.slots, per, items,
+            list_n, queue);
+    } else {
+        static std::atomic<int> cache{0};
+        const int ctas = (int)std::min<long long>(
+            resident_ctas(force_queue_kernel<DERIV, STENCIL, T, BR>, kChunk, 0, cache), most);
+        force_queue_kernel<DERIV, STENCIL, T, BR><<<ctas, kChunk, 0, stream>>>(
+            d_inst, d_grids, d_points, s.ids, s.tile_count, s.inst_total, pairs, s.partial, s.slots, per, items,
+            list_n, queue);
+    }
+}
+
+// Whether the FP32 fast path splits a batch's instances between the cell-corner specialisation
+// and the general kernel (both storages present).
+bool splits(bool stencil, int precision, bool plain, bool bricks) {
+    return precision == kMixed && !stencil && plain && bricks;
 }
 
 template <bool DERIV, bool STENCIL>
-void launch_force_t(dim3 grid, int n_inst, int precision, cudaStream_t stream, const InstanceDesc* d_inst,
-                    BatchInputs in, const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s,
-                    bool plain, bool bricks) {
-    if (s.force_variant == kForceWorkers) {
-        if (precision == kMixed && !STENCIL) {
-            if (plain)
-                launch_workers<DERIV, STENCIL, float, false>(n_inst, stream, d_inst, in, d_grids, d_points, s,
-                                                             s.pair32, bricks ? 1 : 0);
-            if (bricks)
-                launch_workers<DERIV, STENCIL, float, true>(n_inst, stream, d_inst, in, d_grids, d_points, s,
-                                                            s.pair32, plain ? 2 : 0);
-        } else if (precision == kMixed) {
-            launch_workers<DERIV, STENCIL, float, true>(n_inst, stream, d_inst, in, d_grids, d_points, s, s.pair32,
-                                                        0);
-        } else {
-            launch_workers<DERIV, STENCIL, double, true>(n_inst, stream, d_inst, in, d_grids, d_points, s, s.pair64,
-                                                         0);
-        }
-        return;
-    }
+void launch_force_t(int n_inst, int precision, cudaStream_t stream, const InstanceDesc* d_inst, const int* mode,
+                    const GridDesc* d_grids, const PointsDesc* d_points, const BatchScratch& s, bool plain,
+                    bool bricks) {
+    const int l = DERIV ? 0 : 2;
     if (precision == kMixed && !STENCIL) {  // the FP32 fast path: specialised for brick-free grids
         if (plain)
-            force_kernel<DERIV, STENCIL, float, false><<<grid, kChunk, 0, stream>>>(
-                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.pair32, s.partial, bricks ? 1 : 0, s.slots);
+            launch_list<DERIV, STENCIL, float, false>(n_inst, l, bricks ? 1 : 0, stream, d_inst, mode, d_grids,
+                                                      d_points, s, s.pair32);
         if (bricks)
-            force_kernel<DERIV, STENCIL, float, true><<<grid, kChunk, 0, stream>>>(
-                d_inst, in, d_grids, d_points, s.ids, s.tile_count, s.pair32, s.partial, plain ? 2 : 0, s.slots);
+            launch_list<DERIV, STENCIL, float, true>(n_inst, plain ? l + 1 : l, plain ? 2 : 0, stream, d_inst, mode,
+                                                     d_grids, d_points, s, s.pair32);
     } else if (precision == kMixed) {
-        force_kernel<DERIV, STENCIL, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                         s.tile_count, s.pair32, s.partial, 0,
-                                                                         s.slots);
+        launch_list<DERIV, STENCIL, float, true>(n_inst, l, 0, stream, d_inst, mode, d_grids, d_points, s, s.pair32);
     } else {
-        force_kernel<DERIV, STENCIL, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                          s.tile_count, s.pair64, s.partial, 0,
-                                                                          s.slots);
+        launch_list<DERIV, STENCIL, double, true>(n_inst, l, 0, stream, d_inst, mode, d_grids, d_points, s, s.pair64);
     }
 }
 
@@ -1059,20 +1240,23 @@ void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_ins
                    bool plain, bool bricks) {
     if (n_inst <= 0) return;
     prep_kernel<<<dim3((n_inst + 31) / 32, 3), 32, 0, stream>>>(d_inst, n_inst, in, d_grids, d_points, s.prefilter,
-                                                                s.pair32, s.pair64, s.recheck_n, s.badin);
+                                                                s.pair32, s.pair64, s.recheck_n, s.badin,
+                                                                s.inst_total);
     if (total_tiles <= 0) return;
     if (plain)
         detect_kernel<false><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
                                                                          d_points, s.ids, s.tile_count, s.tile_queue,
-                                                                         in.mode, s.recheck_list, s.recheck_n);
+                                                                         in.mode, s.recheck_list, s.recheck_n,
+                                                                         s.inst_total);
     if (bricks)
         detect_kernel<true><<<total_tiles, kDetectThreads, 0, stream>>>(d_inst, d_tile_inst, s.prefilter, d_grids,
                                                                         d_points, s.ids, s.tile_count, s.tile_queue,
-                                                                        in.mode, s.recheck_list, s.recheck_n);
+                                                                        in.mode, s.recheck_list, s.recheck_n,
+                                                                        s.inst_total);
     // one warp per listed tile, up to 16 warps per SM (the list is only known on the device)
     recheck_kernel<<<std::min(total_tiles, device_sm_count() * 16), 32, 0, stream>>>(d_inst, d_tile_inst, in, d_grids, d_points,
                                                                        s.ids, s.tile_count, s.tile_queue, s.recheck,
-                                                                       s.recheck_list, s.recheck_n);
+                                                                       s.recheck_list, s.recheck_n, s.inst_total);
 }
 
 void launch_distance(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
@@ -1096,29 +1280,36 @@ void launch_grid_query(const GridDesc* d_grids, int grid, const double* X, int n
     if (min_d) distance_finalize_kernel<<<1, 32, 0, stream>>>(key_scratch, min_d, 1);
 }
 
+void launch_plan(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids, BatchScratch s,
+                 bool deriv, bool stencil, int precision, cudaStream_t stream, bool plain, bool bricks) {
+    if (n_inst <= 0 || s.force_variant == kForceGrid) return;  // the grid form takes no list
+    plan_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(d_inst, n_inst, in.mode, deriv ? 1 : 0, d_grids,
+                                                          splits(stencil, precision, plain, bricks) ? 1 : 0,
+                                                          chunk_of(s), std::max(s.chunks_per_slot, 1), s.slots,
+                                                          s.inst_total, s.items, s.recheck_n);
+}
+
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,
                   cudaStream_t stream, bool plain, bool bricks) {
     if (n_inst <= 0) return;
-    dim3 grid(s.slots, n_inst);
+    const int* m = in.mode;
     if (deriv) {
         if (stencil)
-            launch_force_t<true, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain, bricks);
+            launch_force_t<true, true>(n_inst, precision, stream, d_inst, m, d_grids, d_points, s, plain, bricks);
         else
-            launch_force_t<true, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain,
-                                        bricks);
+            launch_force_t<true, false>(n_inst, precision, stream, d_inst, m, d_grids, d_points, s, plain, bricks);
     } else {
         if (stencil)
-            launch_force_t<false, true>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain,
-                                        bricks);
+            launch_force_t<false, true>(n_inst, precision, stream, d_inst, m, d_grids, d_points, s, plain, bricks);
         else
-            launch_force_t<false, false>(grid, n_inst, precision, stream, d_inst, in, d_grids, d_points, s, plain,
-                                         bricks);
+            launch_force_t<false, false>(n_inst, precision, stream, d_inst, m, d_grids, d_points, s, plain, bricks);
     }
 }
 
 void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, bool deriv, BatchOutputs out,
                      cudaStream_t stream, const int* mode, bool zero_status, const BatchInputs* derive_q2) {
+    (void)d_inst;
     if (n_inst <= 0) return;
     // without a request mask every instance is finalized here, which then sets each status
     // outright; with one, the statuses are cleared first and each pass sets its instances' flags
@@ -1126,12 +1317,13 @@ void launch_finalize(const InstanceDesc* d_inst, int n_inst, BatchScratch s, boo
     if (zero_status && mode) zero_status_kernel<<<(n_inst + 255) / 256, 256, 0, stream>>>(out, n_inst);
     const double* EA = derive_q2 ? derive_q2->EA : nullptr;
     const double* EB = derive_q2 ? derive_q2->EB : nullptr;
+    const int per = std::max(s.chunks_per_slot, 1);
     if (deriv)
-        finalize_kernel<true><<<n_inst, 320, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode, EA, EB,
-                                                          s.slots, set_status, s.badin);
+        finalize_kernel<true><<<n_inst, 320, 0, stream>>>(n_inst, s.inst_total, chunk_of(s), per, s.partial, out, mode,
+                                                          EA, EB, s.slots, set_status, s.badin);
     else
-        finalize_kernel<false><<<n_inst, 64, 0, stream>>>(d_inst, n_inst, s.tile_count, s.partial, out, mode,
-                                                          nullptr, nullptr, s.slots, set_status, s.badin);
+        finalize_kernel<false><<<n_inst, 64, 0, stream>>>(n_inst, s.inst_total, chunk_of(s), per, s.partial, out,
+                                                          mode, nullptr, nullptr, s.slots, set_status, s.badin);
 }
 
 void launch_zero_status(BatchOutputs out, int n_inst, cudaStream_t stream) {
@@ -1150,20 +1342,24 @@ void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const
                    const PointsDesc* d_points, BatchScratch s, bool stencil, int precision, cudaStream_t stream) {
     if (n_inst <= 0) return;
     dim3 grid(s.slots, n_inst);
+    const int per = std::max(s.chunks_per_slot, 1);
     if (precision == kMixed) {
         if (stencil)
             energy_kernel<true, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids, s.tile_count,
-                                                                     s.pair32, s.partial, s.slots);
+                                                                     s.pair32, s.partial, s.slots, per, s.inst_total);
         else
             energy_kernel<false, float><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                      s.tile_count, s.pair32, s.partial, s.slots);
+                                                                      s.tile_count, s.pair32, s.partial, s.slots, per,
+                                                                      s.inst_total);
     } else {
         if (stencil)
             energy_kernel<true, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                      s.tile_count, s.pair64, s.partial, s.slots);
+                                                                      s.tile_count, s.pair64, s.partial, s.slots, per,
+                                                                      s.inst_total);
         else
             energy_kernel<false, double><<<grid, kChunk, 0, stream>>>(d_inst, in, d_grids, d_points, s.ids,
-                                                                       s.tile_count, s.pair64, s.partial, s.slots);
+                                                                       s.tile_count, s.pair64, s.partial, s.slots, per,
+                                                                       s.inst_total);
     }
 }
 
@@ -1171,8 +1367,8 @@ void launch_energy_finalize(int n_inst, BatchScratch s, double* energy, double* 
                             cudaStream_t stream) {
     if (n_inst <= 0) return;
     const size_t total = (size_t)n_inst * kOutEnergy;
-    energy_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(n_inst, s.partial, energy, dE, mode,
-                                                                                s.slots);
+    energy_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(
+        n_inst, s.partial, energy, dE, mode, s.slots, std::max(s.chunks_per_slot, 1), s.inst_total);
 }
 
 }  // namespace sdfc

@@ -18,26 +18,33 @@
 //                    ones to the tile's list in ascending order.
 //                    Detection as a whole restates
 //                    simulation/redmax/CollisionDetection/CollisionDetection.cpp:124-147.
-//   force_kernel     one CTA per (instance, slot).  The instance's active
-//                    contacts are cut into chunks of kChunk; slot s takes chunks
-//                    s, s+slots, ...  Each thread evaluates one contact; the
+//   plan_kernel      (queue forms) one thread per instance: its items (instance, share
+//                    0..S-1), appended to the item list of its force launch.  S, the
+//                    instance's spread, is the number of partial sums it is cut into: its
+//                    active contacts (counted by detection) over the tuned contacts per share,
+//                    at most `slots` (spread_of).
+//   force_kernel     one CTA per (instance, share) (the grid form), or persistent CTAs taking
+//                    items from the list (force_queue_kernel).  An instance's active contacts
+//                    are cut into chunks of kChunk; share s takes chunks s, s+S, ...  Each
+//                    thread evaluates one contact; the
 //                    per-contact force (12 values) and, with derivatives, the
 //                    Jacobian columns (24 on the FP64 path; 15 on the FP32 path,
 //                    which leaves body B's twist columns to finalize_kernel) are
 //                    summed over the warp with shuffles and over the CTA's warps
 //                    in shared memory, in a fixed order, into one partial row per
-//                    (instance, slot).
+//                    (instance, share).
 //                    On the FP32 path a contact whose derivative stencil could
 //                    leave its cell takes the exact path (the reference's FP64
 //                    stencil); the warp evaluates such contacts' 19 stencil
 //                    queries together, one contact at a time across its lanes
 //                    (warp_exact_jets), so that no lane runs the long FP64
 //                    stencil alone while 31 wait.
-//   finalize_kernel  one CTA per instance: sums its slots partial rows in order,
+//   finalize_kernel  one CTA per instance: sums its S partial rows in order,
 //                    derives the FP32 path's body-B columns (Km: -Km1 Ad; Dm:
 //                    -Dm1 Ad + C) and writes fm / Km / Dm, n_active and status.
 //
-// No atomics touch the results: the sums are deterministic run to run.
+// No atomics touch the results: which CTA takes an item does not change its sums, so they are
+// deterministic run to run (the contact counts are integer atomic sums, exact in any order).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -58,19 +65,21 @@ constexpr int kDetectThreads = 256;  // threads per detection CTA
 #endif
 constexpr int kChunk = SDFC_FORCE_CHUNK;
 constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
-constexpr int kMaxSlots = 32;        // partial rows per instance (force CTAs per instance), at most
+constexpr int kMaxSlots = 32;        // partial rows per instance, at most
 // Multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked up once per
 // device): launch shapes follow it.
 int device_sm_count();
-// Default slots of a batch of n instances on a device with `sms` multiprocessors: about six
-// waves of force CTAs (measured on GB300: 4 for 1024 instances of 50k points, 16 for 256 of 1M).
-// A batch's tuning (sdfc_batch_autotune) may replace it.
-inline int slots_for(int n, int sms) {
-    const long long target = (long long)sms * kForceCtasPerSm * 6;
-    int s = 1;
-    while (s < kMaxSlots && (long long)s * n < target) s *= 2;
+// Default cap on an instance's partial sums for a batch of n instances: kMaxSlots, lowered so
+// that the partial-row buffer (n x slots rows of kOutDeriv doubles) stays within 2^18 rows
+// (630 MB).  An instance takes as many shares as its active contacts fill, up to the cap.
+inline int slots_for(int n) {
+    int s = kMaxSlots;
+    while (s > 1 && (long long)s * n > (1LL << 18)) s /= 2;
     return s;
 }
+// Default chunks per share (sdfc_tuning::chunks_per_slot): an instance with c chunks of active
+// contacts is cut into min(slots, ceil(c / this)) shares.
+constexpr int kDefaultChunksPerSlot = 4;
 constexpr int kMaxTilesPerInstance = 4096;
 constexpr int kOutDeriv = 300;       // fm (12) + Km (144) + Dm (144)
 constexpr int kOutValue = 12;
@@ -85,14 +94,17 @@ struct HullDesc {
     double lo[3], hi[3];
 };
 
-// The two forms of the force pass (a batch's tuning picks one; both sum each instance's contacts
-// into `slots` partial rows in a fixed order, so each is deterministic):
-//   kForceCtas    force_kernel: one CTA of kChunk threads per (instance, slot), chunks of kChunk
-//                 contacts, the CTA's warps merged at the end;
-//   kForceWorkers force_worker_kernel: persistent one-warp CTAs, as many as the SMs hold, taking
-//                 (instance, slot) items from a queue, chunks of 32 contacts.  No CTA barrier: a
-//                 warp that finishes an item takes the next instead of waiting for its CTA.
-enum ForceVariant { kForceCtas = 0, kForceWorkers = 1 };
+// The three forms of the force pass (a batch's tuning picks one; each sums each (instance,
+// share) into its own partial row in a fixed order, so each is deterministic):
+//   kForceCtas    force_queue_kernel: persistent CTAs of kChunk threads taking the items of
+//                 plan_kernel's list from a queue, chunks of kChunk contacts, the CTA's warps
+//                 merged at the end of each item;
+//   kForceWorkers force_worker_kernel: persistent one-warp CTAs, chunks of 32 contacts.  No CTA
+//                 barrier: a warp that finishes an item takes the next instead of waiting for
+//                 its CTA.
+//   kForceGrid    force_kernel: one CTA per (instance, share) for every share up to `slots`
+//                 (CTAs past an instance's spread return at once), no list, no queue.
+enum ForceVariant { kForceCtas = 0, kForceWorkers = 1, kForceGrid = 2 };
 
 // Fixed topology of one batch instance.
 struct InstanceDesc {
@@ -157,19 +169,24 @@ struct BatchScratch {
     int* tile_queue;            // total_tiles: queued recheck count per tile
     double* partial;            // n x slots x kOutDeriv
     unsigned long long* recheck;  // diagnostic counter of FP64 rechecks
-    int slots;                  // force CTAs (partial rows) per instance
+    int slots;                  // partial rows per instance, at most (the spread's cap)
     PairState<float>* pair32;   // n: each instance's pair state for the FP32 kernels (written by prep_kernel)
     PairState<double>* pair64;  // n: the same for the FP64 kernels
     int* recheck_list;          // total_tiles: the tiles with queued points (appended by detect_kernel)
-    // 5 counters, reset by prep_kernel: [0] the count of recheck_list, [1..4] the work queues of the
-    // force workers (force_worker_kernel): derivative pass on cell-corner grids, on other grids,
-    // value pass on cell-corner grids, on other grids
+    // kCounters counters, reset by prep_kernel: [0] the count of recheck_list, [1..4] the queue
+    // forms' queues, [5..8] the lengths of their item lists (plan_kernel).  Lists / queues by
+    // launch: 0 derivative pass, 1 derivative pass on grids without the cell-corner array when the
+    // FP32 fast path splits the instances by storage, 2 / 3 the same for the value pass.
     int* recheck_n;
     int* badin = nullptr;            // n: 1 where the instance's inputs are not all finite (prep_kernel)
     int force_variant = kForceCtas;  // which force kernel runs (set by the batch's tuning)
     int worker_ctas = 0;             // force workers launched (0: the device's multiprocessors x resident)
     int max_ntiles = 0;              // most detection tiles of one instance (the workers' shared prefix)
+    int chunks_per_slot = kDefaultChunksPerSlot;  // chunks of active contacts per share, at least
+    int* inst_total = nullptr;  // n: active contacts per instance (zeroed by prep_kernel, summed by detection)
+    int* items = nullptr;       // 4 lists of n x slots items (instance x kMaxSlots + share), plan_kernel
 };
+constexpr int kCounters = 9;
 
 enum Precision { kFP64 = 0, kMixed = 1 };
 
@@ -178,6 +195,12 @@ enum Precision { kFP64 = 0, kMixed = 1 };
 void launch_detect(const InstanceDesc* d_inst, const int* d_tile_inst, int n_inst, int total_tiles, BatchInputs in,
                    const GridDesc* d_grids, const PointsDesc* d_points, BatchScratch s, cudaStream_t stream,
                    bool plain = true, bool bricks = true);
+
+// The force passes' item lists from detection's contact counts (after launch_detect, before
+// launch_force): without a request mask every instance goes to the pass `deriv` asks for, with
+// one (in.mode) each instance to the pass it requests.  One launch covers both passes.
+void launch_plan(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids, BatchScratch s,
+                 bool deriv, bool stencil, int precision, cudaStream_t stream, bool plain = true, bool bricks = true);
 
 void launch_force(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                   const PointsDesc* d_points, BatchScratch s, bool deriv, bool stencil, int precision,

@@ -1,9 +1,9 @@
 // Launch tuning of a batch's force pass (sdfc_batch_autotune): times each candidate
 // configuration on one evaluation of the caller's inputs and keeps the fastest, per batch
-// shape and context.  The candidates are the force-pass forms (CTAs per (instance, slot), or
-// persistent one-warp workers over a queue of such items) times the number of partial sums per
-// instance; the batch shape decides which wins (few large instances want many slots, many
-// small ones few; uneven instances favour the queue).
+// shape and context.  The candidates are the force-pass forms over the queue of (instance, share)
+// items (persistent 128-thread CTAs or one-warp workers) times the chunks per share, and the
+// grid of one CTA per (instance, share) times the shares per instance; the batch shape decides
+// which wins (even instances favour the grid, uneven ones the queue).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -15,6 +15,8 @@
 
 namespace {
 
+const char* const kVariantName[] = {"ctas", "workers", "grid"};
+
 // The shape a tuning is valid for.
 std::vector<long long> tune_key(const sdfc_batch* b, bool deriv, bool masked) {
     long long tiles = 0;
@@ -25,17 +27,24 @@ std::vector<long long> tune_key(const sdfc_batch* b, bool deriv, bool masked) {
 
 bool valid_tuning(const sdfc_tuning& t) {
     const bool pow2 = t.slots >= 1 && t.slots <= sdfc::kMaxSlots && (t.slots & (t.slots - 1)) == 0;
-    return pow2 && (t.force_variant == SDFC_FORCE_CTAS || t.force_variant == SDFC_FORCE_WORKERS) &&
-           t.worker_ctas >= 0;
+    return pow2 && t.force_variant >= SDFC_FORCE_CTAS && t.force_variant <= SDFC_FORCE_GRID && t.worker_ctas >= 0 &&
+           t.chunks_per_slot >= 1;
 }
 
 int apply(sdfc_batch* b, const sdfc_tuning& t) {
     int rc = sdfc_impl::ensure_partial(b, t.slots);
     if (rc) return rc;
     b->slots = t.slots;
-    b->force_variant = t.force_variant == SDFC_FORCE_WORKERS ? sdfc::kForceWorkers : sdfc::kForceCtas;
+    b->force_variant = t.force_variant;  // SDFC_FORCE_* = sdfc::ForceVariant
     b->worker_ctas = t.worker_ctas;
+    b->chunks_per_slot = t.chunks_per_slot;
     b->tuned_ms = t.ms;
+    // the captured evaluations hold the old configuration (and maybe the old partial rows)
+    for (int k = 0; k < 2; ++k)
+        if (b->eval_exec[k]) {
+            cudaGraphExecDestroy(b->eval_exec[k]);
+            b->eval_exec[k] = nullptr;
+        }
     return SDFC_OK;
 }
 
@@ -53,7 +62,8 @@ int autotune(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc:
             if (rc == SDFC_OK && chosen) *chosen = kv.second;
             return rc;
         }
-    int rc = ensure_partial(b, sdfc::kMaxSlots);
+    const int cap = std::max(b->slots, sdfc::slots_for(b->n));
+    int rc = ensure_partial(b, cap);
     if (rc) return rc;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     SDFC_CUDA_TRY(ctx, cudaEventCreate(&e0));
@@ -63,32 +73,35 @@ int autotune(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc:
     }
     const bool timing = b->timing;
     b->timing = false;
-    sdfc_tuning best{b->slots, b->force_variant == sdfc::kForceWorkers ? SDFC_FORCE_WORKERS : SDFC_FORCE_CTAS, 0,
-                     1e30f};
+    sdfc_tuning best{b->slots, b->force_variant, 0, b->chunks_per_slot, 1e30f};
     constexpr int kReps = 3;
     const bool log = std::getenv("SDFC_TUNE_LOG") != nullptr;  // every candidate's time on stderr
-    for (int variant : {SDFC_FORCE_CTAS, SDFC_FORCE_WORKERS}) {
-        for (int slots = 1; slots <= sdfc::kMaxSlots && rc == SDFC_OK; slots *= 2) {
-            const sdfc_tuning cand{slots, variant, 0, 0.f};
-            if ((rc = apply(b, cand))) break;
-            if ((rc = run_batch(b, in, deriv, out, st))) break;  // warm-up
-            float t_min = 1e30f;
-            for (int r = 0; r < kReps && rc == SDFC_OK; ++r) {
-                cudaEventRecord(e0, st);
-                rc = run_batch(b, in, deriv, out, st);
-                cudaEventRecord(e1, st);
-                if (rc == SDFC_OK && cudaEventSynchronize(e1) != cudaSuccess)
-                    rc = fail(ctx, SDFC_ERR_CUDA, "autotune: evaluation failed");
-                float ms = 0.f;
-                if (rc == SDFC_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) t_min = std::min(t_min, ms);
-            }
-            if (log && rc == SDFC_OK)
-                std::fprintf(stderr, "sdfc autotune: n=%d %s slots=%d %.4f ms\n", b->n,
-                             variant == SDFC_FORCE_WORKERS ? "workers" : "ctas", slots, t_min);
-            if (rc == SDFC_OK && t_min < best.ms) {
-                best = cand;
-                best.ms = t_min;
-            }
+    // the queue forms at the cap with 1-32 chunks per share; the grid form at 1-16 shares
+    std::vector<sdfc_tuning> cands;
+    for (int variant : {SDFC_FORCE_CTAS, SDFC_FORCE_WORKERS})
+        for (int per = 1; per <= 32; per *= 2) cands.push_back(sdfc_tuning{cap, variant, 0, per, 0.f});
+    for (int slots = 1; slots <= std::min(16, cap); slots *= 2)
+        cands.push_back(sdfc_tuning{slots, SDFC_FORCE_GRID, 0, 1, 0.f});
+    for (const sdfc_tuning& cand : cands) {
+        if ((rc = apply(b, cand))) break;
+        if ((rc = run_batch(b, in, deriv, out, st))) break;  // warm-up
+        float t_min = 1e30f;
+        for (int r = 0; r < kReps && rc == SDFC_OK; ++r) {
+            cudaEventRecord(e0, st);
+            rc = run_batch(b, in, deriv, out, st);
+            cudaEventRecord(e1, st);
+            if (rc == SDFC_OK && cudaEventSynchronize(e1) != cudaSuccess)
+                rc = fail(ctx, SDFC_ERR_CUDA, "autotune: evaluation failed");
+            float ms = 0.f;
+            if (rc == SDFC_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) t_min = std::min(t_min, ms);
+        }
+        if (rc) break;
+        if (log)
+            std::fprintf(stderr, "sdfc autotune: n=%d %s slots=%d chunks_per_slot=%d %.4f ms\n", b->n,
+                         kVariantName[cand.force_variant], cand.slots, cand.chunks_per_slot, t_min);
+        if (t_min < best.ms) {
+            best = cand;
+            best.ms = t_min;
         }
     }
     b->timing = timing;
@@ -125,8 +138,9 @@ int sdfc_batch_autotune(sdfc_batch* b, const double* E_A, const double* phi_A, c
 int sdfc_batch_get_tuning(sdfc_batch* b, sdfc_tuning* t) {
     if (!b || !t) return SDFC_ERR_INVALID_ARGUMENT;
     t->slots = b->slots;
-    t->force_variant = b->force_variant == sdfc::kForceWorkers ? SDFC_FORCE_WORKERS : SDFC_FORCE_CTAS;
+    t->force_variant = b->force_variant;
     t->worker_ctas = b->worker_ctas;
+    t->chunks_per_slot = b->chunks_per_slot;
     t->ms = b->tuned_ms;
     return SDFC_OK;
 }

@@ -69,16 +69,17 @@ class Mover(ctypes.Structure):
 
 FORCE_CTAS = 0
 FORCE_WORKERS = 1
+FORCE_GRID = 2
 
 
 class Tuning(ctypes.Structure):
     """sdfc_tuning: the launch configuration of a batch's force pass."""
     _fields_ = [("slots", ctypes.c_int), ("force_variant", ctypes.c_int), ("worker_ctas", ctypes.c_int),
-                ("ms", ctypes.c_float)]
+                ("chunks_per_slot", ctypes.c_int), ("ms", ctypes.c_float)]
 
     def as_dict(self):
-        return {"slots": self.slots, "force_variant": ("ctas", "workers")[self.force_variant],
-                "worker_ctas": self.worker_ctas, "ms": float(self.ms)}
+        return {"slots": self.slots, "force_variant": ("ctas", "workers", "grid")[self.force_variant],
+                "worker_ctas": self.worker_ctas, "chunks_per_slot": self.chunks_per_slot, "ms": float(self.ms)}
 
 
 class Params(ctypes.Structure):
@@ -507,8 +508,8 @@ class Batch:
         self.ctx._check(lib().sdfc_batch_get_tuning(self._h, ctypes.byref(t)), "sdfc_batch_get_tuning")
         return t.as_dict()
 
-    def set_tuning(self, slots: int, force_variant: int, worker_ctas: int = 0):
-        t = Tuning(int(slots), int(force_variant), int(worker_ctas), 0.0)
+    def set_tuning(self, slots: int, force_variant: int, worker_ctas: int = 0, chunks_per_slot: int = 1):
+        t = Tuning(int(slots), int(force_variant), int(worker_ctas), int(chunks_per_slot), 0.0)
         self.ctx._check(lib().sdfc_batch_set_tuning(self._h, ctypes.byref(t)), "sdfc_batch_set_tuning")
 
     def energy(self, E_A, E_B, params):
@@ -594,8 +595,8 @@ class Sim:
         self.ctx._check(lib().sdfc_sim_get_tuning(self._h, ctypes.byref(t)), "sdfc_sim_get_tuning")
         return t.as_dict()
 
-    def set_tuning(self, slots: int, force_variant: int, worker_ctas: int = 0):
-        t = Tuning(int(slots), int(force_variant), int(worker_ctas), 0.0)
+    def set_tuning(self, slots: int, force_variant: int, worker_ctas: int = 0, chunks_per_slot: int = 1):
+        t = Tuning(int(slots), int(force_variant), int(worker_ctas), int(chunks_per_slot), 0.0)
         self.ctx._check(lib().sdfc_sim_set_tuning(self._h, ctypes.byref(t)), "sdfc_sim_set_tuning")
 
     def set_state(self, q, qdot):

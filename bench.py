@@ -391,7 +391,10 @@ def run_gpu(args, world, rank):
                           want_deriv=True, stream=stream.cuda_stream)
 
     tuning = None
-    if not args.no_autotune:  # the batch's launch configuration, timed once on these inputs
+    if args.tuning:  # a given launch configuration: form, slots, chunks per slot
+        form, slots, per = args.tuning.split(",")
+        batch.set_tuning(int(slots), {"ctas": 0, "workers": 1, "grid": 2}[form], chunks_per_slot=int(per))
+    elif not args.no_autotune:  # the batch's launch configuration, timed once on these inputs
         tuning = batch.autotune(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
                                 fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
                                 want_deriv=True, stream=stream.cuda_stream)
@@ -402,6 +405,7 @@ def run_gpu(args, world, rank):
         stream.synchronize()
         assert not st.any().item(), "non-finite contact output"
         n_active = int(nact.sum().item())
+        nact_rows = nact.cpu().numpy().astype(np.int64)
         out_fast = (fm.cpu().numpy().copy(), Km.cpu().numpy().copy(), Dm.cpu().numpy().copy())
 
         # timed region: K steps, each bracketed by CUDA events on the launching stream, L2 flushed between
@@ -526,14 +530,17 @@ def run_gpu(args, world, rank):
     hbm_peak = peaks["hbm_gbs"] if peaks else 6800.0
     # algorithmic bytes: detection reads 12 B per point and 8 FP32 corners (32 B) per query
     det_bytes = pts_per_step * (12 + 8 * 4)
-    # forces: per active contact its id (4 B), point (12 B) and 8 FP32 corners; per instance-slot 300 FP64 partials
-    # per instance-slot 300 FP64 partials (the batch's slots per instance, as tuned)
-    slots = tuning_used["slots"]
-    frc_bytes = n_active * (4 + 12 + 32) + n * slots * 300 * 8
+    # forces: per active contact its id (4 B), point (12 B) and 8 FP32 corners; per (instance, share) 300 FP64
+    # partials, the shares of each instance as the tuning cuts its active contacts
+    chunk = 32 if tuning_used["force_variant"] == "workers" else 128
+    shares = np.minimum(tuning_used["slots"],
+                        -(-(-(-nact_rows // chunk)) // tuning_used["chunks_per_slot"]))
+    rows = int(shares.sum())
+    frc_bytes = n_active * (4 + 12 + 32) + rows * 300 * 8
     kernels = {
         "detect": {"ms": det_ms, "bytes": det_bytes},
         "force_kernel": {"ms": frc_ms, "bytes": frc_bytes},
-        "finalize_kernel": {"ms": red_ms, "bytes": n * slots * 300 * 8 + n * 300 * 8},
+        "finalize_kernel": {"ms": red_ms, "bytes": rows * 300 * 8 + n * 300 * 8},
     }
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     ach = kernels[dom]["bytes"] / (kernels[dom]["ms"] / 1e3) / 1e9
@@ -569,10 +576,13 @@ def run_gpu(args, world, rank):
                          "speedup_of_mixed": f64_ms / step_ms},
         "error_vs_fp64_path": err,
         "tuning": {"chosen": tuning_used, "autotuned": tuning is not None,
-                   "candidates": "force pass as CTAs per (instance, slot) or persistent one-warp workers, "
-                                 "x 1-32 partial sums per instance; each timed on one evaluation"},
+                   "partial_rows": rows,
+                   "candidates": "force pass on persistent 128-thread CTAs or one-warp workers over (instance, share) "
+                                 "items x 1-32 chunks per share (at most 32 shares per instance), or a grid of one CTA "
+                                 "per item x 1-16 shares per instance; each timed on one evaluation"},
         "active_contacts_per_step": n_active, "fp64_rechecked_points_per_step": rechecked,
-        "gpu_launches": 5 * args.steps,  # prep, detect, recheck, force, finalize
+        # prep, detect, recheck, (plan, for the queue forms), force, finalize
+        "gpu_launches": (5 if tuning_used["force_variant"] == "grid" else 6) * args.steps,
         "clocks": clk,
         "wall_s": wall,
     }
@@ -757,6 +767,17 @@ def run_c5(args, sdfc, ctx, torch):
             b.record(stream)
         torch.cuda.synchronize()
     ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    # per-phase device times (separate pass with events between the launches)
+    b16.set_timing(True)
+    phases = []
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            flush.zero_()
+            stream.synchronize()
+            step()
+            phases.append(b16.last_timing())
+    b16.set_timing(False)
+    c5_phases = {k: float(np.mean([x[i] for x in phases])) for i, k in enumerate(("detect", "force", "reduce"))}
     act = nact.cpu().numpy()
     n_active = int(act.sum())
     m = min(n, args.c5_check)
@@ -773,7 +794,7 @@ def run_c5(args, sdfc, ctx, torch):
     b64.close()
     out = {"grid": f"{args.c5_grid}^3 fp16 bricks", "grid_bytes": int(((args.c5_grid + 7) // 8) ** 3 * (512 * 2 + 8)),
            "fp64_grid_bytes": int(args.c5_grid ** 3 * 8), "points": args.c5_points, "instances": n,
-           "ms_per_eval": ms, "contact_pts_per_s": n * args.c5_points / (ms / 1e3),
+           "ms_per_eval": ms, "phases_ms": c5_phases, "contact_pts_per_s": n * args.c5_points / (ms / 1e3),
            "active_contacts_per_eval": n_active, "grid_sample_s": gen_s, "grid_encode_upload_s": up_s,
            "distance_error_vs_fp64_grid": dist_err, "force_error_vs_fp64_grid": force_err}
     if args.c5_steps > 0:
@@ -1271,6 +1292,9 @@ def main():
                     help="SDF-construction leg: torus segments (x segments/2 quads; 0: skip the leg)")
     ap.add_argument("--ls-dx", type=float, default=0.0068, help="SDF-construction leg: grid spacing")
     ap.add_argument("--ls-cpu-dx", type=float, default=0.02, help="SDF-construction leg: spacing of the CPU sample")
+    ap.add_argument("--tuning", default="",
+                    help="headline batch: launch configuration FORM,SLOTS,CHUNKS_PER_SLOT (FORM ctas, workers or "
+                         "grid) instead of the autotuner's")
     ap.add_argument("--c5-grid", type=int, default=512, help="FP16-brick leg: grid nodes per axis")
     ap.add_argument("--c5-points", type=int, default=1000000, help="FP16-brick leg: points (0: skip the leg)")
     ap.add_argument("--c5-dirs", type=int, default=256, help="FP16-brick leg: pull directions")

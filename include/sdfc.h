@@ -237,26 +237,34 @@ int sdfc_batch_last_timing(sdfc_batch* batch, float* ms);
 /* ---------------------------------------------------------------- launch tuning */
 
 /* How a batch's force pass is launched.  No counterpart in the reference (its only
- * parallelism knob is the process count of utils/parallel.py:10).
- *   slots          partial sums per instance: each instance's active contacts are split into
- *                  `slots` interleaved shares, each summed on its own and the shares summed in
- *                  order at the end (1..32, a power of two);
- *   force_variant  SDFC_FORCE_CTAS: one CTA of 128 threads per (instance, slot);
- *                  SDFC_FORCE_WORKERS: persistent one-warp CTAs, as many as the multiprocessors
- *                  hold, taking (instance, slot) items from a queue;
- *   worker_ctas    one-warp CTAs launched by SDFC_FORCE_WORKERS (0: multiprocessors x resident);
- *   ms             measured time of one evaluation with this configuration (0 if not measured).
+ * parallelism knob is the process count of utils/parallel.py:10).  Each instance's active
+ * contacts (counted on the device by detection) are cut into chunks (128 contacts for
+ * SDFC_FORCE_CTAS, 32 for SDFC_FORCE_WORKERS) and the chunks into S interleaved shares,
+ * S = min(slots, ceil(chunks / chunks_per_slot)) (none without contacts): each share is summed
+ * on its own and the shares in order at the end, so an instance with many contacts is spread
+ * over many CTAs and one with few over one.
+ *   slots            partial sums per instance, at most (1..32, a power of two);
+ *   force_variant    SDFC_FORCE_CTAS: persistent CTAs of 128 threads, as many as the
+ *                    multiprocessors hold, taking (instance, share) items from a queue;
+ *                    SDFC_FORCE_WORKERS: persistent one-warp CTAs taking the same items;
+ *                    SDFC_FORCE_GRID: one CTA of 128 threads per (instance, share) for every
+ *                    share up to `slots` (those past an instance's S return at once);
+ *   worker_ctas      one-warp CTAs launched by SDFC_FORCE_WORKERS (0: multiprocessors x resident);
+ *   chunks_per_slot  chunks per share, at least (>= 1);
+ *   ms               measured time of one evaluation with this configuration (0 if not measured).
  * Every configuration sums each share in a fixed order, so results are reproducible run to run
  * for a given configuration; different configurations group the sums differently and may
  * differ in the last bits. */
 #define SDFC_FORCE_CTAS 0
 #define SDFC_FORCE_WORKERS 1
+#define SDFC_FORCE_GRID 2
 typedef struct {
-    int slots, force_variant, worker_ctas;
+    int slots, force_variant, worker_ctas, chunks_per_slot;
     float ms;
 } sdfc_tuning;
 
-/* Times the candidate configurations (force_variant x slots) on one evaluation of these DEVICE
+/* Times the candidate configurations (the queue forms x chunks_per_slot 1-32 with slots at the
+ * batch's cap, the grid form x slots 1-16) on one evaluation of these DEVICE
  * inputs (as sdfc_batch_evaluate_device; want_deriv as there), keeps the fastest for the batch
  * and for later batches of the same shape in this context (instances, tiles, points, grid
  * storages, precision, derivative mode), and writes it to *chosen (may be NULL).  A batch whose

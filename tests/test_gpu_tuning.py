@@ -1,11 +1,13 @@
 """Launch configurations of the force pass (sdfc_tuning) and the autotuner, through the C ABI.
 
-Every configuration (CTAs per (instance, slot) or persistent one-warp workers, 1-32 partial sums
-per instance) must give the reference's results at the parity bars (FP64: fm 1e-10, Km and Dm
-1e-6; mixed precision 1e-5, in the reference's relative-error convention) with identical active
-sets, and be bit-reproducible run to run.  The autotuner must choose one of them, keep it for
-the batch and reuse it for batches of the same shape; a sim must step the same trajectory with
-either force-pass form."""
+Every configuration (persistent 128-thread CTAs or one-warp workers over the (instance, share)
+items, or a grid of one CTA per item; at most 1-32 shares per instance, 1-32 chunks per share)
+must give the reference's
+results at the parity bars (FP64: fm 1e-10, Km and Dm 1e-6; mixed precision 1e-5, in the
+reference's relative-error convention) with identical active sets, and be bit-reproducible run
+to run, also when it replaces a configuration the batch already evaluated with.  The
+autotuner must choose one of them, keep it for the batch and reuse it for batches of the same
+shape; a sim must step the same trajectory with either force-pass form."""
 import numpy as np
 import pytest
 
@@ -14,7 +16,7 @@ from conftest import submodule
 
 pytestmark = pytest.mark.gpu
 
-CONFIGS = [(variant, slots) for variant in (0, 1) for slots in (1, 4, 32)]
+CONFIGS = [(variant, slots, per) for variant in (0, 1, 2) for slots, per in ((1, 1), (4, 1), (32, 1), (32, 4), (8, 32))]
 
 
 @pytest.fixture(scope="module")
@@ -58,15 +60,18 @@ def case(sdfc, ctx, oracle, workloads):
                 prm=prm, ref=ref)
 
 
-@pytest.mark.parametrize("variant,slots", CONFIGS)
+@pytest.mark.parametrize("variant,slots,per", CONFIGS)
 @pytest.mark.parametrize("precision", [0, 1])
-def test_configuration_matches_oracle(sdfc, ctx, case, variant, slots, precision):
+def test_configuration_matches_oracle(sdfc, ctx, case, variant, slots, per, precision):
     b = ctx.batch(case["points"], case["grids"])
     try:
         b.set_precision(precision)
-        b.set_tuning(slots, variant)
-        assert b.tuning()["slots"] == slots
         EA, phiA, EB, phiB = case["states"]
+        # an evaluation with the default configuration first: the new one must replace it
+        b.evaluate(EA, phiA, EB, phiB, case["prm"], want_deriv=True)
+        b.set_tuning(slots, variant, chunks_per_slot=per)
+        t = b.tuning()
+        assert (t["slots"], t["chunks_per_slot"]) == (slots, per)
         out = b.evaluate(EA, phiA, EB, phiB, case["prm"], want_deriv=True)
         fm, Km, Dm, nact, st = out
         assert not st.any()
@@ -106,7 +111,8 @@ def test_autotune_chooses_and_reuses(sdfc, ctx, case):
         b = ctx.batch(case["points"], case["grids"])
         b.set_precision(1)
         t = b.autotune(*ptrs, want_deriv=True)
-        assert t["slots"] in (1, 2, 4, 8, 16, 32) and t["force_variant"] in ("ctas", "workers") and t["ms"] > 0
+        assert t["slots"] in (1, 2, 4, 8, 16, 32) and t["force_variant"] in ("ctas", "workers", "grid") and t["ms"] > 0
+        assert t["chunks_per_slot"] in (1, 2, 4, 8, 16, 32)
         assert b.tuning() == t
         torch.cuda.synchronize()
         out = b.evaluate(EA, phiA, EB, phiB, case["prm"], want_deriv=True)
@@ -151,9 +157,11 @@ def test_sim_workers_match_ctas(sdfc, ctx, workloads, precision, atol):
             sim.close()
 
     q_ctas, _ = run(lambda s: s.set_tuning(4, sdfc.FORCE_CTAS))
-    q_work, _ = run(lambda s: s.set_tuning(8, sdfc.FORCE_WORKERS))
+    q_work, _ = run(lambda s: s.set_tuning(8, sdfc.FORCE_WORKERS, chunks_per_slot=2))
+    q_grid, _ = run(lambda s: s.set_tuning(4, sdfc.FORCE_GRID))
     q_auto, t = run(lambda s: s.autotune())
     assert t["slots"] in (1, 2, 4, 8, 16, 32)
     assert np.abs(q_ctas).max() > 1e-3  # the pegs move
     np.testing.assert_allclose(q_work, q_ctas, rtol=0, atol=atol)
+    np.testing.assert_allclose(q_grid, q_ctas, rtol=0, atol=atol)
     np.testing.assert_allclose(q_auto, q_ctas, rtol=0, atol=atol)
