@@ -82,7 +82,7 @@ int autotune(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc:
         for (int per = 1; per <= 32; per *= 2) cands.push_back(sdfc_tuning{cap, variant, 0, per, 0.f});
     for (int slots = 1; slots <= std::min(16, cap); slots *= 2)
         cands.push_back(sdfc_tuning{slots, SDFC_FORCE_GRID, 0, 1, 0.f});
-    for (const sdfc_tuning& cand : cands) {
+    for (sdfc_tuning& cand : cands) {
         if ((rc = apply(b, cand))) break;
         if ((rc = run_batch(b, in, deriv, out, st))) break;  // warm-up
         float t_min = 1e30f;
@@ -99,10 +99,26 @@ int autotune(sdfc_batch* b, const sdfc::BatchInputs& in, bool deriv, const sdfc:
         if (log)
             std::fprintf(stderr, "sdfc autotune: n=%d %s slots=%d chunks_per_slot=%d %.4f ms\n", b->n,
                          kVariantName[cand.force_variant], cand.slots, cand.chunks_per_slot, t_min);
-        if (t_min < best.ms) {
-            best = cand;
-            best.ms = t_min;
-        }
+        cand.ms = t_min;
+        best.ms = std::min(best.ms, t_min);
+    }
+    // Among the candidates within kTie of the fastest, the one that spreads an instance over the
+    // most shares (its cap over its chunks per share): a batch tuned where its contacts are few
+    // (a sim's opening state) times every form about equally, and the instances whose contacts
+    // grow in later rounds are then spread the widest.
+    if (rc == SDFC_OK) {
+        constexpr float kTie = 1.01f;
+        const float fastest = best.ms;
+        auto spread = [](const sdfc_tuning& t) {
+            const int form = t.force_variant == SDFC_FORCE_CTAS ? 2 : t.force_variant == SDFC_FORCE_GRID ? 1 : 0;
+            return 64LL * t.slots / t.chunks_per_slot * 4 + form;
+        };
+        bool have = false;
+        for (const sdfc_tuning& c : cands)
+            if (c.ms <= kTie * fastest && (!have || spread(c) > spread(best) || (spread(c) == spread(best) && c.ms < best.ms))) {
+                best = c;
+                have = true;
+            }
     }
     b->timing = timing;
     cudaEventDestroy(e0);

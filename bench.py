@@ -83,6 +83,12 @@ def _cpu_eval(args):
     return time.perf_counter() - t
 
 
+def _cpu_result(args):
+    EA, phiA, EB, phiB = args
+    fm, Km, Dm, _ = _G["O"].pair_eval(_G["grid"], _G["pts"], EA, phiA, EB, phiB, _G["prm"], True)
+    return fm, Km, Dm
+
+
 def _cpu_norm_sum(args):
     """Sum of |fm_i| over one instance's active contacts (the error scale of fm where the contacts'
     forces cancel), by the oracle."""
@@ -107,11 +113,69 @@ def _cpu_sim(args):
     return t_fwd, int(evs.sum()), time.perf_counter() - t
 
 
+# The reference's own ForceGeneralSDFContact (oracle/_ref, compiled from the reference's sources
+# where they are staged) in the same kind of worker pool.
+def _ref_init(grid_vals, mn, mx, dx, pts):
+    from oracle import refsim
+    sim, _ = refsim.make_pair_sim()
+    sim.set_sdf("B", grid_vals, mn, mx, dx, COL_TH)
+    sim.set_contact_points("A", pts)
+    sim.set_contact_scale("A", PARAMS[5])
+    _G["ref"] = sim
+
+
+def _ref_eval(args):
+    EA, phiA, EB, phiB = args
+    sim = _G["ref"]
+    sim.set_pose("A", EA, phiA)
+    sim.set_pose("B", EB, phiB)
+    t = time.perf_counter()
+    sim.pair_force("A", "B", *PARAMS[:5], want_deriv=True)
+    return time.perf_counter() - t
+
+
+def _ref_result(args):
+    EA, phiA, EB, phiB = args
+    sim = _G["ref"]
+    sim.set_pose("A", EA, phiA)
+    sim.set_pose("B", EB, phiB)
+    return sim.pair_force("A", "B", *PARAMS[:5], want_deriv=True)
+
+
+def reference_library():
+    """Whether oracle/_ref (the reference compiled from its own sources) is there, building it
+    from the staged sources when they are present; the reason when it is not."""
+    try:
+        from oracle import refsim
+    except Exception as e:  # pragma: no cover
+        return False, f"oracle.refsim: {e}"
+    if refsim.available():
+        return True, ""
+    if refsim.reference_root() is None:
+        return False, "the reference's sources are not staged (baseline/_ref/src)"
+    try:
+        return refsim.build(), "build finished without the library"
+    except Exception as e:
+        return False, f"building the reference failed: {e}"
+
+
+def ref_pool(grid, pts, procs):
+    ctx = mp.get_context("spawn")
+    return ctx.Pool(procs, initializer=_ref_init, initargs=(grid.values, grid.min_box, grid.max_box, grid.dx, pts))
+
+
 def cpu_pool(grid, pts, procs):
     from oracle import oracle as O
     O.build()
     ctx = mp.get_context("spawn")
     return ctx.Pool(procs, initializer=_cpu_init, initargs=(grid.values, grid.min_box, grid.max_box, grid.dx, pts))
+
+
+def ref_time(pool, states, idx):
+    EA, phiA, EB, phiB = states
+    t = time.perf_counter()
+    pool.map(_ref_eval, [(EA[k], phiA[k], EB[k], phiB[k]) for k in idx], chunksize=1)
+    return time.perf_counter() - t
 
 
 def cpu_time(pool, states, idx):
@@ -292,6 +356,21 @@ def load_peaks():
         return None
 
 
+def profile_figures(fname):
+    """name -> value pairs of a committed ncu summary under profiles/ (empty if absent)."""
+    path = os.path.join(ROOT, "profiles", fname)
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and not parts[0].startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
 def profile_traffic(name):
     """DRAM bytes per launch of `name` from the committed ncu summary, if one exists."""
     path = os.path.join(ROOT, "profiles", "ncu_dram_per_launch.txt")
@@ -309,33 +388,55 @@ def profile_traffic(name):
 
 # --------------------------------------------------------------------------- arms
 def run_reference(args, world, rank):
-    """The reference path's CPU cost on the host cores (oracle port), on a bounded sample."""
+    """The reference path's CPU cost on the host cores, on a bounded sample: the reference's own
+    ForceGeneralSDFContact (oracle/_ref) one process per core where it can be built from the
+    staged sources, else the oracle's C port of it."""
     if rank != 0:
         return
     grid, pts, states = build_workload(args.instances, args.points, args.grid)
     procs = os.cpu_count() or 1
-    pool = cpu_pool(grid, pts, procs)
-    sample = max(procs, args.cpu_sample)
+    have_ref, why = reference_library() if not args.ref_port else (False, "--ref-port given")
+    kind = "reference" if have_ref else "port"
+    pool = ref_pool(grid, pts, procs) if have_ref else cpu_pool(grid, pts, procs)
+    sample = max(procs, args.ref_sample if have_ref else args.cpu_sample)
     rng = np.random.default_rng(0)
+    timer = (lambda idx: ref_time(pool, states, idx)) if have_ref else (lambda idx: cpu_time(pool, states, idx))
     for _ in range(args.warmup):
-        cpu_time(pool, states, rng.choice(args.instances, procs, replace=False))
+        timer(rng.choice(args.instances, procs, replace=False))
     times = []
     for _ in range(args.steps):
-        times.append(cpu_time(pool, states, rng.choice(args.instances, sample, replace=False)))
+        times.append(timer(rng.choice(args.instances, sample, replace=False)))
+    agreement = None
+    if have_ref:  # the reference against the oracle port on two instances of the workload
+        ref_out = pool.map(_ref_result, [tuple(x[k] for x in states) for k in (0, 1)])
+        pool.close()
+        port = cpu_pool(grid, pts, 2)
+        port_out = port.map(_cpu_result, [tuple(x[k] for x in states) for k in (0, 1)])
+        port.close()
+        agreement = max(float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+                        for r, p in zip(ref_out, port_out) for a, b in zip(r, p))
+        pool = cpu_pool(grid, pts, procs) if args.sim_steps > 0 else None
     sim = cpu_sim_rate(pool, args.cpu_sim_scenes, min(args.sim_early, 25), procs) if args.sim_steps > 0 else None
-    pool.close()
+    if pool is not None:
+        pool.close()
     per_step = float(np.mean(times))
     value = sample * args.points / per_step
+    sample_desc = f"{sample} of {args.instances} instances per step, derivative evaluation, one process per core"
+    if have_ref:
+        sample_desc += (f"; the reference's ForceGeneralSDFContact::computeForceWithDerivative (oracle/_ref); "
+                        f"fm/Km/Dm against the oracle port {agreement:.1e} relative")
+    else:
+        sample_desc += f"; the oracle's C port ({why})"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{sample} of {args.instances} instances per step, derivative evaluation"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": kind, "sample": sample_desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if sim is not None:
+        sim["kind"] = "port"  # the simulation sample always steps the oracle's BDF1 restatement
         line["sim"] = sim
     print(json.dumps(line), flush=True)
 
@@ -545,6 +646,24 @@ def run_gpu(args, world, rank):
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     ach = kernels[dom]["bytes"] / (kernels[dom]["ms"] / 1e3) / 1e9
     traffic = profile_traffic(dom)
+    # the force kernel's own limit (issue slots, with the FP64 pipe beside it): its warp
+    # instructions per contact from the committed ncu capture x this run's active contacts over the
+    # live force time, against 4 warp instructions per SM per clock
+    issue = profile_figures("ncu_force_kernel_issue.txt")
+    force_issue = None
+    if issue.get("warp_inst_per_contact") and frc_ms > 0:
+        sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        ach_i = issue["warp_inst_per_contact"] * n_active / (frc_ms / 1e3)
+        peak_i = 4.0 * sms * sm_mhz * 1e6
+        force_issue = {"kernel": "force_kernel", "bound": "issue", "achieved": ach_i, "peak": peak_i,
+                       "unit": "warp-inst/s", "frac": ach_i / peak_i,
+                       "warp_inst_per_contact": issue["warp_inst_per_contact"],
+                       "ncu_issue_active": issue.get("issue_active"),
+                       "ncu_fp64_pipe_active": issue.get("fp64_pipe_active"),
+                       "ncu_warps_active": issue.get("warps_active"),
+                       "note": "instructions per contact and pipe fractions from the 512-instance ncu capture "
+                               "(profiles/force_kernel_direction_sweep_512x50k.md); the rate from this run"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -561,6 +680,7 @@ def run_gpu(args, world, rank):
         # the whole evaluation against the same peak, with the per-point algorithmic bytes of a
         # contact-point evaluation (12 B point + 8 FP32 corners), plus the active contacts' force
         # reads and the partial rows
+        "roofline_force_issue": force_issue,
         "roofline_evaluation": {"bound": "hbm", "bytes_per_step": det_bytes + frc_bytes,
                                 "achieved": (det_bytes + frc_bytes) / (step_ms / 1e3) / 1e9, "peak": hbm_peak,
                                 "unit": "GB/s", "frac": (det_bytes + frc_bytes) / (step_ms / 1e3) / 1e9 / hbm_peak,
@@ -755,6 +875,12 @@ def run_c5(args, sdfc, ctx, torch):
                             fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(),
                             want_deriv=True, stream=stream.cuda_stream)
 
+    if not args.no_autotune:  # the batch's launch configuration, timed once on these inputs
+        b16.autotune(dEA.data_ptr(), dphiA.data_ptr(), dEB.data_ptr(), dphiB.data_ptr(), dprm.data_ptr(),
+                     fm.data_ptr(), Km.data_ptr(), Dm.data_ptr(), nact.data_ptr(), st.data_ptr(), want_deriv=True,
+                     stream=stream.cuda_stream)
+    c5_tuning = b16.tuning()
+
     with torch.cuda.stream(stream):
         for _ in range(3):
             step()
@@ -794,7 +920,8 @@ def run_c5(args, sdfc, ctx, torch):
     b64.close()
     out = {"grid": f"{args.c5_grid}^3 fp16 bricks", "grid_bytes": int(((args.c5_grid + 7) // 8) ** 3 * (512 * 2 + 8)),
            "fp64_grid_bytes": int(args.c5_grid ** 3 * 8), "points": args.c5_points, "instances": n,
-           "ms_per_eval": ms, "phases_ms": c5_phases, "contact_pts_per_s": n * args.c5_points / (ms / 1e3),
+           "ms_per_eval": ms, "phases_ms": c5_phases, "tuning": c5_tuning,
+           "contact_pts_per_s": n * args.c5_points / (ms / 1e3),
            "active_contacts_per_eval": n_active, "grid_sample_s": gen_s, "grid_encode_upload_s": up_s,
            "distance_error_vs_fp64_grid": dist_err, "force_error_vs_fp64_grid": force_err}
     if args.c5_steps > 0:
@@ -811,6 +938,8 @@ def run_c5(args, sdfc, ctx, torch):
             sim.set_precision(precision)
             sim.set_state(np.zeros((scenes, 3)), np.zeros((scenes, 3)))
             sim.set_external_force(F[which])
+            if not args.no_autotune and precision == sdfc.PRECISION_MIXED:
+                sim.autotune()
             t0 = time.perf_counter()
             conv = sim.step(args.c5_steps)
             wall = time.perf_counter() - t0
@@ -1270,6 +1399,10 @@ def main():
     ap.add_argument("--points", type=int, default=50000)
     ap.add_argument("--grid", type=int, default=128)
     ap.add_argument("--cpu-sample", type=int, default=512, help="instances per CPU-baseline step")
+    ap.add_argument("--ref-sample", type=int, default=128,
+                    help="--impl reference: instances per step when the reference itself is timed")
+    ap.add_argument("--ref-port", action="store_true",
+                    help="--impl reference: time the oracle's C port even where the reference can be built")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the batches' default launch configuration")
     ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")

@@ -253,7 +253,9 @@ int ref_distance(void* sim, const char* name, const double* xw, int n, double* o
 // Runs ForceGeneralSDFContact(contact body A, SDF body B) through its public
 // Force interface on the bodies' current poses and extracts the 12-dof
 // sub-blocks [A; B] of fm, Km, Dm.  ids receives the active contact ids
-// (ascending) found by collision_detection_general_SDF.
+// (ascending) found by collision_detection_general_SDF; with ids null that second
+// detection is skipped (the timed CPU baseline: one Force call per pair, nothing more)
+// and n_active is left unset.
 int ref_pair_eval(void* sim, const char* name_a, const char* name_b, double kn, double kt, double mu,
                   double damping, double scale, int want_deriv, double* fm12, double* Km144, double* Dm144,
                   int* ids, int ids_cap, int* n_active) {
@@ -285,6 +287,7 @@ int ref_pair_eval(void* sim, const char* name_a, const char* name_b, double kn, 
             Dm144[12 * r + c] = want_deriv ? Dm(idx[r], idx[c]) : 0.0;
         }
     }
+    if (!ids) return 0;
     std::vector<Contact> contacts;
     collision_detection_general_SDF(a, dynamic_cast<BodySDFObj*>(b), contacts);
     *n_active = (int)contacts.size();

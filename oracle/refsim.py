@@ -301,6 +301,14 @@ class RefSim:
                                    cap, ctypes.byref(n)), "pair_eval")
         return fm, Km.reshape(12, 12), Dm.reshape(12, 12), ids[:n.value].copy()
 
+    def pair_force(self, a, b, kn, kt, mu, damping, scale=1.0, want_deriv=True):
+        """One ForceGeneralSDFContact call (pair_eval without the active-id listing)."""
+        fm, Km, Dm = np.zeros(12), np.zeros(144), np.zeros(144)
+        n = ctypes.c_int()
+        _check(lib().ref_pair_eval(self._h, a.encode(), b.encode(), kn, kt, mu, damping, scale, int(want_deriv),
+                                   _dp(fm), _dp(Km), _dp(Dm), None, 0, ctypes.byref(n)), "pair_force")
+        return fm, Km.reshape(12, 12), Dm.reshape(12, 12)
+
     # stepping -----------------------------------------------------------
     def reset(self, backward=False):
         _check(lib().ref_sim_reset(self._h, int(backward)), "reset")
