@@ -398,11 +398,11 @@ def run_reference(args, world, rank):
     have_ref, why = reference_library() if not args.ref_port else (False, "--ref-port given")
     kind = "reference" if have_ref else "port"
     pool = ref_pool(grid, pts, procs) if have_ref else cpu_pool(grid, pts, procs)
-    sample = max(procs, args.ref_sample if have_ref else args.cpu_sample)
+    sample = min(args.instances, max(procs, args.ref_sample if have_ref else args.cpu_sample))
     rng = np.random.default_rng(0)
     timer = (lambda idx: ref_time(pool, states, idx)) if have_ref else (lambda idx: cpu_time(pool, states, idx))
     for _ in range(args.warmup):
-        timer(rng.choice(args.instances, procs, replace=False))
+        timer(rng.choice(args.instances, min(procs, args.instances), replace=False))
     times = []
     for _ in range(args.steps):
         times.append(timer(rng.choice(args.instances, sample, replace=False)))

@@ -132,5 +132,6 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(lines) == 1
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["scaling"] == "weak"
-    assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
+    # the reference's own Force where its library builds from staged sources, else the C port
+    assert line["value"] > 0 and line["cpu_baseline"]["kind"] in ("reference", "port")
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
