@@ -648,9 +648,10 @@ int sdfc_f16_brick_decode(const unsigned short* codes, const float* so, int ni, 
         for (int j = 0; j < nj; ++j)
             for (int i = 0; i < ni; ++i) {
                 const size_t b = (size_t)(i >> 3) + (size_t)nbx * ((size_t)(j >> 3) + (size_t)nby * (k >> 3));
-                const double h = (double)half_value(codes[b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7)]);
+                const float h = half_value(codes[b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7)]);
+                // FP32 fused multiply-add, as the device decodes (correctly rounded on both)
                 values[(size_t)i + (size_t)ni * ((size_t)j + (size_t)nj * k)] =
-                    std::fma((double)so[2 * b], h, (double)so[2 * b + 1]);
+                    (double)std::fmaf(so[2 * b], h, so[2 * b + 1]);
             }
     return SDFC_OK;
 }

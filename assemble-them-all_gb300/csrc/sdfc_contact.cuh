@@ -191,15 +191,15 @@ __device__ __forceinline__ size_t brick_of(const GridDesc& g, int i, int j, int 
 __device__ __forceinline__ float brick_code(const GridDesc& g, size_t b, int i, int j, int k) {
     return __half2float(__ushort_as_half(__ldg(g.b16 + b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7))));
 }
-__device__ __forceinline__ double brick_value64(const GridDesc& g, int i, int j, int k) {
-    const size_t b = brick_of(g, i, j, k);
-    const float2 so = __ldg(g.bso + b);
-    return fma((double)so.x, (double)brick_code(g, b, i, j, k), (double)so.y);
-}
+// A brick node's value: fmaf(scale, code, offset) in FP32 (the FP64 paths read it widened, so
+// the two views are the same number and the FP64 pipe only widens it).
 __device__ __forceinline__ float brick_value32(const GridDesc& g, int i, int j, int k) {
     const size_t b = brick_of(g, i, j, k);
     const float2 so = __ldg(g.bso + b);
     return fmaf(so.x, brick_code(g, b, i, j, k), so.y);
+}
+__device__ __forceinline__ double brick_value64(const GridDesc& g, int i, int j, int k) {
+    return (double)brick_value32(g, i, j, k);
 }
 
 // The brick reads are kept out of line (results returned by value, in registers) so that the
@@ -230,37 +230,6 @@ static __device__ __noinline__ Corners32 brick_corners32(const GridDesc& g, int 
     return r;
 }
 
-// A brick cell's corners decoded both ways from one set of loads: FP32 (as brick_value32) and
-// FP64 (as brick_value64).
-struct Corners3264 {
-    float c[8];
-    double e[8];
-};
-static __device__ __noinline__ Corners3264 brick_corners3264(const GridDesc& g, int i, int j, int k) {
-    Corners3264 r;
-    if (cell_in_one_brick(i, j, k)) {
-        const size_t b = brick_of(g, i, j, k);
-        const float2 so = __ldg(g.bso + b);
-        const unsigned short* cb = g.b16 + b * 512 + (i & 7) + 8 * (j & 7) + 64 * (k & 7);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const float h = __half2float(__ushort_as_half(__ldg(cb + brick_corner_offset(q))));
-            r.c[q] = fmaf(so.x, h, so.y);
-            r.e[q] = fma((double)so.x, (double)h, (double)so.y);
-        }
-        return r;
-    }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const int ii = i + (q & 1), jj = j + ((q >> 1) & 1), kk = k + (q >> 2);
-        const size_t b = brick_of(g, ii, jj, kk);
-        const float2 so = __ldg(g.bso + b);
-        const float h = brick_code(g, b, ii, jj, kk);
-        r.c[q] = fmaf(so.x, h, so.y);
-        r.e[q] = fma((double)so.x, (double)h, (double)so.y);
-    }
-    return r;
-}
 static __device__ __noinline__ double brick_value64_cold(const GridDesc& g, int i, int j, int k) {
     return brick_value64(g, i, j, k);
 }
@@ -318,8 +287,9 @@ __device__ __forceinline__ void plain_corners64(const GridDesc& g, int i, int j,
 }
 __device__ __forceinline__ void cell_corners64(const GridDesc& g, int i, int j, int k, double* c) {
     if (g.b16) {
+        const Corners32 r = brick_corners32(g, i, j, k);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) c[q] = brick_value64_cold(g, i + (q & 1), j + ((q >> 1) & 1), k + (q >> 2));
+        for (int q = 0; q < 8; ++q) c[q] = (double)r.c[q];
         return;
     }
     if (g.v32) {
@@ -399,10 +369,21 @@ __device__ __forceinline__ double trilinear_at(const GridDesc& g, Cell c) {
     int ip = (i == g.ni - 1) ? i : i + 1;
     int jp = (j == g.nj - 1) ? j : j + 1;
     int kp = (k == g.nk - 1) ? k : k + 1;
-    double v00 = lerp_ref(c.u, grid_value(g, i, j, k), grid_value(g, ip, j, k));
-    double v10 = lerp_ref(c.u, grid_value(g, i, jp, k), grid_value(g, ip, jp, k));
-    double v01 = lerp_ref(c.u, grid_value(g, i, j, kp), grid_value(g, ip, j, kp));
-    double v11 = lerp_ref(c.u, grid_value(g, i, jp, kp), grid_value(g, ip, jp, kp));
+    double e[8];
+    if (g.b16 && ip == i + 1 && jp == j + 1 && kp == k + 1) {  // FP16 bricks: the cell's corners in one read
+        const Corners32 r = brick_corners32(g, i, j, k);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) e[q] = (double)r.c[q];
+    } else {
+        e[0] = grid_value(g, i, j, k);   e[1] = grid_value(g, ip, j, k);
+        e[2] = grid_value(g, i, jp, k);  e[3] = grid_value(g, ip, jp, k);
+        e[4] = grid_value(g, i, j, kp);  e[5] = grid_value(g, ip, j, kp);
+        e[6] = grid_value(g, i, jp, kp); e[7] = grid_value(g, ip, jp, kp);
+    }
+    double v00 = lerp_ref(c.u, e[0], e[1]);
+    double v10 = lerp_ref(c.u, e[2], e[3]);
+    double v01 = lerp_ref(c.u, e[4], e[5]);
+    double v11 = lerp_ref(c.u, e[6], e[7]);
     double vk0 = lerp_ref(c.v, v00, v10);
     double vk1 = lerp_ref(c.v, v01, v11);
     return lerp_ref(c.w, vk0, vk1);
@@ -801,12 +782,12 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
             float cc[8];
             bool have32 = false;
             if constexpr (BR) {
-                if (g.b16) {  // FP16 bricks: the codes loaded once, decoded in FP64 and in FP32
-                    const Corners3264 r = brick_corners3264(g, i, j, k);
+                if (g.b16) {  // FP16 bricks: one decode serves both the depth (widened) and the derivatives
+                    const Corners32 r = brick_corners32(g, i, j, k);
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
-                        e[q] = r.e[q];
                         cc[q] = r.c[q];
+                        e[q] = (double)cc[q];
                     }
                     have32 = true;
                 } else if (g.v32) {  // FP32 node values: one set of loads serves both the depth and the derivatives

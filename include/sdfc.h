@@ -139,8 +139,8 @@ int sdfc_grid_values(sdfc_context* ctx, int grid, double* values);
  * b*512 + (i&7) + 8*(j&7) + 64*(k&7) of brick (i>>3, j>>3, k>>3); nodes past the grid's
  * end repeat its last node.  so[2b], so[2b+1] = scale, offset.  Encoding: offset 0 if the
  * brick's values straddle 0, else the value nearest 0; scale = max|v - offset| / 32768;
- * code = FP16(FP32((v - offset) / scale)).  Decoding: value = fma(scale, code, offset) in
- * FP64 (the grid used by the exact paths; the FP32 paths use the same fma in FP32).
+ * code = FP16(FP32((v - offset) / scale)).  Decoding: value = fmaf(scale, code, offset), an
+ * FP32 fused multiply-add (the FP32 paths use it as is, the FP64 paths widened).
  * codes holds nbx*nby*nbz*512 FP16 bit patterns, so 2*nbx*nby*nbz floats. */
 int sdfc_f16_brick_encode(const double* values, int ni, int nj, int nk, unsigned short* codes, float* so);
 int sdfc_f16_brick_decode(const unsigned short* codes, const float* so, int ni, int nj, int nk, double* values);

@@ -47,11 +47,13 @@ def test_codec_matches_numpy_and_bounds_error():
     b = (I >> 3) + nbx * ((J >> 3) + nby * (K >> 3))
     off = so[b, 1].astype(np.float64)
     scale = so[b, 0].astype(np.float64)
-    # FP16 keeps 11 significant bits; the FP32 quotient adds one FP32 rounding
-    bound = np.abs(v - off) * 2.0 ** -11 * 1.001 + scale * 2.0 ** -24 + 1e-300
+    # FP16 keeps 11 significant bits; the FP32 quotient adds one FP32 rounding, the FP32 decode
+    # (fmaf(scale, code, offset)) another, of the decoded value
+    bound = np.abs(v - off) * 2.0 ** -11 * 1.001 + scale * 2.0 ** -24 + np.abs(dec) * 2.0 ** -24 + 1e-300
     assert np.all(np.abs(dec - v) <= bound)
     # bricks the surface crosses keep offset 0, so values near 0 keep relative precision
     crossing = (v.min() < 0 < v.max())
     assert crossing and np.any(so[:, 1] == 0.0)
     near = np.abs(v) < 0.02
-    assert np.all(np.abs(dec[near] - v[near]) <= np.abs(v[near]) * 2.0 ** -11 * 1.001 + scale[near] * 2.0 ** -24)
+    assert np.all(np.abs(dec[near] - v[near]) <= np.abs(v[near]) * 2.0 ** -11 * 1.001 + scale[near] * 2.0 ** -24
+                  + np.abs(dec[near]) * 2.0 ** -24)
