@@ -165,3 +165,45 @@ def test_sim_workers_match_ctas(sdfc, ctx, workloads, precision, atol):
     np.testing.assert_allclose(q_work, q_ctas, rtol=0, atol=atol)
     np.testing.assert_allclose(q_grid, q_ctas, rtol=0, atol=atol)
     np.testing.assert_allclose(q_auto, q_ctas, rtol=0, atol=atol)
+
+
+@pytest.mark.parametrize("variant,slots,per", [(0, 32, 1), (0, 32, 4), (1, 32, 2), (2, 4, 1), (2, 32, 1)])
+def test_heavy_instance_among_empty_ones(sdfc, ctx, oracle, workloads, variant, slots, per):
+    """One instance with tens of thousands of active contacts (spread over up to 32 shares), one
+    with a few hundred, and 30 whose point sets lie away from the grid (no contact: no share, no
+    item, zero outputs): every form gives the oracle's results."""
+    rng = np.random.default_rng(9)
+    g = workloads.socket_grid(64, dtype=np.float32)
+    gh = ctx.upload_grid(g.values, g.min_box, g.max_box, g.dx, 0.01, 1)
+    heavy = workloads.peg_points(120000, seed=5)
+    light = workloads.peg_points(3000, seed=6)
+    ph, pl = ctx.upload_points(heavy, 1), ctx.upload_points(light, 1)
+    n = 32
+    points = [ph, pl] + [pl] * (n - 2)
+    EA = np.tile(np.eye(4), (n, 1, 1))
+    EA[0] = workloads.pose(workloads.rotvec_to_matrix([0.0, 0.003, 0.0]), [0.028, 0.0, 0.0])
+    EA[1] = workloads.pose(workloads.rotvec_to_matrix([0.002, 0.0, 0.0]), [0.0, 0.027, 0.1])
+    for k in range(2, n):
+        EA[k, :3, 3] = [5.0 + k, 3.0, -4.0]  # far outside the grid box
+    EB = np.tile(np.eye(4), (n, 1, 1))
+    phiA = rng.normal(size=(n, 6)) * 0.2
+    phiB = np.zeros((n, 6))
+    prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0)] * n
+    b = ctx.batch(points, [gh] * n)
+    try:
+        b.set_precision(1)
+        b.set_tuning(slots, variant, chunks_per_slot=per)
+        fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
+    finally:
+        b.close()
+    assert not st.any()
+    assert nact[0] > 20000 and 0 < nact[1] < 5000 and not nact[2:].any(), nact[:3]
+    assert not fm[2:].any() and not Km[2:].any() and not Dm[2:].any()
+    og = oracle.Grid(g.values, g.min_box, g.max_box, g.dx, 0.01)
+    op = oracle.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0)
+    for k, pts in ((0, heavy), (1, light)):
+        rf, rK, rD, rids = oracle.pair_eval(og, pts, EA[k], phiA[k], EB[k], phiB[k], op, True)
+        assert nact[k] == len(rids)
+        assert_close(f"inst {k} fm", fm[k], rf, rel=1e-5, abs_=1e-9)
+        assert_close(f"inst {k} Km", Km[k], rK, rel=1e-5, abs_=1e-9)
+        assert_close(f"inst {k} Dm", Dm[k], rD, rel=1e-5, abs_=1e-9)
