@@ -660,7 +660,9 @@ struct FastCell {
     Vec3<float> y;  // grid-frame point (FP32)
     double ud, vd, wd;
     int i, j, k;
-    bool ok;
+    bool ok;    // the reference's derivative stencil stays in the cell
+    bool near;  // it crosses faces of the cell, within the grid's nodes (cross_face_terms applies)
+    signed char dir[3];  // per axis: +1 / -1 when the stencil crosses the upper / lower face
 };
 
 template <typename T>
@@ -685,10 +687,144 @@ __device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const CellMap& 
     // (a margin of 1.0001 eps absorbs the FP32 evaluation of this test)
     const float m = (float)(1.0001 * 1e-5);
     const float u = (float)c.ud, v = (float)c.vd, w = (float)c.wd;
-    c.ok = c.i >= 0 && c.j >= 0 && c.k >= 0 && c.i < g.ni - 1 && c.j < g.nj - 1 && c.k < g.nk - 1 &&
-           u * g.fdx[0] > m && (1.f - u) * g.fdx[0] > m && v * g.fdx[1] > m && (1.f - v) * g.fdx[1] > m &&
-           w * g.fdx[2] > m && (1.f - w) * g.fdx[2] > m;
+    const bool inrange = c.i >= 0 && c.j >= 0 && c.k >= 0 && c.i < g.ni - 1 && c.j < g.nj - 1 && c.k < g.nk - 1;
+    const float f[3] = {u, v, w};
+    const int ci[3] = {c.i, c.j, c.k}, nn[3] = {g.ni, g.nj, g.nk};
+    bool inside = true, near = inrange;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const bool up = (1.f - f[a]) * g.fdx[a] <= m, down = f[a] * g.fdx[a] <= m;
+        inside = inside && !up && !down;
+        c.dir[a] = up ? 1 : (down ? -1 : 0);
+        // a face crossing needs the next layer of nodes, the point within its own cell, and a
+        // cell wider than the stencil
+        near = near && !(up && down) && f[a] >= 0.f && f[a] <= 1.f && (!up || ci[a] + 2 <= nn[a] - 1) &&
+               (!down || ci[a] >= 1);
+    }
+    c.ok = inrange && inside;
+    c.near = near && !inside;
     return c;
+}
+
+// A node's value as the FP32 paths read it: the FP32 node value, the FP16 brick decode, or the
+// cell-corner array's copy (FP64 grids: its FP32 rounding).
+__device__ __forceinline__ float node32(const GridDesc& g, int i, int j, int k) {
+    if (g.b16) return brick_value32(g, i, j, k);
+    const size_t idx = (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k);
+    if (g.v32) return __ldg(g.v32 + idx);
+    if (i < g.ni - 1 && j < g.nj - 1 && k < g.nk - 1)
+        return __ldg(reinterpret_cast<const float*>(
+            g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k))));
+    return (float)__ldg(g.v64 + idx);
+}
+
+// The reference's derivative stencil (BodySDFObj.cpp:176-205: gradient by central differences
+// at +-eps, Hessian by second differences at +-eps and mixed ones at +-eps/2) where it crosses
+// faces of the contact's cell, in closed form.  Along an axis the interpolant over two cells is
+// the cell's multilinear polynomial plus r(t) D2, with r(t) the distance beyond the face (cell
+// units) and D2 the nodes' second difference across it; in 3D the product of those 1D forms.  So
+// the stencil's differences are the cell's analytic derivatives (computed by the caller) plus:
+//   gradient a:  (r(t + d) - r(t - d)) M_a / (2 eps)
+//   Hessian aa:  (r(t + d) + r(t - d)) M_a / eps^2
+//   Hessian ab:  (dr_a 2 h_b dM_a/db + dr_b 2 h_a dM_b/da + dr_a dr_b M_ab) / eps^2
+// with d = eps / dx, h = d / 2, dr = r(t + h) - r(t - h), M_a the second difference along a
+// interpolated bilinearly at the point's other two coordinates, M_ab the product of the two
+// second differences interpolated along the third.  Each term is a product of small numbers, so
+// FP32 keeps its relative precision where the FP64 differences of the reference cancel.  The
+// distances to the faces come from the FP64 fractions (1 - u is formed in FP64).  Equal to the
+// reference's stencil in exact arithmetic (checked against it to 1e-9 on random cells).
+struct FaceTerms {
+    float g[3], h[6];
+};
+static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, const FastCell& fc, Corners32 cc,
+                                                          bool want_hessian) {
+    const double fr[3] = {fc.ud, fc.vd, fc.wd};
+    const int c0[3] = {fc.i, fc.j, fc.k};
+    const float eps = (float)kFdEps;
+    float t[3], rp[3], rm[3], hp[3], hm[3], del[3], hh[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        t[a] = (float)fr[a];
+        const float lo = t[a], hi = (float)(1.0 - fr[a]);  // distances to the lower / upper face
+        del[a] = eps * g.finv_dx[a];
+        hh[a] = 0.5f * del[a];
+        rp[a] = fc.dir[a] == 1 ? fmaxf(del[a] - hi, 0.f) : 0.f;  // r(t + d), r(t - d)
+        rm[a] = fc.dir[a] == -1 ? fmaxf(del[a] - lo, 0.f) : 0.f;
+        hp[a] = fc.dir[a] == 1 ? fmaxf(hh[a] - hi, 0.f) : 0.f;   // r(t + h), r(t - h)
+        hm[a] = fc.dir[a] == -1 ? fmaxf(hh[a] - lo, 0.f) : 0.f;
+    }
+    // node (offsets o[0..2] from the cell's lowest corner, each in -1..2)
+    auto node = [&](int o0, int o1, int o2) -> float {
+        if (o0 >= 0 && o0 <= 1 && o1 >= 0 && o1 <= 1 && o2 >= 0 && o2 <= 1) return cc.c[o0 + 2 * o1 + 4 * o2];
+        return node32(g, c0[0] + o0, c0[1] + o1, c0[2] + o2);
+    };
+    // the second difference along axis a at offsets (b_off, c_off) of the other axes
+    auto d2 = [&](int a, int ob, int oc) -> float {
+        int o[3];
+        const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+        o[b] = ob;
+        o[c] = oc;
+        const int s0 = fc.dir[a] == 1 ? 2 : -1, s2 = fc.dir[a] == 1 ? 0 : 1;
+        o[a] = s0;
+        const float n0 = node(o[0], o[1], o[2]);
+        o[a] = fc.dir[a] == 1 ? 1 : 0;
+        const float n1 = node(o[0], o[1], o[2]);
+        o[a] = s2;
+        const float n2 = node(o[0], o[1], o[2]);
+        return n0 - 2.f * n1 + n2;
+    };
+    FaceTerms r;
+    float Ma[3], dMa[3][2];  // M_a, and its derivatives along a's two other axes (cell units)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        Ma[a] = dMa[a][0] = dMa[a][1] = 0.f;
+        r.g[a] = 0.f;
+        r.h[a] = 0.f;
+        if (fc.dir[a] == 0) continue;
+        const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
+        const float d00 = d2(a, 0, 0), d10 = d2(a, 1, 0), d01 = d2(a, 0, 1), d11 = d2(a, 1, 1);
+        const float tb = t[b], tc = t[c];
+        Ma[a] = (1.f - tc) * ((1.f - tb) * d00 + tb * d10) + tc * ((1.f - tb) * d01 + tb * d11);
+        dMa[a][0] = (1.f - tc) * (d10 - d00) + tc * (d11 - d01);  // along b
+        dMa[a][1] = (1.f - tb) * (d01 - d00) + tb * (d11 - d10);  // along c
+        r.g[a] = (rp[a] - rm[a]) * Ma[a] / (2.f * eps);
+        r.h[a] = (rp[a] + rm[a]) * Ma[a] / (eps * eps);
+    }
+    r.h[3] = r.h[4] = r.h[5] = 0.f;
+    if (!want_hessian) return r;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int a = q < 2 ? 0 : 1, b = q == 0 ? 1 : 2, c = 3 - a - b;
+        const float dra = hp[a] - hm[a], drb = hp[b] - hm[b];
+        float s = 0.f;
+        // dM_a along b: b is a's first other axis when b < c
+        if (dra != 0.f) s += dra * 2.f * hh[b] * dMa[a][b < c ? 0 : 1];
+        if (drb != 0.f) s += drb * 2.f * hh[a] * dMa[b][a < c ? 0 : 1];
+        if (dra != 0.f && drb != 0.f) {
+            float mab[2];
+#pragma unroll
+            for (int oc = 0; oc < 2; ++oc) {
+                float tot = 0.f;
+                const int sa[3] = {fc.dir[a] == 1 ? 2 : -1, fc.dir[a] == 1 ? 1 : 0, fc.dir[a] == 1 ? 0 : 1};
+                const int sb[3] = {fc.dir[b] == 1 ? 2 : -1, fc.dir[b] == 1 ? 1 : 0, fc.dir[b] == 1 ? 0 : 1};
+                const float wt[3] = {1.f, -2.f, 1.f};
+#pragma unroll
+                for (int x = 0; x < 3; ++x)
+#pragma unroll
+                    for (int y = 0; y < 3; ++y) {
+                        int o[3];
+                        o[a] = sa[x];
+                        o[b] = sb[y];
+                        o[c] = oc;
+                        tot += wt[x] * wt[y] * node(o[0], o[1], o[2]);
+                    }
+                mab[oc] = tot;
+            }
+            s += dra * drb * ((1.f - t[c]) * mab[0] + t[c] * mab[1]);
+        }
+        r.h[3 + q] = s / (eps * eps);
+    }
+    return r;
 }
 
 // A contact's grid-frame point and SDF jet from the exact path, computed ahead
@@ -775,7 +911,7 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
         return;
     }
     if constexpr (std::is_same<T, float>::value) {
-        if (fc && fc->ok && !stencil_only) {
+        if (fc && (fc->ok || fc->near) && !stencil_only) {
             const int i = fc->i, j = fc->j, k = fc->k;
             const double ud = fc->ud, vd = fc->vd, wd = fc->wd;
             double e[8];
@@ -835,6 +971,16 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
                 J.h[3] = ((1 - w) * (a10 - a00) + w * (a11 - a01)) * (ix * iy);
                 J.h[4] = ((1 - v) * (a01 - a00) + v * (a11 - a10)) * (ix * iz);
                 J.h[5] = ((b3 - b2) - (b1 - b0)) * (iy * iz);
+            }
+            if (fc->near) {  // the reference's stencil crosses faces: its extra terms in closed form
+                Corners32 c8;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) c8.c[q] = cc[q];
+                const FaceTerms ft = cross_face_terms(g, *fc, c8, want_hessian);
+                J.g = vec3<float>(J.g.x + ft.g[0], J.g.y + ft.g[1], J.g.z + ft.g[2]);
+                if (want_hessian)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) J.h[q] += ft.h[q];
             }
             return;
         }

@@ -568,11 +568,12 @@ __device__ __forceinline__ int acc_index(int k) {
     return b + 12 * (e % 12) + e / 12;
 }
 
-// CTAs of the FP32 path resident per SM (kForceCtasPerSm); the FP64 path is left its full
-// register budget.
-template <typename T>
+// CTAs of the FP32 path resident per SM (kForceCtasPerSm; kForceCtasPerSmGeneral for the
+// instantiation that serves every storage, BR = true); the FP64 path is left its full register
+// budget.
+template <typename T, bool BR = false>
 constexpr int force_min_blocks() {
-    return std::is_same<T, float>::value ? kForceCtasPerSm : 1;
+    return std::is_same<T, float>::value ? (BR ? kForceCtasPerSmGeneral : kForceCtasPerSm) : 1;
 }
 
 // Shares of an instance with `total` active contacts in chunks of `chunk` contacts, at least
@@ -699,7 +700,7 @@ __device__ __forceinline__ void force_item_chunks(ForceSmem<DERIV, T>& sm, const
         if constexpr (kWarpExact) {
             fc = fast_cell<T>(sm.g, sm.S.cm, xi, xf);
             fcp = &fc;
-            warp_exact_jets<T>(sm.g, sm.S, xi, valid && !fc.ok, DERIV, ej);
+            warp_exact_jets<T>(sm.g, sm.S, xi, valid && !fc.ok && !fc.near, DERIV, ej);
             ejp = &ej;
         }
         WarpSink<NV, T> sink{sm.acc + warp * NV, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
@@ -749,7 +750,7 @@ __device__ __forceinline__ void force_item_row(ForceSmem<DERIV, T>& sm, double* 
 // without the cell-corner array, 2 instances on grids with it (when a batch has both kinds,
 // the two instantiations split its instances).
 template <bool DERIV, bool STENCIL, typename T, bool BR = true>
-__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(
+__global__ void __launch_bounds__(kChunk, force_min_blocks<T, BR>()) force_kernel(
     const InstanceDesc* __restrict__ inst, const int* __restrict__ mode, const GridDesc* __restrict__ grids,
     const PointsDesc* __restrict__ points, const int* __restrict__ ids, const int* __restrict__ tile_count,
     const int* __restrict__ inst_total, const PairState<T>* __restrict__ pairs, double* __restrict__ partial, int skip,
@@ -776,7 +777,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_kernel(
 // next item is fetched while the current one runs (two item slots), and the row epilogue clears
 // the accumulators, so an item costs two CTA barriers.
 template <bool DERIV, bool STENCIL, typename T, bool BR = true>
-__global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) force_queue_kernel(
+__global__ void __launch_bounds__(kChunk, force_min_blocks<T, BR>()) force_queue_kernel(
     const InstanceDesc* __restrict__ inst, const GridDesc* __restrict__ grids, const PointsDesc* __restrict__ points,
     const int* __restrict__ ids, const int* __restrict__ tile_count, const int* __restrict__ inst_total,
     const PairState<T>* __restrict__ pairs, double* __restrict__ partial, int slots, int per,
@@ -911,7 +912,7 @@ __global__ void __launch_bounds__(32, worker_min_blocks<T>()) force_worker_kerne
             if constexpr (kWarpExact) {
                 fc = fast_cell<T>(g, S.cm, xi, xf);
                 fcp = &fc;
-                warp_exact_jets<T>(g, S, xi, valid && !fc.ok, DERIV, ej);
+                warp_exact_jets<T>(g, S, xi, valid && !fc.ok && !fc.near, DERIV, ej);
                 ejp = &ej;
             }
             WarpSink<NV, T> sink{acc, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
@@ -1005,7 +1006,7 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
         if constexpr (kWarpExact) {
             fc = fast_cell<T>(g, S.cm, xi, xf);
             fcp = &fc;
-            warp_exact_jets<T>(g, S, xi, valid && !fc.ok, false, ej);
+            warp_exact_jets<T>(g, S, xi, valid && !fc.ok && !fc.near, false, ej);
             ejp = &ej;
         }
         const ContactEnergy<T> E = contact_energy<T>(g, xi, S, fcp, valid, STENCIL, ejp);
@@ -1145,18 +1146,18 @@ __global__ void gather_inputs_kernel(const HostIO* __restrict__ io, double* __re
     }
 }
 
-// CTAs of `kernel` (block `threads`, dynamic shared memory `smem`) resident on the device at
-// once: the persistent force passes launch this many (looked up once per kernel).
+// CTAs of `kernel` (block `threads`, dynamic shared memory `smem`) resident on the current
+// device at once: the persistent force passes launch this many (the per-SM count looked up once
+// per kernel, times the device's SMs).
 template <typename K>
-int resident_ctas(K kernel, int threads, size_t smem, std::atomic<int>& cache) {
-    int c = cache.load(std::memory_order_relaxed);
-    if (c > 0) return c;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    c = per_sm * device_sm_count();
-    cache.store(c, std::memory_order_relaxed);
-    return c;
+int resident_ctas(K kernel, int threads, size_t smem, std::atomic<int>& per_sm_cache) {
+    int per_sm = per_sm_cache.load(std::memory_order_relaxed);
+    if (per_sm <= 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        per_sm_cache.store(per_sm, std::memory_order_relaxed);
+    }
+    return per_sm * device_sm_count();
 }
 
 // Contacts per chunk of the batch's force-pass form.

@@ -65,6 +65,11 @@ constexpr int kDetectThreads = 256;  // threads per detection CTA
 #endif
 constexpr int kChunk = SDFC_FORCE_CHUNK;
 constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
+// the same for the force instantiation that serves every grid storage (FP16 bricks, FP32 nodes)
+#ifndef SDFC_FORCE_MIN_BLOCKS_GENERAL
+#define SDFC_FORCE_MIN_BLOCKS_GENERAL SDFC_FORCE_MIN_BLOCKS
+#endif
+constexpr int kForceCtasPerSmGeneral = SDFC_FORCE_MIN_BLOCKS_GENERAL;
 constexpr int kMaxSlots = 32;        // partial rows per instance, at most
 // Multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked up once per
 // device): launch shapes follow it.
