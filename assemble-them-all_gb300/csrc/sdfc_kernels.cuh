@@ -61,13 +61,13 @@ constexpr int kDetectThreads = 256;  // threads per detection CTA
 #define SDFC_FORCE_CHUNK 128
 #endif
 #ifndef SDFC_FORCE_MIN_BLOCKS
-#define SDFC_FORCE_MIN_BLOCKS 5
+#define SDFC_FORCE_MIN_BLOCKS 4
 #endif
 constexpr int kChunk = SDFC_FORCE_CHUNK;
 constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
 // the same for the force instantiation that serves every grid storage (FP16 bricks, FP32 nodes)
 #ifndef SDFC_FORCE_MIN_BLOCKS_GENERAL
-#define SDFC_FORCE_MIN_BLOCKS_GENERAL SDFC_FORCE_MIN_BLOCKS
+#define SDFC_FORCE_MIN_BLOCKS_GENERAL 5
 #endif
 constexpr int kForceCtasPerSmGeneral = SDFC_FORCE_MIN_BLOCKS_GENERAL;
 constexpr int kMaxSlots = 32;        // partial rows per instance, at most

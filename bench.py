@@ -1187,9 +1187,9 @@ def c4_gradient_check(sdfc, ctx, g, ph, mv, q0, dirs, T, target, g0_mixed, gf_mi
     at the direction (2).  The loss is piecewise smooth (contact points entering the active set
     are kinks), so differences at 1e-6 straddle kinks; at 1e-8 they resolve the derivative except
     for components whose +- rollouts still straddle a kink, which the 3e-9 differences reveal
-    (they disagree with the 1e-8 ones), or that have a kink at the base point itself, which the
-    one-sided 1e-8 differences reveal: those are reported apart, as the GPU test of this check
-    does.  An instance with a step that did not converge (its loss is not differentiable there)
+    (they disagree with the 1e-8 ones), or that have a kink at the base point itself, whose
+    one-sided slopes keep their gap at both 1e-8 and 3e-9: those are reported apart, as the GPU
+    test of this check does.  An instance with a step that did not converge (its loss is not differentiable there)
     is marked.  The FP64 adjoint comes from the tightly solved base scene; the mixed one is the
     timed rollout's (FP32 per-contact algebra, the reference's Newton tolerance 1e-8)."""
     n = len(q0)
@@ -1252,14 +1252,16 @@ def c4_gradient_check(sdfc, ctx, g, ph, mv, q0, dirs, T, target, g0_mixed, gf_mi
             fds[h] = fd
             row[f"fp64_adjoint_vs_fd_{h:g}"] = float(np.linalg.norm(a64 - fd) / np.linalg.norm(fd))
             row[f"all_steps_converged_{h:g}"] = bool(conv[o] and conv[o + 1 + 16 * mm:o + 1 + 16 * (mm + 1)].all())
-        # components whose 1e-8 and 3e-9 central differences agree and whose one-sided 1e-8
-        # differences agree (no kink between the +- rollouts, none at the base point, where both
-        # central differences would average the two one-sided slopes): the adjoint against the
-        # 1e-8 difference there, relative to the gradient's norm
+        # components whose 1e-8 and 3e-9 central differences agree and that show no kink at the
+        # base point (where both central differences average the two one-sided slopes): the
+        # adjoint against the 1e-8 difference there, relative to the gradient's norm
         scale = np.linalg.norm(fds[1e-8])
-        r8 = L[o + 1 + 16:o + 33]
-        one_sided = np.abs((r8[0::2] - L[o]) - (L[o] - r8[1::2])) / 1e-8
-        smooth = (np.abs(fds[1e-8] - fds[3e-9]) <= 1e-5 * scale) & (one_sided <= 1e-5 * scale)
+        gap = {}  # one-sided slope gaps: shrink with the step under curvature, stay at a kink
+        for mm in (1, 2):
+            r = L[o + 1 + 16 * mm:o + 1 + 16 * (mm + 1)]
+            gap[mm] = np.abs((r[0::2] - L[o]) - (L[o] - r[1::2])) / steps[mm]
+        kink_at_base = (gap[1] > 1e-5 * scale) & (gap[2] > 0.6 * gap[1])
+        smooth = (np.abs(fds[1e-8] - fds[3e-9]) <= 1e-5 * scale) & ~kink_at_base
         row["smooth_components"] = int(smooth.sum())
         row["fp64_adjoint_vs_fd_1e-08_smooth"] = float(np.abs(a64 - fds[1e-8])[smooth].max() / scale) if smooth.any() else None
         rows.append(row)
