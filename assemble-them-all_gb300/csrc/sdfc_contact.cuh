@@ -152,6 +152,11 @@ struct GridDesc {
     float fmin[3], fmax[3], finv_dx[3], fdx[3];  // FP32 constants
     float lip;        // bound on |grad| of the interpolant over the grid
     float vmax;       // max |value|
+    // per block of 2^bshift cells per axis (block (bi, bj, bk) at bi + bnx (bj + bny bk)): the
+    // least FP32 node value over the nodes of its cells, so detection can tell that a point is
+    // far outside the surface without reading its cell (null: no table, as for FP16 bricks)
+    const float* bmin;
+    int bshift, bnx, bny, bpad;
 };
 
 // A contact body's points, stored on the device in a spatially sorted order

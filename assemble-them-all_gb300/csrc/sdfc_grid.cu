@@ -1,13 +1,15 @@
 // Device-side preparation of uploaded SDF grids (storages 0, 1 and 3): the bounds the
 // detection prefilter needs (largest |value| and, per axis, the largest difference of
-// neighbouring values), the FP32 cell-corner array and the FP64 copy, built from node values
-// already on the device, so that large grids (256^3 nodes and more) and grids generated on the
+// neighbouring values), detection's block table of least node values, the FP32 cell-corner
+// array and the FP64 copy, built from node values already on the device, so that large grids (256^3 nodes and more) and grids generated on the
 // device never pass through a host loop.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+
+#include <math_constants.h>
 
 #include "sdfc_internal.h"
 
@@ -62,6 +64,25 @@ __global__ void cell_corners_kernel(const T* __restrict__ v, int ni, int nj, int
         cells[2 * c] = make_float4((float)v[b], (float)v[b + 1], (float)v[b + sj], (float)v[b + sj + 1]);
         cells[2 * c + 1] =
             make_float4((float)v[b + sk], (float)v[b + sk + 1], (float)v[b + sk + sj], (float)v[b + sk + sj + 1]);
+    }
+}
+
+// Per block of 2^bs cells per axis, the least FP32 node value over the nodes of its cells
+// (nodes bB .. min(bB + B, n - 1) per axis), block (bi, bj, bk) at bi + bnx (bj + bny bk).
+template <typename T>
+__global__ void block_min_kernel(const T* __restrict__ v, int ni, int nj, int nk, int bs, int bnx, int bny, int bnz,
+                                 float* __restrict__ out) {
+    const size_t nb = (size_t)bnx * bny * bnz, sj = (size_t)ni, sk = (size_t)ni * nj;
+    const int B = 1 << bs;
+    for (size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x; b < nb; b += (size_t)gridDim.x * blockDim.x) {
+        const int bi = (int)(b % bnx), bj = (int)((b / bnx) % bny), bk = (int)(b / ((size_t)bnx * bny));
+        const int i0 = bi * B, j0 = bj * B, k0 = bk * B;
+        const int i1 = min(i0 + B, ni - 1), j1 = min(j0 + B, nj - 1), k1 = min(k0 + B, nk - 1);
+        float m = CUDART_INF_F;
+        for (int k = k0; k <= k1; ++k)
+            for (int j = j0; j <= j1; ++j)
+                for (int i = i0; i <= i1; ++i) m = fminf(m, (float)v[(size_t)i + sj * j + sk * k]);
+        out[b] = m;
     }
 }
 
@@ -121,6 +142,27 @@ int grid_finish_device(sdfc_context* ctx, sdfc::GridDesc& g, const void* d_value
                                                                             (float4*)pc);
         g.cells32 = (const float4*)pc;
         SDFC_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    {
+        // detection's block table: 2-cell blocks beside the 40-byte cell-corner layout (an eighth
+        // of a node's 4 bytes more per node), 4-cell blocks beside 4-byte node values
+        const int bs = cells ? 1 : 2, B = 1 << bs;
+        const int bnx = (ni - 1 + B - 1) / B, bny = (nj - 1 + B - 1) / B, bnz = (nk - 1 + B - 1) / B;
+        const size_t nb = (size_t)bnx * bny * bnz;
+        void* pb = nullptr;
+        if ((rc = dev_alloc(ctx, &pb, nb * sizeof(float)))) return rc;
+        ctx->allocations.push_back(pb);
+        if (fp32)
+            block_min_kernel<float><<<grid_blocks(ctx, nb), 256, 0, s>>>((const float*)d_values, ni, nj, nk, bs, bnx, bny,
+                                                                        bnz, (float*)pb);
+        else
+            block_min_kernel<double><<<grid_blocks(ctx, nb), 256, 0, s>>>((const double*)d_values, ni, nj, nk, bs, bnx,
+                                                                         bny, bnz, (float*)pb);
+        SDFC_CUDA_TRY(ctx, cudaGetLastError());
+        g.bmin = (const float*)pb;
+        g.bshift = bs;
+        g.bnx = bnx;
+        g.bny = bny;
     }
     SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     return SDFC_OK;

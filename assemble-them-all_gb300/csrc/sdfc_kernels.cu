@@ -47,6 +47,19 @@ __device__ void make_prefilter(const GridDesc& g, const PointsDesc& P, const Pos
     f.col_th = (float)g.col_th;
     double bound = (double)g.lip * eps_pos + 12.0 * kU * (double)g.vmax + 2.0 * kU * fabs(g.col_th);
     f.guard = (float)(4.0 * bound) + 1e-30f;
+    // The FP32 trilinear of a cell's FP32 corners is within 16 u vmax of their convex
+    // combination (7 lerps, each difference and fma rounded), and the FP32 fraction of a cell
+    // coordinate up to n may leave [0, 1] by n u, extrapolating by at most that times the largest
+    // corner difference (lip dx); so the computed value is at least the block's least node value
+    // less that margin, and its sum with col_th at least that less one more rounding.
+    int nmax = max(g.ni, max(g.nj, g.nk));
+    double dmax = fmax(g.dx[0], fmax(g.dx[1], g.dx[2]));
+    const double margin = 16.0 * kU * (double)g.vmax + 2.0 * nmax * kU * (double)g.lip * dmax +
+                          4.0 * kU * (fabs(g.col_th) + (double)f.guard + (double)g.vmax);
+    const double th = (double)f.guard - (double)f.col_th + margin;
+    float t = (float)th;
+    if ((double)t < th) t = nextafterf(t, CUDART_INF_F);
+    f.skip_th = t;
 }
 
 __global__ void prep_kernel(const InstanceDesc* __restrict__ inst, int n, BatchInputs in,
@@ -97,14 +110,19 @@ __device__ __forceinline__ void warp_copy(S& dst, const S& src, int lane) {
 
 // FP32 trilinear interpolation for a point certainly inside the box, from the
 // cell-corner array (GridDesc::cells32) or, with `g` non-null, from FP16 bricks.
+// With the block table `bm` (GridDesc::bmin), a point whose cell's block has its least node
+// value above f.skip_th returns +inf without reading the cell: its distance is then neither in
+// the guard band nor active, as the trilinear would have found.
 __device__ __forceinline__ float trilinear32(const float4* __restrict__ cells, const GridDesc* g, int ni, int nj,
-                                             int nk, const Prefilter& f, float x, float y, float z) {
+                                             int nk, const Prefilter& f, float x, float y, float z,
+                                             const float* __restrict__ bm, int bsh, int bnx, int bny) {
     float cx = (x - f.gmin[0]) * f.ginv[0];
     float cy = (y - f.gmin[1]) * f.ginv[1];
     float cz = (z - f.gmin[2]) * f.ginv[2];
     int i = min(max((int)floorf(cx), 0), ni - 2);
     int j = min(max((int)floorf(cy), 0), nj - 2);
     int k = min(max((int)floorf(cz), 0), nk - 2);
+    if (bm && __ldg(bm + (i >> bsh) + bnx * ((j >> bsh) + bny * (k >> bsh))) > f.skip_th) return CUDART_INF_F;
     float u = cx - (float)i, w1 = cy - (float)j, w2 = cz - (float)k;
     float c000, c100, c010, c110, c001, c101, c011, c111;
     if (g) {
@@ -180,7 +198,8 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
     __shared__ DetectGrid<BRICKS> dg;
     __shared__ const float4* gv;
     __shared__ const float* px;
-    __shared__ int gn[3], pn;
+    __shared__ const float* bmin;
+    __shared__ int gn[3], pn, bsh, bnx, bny;
     __shared__ int cnt_a[kTile / 32], cnt_q[kTile / 32];  // per (round, warp): counts, then offsets
     const int t = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -205,6 +224,10 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
         gn[2] = g.nk;
         px = points[I.points].x32;
         pn = points[I.points].n;
+        bmin = g.bmin;
+        bsh = g.bshift;
+        bnx = g.bnx;
+        bny = g.bny;
     }
     __syncthreads();
     {
@@ -257,7 +280,8 @@ __global__ void __launch_bounds__(kDetectThreads) detect_kernel(const InstanceDe
                 const bool surely_in = x >= f.lo_in[0] && x <= f.hi_in[0] && y >= f.lo_in[1] && y <= f.hi_in[1] &&
                                        z >= f.lo_in[2] && z <= f.hi_in[2];
                 if (surely_in) {
-                    const float d32 = trilinear32(gv, dg.get(), gn[0], gn[1], gn[2], f, x, y, z) + f.col_th;
+                    const float d32 =
+                        trilinear32(gv, dg.get(), gn[0], gn[1], gn[2], f, x, y, z, bmin, bsh, bnx, bny) + f.col_th;
                     if (fabsf(d32) <= f.guard)
                         queue = true;
                     else

@@ -127,6 +127,9 @@ struct Prefilter {
     float lo_out[3], hi_out[3];  // certainly outside beyond these
     float col_th;
     float guard;                 // bound on |d32 - d64|, times a safety factor
+    // a point whose cell lies in a block with least node value above this is neither active nor
+    // within the guard band (GridDesc::bmin): guard - col_th plus the FP32 trilinear's error bound
+    float skip_th;
 };
 
 // Per-evaluation inputs, device pointers (row-major 4x4 poses, body twists).
