@@ -156,7 +156,8 @@ def test_edge_cases(sdfc, ctx, oracle, workloads):
     far = ctx.upload_points(np.full((100, 3), 7.0), 1)
     fm, Km, Dm, n = ctx.evaluate(far, grid, I, z, I, z, prm)
     assert n == 0 and not fm.any()
-    # points on grid nodes and cell faces (the reference's stencil straddles cells there)
+    # points a few hundredths of a cell from grid nodes (their stencils stay in the cell; contacts
+    # whose stencil crosses faces: test_contacts_near_cell_faces)
     ax = g.min_box[0] + g.dx[0] * np.arange(3, 13)
     P = np.array([[x, y, zz] for x in ax[::3] for y in ax[::3] for zz in ax]).astype(np.float32).astype(np.float64)
     P = P[np.abs(workloads.socket_sdf(P)) < 0.3]
@@ -169,7 +170,7 @@ def test_edge_cases(sdfc, ctx, oracle, workloads):
     assert_close("nodes fm", fm, rf, rel=FM_REL)
     assert_close("nodes Km", Km, rK, rel=JAC_REL)
     assert_close("nodes Dm", Dm, rD, rel=JAC_REL)
-    # mixed precision: these contacts sit on cell faces and take the deferred exact path
+    # mixed precision on the same contacts
     ctx.set_precision(sdfc.PRECISION_MIXED)
     for deriv in (True, False):
         fm, Km, Dm, n = ctx.evaluate(nodes, grid, EA, z, I, z, prm, want_deriv=deriv)
@@ -195,6 +196,92 @@ def test_edge_cases(sdfc, ctx, oracle, workloads):
     assert n == len(rids)
     assert_close("tiny fm", fm, rf, rel=FM_REL)
     assert_close("tiny Km", Km, rK, rel=JAC_REL)
+
+
+def near_face_cells(rng, shape, mn, dx, count):
+    """Grid-frame points whose derivative stencil (BodySDFObj.cpp:176-205, steps 1e-5 and 5e-6)
+    reaches across faces of their cell: on one, two or three axes (faces, edges, corners), on
+    either side, at distances from the face of 0 to just past the stencil's reach (1e-5 and the
+    1.0001e-5 band the FP32 classification rounds to), some in the grid's outermost cells, where
+    the next layer of nodes does not exist."""
+    dists = (0.0, 2.5e-6, 4.9e-6, 5.1e-6, 9.9e-6, 1e-5 - 1e-9, 1.00005e-5, 1.05e-5)
+    pts = []
+    for q in range(count):
+        cell = np.array([rng.integers(0, n - 1) for n in shape])
+        f = rng.uniform(0.15, 0.85, 3)
+        axes = rng.choice(3, 1 + q % 3, replace=False)
+        for m, a in enumerate(axes):
+            d = dists[rng.integers(len(dists))] / dx[a]
+            up = rng.random() < 0.5
+            if q % 7 == 0 and m == 0:  # toward the grid's outside
+                cell[a] = shape[a] - 2 if up else 0
+            f[a] = 1.0 - d if up else d
+        pts.append(mn + dx * (cell + f))
+    return np.array(pts)
+
+
+@pytest.mark.parametrize("point_storage", [0, 1])
+@pytest.mark.parametrize("grid_storage", [0, 1, 3])
+def test_contacts_near_cell_faces(sdfc, ctx, oracle, workloads, grid_storage, point_storage):
+    """Single contacts whose derivative stencil crosses faces of their cell, each one instance of
+    a batch, against the oracle (the reference's stencil) per contact.  The FP64 path takes the
+    reference's own stencil there; the mixed path its closed form (cell derivatives plus the
+    face-crossing terms).  The grid is anisotropic (12 x 10 x 14 nodes, three spacings) and its
+    values curve along every axis, so every second difference the closed form uses is nonzero;
+    every node lies below -col_th, so every contact inside the grid box is active."""
+    rng = np.random.default_rng(1234)
+    shape = (12, 10, 14)
+    mn, mx = np.array([0.0, 0.0, 0.0]), np.array([0.25, 0.2, 0.3])
+    dx = (mx - mn) / (np.array(shape) - 1)
+    ax = [mn[a] + dx[a] * np.arange(shape[a]) for a in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    S = np.array([1.0, 1.3, 0.8])
+    c = np.array([0.11, 0.1, 0.16])
+    vals = np.sqrt((((np.stack([X, Y, Z], -1) - c) * S) ** 2).sum(-1)) - 0.3
+    vals = vals.astype(np.float32).astype(np.float64)  # (nk, nj, ni)
+    assert vals.max() < -0.05
+    gh = ctx.upload_grid(vals, mn, mx, dx, 0.01, grid_storage)
+    og = oracle.Grid(vals, mn, mx, dx, 0.01)
+    xs = near_face_cells(rng, shape, mn, dx, 180)
+    n = len(xs)
+    EB = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.4), rng.normal(size=3))
+                   for _ in range(n)])
+    EA = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.4), rng.normal(size=3))
+                   for _ in range(n)])
+    # body-A points that the poses carry onto the grid-frame points (x_B = E_B^-1 E_A p)
+    P = np.einsum("nij,nj->ni", np.linalg.inv(EA) @ EB, np.c_[xs, np.ones(n)])[:, :3]
+    if point_storage == 1:
+        P = P.astype(np.float32).astype(np.float64)
+    phs = [ctx.upload_points(P[k:k + 1], point_storage) for k in range(n)]
+    phiA = rng.normal(size=(n, 6)) * 0.2
+    phiB = rng.normal(size=(n, 6)) * 0.1
+    prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0)] * n
+    op = oracle.Params(1e5, 1e3, 0.3, 1e3, 1.0, 1.0)
+    ref = [oracle.pair_eval(og, P[k:k + 1], EA[k], phiA[k], EB[k], phiB[k], op, True) for k in range(n)]
+    # (FP32 point storage can round a point on the grid box's face to outside it: no contact, as
+    # in the reference)
+    active = np.array([len(r[3]) for r in ref])
+    assert active.sum() >= 0.95 * n
+    b = ctx.batch(phs, [gh] * n)
+    try:
+        for precision, stencil, rel_f, rel_j in ((0, 0, FM_REL, JAC_REL), (0, 1, FM_REL_STENCIL, JAC_REL_STENCIL),
+                                                 (1, 0, MIXED_REL, MIXED_REL)):
+            b.set_precision(precision)
+            b.set_derivative_mode(stencil)
+            fm, Km, Dm, nact, st = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=True)
+            assert np.array_equal(nact, active) and not st.any()
+            for k in range(n):
+                rf, rK, rD, _ = ref[k]
+                tag = f"contact {k} at {xs[k]} (precision {precision}, stencil {stencil})"
+                assert_close(f"{tag} fm", fm[k], rf, rel=rel_f)
+                assert_close(f"{tag} Km", Km[k], rK, rel=rel_j)
+                assert_close(f"{tag} Dm", Dm[k], rD, rel=rel_j)
+            fv, _, _, nv, _ = b.evaluate(EA, phiA, EB, phiB, prm, want_deriv=False)
+            assert np.array_equal(nv, active)
+            for k in range(n):
+                assert_close(f"value pass {k}", fv[k], ref[k][0], rel=rel_f)
+    finally:
+        b.close()
 
 
 def test_invalid_arguments(sdfc, ctx):
