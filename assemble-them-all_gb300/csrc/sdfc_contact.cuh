@@ -711,6 +711,18 @@ __device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const CellMap& 
     return c;
 }
 
+// A node's value as the FP32 paths read it: the FP32 node value, the FP16 brick decode, or the
+// cell-corner array's copy (FP64 grids: its FP32 rounding).
+__device__ __forceinline__ float node32(const GridDesc& g, int i, int j, int k) {
+    if (g.b16) return brick_value32(g, i, j, k);
+    const size_t idx = (size_t)i + (size_t)g.ni * ((size_t)j + (size_t)g.nj * (size_t)k);
+    if (g.v32) return __ldg(g.v32 + idx);
+    if (i < g.ni - 1 && j < g.nj - 1 && k < g.nk - 1)
+        return __ldg(reinterpret_cast<const float*>(
+            g.cells32 + 2 * ((size_t)i + (size_t)(g.ni - 1) * ((size_t)j + (size_t)(g.nj - 1) * k))));
+    return (float)__ldg(g.v64 + idx);
+}
+
 // The reference's derivative stencil (BodySDFObj.cpp:176-205: gradient by central differences
 // at +-eps, Hessian by second differences at +-eps and mixed ones at +-eps/2) where it crosses
 // faces of the contact's cell, in closed form.  Along an axis the interpolant over two cells is
@@ -722,17 +734,22 @@ __device__ __forceinline__ FastCell fast_cell(const GridDesc& g, const CellMap& 
 //   Hessian ab:  (dr_a 2 h_b dM_a/db + dr_b 2 h_a dM_b/da + dr_a dr_b M_ab) / eps^2
 // with d = eps / dx, h = d / 2, dr = r(t + h) - r(t - h), M_a the second difference along a
 // interpolated bilinearly at the point's other two coordinates, M_ab the product of the two
-// second differences interpolated along the third.  The second differences are formed in FP64
-// from the nodes' FP64 values as differences of differences ((n0 - n1) - (n1 - n2)): in FP32,
-// n0 - 2 n1 rounds at the larger value's exponent and the cancellation against n2 keeps that
-// error (measured 2e-5 of the face terms on a curved grid).  The rest is products of small
-// numbers, so FP32 keeps its relative precision where the FP64 differences of the reference
-// cancel.  The distances to the faces come from the FP64 fractions.  Equal to the reference's
-// stencil in exact arithmetic (checked against exact rational arithmetic on random cells).
+// second differences interpolated along the third.  The second differences are formed as
+// differences of differences, (n0 - n1) - (n1 - n2): neighbouring node values are close, so the
+// inner differences are exact or nearly so, where n0 - 2 n1 + n2 rounds at the larger value's
+// exponent and the cancellation against n2 keeps that error (measured 1.75e-5 of the face terms on
+// a curved grid, 5e-7 with the nested form).  The in-cell nodes come from the cell's FP32 corners
+// already in registers, the others from the FP32 node reads (FP64 grids: their FP32 rounding, as
+// the cell's own FP32 derivatives use).  The rest is products of small numbers, so FP32 keeps its
+// relative precision where the FP64 differences of the reference cancel.  The distances beyond
+// the faces come from the FP64 fractions (in FP64 where they are small, below).  Equal to the
+// reference's stencil in exact arithmetic
+// (checked against exact rational arithmetic on random cells).
 struct FaceTerms {
     float g[3], h[6];
 };
-static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, const FastCell& fc, bool want_hessian) {
+static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, const FastCell& fc, Corners32 cc,
+                                                          bool want_hessian) {
     const double fr[3] = {fc.ud, fc.vd, fc.wd};
     const int c0[3] = {fc.i, fc.j, fc.k};
     const float eps = (float)kFdEps;
@@ -740,29 +757,48 @@ static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, con
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         t[a] = (float)fr[a];
-        // the distances beyond the faces in FP64: d - (1 - t) cancels where the stencil just
-        // reaches a face, and its FP32 rounding would then cost the term its relative precision
-        const double lo = fr[a], hi = 1.0 - fr[a];  // distances to the lower / upper face
-        const double d64 = kFdEps * g.inv_dx[a], h64 = 0.5 * d64;
-        hh[a] = (float)h64;
-        rp[a] = fc.dir[a] == 1 ? (float)fmax(d64 - hi, 0.0) : 0.f;  // r(t + d), r(t - d)
-        rm[a] = fc.dir[a] == -1 ? (float)fmax(d64 - lo, 0.0) : 0.f;
-        hp[a] = fc.dir[a] == 1 ? (float)fmax(h64 - hi, 0.0) : 0.f;  // r(t + h), r(t - h)
-        hm[a] = fc.dir[a] == -1 ? (float)fmax(h64 - lo, 0.0) : 0.f;
+        hh[a] = 0.5f * eps * g.finv_dx[a];
+        rp[a] = rm[a] = hp[a] = hm[a] = 0.f;  // r(t + d), r(t - d), r(t + h), r(t - h)
+        if (fc.dir[a] != 0) {
+            // the distances beyond the crossed face, r = d - (distance to the face) for the steps d
+            // and d / 2: FP32 where r is at least d / 8, FP64 where it is smaller (the difference
+            // cancels there, and FP32's absolute error 2^-24 d would be a large part of r)
+            const float del = eps * g.finv_dx[a];
+            const float dist = fc.dir[a] == 1 ? (float)(1.0 - fr[a]) : t[a];
+            float r1 = del - dist, r2 = 0.5f * del - dist;
+            const float lim = 0.125f * del;
+            if ((r1 > -lim && r1 < lim) || (r2 > -lim && r2 < lim)) {
+                const double d64 = kFdEps * g.inv_dx[a];
+                const double off = fc.dir[a] == 1 ? fr[a] - 1.0 : -fr[a];
+                r1 = (float)(d64 + off);
+                r2 = (float)fma(0.5, d64, off);
+            }
+            r1 = fmaxf(r1, 0.f);
+            r2 = fmaxf(r2, 0.f);
+            if (fc.dir[a] == 1) {
+                rp[a] = r1;
+                hp[a] = r2;
+            } else {
+                rm[a] = r1;
+                hm[a] = r2;
+            }
+        }
     }
-    // the node at offsets o[0..2] (each in -1..2) from the cell's lowest corner, in FP64
-    auto node = [&](const int* o) -> double { return grid_value(g, c0[0] + o[0], c0[1] + o[1], c0[2] + o[2]); };
+    // the node at offsets o[0..2] (each in -1..2) from the cell's lowest corner
+    auto node = [&](const int* o) -> float {
+        if (o[0] >= 0 && o[0] <= 1 && o[1] >= 0 && o[1] <= 1 && o[2] >= 0 && o[2] <= 1)
+            return cc.c[o[0] + 2 * o[1] + 4 * o[2]];
+        return node32(g, c0[0] + o[0], c0[1] + o[1], c0[2] + o[2]);
+    };
     // node offsets along axis a of the second difference across the crossed face: the node
     // beyond it, the face's node, the cell's other node
-    auto across = [&](int a, int m) -> int {
-        return fc.dir[a] == 1 ? 2 - m : m - 1;
-    };
+    auto across = [&](int a, int m) -> int { return fc.dir[a] == 1 ? 2 - m : m - 1; };
     // the second difference along axis a at offsets (ob, oc) of a's two other axes
-    auto d2 = [&](int a, int ob, int oc) -> double {
+    auto d2 = [&](int a, int ob, int oc) -> float {
         int o[3];
         o[a == 0 ? 1 : 0] = ob;
         o[a == 2 ? 1 : 2] = oc;
-        double n[3];
+        float n[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
             o[a] = across(a, m);
@@ -779,12 +815,11 @@ static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, con
         r.h[a] = 0.f;
         if (fc.dir[a] == 0) continue;
         const int b = a == 0 ? 1 : 0, c = a == 2 ? 1 : 2;
-        const double e00 = d2(a, 0, 0), e10 = d2(a, 1, 0), e01 = d2(a, 0, 1), e11 = d2(a, 1, 1);
-        const float d00 = (float)e00, d10 = (float)e10, d01 = (float)e01, d11 = (float)e11;
+        const float d00 = d2(a, 0, 0), d10 = d2(a, 1, 0), d01 = d2(a, 0, 1), d11 = d2(a, 1, 1);
         const float tb = t[b], tc = t[c];
         Ma[a] = (1.f - tc) * ((1.f - tb) * d00 + tb * d10) + tc * ((1.f - tb) * d01 + tb * d11);
-        dMa[a][0] = (1.f - tc) * (float)(e10 - e00) + tc * (float)(e11 - e01);  // along b
-        dMa[a][1] = (1.f - tb) * (float)(e01 - e00) + tb * (float)(e11 - e10);  // along c
+        dMa[a][0] = (1.f - tc) * (d10 - d00) + tc * (d11 - d01);  // along b
+        dMa[a][1] = (1.f - tb) * (d01 - d00) + tb * (d11 - d10);  // along c
         r.g[a] = (rp[a] - rm[a]) * Ma[a] / (2.f * eps);
         r.h[a] = (rp[a] + rm[a]) * Ma[a] / (eps * eps);
     }
@@ -803,13 +838,13 @@ static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, con
 #pragma unroll
             for (int oc = 0; oc < 2; ++oc) {
                 // the second difference along b of the second differences along a
-                double e[3];
+                float e[3];
 #pragma unroll
                 for (int y = 0; y < 3; ++y) {
                     int o[3];
                     o[b] = across(b, y);
                     o[c] = oc;
-                    double n[3];
+                    float n[3];
 #pragma unroll
                     for (int m = 0; m < 3; ++m) {
                         o[a] = across(a, m);
@@ -817,7 +852,7 @@ static __device__ __noinline__ FaceTerms cross_face_terms(const GridDesc& g, con
                     }
                     e[y] = (n[0] - n[1]) - (n[1] - n[2]);
                 }
-                mab[oc] = (float)((e[0] - e[1]) - (e[1] - e[2]));
+                mab[oc] = (e[0] - e[1]) - (e[1] - e[2]);
             }
             s += dra * drb * ((1.f - t[c]) * mab[0] + t[c] * mab[1]);
         }
@@ -972,7 +1007,10 @@ __device__ inline void contact_geometry(const GridDesc& g, const PairState<T>& S
                 J.h[5] = ((b3 - b2) - (b1 - b0)) * (iy * iz);
             }
             if (fc->near) {  // the reference's stencil crosses faces: its extra terms in closed form
-                const FaceTerms ft = cross_face_terms(g, *fc, want_hessian);
+                Corners32 c8;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) c8.c[q] = cc[q];
+                const FaceTerms ft = cross_face_terms(g, *fc, c8, want_hessian);
                 J.g = vec3<float>(J.g.x + ft.g[0], J.g.y + ft.g[1], J.g.z + ft.g[2]);
                 if (want_hessian)
 #pragma unroll
