@@ -64,6 +64,21 @@ struct SceneState {
     double q0[kMaxDof], qd0[kMaxDof], x[kMaxDof], dx[kMaxDof], xt[kMaxDof];
     double gnorm, alpha;
     int phase, iter, trial, strike, converged;
+    int step;  // steps this scene has finished in the current sdfc_sim_step call
+    int nev;   // evaluations in its current step
+};
+
+// Evaluations one scene may spend on one step: the reference's Newton stops after max_iter
+// iterations of at most 1 + 20 evaluations (Simulation.cpp:1009-1054); past this a step ends at
+// its current iterate, unconverged (a bound that the stopping rules reach first).
+constexpr int kMaxEvalsPerStep = 120 * (1 + kMaxLineSearch) + 2;
+
+// Per sdfc_sim_step call, read by the Newton kernels (device memory, so that the captured round
+// graphs stay valid across calls): the steps every scene takes, the recording row of the call's
+// first step and the recorded trajectory (null when recording is off).
+struct SimCtl {
+    int target, rec_base;
+    double* qhis;
 };
 
 __device__ inline sdfc_joint::FreeBody free_body(const MoverDev& m) {
@@ -126,11 +141,14 @@ __global__ void sim_begin_kernel(int n, int nd, const MoverDev* __restrict__ mov
     s.alpha = 1.0;
     s.phase = kNewton;
     s.iter = s.trial = s.strike = s.converged = 0;
+    s.step = s.nev = 0;
     st[i] = s;
 }
 
-// Poses of pair k (mover posed by its scene's current iterate) into evaluation slot j.
-__device__ inline void pose_pair(int k, int j, const int* __restrict__ pair_inst, const int* __restrict__ role,
+// Poses of pair k (mover posed by its scene's current iterate) into evaluation slot j.  One
+// compiled copy serves the full and the compacted rounds, so both pose a scene with the same
+// arithmetic (inlined into each kernel, the joint's multiply-adds could contract differently).
+__device__ __noinline__ void pose_pair(int k, int j, const int* __restrict__ pair_inst, const int* __restrict__ role,
                                  const double* __restrict__ E_fixed, const MoverDev* __restrict__ mover,
                                  const SceneState* __restrict__ st, double* __restrict__ EA, double* __restrict__ phiA,
                                  double* __restrict__ EB, double* __restrict__ phiB, int* __restrict__ mode) {
@@ -379,13 +397,53 @@ __device__ void trans_system(const MoverDev& m, const double* __restrict__ fe, c
         }
 }
 
+// Ends scene i's step at its current iterate: q = x, qdot = (x - q0) / h, the free joint's
+// rotation vector reparameterised (Simulation::forward, Simulation.cpp:955-957), the step's
+// convergence flag and, when recording, its trajectory row.  When the call has more steps for
+// the scene, starts the next one from that state as sim_begin_kernel does and returns true: a
+// scene does not wait for the other scenes between the steps of one call (scenes are independent
+// and each evaluation's result depends on its own inputs alone, so the trajectories are the ones
+// the scenes take when every step waits for all of them).
+__device__ bool end_step(int i, int n, const MoverDev& m, const SimCtl& c, double* __restrict__ q,
+                         double* __restrict__ qd, int* __restrict__ conv, SceneState& s) {
+    const int nd = m.ndof;
+    double x[kMaxDof], v[kMaxDof];
+    for (int k = 0; k < nd; ++k) {
+        x[k] = s.x[k];
+        v[k] = (s.x[k] - s.q0[k]) / m.h;
+    }
+    if (nd == 6) sdfc_joint::free_reparam(x, v);
+    for (int k = 0; k < nd; ++k) {
+        q[(size_t)nd * i + k] = x[k];
+        qd[(size_t)nd * i + k] = v[k];
+    }
+    conv[i] = s.converged;
+    ++s.step;
+    if (c.qhis)
+        for (int k = 0; k < nd; ++k) c.qhis[(size_t)nd * n * (c.rec_base + s.step) + (size_t)nd * i + k] = x[k];
+    if (s.step >= c.target) return false;
+    for (int k = 0; k < kMaxDof; ++k) s.q0[k] = s.qd0[k] = s.x[k] = s.dx[k] = s.xt[k] = 0.0;
+    for (int k = 0; k < nd; ++k) {
+        s.q0[k] = x[k];
+        s.qd0[k] = v[k];
+        s.x[k] = s.q0[k] + m.h * s.qd0[k];
+    }
+    s.gnorm = 0.0;
+    s.alpha = 1.0;
+    s.phase = kNewton;
+    s.iter = s.trial = s.strike = s.converged = 0;
+    s.nev = 0;
+    return true;
+}
+
 __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, const int* __restrict__ role,
                                   const MoverDev* __restrict__ mover, const double* __restrict__ f_ext,
                                   const double* __restrict__ fm, const double* __restrict__ Km,
                                   const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining,
                                   unsigned long long* evaluations, const int* __restrict__ scene_list,
                                   const int* __restrict__ scene_cnt, const sdfc::InstanceDesc* __restrict__ inst_full,
-                                  CompactLists nx) {
+                                  CompactLists nx, const SimCtl* __restrict__ ctl, double* __restrict__ q,
+                                  double* __restrict__ qd, int* __restrict__ conv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (scene_list) {
         if (i >= *scene_cnt) return;
@@ -452,7 +510,8 @@ __global__ void sim_newton_kernel(int n, const int* __restrict__ pair_begin, con
             }
         }
     }
-    if (done) {
+    if (!done && ++s.nev >= kMaxEvalsPerStep) done = true;
+    if (done && !end_step(i, n, m, *ctl, q, qd, conv, s)) {
         s.phase = kDone;
         atomicSub(remaining, 1);
     } else if (nx.cnt) {
@@ -469,7 +528,8 @@ __global__ void __launch_bounds__(32) sim_newton_free_warp_kernel(
     const double* __restrict__ f_ext, const double* __restrict__ fm, const double* __restrict__ Km,
     const double* __restrict__ Dm, SceneState* __restrict__ st, int* remaining, unsigned long long* evaluations,
     const int* __restrict__ scene_list, const int* __restrict__ scene_cnt,
-    const sdfc::InstanceDesc* __restrict__ inst_full, CompactLists nx) {
+    const sdfc::InstanceDesc* __restrict__ inst_full, CompactLists nx, const SimCtl* __restrict__ ctl,
+    double* __restrict__ q, double* __restrict__ qd, int* __restrict__ conv) {
     __shared__ sdfc_joint::FreeWarp w;
     int i = blockIdx.x;
     const int lane = threadIdx.x;
@@ -558,31 +618,14 @@ __global__ void __launch_bounds__(32) sim_newton_free_warp_kernel(
             }
         }
     }
-    if (done) {
+    if (!done && ++s.nev >= kMaxEvalsPerStep) done = true;
+    if (done && !end_step(i, n, m, *ctl, q, qd, conv, s)) {
         s.phase = kDone;
         atomicSub(remaining, 1);
     } else if (nx.cnt) {
         append_active(i, pair_begin, inst_full, nx);
     }
     st[i] = s;
-}
-
-__global__ void sim_end_kernel(int n, int nd, const MoverDev* __restrict__ mover, const SceneState* __restrict__ st,
-                               double* __restrict__ q, double* __restrict__ qd, int* __restrict__ converged) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const SceneState& s = st[i];
-    double x[kMaxDof], v[kMaxDof];
-    for (int k = 0; k < nd; ++k) {
-        x[k] = s.x[k];
-        v[k] = (s.x[k] - s.q0[k]) / mover[i].h;
-    }
-    if (nd == 6) sdfc_joint::free_reparam(x, v);  // Simulation::forward, Simulation.cpp:955-957
-    for (int k = 0; k < nd; ++k) {
-        q[(size_t)nd * i + k] = x[k];
-        qd[(size_t)nd * i + k] = v[k];
-    }
-    converged[i] = s.converged;
 }
 
 // ---------------------------------------------------------------- adjoint (backward_BDF1)
@@ -632,7 +675,7 @@ __global__ void adj_pose_kernel(int n_pairs, int n, int nd, const int* __restric
     const double* q = q_his + (size_t)nd * ((size_t)t * n + i);
     const double* qp = q_his + (size_t)nd * ((size_t)(t - 1) * n + i);
     double qd[kMaxDof], E0i[16], phi[6];
-    for (int c = 0; c < nd; ++c) qd[c] = (q[c] - qp[c]) / m.h;  // sim_end_kernel's qdot
+    for (int c = 0; c < nd; ++c) qd[c] = (q[c] - qp[c]) / m.h;  // end_step's qdot
     mover_pose(m, q, qd, E0i, phi);
     double *Em = role[k] ? EA + 16 * (size_t)k : EB + 16 * (size_t)k;
     double *pm = role[k] ? phiA + 6 * (size_t)k : phiB + 6 * (size_t)k;
@@ -886,6 +929,13 @@ struct sdfc_sim {
     unsigned long long* d_evals = nullptr;
     int* h_remaining = nullptr;
     long long rounds = 0;
+    // the per-call control block (device copy read by the Newton kernels, pinned host staging)
+    SimCtl* d_ctl = nullptr;
+    SimCtl* h_ctl = nullptr;
+    // SDFC_SIM_LOCKSTEP set at creation: every step waits for all scenes (one step per round
+    // loop, as the scenes of one sdfc_sim_step call otherwise do not; for comparing the two)
+    bool lockstep = false;
+    double* d_qzero = nullptr;  // zero joint velocities (the energy evaluations' poses)
     std::vector<void*> allocations;
     // one Newton round (pose, batched evaluation, Newton update) as a CUDA graph per round
     // parity, captured at the first step and after a precision change
@@ -940,6 +990,7 @@ void free_sim(sdfc_sim* s) {
     cudaFree(s->d_gEhis);
     for (void* p : s->allocations) cudaFree(p);
     if (s->h_remaining) cudaFreeHost(s->h_remaining);
+    if (s->h_ctl) cudaFreeHost(s->h_ctl);
     if (s->batch) sdfc_impl::free_batch(s->batch);
     delete s;
 }
@@ -988,6 +1039,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     s->n_pairs = n_pairs;
     s->nd = nd;
     s->free_thread = std::getenv("SDFC_FREE_NEWTON_THREAD") != nullptr;
+    s->lockstep = std::getenv("SDFC_SIM_LOCKSTEP") != nullptr;
     // pairs grouped by scene (stable), so each scene's pairs are contiguous
     s->order.resize(n_pairs);
     std::iota(s->order.begin(), s->order.end(), 0);
@@ -1042,11 +1094,12 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
         (rc = alloc(s, &s->d_remaining, 1)) || (rc = alloc(s, &s->d_evals, (size_t)n + 1)) || (rc = alloc(s, &s->d_adj, n)) ||
         (rc = alloc(s, &s->d_gout, 18 * (size_t)n)) || (rc = alloc(s, &s->d_t, 2)) ||
         (rc = alloc(s, &s->d_epair, n_pairs)) || (rc = alloc(s, &s->d_dEpair, 12 * (size_t)n_pairs)) ||
-        (rc = alloc(s, &s->d_dfdE, n))) {
+        (rc = alloc(s, &s->d_dfdE, n)) || (rc = alloc(s, &s->d_ctl, 1)) || (rc = alloc(s, &s->d_qzero, (size_t)nd * n))) {
         free_sim(s);
         return rc;
     }
-    if (cudaMallocHost((void**)&s->h_remaining, sizeof(int)) != cudaSuccess) {
+    if (cudaMallocHost((void**)&s->h_remaining, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost((void**)&s->h_ctl, sizeof(SimCtl)) != cudaSuccess) {
         free_sim(s);
         return fail(ctx, SDFC_ERR_CUDA, "sim_create: cudaMallocHost failed");
     }
@@ -1108,6 +1161,7 @@ int sdfc_sim_create(sdfc_context* ctx, int n, const sdfc_mover* movers, int n_pa
     if (e == cudaSuccess) e = cudaMemcpy(s->d_pair_begin, begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(s->d_q, 0, sizeof(double) * nd * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_qd, 0, sizeof(double) * nd * n);
+    if (e == cudaSuccess) e = cudaMemset(s->d_qzero, 0, sizeof(double) * nd * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_fext, 0, sizeof(double) * 6 * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_conv, 0, sizeof(int) * n);
     if (e == cudaSuccess) e = cudaMemset(s->d_evals, 0, sizeof(unsigned long long) * ((size_t)n + 1));
@@ -1251,12 +1305,13 @@ void launch_newton(sdfc_sim* s, cudaStream_t st, int grid_scenes, const int* sce
     if (s->nd == 6 && !s->free_thread) {
         sim_newton_free_warp_kernel<<<grid_scenes, 32, 0, st>>>(s->n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext,
                                                                  s->d_fm, s->d_Km, s->d_Dm, s->d_state, s->d_remaining,
-                                                                 s->d_evals, scene_list, scene_cnt, inst_full, nx);
+                                                                 s->d_evals, scene_list, scene_cnt, inst_full, nx,
+                                                                 s->d_ctl, s->d_q, s->d_qd, s->d_conv);
     } else {
         constexpr int ts = kSceneThreads;
         sim_newton_kernel<<<(grid_scenes + ts - 1) / ts, ts, 0, st>>>(
             s->n, s->d_pair_begin, s->d_role, s->d_mover, s->d_fext, s->d_fm, s->d_Km, s->d_Dm, s->d_state,
-            s->d_remaining, s->d_evals, scene_list, scene_cnt, inst_full, nx);
+            s->d_remaining, s->d_evals, scene_list, scene_cnt, inst_full, nx, s->d_ctl, s->d_q, s->d_qd, s->d_conv);
     }
 }
 
@@ -1384,20 +1439,23 @@ int capture_backward(sdfc_sim* s) {
 
 }  // namespace
 
-// Penetration energy at the end state of the step just recorded (recorded >= 1).
-int record_energy_step(sdfc_sim* s, cudaStream_t st) {
+// Penetration energy at the end state of recorded step t (0-based; its trajectory row t + 1) and
+// its joint-space gradient.  The energy reads the bodies' poses alone, so the poses come from the
+// recorded row with zero velocities.
+int record_energy_step(sdfc_sim* s, cudaStream_t st, int t) {
     const int n = s->n, np = s->n_pairs, nd = s->nd, tb = 128;
-    double* E_out = s->d_Ehis + (size_t)n * (s->recorded - 1);
-    double* g_out = s->d_gEhis + (size_t)nd * n * (s->recorded - 1);
+    const double* q = s->d_qhis + (size_t)nd * n * (t + 1);
+    double* E_out = s->d_Ehis + (size_t)n * t;
+    double* g_out = s->d_gEhis + (size_t)nd * n * t;
     if (np > 0) {
         energy_pose_kernel<<<(np + tb - 1) / tb, tb, 0, st>>>(np, nd, s->d_pair_inst, s->d_role, s->d_Efixed,
-                                                             s->d_mover, s->d_q, s->d_qd, s->d_EA, s->d_phiA, s->d_EB,
+                                                             s->d_mover, q, s->d_qzero, s->d_EA, s->d_phiA, s->d_EB,
                                                              s->d_phiB);
         sdfc::BatchInputs in{s->d_EA, s->d_phiA, s->d_EB, s->d_phiB, s->d_prm};
         int rc = sdfc_impl::run_energy(s->batch, in, s->d_epair, s->d_dEpair, st);
         if (rc) return rc;
     }
-    energy_reduce_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, nd, s->d_pair_begin, s->d_role, s->d_mover, s->d_q,
+    energy_reduce_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, nd, s->d_pair_begin, s->d_role, s->d_mover, q,
                                                           s->d_epair, s->d_dEpair, E_out, g_out);
     return SDFC_OK;
 }
@@ -1566,31 +1624,38 @@ int sdfc_sim_step(sdfc_sim* s, int num_steps, int* converged) {
     cudaStream_t st = ctx->stream;
     const int n = s->n;
     const int tb = 128;
-    const int max_rounds = 100 * (1 + kMaxLineSearch) + 1;
     const int per_check = 2;  // rounds enqueued between completion checks
-    for (int step = 0; step < num_steps; ++step) {
+    // one round loop for the whole call (each scene takes its steps one after another, without
+    // waiting for the others), or one per step (SDFC_SIM_LOCKSTEP)
+    const int loops = num_steps == 0 ? 0 : (s->lockstep ? num_steps : 1);
+    const int target = s->lockstep ? 1 : num_steps;
+    for (int l = 0; l < loops; ++l) {
+        *s->h_ctl = SimCtl{target, s->recorded, s->record_cap > 0 ? s->d_qhis : nullptr};
+        SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_ctl, s->h_ctl, sizeof(SimCtl), cudaMemcpyHostToDevice, st));
         sim_begin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_mover, s->d_q, s->d_qd, s->d_state,
                                                           s->d_remaining);
+        // every scene ends each step within kMaxEvalsPerStep evaluations, one per round
+        const long long max_rounds = (long long)target * kMaxEvalsPerStep + per_check;
         int active = n;
-        for (int r = 0; r < max_rounds && active > 0; r += per_check) {
+        for (long long r = 0; r < max_rounds && active > 0; r += per_check) {
             for (int k = 0; k < per_check; ++k) {
                 cudaGraphExec_t g = nullptr;
                 if ((rc = round_graph(s, active, &g))) return rc;
                 SDFC_CUDA_TRY(ctx, cudaGraphLaunch(g, st));
                 s->parity ^= 1;
             }
+            // (the staged control block has been read once this completes)
             SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_remaining, s->d_remaining, sizeof(int), cudaMemcpyDeviceToHost, st));
             SDFC_CUDA_TRY(ctx, cudaStreamSynchronize(st));
             s->rounds += per_check;
             active = *s->h_remaining;
-            if (active == 0) break;
         }
-        sim_end_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, s->nd, s->d_mover, s->d_state, s->d_q, s->d_qd, s->d_conv);
+        if (active > 0) return fail(ctx, SDFC_ERR_CUDA, "sim_step: scenes still iterating after the round bound");
         if (s->record_cap > 0) {
-            ++s->recorded;
-            SDFC_CUDA_TRY(ctx, cudaMemcpyAsync(s->d_qhis + (size_t)s->nd * n * s->recorded, s->d_q,
-                                               sizeof(double) * s->nd * n, cudaMemcpyDeviceToDevice, st));
-            if (s->energy_on && (rc = record_energy_step(s, st))) return rc;
+            if (s->energy_on)
+                for (int t = 0; t < target; ++t)
+                    if ((rc = record_energy_step(s, st, s->recorded + t))) return rc;
+            s->recorded += target;
         }
     }
     SDFC_CUDA_TRY(ctx, cudaGetLastError());

@@ -332,7 +332,11 @@ int sdfc_sim_get_state(sdfc_sim* sim, double* q, double* qdot);
  * Simulation::set_body_external_force (Body::_f_external; the reference scales
  * it by the inertia diagonal, Body.cpp:267-268). */
 int sdfc_sim_set_external_force(sdfc_sim* sim, const double* f);
-/* num_steps BDF1 steps of every scene (Simulation::forward, :914-990).
+/* num_steps BDF1 steps of every scene (Simulation::forward, :914-990).  Within one call each
+ * scene takes its steps one after another without waiting for the other scenes (a scene whose
+ * step has converged starts its next step in the next round), so the call's rounds follow the
+ * scene with the most evaluations rather than each step's slowest scene; the trajectories are
+ * those of steps taken one call at a time.
  * converged (host, n, may be NULL): 1 where the last step's Newton converged
  * (Simulation::is_converged). */
 int sdfc_sim_step(sdfc_sim* sim, int num_steps, int* converged);

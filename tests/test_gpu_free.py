@@ -147,11 +147,14 @@ def test_warp_newton_matches_thread_newton(sdfc, monkeypatch):
     assert sa == sb
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("joint", ["free", "trans"])
-def test_compacted_rounds_match_full_rounds(sdfc, monkeypatch, joint):
+def test_compacted_rounds_match_full_rounds(sdfc, monkeypatch, joint, precision):
     """Late Newton rounds evaluate only the scenes still iterating (compacted rounds, sized by
-    capacity buckets).  Every pair's evaluation is independent of the others, so a rollout with
-    compaction is bit-identical to one with full rounds only (SDFC_SIM_NO_COMPACT)."""
+    capacity buckets).  Every pair's evaluation is independent of the others, and both kinds of
+    round pose the movers with one compiled function, so a rollout with compaction is
+    bit-identical to one with full rounds only (SDFC_SIM_NO_COMPACT), with FP64 evaluations too
+    (where a pose differing in its last bit would show)."""
     fx = load("sim_free.npz" if joint == "free" else "sim_trans.npz")
     nd = 6 if joint == "free" else 3
     rng = np.random.default_rng(29)
@@ -170,7 +173,7 @@ def test_compacted_rounds_match_full_rounds(sdfc, monkeypatch, joint):
         try:
             sim = make_sim(sdfc, ctx, fx, n=n, f_ext=F, q0=q0, qd0=qd0,
                            joint=sdfc.JOINT_FREE3D_EXP if joint == "free" else sdfc.JOINT_TRANSLATIONAL)
-            sim.set_precision(sdfc.PRECISION_MIXED)
+            sim.set_precision(precision)
             sim.record(T)
             conv = sim.step(T)
             out.append((sim.history(), conv, sim.stats()))
@@ -180,3 +183,52 @@ def test_compacted_rounds_match_full_rounds(sdfc, monkeypatch, joint):
     assert np.array_equal(qa, qb)
     assert np.array_equal(ca, cb)
     assert sa == sb
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("joint", ["free", "trans"])
+def test_free_running_steps_match_lockstep(sdfc, monkeypatch, joint, precision):
+    """Within one sdfc_sim_step call every scene takes its steps one after another without
+    waiting for the other scenes (a scene that has converged starts its next step in the next
+    round).  Scenes are independent and each evaluation depends on its own inputs alone, so the
+    trajectories, convergence flags, recorded energies, adjoint gradients and per-scene evaluation
+    counts are bit-identical to rounds in which every step waits for all scenes
+    (SDFC_SIM_LOCKSTEP), in fewer rounds.  The call is split (5 + 7 steps) to cover a call
+    starting from the state and recording row the previous call left."""
+    fx = load("sim_free.npz" if joint == "free" else "sim_trans.npz")
+    nd = 6 if joint == "free" else 3
+    rng = np.random.default_rng(31)
+    n, T = 48, 12
+    F = np.zeros((n, 6))
+    F[:, 3:] = rng.normal(size=(n, 3)) * 3.0
+    q0 = np.tile(fx["q0"], (n, 1)) + rng.normal(size=(n, nd)) * 0.004
+    qd0 = rng.normal(size=(n, nd)) * 0.3
+    df_dq = rng.normal(size=(n, T, nd))
+    out = []
+    for lockstep in (False, True):
+        if lockstep:
+            monkeypatch.setenv("SDFC_SIM_LOCKSTEP", "1")
+        else:
+            monkeypatch.delenv("SDFC_SIM_LOCKSTEP", raising=False)
+        ctx = sdfc.Context(0)
+        try:
+            sim = make_sim(sdfc, ctx, fx, n=n, f_ext=F, q0=q0, qd0=qd0, precision=precision,
+                           joint=sdfc.JOINT_FREE3D_EXP if joint == "free" else sdfc.JOINT_TRANSLATIONAL)
+            sim.record_energy(True)
+            sim.record(T)
+            c1 = sim.step(5)
+            c2 = sim.step(T - 5)
+            E, Etot = sim.energy()
+            grads = sim.backward(df_dq, np.ones(n))
+            out.append((sim.history(), c1, c2, E, Etot, grads, sim.scene_evaluations(), sim.stats(), sim.get_state()))
+        finally:
+            ctx.close()
+    free, lock = out
+    for a, b in zip(free[:5], lock[:5]):
+        assert np.array_equal(a, b)
+    assert all(np.array_equal(a, b) for a, b in zip(free[5], lock[5]))
+    assert np.array_equal(free[6], lock[6])
+    assert free[7][1] == lock[7][1]  # evaluations
+    assert free[7][0] < lock[7][0]  # rounds
+    assert all(np.array_equal(a, b) for a, b in zip(free[8], lock[8]))
+    assert (free[4] > 0).any()  # the scenes touch the bore
