@@ -378,8 +378,9 @@ int sdfc_sim_backward(sdfc_sim* sim, const double* df_dq, double* df_dq0, double
 
 /* Penetration energy of the rollout (no counterpart in the reference).  With energy recording
  * on (call before sdfc_sim_record; switching it stops a recording), every recorded step also
- * evaluates the penetration energy E_t of each scene at the step's end state (the sum over the
- * scene's pairs of sdfc_batch_energy) and its gradient wrt the joint coordinates.
+ * has the penetration energy E_t of each scene at the step's end state (the sum over the
+ * scene's pairs of sdfc_batch_energy, evaluated from the recorded trajectory when the
+ * sdfc_sim_step call's rounds are done) and its gradient wrt the joint coordinates.
  * sdfc_sim_energy: per_step (host, n x T, may be NULL) and total (host, n, may be NULL) = sum_t E_t.
  * sdfc_sim_backward_energy: sdfc_sim_backward for L(q_1..q_T, sum_t E_t) given also
  * df_dE (host, n) = dL/d(sum_t E_t) per scene (NULL: 0). */
