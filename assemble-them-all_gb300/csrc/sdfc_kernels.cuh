@@ -70,7 +70,7 @@ constexpr int kForceCtasPerSm = SDFC_FORCE_MIN_BLOCKS;
 #define SDFC_FORCE_MIN_BLOCKS_GENERAL 5
 #endif
 constexpr int kForceCtasPerSmGeneral = SDFC_FORCE_MIN_BLOCKS_GENERAL;
-constexpr int kMaxSlots = 32;        // partial rows per instance, at most
+constexpr int kMaxSlots = 128;       // partial rows per instance, at most
 // Multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked up once per
 // device): launch shapes follow it.
 int device_sm_count();

@@ -243,7 +243,8 @@ int sdfc_batch_last_timing(sdfc_batch* batch, float* ms);
  * S = min(slots, ceil(chunks / chunks_per_slot)) (none without contacts): each share is summed
  * on its own and the shares in order at the end, so an instance with many contacts is spread
  * over many CTAs and one with few over one.
- *   slots            partial sums per instance, at most (1..32, a power of two);
+ *   slots            partial sums per instance, at most (1..128, a power of two; by default 128,
+ *                    halved while instances x slots exceeds 2^18 partial rows);
  *   force_variant    SDFC_FORCE_CTAS: persistent CTAs of 128 threads, as many as the
  *                    multiprocessors hold, taking (instance, share) items from a queue;
  *                    SDFC_FORCE_WORKERS: persistent one-warp CTAs taking the same items;
