@@ -11,8 +11,10 @@
 //
 // Every scene runs the reference's Newton iteration as a small state machine;
 // one "round" gives every unfinished scene exactly one force evaluation (with
-// derivatives at a Newton point, value-only at a line-search trial), so a
-// round is one batched evaluation of all contact pairs plus two tiny kernels:
+// derivatives at a Newton point, value-only at a line-search trial), and a scene
+// whose step ends goes on to its next step of the same sdfc_sim_step call in the
+// next round (end_step), so a round is one batched evaluation of all contact pairs
+// plus two tiny kernels:
 //   sim_pose_kernel    per pair: the mover's pose / twist at the scene's current
 //                      point, the pair's inputs and request (skip/value/derivative)
 //   (batched evaluation of every requested pair)
