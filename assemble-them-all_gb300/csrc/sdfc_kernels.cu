@@ -974,10 +974,10 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
     __shared__ GridDesc g;
     __shared__ PointsDesc P;
     __shared__ PairState<T> S;
-    const int i = blockIdx.y, s = blockIdx.x;
+    const int i = blockIdx.y;
     if (in.mode && in.mode[i] == 0) return;
     const int shares = spread_of(inst_total[i], kChunk, per, slots);
-    if (s >= shares) return;  // uniform over the CTA
+    if ((int)blockIdx.x >= shares) return;  // uniform over the CTA
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const InstanceDesc I = inst[i];
     if (warp == 0) {
@@ -999,58 +999,64 @@ __global__ void __launch_bounds__(kChunk, force_min_blocks<T>()) energy_kernel(c
         warp_copy(P, points[I.points], lane);
         warp_copy(S, pairs[i], lane);
     }
-    for (int k = tid; k < NW * 12; k += kChunk) acc[k].zero();
-    if (tid < NW) eacc[tid] = 0.0;
-    __syncthreads();
+    __syncthreads();  // the set-up above
     const int total = prefix[I.ntiles];
     const int nchunks = (total + kChunk - 1) / kChunk;
-    for (int chunk = s; chunk < nchunks; chunk += shares) {
-        if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
-        const int c = chunk * kChunk + tid;
-        const bool valid = c < total;
-        V3 xi = v3(0, 0, 0);
-        Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
-        if (valid) {
-            int lo = 0, hi = I.ntiles;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (prefix[mid] <= c)
-                    lo = mid;
-                else
-                    hi = mid;
+    // the CTA's shares in turn (the grid holds at most a few CTAs per instance): share s sums
+    // chunks s, s + S, ... from zeroed accumulators into its own partial row
+    for (int s = blockIdx.x; s < shares; s += gridDim.x) {
+        for (int k = tid; k < NW * 12; k += kChunk) acc[k].zero();
+        if (tid < NW) eacc[tid] = 0.0;
+        __syncthreads();
+        for (int chunk = s; chunk < nchunks; chunk += shares) {
+            if (chunk * kChunk + warp * 32 >= total) continue;  // a warp with no contact in this chunk
+            const int c = chunk * kChunk + tid;
+            const bool valid = c < total;
+            V3 xi = v3(0, 0, 0);
+            Vec3<float> xf = vec3<float>(0.f, 0.f, 0.f);
+            if (valid) {
+                int lo = 0, hi = I.ntiles;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (prefix[mid] <= c)
+                        lo = mid;
+                    else
+                        hi = mid;
+                }
+                const int sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
+                xi = load_point(P, sid);
+                if constexpr (kWarpExact) xf = load_point32(P, sid);
             }
-            const int sid = ids[(size_t)(I.tile0 + lo) * kTile + (c - prefix[lo])];
-            xi = load_point(P, sid);
-            if constexpr (kWarpExact) xf = load_point32(P, sid);
-        }
-        FastCell fc;
-        const FastCell* fcp = nullptr;
-        ExactJet<T> ej;
-        const ExactJet<T>* ejp = nullptr;
-        if constexpr (kWarpExact) {
-            fc = fast_cell<T>(g, S.cm, xi, xf);
-            fcp = &fc;
-            warp_exact_jets<T>(g, S, xi, valid && !fc.ok && !fc.near, false, ej);
-            ejp = &ej;
-        }
-        const ContactEnergy<T> E = contact_energy<T>(g, xi, S, fcp, valid, STENCIL, ejp);
-        WarpSink<12, T> sink{acc + warp * 12, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
-        T v[12] = {E.aw.x, E.aw.y, E.aw.z, E.av.x, E.av.y, E.av.z, E.bw.x, E.bw.y, E.bw.z, E.bv.x, E.bv.y, E.bv.z};
-        sink.add12(v, 0, 1);
-        double e = E.e;
+            FastCell fc;
+            const FastCell* fcp = nullptr;
+            ExactJet<T> ej;
+            const ExactJet<T>* ejp = nullptr;
+            if constexpr (kWarpExact) {
+                fc = fast_cell<T>(g, S.cm, xi, xf);
+                fcp = &fc;
+                warp_exact_jets<T>(g, S, xi, valid && !fc.ok && !fc.near, false, ej);
+                ejp = &ej;
+            }
+            const ContactEnergy<T> E = contact_energy<T>(g, xi, S, fcp, valid, STENCIL, ejp);
+            WarpSink<12, T> sink{acc + warp * 12, lane, valid, vec3<T>(0, 0, 0), vec3<T>(0, 0, 0)};
+            T v[12] = {E.aw.x, E.aw.y, E.aw.z, E.av.x, E.av.y, E.av.z, E.bw.x, E.bw.y, E.bw.z, E.bv.x, E.bv.y, E.bv.z};
+            sink.add12(v, 0, 1);
+            double e = E.e;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
-        if (lane == 0) eacc[warp] += e;
-    }
-    __syncthreads();
-    double* row = partial + ((size_t)i * slots + s) * kOutDeriv;
-    for (int k = tid; k < kOutEnergy; k += kChunk) {
-        double v = 0.0;
-        if (k == 0)
-            for (int w = 0; w < NW; ++w) v += eacc[w];
-        else
-            for (int w = 0; w < NW; ++w) v += acc[w * 12 + k - 1].value();
-        row[k] = v;
+            for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kFull, e, o);
+            if (lane == 0) eacc[warp] += e;
+        }
+        __syncthreads();
+        double* row = partial + ((size_t)i * slots + s) * kOutDeriv;
+        for (int k = tid; k < kOutEnergy; k += kChunk) {
+            double v = 0.0;
+            if (k == 0)
+                for (int w = 0; w < NW; ++w) v += eacc[w];
+            else
+                for (int w = 0; w < NW; ++w) v += acc[w * 12 + k - 1].value();
+            row[k] = v;
+        }
+        __syncthreads();  // the row is read before the next share zeroes the accumulators
     }
 }
 
@@ -1366,7 +1372,11 @@ bool force_skips_q2(bool deriv, bool stencil, int precision) { return deriv && !
 void launch_energy(const InstanceDesc* d_inst, int n_inst, BatchInputs in, const GridDesc* d_grids,
                    const PointsDesc* d_points, BatchScratch s, bool stencil, int precision, cudaStream_t stream) {
     if (n_inst <= 0) return;
-    dim3 grid(s.slots, n_inst);
+    // at most kEnergyCtas CTAs per instance, each taking its shares in turn: an energy pass
+    // serves batches of many small instances (rollouts), where slots x instances CTAs would
+    // mostly start only to find no share
+    constexpr int kEnergyCtas = 16;
+    dim3 grid(std::min(s.slots, kEnergyCtas), n_inst);
     const int per = std::max(s.chunks_per_slot, 1);
     if (precision == kMixed) {
         if (stencil)
