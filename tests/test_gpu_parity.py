@@ -519,6 +519,49 @@ def test_energy_against_oracle(sdfc, ctx, oracle, workloads, precision, bar):
     b.close()
 
 
+@pytest.mark.parametrize("precision,bar", [(0, 1e-10), (1, 1e-5)])
+def test_energy_many_shares(sdfc, ctx, oracle, workloads, precision, bar):
+    """Instances whose contacts fill more shares than the energy pass has CTAs per instance (12k
+    active contacts in 1-chunk shares: 94 shares, 16 CTAs each taking several in turn), against
+    the oracle.  Every node of the grid lies inside (values below -col_th) and every point in the
+    grid box, so every point is an active contact."""
+    rng = np.random.default_rng(41)
+    shape = (20, 18, 22)
+    mn, mx = np.array([0.0, 0.0, 0.0]), np.array([0.25, 0.2, 0.3])
+    dx = (mx - mn) / (np.array(shape) - 1)
+    ax = [mn[a] + dx[a] * np.arange(shape[a]) for a in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    vals = np.sqrt((((np.stack([X, Y, Z], -1) - [0.11, 0.1, 0.16]) * [1.0, 1.3, 0.8]) ** 2).sum(-1)) - 0.3
+    vals = vals.astype(np.float32).astype(np.float64)
+    assert vals.max() < -0.05
+    gh = ctx.upload_grid(vals, mn, mx, dx, 0.01, 1)
+    og = oracle.Grid(vals, mn, mx, dx, 0.01)
+    n = 2
+    EB = np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.5), rng.normal(size=3))
+                   for _ in range(n)])
+    EA = EB @ np.stack([workloads.pose(workloads.rotvec_to_matrix(rng.normal(size=3) * 0.005), [0.01, -0.01, 0.02])
+                        for _ in range(n)])
+    # points that both poses carry into the grid box (margin 0.03 for the offsets above)
+    xb = rng.uniform(mn + 0.03, mx - 0.03, size=(12000, 3))
+    pts = np.einsum("ij,nj->ni", np.linalg.inv(EA[0]) @ EB[0], np.c_[xb, np.ones(len(xb))])[:, :3]
+    ph = ctx.upload_points(pts, 0)
+    b = ctx.batch([ph] * n, [gh] * n)
+    try:
+        b.set_precision(precision)
+        b.set_tuning(128, sdfc.FORCE_CTAS, 0, 1)
+        prm = [sdfc.Params(1e5, 1e3, 0.3, 1e3, 2.0, 0.5)] * n
+        e, dE = b.energy(EA, EB, prm)
+        for k in range(n):
+            re, rdE = oracle.pair_energy(og, pts, EA[k], EB[k], oracle.Params(1e5, 1e3, 0.3, 1e3, 2.0, 0.5))
+            nact = len(oracle.pair_eval(og, pts, EA[k], np.zeros(6), EB[k], np.zeros(6),
+                                        oracle.Params(1e5, 1e3, 0.3, 1e3, 2.0, 0.5), False)[3])
+            assert nact > 16 * 128, (k, nact)  # more 1-chunk shares than the pass's 16 CTAs per instance
+            assert abs(e[k] - re) <= bar * re, (k, e[k], re)
+            assert np.linalg.norm(dE[k] - rdE) <= bar * np.linalg.norm(rdE), (k, dE[k], rdE)
+    finally:
+        b.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_host_array_paths_agree(sdfc, workloads, precision):
     """sdfc_batch_evaluate's two host-array paths give the same bits: kernels that read the
